@@ -1,0 +1,136 @@
+// Device-side data structures and helpers shared by the FDTD kernels (sm_103a).
+//
+// Layout in HBM: every field is (3, nx, ny, nz) float32, C order, z fastest; the
+// component stride is N = nx*ny*nz.  Material arrays are (n, nx, ny, nz) with
+// n in {1, 3}; an isotropic array is read through component 0.  A CPML slab's
+// psi arrays have the slab's shape: the full domain with `L` cells along the
+// slab axis.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "fdtd_gb300.h"
+
+namespace fdtd {
+
+struct DSlab {
+    int axis, lo, L, kappa_one;
+    int sx, sy, sz;             // slab dims
+    const float* coef;          // device: a_E, b_E, inv_kappa_E, a_H, b_H, inv_kappa_H (each L)
+};
+
+struct Geo {
+    int nx, ny, nz;
+    long long N;                // cells per component
+    int px, py, pz;             // periodic (wrap) flags
+    float c;                    // Courant number
+    float eta0;                 // free-space impedance mu0*c (host-supplied)
+    int pec, pmc;               // face masks, bit (2*axis + side)
+};
+
+// Arguments of one E or H half-step (forward or reverse).
+struct UpdArgs {
+    Geo g;
+    const float* F;             // field differentiated (H for the E step, E for the H step)
+    const float* Uin;           // field updated, read
+    float* Uout;                // field updated, written (may alias Uin)
+    const float* mat;           // inv_eps (E step) or inv_mu (H step); nullptr -> mat_scalar
+    int n_mat;
+    float mat_scalar;
+    const float* sig;           // conductivity (pre-scaled by dx) or nullptr
+    int n_sig;
+    int n_slab;
+    DSlab slab[FDTD_MAX_SLABS];
+    float* psi1[FDTD_MAX_SLABS];
+    float* psi2[FDTD_MAX_SLABS];
+};
+
+struct DSource {
+    int kind, comp, magnetic, normal, profile;
+    int lo[3], hi[3];
+    float sign, coef, omega_dt, ramp_inv, t0, inv2s2;
+    const float* incE;
+    const float* incH;
+    const float* offE;
+    const float* offH;
+    const float* phE;
+    const float* phH;
+    const float* teff;
+    const uint8_t* on;
+};
+
+struct DDet {
+    int kind, comp_mask, exact, reduce, inverse, nfreq, flux_axis, keep_all;
+    int ncomp;                  // recorded components (or Poynting components)
+    int lo[3], hi[3];
+    int rx, ry, rz;
+    long long R;                // region cells
+    float flux_sign, cell_weight;
+    const int* slot;            // device table (n_table)
+    const float2* w;            // device table (n_table, nfreq)
+    float* partial;             // scratch: (nblocks, ncomp) block partial sums
+    int nblocks;
+};
+
+__device__ __forceinline__ long long cell_index(const Geo& g, int i, int j, int k) {
+    return ((long long)i * g.ny + j) * g.nz + k;
+}
+
+// Field value at (i, j, k) with the reference's one-cell halo semantics
+// (fdtdx/core/misc.py:615-641): an out-of-range index on a periodic axis wraps,
+// otherwise the value is zero.  Only one-cell excursions are ever requested.
+__device__ __forceinline__ float ld_halo(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k) {
+    if (i < 0) { if (!g.px) return 0.f; i += g.nx; }
+    else if (i >= g.nx) { if (!g.px) return 0.f; i -= g.nx; }
+    if (j < 0) { if (!g.py) return 0.f; j += g.ny; }
+    else if (j >= g.ny) { if (!g.py) return 0.f; j -= g.ny; }
+    if (k < 0) { if (!g.pz) return 0.f; k += g.nz; }
+    else if (k >= g.nz) { if (!g.pz) return 0.f; k -= g.nz; }
+    return __ldg(f + comp * g.N + cell_index(g, i, j, k));
+}
+
+// Whether component `comp` at (i, j, k) is zeroed by a conductor face in `mask`
+// (PEC for E: fdtdx/objects/boundaries/pec.py:71-77; PMC for H: pmc.py:62-76).
+__device__ __forceinline__ bool face_zero(const Geo& g, int mask, int comp, int i, int j, int k) {
+    if (!mask) return false;
+    const int idx[3] = {i, j, k};
+    const int n[3] = {g.nx, g.ny, g.nz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a == comp) continue;
+        if ((mask & (1 << (2 * a))) && idx[a] == 0) return true;
+        if ((mask & (1 << (2 * a + 1))) && idx[a] == n[a] - 1) return true;
+    }
+    return false;
+}
+
+// Temporal profile at tau (in steps) with a reduced carrier phase `phase` (rad):
+// SingleFrequencyProfile: clip(tau*dt/(N_startup*T), 0, 1) cos(phase);
+// GaussianPulseProfile:   exp(-(tau - t0)^2 dt^2 / (2 sigma^2)) cos(phase).
+__device__ __forceinline__ float profile_amp(const DSource& s, float tau, float phase) {
+    const float carrier = cosf(phase);
+    if (s.profile == FDTD_PROFILE_CW) {
+        const float r = fminf(fmaxf(tau * s.ramp_inv, 0.f), 1.f);
+        return r * carrier;
+    }
+    const float d = tau - s.t0;
+    return expf(-d * d * s.inv2s2) * carrier;
+}
+
+template <typename T>
+__device__ __forceinline__ T to_storage(float v);
+template <>
+__device__ __forceinline__ float to_storage<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_storage<__nv_bfloat16>(float v) { return __float2bfloat16(v); }
+template <>
+__device__ __forceinline__ __half to_storage<__half>(float v) { return __float2half(v); }
+
+__device__ __forceinline__ float from_storage(float v) { return v; }
+__device__ __forceinline__ float from_storage(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float from_storage(__half v) { return __half2float(v); }
+
+}  // namespace fdtd

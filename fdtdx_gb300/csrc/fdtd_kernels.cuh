@@ -1,0 +1,484 @@
+// Forward and time-reversed Yee half-steps, source injection, detector
+// accumulation and PML-interface recording for the GB300 (sm_103a).
+//
+// One thread owns one cell of the updated field; the grid is
+// (ceil(nz/32), ceil(ny/8), nx) with 32 threads along z, so every warp reads and
+// writes 128 contiguous bytes per component.  Neighbour values of the
+// differentiated field come from the L1/L2 (the planes i-1 / i+1 were touched by
+// the previous / next z-blocks of the same block row a few microseconds apart).
+// The CPML correction of a cell is fused into its half-step: a slab is tested by
+// one unsigned compare per slab, so interior cells pay six compares.
+#pragma once
+#include "fdtd_device.cuh"
+
+namespace fdtd {
+
+// ---------------------------------------------------------------------------------
+// E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
+// reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
+// curl_H with CPML psi (fdtdx/core/physics/curl.py:314-397,
+// fdtdx/objects/boundaries/perfectly_matched_layer.py:138-190).
+// ---------------------------------------------------------------------------------
+template <bool REV>
+__global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
+    const Geo& g = a.g;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (j >= g.ny || k >= g.nz) return;
+    const long long N = g.N;
+    const long long c = cell_index(g, i, j, k);
+    const float* __restrict__ H = a.F;
+    const float Hx = __ldg(H + c), Hy = __ldg(H + N + c), Hz = __ldg(H + 2 * N + c);
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const float Hz_jm = j > 0 ? __ldg(H + 2 * N + c - sy) : ld_halo(g, H, 2, i, j - 1, k);
+    const float Hx_jm = j > 0 ? __ldg(H + c - sy) : ld_halo(g, H, 0, i, j - 1, k);
+    const float Hy_km = k > 0 ? __ldg(H + N + c - 1) : ld_halo(g, H, 1, i, j, k - 1);
+    const float Hx_km = k > 0 ? __ldg(H + c - 1) : ld_halo(g, H, 0, i, j, k - 1);
+    const float Hz_im = i > 0 ? __ldg(H + 2 * N + c - sx) : ld_halo(g, H, 2, i - 1, j, k);
+    const float Hy_im = i > 0 ? __ldg(H + N + c - sx) : ld_halo(g, H, 1, i - 1, j, k);
+    const float dyHz = Hz - Hz_jm, dzHy = Hy - Hy_km, dzHx = Hx - Hx_km;
+    const float dxHz = Hz - Hz_im, dxHy = Hy - Hy_im, dyHx = Hx - Hx_jm;
+    float cu[3] = {dyHz - dzHy, dzHx - dxHz, dxHy - dyHx};
+
+    const int idx3[3] = {i, j, k};
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (s >= a.n_slab) break;
+        const DSlab& sl = a.slab[s];
+        const int l = idx3[sl.axis] - sl.lo;
+        if ((unsigned)l >= (unsigned)sl.L) continue;
+        float d1, d2;
+        if (sl.axis == 0) { d1 = dxHz; d2 = dxHy; }
+        else if (sl.axis == 1) { d1 = dyHx; d2 = dyHz; }
+        else { d1 = dzHy; d2 = dzHx; }
+        const float ca = __ldg(sl.coef + l), cb = __ldg(sl.coef + sl.L + l);
+        const long long p = ((long long)(i - (sl.axis == 0 ? sl.lo : 0)) * sl.sy + (j - (sl.axis == 1 ? sl.lo : 0))) * sl.sz +
+                            (k - (sl.axis == 2 ? sl.lo : 0));
+        float p1 = a.psi1[s][p], p2 = a.psi2[s][p];
+        if (!REV) {
+            p1 = cb * p1 + ca * d1;
+            p2 = cb * p2 + ca * d2;
+            a.psi1[s][p] = p1;
+            a.psi2[s][p] = p2;
+        }
+        float c1 = p1, c2 = p2;
+        if (!sl.kappa_one) {
+            const float ikm1 = __ldg(sl.coef + 2 * sl.L + l) - 1.f;
+            c1 = ikm1 * d1 + p1;
+            c2 = ikm1 * d2 + p2;
+        }
+        const int ci = (sl.axis + 1) % 3, cj = (sl.axis + 2) % 3;
+        cu[ci] -= c1;
+        cu[cj] += c2;
+    }
+
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+        const long long o = comp * N + c;
+        float e;
+        if (face_zero(g, g.pec, comp, i, j, k)) {
+            e = 0.f;
+        } else {
+            const float ie = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
+            const float e0 = a.Uin[o];
+            if (a.sig) {
+                const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
+                const float q = g.c * sg * g.eta0 * ie / 2.f;
+                if (!REV) e = ((1.f - q) * e0 + g.c * cu[comp] * ie) / (1.f + q);
+                else e = (e0 * (1.f + q) - g.c * cu[comp] * ie) / (1.f - q);
+            } else {
+                if (!REV) e = e0 + g.c * cu[comp] * ie;
+                else e = e0 - g.c * cu[comp] * ie;
+            }
+        }
+        a.Uout[o] = e;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// H half-step: H <- (g H - c curl_E(E) inv_mu) / e  (fdtdx/fdtd/update.py:717-750)
+// reverse:     H <- (H (1+q) + c curl_E(E) inv_mu) / (1-q)  (update.py:905-930)
+// ---------------------------------------------------------------------------------
+template <bool REV>
+__global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
+    const Geo& g = a.g;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (j >= g.ny || k >= g.nz) return;
+    const long long N = g.N;
+    const long long c = cell_index(g, i, j, k);
+    const float* __restrict__ E = a.F;
+    const float Ex = __ldg(E + c), Ey = __ldg(E + N + c), Ez = __ldg(E + 2 * N + c);
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const float Ez_jp = j < g.ny - 1 ? __ldg(E + 2 * N + c + sy) : ld_halo(g, E, 2, i, j + 1, k);
+    const float Ex_jp = j < g.ny - 1 ? __ldg(E + c + sy) : ld_halo(g, E, 0, i, j + 1, k);
+    const float Ey_kp = k < g.nz - 1 ? __ldg(E + N + c + 1) : ld_halo(g, E, 1, i, j, k + 1);
+    const float Ex_kp = k < g.nz - 1 ? __ldg(E + c + 1) : ld_halo(g, E, 0, i, j, k + 1);
+    const float Ez_ip = i < g.nx - 1 ? __ldg(E + 2 * N + c + sx) : ld_halo(g, E, 2, i + 1, j, k);
+    const float Ey_ip = i < g.nx - 1 ? __ldg(E + N + c + sx) : ld_halo(g, E, 1, i + 1, j, k);
+    const float dyEz = Ez_jp - Ez, dzEy = Ey_kp - Ey, dzEx = Ex_kp - Ex;
+    const float dxEz = Ez_ip - Ez, dxEy = Ey_ip - Ey, dyEx = Ex_jp - Ex;
+    float cu[3] = {dyEz - dzEy, dzEx - dxEz, dxEy - dyEx};
+
+    const int idx3[3] = {i, j, k};
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (s >= a.n_slab) break;
+        const DSlab& sl = a.slab[s];
+        const int l = idx3[sl.axis] - sl.lo;
+        if ((unsigned)l >= (unsigned)sl.L) continue;
+        float d1, d2;
+        if (sl.axis == 0) { d1 = dxEz; d2 = dxEy; }
+        else if (sl.axis == 1) { d1 = dyEx; d2 = dyEz; }
+        else { d1 = dzEy; d2 = dzEx; }
+        const float* co = sl.coef + 3 * sl.L;
+        const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
+        const long long p = ((long long)(i - (sl.axis == 0 ? sl.lo : 0)) * sl.sy + (j - (sl.axis == 1 ? sl.lo : 0))) * sl.sz +
+                            (k - (sl.axis == 2 ? sl.lo : 0));
+        float p1 = a.psi1[s][p], p2 = a.psi2[s][p];
+        if (!REV) {
+            p1 = cb * p1 + ca * d1;
+            p2 = cb * p2 + ca * d2;
+            a.psi1[s][p] = p1;
+            a.psi2[s][p] = p2;
+        }
+        float c1 = p1, c2 = p2;
+        if (!sl.kappa_one) {
+            const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+            c1 = ikm1 * d1 + p1;
+            c2 = ikm1 * d2 + p2;
+        }
+        const int ci = (sl.axis + 1) % 3, cj = (sl.axis + 2) % 3;
+        cu[ci] -= c1;
+        cu[cj] += c2;
+    }
+
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+        const long long o = comp * N + c;
+        float h;
+        if (face_zero(g, g.pmc, comp, i, j, k)) {
+            h = 0.f;
+        } else {
+            const float im = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
+            const float h0 = a.Uin[o];
+            if (a.sig) {
+                const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
+                const float q = g.c * sg / g.eta0 * im / 2.f;
+                if (!REV) h = ((1.f - q) * h0 - g.c * cu[comp] * im) / (1.f + q);
+                else h = (h0 * (1.f + q) + g.c * cu[comp] * im) / (1.f - q);
+            } else {
+                if (!REV) h = h0 - g.c * cu[comp] * im;
+                else h = h0 + g.c * cu[comp] * im;
+            }
+        }
+        a.Uout[o] = h;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Source injection.  One thread per source cell.  `inverse` flips the sign (the
+// reverse step subtracts what the forward step added).  Positions a conductor
+// wall zeroes are skipped: the wall's zeroing runs after the injection in the
+// reference, so an injection there never survives.
+// Point dipole: fdtdx/objects/sources/dipole.py:195-277.
+// TFSF plane:   fdtdx/objects/sources/tfsf.py:193-409, 739-806.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float mat_at(const float* m, int n, float scalar, long long N, int comp, long long c) {
+    if (!m) return scalar;
+    const int cc = comp < n ? comp : n - 1;  // an isotropic array serves every component
+    return __ldg(m + cc * N + c);
+}
+
+template <bool ESIDE>
+__global__ void k_source(const Geo g, const DSource s, const int* __restrict__ tp, float* F, const float* mat, int n_mat,
+                         float mat_scalar, int inverse) {
+    const int t = *tp;
+    const int ti = t + 1;
+    if (!s.on[ti]) return;
+    const float teff = s.teff[ti] + (ESIDE ? 0.f : 0.5f);
+    const float ph0 = ESIDE ? s.phE[ti] : s.phH[ti];
+    const int wall = ESIDE ? g.pec : g.pmc;
+    if (s.kind == FDTD_SRC_DIPOLE) {
+        if (blockIdx.x != 0 || threadIdx.x != 0) return;
+        if (ESIDE == (bool)s.magnetic) return;
+        const int i = s.lo[0], j = s.lo[1], k = s.lo[2];
+        if (face_zero(g, wall, s.comp, i, j, k)) return;
+        const float amp = profile_amp(s, teff, ph0);
+        const float sg = inverse ? 1.f : -1.f;
+        F[s.comp * g.N + cell_index(g, i, j, k)] += sg * (s.coef * amp);
+        return;
+    }
+    const int n = s.normal, ax = (n + 1) % 3, bx = (n + 2) % 3;
+    const int ext[3] = {s.hi[0] - s.lo[0], s.hi[1] - s.lo[1], s.hi[2] - s.lo[2]};
+    const long long P = (long long)ext[0] * ext[1] * ext[2];
+    const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= P) return;
+    const int kk = (int)(f % ext[2]);
+    const int jj = (int)((f / ext[2]) % ext[1]);
+    const int ii = (int)(f / ((long long)ext[2] * ext[1]));
+    const int i = s.lo[0] + ii, j = s.lo[1] + jj, k = s.lo[2] + kk;
+    const long long c = cell_index(g, i, j, k);
+    const float sg = inverse ? -s.sign : s.sign;
+    const float* inc = ESIDE ? s.incH : s.incE;
+    const float* off = ESIDE ? s.offH : s.offE;
+    const float oa = __ldg(off + ax * P + f), ob = __ldg(off + bx * P + f);
+    const float amp_a = profile_amp(s, teff + oa, ph0 + s.omega_dt * oa);
+    const float amp_b = profile_amp(s, teff + ob, ph0 + s.omega_dt * ob);
+    const float inc_a = __ldg(inc + ax * P + f) * amp_a;
+    const float inc_b = __ldg(inc + bx * P + f) * amp_b;
+    if (ESIDE) {
+        // E[a] += sign c inv_eps[a] H_inc,b ;  E[b] -= sign c inv_eps[b] H_inc,a
+        if (!face_zero(g, wall, ax, i, j, k))
+            F[ax * g.N + c] += sg * (inc_b * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, ax, c));
+        if (!face_zero(g, wall, bx, i, j, k))
+            F[bx * g.N + c] -= sg * (inc_a * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, bx, c));
+    } else {
+        // H[b] += sign c inv_mu[b] E_inc,a ;  H[a] -= sign c inv_mu[a] E_inc,b
+        if (!face_zero(g, wall, bx, i, j, k))
+            F[bx * g.N + c] += sg * (inc_a * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, bx, c));
+        if (!face_zero(g, wall, ax, i, j, k))
+            F[ax * g.N + c] -= sg * (inc_b * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, ax, c));
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Detectors (fdtdx/fdtd/update.py:1040-1137).  Fields are co-located at the E_z
+// point (i, j, k+1/2) with H time-centred as (H_prev + H)/2 when
+// exact_interpolation is set (fdtdx/core/physics/curl.py:86-224).
+// ---------------------------------------------------------------------------------
+struct DetFields {
+    const float* E;
+    const float* Hp;   // H before this step's H update
+    const float* H;    // H after it
+    const float* inv_eps;
+    int n_eps;
+    const float* inv_mu;
+    int n_mu;
+    float mu_scalar;
+};
+
+__device__ __forceinline__ float hav(const Geo& g, const DetFields& f, int comp, int i, int j, int k) {
+    return (ld_halo(g, f.Hp, comp, i, j, k) + ld_halo(g, f.H, comp, i, j, k)) / 2.f;
+}
+
+__device__ void colocate(const Geo& g, const DetFields& f, int exact, int mask, int i, int j, int k, float v[6]) {
+    const long long c = cell_index(g, i, j, k);
+    if (!exact) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            v[q] = (mask >> q & 1) ? __ldg(f.E + q * g.N + c) : 0.f;
+            v[3 + q] = (mask >> (3 + q) & 1) ? __ldg(f.H + q * g.N + c) : 0.f;
+        }
+        return;
+    }
+    if (mask & 1) {
+        const float lo = 0.5f * (ld_halo(g, f.E, 0, i, j, k) + ld_halo(g, f.E, 0, i - 1, j, k));
+        const float up = 0.5f * (ld_halo(g, f.E, 0, i, j, k + 1) + ld_halo(g, f.E, 0, i - 1, j, k + 1));
+        v[0] = (lo + up) / 2.f;
+    }
+    if (mask & 2) {
+        const float lo = 0.5f * (ld_halo(g, f.E, 1, i, j, k) + ld_halo(g, f.E, 1, i, j - 1, k));
+        const float up = 0.5f * (ld_halo(g, f.E, 1, i, j, k + 1) + ld_halo(g, f.E, 1, i, j - 1, k + 1));
+        v[1] = (lo + up) / 2.f;
+    }
+    if (mask & 4) v[2] = __ldg(f.E + 2 * g.N + c);
+    if (mask & 8) v[3] = 0.5f * (hav(g, f, 0, i, j, k) + hav(g, f, 0, i, j - 1, k));
+    if (mask & 16) v[4] = 0.5f * (hav(g, f, 1, i, j, k) + hav(g, f, 1, i - 1, j, k));
+    if (mask & 32) {
+        const float lx = 0.5f * (hav(g, f, 2, i, j, k) + hav(g, f, 2, i - 1, j, k));
+        const float lxy = 0.5f * (lx + 0.5f * (hav(g, f, 2, i, j - 1, k) + hav(g, f, 2, i - 1, j - 1, k)));
+        const float ux = 0.5f * (hav(g, f, 2, i, j, k + 1) + hav(g, f, 2, i - 1, j, k + 1));
+        const float uxy = 0.5f * (ux + 0.5f * (hav(g, f, 2, i, j - 1, k + 1) + hav(g, f, 2, i - 1, j - 1, k + 1)));
+        v[5] = (lxy + uxy) / 2.f;
+    }
+}
+
+template <int BLOCK>
+__device__ __forceinline__ float block_sum(float x, float* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[w] = x;
+    __syncthreads();
+    float r = 0.f;
+    if (w == 0) {
+        r = lane < BLOCK / 32 ? sh[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    return r;  // valid in thread 0
+}
+
+constexpr int kDetBlock = 256;
+
+__global__ void __launch_bounds__(kDetBlock) k_detector(const Geo g, const DDet d, const int* __restrict__ tp,
+                                                        const DetFields f, void* state) {
+    __shared__ float sh[kDetBlock / 32];
+    const int t = *tp;
+    const int slot = __ldg(d.slot + t + 1);
+    if (slot < 0) return;
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = r < d.R;
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int i = 0, j = 0, k = 0;
+    if (valid) {
+        k = d.lo[2] + (int)(r % d.rz);
+        j = d.lo[1] + (int)((r / d.rz) % d.ry);
+        i = d.lo[0] + (int)(r / ((long long)d.rz * d.ry));
+    }
+    int need = d.comp_mask;
+    if (d.kind == FDTD_DET_FLUX || d.kind == FDTD_DET_ENERGY) need = 63;
+    if (valid) colocate(g, f, d.exact, need, i, j, k, v);
+
+    // gather the recorded values of this cell
+    float out[6];
+    int nout = 0;
+    if (d.kind == FDTD_DET_FIELD || d.kind == FDTD_DET_PHASOR) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+            if (d.comp_mask >> q & 1) out[nout++] = v[q];
+    } else if (d.kind == FDTD_DET_FLUX) {
+        // S = E x H (real fields; fdtdx/core/physics/metrics.py:99-117)
+        const float S[3] = {v[1] * v[5] - v[2] * v[4], v[2] * v[3] - v[0] * v[5], v[0] * v[4] - v[1] * v[3]};
+        if (d.keep_all) {
+            out[0] = d.flux_sign * S[0];
+            out[1] = d.flux_sign * S[1];
+            out[2] = d.flux_sign * S[2];
+            nout = 3;
+        } else {
+            out[0] = d.flux_sign * S[d.flux_axis];
+            nout = 1;
+        }
+    } else {  // energy: 0.5 sum eps |E|^2 + 0.5 sum mu |H|^2 (fdtdx/core/physics/metrics.py:55-65)
+        float e = 0.f, h = 0.f;
+        if (valid) {
+            const long long c = cell_index(g, i, j, k);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                e += 0.5f * (1.f / mat_at(f.inv_eps, f.n_eps, 1.f, g.N, q, c)) * (v[q] * v[q]);
+                h += 0.5f * (1.f / mat_at(f.inv_mu, f.n_mu, f.mu_scalar, g.N, q, c)) * (v[3 + q] * v[3 + q]);
+            }
+        }
+        out[0] = e + h;
+        nout = 1;
+    }
+
+    if (d.kind == FDTD_DET_PHASOR) {
+        const float2* wt = d.w + (long long)(t + 1) * d.nfreq;
+        if (!d.reduce) {
+            if (!valid) return;
+            float2* st = reinterpret_cast<float2*>(state);
+            for (int fq = 0; fq < d.nfreq; ++fq) {
+                const float2 w = __ldg(wt + fq);
+                for (int q = 0; q < nout; ++q) {
+                    float2* p = st + ((long long)fq * nout + q) * d.R + r;
+                    float2 z = *p;
+                    if (d.inverse) { z.x -= out[q] * w.x; z.y -= out[q] * w.y; }
+                    else { z.x += out[q] * w.x; z.y += out[q] * w.y; }
+                    *p = z;
+                }
+            }
+            return;
+        }
+        // volume mean of the complex samples: partials (2 floats per freq and component)
+        for (int fq = 0; fq < d.nfreq; ++fq) {
+            const float2 w = __ldg(wt + fq);
+            for (int q = 0; q < nout; ++q) {
+                const float re = block_sum<kDetBlock>(valid ? out[q] * w.x : 0.f, sh);
+                const float im = block_sum<kDetBlock>(valid ? out[q] * w.y : 0.f, sh);
+                if (threadIdx.x == 0) {
+                    d.partial[(long long)blockIdx.x * d.ncomp + 2 * (fq * nout + q)] = re;
+                    d.partial[(long long)blockIdx.x * d.ncomp + 2 * (fq * nout + q) + 1] = im;
+                }
+            }
+        }
+        return;
+    }
+    if (!d.reduce) {
+        if (!valid) return;
+        float* st = reinterpret_cast<float*>(state);
+        for (int q = 0; q < nout; ++q) st[((long long)slot * nout + q) * d.R + r] = out[q];
+        return;
+    }
+    for (int q = 0; q < nout; ++q) {
+        const float s = block_sum<kDetBlock>(valid ? out[q] : 0.f, sh);
+        if (threadIdx.x == 0) d.partial[(long long)blockIdx.x * d.ncomp + q] = s;
+    }
+}
+
+// Sums the block partials of a reducing detector in a fixed order (deterministic)
+// and writes (field, flux, energy) or accumulates (phasor) the state entry.
+__global__ void __launch_bounds__(kDetBlock) k_detector_finalize(const DDet d, const int* __restrict__ tp, void* state) {
+    __shared__ float sh[kDetBlock / 32];
+    const int t = *tp;
+    const int slot = __ldg(d.slot + t + 1);
+    if (slot < 0) return;
+    for (int q = 0; q < d.ncomp; ++q) {
+        float acc = 0.f;
+        for (int b = threadIdx.x; b < d.nblocks; b += blockDim.x) acc += d.partial[(long long)b * d.ncomp + q];
+        const float s = block_sum<kDetBlock>(acc, sh);
+        if (threadIdx.x == 0) {
+            if (d.kind == FDTD_DET_PHASOR) {
+                float* st = reinterpret_cast<float*>(state);
+                const float v = s / (float)d.R;
+                st[q] += d.inverse ? -v : v;
+            } else {
+                float* st = reinterpret_cast<float*>(state);
+                const float scale = d.kind == FDTD_DET_FIELD ? 1.f / (float)d.R : d.cell_weight;
+                st[(long long)slot * d.ncomp + q] = s * scale;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// PML-interface recording (fdtdx/fdtd/misc.py:10-66, fdtdx/fdtd/update.py:1140-1222):
+// E and H on the innermost layer of every slab.  Slot layout: for field in (E, H):
+// for slab s: (3, plane_s).  RESTORE copies the slot back into the fields.
+// ---------------------------------------------------------------------------------
+struct IfaceDev {
+    int n;
+    int axis[FDTD_MAX_SLABS];
+    int layer[FDTD_MAX_SLABS];
+    long long start[FDTD_MAX_SLABS + 1];  // prefix sums of plane sizes
+    long long total;                     // sum of plane sizes
+};
+
+template <typename T, bool RESTORE>
+__global__ void k_interfaces(const Geo g, const IfaceDev ifc, const int* __restrict__ tp, int n_slots, float* E, float* H,
+                             T* rec) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ifc.total) return;
+    int t = *tp;
+    if (t < 0) t += n_slots;  // a negative step index wraps like a JAX index
+    if (t < 0 || t >= n_slots) return;
+    int s = 0;
+    while (s + 1 < ifc.n && q >= ifc.start[s + 1]) ++s;
+    const long long pidx = q - ifc.start[s];
+    int i, j, k;
+    if (ifc.axis[s] == 0) { i = ifc.layer[s]; j = (int)(pidx / g.nz); k = (int)(pidx % g.nz); }
+    else if (ifc.axis[s] == 1) { j = ifc.layer[s]; i = (int)(pidx / g.nz); k = (int)(pidx % g.nz); }
+    else { k = ifc.layer[s]; i = (int)(pidx / g.ny); j = (int)(pidx % g.ny); }
+    const long long c = cell_index(g, i, j, k);
+    const long long P = ifc.start[s + 1] - ifc.start[s];
+    T* slotp = rec + (long long)t * 6 * ifc.total;
+#pragma unroll
+    for (int fld = 0; fld < 2; ++fld) {
+        float* F = fld == 0 ? E : H;
+        T* base = slotp + fld * 3 * ifc.total + 3 * ifc.start[s];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            if (RESTORE) F[comp * g.N + c] = from_storage(base[comp * P + pidx]);
+            else base[comp * P + pidx] = to_storage<T>(F[comp * g.N + c]);
+        }
+    }
+}
+
+__global__ void k_set_step(int* tp, int t) { *tp = t; }
+__global__ void k_advance(int* tp, int delta) { *tp += delta; }
+
+}  // namespace fdtd

@@ -1,0 +1,623 @@
+// Host side of the C ABI declared in include/fdtd_gb300.h: plan construction
+// (device copies of the small per-scene tables), the per-step launch sequence,
+// CUDA-graph capture of the step loop and the reverse (time-reversed) loop.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fdtd_kernels.cuh"
+#include "fdtd_adjoint.cuh"
+
+using namespace fdtd;
+
+struct FdtdPlan {
+    FdtdDesc d;  // copy of the description; host table pointers are not used after create
+    Geo g;
+    int n_table = 0;
+    DSlab slab[FDTD_MAX_SLABS];
+    DSource src[FDTD_MAX_SOURCES];
+    DDet det[FDTD_MAX_DETECTORS];
+    IfaceDev ifc{};
+    long long iface_floats = 0;  // floats per recording slot (6 * ifc.total)
+    char* dmem = nullptr;
+    size_t dmem_bytes = 0;
+    int* d_t = nullptr;          // device time-step counter read by every kernel
+    float* h_twin = nullptr;     // second H buffer (ping-pong) when a detector needs H before the H update
+    bool need_hprev = false;
+    // graph cache for the forward loop
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    FdtdBuffers gbufs{};
+    int gsteps = 0;
+    cudaStream_t cap_stream = nullptr;
+    std::string err;
+};
+
+namespace {
+
+size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+int fail(FdtdPlan* p, int code, const std::string& msg) {
+    if (p) p->err = msg;
+    return code;
+}
+
+int cuda_fail(FdtdPlan* p, cudaError_t e, const char* where) {
+    return fail(p, FDTD_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Layout of the plan's single device allocation.
+struct Arena {
+    size_t off = 0;
+    size_t take(size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes);
+        return o;
+    }
+};
+
+long long face_cells(const FdtdSourceDesc& s) {
+    return (long long)(s.hi[0] - s.lo[0]) * (s.hi[1] - s.lo[1]) * (s.hi[2] - s.lo[2]);
+}
+
+int popcount6(int m) {
+    int c = 0;
+    for (int q = 0; q < 6; ++q) c += (m >> q) & 1;
+    return c;
+}
+
+int det_ncomp(const FdtdDetectorDesc& dd) {
+    if (dd.kind == FDTD_DET_FIELD) return popcount6(dd.comp_mask);
+    if (dd.kind == FDTD_DET_PHASOR) return dd.reduce_volume ? 2 * dd.n_freq * popcount6(dd.comp_mask) : popcount6(dd.comp_mask);
+    if (dd.kind == FDTD_DET_FLUX) return dd.keep_all ? 3 : 1;
+    return 1;
+}
+
+bool det_needs_h(const FdtdDetectorDesc& dd) {
+    if (!dd.exact_interpolation) return false;  // non-exact detectors read H after the update only
+    if (dd.kind == FDTD_DET_FLUX || dd.kind == FDTD_DET_ENERGY) return true;
+    return (dd.comp_mask & 56) != 0;
+}
+
+int validate(const FdtdDesc* d, std::string& why) {
+    if (d->nx <= 0 || d->ny <= 0 || d->nz <= 0) { why = "grid dims must be positive"; return FDTD_EINVAL; }
+    if ((long long)d->nx * d->ny * d->nz * 3 >= (1ll << 40)) { why = "grid too large"; return FDTD_EINVAL; }
+    if (d->nx > 65535) { why = "nx above 65535 is not supported"; return FDTD_EINVAL; }
+    if (d->n_steps_total < 0) { why = "n_steps_total must be >= 0"; return FDTD_EINVAL; }
+    if (d->n_eps != 1 && d->n_eps != 3) { why = "n_eps must be 1 or 3"; return FDTD_EINVAL; }
+    if (d->n_mu != 0 && d->n_mu != 1 && d->n_mu != 3) { why = "n_mu must be 0, 1 or 3"; return FDTD_EINVAL; }
+    if (d->n_sigma_E < 0 || d->n_sigma_E > 3 || d->n_sigma_E == 2) { why = "n_sigma_E must be 0, 1 or 3"; return FDTD_EINVAL; }
+    if (d->n_sigma_H < 0 || d->n_sigma_H > 3 || d->n_sigma_H == 2) { why = "n_sigma_H must be 0, 1 or 3"; return FDTD_EINVAL; }
+    if (d->n_slabs < 0 || d->n_slabs > FDTD_MAX_SLABS) { why = "too many slabs"; return FDTD_EINVAL; }
+    if (d->n_sources < 0 || d->n_sources > FDTD_MAX_SOURCES) { why = "too many sources"; return FDTD_EINVAL; }
+    if (d->n_detectors < 0 || d->n_detectors > FDTD_MAX_DETECTORS) { why = "too many detectors"; return FDTD_EINVAL; }
+    const int n[3] = {d->nx, d->ny, d->nz};
+    for (int s = 0; s < d->n_slabs; ++s) {
+        const FdtdSlabDesc& sl = d->slabs[s];
+        if (sl.axis < 0 || sl.axis > 2 || sl.thickness <= 0 || sl.thickness > n[sl.axis] || !sl.coef ||
+            (sl.direction != -1 && sl.direction != 1)) {
+            why = "invalid slab " + std::to_string(s);
+            return FDTD_EINVAL;
+        }
+    }
+    for (int s = 0; s < d->n_sources; ++s) {
+        const FdtdSourceDesc& so = d->sources[s];
+        for (int a = 0; a < 3; ++a)
+            if (so.lo[a] < 0 || so.hi[a] > n[a] || so.hi[a] <= so.lo[a]) { why = "source box out of range"; return FDTD_EINVAL; }
+        if (!so.phase_E || !so.phase_H || !so.teff || !so.on) { why = "source tables missing"; return FDTD_EINVAL; }
+        if (so.kind == FDTD_SRC_PLANE) {
+            if (so.normal_axis < 0 || so.normal_axis > 2 || so.hi[so.normal_axis] - so.lo[so.normal_axis] != 1 || !so.inc_E ||
+                !so.inc_H || !so.off_E || !so.off_H) {
+                why = "invalid plane source";
+                return FDTD_EINVAL;
+            }
+        } else if (so.kind == FDTD_SRC_DIPOLE) {
+            if (so.component < 0 || so.component > 2) { why = "invalid dipole component"; return FDTD_EINVAL; }
+        } else {
+            why = "unknown source kind";
+            return FDTD_EINVAL;
+        }
+    }
+    for (int q = 0; q < d->n_detectors; ++q) {
+        const FdtdDetectorDesc& dd = d->detectors[q];
+        for (int a = 0; a < 3; ++a)
+            if (dd.lo[a] < 0 || dd.hi[a] > n[a] || dd.hi[a] <= dd.lo[a]) { why = "detector box out of range"; return FDTD_EINVAL; }
+        if (dd.kind < 0 || dd.kind > 3 || !dd.slot) { why = "invalid detector"; return FDTD_EINVAL; }
+        if ((dd.kind == FDTD_DET_FIELD || dd.kind == FDTD_DET_PHASOR) && (dd.comp_mask <= 0 || dd.comp_mask > 63)) {
+            why = "invalid detector component mask";
+            return FDTD_EINVAL;
+        }
+        if (dd.kind == FDTD_DET_PHASOR && (dd.n_freq <= 0 || dd.n_freq > FDTD_MAX_FREQS || !dd.weights)) {
+            why = "invalid phasor detector";
+            return FDTD_EINVAL;
+        }
+        if (dd.kind == FDTD_DET_FLUX && (dd.flux_axis < 0 || dd.flux_axis > 2)) { why = "invalid flux axis"; return FDTD_EINVAL; }
+    }
+    if (d->recording_dtype < 0 || d->recording_dtype > 2) { why = "invalid recording dtype"; return FDTD_EINVAL; }
+    return FDTD_OK;
+}
+
+size_t rec_elem_bytes(int dt) { return dt == 0 ? 4 : 2; }
+
+}  // namespace
+
+extern "C" {
+
+int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
+    if (!desc || !out) return FDTD_EINVAL;
+    *out = nullptr;
+    std::string why;
+    if (int rc = validate(desc, why)) {
+        // no plan exists to carry the message: print it once
+        fprintf(stderr, "fdtd_plan_create: %s\n", why.c_str());
+        return rc;
+    }
+    FdtdPlan* p = new FdtdPlan();
+    p->d = *desc;
+    const FdtdDesc& d = p->d;
+    p->n_table = d.n_steps_total + 2;
+    p->g.nx = d.nx; p->g.ny = d.ny; p->g.nz = d.nz;
+    p->g.N = (long long)d.nx * d.ny * d.nz;
+    p->g.px = d.periodic[0]; p->g.py = d.periodic[1]; p->g.pz = d.periodic[2];
+    p->g.c = d.courant;
+    p->g.eta0 = (float)(4e-7 * M_PI * 299792458.0);
+    p->g.pec = d.pec_faces; p->g.pmc = d.pmc_faces;
+
+    // ---- lay out the device arena
+    Arena ar;
+    const size_t o_t = ar.take(sizeof(int) * 4);
+    std::vector<size_t> o_slab(d.n_slabs);
+    for (int s = 0; s < d.n_slabs; ++s) o_slab[s] = ar.take(sizeof(float) * 6 * d.slabs[s].thickness);
+    struct SrcOff { size_t incE, incH, offE, offH, phE, phH, teff, on; };
+    std::vector<SrcOff> o_src(d.n_sources);
+    const size_t tbl = (size_t)p->n_table;
+    for (int s = 0; s < d.n_sources; ++s) {
+        const FdtdSourceDesc& so = d.sources[s];
+        SrcOff& o = o_src[s];
+        if (so.kind == FDTD_SRC_PLANE) {
+            const size_t P = (size_t)face_cells(so);
+            o.incE = ar.take(4 * 3 * P); o.incH = ar.take(4 * 3 * P);
+            o.offE = ar.take(4 * 3 * P); o.offH = ar.take(4 * 3 * P);
+        }
+        o.phE = ar.take(4 * tbl); o.phH = ar.take(4 * tbl); o.teff = ar.take(4 * tbl); o.on = ar.take(tbl);
+    }
+    struct DetOff { size_t slot, w, partial; };
+    std::vector<DetOff> o_det(d.n_detectors);
+    for (int q = 0; q < d.n_detectors; ++q) {
+        const FdtdDetectorDesc& dd = d.detectors[q];
+        DetOff& o = o_det[q];
+        o.slot = ar.take(4 * tbl);
+        o.w = dd.kind == FDTD_DET_PHASOR ? ar.take(8 * tbl * dd.n_freq) : 0;
+        const long long R = (long long)(dd.hi[0] - dd.lo[0]) * (dd.hi[1] - dd.lo[1]) * (dd.hi[2] - dd.lo[2]);
+        const long long nb = (R + kDetBlock - 1) / kDetBlock;
+        const bool red = dd.reduce_volume || dd.kind == FDTD_DET_PHASOR ? dd.reduce_volume : dd.reduce_volume;
+        o.partial = red ? ar.take(4 * (size_t)nb * det_ncomp(dd)) : 0;
+        if (det_needs_h(dd)) p->need_hprev = true;
+    }
+    size_t o_twin = 0;
+    if (p->need_hprev) o_twin = ar.take(sizeof(float) * 3 * (size_t)p->g.N);
+    p->dmem_bytes = ar.off;
+
+    cudaError_t e = cudaMalloc(&p->dmem, p->dmem_bytes);
+    if (e != cudaSuccess) {
+        delete p;
+        fprintf(stderr, "fdtd_plan_create: cudaMalloc(%zu) failed: %s\n", ar.off, cudaGetErrorString(e));
+        return FDTD_ENOMEM;
+    }
+    auto up = [&](size_t off, const void* src, size_t bytes) -> cudaError_t {
+        if (!bytes) return cudaSuccess;
+        return cudaMemcpy(p->dmem + off, src, bytes, cudaMemcpyHostToDevice);
+    };
+    p->d_t = reinterpret_cast<int*>(p->dmem + o_t);
+    e = cudaMemset(p->d_t, 0, sizeof(int) * 4);
+
+    const int n3[3] = {d.nx, d.ny, d.nz};
+    for (int s = 0; s < d.n_slabs && e == cudaSuccess; ++s) {
+        const FdtdSlabDesc& sl = d.slabs[s];
+        DSlab& ds = p->slab[s];
+        ds.axis = sl.axis;
+        ds.L = sl.thickness;
+        ds.lo = sl.direction < 0 ? 0 : n3[sl.axis] - sl.thickness;
+        ds.kappa_one = sl.kappa_is_one;
+        ds.sx = sl.axis == 0 ? sl.thickness : d.nx;
+        ds.sy = sl.axis == 1 ? sl.thickness : d.ny;
+        ds.sz = sl.axis == 2 ? sl.thickness : d.nz;
+        ds.coef = reinterpret_cast<const float*>(p->dmem + o_slab[s]);
+        e = up(o_slab[s], sl.coef, sizeof(float) * 6 * sl.thickness);
+        // interface layer: the slab's innermost cell layer (boundary.py:126-132)
+        p->ifc.axis[s] = sl.axis;
+        p->ifc.layer[s] = sl.direction < 0 ? sl.thickness - 1 : n3[sl.axis] - sl.thickness;
+    }
+    p->ifc.n = d.n_slabs;
+    p->ifc.start[0] = 0;
+    for (int s = 0; s < d.n_slabs; ++s) {
+        const int a = d.slabs[s].axis;
+        const long long plane = (long long)(a == 0 ? 1 : d.nx) * (a == 1 ? 1 : d.ny) * (a == 2 ? 1 : d.nz);
+        p->ifc.start[s + 1] = p->ifc.start[s] + plane;
+    }
+    p->ifc.total = p->ifc.start[d.n_slabs];
+    p->iface_floats = 6 * p->ifc.total;
+
+    for (int s = 0; s < d.n_sources && e == cudaSuccess; ++s) {
+        const FdtdSourceDesc& so = d.sources[s];
+        DSource& ds = p->src[s];
+        const SrcOff& o = o_src[s];
+        ds.kind = so.kind; ds.comp = so.component; ds.magnetic = so.magnetic; ds.normal = so.normal_axis;
+        ds.profile = so.profile;
+        for (int a = 0; a < 3; ++a) { ds.lo[a] = so.lo[a]; ds.hi[a] = so.hi[a]; }
+        ds.sign = so.sign; ds.coef = so.coef; ds.omega_dt = so.omega_dt; ds.ramp_inv = so.ramp_inv_steps;
+        ds.t0 = so.t0_steps; ds.inv2s2 = so.inv_two_sigma2;
+        ds.incE = ds.incH = ds.offE = ds.offH = nullptr;
+        if (so.kind == FDTD_SRC_PLANE) {
+            const size_t P = (size_t)face_cells(so);
+            ds.incE = reinterpret_cast<const float*>(p->dmem + o.incE);
+            ds.incH = reinterpret_cast<const float*>(p->dmem + o.incH);
+            ds.offE = reinterpret_cast<const float*>(p->dmem + o.offE);
+            ds.offH = reinterpret_cast<const float*>(p->dmem + o.offH);
+            e = up(o.incE, so.inc_E, 12 * P);
+            if (e == cudaSuccess) e = up(o.incH, so.inc_H, 12 * P);
+            if (e == cudaSuccess) e = up(o.offE, so.off_E, 12 * P);
+            if (e == cudaSuccess) e = up(o.offH, so.off_H, 12 * P);
+        }
+        ds.phE = reinterpret_cast<const float*>(p->dmem + o.phE);
+        ds.phH = reinterpret_cast<const float*>(p->dmem + o.phH);
+        ds.teff = reinterpret_cast<const float*>(p->dmem + o.teff);
+        ds.on = reinterpret_cast<const uint8_t*>(p->dmem + o.on);
+        if (e == cudaSuccess) e = up(o.phE, so.phase_E, 4 * tbl);
+        if (e == cudaSuccess) e = up(o.phH, so.phase_H, 4 * tbl);
+        if (e == cudaSuccess) e = up(o.teff, so.teff, 4 * tbl);
+        if (e == cudaSuccess) e = up(o.on, so.on, tbl);
+    }
+    for (int q = 0; q < d.n_detectors && e == cudaSuccess; ++q) {
+        const FdtdDetectorDesc& dd = d.detectors[q];
+        DDet& ds = p->det[q];
+        const DetOff& o = o_det[q];
+        ds.kind = dd.kind; ds.comp_mask = dd.comp_mask; ds.exact = dd.exact_interpolation; ds.reduce = dd.reduce_volume;
+        ds.inverse = dd.inverse; ds.nfreq = dd.n_freq; ds.flux_axis = dd.flux_axis; ds.keep_all = dd.keep_all;
+        ds.flux_sign = dd.flux_sign; ds.cell_weight = dd.cell_weight;
+        for (int a = 0; a < 3; ++a) { ds.lo[a] = dd.lo[a]; ds.hi[a] = dd.hi[a]; }
+        ds.rx = dd.hi[0] - dd.lo[0]; ds.ry = dd.hi[1] - dd.lo[1]; ds.rz = dd.hi[2] - dd.lo[2];
+        ds.R = (long long)ds.rx * ds.ry * ds.rz;
+        ds.nblocks = (int)((ds.R + kDetBlock - 1) / kDetBlock);
+        ds.ncomp = det_ncomp(dd);
+        ds.slot = reinterpret_cast<const int*>(p->dmem + o.slot);
+        ds.w = dd.kind == FDTD_DET_PHASOR ? reinterpret_cast<const float2*>(p->dmem + o.w) : nullptr;
+        ds.partial = o.partial ? reinterpret_cast<float*>(p->dmem + o.partial) : nullptr;
+        e = up(o.slot, dd.slot, 4 * tbl);
+        if (e == cudaSuccess && dd.kind == FDTD_DET_PHASOR) e = up(o.w, dd.weights, 8 * tbl * dd.n_freq);
+    }
+    if (p->need_hprev) p->h_twin = reinterpret_cast<float*>(p->dmem + o_twin);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "fdtd_plan_create: %s\n", cudaGetErrorString(e));
+        cudaFree(p->dmem);
+        delete p;
+        return FDTD_ECUDA;
+    }
+    // strip the host pointers from the stored description
+    for (int s = 0; s < p->d.n_slabs; ++s) p->d.slabs[s].coef = nullptr;
+    for (int s = 0; s < p->d.n_sources; ++s) {
+        FdtdSourceDesc& so = p->d.sources[s];
+        so.inc_E = so.inc_H = so.off_E = so.off_H = so.phase_E = so.phase_H = so.teff = nullptr;
+        so.on = nullptr;
+    }
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        p->d.detectors[q].slot = nullptr;
+        p->d.detectors[q].weights = nullptr;
+    }
+    *out = p;
+    return FDTD_OK;
+}
+
+void fdtd_plan_destroy(FdtdPlan* p) {
+    if (!p) return;
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+    cudaFree(p->dmem);
+    delete p;
+}
+
+const char* fdtd_last_error(const FdtdPlan* p) { return p ? p->err.c_str() : "no plan"; }
+
+int64_t fdtd_interface_floats(const FdtdPlan* p) { return p ? p->iface_floats : 0; }
+
+int64_t fdtd_plan_device_bytes(const FdtdPlan* p) { return p ? (int64_t)p->dmem_bytes : 0; }
+
+}  // extern "C"
+
+// -------------------------------------------------------------------------------------
+// launch helpers
+// -------------------------------------------------------------------------------------
+namespace {
+
+dim3 update_grid(const Geo& g) { return dim3((g.nz + 31) / 32, (g.ny + 7) / 8, g.nx); }
+const dim3 kUpdBlock(32, 8, 1);
+
+UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout) {
+    UpdArgs a{};
+    a.g = p->g;
+    a.F = F;
+    a.Uin = Uin;
+    a.Uout = Uout;
+    if (eside) {
+        a.mat = b->inv_eps; a.n_mat = p->d.n_eps; a.mat_scalar = 1.f;
+        a.sig = p->d.n_sigma_E ? b->sigma_E : nullptr; a.n_sig = p->d.n_sigma_E;
+    } else {
+        a.mat = p->d.n_mu ? b->inv_mu : nullptr; a.n_mat = p->d.n_mu ? p->d.n_mu : 1; a.mat_scalar = p->d.inv_mu_scalar;
+        a.sig = p->d.n_sigma_H ? b->sigma_H : nullptr; a.n_sig = p->d.n_sigma_H;
+    }
+    a.n_slab = p->d.n_slabs;
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        a.slab[s] = p->slab[s];
+        a.psi1[s] = eside ? b->psi_E[s][0] : b->psi_H[s][0];
+        a.psi2[s] = eside ? b->psi_E[s][1] : b->psi_H[s][1];
+    }
+    return a;
+}
+
+void launch_sources(const FdtdPlan* p, const FdtdBuffers* b, bool eside, float* F, int inverse, cudaStream_t st) {
+    for (int s = 0; s < p->d.n_sources; ++s) {
+        const DSource& so = p->src[s];
+        if (so.kind == FDTD_SRC_DIPOLE && (bool)so.magnetic == eside) continue;
+        const long long P = so.kind == FDTD_SRC_PLANE
+                                ? (long long)(so.hi[0] - so.lo[0]) * (so.hi[1] - so.lo[1]) * (so.hi[2] - so.lo[2])
+                                : 1;
+        const int blocks = (int)((P + 255) / 256);
+        if (eside)
+            k_source<true><<<blocks, 256, 0, st>>>(p->g, so, p->d_t, F, b->inv_eps, p->d.n_eps, 1.f, inverse);
+        else
+            k_source<false><<<blocks, 256, 0, st>>>(p->g, so, p->d_t, F, p->d.n_mu ? b->inv_mu : nullptr,
+                                                    p->d.n_mu ? p->d.n_mu : 1, p->d.inv_mu_scalar, inverse);
+    }
+}
+
+int sources_launched(const FdtdPlan* p, bool eside) {
+    int n = 0;
+    for (int s = 0; s < p->d.n_sources; ++s) {
+        const DSource& so = p->src[s];
+        if (so.kind == FDTD_SRC_DIPOLE && (bool)so.magnetic == eside) continue;
+        ++n;
+    }
+    return n;
+}
+
+template <typename T, bool RESTORE>
+void launch_ifaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t st) {
+    const int blocks = (int)((p->ifc.total + 255) / 256);
+    k_interfaces<T, RESTORE><<<blocks, 256, 0, st>>>(p->g, p->ifc, p->d_t, p->d.n_steps_total, b->E, H,
+                                                     reinterpret_cast<T*>(b->recording));
+}
+
+template <bool RESTORE>
+void interfaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t st) {
+    if (!p->d.n_slabs || !b->recording) return;
+    if (p->d.recording_dtype == 0) launch_ifaces<float, RESTORE>(p, b, H, st);
+    else if (p->d.recording_dtype == 1) launch_ifaces<__nv_bfloat16, RESTORE>(p, b, H, st);
+    else launch_ifaces<__half, RESTORE>(p, b, H, st);
+}
+
+// One forward step (fdtdx/fdtd/forward.py:83-156): update_E, E sources (+PEC inside the
+// update), update_H, H sources (+PMC), interface recording, detectors, advance t.
+void launch_forward_step(const FdtdPlan* p, const FdtdBuffers* b, float* Hcur, float* Hnext, cudaStream_t st) {
+    const dim3 grid = update_grid(p->g);
+    k_update_E<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, Hcur, b->E, b->E));
+    launch_sources(p, b, true, b->E, 0, st);
+    k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, false, b->E, Hcur, Hnext));
+    launch_sources(p, b, false, Hnext, 0, st);
+    if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
+    DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
+                p->d.inv_mu_scalar};
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        const DDet& dd = p->det[q];
+        k_detector<<<dd.nblocks, kDetBlock, 0, st>>>(p->g, dd, p->d_t, f, b->det_state[q]);
+        if (dd.reduce) k_detector_finalize<<<1, kDetBlock, 0, st>>>(dd, p->d_t, b->det_state[q]);
+    }
+    k_advance<<<1, 1, 0, st>>>(p->d_t, 1);
+}
+
+int check_bufs(FdtdPlan* p, const FdtdBuffers* b) {
+    if (!b || !b->E || !b->H || !b->inv_eps) return fail(p, FDTD_EINVAL, "E, H and inv_eps buffers are required");
+    if (p->d.n_mu && !b->inv_mu) return fail(p, FDTD_EINVAL, "inv_mu buffer required");
+    if (p->d.n_sigma_E && !b->sigma_E) return fail(p, FDTD_EINVAL, "sigma_E buffer required");
+    if (p->d.n_sigma_H && !b->sigma_H) return fail(p, FDTD_EINVAL, "sigma_H buffer required");
+    for (int s = 0; s < p->d.n_slabs; ++s)
+        if (!b->psi_E[s][0] || !b->psi_E[s][1] || !b->psi_H[s][0] || !b->psi_H[s][1])
+            return fail(p, FDTD_EINVAL, "psi buffers required for every slab");
+    for (int q = 0; q < p->d.n_detectors; ++q)
+        if (!b->det_state[q]) return fail(p, FDTD_EINVAL, "detector state buffer missing");
+    return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fdtd_launches_per_step(const FdtdPlan* p) {
+    if (!p) return 0;
+    int n = 2 + sources_launched(p, true) + sources_launched(p, false) + 1;
+    if (p->d.record_interfaces && p->d.n_slabs) n += 1;
+    for (int q = 0; q < p->d.n_detectors; ++q) n += p->det[q].reduce ? 2 : 1;
+    return n;
+}
+
+int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, int32_t flags, void* stream) {
+    if (!p) return FDTD_EINVAL;
+    if (int rc = check_bufs(p, b)) return rc;
+    if (n_steps < 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)
+        return fail(p, FDTD_EINVAL, "time steps out of the range covered by the plan's tables");
+    if (p->d.record_interfaces && p->d.n_slabs && !b->recording) return fail(p, FDTD_EINVAL, "recording buffer required");
+    if (n_steps == 0) return FDTD_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
+    float* Hcur = b->H;
+    float* Hnext = p->need_hprev ? p->h_twin : b->H;
+    int done = 0;
+    const bool use_graph = (flags & 1) != 0;
+    const int unit = p->need_hprev ? 2 : 1;
+    if (use_graph && n_steps >= 8) {
+        int G = std::min(n_steps, 64);
+        G -= G % unit;
+        const bool same = p->gexec && p->gsteps == G && std::memcmp(&p->gbufs, b, sizeof(FdtdBuffers)) == 0;
+        if (!same) {
+            if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+            if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+            if (!p->cap_stream) {
+                cudaError_t e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
+                if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamCreate");
+            }
+            cudaError_t e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamBeginCapture");
+            float* hc = b->H;
+            float* hn = p->need_hprev ? p->h_twin : b->H;
+            for (int s = 0; s < G; ++s) {
+                launch_forward_step(p, b, hc, hn, p->cap_stream);
+                if (p->need_hprev) std::swap(hc, hn);
+            }
+            e = cudaStreamEndCapture(p->cap_stream, &p->graph);
+            if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&p->gexec, p->graph, 0);
+            if (e != cudaSuccess) return cuda_fail(p, e, "cudaGraphInstantiate");
+            p->gbufs = *b;
+            p->gsteps = G;
+        }
+        while (n_steps - done >= G) {
+            cudaError_t e = cudaGraphLaunch(p->gexec, st);
+            if (e != cudaSuccess) return cuda_fail(p, e, "cudaGraphLaunch");
+            done += G;
+        }
+    }
+    for (; done < n_steps; ++done) {
+        launch_forward_step(p, b, Hcur, Hnext, st);
+        if (p->need_hprev) std::swap(Hcur, Hnext);
+    }
+    if (p->need_hprev && Hcur != b->H) {
+        cudaError_t e = cudaMemcpyAsync(b->H, Hcur, sizeof(float) * 3 * p->g.N, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(p, e, "cudaMemcpyAsync");
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_forward launch");
+    return FDTD_OK;
+}
+
+// Reverse steps (fdtdx/fdtd/backward.py:62-135 with reset_fields=False and no
+// detectors, the form the reversible gradient uses): per step t = t_end-1 ... :
+// re-impose the recorded interfaces of step t, reverse H (sources subtracted first,
+// psi frozen), reverse E.
+int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_steps, void* stream) {
+    if (!p) return FDTD_EINVAL;
+    if (int rc = check_bufs(p, b)) return rc;
+    if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)
+        return fail(p, FDTD_EINVAL, "reverse steps out of the range covered by the plan's tables");
+    if (n_steps == 0) return FDTD_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const dim3 grid = update_grid(p->g);
+    k_set_step<<<1, 1, 0, st>>>(p->d_t, t_end - 1);
+    for (int s = 0; s < n_steps; ++s) {
+        interfaces<true>(p, b, b->H, st);
+        launch_sources(p, b, false, b->H, 1, st);
+        k_update_H<true><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, false, b->E, b->H, b->H));
+        launch_sources(p, b, true, b->E, 1, st);
+        k_update_E<true><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, b->H, b->E, b->E));
+        k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_reverse launch");
+    return FDTD_OK;
+}
+
+int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
+    if (!d) return -1;
+    const long long N = (long long)d->nx * d->ny * d->nz;
+    long long bytes = 4ll * N * (3 + 3 + d->n_eps + d->n_mu + d->n_sigma_E + d->n_sigma_H);
+    const int n3[3] = {d->nx, d->ny, d->nz};
+    long long iface = 0;
+    for (int s = 0; s < d->n_slabs; ++s) {
+        const FdtdSlabDesc& sl = d->slabs[s];
+        bytes += 4ll * 4 * (N / n3[sl.axis]) * sl.thickness;  // psi_E and psi_H pairs
+        iface += N / n3[sl.axis];
+    }
+    bool hprev = false;
+    for (int q = 0; q < d->n_detectors; ++q) {
+        const FdtdDetectorDesc& dd = d->detectors[q];
+        const long long R = (long long)(dd.hi[0] - dd.lo[0]) * (dd.hi[1] - dd.lo[1]) * (dd.hi[2] - dd.lo[2]);
+        const int C = popcount6(dd.comp_mask);
+        long long on = 0;
+        if (dd.slot)
+            for (int t = 0; t < d->n_steps_total + 2; ++t) on = std::max<long long>(on, dd.slot[t] + 1);
+        if (dd.kind == FDTD_DET_PHASOR) bytes += 8ll * dd.n_freq * C * (dd.reduce_volume ? 1 : R);
+        else if (dd.kind == FDTD_DET_FIELD) bytes += 4ll * on * C * (dd.reduce_volume ? 1 : R);
+        else bytes += 4ll * on * (dd.keep_all ? 3 : 1) * (dd.reduce_volume ? 1 : R);
+        if (det_needs_h(dd)) hprev = true;
+    }
+    if (hprev) bytes += 12ll * N;
+    if (d->record_interfaces) bytes += (long long)rec_elem_bytes(d->recording_dtype) * 6 * iface * d->n_steps_total;
+    bytes += 1ll << 20;  // tables and scratch
+    return bytes;
+}
+
+}  // extern "C"
+
+extern "C" int fdtd_adjoint_step(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, int32_t t, void* stream) {
+    (void)b; (void)adj; (void)t; (void)stream;
+    return fail(p, FDTD_EINVAL, "fdtd_adjoint_step: not built in this version");
+}
+
+extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, float* out_ms,
+                                    void* stream) {
+    if (!p || !out_ms) return FDTD_EINVAL;
+    if (int rc = check_bufs(p, b)) return rc;
+    if (n_steps <= 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)
+        return fail(p, FDTD_EINVAL, "time steps out of range");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaEvent_t ev[7];
+    for (auto& e : ev) cudaEventCreate(&e);
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
+    float* Hcur = b->H;
+    float* Hnext = p->need_hprev ? p->h_twin : b->H;
+    const dim3 grid = update_grid(p->g);
+    for (int s = 0; s < n_steps; ++s) {
+        cudaEventRecord(ev[0], st);
+        k_update_E<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, Hcur, b->E, b->E));
+        cudaEventRecord(ev[1], st);
+        launch_sources(p, b, true, b->E, 0, st);
+        cudaEventRecord(ev[2], st);
+        k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, false, b->E, Hcur, Hnext));
+        cudaEventRecord(ev[3], st);
+        launch_sources(p, b, false, Hnext, 0, st);
+        cudaEventRecord(ev[4], st);
+        DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
+                    p->d.inv_mu_scalar};
+        for (int q = 0; q < p->d.n_detectors; ++q) {
+            const DDet& dd = p->det[q];
+            k_detector<<<dd.nblocks, kDetBlock, 0, st>>>(p->g, dd, p->d_t, f, b->det_state[q]);
+            if (dd.reduce) k_detector_finalize<<<1, kDetBlock, 0, st>>>(dd, p->d_t, b->det_state[q]);
+        }
+        cudaEventRecord(ev[5], st);
+        if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
+        k_advance<<<1, 1, 0, st>>>(p->d_t, 1);
+        cudaEventRecord(ev[6], st);
+        cudaError_t e = cudaEventSynchronize(ev[6]);
+        if (e != cudaSuccess) {
+            for (auto& x : ev) cudaEventDestroy(x);
+            return cuda_fail(p, e, "fdtd_profile_forward");
+        }
+        for (int k = 0; k < 6; ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            acc[k] += ms;
+        }
+        if (p->need_hprev) std::swap(Hcur, Hnext);
+    }
+    if (p->need_hprev && Hcur != b->H)
+        cudaMemcpyAsync(b->H, Hcur, sizeof(float) * 3 * p->g.N, cudaMemcpyDeviceToDevice, st);
+    for (auto& x : ev) cudaEventDestroy(x);
+    for (int k = 0; k < 6; ++k) out_ms[k] = (float)(acc[k] / n_steps);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_profile_forward");
+    return FDTD_OK;
+}

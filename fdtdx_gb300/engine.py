@@ -1,0 +1,417 @@
+"""Host setup of the native plan: scene -> ``FdtdDesc`` tables, plan lifecycle, calls.
+
+Everything computed here is per-simulation setup that the reference does once in
+``place_on_grid`` / ``apply`` of each object or in the per-step Python of its
+update functions; the kernels receive it as small device tables:
+
+* CPML coefficient vectors (perfectly_matched_layer.py:97-136, 231-275)
+* per-step source tables: on/off, on/off-adjusted time step, and the carrier
+  phase reduced mod 2 pi in float64 (source.py:41-66, profile.py:253-345)
+* TFSF incident profiles and Yee time offsets of a plane source
+  (linear_polarization.py:168-358, tfsf.py:144-190, fdtdx/core/grid.py:720-880)
+* per-step detector tables: state slot, and the complex DFT weight
+  exp(i w t dt) * scale * window[t] of phasor detectors (phasor.py:118-235)
+
+Table index ``t + 1`` holds time step ``t`` for t in [-1, T]; the reference indexes its
+per-step arrays with JAX semantics, so step -1 reads the last entry and step T
+(clamped) reads it too.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from fdtdx_gb300 import _native as N
+from fdtdx_gb300 import constants
+from fdtdx_gb300.config import SimulationConfig
+from fdtdx_gb300.container import ArrayContainer, ObjectContainer
+from fdtdx_gb300.core import GaussianPulseProfile, SingleFrequencyProfile
+from fdtdx_gb300.objects import (
+    COMPONENTS,
+    EnergyDetector,
+    FieldDetector,
+    LinearlyPolarizedPlaneSource,
+    PerfectElectricConductor,
+    PerfectlyMatchedLayer,
+    PerfectMagneticConductor,
+    PeriodicBoundary,
+    PhasorDetector,
+    PointDipoleSource,
+    PoyntingFluxDetector,
+)
+
+TWO_PI = 2.0 * math.pi
+
+
+def _jax_index(t: int, n: int) -> int:
+    """Index a length-n array at t the way a JAX gather does (negative wraps once, overflow clamps)."""
+    if t < 0:
+        t += n
+    return min(max(t, 0), n - 1)
+
+
+@dataclass
+class SourceTables:
+    desc: N.SourceDesc
+    keep: list = field(default_factory=list)  # numpy arrays referenced by desc
+
+
+def _profile_params(profile, wave, dt: float) -> tuple[int, float, float, float, float, float]:
+    """(kind, omega [rad/s], phase0, ramp_inv_steps, t0_steps, inv_two_sigma2) of a temporal profile."""
+    if isinstance(profile, SingleFrequencyProfile):
+        period = wave.get_period()
+        omega = TWO_PI / period
+        phase0 = wave.phase_shift + profile.phase_shift
+        ramp_inv = dt / (profile.num_startup_periods * period)
+        return N.PROFILE_CW, omega, phase0, ramp_inv, 0.0, 0.0
+    if isinstance(profile, GaussianPulseProfile):
+        omega = TWO_PI * profile.center_wave.get_frequency()
+        phase0 = wave.phase_shift + profile.center_wave.phase_shift
+        sigma = profile.sigma_t
+        return N.PROFILE_GAUSSIAN, omega, phase0, 0.0, 6.0 * sigma / dt, dt * dt / (2.0 * sigma * sigma)
+    raise NotImplementedError(f"temporal profile {type(profile).__name__} is not supported")
+
+
+def source_time_tables(src, config: SimulationConfig) -> tuple[np.ndarray, np.ndarray]:
+    """(on, teff) for t in [-1, T]: the on/off state and the on/off-adjusted time step."""
+    T = config.time_steps_total
+    ts = np.arange(-1, T + 1)
+    if src.switch.is_default_always_on:
+        return np.ones(T + 2, np.uint8), ts.astype(np.float64)
+    on_list = src.switch.calculate_on_list(T, config.time_step_duration)
+    idx = src.switch.calculate_time_step_to_on_arr_idx(T, config.time_step_duration)
+    on = np.array([on_list[_jax_index(t, T)] for t in ts], np.uint8)
+    # linear_interpolated_indexing at an integer point: the entry, or 0 outside the array
+    teff = np.array([float(idx[t]) if 0 <= t < T else 0.0 for t in ts], np.float64)
+    return on, teff
+
+
+def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> SourceTables:
+    dt = config.time_step_duration
+    c = config.courant_number
+    kind, omega, phase0, ramp_inv, t0s, inv2s2 = _profile_params(src.temporal_profile, src.wave_character, dt)
+    on, teff = source_time_tables(src, config)
+    ph_E = np.mod(omega * dt * teff + phase0, TWO_PI).astype(np.float32)
+    ph_H = np.mod(omega * dt * (teff + 0.5) + phase0, TWO_PI).astype(np.float32)
+    d = N.SourceDesc()
+    st = src.grid_slice_tuple
+    for a in range(3):
+        d.lo[a], d.hi[a] = st[a]
+    d.profile = kind
+    d.omega_dt = omega * dt
+    d.ramp_inv_steps = ramp_inv
+    d.t0_steps = t0s
+    d.inv_two_sigma2 = inv2s2
+    keep = [ph_E, ph_H, teff.astype(np.float32), on]
+    d.phase_E = ph_E.ctypes.data
+    d.phase_H = ph_H.ctypes.data
+    d.teff = keep[2].ctypes.data
+    d.on = on.ctypes.data
+    if isinstance(src, PointDipoleSource):
+        d.kind = N.SRC_DIPOLE
+        d.component = src.polarization
+        d.magnetic = 1 if src.source_type == "magnetic" else 0
+        i, j, k = (st[0][0], st[1][0], st[2][0])
+        if src.grid_shape != (1, 1, 1):
+            raise ValueError("a point dipole occupies exactly one cell")
+        if d.magnetic:
+            m = arrays.inv_permeabilities
+            local = float(m) if not isinstance(m, torch.Tensor) else float(m[min(src.polarization, m.shape[0] - 1), i, j, k])
+        else:
+            m = arrays.inv_permittivities
+            local = float(m[min(src.polarization, m.shape[0] - 1), i, j, k])
+        d.coef = c * src.amplitude * src.static_amplitude_factor * local
+        return SourceTables(d, keep)
+    if isinstance(src, LinearlyPolarizedPlaneSource):
+        d.kind = N.SRC_PLANE
+        d.normal_axis = src.propagation_axis
+        d.sign = 1.0 if src.direction == "+" else -1.0
+        d.coef = c * src.static_amplitude_factor
+        incE, incH, offE, offH = plane_source_profiles(src, arrays, config)
+        keep += [incE, incH, offE, offH]
+        d.inc_E, d.inc_H, d.off_E, d.off_H = (x.ctypes.data for x in (incE, incH, offE, offH))
+        return SourceTables(d, keep)
+    raise NotImplementedError(f"source type {type(src).__name__} is not supported")
+
+
+def plane_source_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContainer, config: SimulationConfig):
+    """Incident E/H profiles and Yee time offsets of an untilted plane source, each (3, face cells).
+
+    Restates LinearlyPolarizedPlaneSource.apply (linear_polarization.py:168-358) for normal
+    incidence on a uniform grid: profile -> E = a e_pol, H = a h_pol -> energy normalisation ->
+    H / sqrt(inv_eps / inv_mu) -> offsets = -(k . r) n / (c dt) with r the Yee position of
+    each component relative to the plane (calculate_time_offset_yee, fdtdx/core/grid.py:720-880).
+    """
+    n = src.propagation_axis
+    h_ax, v_ax = src.horizontal_axis, src.vertical_axis
+    shape = src.grid_shape
+    prof_hv = src.amplitude_raw_hv(config.uniform_spacing())
+    prof = prof_hv.T if h_ax > v_ax else prof_hv
+    amp = np.expand_dims(prof, axis=n)  # grid-shaped (face in x, y, z order)
+    e_pol, h_pol, k = src.polarization_vectors()
+    E = amp[None] * e_pol[:, None, None, None]
+    Hf = amp[None] * h_pol[:, None, None, None]
+    sl = (slice(None), *src.grid_slice)
+    ie = arrays.inv_permittivities[sl].detach().double().cpu().numpy()
+    mu = arrays.inv_permeabilities
+    im = mu[sl].detach().double().cpu().numpy() if isinstance(mu, torch.Tensor) else float(mu)
+    if src.normalize_by_energy:
+        energy = (0.5 * (1.0 / ie) * E**2).sum(axis=0) + (0.5 * (1.0 / im) * Hf**2).sum(axis=0)
+        root = math.sqrt(float(energy.sum()))
+        E = E / root
+        Hf = Hf / root
+    Hf = Hf / np.sqrt(ie / im)
+    # Yee positions along the normal: 0.5 dx for components staggered along it
+    stag_E = [0.5 if comp == n else 0.0 for comp in range(3)]
+    stag_H = [0.0 if comp == n else 0.5 for comp in range(3)]
+    dx, dt = config.uniform_spacing(), config.time_step_duration
+    ie0 = ie[0]
+    im0 = im[0] if isinstance(im, np.ndarray) else im
+    n_r = 1.0 / np.sqrt(ie0 * im0)
+    scale = n_r / (constants.c * dt)
+    kn = k[n]
+    offE = np.stack([np.broadcast_to(-(stag_E[q] * dx * kn) * scale, shape) for q in range(3)])
+    offH = np.stack([np.broadcast_to(-(stag_H[q] * dx * kn) * scale, shape) for q in range(3)])
+    P = int(np.prod(shape))
+    f32 = lambda x: np.ascontiguousarray(np.broadcast_to(x, (3, *shape)).reshape(3, P), dtype=np.float32)  # noqa: E731
+    return f32(E), f32(Hf), f32(offE), f32(offH)
+
+
+@dataclass
+class DetectorTables:
+    desc: N.DetectorDesc
+    keep: list = field(default_factory=list)
+
+
+def detector_tables(det, config: SimulationConfig) -> tuple[np.ndarray, np.ndarray | None]:
+    """(slot, weights) for t in [-1, T]."""
+    T = config.time_steps_total
+    dt = config.time_step_duration
+    on_list = det.on_list(config)
+    ts = np.arange(-1, T + 1)
+    if T == 0:
+        return np.full(T + 2, -1, np.int32), None
+    on = np.array([on_list[_jax_index(t, T)] for t in ts], bool)
+    if isinstance(det, PhasorDetector):
+        slot = np.where(on, 0, -1).astype(np.int32)
+        on_arr = np.asarray(on_list, np.float64)
+        if det.apodization is None:
+            window = on_arr
+        else:
+            window = det.apodization.get_window(np.arange(T) * dt) * on_arr
+        wsum = float(window.sum())
+        if not math.isfinite(wsum) or wsum <= 0.0:
+            raise Exception(f"Detector '{det.name}': the apodization window sums to {wsum} over the recorded time steps")
+        if det.scaling_mode == "continuous":
+            scale = 2.0 / wsum
+        elif det.scaling_mode == "pulse":
+            scale = float(det.resolve_dft_stride(config))
+        else:
+            raise Exception(f"Invalid scaling mode: {det.scaling_mode=}")
+        omegas = np.array([TWO_PI * wc.get_frequency() for wc in det.wave_characters])
+        wt = np.array([window[_jax_index(t, T)] for t in ts])
+        phase = omegas[None, :] * (ts[:, None] * dt)
+        w = np.exp(1j * phase) * scale * wt[:, None]
+        weights = np.empty((T + 2, len(omegas), 2), np.float32)
+        weights[..., 0] = w.real
+        weights[..., 1] = w.imag
+        return slot, weights
+    idx, counter = [-1] * T, 0
+    for t in range(T):
+        if on_list[t]:
+            idx[t] = counter
+            counter += 1
+    slot = np.array([idx[_jax_index(t, T)] if on[q] else -1 for q, t in enumerate(ts)], np.int32)
+    return slot, None
+
+
+def build_detector(det, config: SimulationConfig) -> DetectorTables:
+    d = N.DetectorDesc()
+    st = det.grid_slice_tuple
+    for a in range(3):
+        d.lo[a], d.hi[a] = st[a]
+    d.exact_interpolation = 1 if det.exact_interpolation else 0
+    d.inverse = 1 if det.inverse else 0
+    dx = config.uniform_spacing()
+    if isinstance(det, PhasorDetector):
+        d.kind = N.DET_PHASOR
+        d.n_freq = len(det.wave_characters)
+        if d.n_freq > N.MAX_FREQS:
+            raise ValueError(f"at most {N.MAX_FREQS} frequencies per phasor detector")
+        d.reduce_volume = 1 if det.reduce_volume else 0
+        d.comp_mask = sum(1 << COMPONENTS.index(c) for c in det.recorded_components)
+    elif isinstance(det, FieldDetector):
+        d.kind = N.DET_FIELD
+        d.reduce_volume = 1 if det.reduce_volume else 0
+        d.comp_mask = sum(1 << COMPONENTS.index(c) for c in det.recorded_components)
+    elif isinstance(det, PoyntingFluxDetector):
+        d.kind = N.DET_FLUX
+        d.reduce_volume = 1 if det.reduce_volume else 0
+        d.keep_all = 1 if det.keep_all_components else 0
+        d.flux_axis = det.propagation_axis if not det.keep_all_components else 0
+        d.flux_sign = -1.0 if det.direction == "-" else 1.0
+        d.cell_weight = dx * dx
+        d.comp_mask = 63
+    elif isinstance(det, EnergyDetector):
+        d.kind = N.DET_ENERGY
+        d.reduce_volume = 1 if det.reduce_volume else 0
+        d.cell_weight = dx**3
+        d.comp_mask = 63
+    else:
+        raise NotImplementedError(f"detector type {type(det).__name__} is not supported")
+    slot, weights = detector_tables(det, config)
+    keep = [slot]
+    d.slot = slot.ctypes.data
+    if weights is not None:
+        keep.append(weights)
+        d.weights = weights.ctypes.data
+    return DetectorTables(d, keep)
+
+
+class Scene:
+    """The native description of one placed simulation and its plan."""
+
+    def __init__(self, objects: ObjectContainer, arrays: ArrayContainer, config: SimulationConfig,
+                 record_interfaces: bool = False):
+        self.objects = objects
+        self.config = config
+        self.desc = N.Desc()
+        self._keep: list = []
+        d = self.desc
+        shape = objects.volume.grid_shape
+        d.nx, d.ny, d.nz = shape
+        d.n_steps_total = config.time_steps_total
+        d.courant = config.courant_number
+        d.n_eps = arrays.inv_permittivities.shape[0]
+        mu = arrays.inv_permeabilities
+        d.n_mu = mu.shape[0] if isinstance(mu, torch.Tensor) else 0
+        d.inv_mu_scalar = 1.0 if isinstance(mu, torch.Tensor) else float(mu)
+        d.n_sigma_E = arrays.electric_conductivity.shape[0] if arrays.electric_conductivity is not None else 0
+        d.n_sigma_H = arrays.magnetic_conductivity.shape[0] if arrays.magnetic_conductivity is not None else 0
+        for b in objects.boundary_objects:
+            side = 1 if b.direction == "+" else 0
+            if isinstance(b, PeriodicBoundary):
+                d.periodic[b.axis] = 1
+            elif isinstance(b, PerfectElectricConductor):
+                d.pec_faces |= 1 << (2 * b.axis + side)
+            elif isinstance(b, PerfectMagneticConductor):
+                d.pmc_faces |= 1 << (2 * b.axis + side)
+        self.pmls: list[PerfectlyMatchedLayer] = objects.pml_objects
+        if len(self.pmls) > N.MAX_SLABS:
+            raise ValueError("at most six PML slabs")
+        d.n_slabs = len(self.pmls)
+        for s, p in enumerate(self.pmls):
+            lo, hi = p.grid_slice_tuple[p.axis]
+            full = [(0, n) for n in shape]
+            full[p.axis] = (lo, hi)
+            if tuple(p.grid_slice_tuple) != tuple(full):
+                raise NotImplementedError("a PML slab must span the whole domain transverse to its axis")
+            if (p.direction == "-" and lo != 0) or (p.direction == "+" and hi != shape[p.axis]):
+                raise NotImplementedError("a PML slab must touch its domain face")
+            co = p.coefficients(config.uniform_spacing(), config.time_step_duration)
+            tbl = np.ascontiguousarray(
+                np.concatenate([co["a_E"], co["b_E"], co["inv_kappa_E"], co["a_H"], co["b_H"], co["inv_kappa_H"]]),
+                dtype=np.float32,
+            )
+            self._keep.append(tbl)
+            sd = d.slabs[s]
+            sd.axis = p.axis
+            sd.direction = -1 if p.direction == "-" else 1
+            sd.thickness = p.thickness
+            sd.kappa_is_one = 1 if p.kappa_is_one else 0
+            sd.coef = tbl.ctypes.data
+        self.sources = list(objects.sources)
+        if len(self.sources) > N.MAX_SOURCES:
+            raise ValueError(f"at most {N.MAX_SOURCES} sources")
+        d.n_sources = len(self.sources)
+        for s, src in enumerate(self.sources):
+            tb = build_source(src, arrays, config)
+            self._keep.append(tb)
+            d.sources[s] = tb.desc
+        self.detectors = list(objects.forward_detectors)
+        if len(self.detectors) > N.MAX_DETECTORS:
+            raise ValueError(f"at most {N.MAX_DETECTORS} detectors")
+        d.n_detectors = len(self.detectors)
+        for q, det in enumerate(self.detectors):
+            tb = build_detector(det, config)
+            self._keep.append(tb)
+            d.detectors[q] = tb.desc
+        d.record_interfaces = 1 if record_interfaces else 0
+        rec_dtype = torch.float32
+        gc = config.gradient_config
+        if gc is not None and gc.recorder is not None:
+            rec_dtype = gc.recorder.storage_dtype
+        d.recording_dtype = {torch.float32: 0, torch.bfloat16: 1, torch.float16: 2}[rec_dtype]
+        self._plan: int | None = None
+
+    # ---- plan lifecycle
+    @property
+    def plan(self) -> int:
+        if self._plan is None:
+            lib = N.load()
+            h = C.c_void_p()
+            rc = lib.fdtd_plan_create(C.byref(self.desc), C.byref(h))
+            N.check(rc, None, "fdtd_plan_create")
+            self._plan = h.value
+        return self._plan
+
+    def close(self) -> None:
+        if self._plan is not None:
+            N.load().fdtd_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def footprint_bytes(self) -> int:
+        return int(N.load().fdtd_footprint_bytes(C.byref(self.desc)))
+
+    def launches_per_step(self) -> int:
+        return int(N.load().fdtd_launches_per_step(self.plan))
+
+    def interface_floats(self) -> int:
+        return int(N.load().fdtd_interface_floats(self.plan))
+
+    # ---- buffers
+    def buffers(self, arrays: ArrayContainer) -> N.Buffers:
+        b = N.Buffers()
+        f = arrays.fields
+        for t in (f.E, f.H, arrays.inv_permittivities):
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
+                raise ValueError("fields and materials must be contiguous float32 CUDA tensors")
+        b.E, b.H = N.ptr(f.E), N.ptr(f.H)
+        b.inv_eps = N.ptr(arrays.inv_permittivities)
+        mu = arrays.inv_permeabilities
+        b.inv_mu = N.ptr(mu) if isinstance(mu, torch.Tensor) else None
+        b.sigma_E = N.ptr(arrays.electric_conductivity)
+        b.sigma_H = N.ptr(arrays.magnetic_conductivity)
+        for s, p in enumerate(self.pmls):
+            b.psi_E[s][0], b.psi_E[s][1] = N.ptr(f.psi_E[p.name][0]), N.ptr(f.psi_E[p.name][1])
+            b.psi_H[s][0], b.psi_H[s][1] = N.ptr(f.psi_H[p.name][0]), N.ptr(f.psi_H[p.name][1])
+        for q, det in enumerate(self.detectors):
+            st = arrays.detector_states[det.name]
+            b.det_state[q] = N.ptr(next(iter(st.values())))
+        if arrays.recording_state is not None:
+            b.recording = N.ptr(arrays.recording_state.data["interfaces"])
+        return b
+
+    def forward(self, arrays: ArrayContainer, t0: int, n_steps: int, graph: bool = True, stream=None) -> None:
+        st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
+        b = self.buffers(arrays)
+        rc = N.load().fdtd_forward(self.plan, C.byref(b), int(t0), int(n_steps), 1 if graph else 0,
+                                   C.c_void_p(st.cuda_stream))
+        N.check(rc, self.plan, "fdtd_forward")
+
+    def reverse(self, arrays: ArrayContainer, t_end: int, n_steps: int, stream=None) -> None:
+        st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
+        b = self.buffers(arrays)
+        rc = N.load().fdtd_reverse(self.plan, C.byref(b), int(t_end), int(n_steps), C.c_void_p(st.cuda_stream))
+        N.check(rc, self.plan, "fdtd_reverse")

@@ -1,0 +1,207 @@
+/*
+ * fdtd_gb300.h -- C ABI of the GB300 (sm_103a) FDTD time-stepping library.
+ *
+ * The library replaces the per-step hot path of fdtdx (a JAX package):
+ *
+ *   fdtd_forward          one or more forward Yee steps: update_E, source E-injection,
+ *                         PEC zeroing, update_H, source H-injection, PMC zeroing,
+ *                         detector accumulation and PML-interface recording.
+ *                         Replaces the body of the time loop in
+ *                         fdtdx/fdtd/fdtd.py:482-493 (checkpointed_fdtd) and
+ *                         fdtdx/fdtd/fdtd.py:157-163 (reversible forward), i.e.
+ *                         fdtdx/fdtd/forward.py:83-156 with
+ *                         fdtdx/fdtd/update.py:256-523, 689-853, 1040-1178.
+ *   fdtd_reverse          one or more time-reversed steps (interface re-imposition,
+ *                         reverse H, reverse E with frozen CPML psi).  Replaces
+ *                         fdtdx/fdtd/backward.py:62-135 with
+ *                         fdtdx/fdtd/update.py:526-686, 856-1007, 1181-1222.
+ *   fdtd_adjoint_step     the transposed (vector-Jacobian) forward step used by the
+ *                         reversible gradient: replaces the jax.vjp of
+ *                         forward_single_args_wrapper inside body_fn,
+ *                         fdtdx/fdtd/fdtd.py:215-251, accumulating d/d inv_eps and
+ *                         d/d inv_mu as fdtdx/fdtd/fdtd.py:324-333 returns them.
+ *
+ * Conventions
+ *   - Every buffer is caller-owned device memory, float32, C order, z fastest.
+ *     Fields are (3, nx, ny, nz).  Material arrays are (n, nx, ny, nz), n in {1, 3}.
+ *   - The plan copies the small host tables of FdtdDesc (PML coefficients,
+ *     per-step source and detector tables, plane-source profiles) to device
+ *     memory it owns, plus scratch for reductions.  It never touches caller buffers
+ *     outside the calls below.
+ *   - Errors are returned as FDTD_* status codes; fdtd_last_error(plan) gives a
+ *     message.  No exception crosses the ABI.
+ *   - Streams are passed as void* (a cudaStream_t); a plan must not be used from
+ *     two host threads at once.  Independent plans are independent.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_OK 0
+#define FDTD_EINVAL 1
+#define FDTD_ENOMEM 2
+#define FDTD_ECUDA 3
+#define FDTD_ETIMEOUT 4
+#define FDTD_ENONFINITE 5
+
+#define FDTD_MAX_SLABS 6
+#define FDTD_MAX_SOURCES 16
+#define FDTD_MAX_DETECTORS 32
+#define FDTD_MAX_FREQS 16
+
+#define FDTD_PROFILE_CW 0       /* SingleFrequencyProfile (fdtdx/objects/sources/profile.py:253-273) */
+#define FDTD_PROFILE_GAUSSIAN 1 /* GaussianPulseProfile   (fdtdx/objects/sources/profile.py:276-345) */
+
+#define FDTD_SRC_DIPOLE 0 /* PointDipoleSource  (fdtdx/objects/sources/dipole.py:195-277) */
+#define FDTD_SRC_PLANE 1  /* TFSF plane source  (fdtdx/objects/sources/tfsf.py:193-409, 739-806) */
+
+#define FDTD_DET_FIELD 0  /* FieldDetector        (fdtdx/objects/detectors/field.py:31-63) */
+#define FDTD_DET_PHASOR 1 /* PhasorDetector       (fdtdx/objects/detectors/phasor.py:190-235) */
+#define FDTD_DET_FLUX 2   /* PoyntingFluxDetector (fdtdx/objects/detectors/poynting_flux.py:171-195) */
+#define FDTD_DET_ENERGY 3 /* EnergyDetector       (fdtdx/objects/detectors/energy.py) */
+
+/* One CPML slab (fdtdx/objects/boundaries/perfectly_matched_layer.py:97-190).
+ * The slab spans the whole domain transverse to `axis` and `thickness` cells along it. */
+typedef struct {
+    int32_t axis;          /* 0, 1, 2 */
+    int32_t direction;     /* -1: min side ("-"), +1: max side ("+") */
+    int32_t thickness;     /* L */
+    int32_t kappa_is_one;  /* 1: corrections are psi alone (perfectly_matched_layer.py:184-185) */
+    const float* coef;     /* host, 6*L floats: a_E, b_E, inv_kappa_E, a_H, b_H, inv_kappa_H */
+} FdtdSlabDesc;
+
+/* One source.  All per-step tables are host arrays of length n_table = T + 2,
+ * entry (t + 1) for time step t in [-1, T]. */
+typedef struct {
+    int32_t kind;          /* FDTD_SRC_* */
+    int32_t lo[3], hi[3];  /* cell box: one cell (dipole) or one plane (TFSF) */
+    int32_t component;     /* dipole: polarization axis */
+    int32_t magnetic;      /* dipole: 1 injects into H (source_type "magnetic") */
+    int32_t normal_axis;   /* plane: propagation axis */
+    float sign;            /* plane: +1 for direction "+", -1 for "-"; dipole: unused */
+    float coef;            /* dipole: c*amplitude*static_factor*inv_material_local; plane: c*static_factor */
+    const float* inc_E;    /* plane: host (3, face cells) incident E profile (energy-normalised) */
+    const float* inc_H;    /* plane: host (3, face cells) incident H profile (impedance-divided) */
+    const float* off_E;    /* plane: host (3, face cells) Yee time offsets of E, in steps */
+    const float* off_H;    /* plane: host (3, face cells) Yee time offsets of H, in steps */
+    int32_t profile;       /* FDTD_PROFILE_* */
+    float omega_dt;        /* carrier phase advance per step, rad */
+    float ramp_inv_steps;  /* CW: dt / (num_startup_periods * period) */
+    float t0_steps;        /* Gaussian: envelope centre in steps */
+    float inv_two_sigma2;  /* Gaussian: dt^2 / (2 sigma_t^2) */
+    const float* phase_E;  /* (omega*dt*teff + phase0) mod 2 pi, E-side time */
+    const float* phase_H;  /* same at teff + 0.5, H-side time */
+    const float* teff;     /* on/off-adjusted time step (fdtdx/objects/sources/source.py:41-49) */
+    const uint8_t* on;     /* 1 when the source is on */
+} FdtdSourceDesc;
+
+/* One detector.  Tables are host arrays of length n_table (entry t + 1). */
+typedef struct {
+    int32_t kind;           /* FDTD_DET_* */
+    int32_t lo[3], hi[3];   /* region box */
+    int32_t comp_mask;      /* bit c for component c of (Ex, Ey, Ez, Hx, Hy, Hz) */
+    int32_t exact_interpolation;
+    int32_t reduce_volume;
+    int32_t inverse;        /* phasor: subtract instead of add */
+    int32_t n_freq;         /* phasor */
+    int32_t flux_axis;      /* flux: propagation axis */
+    float flux_sign;        /* flux: -1 for direction "-" */
+    int32_t keep_all;       /* flux: keep the three Poynting components */
+    float cell_weight;      /* dx^3 (volume means, energy sums) or dx^2 (flux sums) */
+    const int32_t* slot;    /* state slot for time step t, -1 when off */
+    const float* weights;   /* phasor: (n_table, n_freq, 2) complex weight per step */
+} FdtdDetectorDesc;
+
+typedef struct {
+    int32_t nx, ny, nz;
+    int32_t n_steps_total;  /* T; tables hold T + 2 entries */
+    float courant;          /* courant_factor / sqrt(3) */
+    int32_t n_eps;          /* 1 or 3 */
+    int32_t n_mu;           /* 0 (scalar inv_mu), 1 or 3 */
+    float inv_mu_scalar;
+    int32_t n_sigma_E;      /* 0 (no conductivity), 1 or 3 */
+    int32_t n_sigma_H;
+    int32_t periodic[3];
+    int32_t pec_faces;      /* bit (2*axis + side), side 1 = max face */
+    int32_t pmc_faces;
+    int32_t n_slabs;
+    FdtdSlabDesc slabs[FDTD_MAX_SLABS];
+    int32_t n_sources;
+    FdtdSourceDesc sources[FDTD_MAX_SOURCES];
+    int32_t n_detectors;
+    FdtdDetectorDesc detectors[FDTD_MAX_DETECTORS];
+    int32_t record_interfaces; /* 1: record E, H on each slab's innermost layer after every step */
+    int32_t recording_dtype;   /* 0: float32, 1: bfloat16, 2: float16 */
+} FdtdDesc;
+
+typedef struct {
+    float* E;                   /* (3, nx, ny, nz) */
+    float* H;                   /* (3, nx, ny, nz) */
+    const float* inv_eps;       /* (n_eps, nx, ny, nz) */
+    const float* inv_mu;        /* (n_mu, nx, ny, nz) or NULL */
+    const float* sigma_E;       /* (n_sigma_E, ...) or NULL */
+    const float* sigma_H;
+    float* psi_E[FDTD_MAX_SLABS][2];  /* slab-shaped psi pairs (psi_1, psi_2) */
+    float* psi_H[FDTD_MAX_SLABS][2];
+    void* det_state[FDTD_MAX_DETECTORS];
+    void* recording;            /* (T, fdtd_interface_floats(plan)) in recording_dtype, or NULL */
+} FdtdBuffers;
+
+/* Cotangent (adjoint) buffers of the reversible gradient. */
+typedef struct {
+    float* lam_E;               /* (3, nx, ny, nz) cotangent of E */
+    float* lam_H;               /* (3, nx, ny, nz) cotangent of H */
+    float* lam_psi_E[FDTD_MAX_SLABS][2];
+    float* lam_psi_H[FDTD_MAX_SLABS][2];
+    const void* lam_det[FDTD_MAX_DETECTORS];  /* cotangent of each detector state (same layout), or NULL */
+    float* grad_inv_eps;        /* (n_eps, nx, ny, nz), accumulated (+=) */
+    float* grad_inv_mu;         /* (n_mu, ...) accumulated, or NULL when inv_mu is a scalar */
+    double* grad_inv_mu_scalar; /* device scalar accumulated when inv_mu is a scalar, or NULL */
+} FdtdAdjointBuffers;
+
+typedef struct FdtdPlan FdtdPlan;
+
+/* Build a plan from a scene description.  Copies all host tables. */
+int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out);
+void fdtd_plan_destroy(FdtdPlan* plan);
+const char* fdtd_last_error(const FdtdPlan* plan);
+/* Floats per time step in the interface recording (E and H on every slab interface). */
+int64_t fdtd_interface_floats(const FdtdPlan* plan);
+/* Device bytes the plan itself holds (tables + scratch). */
+int64_t fdtd_plan_device_bytes(const FdtdPlan* plan);
+/* Device bytes one simulation of this description needs (fields, materials, psi,
+ * detector states, recording, plan tables and scratch): serving admission. */
+int64_t fdtd_footprint_bytes(const FdtdDesc* desc);
+
+/* Forward steps t0 .. t0+n_steps-1.  flags bit 0: use a CUDA graph for the loop. */
+int fdtd_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_steps, int32_t flags, void* stream);
+
+/* Reverse steps: state at t_end is taken back to t_end - n_steps.  Uses the
+ * recording (interfaces re-imposed before each step) when it is non-NULL. */
+int fdtd_reverse(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t_end, int32_t n_steps, void* stream);
+
+/* Transposed forward step at time step t: the fields in bufs hold the forward
+ * state at t (reconstructed by fdtd_reverse); the cotangents of the state at t+1
+ * in adj are replaced by the cotangents of the state at t, and the material
+ * gradients are accumulated. */
+int fdtd_adjoint_step(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t, void* stream);
+
+/* Number of launches of this library's kernels one forward step issues. */
+int32_t fdtd_launches_per_step(const FdtdPlan* plan);
+
+/* Benchmark helper: runs forward steps t0 .. t0+n_steps-1 with CUDA events on `stream`
+ * around each launch group and writes the mean device time per step, in ms, of:
+ * out_ms[0] E update, [1] E-side sources, [2] H update, [3] H-side sources,
+ * [4] detectors, [5] interface recording.  Synchronises the stream. */
+int fdtd_profile_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_steps, float* out_ms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_GB300_H */

@@ -1,0 +1,859 @@
+"""ORACLE -- test infrastructure only.  CPU restatement of fdtdx's time-stepping path.
+
+This module is the checker of the GB300 library: only ``tests/``, the smoke test
+of ``__graft_entry__`` and the CPU-baseline leg of ``bench.py`` may import it.
+The product path (``fdtdx_gb300``) never calls it.
+
+It restates, line by line in torch-CPU tensors (so that the same code runs in
+float64 for the error reference, in float32 for the parity reference, and under
+torch autograd for per-step vector-Jacobian products), the reference files:
+
+* fdtdx/fdtd/update.py:256-1007       update_E / update_H and their reverses
+* fdtdx/core/physics/curl.py:86-397   curls with CPML corrections, co-location
+* fdtdx/core/misc.py:615-641          halo padding
+* fdtdx/objects/boundaries/perfectly_matched_layer.py:69-275   CPML coefficients
+* fdtdx/objects/boundaries/pec.py:71-77, pmc.py:62-76          conductor walls
+* fdtdx/objects/sources/dipole.py:150-277                      point dipole
+* fdtdx/objects/sources/profile.py:253-345, core/window.py:16-30  temporal profiles
+* fdtdx/objects/sources/linear_polarization.py:168-468, tfsf.py:144-409, 739-806,
+  fdtdx/core/grid.py:720-880                                   TFSF plane source
+* fdtdx/objects/detectors/{detector,phasor,field,poynting_flux,energy}.py  detectors
+* fdtdx/fdtd/update.py:1040-1222, fdtdx/fdtd/misc.py:10-66     detectors, interfaces
+* fdtdx/fdtd/forward.py:83-156, backward.py:62-135, fdtd.py:39-418  step and VJP loop
+
+Parity status: the reference is JAX and JAX cannot be installed on these machines,
+so the reference itself cannot be run.  The reference's tests hold no stored field
+or detector values; what they hold are known-answer tests and invariants (curl of
+a linear field, CPML scatter signs, update formulas, forward/backward round trips,
+PML profile values, phasor semantics), and those are replayed against this oracle
+in tests/test_oracle_kats.py.  Beyond those, field-level parity is unpinned.
+
+Objects are read through their fdtdx attribute names (duck typing), so a scene
+built with ``fdtdx_gb300`` objects drives this oracle without using any of that
+package's setup code.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Any
+
+import numpy as np
+import torch
+
+C0 = 299792458.0
+MU0 = 4e-7 * math.pi
+EPS0 = 1.0 / (MU0 * C0**2)
+ETA0 = MU0 * C0
+COMPONENTS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+
+def jax_index(n: int, t: int) -> int:
+    """Index of a length-n array read at t by a JAX gather: negative wraps, overflow clamps."""
+    if t < 0:
+        t += n
+    return min(max(t, 0), n - 1)
+
+
+# --------------------------------------------------------------------------------------------
+# padding and curls
+# --------------------------------------------------------------------------------------------
+
+
+def pad_fields(f: torch.Tensor, periodic: tuple[bool, bool, bool]) -> torch.Tensor:
+    """One-cell halo per axis, wrap or zero, applied axis by axis (fdtdx/core/misc.py:615-641)."""
+    for ax, per in enumerate(periodic):
+        d = ax + 1
+        n = f.shape[d]
+        if per:
+            lo, hi = f.narrow(d, n - 1, 1), f.narrow(d, 0, 1)
+        else:
+            z = torch.zeros_like(f.narrow(d, 0, 1))
+            lo, hi = z, z
+        f = torch.cat([lo, f, hi], dim=d)
+    return f
+
+
+def _add_at(a: torch.Tensor, sl, v) -> torch.Tensor:
+    out = a.clone()
+    out[sl] = out[sl] + v
+    return out
+
+
+def _set_at(a: torch.Tensor, sl, v) -> torch.Tensor:
+    out = a.clone()
+    out[sl] = v
+    return out
+
+
+@dataclass
+class OPml:
+    name: str
+    axis: int
+    direction: str
+    grid_slice: tuple
+    kappa_start: float
+    kappa_end: float
+    a_E: torch.Tensor
+    b_E: torch.Tensor
+    inv_kappa_E: torch.Tensor
+    a_H: torch.Tensor
+    b_H: torch.Tensor
+    inv_kappa_H: torch.Tensor
+
+
+def pml_coefficients(pml, dx: float, dt: float, dtype) -> dict[str, torch.Tensor]:
+    """perfectly_matched_layer.py:97-136 and _compute_pml_profile :231-275 (uniform grid)."""
+    L = pml.grid_shape[pml.axis]
+    sigma_end = pml.sigma_end
+    if sigma_end is None:
+        sigma_end = -(pml.sigma_order + 1) * math.log(1e-6) / (2 * (ETA0 / 1.0) * (L * dx))
+    if pml.direction == "-":
+        dE = np.arange(L - 1, -1, -1, dtype=np.float64)
+        dH = np.append(np.arange(L - 1.5, -0.5, -1, dtype=np.float64), 0)
+    else:
+        dE = np.insert(np.arange(0.5, L - 0.5, 1, dtype=np.float64), 0, 0)
+        dH = np.arange(0, L, 1, dtype=np.float64)
+    dE = torch.tensor(dE, dtype=dtype)
+    dH = torch.tensor(dH, dtype=dtype)
+
+    def profile(v0, v1, order):
+        return v0 + (v1 - v0) * torch.pow(dE / L, order), v0 + (v1 - v0) * torch.pow(dH / L, order)
+
+    sigma_E, sigma_H = profile(pml.sigma_start, sigma_end, pml.sigma_order)
+    kappa_E, kappa_H = profile(pml.kappa_start, pml.kappa_end, pml.kappa_order)
+    alpha_E, alpha_H = profile(pml.alpha_start, pml.alpha_end, pml.alpha_order)
+    b_E = torch.expm1(-dt / EPS0 * (sigma_E / kappa_E + alpha_E)) + 1
+    a_E = torch.nan_to_num((b_E - 1.0) * sigma_E / (sigma_E + alpha_E * kappa_E) / kappa_E, nan=0.0)
+    b_H = torch.expm1(-dt / EPS0 * (sigma_H / kappa_H + alpha_H)) + 1
+    a_H = torch.nan_to_num((b_H - 1.0) * sigma_H / (sigma_H + alpha_H * kappa_H) / kappa_H, nan=0.0)
+    shape = [1, 1, 1]
+    shape[pml.axis] = L
+    return {
+        "a_E": a_E.reshape(shape), "b_E": b_E.reshape(shape), "inv_kappa_E": (1.0 / kappa_E).reshape(shape),
+        "a_H": a_H.reshape(shape), "b_H": b_H.reshape(shape), "inv_kappa_H": (1.0 / kappa_H).reshape(shape),
+        "sigma_end": sigma_end,
+    }
+
+
+def step_cpml(pml: OPml, d1, d2, psi1, psi2, is_curl_E: bool, simulate_boundaries: bool):
+    """perfectly_matched_layer.py:138-190."""
+    if is_curl_E:
+        a, b, ik = pml.a_H, pml.b_H, pml.inv_kappa_H
+    else:
+        a, b, ik = pml.a_E, pml.b_E, pml.inv_kappa_E
+    if simulate_boundaries:
+        p1 = b * psi1 + a * d1
+        p2 = b * psi2 + a * d2
+    else:
+        p1, p2 = psi1, psi2
+    if pml.kappa_start == 1.0 and pml.kappa_end == 1.0:
+        c1, c2 = p1, p2
+    else:
+        c1 = (ik - 1.0) * d1 + p1
+        c2 = (ik - 1.0) * d2 + p2
+    return c1, c2, p1, p2
+
+
+def curl_E(E_pad, psi_H, pmls, simulate_boundaries):
+    """fdtdx/core/physics/curl.py:227-311 (uniform grid: metric scale 1)."""
+    Ex, Ey, Ez = E_pad[0], E_pad[1], E_pad[2]
+    c = (slice(1, -1), slice(1, -1), slice(1, -1))
+    dyEz = Ez[1:-1, 2:, 1:-1] - Ez[c]
+    dzEy = Ey[1:-1, 1:-1, 2:] - Ey[c]
+    dzEx = Ex[1:-1, 1:-1, 2:] - Ex[c]
+    dxEz = Ez[2:, 1:-1, 1:-1] - Ez[c]
+    dxEy = Ey[2:, 1:-1, 1:-1] - Ey[c]
+    dyEx = Ex[1:-1, 2:, 1:-1] - Ex[c]
+    comps = [dyEz - dzEy, dzEx - dxEz, dxEy - dyEx]
+    new_psi = {}
+    for pml in pmls:
+        a = pml.axis
+        i, j = (a + 1) % 3, (a + 2) % 3
+        if a == 0:
+            dj, di = dxEz, dxEy
+        elif a == 1:
+            dj, di = dyEx, dyEz
+        else:
+            dj, di = dzEy, dzEx
+        gs = pml.grid_slice
+        p1, p2 = psi_H[pml.name]
+        c1, c2, p1n, p2n = step_cpml(pml, dj[gs], di[gs], p1, p2, True, simulate_boundaries)
+        comps[i] = _add_at(comps[i], gs, -c1)
+        comps[j] = _add_at(comps[j], gs, c2)
+        new_psi[pml.name] = (p1n, p2n)
+    return torch.stack(comps, 0), new_psi
+
+
+def curl_H(H_pad, psi_E, pmls, simulate_boundaries):
+    """fdtdx/core/physics/curl.py:314-397 (uniform grid)."""
+    Hx, Hy, Hz = H_pad[0], H_pad[1], H_pad[2]
+    c = (slice(1, -1), slice(1, -1), slice(1, -1))
+    dyHz = Hz[c] - Hz[1:-1, :-2, 1:-1]
+    dzHy = Hy[c] - Hy[1:-1, 1:-1, :-2]
+    dzHx = Hx[c] - Hx[1:-1, 1:-1, :-2]
+    dxHz = Hz[c] - Hz[:-2, 1:-1, 1:-1]
+    dxHy = Hy[c] - Hy[:-2, 1:-1, 1:-1]
+    dyHx = Hx[c] - Hx[1:-1, :-2, 1:-1]
+    comps = [dyHz - dzHy, dzHx - dxHz, dxHy - dyHx]
+    new_psi = {}
+    for pml in pmls:
+        a = pml.axis
+        i, j = (a + 1) % 3, (a + 2) % 3
+        if a == 0:
+            dj, di = dxHz, dxHy
+        elif a == 1:
+            dj, di = dyHx, dyHz
+        else:
+            dj, di = dzHy, dzHx
+        gs = pml.grid_slice
+        p1, p2 = psi_E[pml.name]
+        c1, c2, p1n, p2n = step_cpml(pml, dj[gs], di[gs], p1, p2, False, simulate_boundaries)
+        comps[i] = _add_at(comps[i], gs, -c1)
+        comps[j] = _add_at(comps[j], gs, c2)
+        new_psi[pml.name] = (p1n, p2n)
+    return torch.stack(comps, 0), new_psi
+
+
+def interpolate_fields(E_pad, H_pad):
+    """Co-location at the E_z point (i, j, k+1/2), fdtdx/core/physics/curl.py:86-224 (uniform grid)."""
+    Ex, Ey, Ez = E_pad[0], E_pad[1], E_pad[2]
+    Hx, Hy, Hz = H_pad[0], H_pad[1], H_pad[2]
+
+    def avg(cur, prev):
+        return 0.5 * (cur + prev)
+
+    Ex_lo = avg(Ex[1:-1, 1:-1, 1:-1], Ex[:-2, 1:-1, 1:-1])
+    Ex_up = avg(Ex[1:-1, 1:-1, 2:], Ex[:-2, 1:-1, 2:])
+    ex = (Ex_lo + Ex_up) / 2.0
+    Ey_lo = avg(Ey[1:-1, 1:-1, 1:-1], Ey[1:-1, :-2, 1:-1])
+    Ey_up = avg(Ey[1:-1, 1:-1, 2:], Ey[1:-1, :-2, 2:])
+    ey = (Ey_lo + Ey_up) / 2.0
+    ez = Ez[1:-1, 1:-1, 1:-1]
+    hx = avg(Hx[1:-1, 1:-1, 1:-1], Hx[1:-1, :-2, 1:-1])
+    hy = avg(Hy[1:-1, 1:-1, 1:-1], Hy[:-2, 1:-1, 1:-1])
+    lx = avg(Hz[1:-1, 1:-1, 1:-1], Hz[:-2, 1:-1, 1:-1])
+    lxy = avg(lx, avg(Hz[1:-1, :-2, 1:-1], Hz[:-2, :-2, 1:-1]))
+    ux = avg(Hz[1:-1, 1:-1, 2:], Hz[:-2, 1:-1, 2:])
+    uxy = avg(ux, avg(Hz[1:-1, :-2, 2:], Hz[:-2, :-2, 2:]))
+    hz = (lxy + uxy) / 2.0
+    return torch.stack([ex, ey, ez], 0), torch.stack([hx, hy, hz], 0)
+
+
+# --------------------------------------------------------------------------------------------
+# temporal profiles
+# --------------------------------------------------------------------------------------------
+
+
+def profile_amplitude(profile, time: torch.Tensor, period: float, phase_shift: float) -> torch.Tensor:
+    """fdtdx/objects/sources/profile.py:253-345 with core/window.py:16-30 (Re(exp(-i p)) = cos p)."""
+    name = type(profile).__name__
+    if name == "SingleFrequencyProfile":
+        phase = 2 * math.pi * time / period + phase_shift + profile.phase_shift
+        raw = torch.cos(phase)
+        factor = torch.clamp(time / (profile.num_startup_periods * period), 0.0, 1.0)
+        return factor * raw
+    if name == "GaussianPulseProfile":
+        sigma_t = 1.0 / (2 * math.pi * profile.spectral_width.get_frequency())
+        t0 = 6 * sigma_t
+        env = torch.exp(-((time - t0) ** 2) / (2.0 * sigma_t**2))
+        phase = 2 * math.pi * profile.center_wave.get_frequency() * time + phase_shift + profile.center_wave.phase_shift
+        return env * torch.cos(phase)
+    raise NotImplementedError(name)
+
+
+# --------------------------------------------------------------------------------------------
+# scene
+# --------------------------------------------------------------------------------------------
+
+
+@dataclass
+class OSource:
+    obj: Any
+    kind: str
+    on: list
+    on_idx: list
+    default_on: bool
+    # dipole
+    inv_local: torch.Tensor | None = None
+    # plane
+    E_inc: torch.Tensor | None = None
+    H_inc: torch.Tensor | None = None
+    off_E: torch.Tensor | None = None
+    off_H: torch.Tensor | None = None
+
+
+@dataclass
+class ODetector:
+    obj: Any
+    kind: str
+    on: list
+    arr_idx: list
+    window: np.ndarray | None = None
+    scale: float = 1.0
+
+
+class OracleScene:
+    """A placed scene restated for the oracle in one dtype (float32 or float64)."""
+
+    def __init__(self, objects, arrays, config, dtype=torch.float64):
+        self.dtype = dtype
+        vol = objects.volume
+        self.shape = tuple(vol.grid_shape)
+        self.dx = float(config.grid.spacing)
+        self.courant = config.courant_factor / math.sqrt(3)
+        self.dt = self.courant * self.dx / C0
+        self.T = round(config.time / self.dt)
+        self.inv_eps = arrays.inv_permittivities.detach().to("cpu", dtype)
+        mu = arrays.inv_permeabilities
+        self.inv_mu = mu.detach().to("cpu", dtype) if isinstance(mu, torch.Tensor) else float(mu)
+        se, sh = arrays.electric_conductivity, arrays.magnetic_conductivity
+        self.sigma_E = se.detach().to("cpu", dtype) if se is not None else None
+        self.sigma_H = sh.detach().to("cpu", dtype) if sh is not None else None
+        self.periodic = [False, False, False]
+        self.pec, self.pmc, self.pmls = [], [], []
+        for b in objects.boundary_objects:
+            name = type(b).__name__
+            if name in ("PeriodicBoundary", "BlochBoundary"):
+                self.periodic[b.axis] = True
+            elif name == "PerfectElectricConductor":
+                self.pec.append(b)
+            elif name == "PerfectMagneticConductor":
+                self.pmc.append(b)
+            elif name == "PerfectlyMatchedLayer":
+                co = pml_coefficients(b, self.dx, self.dt, dtype)
+                self.pmls.append(
+                    OPml(b.name, b.axis, b.direction, b.grid_slice, b.kappa_start, b.kappa_end, co["a_E"], co["b_E"],
+                         co["inv_kappa_E"], co["a_H"], co["b_H"], co["inv_kappa_H"])
+                )
+        self.periodic = tuple(self.periodic)
+        self.sources = [self._setup_source(s) for s in objects.sources]
+        self.detectors = [self._setup_detector(d) for d in objects.detectors if not d.inverse]
+
+    # ---- sources
+    def _switch_tables(self, sw):
+        on = sw.calculate_on_list(self.T, self.dt)
+        idx = sw.calculate_time_step_to_on_arr_idx(self.T, self.dt)
+        return on, idx
+
+    def _setup_source(self, s) -> OSource:
+        on, idx = self._switch_tables(s.switch)
+        default_on = s.switch.is_default_always_on
+        name = type(s).__name__
+        if name == "PointDipoleSource":
+            inv = self.inv_eps if s.source_type == "electric" else self.inv_mu
+            if isinstance(inv, torch.Tensor):
+                local = inv[(slice(None), *s.grid_slice)]
+            else:
+                local = torch.tensor(inv, dtype=self.dtype)
+            return OSource(s, "dipole", on, idx, default_on, inv_local=local)
+        if name in ("GaussianPlaneSource", "UniformPlaneSource"):
+            E, H, oE, oH = self._plane_apply(s)
+            return OSource(s, "plane", on, idx, default_on, E_inc=E, H_inc=H, off_E=oE, off_H=oH)
+        raise NotImplementedError(name)
+
+    def _plane_apply(self, s):
+        """LinearlyPolarizedPlaneSource.apply for normal incidence (linear_polarization.py:168-358)."""
+        dt_ = self.dtype
+        gs = s.grid_shape
+        n = gs.index(1)
+        h_ax, v_ax = (n + 1) % 3, (n + 2) % 3
+        W, Hh = gs[h_ax], gs[v_ax]
+        center = torch.tensor([0.5 * (0 + W - 1), 0.5 * (0 + Hh - 1)], dtype=dt_)
+        # polarization (core/misc.py:471-505, core/linalg.py:7-47)
+        k = torch.zeros(3, dtype=dt_)
+        k[n] = 1.0 if s.direction == "+" else -1.0
+        e = None if s.fixed_E_polarization_vector is None else torch.tensor(s.fixed_E_polarization_vector, dtype=dt_)
+        h = None if s.fixed_H_polarization_vector is None else torch.tensor(s.fixed_H_polarization_vector, dtype=dt_)
+        if h is not None:
+            h = h / torch.linalg.norm(h)
+        if e is not None:
+            e = e / torch.linalg.norm(e)
+        if e is None:
+            e = torch.linalg.cross(h, k)
+        if h is None:
+            h = torch.linalg.cross(k, e)
+        # raw amplitude (linear_polarization.py:392-482)
+        if type(s).__name__ == "GaussianPlaneSource":
+            r = s.radius / self.dx
+            w_, h_ = torch.meshgrid(torch.arange(W, dtype=dt_), torch.arange(Hh, dtype=dt_), indexing="ij")
+            grid = (torch.stack([w_, h_], -1) - center) / torch.tensor([r, r], dtype=dt_)
+            d2 = (grid**2).sum(-1)
+            prof = torch.where(d2 < 1, torch.exp(-0.5 * d2 / s.std**2), torch.zeros_like(d2))
+            prof_hv = prof / prof.sum()
+        else:
+            prof_hv = s.amplitude * torch.ones((W, Hh), dtype=dt_)
+        # projection of the untilted plane is the identity; linear_interpolated_indexing at an
+        # integer point returns 4 v / (4 + 1e-8) (core/misc.py:363-390)
+        interp = (4.0 * prof_hv) / (4.0 + 1e-8)
+        prof2 = interp.T if h_ax > v_ax else interp
+        amp = prof2.unsqueeze(n)[None]
+        E = amp * e[:, None, None, None]
+        H = amp * h[:, None, None, None]
+        sl = (slice(None), *s.grid_slice)
+        ie = self.inv_eps[sl]
+        im = self.inv_mu[sl] if isinstance(self.inv_mu, torch.Tensor) else self.inv_mu
+        if s.normalize_by_energy:
+            energy = (0.5 * (1 / ie) * E.abs() ** 2).sum(0) + (0.5 * (1 / im) * H.abs() ** 2).sum(0)
+            root = torch.sqrt(energy.sum())
+            E = E / root
+            H = H / root
+        H = H / torch.sqrt(ie / im)
+        # calculate_time_offset_yee (fdtdx/core/grid.py:720-880), uniform edges
+        edges = [torch.arange(gs[ax] + 1, dtype=dt_) * self.dx for ax in range(3)]
+        cphys = torch.zeros(3, dtype=dt_)
+        cphys[h_ax] = center[0] * self.dx
+        cphys[v_ax] = center[1] * self.dx
+
+        def pos(offsets):
+            coords = []
+            for ax in range(3):
+                ed = edges[ax]
+                coords.append(ed[:-1] if offsets[ax] == 0 else 0.5 * (ed[:-1] + ed[1:]))
+            X, Y, Z = torch.meshgrid(*coords, indexing="ij")
+            return torch.stack([X, Y, Z], -1) - cphys
+
+        xyz_E = torch.stack([pos((0.5, 0, 0)), pos((0, 0.5, 0)), pos((0, 0, 0.5))])
+        xyz_H = torch.stack([pos((0, 0.5, 0.5)), pos((0.5, 0, 0.5)), pos((0.5, 0.5, 0))])
+        travel_E = -(xyz_E @ k)
+        travel_H = -(xyz_H @ k)
+        ie0 = ie[0]
+        im0 = im[0] if isinstance(im, torch.Tensor) else im
+        n_r = 1 / torch.sqrt(ie0 * im0)
+        vel = (C0 / n_r)[None]
+        return E, H, travel_E / (vel * self.dt), travel_H / (vel * self.dt)
+
+    # ---- detectors
+    def _setup_detector(self, d) -> ODetector:
+        name = type(d).__name__
+        on = d.on_list(_ConfigShim(self))
+        idx, cnt = [-1] * self.T, 0
+        for t in range(self.T):
+            if on[t]:
+                idx[t] = cnt
+                cnt += 1
+        if name in ("PhasorDetector", "PhasorPoyntingFluxDetector"):
+            on_arr = np.asarray(on, np.float64)
+            window = on_arr if d.apodization is None else d.apodization.get_window(np.arange(self.T) * self.dt) * on_arr
+            wsum = float(window.sum())
+            scale = 2 / wsum if d.scaling_mode == "continuous" else float(d.resolve_dft_stride(_ConfigShim(self)))
+            return ODetector(d, "phasor", on, idx, window=window, scale=scale)
+        kind = {"FieldDetector": "field", "PoyntingFluxDetector": "flux", "EnergyDetector": "energy"}[name]
+        return ODetector(d, kind, on, idx)
+
+    # ---- state
+    def init_state(self) -> "OState":
+        z = torch.zeros((3, *self.shape), dtype=self.dtype)
+        psi_E = {p.name: (torch.zeros(_slab_shape(self.shape, p), dtype=self.dtype),) * 2 for p in self.pmls}
+        psi_H = {p.name: (torch.zeros(_slab_shape(self.shape, p), dtype=self.dtype),) * 2 for p in self.pmls}
+        det = {}
+        for od in self.detectors:
+            d = od.obj
+            gs = d.grid_shape
+            n_on = sum(od.on)
+            if od.kind == "phasor":
+                F, Cc = len(d.wave_characters), len(d.recorded_components)
+                cdt = torch.complex128 if self.dtype == torch.float64 else torch.complex64
+                shp = (1, F, Cc) if d.reduce_volume else (1, F, Cc, *gs)
+                det[d.name] = {"phasor": torch.zeros(shp, dtype=cdt)}
+            elif od.kind == "field":
+                Cc = len(d.recorded_components)
+                det[d.name] = {"fields": torch.zeros((n_on, Cc) if d.reduce_volume else (n_on, Cc, *gs), dtype=self.dtype)}
+            elif od.kind == "flux":
+                if d.keep_all_components:
+                    shp = (n_on, 3) if d.reduce_volume else (n_on, 3, *gs)
+                else:
+                    shp = (n_on, 1) if d.reduce_volume else (n_on, *gs)
+                det[d.name] = {"poynting_flux": torch.zeros(shp, dtype=self.dtype)}
+            else:
+                det[d.name] = {"energy": torch.zeros((n_on, 1) if d.reduce_volume else (n_on, *gs), dtype=self.dtype)}
+        return OState(0, z.clone(), z.clone(), psi_E, psi_H, det, [])
+
+
+class _ConfigShim:
+    """The few config attributes the objects' on-list helpers read."""
+
+    def __init__(self, sc: OracleScene):
+        self.time_steps_total = sc.T
+        self.time_step_duration = sc.dt
+
+
+def _slab_shape(shape, p: OPml):
+    return tuple(b - a for a, b in (s.indices(n)[:2] for s, n in zip(p.grid_slice, shape)))
+
+
+@dataclass
+class OState:
+    t: int
+    E: torch.Tensor
+    H: torch.Tensor
+    psi_E: dict
+    psi_H: dict
+    det: dict
+    rec: list = field(default_factory=list)
+
+
+# --------------------------------------------------------------------------------------------
+# sources
+# --------------------------------------------------------------------------------------------
+
+
+def _src_time(sc: OracleScene, s: OSource, t: float, eside: bool):
+    """(is_on, time step used) per update.py:494-519 / 824-849 and source.py:41-49."""
+    half = 0.0 if eside else 0.5
+    if s.default_on:
+        return True, t + half
+    ti = int(t)
+    on = s.on[jax_index(sc.T, ti)]
+    adj = float(s.on_idx[ti]) if 0 <= ti < sc.T else 0.0
+    return on, adj + half
+
+
+def _source_update_E(sc: OracleScene, s: OSource, E, inv_eps, t: float, inverse: bool):
+    o = s.obj
+    c = sc.courant
+    dt_ = sc.dtype
+    if s.kind == "dipole":
+        if o.source_type != "electric":
+            return E
+        amp = profile_amplitude(o.temporal_profile, torch.tensor(t, dtype=dt_) * sc.dt,
+                                o.wave_character.get_period(), o.wave_character.phase_shift)
+        sign = -1.0 if not inverse else 1.0
+        scale = c * o.amplitude * o.static_amplitude_factor * amp
+        orient = torch.zeros(3, dtype=dt_)
+        orient[o.polarization] = 1.0
+        oriented = s.inv_local * orient.reshape(3, 1, 1, 1)
+        inj = scale * oriented[o.polarization]
+        return _add_at(E, (o.polarization, *o.grid_slice), sign * inj)
+    # TFSF plane E-side (tfsf.py:193-308, 739-771)
+    n = o.grid_shape.index(1)
+    a_ax, b_ax = (n + 1) % 3, (n + 2) % 3
+    sign = 1 if o.direction == "+" else -1
+    if inverse:
+        sign = -sign
+    ies = inv_eps.detach()[(slice(None), *o.grid_slice)]
+    amp = {}
+    for ax in (a_ax, b_ax):
+        time_H = (t + s.off_H[ax]) * sc.dt
+        amp[ax] = profile_amplitude(o.temporal_profile, time_H, o.wave_character.get_period(),
+                                    o.wave_character.phase_shift) * o.static_amplitude_factor
+    Hb = s.H_inc[b_ax] * amp[b_ax] * c * ies[min(a_ax, ies.shape[0] - 1)]
+    Ha = s.H_inc[a_ax] * amp[a_ax] * c * ies[min(b_ax, ies.shape[0] - 1)]
+    E = _add_at(E, (a_ax, *o.grid_slice), sign * Hb)
+    E = _add_at(E, (b_ax, *o.grid_slice), -sign * Ha)
+    return E
+
+
+def _source_update_H(sc: OracleScene, s: OSource, H, inv_mu, t: float, inverse: bool):
+    o = s.obj
+    c = sc.courant
+    dt_ = sc.dtype
+    if s.kind == "dipole":
+        if o.source_type != "magnetic":
+            return H
+        amp = profile_amplitude(o.temporal_profile, torch.tensor(t, dtype=dt_) * sc.dt,
+                                o.wave_character.get_period(), o.wave_character.phase_shift)
+        sign = -1.0 if not inverse else 1.0
+        scale = c * o.amplitude * o.static_amplitude_factor * amp
+        orient = torch.zeros(3, dtype=dt_)
+        orient[o.polarization] = 1.0
+        oriented = s.inv_local * orient.reshape(3, 1, 1, 1)
+        inj = scale * oriented[o.polarization]
+        return _add_at(H, (o.polarization, *o.grid_slice), sign * inj)
+    n = o.grid_shape.index(1)
+    a_ax, b_ax = (n + 1) % 3, (n + 2) % 3
+    sign = 1 if o.direction == "+" else -1
+    if inverse:
+        sign = -sign
+    if isinstance(inv_mu, torch.Tensor):
+        ims = inv_mu.detach()[(slice(None), *o.grid_slice)]
+        im_a, im_b = ims[min(a_ax, ims.shape[0] - 1)], ims[min(b_ax, ims.shape[0] - 1)]
+    else:
+        im_a = im_b = inv_mu
+    amp = {}
+    for ax in (a_ax, b_ax):
+        time_E = (t + s.off_E[ax]) * sc.dt
+        amp[ax] = profile_amplitude(o.temporal_profile, time_E, o.wave_character.get_period(),
+                                    o.wave_character.phase_shift) * o.static_amplitude_factor
+    Ea = s.E_inc[a_ax] * amp[a_ax] * c * im_b
+    Eb = s.E_inc[b_ax] * amp[b_ax] * c * im_a
+    H = _add_at(H, (b_ax, *o.grid_slice), sign * Ea)
+    H = _add_at(H, (a_ax, *o.grid_slice), -sign * Eb)
+    return H
+
+
+def _apply_sources(sc, field_, mat, t: int, eside: bool, inverse: bool):
+    for s in sc.sources:
+        on, tt = _src_time(sc, s, t, eside)
+        if not on:
+            continue
+        if eside:
+            field_ = _source_update_E(sc, s, field_, mat, tt, inverse)
+        else:
+            field_ = _source_update_H(sc, s, field_, mat, tt, inverse)
+    return field_
+
+
+def _walls(sc, F, walls):
+    for b in walls:
+        c1, c2 = ((1, 2), (0, 2), (0, 1))[b.axis]
+        F = _set_at(F, (c1, *b.grid_slice), 0.0)
+        F = _set_at(F, (c2, *b.grid_slice), 0.0)
+    return F
+
+
+# --------------------------------------------------------------------------------------------
+# updates
+# --------------------------------------------------------------------------------------------
+
+
+def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=True):
+    """fdtdx/fdtd/update.py:256-523 (isotropic / diagonal branch)."""
+    c = sc.courant
+    curl, psi_E = curl_H(pad_fields(H, sc.periodic), psi_E, sc.pmls, simulate_boundaries)
+    sig = sc.sigma_E
+    factor = 1
+    if sig is not None:
+        factor = 1 - c * sig * ETA0 * inv_eps / 2
+    E = factor * E + c * curl * inv_eps
+    if sig is not None:
+        E = E / (1 + c * sig * ETA0 * inv_eps / 2)
+    E = _apply_sources(sc, E, inv_eps, t, True, False)
+    return _walls(sc, E, sc.pec), psi_E
+
+
+def update_H(sc: OracleScene, t: int, E, H, psi_H, inv_mu, simulate_boundaries=True):
+    """fdtdx/fdtd/update.py:689-853 (isotropic / diagonal branch)."""
+    c = sc.courant
+    curl, psi_H = curl_E(pad_fields(E, sc.periodic), psi_H, sc.pmls, simulate_boundaries)
+    sig = sc.sigma_H
+    factor = 1
+    if sig is not None:
+        factor = 1 - c * sig / ETA0 * inv_mu / 2
+    H = factor * H - c * curl * inv_mu
+    if sig is not None:
+        H = H / (1 + c * sig / ETA0 * inv_mu / 2)
+    H = _apply_sources(sc, H, inv_mu, t, False, False)
+    return _walls(sc, H, sc.pmc), psi_H
+
+
+def update_E_reverse(sc: OracleScene, t: int, E, H, psi_E, inv_eps):
+    """fdtdx/fdtd/update.py:526-686."""
+    c = sc.courant
+    E = _apply_sources(sc, E, inv_eps, t, True, True)
+    curl, _ = curl_H(pad_fields(H, sc.periodic), psi_E, sc.pmls, False)
+    sig = sc.sigma_E
+    factor = 1
+    if sig is not None:
+        E = E * (1 + c * sig * ETA0 * inv_eps / 2)
+        factor = 1 - c * sig * ETA0 * inv_eps / 2
+    E = (E - c * curl * inv_eps) / factor
+    return _walls(sc, E, sc.pec)
+
+
+def update_H_reverse(sc: OracleScene, t: int, E, H, psi_H, inv_mu):
+    """fdtdx/fdtd/update.py:856-1007."""
+    c = sc.courant
+    H = _apply_sources(sc, H, inv_mu, t, False, True)
+    curl, _ = curl_E(pad_fields(E, sc.periodic), psi_H, sc.pmls, False)
+    sig = sc.sigma_H
+    factor = 1
+    if sig is not None:
+        H = H * (1 + c * sig / ETA0 * inv_mu / 2)
+        factor = 1 - c * sig / ETA0 * inv_mu / 2
+    H = (H + c * curl * inv_mu) / factor
+    return _walls(sc, H, sc.pmc)
+
+
+# --------------------------------------------------------------------------------------------
+# detectors and interfaces
+# --------------------------------------------------------------------------------------------
+
+
+def update_detectors(sc: OracleScene, t: int, E, H, H_prev, det: dict, inv_eps, inv_mu) -> dict:
+    """fdtdx/fdtd/update.py:1040-1137 with each detector's update()."""
+    out = dict(det)
+    full = None
+    for od in sc.detectors:
+        d = od.obj
+        if not od.on[jax_index(sc.T, t)]:
+            continue
+        gs = (slice(None), *d.grid_slice)
+        if d.exact_interpolation:
+            if full is None:
+                full = interpolate_fields(pad_fields(E, sc.periodic), pad_fields((H_prev + H) / 2, sc.periodic))
+            Er, Hr = full[0][gs], full[1][gs]
+        else:
+            Er, Hr = E[gs], H[gs]
+        st = det[d.name]
+        if od.kind in ("phasor", "field"):
+            EH = torch.stack([torch.cat([Er, Hr], 0)[COMPONENTS.index(cn)] for cn in d.recorded_components], 0)
+        if od.kind == "phasor":
+            time_passed = torch.tensor(float(t), dtype=sc.dtype) * sc.dt
+            omegas = torch.tensor([2 * math.pi * wc.get_frequency() for wc in d.wave_characters], dtype=sc.dtype)
+            ph = torch.exp(1j * (omegas * time_passed))
+            ph = ph.reshape((len(omegas),) + (1,) * EH.ndim)
+            w = float(od.window[jax_index(sc.T, t)])
+            new = EH * ph * od.scale * w
+            if d.reduce_volume:
+                new = new.mean(dim=tuple(range(2, new.ndim)))
+            res = st["phasor"] - new[None] if d.inverse else st["phasor"] + new[None]
+            out[d.name] = {"phasor": res}
+        elif od.kind == "field":
+            if d.reduce_volume:
+                EH = EH.mean(dim=(1, 2, 3))
+            idx = od.arr_idx[jax_index(sc.T, t)]
+            out[d.name] = {"fields": _set_at(st["fields"], idx, EH)}
+        elif od.kind == "flux":
+            S = torch.stack([
+                Er[1] * Hr[2] - Er[2] * Hr[1],
+                Er[2] * Hr[0] - Er[0] * Hr[2],
+                Er[0] * Hr[1] - Er[1] * Hr[0],
+            ], 0)
+            pf = S if d.keep_all_components else S[d.propagation_axis]
+            if d.direction == "-":
+                pf = -pf
+            if d.reduce_volume:
+                pf = pf * (sc.dx * sc.dx)
+                pf = pf.sum(dim=(1, 2, 3)) if d.keep_all_components else pf.sum().reshape(1)
+            idx = od.arr_idx[jax_index(sc.T, t)]
+            out[d.name] = {"poynting_flux": _set_at(st["poynting_flux"], idx, pf)}
+        else:  # energy
+            ie = inv_eps[gs]
+            im = inv_mu[gs] if isinstance(inv_mu, torch.Tensor) else inv_mu
+            e = (0.5 * (1 / ie) * Er**2).sum(0) + (0.5 * (1 / im) * Hr**2).sum(0)
+            if d.reduce_volume:
+                e = (e * sc.dx**3).sum().reshape(1)
+            idx = od.arr_idx[jax_index(sc.T, t)]
+            out[d.name] = {"energy": _set_at(st["energy"], idx, e)}
+    return out
+
+
+def interface_slice(p: OPml, shape):
+    st = [s.indices(n)[:2] for s, n in zip(p.grid_slice, shape)]
+    lo, hi = st[p.axis]
+    st[p.axis] = (lo, lo + 1) if p.direction == "+" else (hi - 1, hi)
+    return tuple(slice(a, b) for a, b in st)
+
+
+def collect_interfaces(sc: OracleScene, E, H) -> dict:
+    """fdtdx/fdtd/misc.py:10-35."""
+    return {f"{p.name}_{fs}": F[(slice(None), *interface_slice(p, sc.shape))].clone()
+            for fs, F in (("E", E), ("H", H)) for p in sc.pmls}
+
+
+def add_interfaces(sc: OracleScene, E, H, values: dict):
+    """fdtdx/fdtd/misc.py:38-66."""
+    for p in sc.pmls:
+        sl = (slice(None), *interface_slice(p, sc.shape))
+        E = _set_at(E, sl, values[f"{p.name}_E"])
+        H = _set_at(H, sl, values[f"{p.name}_H"])
+    return E, H
+
+
+# --------------------------------------------------------------------------------------------
+# steps and runs
+# --------------------------------------------------------------------------------------------
+
+
+def forward(sc: OracleScene, st: OState, inv_eps=None, inv_mu=None, record_detectors=True,
+            record_boundaries=False, simulate_boundaries=True) -> OState:
+    """One forward step, fdtdx/fdtd/forward.py:83-156."""
+    inv_eps = sc.inv_eps if inv_eps is None else inv_eps
+    inv_mu = sc.inv_mu if inv_mu is None else inv_mu
+    t = st.t
+    H_prev = st.H
+    E, psi_E = update_E(sc, t, st.E, st.H, st.psi_E, inv_eps, simulate_boundaries)
+    H, psi_H = update_H(sc, t, E, st.H, st.psi_H, inv_mu, simulate_boundaries)
+    rec = st.rec
+    if record_boundaries:
+        rec = rec + [collect_interfaces(sc, E, H)]
+    det = update_detectors(sc, t, E, H, H_prev, st.det, inv_eps, inv_mu) if record_detectors else st.det
+    return OState(t + 1, E, H, psi_E, psi_H, det, rec)
+
+
+def backward(sc: OracleScene, st: OState) -> OState:
+    """One reverse step with reset_fields=False and no detectors (fdtdx/fdtd/backward.py:62-135)."""
+    t = st.t - 1
+    E, H = st.E, st.H
+    if st.rec:
+        E, H = add_interfaces(sc, E, H, st.rec[t])  # a Python list wraps t = -1 like the JAX gather
+    H = update_H_reverse(sc, t, E, H, st.psi_H, sc.inv_mu)
+    E = update_E_reverse(sc, t, E, H, st.psi_E, sc.inv_eps)
+    return OState(t, E, H, st.psi_E, st.psi_H, st.det, st.rec)
+
+
+def run(sc: OracleScene, n_steps: int | None = None, record_boundaries=False, state: OState | None = None) -> OState:
+    st = sc.init_state() if state is None else state
+    n = sc.T if n_steps is None else n_steps
+    with torch.no_grad():
+        for _ in range(n):
+            st = forward(sc, st, record_boundaries=record_boundaries)
+    return st
+
+
+def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=None, cot_H=None) -> torch.Tensor:
+    """d loss / d inv_eps by the reference's custom VJP (fdtdx/fdtd/fdtd.py:215-333).
+
+    Reverse-reconstructs the state step by step (psi frozen, interfaces re-imposed) and
+    applies the VJP of one forward step at each reconstructed state, from t = T-1 down to
+    t = -1 (the reference's loop condition ``time_step >= 0`` admits one step at t = -1).
+    Cotangents follow torch's convention for complex detector states.
+    """
+    zE = torch.zeros_like(final.E)
+    lam = {
+        "E": zE.clone() if cot_E is None else cot_E.clone(),
+        "H": zE.clone() if cot_H is None else cot_H.clone(),
+        "psi_E": {k: (torch.zeros_like(a), torch.zeros_like(b)) for k, (a, b) in final.psi_E.items()},
+        "psi_H": {k: (torch.zeros_like(a), torch.zeros_like(b)) for k, (a, b) in final.psi_H.items()},
+        "det": {k: {k2: cot_det.get(k, {}).get(k2, torch.zeros_like(v2)) for k2, v2 in v.items()}
+                for k, v in final.det.items()},
+    }
+    grad = torch.zeros_like(sc.inv_eps)
+    st = final
+    while st.t >= 0:
+        st = backward(sc, st)
+        E = st.E.clone().requires_grad_(True)
+        H = st.H.clone().requires_grad_(True)
+        pE = {k: (a.clone().requires_grad_(True), b.clone().requires_grad_(True)) for k, (a, b) in st.psi_E.items()}
+        pH = {k: (a.clone().requires_grad_(True), b.clone().requires_grad_(True)) for k, (a, b) in st.psi_H.items()}
+        det_in = {k: {k2: v2.clone().requires_grad_(True) for k2, v2 in v.items()} for k, v in st.det.items()}
+        ie = sc.inv_eps.clone().requires_grad_(True)
+        out = forward(sc, OState(st.t, E, H, pE, pH, det_in, []), inv_eps=ie, record_detectors=True)
+        outs, cots, ins = [out.E, out.H], [lam["E"], lam["H"]], [E, H, ie]
+        for k in pE:
+            outs += [out.psi_E[k][0], out.psi_E[k][1], out.psi_H[k][0], out.psi_H[k][1]]
+            cots += [lam["psi_E"][k][0], lam["psi_E"][k][1], lam["psi_H"][k][0], lam["psi_H"][k][1]]
+            ins += [pE[k][0], pE[k][1], pH[k][0], pH[k][1]]
+        dkeys = [(k, k2) for k, v in det_in.items() for k2 in v]
+        for k, k2 in dkeys:
+            outs.append(out.det[k][k2])
+            cots.append(lam["det"][k][k2])
+            ins.append(det_in[k][k2])
+        pairs = [(o, c) for o, c in zip(outs, cots) if o.requires_grad]
+        g = torch.autograd.grad([o for o, _ in pairs], ins, grad_outputs=[c for _, c in pairs], allow_unused=True)
+        g = [torch.zeros_like(x) if gi is None else gi for gi, x in zip(g, ins)]
+        lam["E"], lam["H"] = g[0], g[1]
+        grad = grad + g[2]
+        q = 3
+        for k in pE:
+            lam["psi_E"][k] = (g[q], g[q + 1])
+            lam["psi_H"][k] = (g[q + 2], g[q + 3])
+            q += 4
+        for k, k2 in dkeys:
+            lam["det"][k][k2] = g[q]
+            q += 1
+    return grad
+
+
+def autograd_gradient(sc: OracleScene, loss_fn, n_steps: int | None = None) -> torch.Tensor:
+    """Exact gradient of loss_fn(final detector states) by autograd through the whole forward run."""
+    ie = sc.inv_eps.clone().requires_grad_(True)
+    st = sc.init_state()
+    n = sc.T if n_steps is None else n_steps
+    for _ in range(n):
+        st = forward(sc, st, inv_eps=ie)
+    loss = loss_fn(st.det)
+    (g,) = torch.autograd.grad(loss, [ie])
+    return g
