@@ -134,10 +134,13 @@ def run_gpu(args):
     if ws > 1:
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    objects, arrays, _, cfg, _ = scenes.coupler(shape=SHAPE, steps=T_TOTAL, device=dev)
+    shape = tuple(int(x) for x in args.shape.split(",")) if args.shape else SHAPE
+    objects, arrays, _, cfg, _ = scenes.coupler(shape=shape, steps=T_TOTAL, device=dev)
     arrays = arrays.reset()
     scene = get_scene(objects, arrays, cfg)
-    ncell = SHAPE[0] * SHAPE[1] * SHAPE[2]
+    if args.chunk:
+        NATIVE.check(NATIVE.load().fdtd_plan_tune(scene.plan, args.chunk), scene.plan, "fdtd_plan_tune")
+    ncell = shape[0] * shape[1] * shape[2]
     W, K = args.warmup, args.steps
     if W + K + 8 > T_TOTAL:
         raise SystemExit("warmup + steps must stay below the 8000-step run")
@@ -190,17 +193,20 @@ def run_gpu(args):
         res = [out.detector_states[n]["phasor"].to("cpu") for n in ("flux1", "flux2")]
         return res
 
-    e2e_once()
-    torch.cuda.synchronize()
-    reps = 2
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        res = e2e_once()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / reps
-    h2d = host_eps.numel() * 4
-    d2h = sum(r.numel() * 8 for r in res)
-    e2e_val = ncell * K * ws / e2e_s
+    e2e = None
+    if not args.no_e2e:
+        e2e_once()
+        torch.cuda.synchronize()
+        reps = 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            res = e2e_once()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / reps
+        h2d = host_eps.numel() * 4
+        d2h = sum(r.numel() * 8 for r in res)
+        e2e = {"value": ncell * K * ws / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / K,
+               "d2h_bytes_per_step": d2h / K, "api": "fdtdx_gb300.run_fdtd"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -220,11 +226,12 @@ def run_gpu(args):
         "dtype": "f32",
         "data": "synthetic (seeded scene builder)",
         "config": {
-            "workload": "coupler 400x400x200 @20nm, 10-cell CPML, CW Gaussian TFSF source, full-volume Ex/Ey/Ez "
+            "workload": f"coupler {shape[0]}x{shape[1]}x{shape[2]} @20nm, 10-cell CPML, CW Gaussian TFSF source, full-volume Ex/Ey/Ez "
                         "phasor + 2 phasor-flux planes (8000-step run; K consecutive steps timed)",
             "cells": ncell,
             "l2": "inputs larger than L2 (fields 384 MB, phasor 768 MB)",
             "parallelism": f"replicas x{ws}",
+            "chunk": int(NATIVE.load().fdtd_plan_chunk(scene.plan)),
             "hbm_gbs_effective": round(sum(alg.values()) / (ms / K / 1e3) / 1e9, 1),
         },
         "roofline": {
@@ -239,8 +246,7 @@ def run_gpu(args):
             "alg_bytes_per_launch": alg[dom],
             "kernel_ms": {k: round(v, 4) for k, v in times.items()},
         },
-        "e2e": {"value": e2e_val, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
-                "api": "fdtdx_gb300.run_fdtd"},
+        "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -328,6 +334,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--shape", default="", help="grid override nx,ny,nz (profiling cases)")
+    ap.add_argument("--chunk", type=int, default=0, help="x planes per update block (0: plan default)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("warmup must be >= 3")

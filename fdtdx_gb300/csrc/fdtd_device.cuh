@@ -31,6 +31,22 @@ struct Geo {
     int pec, pmc;               // face masks, bit (2*axis + side)
 };
 
+// A detector accumulated inside the H half-step: E components only, so every value
+// it needs is final when the H step runs (phasor or time-domain field, no reduction).
+struct DFuse {
+    int kind;                   // FDTD_DET_PHASOR or FDTD_DET_FIELD
+    int exact, mask, nout, nfreq, inverse;
+    int lo[3], hi[3];
+    int rx, ry, rz;
+    long long R;
+    const int* slot;
+    const float2* w;
+    void* state;
+};
+
+constexpr int kMaxFuse = 2;
+constexpr int kMaxFuseFreq = 4;
+
 // Arguments of one E or H half-step (forward or reverse).
 struct UpdArgs {
     Geo g;
@@ -46,6 +62,10 @@ struct UpdArgs {
     DSlab slab[FDTD_MAX_SLABS];
     float* psi1[FDTD_MAX_SLABS];
     float* psi2[FDTD_MAX_SLABS];
+    int chunk;                  // x planes per block (the block marches along x)
+    const int* tp;              // device time-step counter
+    int n_fuse;
+    DFuse fuse[kMaxFuse];
 };
 
 struct DSource {

@@ -13,34 +13,13 @@
 
 namespace fdtd {
 
-// ---------------------------------------------------------------------------------
-// E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
-// reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
-// curl_H with CPML psi (fdtdx/core/physics/curl.py:314-397,
-// fdtdx/objects/boundaries/perfectly_matched_layer.py:138-190).
-// ---------------------------------------------------------------------------------
-template <bool REV>
-__global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
-    const Geo& g = a.g;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (j >= g.ny || k >= g.nz) return;
-    const long long N = g.N;
-    const long long c = cell_index(g, i, j, k);
-    const float* __restrict__ H = a.F;
-    const float Hx = __ldg(H + c), Hy = __ldg(H + N + c), Hz = __ldg(H + 2 * N + c);
-    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
-    const float Hz_jm = j > 0 ? __ldg(H + 2 * N + c - sy) : ld_halo(g, H, 2, i, j - 1, k);
-    const float Hx_jm = j > 0 ? __ldg(H + c - sy) : ld_halo(g, H, 0, i, j - 1, k);
-    const float Hy_km = k > 0 ? __ldg(H + N + c - 1) : ld_halo(g, H, 1, i, j, k - 1);
-    const float Hx_km = k > 0 ? __ldg(H + c - 1) : ld_halo(g, H, 0, i, j, k - 1);
-    const float Hz_im = i > 0 ? __ldg(H + 2 * N + c - sx) : ld_halo(g, H, 2, i - 1, j, k);
-    const float Hy_im = i > 0 ? __ldg(H + N + c - sx) : ld_halo(g, H, 1, i - 1, j, k);
-    const float dyHz = Hz - Hz_jm, dzHy = Hy - Hy_km, dzHx = Hx - Hx_km;
-    const float dxHz = Hz - Hz_im, dxHy = Hy - Hy_im, dyHx = Hx - Hx_jm;
-    float cu[3] = {dyHz - dzHy, dzHx - dxHz, dxHy - dyHx};
-
+// CPML correction of one cell (fdtdx/core/physics/curl.py:284-308, 371-394;
+// fdtdx/objects/boundaries/perfectly_matched_layer.py:138-190).  d[] holds the six raw
+// differences in the order (dy Fz, dz Fy, dz Fx, dx Fz, dx Fy, dy Fx); for a slab on axis a
+// d_a F_j and d_a F_i are (3, 4), (5, 0), (1, 2) and the corrections go to
+// curl[(a+1)%3] (minus) and curl[(a+2)%3] (plus).
+template <bool REV, bool HSIDE>
+__device__ __forceinline__ void cpml_correct(const UpdArgs& a, int i, int j, int k, const float d[6], float cu[3]) {
     const int idx3[3] = {i, j, k};
 #pragma unroll
     for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
@@ -48,92 +27,9 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
         const DSlab& sl = a.slab[s];
         const int l = idx3[sl.axis] - sl.lo;
         if ((unsigned)l >= (unsigned)sl.L) continue;
-        float d1, d2;
-        if (sl.axis == 0) { d1 = dxHz; d2 = dxHy; }
-        else if (sl.axis == 1) { d1 = dyHx; d2 = dyHz; }
-        else { d1 = dzHy; d2 = dzHx; }
-        const float ca = __ldg(sl.coef + l), cb = __ldg(sl.coef + sl.L + l);
-        const long long p = ((long long)(i - (sl.axis == 0 ? sl.lo : 0)) * sl.sy + (j - (sl.axis == 1 ? sl.lo : 0))) * sl.sz +
-                            (k - (sl.axis == 2 ? sl.lo : 0));
-        float p1 = a.psi1[s][p], p2 = a.psi2[s][p];
-        if (!REV) {
-            p1 = cb * p1 + ca * d1;
-            p2 = cb * p2 + ca * d2;
-            a.psi1[s][p] = p1;
-            a.psi2[s][p] = p2;
-        }
-        float c1 = p1, c2 = p2;
-        if (!sl.kappa_one) {
-            const float ikm1 = __ldg(sl.coef + 2 * sl.L + l) - 1.f;
-            c1 = ikm1 * d1 + p1;
-            c2 = ikm1 * d2 + p2;
-        }
-        const int ci = (sl.axis + 1) % 3, cj = (sl.axis + 2) % 3;
-        cu[ci] -= c1;
-        cu[cj] += c2;
-    }
-
-#pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-        const long long o = comp * N + c;
-        float e;
-        if (face_zero(g, g.pec, comp, i, j, k)) {
-            e = 0.f;
-        } else {
-            const float ie = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
-            const float e0 = a.Uin[o];
-            if (a.sig) {
-                const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
-                const float q = g.c * sg * g.eta0 * ie / 2.f;
-                if (!REV) e = ((1.f - q) * e0 + g.c * cu[comp] * ie) / (1.f + q);
-                else e = (e0 * (1.f + q) - g.c * cu[comp] * ie) / (1.f - q);
-            } else {
-                if (!REV) e = e0 + g.c * cu[comp] * ie;
-                else e = e0 - g.c * cu[comp] * ie;
-            }
-        }
-        a.Uout[o] = e;
-    }
-}
-
-// ---------------------------------------------------------------------------------
-// H half-step: H <- (g H - c curl_E(E) inv_mu) / e  (fdtdx/fdtd/update.py:717-750)
-// reverse:     H <- (H (1+q) + c curl_E(E) inv_mu) / (1-q)  (update.py:905-930)
-// ---------------------------------------------------------------------------------
-template <bool REV>
-__global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
-    const Geo& g = a.g;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (j >= g.ny || k >= g.nz) return;
-    const long long N = g.N;
-    const long long c = cell_index(g, i, j, k);
-    const float* __restrict__ E = a.F;
-    const float Ex = __ldg(E + c), Ey = __ldg(E + N + c), Ez = __ldg(E + 2 * N + c);
-    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
-    const float Ez_jp = j < g.ny - 1 ? __ldg(E + 2 * N + c + sy) : ld_halo(g, E, 2, i, j + 1, k);
-    const float Ex_jp = j < g.ny - 1 ? __ldg(E + c + sy) : ld_halo(g, E, 0, i, j + 1, k);
-    const float Ey_kp = k < g.nz - 1 ? __ldg(E + N + c + 1) : ld_halo(g, E, 1, i, j, k + 1);
-    const float Ex_kp = k < g.nz - 1 ? __ldg(E + c + 1) : ld_halo(g, E, 0, i, j, k + 1);
-    const float Ez_ip = i < g.nx - 1 ? __ldg(E + 2 * N + c + sx) : ld_halo(g, E, 2, i + 1, j, k);
-    const float Ey_ip = i < g.nx - 1 ? __ldg(E + N + c + sx) : ld_halo(g, E, 1, i + 1, j, k);
-    const float dyEz = Ez_jp - Ez, dzEy = Ey_kp - Ey, dzEx = Ex_kp - Ex;
-    const float dxEz = Ez_ip - Ez, dxEy = Ey_ip - Ey, dyEx = Ex_jp - Ex;
-    float cu[3] = {dyEz - dzEy, dzEx - dxEz, dxEy - dyEx};
-
-    const int idx3[3] = {i, j, k};
-#pragma unroll
-    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
-        if (s >= a.n_slab) break;
-        const DSlab& sl = a.slab[s];
-        const int l = idx3[sl.axis] - sl.lo;
-        if ((unsigned)l >= (unsigned)sl.L) continue;
-        float d1, d2;
-        if (sl.axis == 0) { d1 = dxEz; d2 = dxEy; }
-        else if (sl.axis == 1) { d1 = dyEx; d2 = dyEz; }
-        else { d1 = dzEy; d2 = dzEx; }
-        const float* co = sl.coef + 3 * sl.L;
+        const float d1 = sl.axis == 0 ? d[3] : (sl.axis == 1 ? d[5] : d[1]);
+        const float d2 = sl.axis == 0 ? d[4] : (sl.axis == 1 ? d[0] : d[2]);
+        const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
         const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
         const long long p = ((long long)(i - (sl.axis == 0 ? sl.lo : 0)) * sl.sy + (j - (sl.axis == 1 ? sl.lo : 0))) * sl.sz +
                             (k - (sl.axis == 2 ? sl.lo : 0));
@@ -150,31 +46,206 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
             c1 = ikm1 * d1 + p1;
             c2 = ikm1 * d2 + p2;
         }
-        const int ci = (sl.axis + 1) % 3, cj = (sl.axis + 2) % 3;
-        cu[ci] -= c1;
-        cu[cj] += c2;
+        if (sl.axis == 0) { cu[1] -= c1; cu[2] += c2; }
+        else if (sl.axis == 1) { cu[2] -= c1; cu[0] += c2; }
+        else { cu[0] -= c1; cu[1] += c2; }
+    }
+}
+
+// Neighbour on one axis with the halo rule (wrap on a periodic axis, else zero).
+__device__ __forceinline__ float nb(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp, int i,
+                                    int j, int k) {
+    return inside ? __ldg(f + off) : ld_halo(g, f, comp, i, j, k);
+}
+
+// ---------------------------------------------------------------------------------
+// E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
+// reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
+// The block covers 32 z x 8 y columns and marches over `chunk` x planes; H(i-1) of
+// the column stays in registers, y/z neighbours come through L1.
+// ---------------------------------------------------------------------------------
+template <bool REV>
+__global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
+    const Geo& g = a.g;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.ny || k >= g.nz) return;
+    const int i0 = blockIdx.z * a.chunk;
+    const int i1 = min(i0 + a.chunk, g.nx);
+    const long long N = g.N;
+    const long long sy = g.nz;
+    const float* __restrict__ H = a.F;
+    float Hy_m = ld_halo(g, H, 1, i0 - 1, j, k);
+    float Hz_m = ld_halo(g, H, 2, i0 - 1, j, k);
+    for (int i = i0; i < i1; ++i) {
+        const long long c = cell_index(g, i, j, k);
+        const float Hx = __ldg(H + c), Hy = __ldg(H + N + c), Hz = __ldg(H + 2 * N + c);
+        const float Hz_jm = nb(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k);
+        const float Hx_jm = nb(g, H, c - sy, j > 0, 0, i, j - 1, k);
+        const float Hy_km = nb(g, H, N + c - 1, k > 0, 1, i, j, k - 1);
+        const float Hx_km = nb(g, H, c - 1, k > 0, 0, i, j, k - 1);
+        const float d[6] = {Hz - Hz_jm, Hy - Hy_km, Hx - Hx_km, Hz - Hz_m, Hy - Hy_m, Hx - Hx_jm};
+        Hy_m = Hy;
+        Hz_m = Hz;
+        float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+        cpml_correct<REV, false>(a, i, j, k, d, cu);
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            const long long o = comp * N + c;
+            float e;
+            if (face_zero(g, g.pec, comp, i, j, k)) {
+                e = 0.f;
+            } else {
+                const float ie = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
+                const float e0 = a.Uin[o];
+                if (a.sig) {
+                    const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
+                    const float q = g.c * sg * g.eta0 * ie / 2.f;
+                    if (!REV) e = ((1.f - q) * e0 + g.c * cu[comp] * ie) / (1.f + q);
+                    else e = (e0 * (1.f + q) - g.c * cu[comp] * ie) / (1.f - q);
+                } else {
+                    if (!REV) e = e0 + g.c * cu[comp] * ie;
+                    else e = e0 - g.c * cu[comp] * ie;
+                }
+            }
+            a.Uout[o] = e;
+        }
+    }
+}
+
+// Accumulates the fused E-only detectors at cell (i, j, k) from the E values the H
+// half-step already holds.  Co-location at (i, j, k+1/2) (fdtdx/core/physics/curl.py:120-158):
+// Ex <- (avg_x(Ex)(k) + avg_x(Ex)(k+1)) / 2, Ey <- (avg_y(Ey)(k) + avg_y(Ey)(k+1)) / 2, Ez.
+__device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot[kMaxFuse],
+                                                const float2 w[kMaxFuse][kMaxFuseFreq], int i, int j, int k,
+                                                float Ex, float Ex_kp, float Ex_im, float Exkp_im, float Ey, float Ey_kp,
+                                                float Ez) {
+    const Geo& g = a.g;
+#pragma unroll
+    for (int q = 0; q < kMaxFuse; ++q) {
+        if (q >= a.n_fuse) break;
+        if (slot[q] < 0) continue;
+        const DFuse& d = a.fuse[q];
+        if (i < d.lo[0] || i >= d.hi[0] || j < d.lo[1] || j >= d.hi[1] || k < d.lo[2] || k >= d.hi[2]) continue;
+        float v[3];
+        if (d.exact) {
+            if (d.mask & 1) v[0] = (0.5f * (Ex + Ex_im) + 0.5f * (Ex_kp + Exkp_im)) / 2.f;
+            if (d.mask & 2) {
+                const float Ey_jm = ld_halo(g, a.F, 1, i, j - 1, k);
+                const float Eykp_jm = ld_halo(g, a.F, 1, i, j - 1, k + 1);
+                v[1] = (0.5f * (Ey + Ey_jm) + 0.5f * (Ey_kp + Eykp_jm)) / 2.f;
+            }
+            v[2] = Ez;
+        } else {
+            v[0] = Ex;
+            v[1] = Ey;
+            v[2] = Ez;
+        }
+        const long long r = ((long long)(i - d.lo[0]) * d.ry + (j - d.lo[1])) * d.rz + (k - d.lo[2]);
+        int o = 0;
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            if (!(d.mask >> comp & 1)) continue;
+            if (d.kind == FDTD_DET_PHASOR) {
+                float2* st = reinterpret_cast<float2*>(d.state);
+#pragma unroll
+                for (int f = 0; f < kMaxFuseFreq; ++f) {
+                    if (f >= d.nfreq) break;
+                    float2* pp = st + ((long long)f * d.nout + o) * d.R + r;
+                    float2 z = *pp;
+                    if (d.inverse) { z.x -= v[comp] * w[q][f].x; z.y -= v[comp] * w[q][f].y; }
+                    else { z.x += v[comp] * w[q][f].x; z.y += v[comp] * w[q][f].y; }
+                    *pp = z;
+                }
+            } else {
+                float* st = reinterpret_cast<float*>(d.state);
+                st[((long long)slot[q] * d.nout + o) * d.R + r] = v[comp];
+            }
+            ++o;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// H half-step: H <- (g H - c curl_E(E) inv_mu) / e  (fdtdx/fdtd/update.py:717-750)
+// reverse:     H <- (H (1+q) + c curl_E(E) inv_mu) / (1-q)  (update.py:905-930)
+// Marches along +x keeping E(i+1) (next iteration's E(i)) and E(i-1) in registers;
+// fused E-only detectors are accumulated in the same pass (forward only).
+// ---------------------------------------------------------------------------------
+template <bool REV>
+__global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
+    const Geo& g = a.g;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.ny || k >= g.nz) return;
+    const int i0 = blockIdx.z * a.chunk;
+    const int i1 = min(i0 + a.chunk, g.nx);
+    const long long N = g.N;
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const float* __restrict__ E = a.F;
+
+    int slot[kMaxFuse];
+    float2 w[kMaxFuse][kMaxFuseFreq];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < kMaxFuse; ++q) {
+        slot[q] = -1;
+        if (REV || q >= a.n_fuse) continue;
+        const int t = *a.tp;
+        slot[q] = __ldg(a.fuse[q].slot + t + 1);
+        any |= slot[q] >= 0;
+#pragma unroll
+        for (int f = 0; f < kMaxFuseFreq; ++f)
+            w[q][f] = (slot[q] >= 0 && f < a.fuse[q].nfreq && a.fuse[q].kind == FDTD_DET_PHASOR)
+                          ? __ldg(a.fuse[q].w + (long long)(t + 1) * a.fuse[q].nfreq + f)
+                          : make_float2(0.f, 0.f);
     }
 
+    const long long c0 = cell_index(g, i0, j, k);
+    float Ey = __ldg(E + N + c0), Ez = __ldg(E + 2 * N + c0);
+    float Ex_im = 0.f, Exkp_im = 0.f;
+    if (any) {
+        Ex_im = ld_halo(g, E, 0, i0 - 1, j, k);
+        Exkp_im = ld_halo(g, E, 0, i0 - 1, j, k + 1);
+    }
+    for (int i = i0; i < i1; ++i) {
+        const long long c = cell_index(g, i, j, k);
+        const float Ex = __ldg(E + c);
+        const float Ey_ip = nb(g, E, N + c + sx, i < g.nx - 1, 1, i + 1, j, k);
+        const float Ez_ip = nb(g, E, 2 * N + c + sx, i < g.nx - 1, 2, i + 1, j, k);
+        const float Ez_jp = nb(g, E, 2 * N + c + sy, j < g.ny - 1, 2, i, j + 1, k);
+        const float Ex_jp = nb(g, E, c + sy, j < g.ny - 1, 0, i, j + 1, k);
+        const float Ey_kp = nb(g, E, N + c + 1, k < g.nz - 1, 1, i, j, k + 1);
+        const float Ex_kp = nb(g, E, c + 1, k < g.nz - 1, 0, i, j, k + 1);
+        const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
+        float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+        cpml_correct<REV, true>(a, i, j, k, d, cu);
 #pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-        const long long o = comp * N + c;
-        float h;
-        if (face_zero(g, g.pmc, comp, i, j, k)) {
-            h = 0.f;
-        } else {
-            const float im = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
-            const float h0 = a.Uin[o];
-            if (a.sig) {
-                const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
-                const float q = g.c * sg / g.eta0 * im / 2.f;
-                if (!REV) h = ((1.f - q) * h0 - g.c * cu[comp] * im) / (1.f + q);
-                else h = (h0 * (1.f + q) + g.c * cu[comp] * im) / (1.f - q);
+        for (int comp = 0; comp < 3; ++comp) {
+            const long long o = comp * N + c;
+            float h;
+            if (face_zero(g, g.pmc, comp, i, j, k)) {
+                h = 0.f;
             } else {
-                if (!REV) h = h0 - g.c * cu[comp] * im;
-                else h = h0 + g.c * cu[comp] * im;
+                const float im = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
+                const float h0 = a.Uin[o];
+                if (a.sig) {
+                    const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
+                    const float q = g.c * sg / g.eta0 * im / 2.f;
+                    if (!REV) h = ((1.f - q) * h0 - g.c * cu[comp] * im) / (1.f + q);
+                    else h = (h0 * (1.f + q) + g.c * cu[comp] * im) / (1.f - q);
+                } else {
+                    if (!REV) h = h0 - g.c * cu[comp] * im;
+                    else h = h0 + g.c * cu[comp] * im;
+                }
             }
+            a.Uout[o] = h;
         }
-        a.Uout[o] = h;
+        if (!REV && any) fused_detectors(a, slot, w, i, j, k, Ex, Ex_kp, Ex_im, Exkp_im, Ey, Ey_kp, Ez);
+        Ex_im = Ex;
+        Exkp_im = Ex_kp;
+        Ey = Ey_ip;
+        Ez = Ez_ip;
     }
 }
 

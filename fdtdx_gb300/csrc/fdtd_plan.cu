@@ -27,6 +27,10 @@ struct FdtdPlan {
     int* d_t = nullptr;          // device time-step counter read by every kernel
     float* h_twin = nullptr;     // second H buffer (ping-pong) when a detector needs H before the H update
     bool need_hprev = false;
+    bool fused[FDTD_MAX_DETECTORS] = {};  // accumulated inside the H half-step
+    int n_fused = 0;
+    int chunk = 1;                        // x planes per update block
+    int sm_count = 1;
     // graph cache for the forward loop
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -80,6 +84,23 @@ bool det_needs_h(const FdtdDetectorDesc& dd) {
     if (!dd.exact_interpolation) return false;  // non-exact detectors read H after the update only
     if (dd.kind == FDTD_DET_FLUX || dd.kind == FDTD_DET_ENERGY) return true;
     return (dd.comp_mask & 56) != 0;
+}
+
+// E-only phasor / field detectors without volume reduction are accumulated by the
+// H half-step itself (all their inputs are final E values held in registers there).
+bool det_fusable(const FdtdDetectorDesc& dd) {
+    if (dd.kind != FDTD_DET_PHASOR && dd.kind != FDTD_DET_FIELD) return false;
+    if ((dd.comp_mask & ~7) != 0 || dd.reduce_volume) return false;
+    if (dd.kind == FDTD_DET_PHASOR && dd.n_freq > kMaxFuseFreq) return false;
+    return true;
+}
+
+int default_chunk(int nx, int ny, int nz, int sms) {
+    const long long cols = (long long)((nz + 31) / 32) * ((ny + 7) / 8);
+    const long long target = (long long)sms * 24;  // ~3 waves of 8 resident 256-thread blocks per SM
+    long long nchunks = (target + cols - 1) / cols;
+    nchunks = std::max(1ll, std::min<long long>(nx, nchunks));
+    return (int)((nx + nchunks - 1) / nchunks);
 }
 
 int validate(const FdtdDesc* d, std::string& why) {
@@ -165,6 +186,12 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     p->g.c = d.courant;
     p->g.eta0 = (float)(4e-7 * M_PI * 299792458.0);
     p->g.pec = d.pec_faces; p->g.pmc = d.pmc_faces;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) p->sm_count = 152;
+        p->chunk = default_chunk(d.nx, d.ny, d.nz, p->sm_count);
+    }
 
     // ---- lay out the device arena
     Arena ar;
@@ -195,7 +222,12 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         const long long nb = (R + kDetBlock - 1) / kDetBlock;
         const bool red = dd.reduce_volume || dd.kind == FDTD_DET_PHASOR ? dd.reduce_volume : dd.reduce_volume;
         o.partial = red ? ar.take(4 * (size_t)nb * det_ncomp(dd)) : 0;
-        if (det_needs_h(dd)) p->need_hprev = true;
+        if (det_fusable(dd) && p->n_fused < kMaxFuse) {
+            p->fused[q] = true;
+            ++p->n_fused;
+        } else if (det_needs_h(dd)) {
+            p->need_hprev = true;
+        }
     }
     size_t o_twin = 0;
     if (p->need_hprev) o_twin = ar.take(sizeof(float) * 3 * (size_t)p->g.N);
@@ -334,7 +366,10 @@ int64_t fdtd_plan_device_bytes(const FdtdPlan* p) { return p ? (int64_t)p->dmem_
 // -------------------------------------------------------------------------------------
 namespace {
 
-dim3 update_grid(const Geo& g) { return dim3((g.nz + 31) / 32, (g.ny + 7) / 8, g.nx); }
+dim3 update_grid(const FdtdPlan* p) {
+    const Geo& g = p->g;
+    return dim3((g.nz + 31) / 32, (g.ny + 7) / 8, (g.nx + p->chunk - 1) / p->chunk);
+}
 const dim3 kUpdBlock(32, 8, 1);
 
 UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout) {
@@ -355,6 +390,25 @@ UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const floa
         a.slab[s] = p->slab[s];
         a.psi1[s] = eside ? b->psi_E[s][0] : b->psi_H[s][0];
         a.psi2[s] = eside ? b->psi_E[s][1] : b->psi_H[s][1];
+    }
+    a.chunk = p->chunk;
+    a.tp = p->d_t;
+    a.n_fuse = 0;
+    return a;
+}
+
+// The forward H step also accumulates the fused detectors.
+UpdArgs make_upd_fwd_H(const FdtdPlan* p, const FdtdBuffers* b, const float* Hin, float* Hout) {
+    UpdArgs a = make_upd(p, b, false, b->E, Hin, Hout);
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (!p->fused[q]) continue;
+        const DDet& dd = p->det[q];
+        DFuse& f = a.fuse[a.n_fuse++];
+        f.kind = dd.kind; f.exact = dd.exact; f.mask = dd.comp_mask; f.nout = dd.ncomp; f.nfreq = dd.nfreq;
+        f.inverse = dd.inverse;
+        for (int x = 0; x < 3; ++x) { f.lo[x] = dd.lo[x]; f.hi[x] = dd.hi[x]; }
+        f.rx = dd.rx; f.ry = dd.ry; f.rz = dd.rz; f.R = dd.R;
+        f.slot = dd.slot; f.w = dd.w; f.state = b->det_state[q];
     }
     return a;
 }
@@ -403,15 +457,16 @@ void interfaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t 
 // One forward step (fdtdx/fdtd/forward.py:83-156): update_E, E sources (+PEC inside the
 // update), update_H, H sources (+PMC), interface recording, detectors, advance t.
 void launch_forward_step(const FdtdPlan* p, const FdtdBuffers* b, float* Hcur, float* Hnext, cudaStream_t st) {
-    const dim3 grid = update_grid(p->g);
+    const dim3 grid = update_grid(p);
     k_update_E<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, Hcur, b->E, b->E));
     launch_sources(p, b, true, b->E, 0, st);
-    k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, false, b->E, Hcur, Hnext));
+    k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd_fwd_H(p, b, Hcur, Hnext));
     launch_sources(p, b, false, Hnext, 0, st);
     if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
     DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
                 p->d.inv_mu_scalar};
     for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (p->fused[q]) continue;
         const DDet& dd = p->det[q];
         k_detector<<<dd.nblocks, kDetBlock, 0, st>>>(p->g, dd, p->d_t, f, b->det_state[q]);
         if (dd.reduce) k_detector_finalize<<<1, kDetBlock, 0, st>>>(dd, p->d_t, b->det_state[q]);
@@ -440,7 +495,8 @@ int32_t fdtd_launches_per_step(const FdtdPlan* p) {
     if (!p) return 0;
     int n = 2 + sources_launched(p, true) + sources_launched(p, false) + 1;
     if (p->d.record_interfaces && p->d.n_slabs) n += 1;
-    for (int q = 0; q < p->d.n_detectors; ++q) n += p->det[q].reduce ? 2 : 1;
+    for (int q = 0; q < p->d.n_detectors; ++q)
+        if (!p->fused[q]) n += p->det[q].reduce ? 2 : 1;
     return n;
 }
 
@@ -514,7 +570,7 @@ int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_ste
         return fail(p, FDTD_EINVAL, "reverse steps out of the range covered by the plan's tables");
     if (n_steps == 0) return FDTD_OK;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const dim3 grid = update_grid(p->g);
+    const dim3 grid = update_grid(p);
     k_set_step<<<1, 1, 0, st>>>(p->d_t, t_end - 1);
     for (int s = 0; s < n_steps; ++s) {
         interfaces<true>(p, b, b->H, st);
@@ -579,20 +635,21 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
     float* Hcur = b->H;
     float* Hnext = p->need_hprev ? p->h_twin : b->H;
-    const dim3 grid = update_grid(p->g);
+    const dim3 grid = update_grid(p);
     for (int s = 0; s < n_steps; ++s) {
         cudaEventRecord(ev[0], st);
         k_update_E<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, Hcur, b->E, b->E));
         cudaEventRecord(ev[1], st);
         launch_sources(p, b, true, b->E, 0, st);
         cudaEventRecord(ev[2], st);
-        k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, false, b->E, Hcur, Hnext));
+        k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd_fwd_H(p, b, Hcur, Hnext));
         cudaEventRecord(ev[3], st);
         launch_sources(p, b, false, Hnext, 0, st);
         cudaEventRecord(ev[4], st);
         DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
                     p->d.inv_mu_scalar};
         for (int q = 0; q < p->d.n_detectors; ++q) {
+            if (p->fused[q]) continue;
             const DDet& dd = p->det[q];
             k_detector<<<dd.nblocks, kDetBlock, 0, st>>>(p->g, dd, p->d_t, f, b->det_state[q]);
             if (dd.reduce) k_detector_finalize<<<1, kDetBlock, 0, st>>>(dd, p->d_t, b->det_state[q]);
@@ -621,3 +678,18 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_profile_forward");
     return FDTD_OK;
 }
+
+extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk) {
+    if (!p) return FDTD_EINVAL;
+    if (chunk <= 0) chunk = default_chunk(p->g.nx, p->g.ny, p->g.nz, p->sm_count);
+    if (chunk > p->g.nx) chunk = p->g.nx;
+    if (chunk != p->chunk) {
+        p->chunk = chunk;
+        if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+        if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+        p->gsteps = 0;
+    }
+    return FDTD_OK;
+}
+
+extern "C" int32_t fdtd_plan_chunk(const FdtdPlan* p) { return p ? p->chunk : 0; }

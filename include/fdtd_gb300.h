@@ -191,6 +191,11 @@ int fdtd_reverse(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t_end, int32_t
  * gradients are accumulated. */
 int fdtd_adjoint_step(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t, void* stream);
 
+/* Tuning: x planes each update block marches over (0 restores the default).
+ * Invalidates a cached CUDA graph.  fdtd_plan_chunk returns the current value. */
+int fdtd_plan_tune(FdtdPlan* plan, int32_t chunk);
+int32_t fdtd_plan_chunk(const FdtdPlan* plan);
+
 /* Number of launches of this library's kernels one forward step issues. */
 int32_t fdtd_launches_per_step(const FdtdPlan* plan);
 
