@@ -138,8 +138,8 @@ def run_gpu(args):
     objects, arrays, _, cfg, _ = scenes.coupler(shape=shape, steps=T_TOTAL, device=dev)
     arrays = arrays.reset()
     scene = get_scene(objects, arrays, cfg)
-    if args.chunk:
-        NATIVE.check(NATIVE.load().fdtd_plan_tune(scene.plan, args.chunk), scene.plan, "fdtd_plan_tune")
+    if args.chunk or args.vec:
+        NATIVE.check(NATIVE.load().fdtd_plan_tune(scene.plan, args.chunk, args.vec), scene.plan, "fdtd_plan_tune")
     ncell = shape[0] * shape[1] * shape[2]
     W, K = args.warmup, args.steps
     if W + K + 8 > T_TOTAL:
@@ -232,6 +232,7 @@ def run_gpu(args):
             "l2": "inputs larger than L2 (fields 384 MB, phasor 768 MB)",
             "parallelism": f"replicas x{ws}",
             "chunk": int(NATIVE.load().fdtd_plan_chunk(scene.plan)),
+            "vec": int(NATIVE.load().fdtd_plan_vec(scene.plan)),
             "hbm_gbs_effective": round(sum(alg.values()) / (ms / K / 1e3) / 1e9, 1),
         },
         "roofline": {
@@ -337,6 +338,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--shape", default="", help="grid override nx,ny,nz (profiling cases)")
     ap.add_argument("--chunk", type=int, default=0, help="x planes per update block (0: plan default)")
+    ap.add_argument("--vec", type=int, default=0, help="z cells per thread (0: plan default)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("warmup must be >= 3")

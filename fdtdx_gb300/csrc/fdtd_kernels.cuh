@@ -58,58 +58,170 @@ __device__ __forceinline__ float nb(const Geo& g, const float* __restrict__ f, l
     return inside ? __ldg(f + off) : ld_halo(g, f, comp, i, j, k);
 }
 
+// VEC consecutive z values (16/8/4-byte aligned: nz is a multiple of VEC).
+template <int VEC>
+struct Vec {
+    float v[VEC];
+};
+
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> ldv(const float* __restrict__ p) {
+    Vec<VEC> r;
+    if constexpr (VEC == 4) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+    } else if constexpr (VEC == 2) {
+        const float2 q = __ldg(reinterpret_cast<const float2*>(p));
+        r.v[0] = q.x; r.v[1] = q.y;
+    } else {
+        r.v[0] = __ldg(p);
+    }
+    return r;
+}
+
+// Plain (coherent) load of a field this kernel also writes at the same cells.
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> ldv_rw(const float* p) {
+    Vec<VEC> r;
+    if constexpr (VEC == 4) {
+        const float4 q = *reinterpret_cast<const float4*>(p);
+        r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+    } else if constexpr (VEC == 2) {
+        const float2 q = *reinterpret_cast<const float2*>(p);
+        r.v[0] = q.x; r.v[1] = q.y;
+    } else {
+        r.v[0] = *p;
+    }
+    return r;
+}
+
+template <int VEC>
+__device__ __forceinline__ void stv(float* p, const Vec<VEC>& r) {
+    if constexpr (VEC == 4) *reinterpret_cast<float4*>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+    else if constexpr (VEC == 2) *reinterpret_cast<float2*>(p) = make_float2(r.v[0], r.v[1]);
+    else *p = r.v[0];
+}
+
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> ldv_halo(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k0) {
+    Vec<VEC> r;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r.v[e] = ld_halo(g, f, comp, i, j, k0 + e);
+    return r;
+}
+
+// A neighbour vector one cell away along x or y (all VEC cells share the halo test).
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> nbv(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp,
+                                        int i, int j, int k0) {
+    return inside ? ldv<VEC>(f + off) : ldv_halo<VEC>(g, f, comp, i, j, k0);
+}
+
+// Whether (i, j, k0 .. k0+VEC-1) can lie in any CPML slab.
+__device__ __forceinline__ bool maybe_slab(const UpdArgs& a, int i, int j, int k0, int vec) {
+    const int idx[3] = {i, j, k0};
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (s >= a.n_slab) break;
+        const DSlab& sl = a.slab[s];
+        const int lo = idx[sl.axis] - sl.lo;
+        const int hi = lo + (sl.axis == 2 ? vec - 1 : 0);
+        if (hi >= 0 && lo < sl.L) return true;
+    }
+    return false;
+}
+
+// The material update of one component of one cell.
+template <bool REV, bool HSIDE>
+__device__ __forceinline__ float material_update(const UpdArgs& a, float u0, float cu, float m, const float* sig_p,
+                                                 long long so) {
+    const Geo& g = a.g;
+    if (sig_p) {
+        const float sg = __ldg(sig_p + so);
+        const float q = HSIDE ? g.c * sg / g.eta0 * m / 2.f : g.c * sg * g.eta0 * m / 2.f;
+        if (!HSIDE) {
+            if (!REV) return ((1.f - q) * u0 + g.c * cu * m) / (1.f + q);
+            return (u0 * (1.f + q) - g.c * cu * m) / (1.f - q);
+        }
+        if (!REV) return ((1.f - q) * u0 - g.c * cu * m) / (1.f + q);
+        return (u0 * (1.f + q) + g.c * cu * m) / (1.f - q);
+    }
+    if (!HSIDE) return REV ? u0 - g.c * cu * m : u0 + g.c * cu * m;
+    return REV ? u0 + g.c * cu * m : u0 - g.c * cu * m;
+}
+
+// Column decomposition shared by both half-steps: a thread owns VEC consecutive z cells
+// of one (j) row and marches over the block's `chunk` x planes.
+template <int VEC>
+__device__ __forceinline__ bool column_of(const Geo& g, int& j, int& k0) {
+    const int nq = g.nz / VEC;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)g.ny * nq) return false;
+    j = (int)(q / nq);
+    k0 = (int)(q - (long long)j * nq) * VEC;
+    return true;
+}
+
 // ---------------------------------------------------------------------------------
 // E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
 // reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
-// The block covers 32 z x 8 y columns and marches over `chunk` x planes; H(i-1) of
-// the column stays in registers, y/z neighbours come through L1.
 // ---------------------------------------------------------------------------------
-template <bool REV>
+template <bool REV, int VEC>
 __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
     const Geo& g = a.g;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (j >= g.ny || k >= g.nz) return;
-    const int i0 = blockIdx.z * a.chunk;
+    int j, k0;
+    if (!column_of<VEC>(g, j, k0)) return;
+    const int i0 = blockIdx.y * a.chunk;
     const int i1 = min(i0 + a.chunk, g.nx);
     const long long N = g.N;
     const long long sy = g.nz;
     const float* __restrict__ H = a.F;
-    float Hy_m = ld_halo(g, H, 1, i0 - 1, j, k);
-    float Hz_m = ld_halo(g, H, 2, i0 - 1, j, k);
+    Vec<VEC> Hy_m = ldv_halo<VEC>(g, H, 1, i0 - 1, j, k0);
+    Vec<VEC> Hz_m = ldv_halo<VEC>(g, H, 2, i0 - 1, j, k0);
     for (int i = i0; i < i1; ++i) {
-        const long long c = cell_index(g, i, j, k);
-        const float Hx = __ldg(H + c), Hy = __ldg(H + N + c), Hz = __ldg(H + 2 * N + c);
-        const float Hz_jm = nb(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k);
-        const float Hx_jm = nb(g, H, c - sy, j > 0, 0, i, j - 1, k);
-        const float Hy_km = nb(g, H, N + c - 1, k > 0, 1, i, j, k - 1);
-        const float Hx_km = nb(g, H, c - 1, k > 0, 0, i, j, k - 1);
-        const float d[6] = {Hz - Hz_jm, Hy - Hy_km, Hx - Hx_km, Hz - Hz_m, Hy - Hy_m, Hx - Hx_jm};
+        const long long c = cell_index(g, i, j, k0);
+        const Vec<VEC> Hx = ldv<VEC>(H + c), Hy = ldv<VEC>(H + N + c), Hz = ldv<VEC>(H + 2 * N + c);
+        const Vec<VEC> Hz_jm = nbv<VEC>(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k0);
+        const Vec<VEC> Hx_jm = nbv<VEC>(g, H, c - sy, j > 0, 0, i, j - 1, k0);
+        const float Hy_k = nb(g, H, N + c - 1, k0 > 0, 1, i, j, k0 - 1);   // z neighbour below the vector
+        const float Hx_k = nb(g, H, c - 1, k0 > 0, 0, i, j, k0 - 1);
+        Vec<VEC> ie[3];
+        if (a.mat) {
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp)
+                if (comp == 0 || a.n_mat == 3) ie[comp] = ldv<VEC>(a.mat + (a.n_mat == 3 ? comp * N : 0) + c);
+            if (a.n_mat != 3) { ie[1] = ie[0]; ie[2] = ie[0]; }
+        } else {
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp)
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) ie[comp].v[e] = a.mat_scalar;
+        }
+        Vec<VEC> Eo[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) Eo[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
+        const bool pml = a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int k = k0 + e;
+            const float hy_km = e == 0 ? Hy_k : Hy.v[e - 1];
+            const float hx_km = e == 0 ? Hx_k : Hx.v[e - 1];
+            const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
+                                Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
+            float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+            if (pml) cpml_correct<REV, false>(a, i, j, k, d, cu);
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp) {
+                const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
+                float u = material_update<REV, false>(a, Eo[comp].v[e], cu[comp], ie[comp].v[e], sp, c + e);
+                if (g.pec && face_zero(g, g.pec, comp, i, j, k)) u = 0.f;
+                Eo[comp].v[e] = u;
+            }
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) stv<VEC>(a.Uout + comp * N + c, Eo[comp]);
         Hy_m = Hy;
         Hz_m = Hz;
-        float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-        cpml_correct<REV, false>(a, i, j, k, d, cu);
-#pragma unroll
-        for (int comp = 0; comp < 3; ++comp) {
-            const long long o = comp * N + c;
-            float e;
-            if (face_zero(g, g.pec, comp, i, j, k)) {
-                e = 0.f;
-            } else {
-                const float ie = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
-                const float e0 = a.Uin[o];
-                if (a.sig) {
-                    const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
-                    const float q = g.c * sg * g.eta0 * ie / 2.f;
-                    if (!REV) e = ((1.f - q) * e0 + g.c * cu[comp] * ie) / (1.f + q);
-                    else e = (e0 * (1.f + q) - g.c * cu[comp] * ie) / (1.f - q);
-                } else {
-                    if (!REV) e = e0 + g.c * cu[comp] * ie;
-                    else e = e0 - g.c * cu[comp] * ie;
-                }
-            }
-            a.Uout[o] = e;
-        }
     }
 }
 
@@ -119,8 +231,7 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
 __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot[kMaxFuse],
                                                 const float2 w[kMaxFuse][kMaxFuseFreq], int i, int j, int k,
                                                 float Ex, float Ex_kp, float Ex_im, float Exkp_im, float Ey, float Ey_kp,
-                                                float Ez) {
-    const Geo& g = a.g;
+                                                float Ey_jm, float Eykp_jm, float Ez) {
 #pragma unroll
     for (int q = 0; q < kMaxFuse; ++q) {
         if (q >= a.n_fuse) break;
@@ -129,12 +240,8 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
         if (i < d.lo[0] || i >= d.hi[0] || j < d.lo[1] || j >= d.hi[1] || k < d.lo[2] || k >= d.hi[2]) continue;
         float v[3];
         if (d.exact) {
-            if (d.mask & 1) v[0] = (0.5f * (Ex + Ex_im) + 0.5f * (Ex_kp + Exkp_im)) / 2.f;
-            if (d.mask & 2) {
-                const float Ey_jm = ld_halo(g, a.F, 1, i, j - 1, k);
-                const float Eykp_jm = ld_halo(g, a.F, 1, i, j - 1, k + 1);
-                v[1] = (0.5f * (Ey + Ey_jm) + 0.5f * (Ey_kp + Eykp_jm)) / 2.f;
-            }
+            v[0] = (0.5f * (Ex + Ex_im) + 0.5f * (Ex_kp + Exkp_im)) / 2.f;
+            v[1] = (0.5f * (Ey + Ey_jm) + 0.5f * (Ey_kp + Eykp_jm)) / 2.f;
             v[2] = Ez;
         } else {
             v[0] = Ex;
@@ -169,20 +276,20 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
 // ---------------------------------------------------------------------------------
 // H half-step: H <- (g H - c curl_E(E) inv_mu) / e  (fdtdx/fdtd/update.py:717-750)
 // reverse:     H <- (H (1+q) + c curl_E(E) inv_mu) / (1-q)  (update.py:905-930)
-// Marches along +x keeping E(i+1) (next iteration's E(i)) and E(i-1) in registers;
+// Marches along +x keeping E(i+1) (the next iteration's E(i)) and Ex(i-1) in registers;
 // fused E-only detectors are accumulated in the same pass (forward only).
 // ---------------------------------------------------------------------------------
-template <bool REV>
+template <bool REV, int VEC>
 __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
     const Geo& g = a.g;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (j >= g.ny || k >= g.nz) return;
-    const int i0 = blockIdx.z * a.chunk;
+    int j, k0;
+    if (!column_of<VEC>(g, j, k0)) return;
+    const int i0 = blockIdx.y * a.chunk;
     const int i1 = min(i0 + a.chunk, g.nx);
     const long long N = g.N;
     const long long sy = g.nz, sx = (long long)g.ny * g.nz;
     const float* __restrict__ E = a.F;
+    const bool kin = k0 + VEC < g.nz;
 
     int slot[kMaxFuse];
     float2 w[kMaxFuse][kMaxFuseFreq];
@@ -201,49 +308,72 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
                           : make_float2(0.f, 0.f);
     }
 
-    const long long c0 = cell_index(g, i0, j, k);
-    float Ey = __ldg(E + N + c0), Ez = __ldg(E + 2 * N + c0);
-    float Ex_im = 0.f, Exkp_im = 0.f;
+    const long long c0 = cell_index(g, i0, j, k0);
+    Vec<VEC> Ey = ldv<VEC>(E + N + c0), Ez = ldv<VEC>(E + 2 * N + c0);
+    Vec<VEC> Ex_im{};
+    float Exk_im = 0.f;
     if (any) {
-        Ex_im = ld_halo(g, E, 0, i0 - 1, j, k);
-        Exkp_im = ld_halo(g, E, 0, i0 - 1, j, k + 1);
+        Ex_im = ldv_halo<VEC>(g, E, 0, i0 - 1, j, k0);
+        Exk_im = ld_halo(g, E, 0, i0 - 1, j, k0 + VEC);
     }
     for (int i = i0; i < i1; ++i) {
-        const long long c = cell_index(g, i, j, k);
-        const float Ex = __ldg(E + c);
-        const float Ey_ip = nb(g, E, N + c + sx, i < g.nx - 1, 1, i + 1, j, k);
-        const float Ez_ip = nb(g, E, 2 * N + c + sx, i < g.nx - 1, 2, i + 1, j, k);
-        const float Ez_jp = nb(g, E, 2 * N + c + sy, j < g.ny - 1, 2, i, j + 1, k);
-        const float Ex_jp = nb(g, E, c + sy, j < g.ny - 1, 0, i, j + 1, k);
-        const float Ey_kp = nb(g, E, N + c + 1, k < g.nz - 1, 1, i, j, k + 1);
-        const float Ex_kp = nb(g, E, c + 1, k < g.nz - 1, 0, i, j, k + 1);
-        const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
-        float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-        cpml_correct<REV, true>(a, i, j, k, d, cu);
+        const long long c = cell_index(g, i, j, k0);
+        const Vec<VEC> Ex = ldv<VEC>(E + c);
+        const Vec<VEC> Ey_ip = nbv<VEC>(g, E, N + c + sx, i < g.nx - 1, 1, i + 1, j, k0);
+        const Vec<VEC> Ez_ip = nbv<VEC>(g, E, 2 * N + c + sx, i < g.nx - 1, 2, i + 1, j, k0);
+        const Vec<VEC> Ez_jp = nbv<VEC>(g, E, 2 * N + c + sy, j < g.ny - 1, 2, i, j + 1, k0);
+        const Vec<VEC> Ex_jp = nbv<VEC>(g, E, c + sy, j < g.ny - 1, 0, i, j + 1, k0);
+        const float Ey_k = nb(g, E, N + c + VEC, kin, 1, i, j, k0 + VEC);  // z neighbour above the vector
+        const float Ex_k = nb(g, E, c + VEC, kin, 0, i, j, k0 + VEC);
+        Vec<VEC> im[3];
+        if (a.mat) {
 #pragma unroll
-        for (int comp = 0; comp < 3; ++comp) {
-            const long long o = comp * N + c;
-            float h;
-            if (face_zero(g, g.pmc, comp, i, j, k)) {
-                h = 0.f;
-            } else {
-                const float im = a.mat ? __ldg(a.mat + (a.n_mat == 3 ? comp * N : 0) + c) : a.mat_scalar;
-                const float h0 = a.Uin[o];
-                if (a.sig) {
-                    const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
-                    const float q = g.c * sg / g.eta0 * im / 2.f;
-                    if (!REV) h = ((1.f - q) * h0 - g.c * cu[comp] * im) / (1.f + q);
-                    else h = (h0 * (1.f + q) + g.c * cu[comp] * im) / (1.f - q);
-                } else {
-                    if (!REV) h = h0 - g.c * cu[comp] * im;
-                    else h = h0 + g.c * cu[comp] * im;
-                }
-            }
-            a.Uout[o] = h;
+            for (int comp = 0; comp < 3; ++comp)
+                if (comp == 0 || a.n_mat == 3) im[comp] = ldv<VEC>(a.mat + (a.n_mat == 3 ? comp * N : 0) + c);
+            if (a.n_mat != 3) { im[1] = im[0]; im[2] = im[0]; }
+        } else {
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp)
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) im[comp].v[e] = a.mat_scalar;
         }
-        if (!REV && any) fused_detectors(a, slot, w, i, j, k, Ex, Ex_kp, Ex_im, Exkp_im, Ey, Ey_kp, Ez);
+        Vec<VEC> Ho[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) Ho[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
+        const bool pml = a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        Vec<VEC> Ey_jm{};
+        float Eyk_jm = 0.f;
+        if (!REV && any) {
+            Ey_jm = nbv<VEC>(g, E, N + c - sy, j > 0, 1, i, j - 1, k0);
+            Eyk_jm = ld_halo(g, E, 1, i, j - 1, k0 + VEC);
+        }
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int k = k0 + e;
+            const float ey_kp = e + 1 < VEC ? Ey.v[e + 1] : Ey_k;
+            const float ex_kp = e + 1 < VEC ? Ex.v[e + 1] : Ex_k;
+            const float d[6] = {Ez_jp.v[e] - Ez.v[e], ey_kp - Ey.v[e], ex_kp - Ex.v[e],
+                                Ez_ip.v[e] - Ez.v[e], Ey_ip.v[e] - Ey.v[e], Ex_jp.v[e] - Ex.v[e]};
+            float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+            if (pml) cpml_correct<REV, true>(a, i, j, k, d, cu);
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp) {
+                const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
+                float u = material_update<REV, true>(a, Ho[comp].v[e], cu[comp], im[comp].v[e], sp, c + e);
+                if (g.pmc && face_zero(g, g.pmc, comp, i, j, k)) u = 0.f;
+                Ho[comp].v[e] = u;
+            }
+            if (!REV && any) {
+                const float exkp_im = e + 1 < VEC ? Ex_im.v[e + 1] : Exk_im;
+                const float eykp_jm = e + 1 < VEC ? Ey_jm.v[e + 1] : Eyk_jm;
+                fused_detectors(a, slot, w, i, j, k, Ex.v[e], ex_kp, Ex_im.v[e], exkp_im, Ey.v[e], ey_kp, Ey_jm.v[e],
+                                eykp_jm, Ez.v[e]);
+            }
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) stv<VEC>(a.Uout + comp * N + c, Ho[comp]);
         Ex_im = Ex;
-        Exkp_im = Ex_kp;
+        Exk_im = Ex_k;
         Ey = Ey_ip;
         Ez = Ez_ip;
     }

@@ -30,6 +30,7 @@ struct FdtdPlan {
     bool fused[FDTD_MAX_DETECTORS] = {};  // accumulated inside the H half-step
     int n_fused = 0;
     int chunk = 1;                        // x planes per update block
+    int vec = 1;                          // z cells per thread (4, 2 or 1: nz % vec == 0)
     int sm_count = 1;
     // graph cache for the forward loop
     cudaGraphExec_t gexec = nullptr;
@@ -95,8 +96,13 @@ bool det_fusable(const FdtdDetectorDesc& dd) {
     return true;
 }
 
+constexpr int kUpdThreads = 256;
+
+int pick_vec(int nz) { return nz % 4 == 0 ? 4 : (nz % 2 == 0 ? 2 : 1); }
+
 int default_chunk(int nx, int ny, int nz, int sms) {
-    const long long cols = (long long)((nz + 31) / 32) * ((ny + 7) / 8);
+    const int vec = pick_vec(nz);
+    const long long cols = ((long long)ny * (nz / vec) + kUpdThreads - 1) / kUpdThreads;
     const long long target = (long long)sms * 24;  // ~3 waves of 8 resident 256-thread blocks per SM
     long long nchunks = (target + cols - 1) / cols;
     nchunks = std::max(1ll, std::min<long long>(nx, nchunks));
@@ -191,6 +197,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) p->sm_count = 152;
         p->chunk = default_chunk(d.nx, d.ny, d.nz, p->sm_count);
+        p->vec = pick_vec(d.nz);
     }
 
     // ---- lay out the device arena
@@ -368,9 +375,26 @@ namespace {
 
 dim3 update_grid(const FdtdPlan* p) {
     const Geo& g = p->g;
-    return dim3((g.nz + 31) / 32, (g.ny + 7) / 8, (g.nx + p->chunk - 1) / p->chunk);
+    const long long cols = (long long)g.ny * (g.nz / p->vec);
+    return dim3((unsigned)((cols + kUpdThreads - 1) / kUpdThreads), (g.nx + p->chunk - 1) / p->chunk, 1);
 }
-const dim3 kUpdBlock(32, 8, 1);
+const dim3 kUpdBlock(kUpdThreads, 1, 1);
+
+template <bool REV>
+void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+    const dim3 grid = update_grid(p);
+    if (p->vec == 4) k_update_E<REV, 4><<<grid, kUpdBlock, 0, st>>>(a);
+    else if (p->vec == 2) k_update_E<REV, 2><<<grid, kUpdBlock, 0, st>>>(a);
+    else k_update_E<REV, 1><<<grid, kUpdBlock, 0, st>>>(a);
+}
+
+template <bool REV>
+void launch_H(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+    const dim3 grid = update_grid(p);
+    if (p->vec == 4) k_update_H<REV, 4><<<grid, kUpdBlock, 0, st>>>(a);
+    else if (p->vec == 2) k_update_H<REV, 2><<<grid, kUpdBlock, 0, st>>>(a);
+    else k_update_H<REV, 1><<<grid, kUpdBlock, 0, st>>>(a);
+}
 
 UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout) {
     UpdArgs a{};
@@ -457,10 +481,9 @@ void interfaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t 
 // One forward step (fdtdx/fdtd/forward.py:83-156): update_E, E sources (+PEC inside the
 // update), update_H, H sources (+PMC), interface recording, detectors, advance t.
 void launch_forward_step(const FdtdPlan* p, const FdtdBuffers* b, float* Hcur, float* Hnext, cudaStream_t st) {
-    const dim3 grid = update_grid(p);
-    k_update_E<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, Hcur, b->E, b->E));
+    launch_E<false>(p, make_upd(p, b, true, Hcur, b->E, b->E), st);
     launch_sources(p, b, true, b->E, 0, st);
-    k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd_fwd_H(p, b, Hcur, Hnext));
+    launch_H<false>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st);
     launch_sources(p, b, false, Hnext, 0, st);
     if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
     DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
@@ -484,6 +507,11 @@ int check_bufs(FdtdPlan* p, const FdtdBuffers* b) {
             return fail(p, FDTD_EINVAL, "psi buffers required for every slab");
     for (int q = 0; q < p->d.n_detectors; ++q)
         if (!b->det_state[q]) return fail(p, FDTD_EINVAL, "detector state buffer missing");
+    // the update kernels read and write `vec` consecutive floats at once
+    const uintptr_t mask = (uintptr_t)(4 * p->vec - 1);
+    const void* vecbufs[] = {b->E, b->H, b->inv_eps, b->inv_mu, b->sigma_E, b->sigma_H};
+    for (const void* q : vecbufs)
+        if (q && ((uintptr_t)q & mask)) return fail(p, FDTD_EINVAL, "field and material buffers must be 16-byte aligned");
     return FDTD_OK;
 }
 
@@ -570,14 +598,13 @@ int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_ste
         return fail(p, FDTD_EINVAL, "reverse steps out of the range covered by the plan's tables");
     if (n_steps == 0) return FDTD_OK;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const dim3 grid = update_grid(p);
     k_set_step<<<1, 1, 0, st>>>(p->d_t, t_end - 1);
     for (int s = 0; s < n_steps; ++s) {
         interfaces<true>(p, b, b->H, st);
         launch_sources(p, b, false, b->H, 1, st);
-        k_update_H<true><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, false, b->E, b->H, b->H));
+        launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H), st);
         launch_sources(p, b, true, b->E, 1, st);
-        k_update_E<true><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, b->H, b->E, b->E));
+        launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E), st);
         k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
     }
     cudaError_t e = cudaGetLastError();
@@ -635,14 +662,13 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
     float* Hcur = b->H;
     float* Hnext = p->need_hprev ? p->h_twin : b->H;
-    const dim3 grid = update_grid(p);
     for (int s = 0; s < n_steps; ++s) {
         cudaEventRecord(ev[0], st);
-        k_update_E<false><<<grid, kUpdBlock, 0, st>>>(make_upd(p, b, true, Hcur, b->E, b->E));
+        launch_E<false>(p, make_upd(p, b, true, Hcur, b->E, b->E), st);
         cudaEventRecord(ev[1], st);
         launch_sources(p, b, true, b->E, 0, st);
         cudaEventRecord(ev[2], st);
-        k_update_H<false><<<grid, kUpdBlock, 0, st>>>(make_upd_fwd_H(p, b, Hcur, Hnext));
+        launch_H<false>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st);
         cudaEventRecord(ev[3], st);
         launch_sources(p, b, false, Hnext, 0, st);
         cudaEventRecord(ev[4], st);
@@ -679,12 +705,15 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     return FDTD_OK;
 }
 
-extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk) {
+extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk, int32_t vec) {
     if (!p) return FDTD_EINVAL;
     if (chunk <= 0) chunk = default_chunk(p->g.nx, p->g.ny, p->g.nz, p->sm_count);
     if (chunk > p->g.nx) chunk = p->g.nx;
-    if (chunk != p->chunk) {
+    if (vec <= 0) vec = pick_vec(p->g.nz);
+    if ((vec != 1 && vec != 2 && vec != 4) || p->g.nz % vec) return fail(p, FDTD_EINVAL, "vec must be 1, 2 or 4 and divide nz");
+    if (chunk != p->chunk || vec != p->vec) {
         p->chunk = chunk;
+        p->vec = vec;
         if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
         if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
         p->gsteps = 0;
@@ -693,3 +722,4 @@ extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk) {
 }
 
 extern "C" int32_t fdtd_plan_chunk(const FdtdPlan* p) { return p ? p->chunk : 0; }
+extern "C" int32_t fdtd_plan_vec(const FdtdPlan* p) { return p ? p->vec : 0; }

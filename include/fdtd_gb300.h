@@ -191,10 +191,12 @@ int fdtd_reverse(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t_end, int32_t
  * gradients are accumulated. */
 int fdtd_adjoint_step(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t, void* stream);
 
-/* Tuning: x planes each update block marches over (0 restores the default).
- * Invalidates a cached CUDA graph.  fdtd_plan_chunk returns the current value. */
-int fdtd_plan_tune(FdtdPlan* plan, int32_t chunk);
+/* Tuning of the update kernels: `chunk` x planes per block, `vec` z cells per thread
+ * (1, 2 or 4, dividing nz); 0 restores a default.  Invalidates a cached CUDA graph.
+ * fdtd_plan_chunk / fdtd_plan_vec return the current values. */
+int fdtd_plan_tune(FdtdPlan* plan, int32_t chunk, int32_t vec);
 int32_t fdtd_plan_chunk(const FdtdPlan* plan);
+int32_t fdtd_plan_vec(const FdtdPlan* plan);
 
 /* Number of launches of this library's kernels one forward step issues. */
 int32_t fdtd_launches_per_step(const FdtdPlan* plan);
