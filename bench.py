@@ -138,8 +138,12 @@ def run_gpu(args):
     objects, arrays, _, cfg, _ = scenes.coupler(shape=shape, steps=T_TOTAL, device=dev)
     arrays = arrays.reset()
     scene = get_scene(objects, arrays, cfg)
+    if args.tma == "0":
+        scene.tune_tma(False)
+    elif args.tma == "1" or args.tz or args.ty or args.stages or args.tchunk:
+        scene.tune_tma(True, args.tz, args.ty, args.stages, args.tchunk)
     if args.chunk or args.vec:
-        NATIVE.check(NATIVE.load().fdtd_plan_tune(scene.plan, args.chunk, args.vec), scene.plan, "fdtd_plan_tune")
+        scene.tune(args.chunk, args.vec)
     ncell = shape[0] * shape[1] * shape[2]
     W, K = args.warmup, args.steps
     if W + K + 8 > T_TOTAL:
@@ -156,6 +160,7 @@ def run_gpu(args):
         scene.forward(arrays, W, K)
         ev1.record(stream)
         torch.cuda.synchronize()
+    scene.status()
     ms = ev0.elapsed_time(ev1)
     if ws > 1:
         t = torch.tensor([ms], device=dev)
@@ -233,6 +238,7 @@ def run_gpu(args):
             "parallelism": f"replicas x{ws}",
             "chunk": int(NATIVE.load().fdtd_plan_chunk(scene.plan)),
             "vec": int(NATIVE.load().fdtd_plan_vec(scene.plan)),
+            "tma": scene.uses_tma,
             "hbm_gbs_effective": round(sum(alg.values()) / (ms / K / 1e3) / 1e9, 1),
         },
         "roofline": {
@@ -339,6 +345,11 @@ def main():
     ap.add_argument("--shape", default="", help="grid override nx,ny,nz (profiling cases)")
     ap.add_argument("--chunk", type=int, default=0, help="x planes per update block (0: plan default)")
     ap.add_argument("--vec", type=int, default=0, help="z cells per thread (0: plan default)")
+    ap.add_argument("--tma", default="auto", choices=["auto", "0", "1"], help="TMA-pipelined update kernels")
+    ap.add_argument("--tz", type=int, default=0)
+    ap.add_argument("--ty", type=int, default=0)
+    ap.add_argument("--stages", type=int, default=0)
+    ap.add_argument("--tchunk", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("warmup must be >= 3")

@@ -153,6 +153,9 @@ SIGNATURES = {
     "fdtd_plan_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "fdtd_plan_chunk": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_vec": (C.c_int32, [C.c_void_p]),
+    "fdtd_plan_tune_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "fdtd_plan_uses_tma": (C.c_int32, [C.c_void_p]),
+    "fdtd_plan_status": (C.c_int, [C.c_void_p]),
     "fdtd_profile_forward": (
         C.c_int,
         [C.c_void_p, C.POINTER(Buffers), C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p],

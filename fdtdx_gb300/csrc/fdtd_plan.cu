@@ -10,6 +10,9 @@
 
 #include "fdtd_kernels.cuh"
 #include "fdtd_adjoint.cuh"
+#include "fdtd_tma.cuh"
+
+#include <cudaTypedefs.h>
 
 using namespace fdtd;
 
@@ -32,6 +35,12 @@ struct FdtdPlan {
     int chunk = 1;                        // x planes per update block
     int vec = 1;                          // z cells per thread (4, 2 or 1: nz % vec == 0)
     int sm_count = 1;
+    // TMA-pipelined update kernels (non-periodic scenes with nz % 4 == 0)
+    bool tma_ok = false;                  // the scene admits the TMA kernels
+    bool use_tma = false;                 // they are selected
+    int tma_tz = 32, tma_ty = 8, tma_ns = 4;
+    int tma_chunk = 1;
+    int* d_err = nullptr;                 // kernel error word (FDTD_ETIMEOUT on a wait that ran out)
     // graph cache for the forward loop
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -109,6 +118,49 @@ int default_chunk(int nx, int ny, int nz, int sms) {
     return (int)((nx + nchunks - 1) / nchunks);
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
+// z tile: a multiple of 4 in [8, 64] that wastes the fewest cells, the larger on ties.
+int pick_tz(int nz) {
+    int best = 64, waste = 1 << 30;
+    for (int tz = 64; tz >= 8; tz -= 4) {
+        const int w = (nz + tz - 1) / tz * tz - nz;
+        if (w < waste) { waste = w; best = tz; }
+    }
+    return best;
+}
+
+int align32(int x) { return (x + 31) / 32 * 32; }
+
+// Shared-memory layout of one pipeline stage (floats): differentiated field with halo, then the
+// updated field, material and conductivity tiles, each 128-byte aligned.
+TmaCfg tma_cfg(int tz, int ty, int ns, bool hside, int nm, int nsig, int* err) {
+    TmaCfg c{};
+    c.TZ = tz; c.TY = ty; c.ns = ns; c.nm = nm; c.nsig = nsig; c.err = err;
+    const int fz = hside ? tz + 8 : tz + 4, fy = hside ? ty + 2 : ty + 1;
+    const int nF = 3 * fy * fz, nU = 3 * ty * tz, nM = nm * ty * tz, nS = nsig * ty * tz;
+    c.off_U = align32(nF);
+    c.off_M = c.off_U + align32(nU);
+    c.off_S = c.off_M + align32(nM);
+    c.stage_floats = c.off_S + align32(nS);
+    c.stage_bytes = (uint32_t)(4 * (nF + nU + nM + nS));
+    return c;
+}
+
+size_t tma_smem(const TmaCfg& c) { return (size_t)c.ns * c.stage_floats * 4 + (size_t)c.ns * 8; }
+
 int validate(const FdtdDesc* d, std::string& why) {
     if (d->nx <= 0 || d->ny <= 0 || d->nz <= 0) { why = "grid dims must be positive"; return FDTD_EINVAL; }
     if ((long long)d->nx * d->ny * d->nz * 3 >= (1ll << 40)) { why = "grid too large"; return FDTD_EINVAL; }
@@ -169,6 +221,35 @@ int validate(const FdtdDesc* d, std::string& why) {
 
 size_t rec_elem_bytes(int dt) { return dt == 0 ? 4 : 2; }
 
+// Shared memory, occupancy and the x-chunk of the TMA kernels for the current tile choice.
+void configure_tma(FdtdPlan* p) {
+    p->use_tma = false;
+    if (!p->tma_ok) return;
+    const int tz = p->tma_tz, ty = p->tma_ty, ns = p->tma_ns;
+    const int threads = ty * tz / 2;
+    const int nmE = p->d.n_eps, nsE = p->d.n_sigma_E, nmH = p->d.n_mu, nsH = p->d.n_sigma_H;
+    const size_t smE = tma_smem(tma_cfg(tz, ty, ns, false, nmE, nsE, nullptr));
+    const size_t smH = tma_smem(tma_cfg(tz, ty, ns, true, nmH, nsH, nullptr));
+    int occ = 1 << 30;
+    auto setup = [&](const void* fn, size_t sm) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, sm) != cudaSuccess) nb = 0;
+        occ = std::min(occ, nb);
+    };
+    setup((const void*)k_tma_E<false>, smE);
+    setup((const void*)k_tma_E<true>, smE);
+    setup((const void*)k_tma_H<false>, smH);
+    setup((const void*)k_tma_H<true>, smH);
+    cudaGetLastError();
+    if (occ <= 0 || threads > 256 || threads < 32) return;
+    const long long tiles = (long long)((p->g.nz + tz - 1) / tz) * ((p->g.ny + ty - 1) / ty);
+    long long nchunks = std::max(1ll, (long long)occ * p->sm_count / tiles);
+    nchunks = std::min<long long>(nchunks, std::max(1, p->g.nx / 8));
+    p->tma_chunk = (int)((p->g.nx + nchunks - 1) / nchunks);
+    p->use_tma = true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -198,6 +279,9 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         if (cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) p->sm_count = 152;
         p->chunk = default_chunk(d.nx, d.ny, d.nz, p->sm_count);
         p->vec = pick_vec(d.nz);
+        p->tma_ok = d.nz % 4 == 0 && d.nz >= 8 && !d.periodic[0] && !d.periodic[1] && !d.periodic[2] && encode_fn();
+        p->tma_tz = pick_tz(d.nz);
+        p->tma_ty = 8;
     }
 
     // ---- lay out the device arena
@@ -251,6 +335,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         return cudaMemcpy(p->dmem + off, src, bytes, cudaMemcpyHostToDevice);
     };
     p->d_t = reinterpret_cast<int*>(p->dmem + o_t);
+    p->d_err = p->d_t + 1;
     e = cudaMemset(p->d_t, 0, sizeof(int) * 4);
 
     const int n3[3] = {d.nx, d.ny, d.nz};
@@ -347,6 +432,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         p->d.detectors[q].slot = nullptr;
         p->d.detectors[q].weights = nullptr;
     }
+    configure_tma(p);
     *out = p;
     return FDTD_OK;
 }
@@ -380,8 +466,45 @@ dim3 update_grid(const FdtdPlan* p) {
 }
 const dim3 kUpdBlock(kUpdThreads, 1, 1);
 
+bool make_map(CUtensorMap* m, const float* base, int ncomp, const Geo& g, int bz, int by, int bc) {
+    auto fn = encode_fn();
+    if (!fn || !base) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)g.nz, (cuuint64_t)g.ny, (cuuint64_t)g.nx, (cuuint64_t)ncomp};
+    const cuuint64_t strides[3] = {(cuuint64_t)g.nz * 4, (cuuint64_t)g.ny * g.nz * 4, (cuuint64_t)g.N * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)bz, (cuuint32_t)by, 1, (cuuint32_t)bc};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launch of a TMA-pipelined half-step; false when a tensor map cannot be built (the caller
+// then uses the register-queue kernel).
+template <bool REV, bool HSIDE>
+bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+    const Geo& g = p->g;
+    const int tz = p->tma_tz, ty = p->tma_ty;
+    const int nm = a.mat ? a.n_mat : 0, nsig = a.sig ? a.n_sig : 0;
+    const TmaCfg c = tma_cfg(tz, ty, p->tma_ns, HSIDE, nm, nsig, p->d_err);
+    CUtensorMap mF, mU, mM, mS;
+    std::memset(&mM, 0, sizeof(mM));
+    std::memset(&mS, 0, sizeof(mS));
+    const int fz = HSIDE ? tz + 8 : tz + 4, fy = HSIDE ? ty + 2 : ty + 1;
+    if (!make_map(&mF, a.F, 3, g, fz, fy, 3) || !make_map(&mU, a.Uin, 3, g, tz, ty, 3)) return false;
+    if (nm && !make_map(&mM, a.mat, nm, g, tz, ty, nm)) return false;
+    if (nsig && !make_map(&mS, a.sig, nsig, g, tz, ty, nsig)) return false;
+    UpdArgs aa = a;
+    aa.chunk = p->tma_chunk;
+    const dim3 grid((g.nz + tz - 1) / tz, (g.ny + ty - 1) / ty, (g.nx + aa.chunk - 1) / aa.chunk);
+    const dim3 block(ty * tz / 2);
+    if (HSIDE) k_tma_H<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
+    else k_tma_E<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
+    return true;
+}
+
 template <bool REV>
 void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+    if (p->use_tma && launch_tma<REV, false>(p, a, st)) return;
     const dim3 grid = update_grid(p);
     if (p->vec == 4) k_update_E<REV, 4><<<grid, kUpdBlock, 0, st>>>(a);
     else if (p->vec == 2) k_update_E<REV, 2><<<grid, kUpdBlock, 0, st>>>(a);
@@ -390,6 +513,7 @@ void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
 
 template <bool REV>
 void launch_H(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+    if (p->use_tma && launch_tma<REV, true>(p, a, st)) return;
     const dim3 grid = update_grid(p);
     if (p->vec == 4) k_update_H<REV, 4><<<grid, kUpdBlock, 0, st>>>(a);
     else if (p->vec == 2) k_update_H<REV, 2><<<grid, kUpdBlock, 0, st>>>(a);
@@ -723,3 +847,41 @@ extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk, int32_t vec) {
 
 extern "C" int32_t fdtd_plan_chunk(const FdtdPlan* p) { return p ? p->chunk : 0; }
 extern "C" int32_t fdtd_plan_vec(const FdtdPlan* p) { return p ? p->vec : 0; }
+
+extern "C" int fdtd_plan_tune_tma(FdtdPlan* p, int32_t enable, int32_t tz, int32_t ty, int32_t stages, int32_t chunk) {
+    if (!p) return FDTD_EINVAL;
+    if (enable && !p->tma_ok) return fail(p, FDTD_EINVAL, "this scene cannot use the TMA kernels (periodic axis or nz % 4 != 0)");
+    if (tz <= 0) tz = pick_tz(p->g.nz);
+    if (ty <= 0) ty = 8;
+    if (stages <= 0) stages = 4;
+    if (tz % 4 || tz < 8 || tz > 120 || ty < 1 || ty * tz / 2 > 256 || stages < 2 || stages > kMaxStages)
+        return fail(p, FDTD_EINVAL, "invalid TMA tile (tz a multiple of 4 in [8, 120], ty*tz/2 <= 256, 2..6 stages)");
+    p->tma_tz = tz;
+    p->tma_ty = ty;
+    p->tma_ns = stages;
+    if (enable) {
+        configure_tma(p);
+        if (!p->use_tma) return fail(p, FDTD_EINVAL, "TMA configuration does not fit the device");
+        if (chunk > 0) p->tma_chunk = std::min(chunk, p->g.nx);
+    } else {
+        p->use_tma = false;
+    }
+    if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    p->gsteps = 0;
+    return FDTD_OK;
+}
+
+extern "C" int32_t fdtd_plan_uses_tma(const FdtdPlan* p) { return p && p->use_tma ? 1 : 0; }
+
+extern "C" int fdtd_plan_status(FdtdPlan* p) {
+    if (!p) return FDTD_EINVAL;
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, p->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_plan_status");
+    if (h) {
+        cudaMemset(p->d_err, 0, sizeof(int));
+        return fail(p, h, "a pipeline wait in a kernel ran out (the step's results are invalid)");
+    }
+    return FDTD_OK;
+}

@@ -380,6 +380,23 @@ class Scene:
     def interface_floats(self) -> int:
         return int(N.load().fdtd_interface_floats(self.plan))
 
+    def tune(self, chunk: int = 0, vec: int = 0) -> None:
+        """Launch shape of the register-queue update kernels (0 keeps the default)."""
+        N.check(N.load().fdtd_plan_tune(self.plan, int(chunk), int(vec)), self.plan, "fdtd_plan_tune")
+
+    def tune_tma(self, enable: bool = True, tz: int = 0, ty: int = 0, stages: int = 0, chunk: int = 0) -> None:
+        """Select the TMA-pipelined update kernels and their tile (0 keeps a default)."""
+        N.check(N.load().fdtd_plan_tune_tma(self.plan, 1 if enable else 0, int(tz), int(ty), int(stages), int(chunk)),
+                self.plan, "fdtd_plan_tune_tma")
+
+    @property
+    def uses_tma(self) -> bool:
+        return bool(N.load().fdtd_plan_uses_tma(self.plan))
+
+    def status(self) -> None:
+        """Raise if a kernel reported an error (a bounded pipeline wait that ran out)."""
+        N.check(N.load().fdtd_plan_status(self.plan), self.plan, "fdtd_plan_status")
+
     # ---- buffers
     def buffers(self, arrays: ArrayContainer) -> N.Buffers:
         b = N.Buffers()

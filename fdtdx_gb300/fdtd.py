@@ -80,6 +80,7 @@ def checkpointed_fdtd(
     scene = get_scene(objects, arrays, config, record_interfaces=config.invertible_optimization)
     T = config.time_steps_total
     scene.forward(arrays, 0, T)
+    scene.status()
     if progress_callback is not None:
         progress_callback(T, T)
     return T, arrays

@@ -198,6 +198,17 @@ int fdtd_plan_tune(FdtdPlan* plan, int32_t chunk, int32_t vec);
 int32_t fdtd_plan_chunk(const FdtdPlan* plan);
 int32_t fdtd_plan_vec(const FdtdPlan* plan);
 
+/* Selects the TMA-pipelined update kernels (enable=1; scenes without periodic axes and
+ * with nz % 4 == 0) or the register-queue kernels (enable=0), with a (y, z) tile of
+ * ty x tz cells (tz a multiple of 4), `stages` pipeline stages and `chunk` x planes per
+ * block; 0 picks a default.  fdtd_plan_uses_tma reports the current choice. */
+int fdtd_plan_tune_tma(FdtdPlan* plan, int32_t enable, int32_t tz, int32_t ty, int32_t stages, int32_t chunk);
+int32_t fdtd_plan_uses_tma(const FdtdPlan* plan);
+
+/* Reads and clears the kernels' error word (synchronises the device): FDTD_OK, or
+ * FDTD_ETIMEOUT when a bounded pipeline wait ran out during an earlier call. */
+int fdtd_plan_status(FdtdPlan* plan);
+
 /* Number of launches of this library's kernels one forward step issues. */
 int32_t fdtd_launches_per_step(const FdtdPlan* plan);
 

@@ -231,3 +231,46 @@ def test_vec_and_chunk_variants_agree(nz):
             else:
                 for x, y in zip(got, ref):
                     assert torch.equal(x, y), (vec, chunk)
+
+
+@pytest.mark.parametrize("tile", [(0, 0, 0, 0), (16, 8, 2, 3), (24, 4, 3, 7), (64, 8, 6, 0)])
+def test_tma_kernels_match_register_kernels(tile):
+    """The TMA-pipelined half-steps agree with the register-queue half-steps (every tile shape,
+    partial tiles in y and z, chunked x, CPML, conductivity, fused detectors)."""
+    tz, ty, ns, chunk = tile
+    cfg = _cfg(50)
+    vol = fx.SimulationVolume(shape=(30, 27, 44))
+    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(5), vol).values())
+    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((8, 20), (6, 20), (10, 30)),
+                                         material=fx.Material(permittivity=(4.0, 3.0, 5.0), electric_conductivity=1e4,
+                                                              magnetic_conductivity=1e9, permeability=1.5)))
+    objs.append(fx.PointDipoleSource(name="d", grid_slice_tuple=((15, 16), (13, 14), (22, 23)), polarization=1,
+                                     wave_character=fx.WaveCharacter(wavelength=1.55e-6),
+                                     temporal_profile=scenes.pulse_5fs()))
+    objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((0, 30), (3, 25), (0, 44)),
+                                  wave_characters=(fx.WaveCharacter(wavelength=1.55e-6),), components=("Ex", "Ey", "Ez")))
+    objs.append(fx.FieldDetector(name="ez", grid_slice_tuple=((0, 30), (0, 27), (20, 21)), components=("Ez", "Ey")))
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
+    outs = []
+    for tma in (True, False):
+        a = arrays.reset()
+        s = Scene(objects, a, cfg)
+        if tma:
+            s.tune_tma(True, tz, ty, ns, chunk)
+            assert s.uses_tma
+        else:
+            s.tune_tma(False)
+        s.forward(a, 0, 50)
+        s.status()
+        torch.cuda.synchronize()
+        outs.append(a)
+        s.close()
+    for k in ("E", "H"):
+        assert rel_l2(getattr(outs[0].fields, k), getattr(outs[1].fields, k)) < 1e-6
+    for dn in ("ph", "ez"):
+        for kk, v in outs[0].detector_states[dn].items():
+            assert rel_l2(v, outs[1].detector_states[dn][kk]) < 1e-6
+    for n in outs[0].fields.psi_E:
+        for q in range(2):
+            assert rel_l2(outs[0].fields.psi_E[n][q], outs[1].fields.psi_E[n][q]) < 1e-6
+            assert rel_l2(outs[0].fields.psi_H[n][q], outs[1].fields.psi_H[n][q]) < 1e-6
