@@ -52,6 +52,68 @@ __device__ __forceinline__ void cpml_correct(const UpdArgs& a, int i, int j, int
     }
 }
 
+// CPML psi of one cell fetched ahead of its use (one plane early in the TMA kernels, so
+// the latency of these scattered slab reads overlaps the previous plane's work).
+struct PsiPre {
+    float v[FDTD_MAX_SLABS][2];
+};
+
+__device__ __forceinline__ long long psi_offset(const DSlab& sl, int i, int j, int k) {
+    return ((long long)(i - (sl.axis == 0 ? sl.lo : 0)) * sl.sy + (j - (sl.axis == 1 ? sl.lo : 0))) * sl.sz +
+           (k - (sl.axis == 2 ? sl.lo : 0));
+}
+
+__device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k, PsiPre& pr) {
+    const int idx3[3] = {i, j, k};
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        pr.v[s][0] = 0.f;
+        pr.v[s][1] = 0.f;
+        if (s >= a.n_slab) continue;
+        const DSlab& sl = a.slab[s];
+        const int l = idx3[sl.axis] - sl.lo;
+        if ((unsigned)l >= (unsigned)sl.L) continue;
+        const long long p = psi_offset(sl, i, j, k);
+        pr.v[s][0] = a.psi1[s][p];
+        pr.v[s][1] = a.psi2[s][p];
+    }
+}
+
+// cpml_correct with the psi values taken from a prefetch.
+template <bool REV, bool HSIDE>
+__device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k, const float d[6], float cu[3],
+                                           const PsiPre& pr) {
+    const int idx3[3] = {i, j, k};
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (s >= a.n_slab) break;
+        const DSlab& sl = a.slab[s];
+        const int l = idx3[sl.axis] - sl.lo;
+        if ((unsigned)l >= (unsigned)sl.L) continue;
+        const float d1 = sl.axis == 0 ? d[3] : (sl.axis == 1 ? d[5] : d[1]);
+        const float d2 = sl.axis == 0 ? d[4] : (sl.axis == 1 ? d[0] : d[2]);
+        const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
+        float p1 = pr.v[s][0], p2 = pr.v[s][1];
+        if (!REV) {
+            const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
+            p1 = cb * p1 + ca * d1;
+            p2 = cb * p2 + ca * d2;
+            const long long p = psi_offset(sl, i, j, k);
+            a.psi1[s][p] = p1;
+            a.psi2[s][p] = p2;
+        }
+        float c1 = p1, c2 = p2;
+        if (!sl.kappa_one) {
+            const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+            c1 = ikm1 * d1 + p1;
+            c2 = ikm1 * d2 + p2;
+        }
+        if (sl.axis == 0) { cu[1] -= c1; cu[2] += c2; }
+        else if (sl.axis == 1) { cu[2] -= c1; cu[0] += c2; }
+        else { cu[0] -= c1; cu[1] += c2; }
+    }
+}
+
 // Neighbour on one axis with the halo rule (wrap on a periodic axis, else zero).
 __device__ __forceinline__ float nb(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp, int i,
                                     int j, int k) {
@@ -228,10 +290,14 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
 // Accumulates the fused E-only detectors at cell (i, j, k) from the E values the H
 // half-step already holds.  Co-location at (i, j, k+1/2) (fdtdx/core/physics/curl.py:120-158):
 // Ex <- (avg_x(Ex)(k) + avg_x(Ex)(k+1)) / 2, Ey <- (avg_y(Ey)(k) + avg_y(Ey)(k+1)) / 2, Ez.
+// `staged` (optional) points at this cell's previous phasor values of detector 0 in a
+// shared-memory tile (complex planes `staged_stride` floats apart), so the read half of
+// its read-modify-write comes from the TMA pipeline instead of HBM.
 __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot[kMaxFuse],
                                                 const float2 w[kMaxFuse][kMaxFuseFreq], int i, int j, int k,
                                                 float Ex, float Ex_kp, float Ex_im, float Exkp_im, float Ey, float Ey_kp,
-                                                float Ey_jm, float Eykp_jm, float Ez) {
+                                                float Ey_jm, float Eykp_jm, float Ez, const float* staged = nullptr,
+                                                int staged_stride = 0) {
 #pragma unroll
     for (int q = 0; q < kMaxFuse; ++q) {
         if (q >= a.n_fuse) break;
@@ -259,7 +325,13 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
                 for (int f = 0; f < kMaxFuseFreq; ++f) {
                     if (f >= d.nfreq) break;
                     float2* pp = st + ((long long)f * d.nout + o) * d.R + r;
-                    float2 z = *pp;
+                    float2 z;
+                    if (q == 0 && staged) {
+                        const float* sp = staged + (f * d.nout + o) * staged_stride;
+                        z = make_float2(sp[0], sp[1]);
+                    } else {
+                        z = *pp;
+                    }
                     if (d.inverse) { z.x -= v[comp] * w[q][f].x; z.y -= v[comp] * w[q][f].y; }
                     else { z.x += v[comp] * w[q][f].x; z.y += v[comp] * w[q][f].y; }
                     *pp = z;

@@ -146,16 +146,17 @@ int align32(int x) { return (x + 31) / 32 * 32; }
 
 // Shared-memory layout of one pipeline stage (floats): differentiated field with halo, then the
 // updated field, material and conductivity tiles, each 128-byte aligned.
-TmaCfg tma_cfg(int tz, int ty, int ns, bool hside, int nm, int nsig, int* err) {
+TmaCfg tma_cfg(int tz, int ty, int ns, bool hside, int nm, int nsig, int* err, int nd = 0) {
     TmaCfg c{};
-    c.TZ = tz; c.TY = ty; c.ns = ns; c.nm = nm; c.nsig = nsig; c.err = err;
+    c.TZ = tz; c.TY = ty; c.ns = ns; c.nm = nm; c.nsig = nsig; c.nd = nd; c.err = err;
     const int fz = hside ? tz + 8 : tz + 4, fy = hside ? ty + 2 : ty + 1;
-    const int nF = 3 * fy * fz, nU = 3 * ty * tz, nM = nm * ty * tz, nS = nsig * ty * tz;
+    const int nF = 3 * fy * fz, nU = 3 * ty * tz, nM = nm * ty * tz, nS = nsig * ty * tz, nD = nd * ty * 2 * tz;
     c.off_U = align32(nF);
     c.off_M = c.off_U + align32(nU);
     c.off_S = c.off_M + align32(nM);
-    c.stage_floats = c.off_S + align32(nS);
-    c.stage_bytes = (uint32_t)(4 * (nF + nU + nM + nS));
+    c.off_D = c.off_S + align32(nS);
+    c.stage_floats = c.off_D + align32(nD);
+    c.stage_bytes = (uint32_t)(4 * (nF + nU + nM + nS + nD));
     return c;
 }
 
@@ -221,6 +222,18 @@ int validate(const FdtdDesc* d, std::string& why) {
 
 size_t rec_elem_bytes(int dt) { return dt == 0 ? 4 : 2; }
 
+// The first fused detector is staged through the H pipeline when it is a phasor whose region
+// origin and z extent keep every complex tile row 16-byte aligned.
+int staged_planes(const FdtdPlan* p) {
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (!p->fused[q]) continue;
+        const DDet& d = p->det[q];
+        if (d.kind != FDTD_DET_PHASOR || d.lo[2] % 2 || d.rz % 2 || d.nfreq * d.ncomp > 16) return 0;
+        return d.nfreq * d.ncomp;
+    }
+    return 0;
+}
+
 // Shared memory, occupancy and the x-chunk of the TMA kernels for the current tile choice.
 void configure_tma(FdtdPlan* p) {
     p->use_tma = false;
@@ -229,7 +242,7 @@ void configure_tma(FdtdPlan* p) {
     const int threads = ty * tz / 2;
     const int nmE = p->d.n_eps, nsE = p->d.n_sigma_E, nmH = p->d.n_mu, nsH = p->d.n_sigma_H;
     const size_t smE = tma_smem(tma_cfg(tz, ty, ns, false, nmE, nsE, nullptr));
-    const size_t smH = tma_smem(tma_cfg(tz, ty, ns, true, nmH, nsH, nullptr));
+    const size_t smH = tma_smem(tma_cfg(tz, ty, ns, true, nmH, nsH, nullptr, staged_planes(p)));
     int occ = 1 << 30;
     auto setup = [&](const void* fn, size_t sm) {
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -485,7 +498,26 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     const Geo& g = p->g;
     const int tz = p->tma_tz, ty = p->tma_ty;
     const int nm = a.mat ? a.n_mat : 0, nsig = a.sig ? a.n_sig : 0;
-    const TmaCfg c = tma_cfg(tz, ty, p->tma_ns, HSIDE, nm, nsig, p->d_err);
+    // the staged phasor tile of the first fused detector (forward H step only)
+    int nd = 0;
+    CUtensorMap mD;
+    std::memset(&mD, 0, sizeof(mD));
+    if (HSIDE && !REV && a.n_fuse > 0 && staged_planes(p) && !((uintptr_t)a.fuse[0].state & 15)) {
+        const DFuse& f = a.fuse[0];
+        auto fn = encode_fn();
+        const int planes = f.nfreq * f.nout;
+        const cuuint64_t dims[4] = {(cuuint64_t)2 * f.rz, (cuuint64_t)f.ry, (cuuint64_t)f.rx, (cuuint64_t)planes};
+        const cuuint64_t strides[3] = {(cuuint64_t)8 * f.rz, (cuuint64_t)8 * f.rz * f.ry, (cuuint64_t)8 * f.R};
+        const cuuint32_t box[4] = {(cuuint32_t)(2 * tz), (cuuint32_t)ty, 1, (cuuint32_t)planes};
+        const cuuint32_t es[4] = {1, 1, 1, 1};
+        if (fn && fn(&mD, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, f.state, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+            nd = planes;
+    }
+    TmaCfg c = tma_cfg(tz, ty, p->tma_ns, HSIDE, nm, nsig, p->d_err, nd);
+    if (nd)
+        for (int x = 0; x < 3; ++x) c.dlo[x] = a.fuse[0].lo[x];
     CUtensorMap mF, mU, mM, mS;
     std::memset(&mM, 0, sizeof(mM));
     std::memset(&mS, 0, sizeof(mS));
@@ -497,7 +529,7 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     aa.chunk = p->tma_chunk;
     const dim3 grid((g.nz + tz - 1) / tz, (g.ny + ty - 1) / ty, (g.nx + aa.chunk - 1) / aa.chunk);
     const dim3 block(ty * tz / 2);
-    if (HSIDE) k_tma_H<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
+    if (HSIDE) k_tma_H<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
     else k_tma_E<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
     return true;
 }

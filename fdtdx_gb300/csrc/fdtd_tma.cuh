@@ -26,7 +26,9 @@ constexpr int kMaxStages = 6;
 struct TmaCfg {
     int TZ, TY, ns;
     int nm, nsig;          // components of the material / conductivity tiles (0: none)
-    int off_U, off_M, off_S, stage_floats;
+    int nd;                // complex planes (freqs x components) of the staged detector tile (0: none)
+    int dlo[3];            // region origin of the staged detector
+    int off_U, off_M, off_S, off_D, stage_floats;
     uint32_t stage_bytes;  // bytes the TMA loads of one stage deliver
     int* err;
 };
@@ -127,6 +129,12 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     float Hy_m[2] = {0.f, 0.f}, Hz_m[2] = {0.f, 0.f};
+    PsiPre pre[2];
+    bool pml = valid && a.n_slab > 0 && maybe_slab(a, i0, j, k0, 2);
+    if (pml) {
+        psi_fetch(a, i0, j, k0, pre[0]);
+        psi_fetch(a, i0, j, k0 + 1, pre[1]);
+    }
     for (int p = 0; p < P; ++p) {
         const int s = p % NS;
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
@@ -143,7 +151,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
             const float* M = F + tc.off_M;
             const float* S = F + tc.off_S;
             const long long c = cell_index(g, i, j, k0);
-            const bool pml = a.n_slab > 0 && maybe_slab(a, i, j, k0, 2);
             float out[3][2];
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
@@ -160,7 +167,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (pml) cpml_correct<REV, false>(a, i, j, k0 + e, d, cu);
+                if (pml) cpml_apply<REV, false>(a, i, j, k0 + e, d, cu, pre[e]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -181,6 +188,14 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
+            // psi of the next plane, fetched while the pipeline delivers it
+            if (i + 1 < i1) {
+                pml = a.n_slab > 0 && maybe_slab(a, i + 1, j, k0, 2);
+                if (pml) {
+                    psi_fetch(a, i + 1, j, k0, pre[0]);
+                    psi_fetch(a, i + 1, j, k0 + 1, pre[1]);
+                }
+            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -207,7 +222,8 @@ template <bool REV>
 __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
-                                               const __grid_constant__ CUtensorMap mS, const TmaCfg tc) {
+                                               const __grid_constant__ CUtensorMap mS,
+                                               const __grid_constant__ CUtensorMap mD, const TmaCfg tc) {
     extern __shared__ __align__(128) float sm[];
     const Geo& g = a.g;
     const int TZ = tc.TZ, TY = tc.TY, NS = tc.ns;
@@ -254,11 +270,18 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
         tma_load4(st + tc.off_U, &mU, &bar[s], kt, jt, i, 0);
         if (tc.nm) tma_load4(st + tc.off_M, &mM, &bar[s], kt, jt, i, 0);
         if (tc.nsig) tma_load4(st + tc.off_S, &mS, &bar[s], kt, jt, i, 0);
+        if (tc.nd) tma_load4(st + tc.off_D, &mD, &bar[s], 2 * (kt - tc.dlo[2]), jt - tc.dlo[1], i - tc.dlo[0], 0);
     };
     if (tid == 0)
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     bool ok = mbar_wait_bounded(&bar[0], 0);
+    PsiPre pre[2];
+    bool pml = valid && a.n_slab > 0 && maybe_slab(a, i0, j, k0, 2);
+    if (pml) {
+        psi_fetch(a, i0, j, k0, pre[0]);
+        psi_fetch(a, i0, j, k0 + 1, pre[1]);
+    }
     // Ex(i-1) at k and k+1 of this thread's two cells (fused co-location), seeded at the chunk start
     float Exm[3] = {0.f, 0.f, 0.f};
     if (any && valid) {
@@ -276,7 +299,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
             const float* M = E + tc.off_M;
             const float* S = E + tc.off_S;
             const long long c = cell_index(g, i, j, k0);
-            const bool pml = a.n_slab > 0 && maybe_slab(a, i, j, k0, 2);
             const int r0 = ty + 1;
             float out[3][2];
             float Exc[3];
@@ -297,7 +319,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (pml) cpml_correct<REV, true>(a, i, j, k0 + e, d, cu);
+                if (pml) cpml_apply<REV, true>(a, i, j, k0 + e, d, cu, pre[e]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -317,8 +339,9 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 if (!REV && any) {
                     const float Ey_jm = E[(1 * EY + r0 - 1) * EZ + kk];
                     const float Eykp_jm = E[(1 * EY + r0 - 1) * EZ + kk + 1];
+                    const float* staged = tc.nd ? E + tc.off_D + ty * 2 * TZ + 2 * cz : nullptr;
                     fused_detectors(a, slot, w, i, j, k0 + e, Ex, Ex_kp, Exm[e], Exm[e + 1], Ey, Ey_kp, Ey_jm, Eykp_jm,
-                                    Ez);
+                                    Ez, staged, TY * 2 * TZ);
                 }
             }
 #pragma unroll
@@ -326,6 +349,13 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
+            if (i + 1 < i1) {
+                pml = a.n_slab > 0 && maybe_slab(a, i + 1, j, k0, 2);
+                if (pml) {
+                    psi_fetch(a, i + 1, j, k0, pre[0]);
+                    psi_fetch(a, i + 1, j, k0 + 1, pre[1]);
+                }
+            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
