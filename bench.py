@@ -135,7 +135,8 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     shape = tuple(int(x) for x in args.shape.split(",")) if args.shape else SHAPE
-    objects, arrays, _, cfg, _ = scenes.coupler(shape=shape, steps=T_TOTAL, device=dev)
+    objects, arrays, _, cfg, _ = scenes.coupler(shape=shape, steps=T_TOTAL, device=dev, boundary=args.boundary,
+                                                full_phasor=not args.no_phasor)
     arrays = arrays.reset()
     scene = get_scene(objects, arrays, cfg)
     if args.tma == "0":
@@ -195,7 +196,7 @@ def run_gpu(args):
         ie = host_eps.to(dev, non_blocking=True)
         arr = base.aset("inv_permittivities", ie)
         _, out = fx.run_fdtd(arr, objects, cfg_e2e)
-        res = [out.detector_states[n]["phasor"].to("cpu") for n in ("flux1", "flux2")]
+        res = [out.detector_states[n]["phasor"].to("cpu") for n in ("flux1", "flux2")]  # the flux planes' phasors
         return res
 
     e2e = None
@@ -350,6 +351,8 @@ def main():
     ap.add_argument("--ty", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--tchunk", type=int, default=0)
+    ap.add_argument("--boundary", default="pml", help="boundary type of the workload (profiling ablations)")
+    ap.add_argument("--no-phasor", action="store_true", help="drop the full-volume phasor (profiling ablations)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("warmup must be >= 3")

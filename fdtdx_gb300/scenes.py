@@ -88,7 +88,7 @@ def dipole_boxes(shape=(100, 100, 100), steps: int = 1000, seed: int = 0, n_boxe
 
 
 def coupler(shape=(400, 400, 200), steps: int = 8000, scale: float = 1.0, dx: float = 20e-9, pml: int = 10,
-            full_phasor: bool = True, device=None):
+            full_phasor: bool = True, boundary: str = "pml", device=None):
     """Two parallel Si strips (500 x 220 nm, 200 nm gap) spanning x in SiO2, CW Gaussian source on strip 1."""
     nx, ny, nz = shape
     s = scale
@@ -96,7 +96,8 @@ def coupler(shape=(400, 400, 200), steps: int = 8000, scale: float = 1.0, dx: fl
     cfg = _config(dx, steps)
     vol = SimulationVolume(shape=shape, material=Material(permittivity=EPS_SIO2))
     objs = [vol]
-    objs += list(boundary_objects_from_config(BoundaryConfig.from_uniform_bound(thickness=pml), vol).values())
+    objs += list(boundary_objects_from_config(BoundaryConfig.from_uniform_bound(thickness=pml, boundary_type=boundary),
+                                              vol).values())
     yc, zc = ny // 2, nz // 2
     y1 = (yc - gap // 2 - w, yc - gap // 2)
     y2 = (yc + (gap - gap // 2), yc + (gap - gap // 2) + w)
