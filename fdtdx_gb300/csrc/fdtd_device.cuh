@@ -63,6 +63,7 @@ struct UpdArgs {
     float* psi1[FDTD_MAX_SLABS];
     float* psi2[FDTD_MAX_SLABS];
     int chunk;                  // x planes per block (the block marches along x)
+    int lo[3], hi[3];           // the box of cells this launch updates
     const int* tp;              // device time-step counter
     int n_fuse;
     DFuse fuse[kMaxFuse];

@@ -214,13 +214,15 @@ __device__ __forceinline__ float material_update(const UpdArgs& a, float u0, flo
 
 // Column decomposition shared by both half-steps: a thread owns VEC consecutive z cells
 // of one (j) row and marches over the block's `chunk` x planes.
+// (the launch's box has VEC-aligned z bounds)
 template <int VEC>
-__device__ __forceinline__ bool column_of(const Geo& g, int& j, int& k0) {
-    const int nq = g.nz / VEC;
+__device__ __forceinline__ bool column_of(const UpdArgs& a, int& j, int& k0) {
+    const int nq = (a.hi[2] - a.lo[2]) / VEC;
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (long long)g.ny * nq) return false;
-    j = (int)(q / nq);
-    k0 = (int)(q - (long long)j * nq) * VEC;
+    if (q >= (long long)(a.hi[1] - a.lo[1]) * nq) return false;
+    const int jj = (int)(q / nq);
+    j = a.lo[1] + jj;
+    k0 = a.lo[2] + (int)(q - (long long)jj * nq) * VEC;
     return true;
 }
 
@@ -228,13 +230,13 @@ __device__ __forceinline__ bool column_of(const Geo& g, int& j, int& k0) {
 // E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
 // reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
 // ---------------------------------------------------------------------------------
-template <bool REV, int VEC>
+template <bool REV, int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
     const Geo& g = a.g;
     int j, k0;
-    if (!column_of<VEC>(g, j, k0)) return;
-    const int i0 = blockIdx.y * a.chunk;
-    const int i1 = min(i0 + a.chunk, g.nx);
+    if (!column_of<VEC>(a, j, k0)) return;
+    const int i0 = a.lo[0] + blockIdx.y * a.chunk;
+    const int i1 = min(i0 + a.chunk, a.hi[0]);
     const long long N = g.N;
     const long long sy = g.nz;
     const float* __restrict__ H = a.F;
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
         Vec<VEC> Eo[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) Eo[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
-        const bool pml = a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        const bool pml = PML && a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
             const int k = k0 + e;
@@ -351,13 +353,13 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
 // Marches along +x keeping E(i+1) (the next iteration's E(i)) and Ex(i-1) in registers;
 // fused E-only detectors are accumulated in the same pass (forward only).
 // ---------------------------------------------------------------------------------
-template <bool REV, int VEC>
+template <bool REV, int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
     const Geo& g = a.g;
     int j, k0;
-    if (!column_of<VEC>(g, j, k0)) return;
-    const int i0 = blockIdx.y * a.chunk;
-    const int i1 = min(i0 + a.chunk, g.nx);
+    if (!column_of<VEC>(a, j, k0)) return;
+    const int i0 = a.lo[0] + blockIdx.y * a.chunk;
+    const int i1 = min(i0 + a.chunk, a.hi[0]);
     const long long N = g.N;
     const long long sy = g.nz, sx = (long long)g.ny * g.nz;
     const float* __restrict__ E = a.F;
@@ -412,7 +414,7 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
         Vec<VEC> Ho[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) Ho[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
-        const bool pml = a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        const bool pml = PML && a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
         Vec<VEC> Ey_jm{};
         float Eyk_jm = 0.f;
         if (!REV && any) {

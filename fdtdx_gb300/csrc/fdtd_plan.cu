@@ -107,7 +107,7 @@ bool det_fusable(const FdtdDetectorDesc& dd) {
 
 constexpr int kUpdThreads = 256;
 
-int pick_vec(int nz) { return nz % 4 == 0 ? 4 : (nz % 2 == 0 ? 2 : 1); }
+int pick_vec(int nz) { return nz % 2 == 0 ? 2 : 1; }  // 4 measured slower (register pressure)
 
 int default_chunk(int nx, int ny, int nz, int sms) {
     const int vec = pick_vec(nz);
@@ -134,8 +134,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // z tile: a multiple of 4 in [8, 64] that wastes the fewest cells, the larger on ties.
 int pick_tz(int nz) {
-    int best = 64, waste = 1 << 30;
-    for (int tz = 64; tz >= 8; tz -= 4) {
+    int best = 48, waste = 1 << 30;
+    for (int tz = 48; tz >= 8; tz -= 4) {
         const int w = (nz + tz - 1) / tz * tz - nz;
         if (w < waste) { waste = w; best = tz; }
     }
@@ -222,6 +222,50 @@ int validate(const FdtdDesc* d, std::string& why) {
 
 size_t rec_elem_bytes(int dt) { return dt == 0 ? 4 : 2; }
 
+// The update of a half-step is split into the core box (no CPML cell; TMA or register-queue
+// kernel without CPML code) and up to six shell boxes (the CPML slabs; register-queue kernel
+// with the corrections), so no core warp ever waits on a scattered psi read.
+struct Box {
+    int lo[3], hi[3];
+    bool empty() const { return hi[0] <= lo[0] || hi[1] <= lo[1] || hi[2] <= lo[2]; }
+};
+
+struct Split {
+    bool split = false;  // false: one CPML launch over the whole domain
+    Box core;
+    int n_shell = 0;
+    Box shell[6];
+};
+
+Split split_boxes(const FdtdPlan* p) {
+    Split sp;
+    const Geo& g = p->g;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    int L[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        const int ax = p->slab[s].axis, side = p->d.slabs[s].direction > 0 ? 1 : 0;
+        if (L[ax][side]) return sp;  // two slabs on one face: no split
+        L[ax][side] = p->slab[s].L;
+    }
+    const int A = g.nz % 4 == 0 ? 4 : p->vec;
+    const int zlo = (L[2][0] + A - 1) / A * A, zhi = (n[2] - L[2][1]) / A * A;
+    Box core{{L[0][0], L[1][0], zlo}, {n[0] - L[0][1], n[1] - L[1][1], zhi}};
+    if (core.empty()) return sp;
+    sp.split = true;
+    sp.core = core;
+    const Box cand[6] = {
+        {{0, 0, 0}, {L[0][0], n[1], n[2]}},
+        {{n[0] - L[0][1], 0, 0}, {n[0], n[1], n[2]}},
+        {{core.lo[0], 0, 0}, {core.hi[0], L[1][0], n[2]}},
+        {{core.lo[0], n[1] - L[1][1], 0}, {core.hi[0], n[1], n[2]}},
+        {{core.lo[0], core.lo[1], 0}, {core.hi[0], core.hi[1], zlo}},
+        {{core.lo[0], core.lo[1], zhi}, {core.hi[0], core.hi[1], n[2]}},
+    };
+    for (const Box& b : cand)
+        if (!b.empty()) sp.shell[sp.n_shell++] = b;
+    return sp;
+}
+
 // The first fused detector is staged through the H pipeline when it is a phasor whose region
 // origin and z extent keep every complex tile row 16-byte aligned.
 int staged_planes(const FdtdPlan* p) {
@@ -256,10 +300,14 @@ void configure_tma(FdtdPlan* p) {
     setup((const void*)k_tma_H<true>, smH);
     cudaGetLastError();
     if (occ <= 0 || threads > 256 || threads < 32) return;
-    const long long tiles = (long long)((p->g.nz + tz - 1) / tz) * ((p->g.ny + ty - 1) / ty);
-    long long nchunks = std::max(1ll, (long long)occ * p->sm_count / tiles);
-    nchunks = std::min<long long>(nchunks, std::max(1, p->g.nx / 8));
-    p->tma_chunk = (int)((p->g.nx + nchunks - 1) / nchunks);
+    const Split sp = split_boxes(p);
+    const Box core = sp.split ? sp.core : Box{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
+    const int cx = core.hi[0] - core.lo[0], cy = core.hi[1] - core.lo[1], cz = core.hi[2] - core.lo[2];
+    const long long tiles = (long long)((cz + tz - 1) / tz) * ((cy + ty - 1) / ty);
+    // about four waves of resident blocks: long x-marches leave too few blocks in flight
+    long long nchunks = std::max(1ll, 4ll * occ * p->sm_count / tiles);
+    nchunks = std::min<long long>(nchunks, std::max(1, cx / 4));
+    p->tma_chunk = (int)((cx + nchunks - 1) / nchunks);
     p->use_tma = true;
 }
 
@@ -293,7 +341,6 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         p->chunk = default_chunk(d.nx, d.ny, d.nz, p->sm_count);
         p->vec = pick_vec(d.nz);
         p->tma_ok = d.nz % 4 == 0 && d.nz >= 8 && !d.periodic[0] && !d.periodic[1] && !d.periodic[2] && encode_fn();
-        p->tma_tz = pick_tz(d.nz);
         p->tma_ty = 8;
     }
 
@@ -445,6 +492,10 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         p->d.detectors[q].slot = nullptr;
         p->d.detectors[q].weights = nullptr;
     }
+    {
+        const Split sp = split_boxes(p);
+        p->tma_tz = pick_tz(sp.split ? sp.core.hi[2] - sp.core.lo[2] : p->g.nz);
+    }
     configure_tma(p);
     *out = p;
     return FDTD_OK;
@@ -527,30 +578,57 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     if (nsig && !make_map(&mS, a.sig, nsig, g, tz, ty, nsig)) return false;
     UpdArgs aa = a;
     aa.chunk = p->tma_chunk;
-    const dim3 grid((g.nz + tz - 1) / tz, (g.ny + ty - 1) / ty, (g.nx + aa.chunk - 1) / aa.chunk);
+    const int bx = aa.hi[0] - aa.lo[0], by = aa.hi[1] - aa.lo[1], bz = aa.hi[2] - aa.lo[2];
+    const dim3 grid((bz + tz - 1) / tz, (by + ty - 1) / ty, (bx + aa.chunk - 1) / aa.chunk);
     const dim3 block(ty * tz / 2);
     if (HSIDE) k_tma_H<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
     else k_tma_E<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
     return true;
 }
 
-template <bool REV>
-void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
-    if (p->use_tma && launch_tma<REV, false>(p, a, st)) return;
-    const dim3 grid = update_grid(p);
-    if (p->vec == 4) k_update_E<REV, 4><<<grid, kUpdBlock, 0, st>>>(a);
-    else if (p->vec == 2) k_update_E<REV, 2><<<grid, kUpdBlock, 0, st>>>(a);
-    else k_update_E<REV, 1><<<grid, kUpdBlock, 0, st>>>(a);
+constexpr int kShellChunk = 4;
+
+template <bool REV, bool HSIDE, bool PML>
+void launch_plain_box(const FdtdPlan* p, UpdArgs a, const Box& b, int chunk, cudaStream_t st) {
+    for (int x = 0; x < 3; ++x) { a.lo[x] = b.lo[x]; a.hi[x] = b.hi[x]; }
+    a.chunk = chunk;
+    const long long cols = (long long)(b.hi[1] - b.lo[1]) * ((b.hi[2] - b.lo[2]) / p->vec);
+    const dim3 grid((unsigned)((cols + kUpdThreads - 1) / kUpdThreads), (b.hi[0] - b.lo[0] + chunk - 1) / chunk, 1);
+    if (HSIDE) {
+        if (p->vec == 4) k_update_H<REV, 4, PML><<<grid, kUpdBlock, 0, st>>>(a);
+        else if (p->vec == 2) k_update_H<REV, 2, PML><<<grid, kUpdBlock, 0, st>>>(a);
+        else k_update_H<REV, 1, PML><<<grid, kUpdBlock, 0, st>>>(a);
+    } else {
+        if (p->vec == 4) k_update_E<REV, 4, PML><<<grid, kUpdBlock, 0, st>>>(a);
+        else if (p->vec == 2) k_update_E<REV, 2, PML><<<grid, kUpdBlock, 0, st>>>(a);
+        else k_update_E<REV, 1, PML><<<grid, kUpdBlock, 0, st>>>(a);
+    }
+}
+
+template <bool REV, bool HSIDE>
+void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+    const Split sp = split_boxes(p);
+    if (!sp.split) {
+        const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
+        launch_plain_box<REV, HSIDE, true>(p, a, all, p->chunk, st);
+        return;
+    }
+    UpdArgs ac = a;
+    for (int x = 0; x < 3; ++x) { ac.lo[x] = sp.core.lo[x]; ac.hi[x] = sp.core.hi[x]; }
+    if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_box<REV, HSIDE, false>(p, a, sp.core, p->chunk, st);
+    for (int q = 0; q < sp.n_shell; ++q) launch_plain_box<REV, HSIDE, true>(p, a, sp.shell[q], kShellChunk, st);
+}
+
+int half_step_launches(const FdtdPlan* p) {
+    const Split sp = split_boxes(p);
+    return sp.split ? 1 + sp.n_shell : 1;
 }
 
 template <bool REV>
-void launch_H(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
-    if (p->use_tma && launch_tma<REV, true>(p, a, st)) return;
-    const dim3 grid = update_grid(p);
-    if (p->vec == 4) k_update_H<REV, 4><<<grid, kUpdBlock, 0, st>>>(a);
-    else if (p->vec == 2) k_update_H<REV, 2><<<grid, kUpdBlock, 0, st>>>(a);
-    else k_update_H<REV, 1><<<grid, kUpdBlock, 0, st>>>(a);
-}
+void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) { launch_half<REV, false>(p, a, st); }
+
+template <bool REV>
+void launch_H(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) { launch_half<REV, true>(p, a, st); }
 
 UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout) {
     UpdArgs a{};
@@ -574,6 +652,8 @@ UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const floa
     a.chunk = p->chunk;
     a.tp = p->d_t;
     a.n_fuse = 0;
+    a.lo[0] = a.lo[1] = a.lo[2] = 0;
+    a.hi[0] = p->g.nx; a.hi[1] = p->g.ny; a.hi[2] = p->g.nz;
     return a;
 }
 
@@ -677,7 +757,7 @@ extern "C" {
 
 int32_t fdtd_launches_per_step(const FdtdPlan* p) {
     if (!p) return 0;
-    int n = 2 + sources_launched(p, true) + sources_launched(p, false) + 1;
+    int n = 2 * half_step_launches(p) + sources_launched(p, true) + sources_launched(p, false) + 1;
     if (p->d.record_interfaces && p->d.n_slabs) n += 1;
     for (int q = 0; q < p->d.n_detectors; ++q)
         if (!p->fused[q]) n += p->det[q].reduce ? 2 : 1;
@@ -883,7 +963,10 @@ extern "C" int32_t fdtd_plan_vec(const FdtdPlan* p) { return p ? p->vec : 0; }
 extern "C" int fdtd_plan_tune_tma(FdtdPlan* p, int32_t enable, int32_t tz, int32_t ty, int32_t stages, int32_t chunk) {
     if (!p) return FDTD_EINVAL;
     if (enable && !p->tma_ok) return fail(p, FDTD_EINVAL, "this scene cannot use the TMA kernels (periodic axis or nz % 4 != 0)");
-    if (tz <= 0) tz = pick_tz(p->g.nz);
+    if (tz <= 0) {
+        const Split sp = split_boxes(p);
+        tz = pick_tz(sp.split ? sp.core.hi[2] - sp.core.lo[2] : p->g.nz);
+    }
     if (ty <= 0) ty = 8;
     if (stages <= 0) stages = 4;
     if (tz % 4 || tz < 8 || tz > 120 || ty < 1 || ty * tz / 2 > 256 || stages < 2 || stages > kMaxStages)

@@ -7,7 +7,9 @@
 // stage's mbarrier; NS stages are in flight, so the data waiting on HBM lives in
 // shared memory instead of registers.  Out-of-range tile cells read as zero (TMA
 // fill), which is exactly the reference's zero halo (fdtdx/core/misc.py:615-641);
-// scenes with a periodic axis use the register-queue kernels instead.
+// scenes with a periodic axis use the register-queue kernels instead.  These kernels
+// update the core box of the grid, which holds no CPML cell; the slabs are updated by
+// the register-queue kernels with their CPML corrections.
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the plan's error word to
 // FDTD_ETIMEOUT, the block learns it through __syncthreads_or, the elected thread waits
@@ -103,11 +105,11 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    const int kt = blockIdx.x * TZ, jt = blockIdx.y * TY;
-    const int i0 = blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, g.nx);
+    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < g.nz && j < g.ny;
+    const bool valid = k0 < a.hi[2] && j < a.hi[1];
     const long long N = g.N;
 
     if (tid == 0) {
@@ -129,12 +131,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     float Hy_m[2] = {0.f, 0.f}, Hz_m[2] = {0.f, 0.f};
-    PsiPre pre[2];
-    bool pml = valid && a.n_slab > 0 && maybe_slab(a, i0, j, k0, 2);
-    if (pml) {
-        psi_fetch(a, i0, j, k0, pre[0]);
-        psi_fetch(a, i0, j, k0 + 1, pre[1]);
-    }
     for (int p = 0; p < P; ++p) {
         const int s = p % NS;
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
@@ -166,8 +162,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 const float d[6] = {Hz - Hz_jm, Hy - Hy_km, Hx - Hx_km, Hz - Hz_m[e], Hy - Hy_m[e], Hx - Hx_jm};
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
-                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (pml) cpml_apply<REV, false>(a, i, j, k0 + e, d, cu, pre[e]);
+                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -188,14 +183,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            // psi of the next plane, fetched while the pipeline delivers it
-            if (i + 1 < i1) {
-                pml = a.n_slab > 0 && maybe_slab(a, i + 1, j, k0, 2);
-                if (pml) {
-                    psi_fetch(a, i + 1, j, k0, pre[0]);
-                    psi_fetch(a, i + 1, j, k0 + 1, pre[1]);
-                }
-            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -232,11 +219,11 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    const int kt = blockIdx.x * TZ, jt = blockIdx.y * TY;
-    const int i0 = blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, g.nx);
+    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < g.nz && j < g.ny;
+    const bool valid = k0 < a.hi[2] && j < a.hi[1];
     const long long N = g.N;
 
     int slot[kMaxFuse];
@@ -276,12 +263,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     bool ok = mbar_wait_bounded(&bar[0], 0);
-    PsiPre pre[2];
-    bool pml = valid && a.n_slab > 0 && maybe_slab(a, i0, j, k0, 2);
-    if (pml) {
-        psi_fetch(a, i0, j, k0, pre[0]);
-        psi_fetch(a, i0, j, k0 + 1, pre[1]);
-    }
     // Ex(i-1) at k and k+1 of this thread's two cells (fused co-location), seeded at the chunk start
     float Exm[3] = {0.f, 0.f, 0.f};
     if (any && valid) {
@@ -318,8 +299,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ez_ip = E1[(2 * EY + r0) * EZ + kk];
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
-                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (pml) cpml_apply<REV, true>(a, i, j, k0 + e, d, cu, pre[e]);
+                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -349,13 +329,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (i + 1 < i1) {
-                pml = a.n_slab > 0 && maybe_slab(a, i + 1, j, k0, 2);
-                if (pml) {
-                    psi_fetch(a, i + 1, j, k0, pre[0]);
-                    psi_fetch(a, i + 1, j, k0 + 1, pre[1]);
-                }
-            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
