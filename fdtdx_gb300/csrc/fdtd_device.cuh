@@ -63,7 +63,11 @@ struct UpdArgs {
     float* psi1[FDTD_MAX_SLABS];
     float* psi2[FDTD_MAX_SLABS];
     int chunk;                  // x planes per block (the block marches along x)
-    int lo[3], hi[3];           // the box of cells this launch updates
+    int lo[3], hi[3];           // the box of cells a TMA launch updates
+    // the boxes a register-queue launch updates: its 1-D grid is cut into nbox ranges of
+    // blocks, box b owning blocks [bstart[b], bstart[b+1]) laid out as (nbx[b] columns) x (x chunks)
+    int nbox;
+    int blo[6][3], bhi[6][3], bchunk[6], nbx[6], bstart[7];
     const int* tp;              // device time-step counter
     int n_fuse;
     DFuse fuse[kMaxFuse];

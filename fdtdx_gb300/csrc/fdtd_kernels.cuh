@@ -17,43 +17,8 @@ namespace fdtd {
 // fdtdx/objects/boundaries/perfectly_matched_layer.py:138-190).  d[] holds the six raw
 // differences in the order (dy Fz, dz Fy, dz Fx, dx Fz, dx Fy, dy Fx); for a slab on axis a
 // d_a F_j and d_a F_i are (3, 4), (5, 0), (1, 2) and the corrections go to
-// curl[(a+1)%3] (minus) and curl[(a+2)%3] (plus).
-template <bool REV, bool HSIDE>
-__device__ __forceinline__ void cpml_correct(const UpdArgs& a, int i, int j, int k, const float d[6], float cu[3]) {
-    const int idx3[3] = {i, j, k};
-#pragma unroll
-    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
-        if (s >= a.n_slab) break;
-        const DSlab& sl = a.slab[s];
-        const int l = idx3[sl.axis] - sl.lo;
-        if ((unsigned)l >= (unsigned)sl.L) continue;
-        const float d1 = sl.axis == 0 ? d[3] : (sl.axis == 1 ? d[5] : d[1]);
-        const float d2 = sl.axis == 0 ? d[4] : (sl.axis == 1 ? d[0] : d[2]);
-        const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
-        const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
-        const long long p = ((long long)(i - (sl.axis == 0 ? sl.lo : 0)) * sl.sy + (j - (sl.axis == 1 ? sl.lo : 0))) * sl.sz +
-                            (k - (sl.axis == 2 ? sl.lo : 0));
-        float p1 = a.psi1[s][p], p2 = a.psi2[s][p];
-        if (!REV) {
-            p1 = cb * p1 + ca * d1;
-            p2 = cb * p2 + ca * d2;
-            a.psi1[s][p] = p1;
-            a.psi2[s][p] = p2;
-        }
-        float c1 = p1, c2 = p2;
-        if (!sl.kappa_one) {
-            const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
-            c1 = ikm1 * d1 + p1;
-            c2 = ikm1 * d2 + p2;
-        }
-        if (sl.axis == 0) { cu[1] -= c1; cu[2] += c2; }
-        else if (sl.axis == 1) { cu[2] -= c1; cu[0] += c2; }
-        else { cu[0] -= c1; cu[1] += c2; }
-    }
-}
-
-// CPML psi of one cell fetched ahead of its use (one plane early in the TMA kernels, so
-// the latency of these scattered slab reads overlaps the previous plane's work).
+// curl[(a+1)%3] (minus) and curl[(a+2)%3] (plus).  psi is fetched by psi_fetch before the
+// differences are formed, so its scattered slab reads overlap the field loads.
 struct PsiPre {
     float v[FDTD_MAX_SLABS][2];
 };
@@ -214,16 +179,31 @@ __device__ __forceinline__ float material_update(const UpdArgs& a, float u0, flo
 
 // Column decomposition shared by both half-steps: a thread owns VEC consecutive z cells
 // of one (j) row and marches over the block's `chunk` x planes.
-// (the launch's box has VEC-aligned z bounds)
+// The block's box, its column (j, k0) and its x range [i0, i1).  Boxes have VEC-aligned z
+// bounds; the box table is indexed with unrolled static indices (no dynamic param access).
 template <int VEC>
-__device__ __forceinline__ bool column_of(const UpdArgs& a, int& j, int& k0) {
-    const int nq = (a.hi[2] - a.lo[2]) / VEC;
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (long long)(a.hi[1] - a.lo[1]) * nq) return false;
+__device__ __forceinline__ bool column_of(const UpdArgs& a, int& j, int& k0, int& i0, int& i1) {
+    const int b = blockIdx.x;
+    int lo0 = 0, lo1 = 0, lo2 = 0, hi0 = 0, hi1 = 0, hi2 = 0, chunk = 1, nbx = 1, start = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        if (q < a.nbox && b >= a.bstart[q]) {
+            lo0 = a.blo[q][0]; lo1 = a.blo[q][1]; lo2 = a.blo[q][2];
+            hi0 = a.bhi[q][0]; hi1 = a.bhi[q][1]; hi2 = a.bhi[q][2];
+            chunk = a.bchunk[q]; nbx = a.nbx[q]; start = a.bstart[q];
+        }
+    }
+    const int lb = b - start;
+    const int bx = lb % nbx, by = lb / nbx;
+    const int nq = (hi2 - lo2) / VEC;
+    const long long q = (long long)bx * blockDim.x + threadIdx.x;
+    if (q >= (long long)(hi1 - lo1) * nq) return false;
     const int jj = (int)(q / nq);
-    j = a.lo[1] + jj;
-    k0 = a.lo[2] + (int)(q - (long long)jj * nq) * VEC;
-    return true;
+    j = lo1 + jj;
+    k0 = lo2 + (int)(q - (long long)jj * nq) * VEC;
+    i0 = lo0 + by * chunk;
+    i1 = min(i0 + chunk, hi0);
+    return i0 < i1;
 }
 
 // ---------------------------------------------------------------------------------
@@ -233,10 +213,8 @@ __device__ __forceinline__ bool column_of(const UpdArgs& a, int& j, int& k0) {
 template <bool REV, int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
     const Geo& g = a.g;
-    int j, k0;
-    if (!column_of<VEC>(a, j, k0)) return;
-    const int i0 = a.lo[0] + blockIdx.y * a.chunk;
-    const int i1 = min(i0 + a.chunk, a.hi[0]);
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
     const long long N = g.N;
     const long long sy = g.nz;
     const float* __restrict__ H = a.F;
@@ -265,6 +243,11 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) Eo[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
         const bool pml = PML && a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        PsiPre pre[VEC];
+        if (pml) {  // issued with the field loads, so both round trips overlap
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e]);
+        }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
             const int k = k0 + e;
@@ -273,7 +256,7 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
             const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
                                 Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
             float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-            if (pml) cpml_correct<REV, false>(a, i, j, k, d, cu);
+            if (pml) cpml_apply<REV, false>(a, i, j, k, d, cu, pre[e]);
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
@@ -356,10 +339,8 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
 template <bool REV, int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
     const Geo& g = a.g;
-    int j, k0;
-    if (!column_of<VEC>(a, j, k0)) return;
-    const int i0 = a.lo[0] + blockIdx.y * a.chunk;
-    const int i1 = min(i0 + a.chunk, a.hi[0]);
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
     const long long N = g.N;
     const long long sy = g.nz, sx = (long long)g.ny * g.nz;
     const float* __restrict__ E = a.F;
@@ -415,6 +396,11 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) Ho[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
         const bool pml = PML && a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        PsiPre pre[VEC];
+        if (pml) {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e]);
+        }
         Vec<VEC> Ey_jm{};
         float Eyk_jm = 0.f;
         if (!REV && any) {
@@ -429,7 +415,7 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
             const float d[6] = {Ez_jp.v[e] - Ez.v[e], ey_kp - Ey.v[e], ex_kp - Ex.v[e],
                                 Ez_ip.v[e] - Ez.v[e], Ey_ip.v[e] - Ey.v[e], Ex_jp.v[e] - Ex.v[e]};
             float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-            if (pml) cpml_correct<REV, true>(a, i, j, k, d, cu);
+            if (pml) cpml_apply<REV, true>(a, i, j, k, d, cu, pre[e]);
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;

@@ -523,11 +523,6 @@ int64_t fdtd_plan_device_bytes(const FdtdPlan* p) { return p ? (int64_t)p->dmem_
 // -------------------------------------------------------------------------------------
 namespace {
 
-dim3 update_grid(const FdtdPlan* p) {
-    const Geo& g = p->g;
-    const long long cols = (long long)g.ny * (g.nz / p->vec);
-    return dim3((unsigned)((cols + kUpdThreads - 1) / kUpdThreads), (g.nx + p->chunk - 1) / p->chunk, 1);
-}
 const dim3 kUpdBlock(kUpdThreads, 1, 1);
 
 bool make_map(CUtensorMap* m, const float* base, int ncomp, const Geo& g, int bz, int by, int bc) {
@@ -588,12 +583,30 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
 
 constexpr int kShellChunk = 4;
 
+// Fills the launch's box table; returns the number of blocks of the 1-D grid.
+long long fill_boxes(const FdtdPlan* p, UpdArgs& a, const Box* boxes, const int* chunks, int n) {
+    a.nbox = n;
+    long long start = 0;
+    for (int q = 0; q < n; ++q) {
+        const Box& b = boxes[q];
+        for (int x = 0; x < 3; ++x) { a.blo[q][x] = b.lo[x]; a.bhi[q][x] = b.hi[x]; }
+        const long long cols = (long long)(b.hi[1] - b.lo[1]) * ((b.hi[2] - b.lo[2]) / p->vec);
+        const int nbx = (int)((cols + kUpdThreads - 1) / kUpdThreads);
+        const int nby = (b.hi[0] - b.lo[0] + chunks[q] - 1) / chunks[q];
+        a.bchunk[q] = chunks[q];
+        a.nbx[q] = nbx;
+        a.bstart[q] = (int)start;
+        start += (long long)nbx * nby;
+    }
+    a.bstart[n] = (int)start;
+    return start;
+}
+
 template <bool REV, bool HSIDE, bool PML>
-void launch_plain_box(const FdtdPlan* p, UpdArgs a, const Box& b, int chunk, cudaStream_t st) {
-    for (int x = 0; x < 3; ++x) { a.lo[x] = b.lo[x]; a.hi[x] = b.hi[x]; }
-    a.chunk = chunk;
-    const long long cols = (long long)(b.hi[1] - b.lo[1]) * ((b.hi[2] - b.lo[2]) / p->vec);
-    const dim3 grid((unsigned)((cols + kUpdThreads - 1) / kUpdThreads), (b.hi[0] - b.lo[0] + chunk - 1) / chunk, 1);
+void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const int* chunks, int n, cudaStream_t st) {
+    const long long blocks = fill_boxes(p, a, boxes, chunks, n);
+    if (blocks <= 0) return;
+    const dim3 grid((unsigned)blocks, 1, 1);
     if (HSIDE) {
         if (p->vec == 4) k_update_H<REV, 4, PML><<<grid, kUpdBlock, 0, st>>>(a);
         else if (p->vec == 2) k_update_H<REV, 2, PML><<<grid, kUpdBlock, 0, st>>>(a);
@@ -610,18 +623,20 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     const Split sp = split_boxes(p);
     if (!sp.split) {
         const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
-        launch_plain_box<REV, HSIDE, true>(p, a, all, p->chunk, st);
+        launch_plain_boxes<REV, HSIDE, true>(p, a, &all, &p->chunk, 1, st);
         return;
     }
     UpdArgs ac = a;
     for (int x = 0; x < 3; ++x) { ac.lo[x] = sp.core.lo[x]; ac.hi[x] = sp.core.hi[x]; }
-    if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_box<REV, HSIDE, false>(p, a, sp.core, p->chunk, st);
-    for (int q = 0; q < sp.n_shell; ++q) launch_plain_box<REV, HSIDE, true>(p, a, sp.shell[q], kShellChunk, st);
+    if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
+    int chunks[6];
+    for (int q = 0; q < sp.n_shell; ++q) chunks[q] = kShellChunk;
+    launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st);
 }
 
 int half_step_launches(const FdtdPlan* p) {
     const Split sp = split_boxes(p);
-    return sp.split ? 1 + sp.n_shell : 1;
+    return sp.split ? 1 + (sp.n_shell > 0) : 1;
 }
 
 template <bool REV>
