@@ -28,7 +28,6 @@ __device__ __forceinline__ long long psi_offset(const DSlab& sl, int i, int j, i
            (k - (sl.axis == 2 ? sl.lo : 0));
 }
 
-template <int AXMASK = 7>
 __device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k, PsiPre& pr) {
     const int idx3[3] = {i, j, k};
 #pragma unroll
@@ -37,7 +36,6 @@ __device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k,
         pr.v[s][1] = 0.f;
         if (s >= a.n_slab) continue;
         const DSlab& sl = a.slab[s];
-        if (!((AXMASK >> sl.axis) & 1)) continue;
         const int l = idx3[sl.axis] - sl.lo;
         if ((unsigned)l >= (unsigned)sl.L) continue;
         const long long p = psi_offset(sl, i, j, k);
@@ -47,7 +45,7 @@ __device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k,
 }
 
 // cpml_correct with the psi values taken from a prefetch.
-template <bool REV, bool HSIDE, int AXMASK = 7>
+template <bool REV, bool HSIDE>
 __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k, const float d[6], float cu[3],
                                            const PsiPre& pr) {
     const int idx3[3] = {i, j, k};
@@ -55,7 +53,6 @@ __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k
     for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
         if (s >= a.n_slab) break;
         const DSlab& sl = a.slab[s];
-        if (!((AXMASK >> sl.axis) & 1)) continue;
         const int l = idx3[sl.axis] - sl.lo;
         if ((unsigned)l >= (unsigned)sl.L) continue;
         const float d1 = sl.axis == 0 ? d[3] : (sl.axis == 1 ? d[5] : d[1]);
@@ -156,19 +153,6 @@ __device__ __forceinline__ bool maybe_slab(const UpdArgs& a, int i, int j, int k
         const DSlab& sl = a.slab[s];
         const int lo = idx[sl.axis] - sl.lo;
         const int hi = lo + (sl.axis == 2 ? vec - 1 : 0);
-        if (hi >= 0 && lo < sl.L) return true;
-    }
-    return false;
-}
-
-// Whether z cells k0 .. k0+vec-1 can lie in a z-axis CPML slab.
-__device__ __forceinline__ bool maybe_slab_z(const UpdArgs& a, int k0, int vec) {
-#pragma unroll
-    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
-        if (s >= a.n_slab) break;
-        const DSlab& sl = a.slab[s];
-        if (sl.axis != 2) continue;
-        const int lo = k0 - sl.lo, hi = lo + vec - 1;
         if (hi >= 0 && lo < sl.L) return true;
     }
     return false;
@@ -419,31 +403,9 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
         }
         Vec<VEC> Ey_jm{};
         float Eyk_jm = 0.f;
-        // previous phasor values of the first fused detector, loaded with this plane's fields
-        float ph_old[VEC][3][2];
-        bool ph_pre = false;
         if (!REV && any) {
             Ey_jm = nbv<VEC>(g, E, N + c - sy, j > 0, 1, i, j - 1, k0);
             Eyk_jm = ld_halo(g, E, 1, i, j - 1, k0 + VEC);
-            const DFuse& d0 = a.fuse[0];
-            if (slot[0] >= 0 && d0.kind == FDTD_DET_PHASOR && d0.nfreq == 1 && d0.nout <= 3) {
-                ph_pre = true;
-                const float2* st = reinterpret_cast<const float2*>(d0.state);
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) {
-                    const int k = k0 + e;
-                    const bool in = i >= d0.lo[0] && i < d0.hi[0] && j >= d0.lo[1] && j < d0.hi[1] && k >= d0.lo[2] &&
-                                    k < d0.hi[2];
-                    const long long r = ((long long)(i - d0.lo[0]) * d0.ry + (j - d0.lo[1])) * d0.rz + (k - d0.lo[2]);
-#pragma unroll
-                    for (int o = 0; o < 3; ++o) {
-                        float2 z = make_float2(0.f, 0.f);
-                        if (in && o < d0.nout) z = st[(long long)o * d0.R + r];
-                        ph_old[e][o][0] = z.x;
-                        ph_old[e][o][1] = z.y;
-                    }
-                }
-            }
         }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
@@ -465,7 +427,7 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
                 const float exkp_im = e + 1 < VEC ? Ex_im.v[e + 1] : Exk_im;
                 const float eykp_jm = e + 1 < VEC ? Ey_jm.v[e + 1] : Eyk_jm;
                 fused_detectors(a, slot, w, i, j, k, Ex.v[e], ex_kp, Ex_im.v[e], exkp_im, Ey.v[e], ey_kp, Ey_jm.v[e],
-                                eykp_jm, Ez.v[e], ph_pre ? &ph_old[e][0][0] : nullptr, 2);
+                                eykp_jm, Ez.v[e]);
             }
         }
 #pragma unroll

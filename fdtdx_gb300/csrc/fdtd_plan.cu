@@ -237,11 +237,8 @@ struct Split {
     Box shell[6];
 };
 
-// With the TMA kernels the core spans the whole z range (they apply the z slabs' CPML);
-// otherwise the z slabs are shell boxes too.
 Split split_boxes(const FdtdPlan* p) {
     Split sp;
-    const bool zcore = p->use_tma;
     const Geo& g = p->g;
     const int n[3] = {g.nx, g.ny, g.nz};
     int L[3][2] = {{0, 0}, {0, 0}, {0, 0}};
@@ -251,7 +248,7 @@ Split split_boxes(const FdtdPlan* p) {
         L[ax][side] = p->slab[s].L;
     }
     const int A = g.nz % 4 == 0 ? 4 : p->vec;
-    const int zlo = zcore ? 0 : (L[2][0] + A - 1) / A * A, zhi = zcore ? n[2] : (n[2] - L[2][1]) / A * A;
+    const int zlo = (L[2][0] + A - 1) / A * A, zhi = (n[2] - L[2][1]) / A * A;
     Box core{{L[0][0], L[1][0], zlo}, {n[0] - L[0][1], n[1] - L[1][1], zhi}};
     if (core.empty()) return sp;
     sp.split = true;
@@ -303,9 +300,7 @@ void configure_tma(FdtdPlan* p) {
     setup((const void*)k_tma_H<true>, smH);
     cudaGetLastError();
     if (occ <= 0 || threads > 256 || threads < 32) return;
-    p->use_tma = true;  // the core box depends on it
     const Split sp = split_boxes(p);
-    p->use_tma = false;
     const Box core = sp.split ? sp.core : Box{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
     const int cx = core.hi[0] - core.lo[0], cy = core.hi[1] - core.lo[1], cz = core.hi[2] - core.lo[2];
     const long long tiles = (long long)((cz + tz - 1) / tz) * ((cy + ty - 1) / ty);
@@ -497,7 +492,10 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         p->d.detectors[q].slot = nullptr;
         p->d.detectors[q].weights = nullptr;
     }
-    p->tma_tz = pick_tz(p->g.nz);
+    {
+        const Split sp = split_boxes(p);
+        p->tma_tz = pick_tz(sp.split ? sp.core.hi[2] - sp.core.lo[2] : p->g.nz);
+    }
     configure_tma(p);
     *out = p;
     return FDTD_OK;
@@ -980,7 +978,10 @@ extern "C" int32_t fdtd_plan_vec(const FdtdPlan* p) { return p ? p->vec : 0; }
 extern "C" int fdtd_plan_tune_tma(FdtdPlan* p, int32_t enable, int32_t tz, int32_t ty, int32_t stages, int32_t chunk) {
     if (!p) return FDTD_EINVAL;
     if (enable && !p->tma_ok) return fail(p, FDTD_EINVAL, "this scene cannot use the TMA kernels (periodic axis or nz % 4 != 0)");
-    if (tz <= 0) tz = pick_tz(p->g.nz);
+    if (tz <= 0) {
+        const Split sp = split_boxes(p);
+        tz = pick_tz(sp.split ? sp.core.hi[2] - sp.core.lo[2] : p->g.nz);
+    }
     if (ty <= 0) ty = 8;
     if (stages <= 0) stages = 4;
     if (tz % 4 || tz < 8 || tz > 120 || ty < 1 || ty * tz / 2 > 256 || stages < 2 || stages > kMaxStages)

@@ -8,10 +8,8 @@
 // shared memory instead of registers.  Out-of-range tile cells read as zero (TMA
 // fill), which is exactly the reference's zero halo (fdtdx/core/misc.py:615-641);
 // scenes with a periodic axis use the register-queue kernels instead.  These kernels
-// update the core box of the grid: every x and y position outside the x and y CPML slabs,
-// over the whole z range.  The z slabs' corrections are applied here (a thread's z is
-// fixed, so it fetches its psi one plane ahead); the x and y slabs are updated by the
-// register-queue kernels.
+// update the core box of the grid, which holds no CPML cell; the slabs are updated by
+// the register-queue kernels with their CPML corrections.
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the plan's error word to
 // FDTD_ETIMEOUT, the block learns it through __syncthreads_or, the elected thread waits
@@ -133,13 +131,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     float Hy_m[2] = {0.f, 0.f}, Hz_m[2] = {0.f, 0.f};
-    // z-slab CPML: this thread's column lies in a z slab or not for every plane
-    const bool zpml = valid && a.n_slab > 0 && maybe_slab_z(a, k0, 2);
-    PsiPre pre[2];
-    if (zpml) {
-        psi_fetch<4>(a, i0, j, k0, pre[0]);
-        psi_fetch<4>(a, i0, j, k0 + 1, pre[1]);
-    }
     for (int p = 0; p < P; ++p) {
         const int s = p % NS;
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
@@ -171,8 +162,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 const float d[6] = {Hz - Hz_jm, Hy - Hy_km, Hx - Hx_km, Hz - Hz_m[e], Hy - Hy_m[e], Hx - Hx_jm};
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
-                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (zpml) cpml_apply<REV, false, 4>(a, i, j, k0 + e, d, cu, pre[e]);
+                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -193,10 +183,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (zpml && i + 1 < i1) {  // psi of the next plane, fetched while the pipeline delivers it
-                psi_fetch<4>(a, i + 1, j, k0, pre[0]);
-                psi_fetch<4>(a, i + 1, j, k0 + 1, pre[1]);
-            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -277,12 +263,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     bool ok = mbar_wait_bounded(&bar[0], 0);
-    const bool zpml = valid && a.n_slab > 0 && maybe_slab_z(a, k0, 2);
-    PsiPre pre[2];
-    if (zpml) {
-        psi_fetch<4>(a, i0, j, k0, pre[0]);
-        psi_fetch<4>(a, i0, j, k0 + 1, pre[1]);
-    }
     // Ex(i-1) at k and k+1 of this thread's two cells (fused co-location), seeded at the chunk start
     float Exm[3] = {0.f, 0.f, 0.f};
     if (any && valid) {
@@ -319,8 +299,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ez_ip = E1[(2 * EY + r0) * EZ + kk];
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
-                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (zpml) cpml_apply<REV, true, 4>(a, i, j, k0 + e, d, cu, pre[e]);
+                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -350,10 +329,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (zpml && i + 1 < i1) {
-                psi_fetch<4>(a, i + 1, j, k0, pre[0]);
-                psi_fetch<4>(a, i + 1, j, k0 + 1, pre[1]);
-            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
