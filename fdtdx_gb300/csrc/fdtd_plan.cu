@@ -235,7 +235,6 @@ struct Split {
     Box core;
     int n_shell = 0;
     Box shell[6];
-    bool shell_is_z[6] = {};
 };
 
 Split split_boxes(const FdtdPlan* p) {
@@ -262,11 +261,8 @@ Split split_boxes(const FdtdPlan* p) {
         {{core.lo[0], core.lo[1], 0}, {core.hi[0], core.hi[1], zlo}},
         {{core.lo[0], core.lo[1], zhi}, {core.hi[0], core.hi[1], n[2]}},
     };
-    for (int q = 0; q < 6; ++q)
-        if (!cand[q].empty()) {
-            sp.shell_is_z[sp.n_shell] = q >= 4;
-            sp.shell[sp.n_shell++] = cand[q];
-        }
+    for (const Box& b : cand)
+        if (!b.empty()) sp.shell[sp.n_shell++] = b;
     return sp;
 }
 
@@ -292,24 +288,16 @@ void configure_tma(FdtdPlan* p) {
     const size_t smE = tma_smem(tma_cfg(tz, ty, ns, false, nmE, nsE, nullptr));
     const size_t smH = tma_smem(tma_cfg(tz, ty, ns, true, nmH, nsH, nullptr, staged_planes(p)));
     int occ = 1 << 30;
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    auto setup = [&](const void* fn, size_t sm, bool core) {
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-        if (!core) return;
+    auto setup = [&](const void* fn, size_t sm) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, sm) != cudaSuccess) nb = 0;
         occ = std::min(occ, nb);
     };
-    setup((const void*)k_tma_E<false, false>, smE, true);
-    setup((const void*)k_tma_E<true, false>, smE, true);
-    setup((const void*)k_tma_H<false, false>, smH, true);
-    setup((const void*)k_tma_H<true, false>, smH, true);
-    setup((const void*)k_tma_E<false, true>, smE, false);
-    setup((const void*)k_tma_E<true, true>, smE, false);
-    setup((const void*)k_tma_H<false, true>, smH, false);
-    setup((const void*)k_tma_H<true, true>, smH, false);
+    setup((const void*)k_tma_E<false>, smE);
+    setup((const void*)k_tma_E<true>, smE);
+    setup((const void*)k_tma_H<false>, smH);
+    setup((const void*)k_tma_H<true>, smH);
     cudaGetLastError();
     if (occ <= 0 || threads > 256 || threads < 32) return;
     const Split sp = split_boxes(p);
@@ -549,12 +537,12 @@ bool make_map(CUtensorMap* m, const float* base, int ncomp, const Geo& g, int bz
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Launch of a TMA-pipelined half-step over `n` boxes with a ty x tz tile; false when a
-// tensor map cannot be built (the caller then uses the register-queue kernel).
-template <bool REV, bool HSIDE, bool PML>
-bool launch_tma(const FdtdPlan* p, const UpdArgs& a, const Box* boxes, int n, int tz, int ty, int chunk,
-                cudaStream_t st) {
+// Launch of a TMA-pipelined half-step; false when a tensor map cannot be built (the caller
+// then uses the register-queue kernel).
+template <bool REV, bool HSIDE>
+bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     const Geo& g = p->g;
+    const int tz = p->tma_tz, ty = p->tma_ty;
     const int nm = a.mat ? a.n_mat : 0, nsig = a.sig ? a.n_sig : 0;
     // the staged phasor tile of the first fused detector (forward H step only)
     int nd = 0;
@@ -584,21 +572,12 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, const Box* boxes, int n, in
     if (nm && !make_map(&mM, a.mat, nm, g, tz, ty, nm)) return false;
     if (nsig && !make_map(&mS, a.sig, nsig, g, tz, ty, nsig)) return false;
     UpdArgs aa = a;
-    aa.nbox = n;
-    long long blocks = 0;
-    for (int q = 0; q < n; ++q) {
-        const Box& b = boxes[q];
-        for (int x = 0; x < 3; ++x) { aa.blo[q][x] = b.lo[x]; aa.bhi[q][x] = b.hi[x]; }
-        aa.bchunk[q] = chunk;
-        aa.bstart[q] = (int)blocks;
-        const long long ntz = (b.hi[2] - b.lo[2] + tz - 1) / tz, nty = (b.hi[1] - b.lo[1] + ty - 1) / ty;
-        blocks += ntz * nty * ((b.hi[0] - b.lo[0] + chunk - 1) / chunk);
-    }
-    aa.bstart[n] = (int)blocks;
-    if (blocks <= 0) return true;
-    const dim3 grid((unsigned)blocks), block(ty * tz / 2);
-    if (HSIDE) k_tma_H<REV, PML><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
-    else k_tma_E<REV, PML><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
+    aa.chunk = p->tma_chunk;
+    const int bx = aa.hi[0] - aa.lo[0], by = aa.hi[1] - aa.lo[1], bz = aa.hi[2] - aa.lo[2];
+    const dim3 grid((bz + tz - 1) / tz, (by + ty - 1) / ty, (bx + aa.chunk - 1) / aa.chunk);
+    const dim3 block(ty * tz / 2);
+    if (HSIDE) k_tma_H<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
+    else k_tma_E<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
     return true;
 }
 
@@ -639,14 +618,6 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
     }
 }
 
-// The z tile of the z-slab shell boxes: their z extent rounded up to a multiple of 4.
-int zshell_tz(const Split& sp) {
-    int w = 4;
-    for (int q = 0; q < sp.n_shell; ++q)
-        if (sp.shell_is_z[q]) w = std::max(w, sp.shell[q].hi[2] - sp.shell[q].lo[2]);
-    return (w + 3) / 4 * 4;
-}
-
 template <bool REV, bool HSIDE>
 void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     const Split sp = split_boxes(p);
@@ -655,21 +626,9 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
         launch_plain_boxes<REV, HSIDE, true>(p, a, &all, &p->chunk, 1, st);
         return;
     }
-    if (p->use_tma) {
-        Box xy[6], zb[6];
-        int nxy = 0, nzb = 0;
-        for (int q = 0; q < sp.n_shell; ++q) {
-            if (sp.shell_is_z[q]) zb[nzb++] = sp.shell[q];
-            else xy[nxy++] = sp.shell[q];
-        }
-        const int ztz = zshell_tz(sp);
-        const int zty = std::max(1, std::min(32, 256 * 2 / ztz));
-        if (launch_tma<REV, HSIDE, false>(p, a, &sp.core, 1, p->tma_tz, p->tma_ty, p->tma_chunk, st) &&
-            launch_tma<REV, HSIDE, true>(p, a, xy, nxy, p->tma_tz, p->tma_ty, kShellChunk, st) &&
-            launch_tma<REV, HSIDE, true>(p, a, zb, nzb, ztz, zty, kShellChunk, st))
-            return;
-    }
-    launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
+    UpdArgs ac = a;
+    for (int x = 0; x < 3; ++x) { ac.lo[x] = sp.core.lo[x]; ac.hi[x] = sp.core.hi[x]; }
+    if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
     int chunks[6];
     for (int q = 0; q < sp.n_shell; ++q) chunks[q] = kShellChunk;
     launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st);
@@ -677,11 +636,7 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
 
 int half_step_launches(const FdtdPlan* p) {
     const Split sp = split_boxes(p);
-    if (!sp.split) return 1;
-    if (!p->use_tma) return 1 + (sp.n_shell > 0);
-    int nz = 0;
-    for (int q = 0; q < sp.n_shell; ++q) nz += sp.shell_is_z[q];
-    return 1 + (sp.n_shell - nz > 0) + (nz > 0);
+    return sp.split ? 1 + (sp.n_shell > 0) : 1;
 }
 
 template <bool REV>

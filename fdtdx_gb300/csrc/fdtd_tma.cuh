@@ -7,10 +7,9 @@
 // stage's mbarrier; NS stages are in flight, so the data waiting on HBM lives in
 // shared memory instead of registers.  Out-of-range tile cells read as zero (TMA
 // fill), which is exactly the reference's zero halo (fdtdx/core/misc.py:615-641);
-// scenes with a periodic axis use the register-queue kernels instead.  A launch updates
-// a table of boxes: the core box of the grid (no CPML cell, PML = false) or the CPML
-// slabs (PML = true: a thread fetches the psi of its next plane one plane ahead, so the
-// scattered slab reads overlap the pipeline).
+// scenes with a periodic axis use the register-queue kernels instead.  These kernels
+// update the core box of the grid, which holds no CPML cell; the slabs are updated by
+// the register-queue kernels with their CPML corrections.
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the plan's error word to
 // FDTD_ETIMEOUT, the block learns it through __syncthreads_or, the elected thread waits
@@ -87,37 +86,13 @@ __device__ __forceinline__ void drain(uint64_t* bar, int ns, int from, int to) {
     for (int p = from; p < to; ++p) mbar_wait_bounded(&bar[p % ns], (uint32_t)((p / ns) & 1));
 }
 
-// The block's tile: box b of the launch's box table owns blocks [bstart[b], bstart[b+1]),
-// laid out as (z tiles) x (y tiles) x (x chunks); box z bounds are multiples of 4.
-__device__ __forceinline__ void tma_tile(const UpdArgs& a, int TZ, int TY, int& kt, int& jt, int& i0, int& i1, int& hy,
-                                         int& hz) {
-    const int b = blockIdx.x;
-    int lo0 = 0, lo1 = 0, lo2 = 0, hi0 = 0, hi1 = 0, hi2 = 0, chunk = 1, start = 0;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        if (q < a.nbox && b >= a.bstart[q]) {
-            lo0 = a.blo[q][0]; lo1 = a.blo[q][1]; lo2 = a.blo[q][2];
-            hi0 = a.bhi[q][0]; hi1 = a.bhi[q][1]; hi2 = a.bhi[q][2];
-            chunk = a.bchunk[q]; start = a.bstart[q];
-        }
-    }
-    const int lb = b - start;
-    const int ntz = (hi2 - lo2 + TZ - 1) / TZ, nty = (hi1 - lo1 + TY - 1) / TY;
-    kt = lo2 + (lb % ntz) * TZ;
-    jt = lo1 + ((lb / ntz) % nty) * TY;
-    i0 = lo0 + (lb / (ntz * nty)) * chunk;
-    i1 = min(i0 + chunk, hi0);
-    hy = hi1;
-    hz = hi2;
-}
-
 // ---------------------------------------------------------------------------------
 // E half-step (forward / reverse), tile loads per plane i:
 //   H (3 comps) z in [kt-4, kt+TZ), y in [jt-1, jt+TY)   (backward differences)
 //   E, inv_eps, sigma_E on the tile
 // Loads cover planes i0-1 .. i1-1; the first only seeds H(i-1) of each column.
 // ---------------------------------------------------------------------------------
-template <bool REV, bool PML>
+template <bool REV>
 __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -130,11 +105,11 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    int kt, jt, i0, i1, hy, hz;
-    tma_tile(a, TZ, TY, kt, jt, i0, i1, hy, hz);
+    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < hz && j < hy;
+    const bool valid = k0 < a.hi[2] && j < a.hi[1];
     const long long N = g.N;
 
     if (tid == 0) {
@@ -156,17 +131,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     float Hy_m[2] = {0.f, 0.f}, Hz_m[2] = {0.f, 0.f};
-    // CPML psi of the next computed plane, fetched one plane ahead of its use
-    PsiPre pre[2];
-    bool pml = false;
-    auto fetch = [&](int ii) {
-        pml = PML && valid && a.n_slab > 0 && maybe_slab(a, ii, j, k0, 2);
-        if (pml) {
-            psi_fetch(a, ii, j, k0, pre[0]);
-            psi_fetch(a, ii, j, k0 + 1, pre[1]);
-        }
-    };
-    fetch(i0);
     for (int p = 0; p < P; ++p) {
         const int s = p % NS;
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
@@ -198,8 +162,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 const float d[6] = {Hz - Hz_jm, Hy - Hy_km, Hx - Hx_km, Hz - Hz_m[e], Hy - Hy_m[e], Hx - Hx_jm};
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
-                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (PML && pml) cpml_apply<REV, false>(a, i, j, k0 + e, d, cu, pre[e]);
+                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -220,7 +183,6 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (PML && i + 1 < i1) fetch(i + 1);
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -243,7 +205,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 //   H, inv_mu, sigma_H on the tile
 // Loads cover planes i0 .. i1; plane i is computed once the loads of i and i+1 landed.
 // ---------------------------------------------------------------------------------
-template <bool REV, bool PML>
+template <bool REV>
 __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -257,11 +219,11 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    int kt, jt, i0, i1, hy, hz;
-    tma_tile(a, TZ, TY, kt, jt, i0, i1, hy, hz);
+    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < hz && j < hy;
+    const bool valid = k0 < a.hi[2] && j < a.hi[1];
     const long long N = g.N;
 
     int slot[kMaxFuse];
@@ -301,16 +263,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     bool ok = mbar_wait_bounded(&bar[0], 0);
-    PsiPre pre[2];
-    bool pml = false;
-    auto fetch = [&](int ii) {
-        pml = PML && valid && a.n_slab > 0 && maybe_slab(a, ii, j, k0, 2);
-        if (pml) {
-            psi_fetch(a, ii, j, k0, pre[0]);
-            psi_fetch(a, ii, j, k0 + 1, pre[1]);
-        }
-    };
-    fetch(i0);
     // Ex(i-1) at k and k+1 of this thread's two cells (fused co-location), seeded at the chunk start
     float Exm[3] = {0.f, 0.f, 0.f};
     if (any && valid) {
@@ -347,8 +299,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ez_ip = E1[(2 * EY + r0) * EZ + kk];
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
-                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (PML && pml) cpml_apply<REV, true>(a, i, j, k0 + e, d, cu, pre[e]);
+                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -378,7 +329,6 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (PML && i + 1 < i1) fetch(i + 1);
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
