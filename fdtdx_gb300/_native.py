@@ -127,8 +127,6 @@ class AdjointBuffers(C.Structure):
         ("lam_psi_H", (C.c_void_p * 2) * MAX_SLABS),
         ("lam_det", C.c_void_p * MAX_DETECTORS),
         ("grad_inv_eps", C.c_void_p),
-        ("grad_inv_mu", C.c_void_p),
-        ("grad_inv_mu_scalar", C.c_void_p),
     ]
 
 
@@ -145,9 +143,9 @@ SIGNATURES = {
     "fdtd_footprint_bytes": (C.c_int64, [C.POINTER(Desc)]),
     "fdtd_forward": (C.c_int, [C.c_void_p, C.POINTER(Buffers), C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "fdtd_reverse": (C.c_int, [C.c_void_p, C.POINTER(Buffers), C.c_int32, C.c_int32, C.c_void_p]),
-    "fdtd_adjoint_step": (
+    "fdtd_adjoint": (
         C.c_int,
-        [C.c_void_p, C.POINTER(Buffers), C.POINTER(AdjointBuffers), C.c_int32, C.c_void_p],
+        [C.c_void_p, C.POINTER(Buffers), C.POINTER(AdjointBuffers), C.c_int32, C.c_int32, C.c_void_p],
     ),
     "fdtd_launches_per_step": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),

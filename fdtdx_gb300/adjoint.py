@@ -1,0 +1,205 @@
+"""Reversible (time-reversal) gradient: ``reversible_fdtd`` (fdtdx/fdtd/fdtd.py:39-418).
+
+The forward pass runs on the native library and records the PML-interface planes
+(``record_boundaries=config.invertible_optimization``).  The backward pass is the
+reference's custom VJP: for t = T-1 down to -1, reconstruct the state at t by a
+reverse step (interfaces re-imposed, psi frozen) and apply the transpose of the
+forward step at t, accumulating d/d inv_permittivities.  Both run in one native call
+(``fdtd_adjoint``); here the cotangents are marshalled and the call is wrapped as a
+``torch.autograd.Function``, the PyTorch counterpart of ``jax.custom_vjp``.
+
+The sliced backward pass of ``num_checkpoints_reversible`` (fdtd.py:96-121, 292-322)
+stores the full field state at the interior slice boundaries during the forward run
+and resets the reconstruction to it when the backward loop reaches that step.
+
+As in the reference only the materials receive a gradient (fdtd.py:324-333); the
+initial fields, psi, detector states and recording get none.  The inv_permeability
+gradient of the reference is not provided: a magnetic-material input that requires a
+gradient raises.
+"""
+
+from __future__ import annotations
+
+from typing import Callable
+
+import torch
+
+from fdtdx_gb300.config import SimulationConfig
+from fdtdx_gb300.container import ArrayContainer, FieldState, ObjectContainer, SimulationState
+
+
+def reversible_slice_boundaries(time_steps_total: int, num_slices: int) -> list[int]:
+    """Slice boundaries [s_0 = 0, ..., s_k = T] of the sliced backward pass (fdtd.py:20-36)."""
+    return [round(i * time_steps_total / num_slices) for i in range(num_slices + 1)]
+
+
+def _clone_fields(f: FieldState) -> FieldState:
+    return FieldState(
+        E=f.E.clone(),
+        H=f.H.clone(),
+        psi_E={k: (a.clone(), b.clone()) for k, (a, b) in f.psi_E.items()},
+        psi_H={k: (a.clone(), b.clone()) for k, (a, b) in f.psi_H.items()},
+    )
+
+
+def _copy_fields(dst: FieldState, src: FieldState) -> None:
+    dst.E.copy_(src.E)
+    dst.H.copy_(src.H)
+    for k in dst.psi_E:
+        dst.psi_E[k][0].copy_(src.psi_E[k][0])
+        dst.psi_E[k][1].copy_(src.psi_E[k][1])
+        dst.psi_H[k][0].copy_(src.psi_H[k][0])
+        dst.psi_H[k][1].copy_(src.psi_H[k][1])
+
+
+class _Layout:
+    """Flat tensor order of the run's outputs: E, H, psi_E, psi_H, detector states."""
+
+    def __init__(self, arrays: ArrayContainer):
+        f = arrays.fields
+        self.pml_names = list(f.psi_E.keys())
+        self.det_keys = [(n, k) for n, st in arrays.detector_states.items() for k in st]
+
+    def flatten(self, arrays: ArrayContainer) -> list[torch.Tensor]:
+        f = arrays.fields
+        out = [f.E, f.H]
+        for n in self.pml_names:
+            out += [f.psi_E[n][0], f.psi_E[n][1]]
+        for n in self.pml_names:
+            out += [f.psi_H[n][0], f.psi_H[n][1]]
+        out += [arrays.detector_states[n][k] for n, k in self.det_keys]
+        return out
+
+    def unflatten(self, arrays: ArrayContainer, flat: list[torch.Tensor]) -> ArrayContainer:
+        it = iter(flat)
+        E, H = next(it), next(it)
+        psi_E = {n: (next(it), next(it)) for n in self.pml_names}
+        psi_H = {n: (next(it), next(it)) for n in self.pml_names}
+        det: dict[str, dict[str, torch.Tensor]] = {n: {} for n in arrays.detector_states}
+        for n, k in self.det_keys:
+            det[n][k] = next(it)
+        arrays = arrays.aset("fields", FieldState(E=E, H=H, psi_E=psi_E, psi_H=psi_H))
+        return arrays.aset("detector_states", det)
+
+
+class _ReversibleRun(torch.autograd.Function):
+    """Forward run + reversible backward; the only differentiable input is inv_permittivities."""
+
+    @staticmethod
+    def forward(ctx, ctl: dict, inv_eps: torch.Tensor):
+        scene, arrays, T = ctl["scene"], ctl["arrays"], ctl["T"]
+        bounds = ctl["bounds"]
+        checkpoints = []
+        for seg in range(len(bounds) - 1):
+            scene.forward(arrays, bounds[seg], bounds[seg + 1] - bounds[seg])
+            if seg < len(bounds) - 2:
+                checkpoints.append(_clone_fields(arrays.fields))
+        scene.status()
+        ctl["checkpoints"] = checkpoints
+        ctl["final"] = arrays
+        ctx.ctl = ctl
+        flat = ctl["layout"].flatten(arrays)
+        return tuple(flat)
+
+    @staticmethod
+    def backward(ctx, *grads):
+        ctl = ctx.ctl
+        scene, layout, T = ctl["scene"], ctl["layout"], ctl["T"]
+        final: ArrayContainer = ctl["final"]
+        bounds, checkpoints = ctl["bounds"], ctl["checkpoints"]
+        # reconstruct on a copy: the outputs handed to the caller stay intact
+        state = final.aset("fields", _clone_fields(final.fields))
+        f = state.fields
+        outs = layout.flatten(final)
+
+        def cot(i):
+            g = grads[i]
+            if g is None:
+                return torch.zeros_like(outs[i])
+            return g.detach().to(outs[i].dtype).contiguous().clone()
+
+        lam = {"E": cot(0), "H": cot(1)}
+        i = 2
+        lam["psi_E"] = {}
+        for n in layout.pml_names:
+            lam["psi_E"][n] = (cot(i), cot(i + 1))
+            i += 2
+        lam["psi_H"] = {}
+        for n in layout.pml_names:
+            lam["psi_H"][n] = (cot(i), cot(i + 1))
+            i += 2
+        lam["det"] = {}
+        for n, _k in layout.det_keys:
+            if grads[i] is not None:
+                lam["det"][n] = cot(i)
+            i += 1
+        ie = ctl["inv_eps"]
+        grad = torch.zeros_like(ie, dtype=torch.float32).contiguous()
+        lam["grad_inv_eps"] = grad
+        # slices from the last to the first; the last call runs down to t = -1
+        k = len(bounds) - 1
+        for seg in range(k - 1, -1, -1):
+            t_end = bounds[seg + 1]
+            n = t_end - bounds[seg] + (1 if seg == 0 else 0)
+            scene.adjoint(state, lam, t_end, n)
+            if seg > 0:
+                _copy_fields(f, checkpoints[seg - 1])
+        scene.status()
+        ctl["checkpoints"] = []
+        return None, grad.to(ie.dtype)
+
+
+def reversible_fdtd(
+    arrays: ArrayContainer,
+    objects: ObjectContainer,
+    config: SimulationConfig,
+    key=None,
+    show_progress: bool = False,
+    progress_callback: Callable[[int, int], None] | None = None,
+) -> SimulationState:
+    """Differentiable forward run with the time-reversal gradient (fdtd.py:39-418).
+
+    Returns ``(T, arrays)`` like the reference.  When ``arrays.inv_permittivities``
+    requires a gradient, the returned fields and detector states are connected to it
+    through the reversible backward pass.
+    """
+    del key, show_progress
+    from fdtdx_gb300.fdtd import _materials_detached, get_scene
+
+    if arrays.inv_permittivities.shape[0] not in (1, 3):
+        raise NotImplementedError("fully anisotropic (9-component) materials are not supported")
+    mu = arrays.inv_permeabilities
+    if isinstance(mu, torch.Tensor) and mu.requires_grad:
+        raise NotImplementedError("the inv_permeabilities gradient is not provided by the reversible path")
+    gc = config.gradient_config
+    num_ckpt = 0 if gc is None else gc.num_checkpoints_reversible
+    T = config.time_steps_total
+    num_slices = num_ckpt + 1
+    if num_ckpt > 0 and num_slices > T:
+        raise Exception(
+            "num_checkpoints_reversible must be <= time_steps_total - 1 "
+            f"(got num_checkpoints_reversible={num_ckpt}, time_steps_total={T})"
+        )
+    bounds = reversible_slice_boundaries(T, num_slices)
+    ie_in = arrays.inv_permittivities
+    work = _materials_detached(arrays).reset()
+    if work.recording_state is None and config.invertible_optimization and objects.pml_objects:
+        raise ValueError("the reversible gradient needs a recording state (init_arrays with a recorder)")
+    scene = get_scene(objects, work, config, record_interfaces=config.invertible_optimization)
+    layout = _Layout(work)
+    ctl = {"scene": scene, "arrays": work, "T": T, "bounds": bounds, "layout": layout,
+           "inv_eps": work.inv_permittivities}
+    if not (torch.is_grad_enabled() and ie_in.requires_grad):
+        _ReversibleRun.forward(_NoCtx(), ctl, work.inv_permittivities)
+        out = work
+    else:
+        flat = _ReversibleRun.apply(ctl, ie_in)
+        out = layout.unflatten(work, list(flat))
+        out = out.aset("inv_permittivities", ie_in)
+    if progress_callback is not None:
+        progress_callback(T, T)
+    return T, out
+
+
+class _NoCtx:
+    """Stand-in context for a forward run that needs no backward."""

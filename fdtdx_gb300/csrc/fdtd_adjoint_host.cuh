@@ -1,0 +1,216 @@
+// Host side of fdtd_adjoint (included by fdtd_plan.cu, which owns the plan type and the
+// launch helpers): scratch layout, per-step launch sequence of the reversible gradient.
+#pragma once
+
+namespace {
+
+bool det_exact_h(const DDet& d) {
+    if (!d.exact) return false;
+    if (d.kind == FDTD_DET_FLUX || d.kind == FDTD_DET_ENERGY) return true;
+    return (d.comp_mask & 56) != 0;
+}
+
+bool det_bilinear(const DDet& d) { return d.kind == FDTD_DET_FLUX || d.kind == FDTD_DET_ENERGY; }
+
+// Bounding box [lo - 1, hi + 1) of a detector's stencil on one axis, clipped to the grid;
+// a stencil that wraps around a periodic axis takes the whole axis.
+void stencil_range(int lo, int hi, int n, bool periodic, int& blo, int& bhi) {
+    blo = lo - 1;
+    bhi = hi + 1;
+    if (periodic && (blo < 0 || bhi > n)) { blo = 0; bhi = n; return; }
+    blo = std::max(blo, 0);
+    bhi = std::min(bhi, n);
+}
+
+int ensure_adjoint_scratch(FdtdPlan* p) {
+    if (p->amem) return FDTD_OK;
+    const FdtdDesc& d = p->d;
+    const long long N = p->g.N;
+    const int n3[3] = {d.nx, d.ny, d.nz};
+    const bool per[3] = {d.periodic[0] != 0, d.periodic[1] != 0, d.periodic[2] != 0};
+    Arena ar;
+    const size_t o_lam = ar.take(sizeof(float) * 6 * (size_t)N);
+    size_t o_psi[FDTD_MAX_SLABS][4] = {};
+    for (int s = 0; s < d.n_slabs; ++s) {
+        const DSlab& sl = p->slab[s];
+        const size_t cells = (size_t)sl.sx * sl.sy * sl.sz;
+        for (int q = 0; q < 4; ++q) o_psi[s][q] = ar.take(sizeof(float) * cells);
+    }
+    // the H-before-update box: union of the exact H-reading detectors' stencils
+    DBox hp{};
+    bool any = false;
+    int blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
+    for (int q = 0; q < d.n_detectors; ++q) {
+        const DDet& dd = p->det[q];
+        if (!det_exact_h(dd)) continue;
+        for (int a = 0; a < 3; ++a) {
+            int l, h;
+            stencil_range(dd.lo[a], dd.hi[a], n3[a], per[a], l, h);
+            blo[a] = any ? std::min(blo[a], l) : l;
+            bhi[a] = any ? std::max(bhi[a], h) : h;
+        }
+        any = true;
+    }
+    size_t o_hp = 0;
+    if (any) {
+        for (int a = 0; a < 3; ++a) { hp.lo[a] = blo[a]; hp.n[a] = bhi[a] - blo[a]; }
+        hp.M = (long long)hp.n[0] * hp.n[1] * hp.n[2];
+        o_hp = ar.take(sizeof(float) * 3 * (size_t)hp.M);
+    }
+    DBox snap[FDTD_MAX_DETECTORS] = {};
+    size_t o_snap[FDTD_MAX_DETECTORS] = {};
+    for (int q = 0; q < d.n_detectors; ++q) {
+        const DDet& dd = p->det[q];
+        if (!det_bilinear(dd)) continue;
+        DBox& b = snap[q];
+        for (int a = 0; a < 3; ++a) { b.lo[a] = dd.lo[a] - 1; b.n[a] = dd.hi[a] - dd.lo[a] + 2; }
+        b.M = (long long)b.n[0] * b.n[1] * b.n[2];
+        o_snap[q] = ar.take(sizeof(float) * 6 * (size_t)b.M);
+    }
+    char* mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, ar.off);
+    if (e != cudaSuccess) return fail(p, FDTD_ENOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
+    e = cudaMemset(mem, 0, ar.off);
+    if (e != cudaSuccess) {
+        cudaFree(mem);
+        return cuda_fail(p, e, "adjoint scratch memset");
+    }
+    p->amem = mem;
+    p->amem_bytes = ar.off;
+    p->lam_twin[0] = reinterpret_cast<float*>(mem + o_lam);
+    p->lam_twin[1] = p->lam_twin[0] + 3 * N;
+    for (int s = 0; s < d.n_slabs; ++s)
+        for (int q = 0; q < 4; ++q) p->lpsi_twin[s][q] = reinterpret_cast<float*>(mem + o_psi[s][q]);
+    p->hp = hp;
+    if (any) p->hp.buf = reinterpret_cast<float*>(mem + o_hp);
+    for (int q = 0; q < d.n_detectors; ++q) {
+        p->snap[q] = snap[q];
+        if (det_bilinear(p->det[q])) p->snap[q].buf = reinterpret_cast<float*>(mem + o_snap[q]);
+    }
+    return FDTD_OK;
+}
+
+// One set of cotangent buffers of the state (E, H, psi).
+struct LamSet {
+    float* E;
+    float* H;
+    float* psi[FDTD_MAX_SLABS][4];
+};
+
+AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, const LamSet& cur,
+                 const LamSet& nxt) {
+    AdjArgs a{};
+    a.g = p->g;
+    a.E = b->E;
+    a.H = b->H;
+    a.ie = b->inv_eps;
+    a.n_eps = p->d.n_eps;
+    a.im = p->d.n_mu ? b->inv_mu : nullptr;
+    a.n_mu = p->d.n_mu ? p->d.n_mu : 1;
+    a.im_scalar = p->d.inv_mu_scalar;
+    a.sigE = p->d.n_sigma_E ? b->sigma_E : nullptr;
+    a.n_sigE = p->d.n_sigma_E;
+    a.sigH = p->d.n_sigma_H ? b->sigma_H : nullptr;
+    a.n_sigH = p->d.n_sigma_H;
+    a.n_slab = p->d.n_slabs;
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        a.slab[s] = p->slab[s];
+        a.psiE1[s] = b->psi_E[s][0];
+        a.psiE2[s] = b->psi_E[s][1];
+        a.lpE[s][0] = cur.psi[s][0]; a.lpE[s][1] = cur.psi[s][1];
+        a.lpH[s][0] = cur.psi[s][2]; a.lpH[s][1] = cur.psi[s][3];
+        a.lpE_out[s][0] = nxt.psi[s][0]; a.lpE_out[s][1] = nxt.psi[s][1];
+        a.lpH_out[s][0] = nxt.psi[s][2]; a.lpH_out[s][1] = nxt.psi[s][3];
+    }
+    a.lE = cur.E;
+    a.lH = cur.H;
+    a.lE_out = nxt.E;
+    a.lH_out = nxt.H;
+    a.grad_ie = adj->grad_inv_eps;
+    a.hp = p->hp;
+    return a;
+}
+
+int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
+    if (!adj || !adj->lam_E || !adj->lam_H) return fail(p, FDTD_EINVAL, "lam_E and lam_H buffers are required");
+    for (int s = 0; s < p->d.n_slabs; ++s)
+        if (!adj->lam_psi_E[s][0] || !adj->lam_psi_E[s][1] || !adj->lam_psi_H[s][0] || !adj->lam_psi_H[s][1])
+            return fail(p, FDTD_EINVAL, "psi cotangent buffers required for every slab");
+    return FDTD_OK;
+}
+
+// One step of the backward loop at t = *d_t: snapshot, reconstruction, transposed step.
+void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, const LamSet& cur,
+                         const LamSet& nxt, cudaStream_t st) {
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (!adj->lam_det[q] || !p->snap[q].buf) continue;
+        const DBox& sb = p->snap[q];
+        k_adj_snap<<<(unsigned)((sb.M + 255) / 256), 256, 0, st>>>(p->g, sb, p->det[q].slot, p->d_t, b->E, b->H);
+    }
+    interfaces<true>(p, b, b->H, st);
+    launch_sources(p, b, false, b->H, 1, st);
+    launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H), st);
+    launch_sources(p, b, true, b->E, 1, st);
+    launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E), st);
+    const AdjArgs a = make_adj(p, b, adj, cur, nxt);
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (!adj->lam_det[q]) continue;
+        const DDet& dd = p->det[q];
+        AdjDet x{};
+        x.d = dd;
+        x.lam = adj->lam_det[q];
+        x.snap = p->snap[q];
+        k_adj_det<<<dd.nblocks, kDetBlock, 0, st>>>(a, x, p->d_t);
+        if (dd.reduce && dd.kind != FDTD_DET_PHASOR) k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
+    }
+    const unsigned blocks = (unsigned)((p->g.N + 255) / 256);
+    k_adj_H<<<blocks, 256, 0, st>>>(a);
+    k_adj_E<<<blocks, 256, 0, st>>>(a);
+    k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
+}
+
+}  // namespace
+
+extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, int32_t t_end,
+                            int32_t n_steps, void* stream) {
+    if (!p) return FDTD_EINVAL;
+    if (int rc = check_bufs(p, b)) return rc;
+    if (int rc = check_adj(p, adj)) return rc;
+    if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)
+        return fail(p, FDTD_EINVAL, "adjoint steps out of the range covered by the plan's tables");
+    if (n_steps == 0) return FDTD_OK;
+    if (int rc = ensure_adjoint_scratch(p)) return rc;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    LamSet user{}, twin{};
+    user.E = adj->lam_E;
+    user.H = adj->lam_H;
+    twin.E = p->lam_twin[0];
+    twin.H = p->lam_twin[1];
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        user.psi[s][0] = adj->lam_psi_E[s][0]; user.psi[s][1] = adj->lam_psi_E[s][1];
+        user.psi[s][2] = adj->lam_psi_H[s][0]; user.psi[s][3] = adj->lam_psi_H[s][1];
+        for (int q = 0; q < 4; ++q) twin.psi[s][q] = p->lpsi_twin[s][q];
+    }
+    k_set_step<<<1, 1, 0, st>>>(p->d_t, t_end - 1);
+    const LamSet* cur = &user;
+    const LamSet* nxt = &twin;
+    for (int s = 0; s < n_steps; ++s) {
+        launch_adjoint_step(p, b, adj, *cur, *nxt, st);
+        std::swap(cur, nxt);
+    }
+    if (cur != &user) {  // odd step count: the result sits in the twins
+        const size_t fb = sizeof(float) * 3 * (size_t)p->g.N;
+        cudaError_t e = cudaMemcpyAsync(user.E, cur->E, fb, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(user.H, cur->H, fb, cudaMemcpyDeviceToDevice, st);
+        for (int s = 0; s < p->d.n_slabs && e == cudaSuccess; ++s) {
+            const DSlab& sl = p->slab[s];
+            const size_t pb = sizeof(float) * (size_t)sl.sx * sl.sy * sl.sz;
+            for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+                e = cudaMemcpyAsync(user.psi[s][q], cur->psi[s][q], pb, cudaMemcpyDeviceToDevice, st);
+        }
+        if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_adjoint copy-back");
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_adjoint launch");
+    return FDTD_OK;
+}

@@ -47,6 +47,13 @@ struct FdtdPlan {
     FdtdBuffers gbufs{};
     int gsteps = 0;
     cudaStream_t cap_stream = nullptr;
+    // reversible-gradient scratch, allocated by the first fdtd_adjoint call
+    char* amem = nullptr;
+    size_t amem_bytes = 0;
+    float* lam_twin[2] = {nullptr, nullptr};      // cotangent twins of E and H
+    float* lpsi_twin[FDTD_MAX_SLABS][4] = {};     // twins of the psi_E (1, 2) and psi_H (1, 2) cotangents
+    DBox hp{};                                    // H-before-update cotangents of exact detectors
+    DBox snap[FDTD_MAX_DETECTORS] = {};           // (E3, H3) snapshots of bilinear detectors
     std::string err;
 };
 
@@ -507,6 +514,7 @@ void fdtd_plan_destroy(FdtdPlan* p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
     cudaFree(p->dmem);
+    cudaFree(p->amem);
     delete p;
 }
 
@@ -514,7 +522,7 @@ const char* fdtd_last_error(const FdtdPlan* p) { return p ? p->err.c_str() : "no
 
 int64_t fdtd_interface_floats(const FdtdPlan* p) { return p ? p->iface_floats : 0; }
 
-int64_t fdtd_plan_device_bytes(const FdtdPlan* p) { return p ? (int64_t)p->dmem_bytes : 0; }
+int64_t fdtd_plan_device_bytes(const FdtdPlan* p) { return p ? (int64_t)(p->dmem_bytes + p->amem_bytes) : 0; }
 
 }  // extern "C"
 
@@ -895,10 +903,7 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
 
 }  // extern "C"
 
-extern "C" int fdtd_adjoint_step(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, int32_t t, void* stream) {
-    (void)b; (void)adj; (void)t; (void)stream;
-    return fail(p, FDTD_EINVAL, "fdtd_adjoint_step: not built in this version");
-}
+#include "fdtd_adjoint_host.cuh"
 
 extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, float* out_ms,
                                     void* stream) {

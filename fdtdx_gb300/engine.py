@@ -432,3 +432,34 @@ class Scene:
         b = self.buffers(arrays)
         rc = N.load().fdtd_reverse(self.plan, C.byref(b), int(t_end), int(n_steps), C.c_void_p(st.cuda_stream))
         N.check(rc, self.plan, "fdtd_reverse")
+
+    def adjoint(self, arrays: ArrayContainer, lam: dict, t_end: int, n_steps: int, stream=None) -> None:
+        """Backward loop of the reversible gradient on the native path (``fdtd_adjoint``).
+
+        ``arrays`` holds the forward state at ``t_end`` and is reconstructed in place down to
+        ``t_end - n_steps``.  ``lam`` holds the cotangents of that state: ``"E"``, ``"H"``,
+        ``"psi_E"`` / ``"psi_H"`` (name -> (psi1, psi2)), ``"det"`` (detector name -> tensor
+        of the state's layout, complex states with torch's convention) and ``"grad_inv_eps"``
+        (accumulated); all are updated in place.
+        """
+        st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
+        b = self.buffers(arrays)
+        a = N.AdjointBuffers()
+        for key in ("E", "H"):
+            t = lam[key]
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
+                raise ValueError("cotangents must be contiguous float32 CUDA tensors")
+        a.lam_E, a.lam_H = N.ptr(lam["E"]), N.ptr(lam["H"])
+        for s, p in enumerate(self.pmls):
+            a.lam_psi_E[s][0], a.lam_psi_E[s][1] = N.ptr(lam["psi_E"][p.name][0]), N.ptr(lam["psi_E"][p.name][1])
+            a.lam_psi_H[s][0], a.lam_psi_H[s][1] = N.ptr(lam["psi_H"][p.name][0]), N.ptr(lam["psi_H"][p.name][1])
+        dets = lam.get("det", {})
+        for q, det in enumerate(self.detectors):
+            t = dets.get(det.name)
+            if t is not None and not (t.is_cuda and t.is_contiguous()):
+                raise ValueError("detector cotangents must be contiguous CUDA tensors")
+            a.lam_det[q] = N.ptr(t)
+        a.grad_inv_eps = N.ptr(lam.get("grad_inv_eps"))
+        rc = N.load().fdtd_adjoint(self.plan, C.byref(b), C.byref(a), int(t_end), int(n_steps),
+                                   C.c_void_p(st.cuda_stream))
+        N.check(rc, self.plan, "fdtd_adjoint")

@@ -179,14 +179,16 @@ def place_objects(
         d.name: torch.full(d.grid_shape, 0.5, dtype=torch.float32, device=arrays.device) for d in objects.devices
     }
     if objects.devices:
-        arrays = apply_params(arrays, objects, params)
+        arrays, objects, _ = apply_params(arrays, objects, params)
     return objects, arrays, params, config, {}
 
 
-def apply_params(arrays: ArrayContainer, objects: ObjectContainer, params: ParameterContainer, key=None) -> ArrayContainer:
-    """Map device parameters to inv_eps: eps = eps_lo + p (eps_hi - eps_lo) (initialization.py:404-417).
+def apply_params(arrays: ArrayContainer, objects: ObjectContainer, params: ParameterContainer,
+                 key=None) -> tuple[ArrayContainer, ObjectContainer, dict]:
+    """Map device parameters to inv_eps: eps = eps_lo + p (eps_hi - eps_lo) (initialization.py:317-417).
 
-    Out-of-place, so a ``params`` tensor with ``requires_grad`` carries the gradient.
+    Returns ``(arrays, objects, info)`` like the reference.  Out-of-place, so a ``params``
+    tensor with ``requires_grad`` carries the gradient.
     """
     del key
     inv = arrays.inv_permittivities.clone()
@@ -194,4 +196,4 @@ def apply_params(arrays: ArrayContainer, objects: ObjectContainer, params: Param
         p = params[d.name]
         eps = d.permittivity_low + p * (d.permittivity_high - d.permittivity_low)
         inv[(slice(None), *d.grid_slice)] = (1.0 / eps)[None].expand(inv.shape[0], *p.shape)
-    return dataclasses.replace(arrays, inv_permittivities=inv)
+    return dataclasses.replace(arrays, inv_permittivities=inv), objects, {}

@@ -15,11 +15,12 @@
  *                         reverse H, reverse E with frozen CPML psi).  Replaces
  *                         fdtdx/fdtd/backward.py:62-135 with
  *                         fdtdx/fdtd/update.py:526-686, 856-1007, 1181-1222.
- *   fdtd_adjoint_step     the transposed (vector-Jacobian) forward step used by the
- *                         reversible gradient: replaces the jax.vjp of
- *                         forward_single_args_wrapper inside body_fn,
- *                         fdtdx/fdtd/fdtd.py:215-251, accumulating d/d inv_eps and
- *                         d/d inv_mu as fdtdx/fdtd/fdtd.py:324-333 returns them.
+ *   fdtd_adjoint          the backward loop of the reversible gradient: per step a
+ *                         reverse step (the reconstruction) followed by the transposed
+ *                         (vector-Jacobian) forward step.  Replaces body_fn of the
+ *                         custom VJP, fdtdx/fdtd/fdtd.py:215-251 (backward() then
+ *                         jax.vjp of forward_single_args_wrapper), accumulating
+ *                         d/d inv_eps as fdtdx/fdtd/fdtd.py:324-333 returns it.
  *
  * Conventions
  *   - Every buffer is caller-owned device memory, float32, C order, z fastest.
@@ -158,10 +159,11 @@ typedef struct {
     float* lam_H;               /* (3, nx, ny, nz) cotangent of H */
     float* lam_psi_E[FDTD_MAX_SLABS][2];
     float* lam_psi_H[FDTD_MAX_SLABS][2];
-    const void* lam_det[FDTD_MAX_DETECTORS];  /* cotangent of each detector state (same layout), or NULL */
-    float* grad_inv_eps;        /* (n_eps, nx, ny, nz), accumulated (+=) */
-    float* grad_inv_mu;         /* (n_mu, ...) accumulated, or NULL when inv_mu is a scalar */
-    double* grad_inv_mu_scalar; /* device scalar accumulated when inv_mu is a scalar, or NULL */
+    /* cotangent of each detector state (same layout; complex states interleaved re, im,
+     * with torch's convention dL/dRe + i dL/dIm), or NULL for zero.  Entries the forward
+     * step overwrote (field, flux, energy slots) are cleared as the loop passes them. */
+    void* lam_det[FDTD_MAX_DETECTORS];
+    float* grad_inv_eps;        /* (n_eps, nx, ny, nz), accumulated (+=), or NULL */
 } FdtdAdjointBuffers;
 
 typedef struct FdtdPlan FdtdPlan;
@@ -185,11 +187,15 @@ int fdtd_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_
  * recording (interfaces re-imposed before each step) when it is non-NULL. */
 int fdtd_reverse(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t_end, int32_t n_steps, void* stream);
 
-/* Transposed forward step at time step t: the fields in bufs hold the forward
- * state at t (reconstructed by fdtd_reverse); the cotangents of the state at t+1
- * in adj are replaced by the cotangents of the state at t, and the material
- * gradients are accumulated. */
-int fdtd_adjoint_step(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t, void* stream);
+/* Backward loop of the reversible gradient, for t = t_end-1 down to t_end-n_steps
+ * (t = -1 is admitted, as the reference's loop runs one step there): reverse step
+ * t+1 -> t on bufs (interfaces re-imposed, psi frozen), then the transposed forward
+ * step at t.  On entry adj holds the cotangents of the state at t_end, on return
+ * those of the state at t_end - n_steps; grad_inv_eps accumulates.  The first call
+ * allocates the plan's adjoint scratch (cotangent twins, detector snapshots);
+ * fdtd_plan_device_bytes counts it from then on. */
+int fdtd_adjoint(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t_end,
+                 int32_t n_steps, void* stream);
 
 /* Tuning of the update kernels: `chunk` x planes per block, `vec` z cells per thread
  * (1, 2 or 4, dividing nz); 0 restores a default.  Invalidates a cached CUDA graph.
