@@ -130,6 +130,8 @@ class AdjointBuffers(C.Structure):
     ]
 
 
+NOALLOC_SCRATCH_FLOATS = 65536  # FDTD_NOALLOC_SCRATCH_FLOATS
+
 LIB_PATH = Path(__file__).resolve().parent / "libfdtd_gb300.so"
 _lib: C.CDLL | None = None
 
@@ -154,6 +156,11 @@ SIGNATURES = {
     "fdtd_plan_tune_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "fdtd_plan_uses_tma": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_status": (C.c_int, [C.c_void_p]),
+    "fdtd_detector_sample_noalloc": (
+        C.c_int,
+        [C.POINTER(DetectorDesc), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_void_p, C.c_void_p,
+         C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p],
+    ),
     "fdtd_profile_forward": (
         C.c_int,
         [C.c_void_p, C.POINTER(Buffers), C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p],

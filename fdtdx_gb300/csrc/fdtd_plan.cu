@@ -1020,3 +1020,4 @@ extern "C" int fdtd_plan_status(FdtdPlan* p) {
     }
     return FDTD_OK;
 }
+#include "fdtd_noalloc.cuh"

@@ -224,6 +224,32 @@ int32_t fdtd_launches_per_step(const FdtdPlan* plan);
  * [4] detectors, [5] interface recording.  Synchronises the stream. */
 int fdtd_profile_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_steps, float* out_ms, void* stream);
 
+/* Allocation-free sample of one volume-reducing detector (no counterpart in the
+ * reference: there the sample is part of the jitted step, fdtdx/fdtd/update.py:1040-1137).
+ *
+ * Evaluates the reduced value a FIELD (component mean), FLUX (Poynting flux summed over
+ * the region times cell_weight) or ENERGY (energy summed times cell_weight) detector
+ * records at one step, from the fields E (after the step), H_prev (H before the step's H
+ * update; read only when det->exact_interpolation) and H, and writes its ncomp floats to
+ * the device buffer `out` (ncomp: the recorded components for FIELD, 3 or 1 for FLUX,
+ * 1 for ENERGY).  det->slot, det->weights and det->reduce_volume are ignored.
+ *
+ * It needs no plan and allocates no device memory: the block partial sums live in a
+ * static device array of FDTD_NOALLOC_SCRATCH_FLOATS floats, so a region needing more
+ * than that many partials (ceil(cells / 256) x ncomp) is rejected with FDTD_EINVAL and a
+ * message on stderr.  Nothing in the scratch has to start at zero: every partial is
+ * written before it is read, and the step word and slot table it also holds are
+ * zero-initialised with the library and never written.  The first call on a device
+ * looks up the scratch address (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture.  The scratch is shared by all calls on a
+ * device: calls that overlap (other streams, other host threads) race on it and must be
+ * serialised by the caller.  Same arithmetic as the plan's detector kernels. */
+#define FDTD_NOALLOC_SCRATCH_FLOATS 65536
+int fdtd_detector_sample_noalloc(const FdtdDetectorDesc* det, int32_t nx, int32_t ny, int32_t nz,
+                                 const int32_t periodic[3], const float* E, const float* H_prev, const float* H,
+                                 const float* inv_eps, int32_t n_eps, const float* inv_mu, int32_t n_mu,
+                                 float inv_mu_scalar, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
