@@ -67,7 +67,20 @@ struct AdjArgs {
     float* lpH_out[FDTD_MAX_SLABS][2];
     float* grad_ie;        // (n_eps, N), accumulated; nullptr: not wanted
     DBox hp;               // detector cotangents of H before the H update (added to lam H(t), then cleared)
+    // the boxes a launch covers (the layout of UpdArgs' box table, read by column_of)
+    int nbox;
+    int blo[6][3], bhi[6][3], bchunk[6], nbx[6], bstart[7];
+    int bslab[6];          // per box: bit s set when slab s can reach the box or its one-cell rim
 };
+
+// The slab mask of this block's box.
+__device__ __forceinline__ int block_slab_mask(const AdjArgs& a) {
+    int m = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        if (q < a.nbox && (int)blockIdx.x >= a.bstart[q]) m = a.bslab[q];
+    return m;
+}
 
 __device__ __forceinline__ float adj_mat(const float* m, int n, float scalar, long long N, int comp, long long c) {
     if (!m) return scalar;
@@ -82,15 +95,23 @@ __device__ __forceinline__ bool wrap_idx(const Geo& g, int& i, int& j, int& k) {
     return true;
 }
 
-// Cotangents D[6] of the six raw differences of one half-step at cell (i, j, k), in the
-// order the forward kernels use: (dy Fz, dz Fy, dz Fx, dx Fz, dx Fy, dy Fx).  HSIDE selects
-// the H-step (F = E3, lam = lam H3, PMC, inv_mu, psi_H) or the E-step (F = H, lam = lam E3,
-// PEC, inv_eps, psi_E).  lc[comp] is the cotangent of curl[comp]: -c im/e lam (H) or
-// c ie/d lam (E).  A CPML slab adds psi' = b psi + a d and curl corrections
-// (-c1 on curl[(a+1)%3], +c2 on curl[(a+2)%3], c = psi' (+ (1/kappa - 1) d)), whose
-// transposes feed D and, at the centre cell (OUT), the psi cotangent of step t.
-template <bool HSIDE, bool OUT>
-__device__ __forceinline__ void lam_diff(const AdjArgs& a, int i, int j, int k, float D[6]) {
+// The slab a cell lies in along one axis: its layer index l (out: -1 when outside).
+__device__ __forceinline__ int slab_layer(const DSlab& sl, int i, int j, int k) {
+    const int x = sl.axis == 0 ? i : (sl.axis == 1 ? j : k);
+    const int l = x - sl.lo;
+    return (unsigned)l < (unsigned)sl.L ? l : -1;
+}
+
+// Cotangents D[6] of the six raw differences of one half-step at cell (i, j, k) (wrapped
+// with the halo rule; zero in a zero halo), in the order the forward kernels use:
+// (dy Fz, dz Fy, dz Fx, dx Fz, dx Fy, dy Fx).  HSIDE selects the H-step (F = E3, lam =
+// lam H3, PMC, inv_mu, psi_H) or the E-step (F = H, lam = lam E3, PEC, inv_eps, psi_E).
+// lc[comp] is the cotangent of curl[comp]: -c im/e lam (H) or c ie/d lam (E).  A CPML slab
+// adds psi' = b psi + a d and curl corrections (-c1 on curl[(a+1)%3], +c2 on curl[(a+2)%3],
+// c = psi' (+ (1/kappa - 1) d)); their transposes feed D and, when `out` (the cell is the
+// caller's own), the psi cotangent of step t.  PML = false: the cell lies in no slab.
+template <bool HSIDE, bool PML>
+__device__ __forceinline__ void dcell(const AdjArgs& a, int i, int j, int k, bool out, float D[6], int smask = 63) {
     const Geo& g = a.g;
 #pragma unroll
     for (int q = 0; q < 6; ++q) D[q] = 0.f;
@@ -116,82 +137,97 @@ __device__ __forceinline__ void lam_diff(const AdjArgs& a, int i, int j, int k, 
         }
     }
     D[0] = lc[0]; D[1] = -lc[0]; D[2] = lc[1]; D[3] = -lc[1]; D[4] = lc[2]; D[5] = -lc[2];
-    const int idx3[3] = {i, j, k};
+    if (!PML) return;
 #pragma unroll
     for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
         if (s >= a.n_slab) break;
+        if (!(smask >> s & 1)) continue;
         const DSlab& sl = a.slab[s];
-        const int l = idx3[sl.axis] - sl.lo;
-        if ((unsigned)l >= (unsigned)sl.L) continue;
+        const int l = slab_layer(sl, i, j, k);
+        if (l < 0) continue;
         const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
         const long long p = psi_offset(sl, i, j, k);
-        const int ci = (sl.axis + 1) % 3, cj = (sl.axis + 2) % 3;
-        const float* const* lp = HSIDE ? a.lpH[s] : a.lpE[s];
-        const float t1 = lp[0][p] - lc[ci];  // cotangent of psi1' (state output + correction c1)
-        const float t2 = lp[1][p] + lc[cj];
+        const float lci = sl.axis == 0 ? lc[1] : (sl.axis == 1 ? lc[2] : lc[0]);  // curl[(a+1)%3]
+        const float lcj = sl.axis == 0 ? lc[2] : (sl.axis == 1 ? lc[0] : lc[1]);  // curl[(a+2)%3]
+        const float* lp0 = HSIDE ? a.lpH[s][0] : a.lpE[s][0];
+        const float* lp1 = HSIDE ? a.lpH[s][1] : a.lpE[s][1];
+        const float t1 = lp0[p] - lci;  // cotangent of psi1' (state output + correction c1)
+        const float t2 = lp1[p] + lcj;
         const float ca = __ldg(co + l);
         float d1 = ca * t1, d2 = ca * t2;
         if (!sl.kappa_one) {
             const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
-            d1 -= ikm1 * lc[ci];
-            d2 += ikm1 * lc[cj];
+            d1 -= ikm1 * lci;
+            d2 += ikm1 * lcj;
         }
         if (sl.axis == 0) { D[3] += d1; D[4] += d2; }
         else if (sl.axis == 1) { D[5] += d1; D[0] += d2; }
         else { D[1] += d1; D[2] += d2; }
-        if (OUT) {
+        if (out) {
             const float cb = __ldg(co + sl.L + l);
-            float* const* lo = HSIDE ? a.lpH_out[s] : a.lpE_out[s];
-            lo[0][p] = cb * t1;
-            lo[1][p] = cb * t2;
+            float* o0 = HSIDE ? a.lpH_out[s][0] : a.lpE_out[s][0];
+            float* o1 = HSIDE ? a.lpH_out[s][1] : a.lpE_out[s][1];
+            o0[p] = cb * t1;
+            o1[p] = cb * t2;
         }
     }
 }
 
-// Transpose of the H-step: lam E3 = lam E(t+1) + (forward differences)^T lam D.  E3(c)
-// enters D(c) with a minus sign and D(c - axis) with a plus sign.
+// Transpose of the H-step: lam E3 = lam E(t+1) + (forward differences)^T D, in place.
+// E3(c) enters D(c) with a minus sign and D(c - axis) with a plus sign.  A thread owns VEC
+// z cells of one (j) row and marches along +x, carrying D(c - x) in registers.
+template <int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_adj_H(const __grid_constant__ AdjArgs a) {
     const Geo& g = a.g;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.N) return;
-    const int k = (int)(c % g.nz);
-    const int j = (int)((c / g.nz) % g.ny);
-    const int i = (int)(c / ((long long)g.nz * g.ny));
-    float D[6], Dx[6], Dy[6], Dz[6];
-    lam_diff<true, true>(a, i, j, k, D);
-    lam_diff<true, false>(a, i - 1, j, k, Dx);
-    lam_diff<true, false>(a, i, j - 1, k, Dy);
-    lam_diff<true, false>(a, i, j, k - 1, Dz);
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
     const long long N = g.N;
-    a.lE[c] += (Dz[2] - D[2]) + (Dy[5] - D[5]);
-    a.lE[N + c] += (Dz[1] - D[1]) + (Dx[4] - D[4]);
-    a.lE[2 * N + c] += (Dy[0] - D[0]) + (Dx[3] - D[3]);
+    const int sm = PML ? block_slab_mask(a) : 0;
+    float Dxm[VEC][2];  // D3, D4 at (i - 1)
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+        float D[6];
+        dcell<true, PML>(a, i0 - 1, j, k0 + e, false, D, sm);
+        Dxm[e][0] = D[3];
+        Dxm[e][1] = D[4];
+    }
+    for (int i = i0; i < i1; ++i) {
+        const long long c = cell_index(g, i, j, k0);
+        float Dz[6];
+        dcell<true, PML>(a, i, j, k0 - 1, false, Dz, sm);
+        Vec<VEC> lE[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) lE[comp] = ldv_rw<VEC>(a.lE + comp * N + c);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            float D[6], Dy[6];
+            dcell<true, PML>(a, i, j, k0 + e, true, D, sm);
+            dcell<true, PML>(a, i, j - 1, k0 + e, false, Dy, sm);
+            lE[0].v[e] += (Dz[2] - D[2]) + (Dy[5] - D[5]);
+            lE[1].v[e] += (Dz[1] - D[1]) + (Dxm[e][1] - D[4]);
+            lE[2].v[e] += (Dy[0] - D[0]) + (Dxm[e][0] - D[3]);
+            Dxm[e][0] = D[3];
+            Dxm[e][1] = D[4];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) Dz[q] = D[q];
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) stv<VEC>(a.lE + comp * N + c, lE[comp]);
+    }
 }
 
-// curl_H of the reconstructed H at (i, j, k) with the CPML psi advanced from the frozen
-// psi_E (psi' = bE psi + aE d, not stored), as the forward E-step evaluates it.
-__device__ __forceinline__ void curl_H_at(const AdjArgs& a, int i, int j, int k, float cu[3]) {
-    const Geo& g = a.g;
-    const float* H = a.H;
-    const long long c = cell_index(g, i, j, k);
-    const float hx = __ldg(H + c), hy = __ldg(H + g.N + c), hz = __ldg(H + 2 * g.N + c);
-    float d[6];
-    d[0] = hz - ld_halo(g, H, 2, i, j - 1, k);
-    d[1] = hy - ld_halo(g, H, 1, i, j, k - 1);
-    d[2] = hx - ld_halo(g, H, 0, i, j, k - 1);
-    d[3] = hz - ld_halo(g, H, 2, i - 1, j, k);
-    d[4] = hy - ld_halo(g, H, 1, i - 1, j, k);
-    d[5] = hx - ld_halo(g, H, 0, i, j - 1, k);
-    cu[0] = d[0] - d[1];
-    cu[1] = d[2] - d[3];
-    cu[2] = d[4] - d[5];
-    const int idx3[3] = {i, j, k};
+// curl_H of the reconstructed H at (i, j, k) given its six raw differences d[], with the
+// CPML psi advanced from the frozen psi_E (psi' = bE psi + aE d, not stored), as the
+// forward E-step evaluates it.
+__device__ __forceinline__ void curl_H_cpml(const AdjArgs& a, int i, int j, int k, const float d[6], float cu[3],
+                                            int smask) {
 #pragma unroll
     for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
         if (s >= a.n_slab) break;
+        if (!(smask >> s & 1)) continue;
         const DSlab& sl = a.slab[s];
-        const int l = idx3[sl.axis] - sl.lo;
-        if ((unsigned)l >= (unsigned)sl.L) continue;
+        const int l = slab_layer(sl, i, j, k);
+        if (l < 0) continue;
         const float d1 = sl.axis == 0 ? d[3] : (sl.axis == 1 ? d[5] : d[1]);
         const float d2 = sl.axis == 0 ? d[4] : (sl.axis == 1 ? d[0] : d[2]);
         const float* co = sl.coef;
@@ -211,72 +247,519 @@ __device__ __forceinline__ void curl_H_at(const AdjArgs& a, int i, int j, int k,
 }
 
 // Transpose of the E-step: lam E(t) = (f/d) PEC(lam E3); lam H(t) = (g/e) PMC(lam H3) +
-// (backward differences)^T lam D + the detectors' H-before-update part.  H(c) enters D(c)
-// with a plus sign and D(c + axis) with a minus sign.  The inv_eps cotangent of the cell
-// is lam E1 . dE1/d ie with dE1/d ie = (c curl - (c sigma eta0 / 2)(E + E1)) / d.
+// (backward differences)^T D + the detectors' H-before-update part.  H(c) enters D(c) with
+// a plus sign and D(c + axis) with a minus sign.  The inv_eps cotangent of the cell is
+// lam E1 . dE1/d ie with dE1/d ie = (c curl - (c sigma eta0 / 2)(E + E1)) / d, curl_H taken
+// at the reconstructed H (whose x-neighbour below is carried in registers).  Marches along
+// +x carrying D(c + x), computed one plane ahead.
+template <int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_adj_E(const __grid_constant__ AdjArgs a) {
     const Geo& g = a.g;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.N) return;
-    const int k = (int)(c % g.nz);
-    const int j = (int)((c / g.nz) % g.ny);
-    const int i = (int)(c / ((long long)g.nz * g.ny));
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
     const long long N = g.N;
-    float D[6], Dx[6], Dy[6], Dz[6];
-    lam_diff<false, true>(a, i, j, k, D);
-    lam_diff<false, false>(a, i + 1, j, k, Dx);
-    lam_diff<false, false>(a, i, j + 1, k, Dy);
-    lam_diff<false, false>(a, i, j, k + 1, Dz);
-    float lh[3];
-    lh[0] = (D[2] - Dz[2]) + (D[5] - Dy[5]);
-    lh[1] = (D[1] - Dz[1]) + (D[4] - Dx[4]);
-    lh[2] = (D[0] - Dy[0]) + (D[3] - Dx[3]);
-    long long q;
-    const bool in_hp = a.hp.buf && box_local(a.hp, i, j, k, q);
+    const long long sy = g.nz;
+    const float* __restrict__ H = a.H;
+    const bool want_grad = a.grad_ie != nullptr;
+    const int sm = PML ? block_slab_mask(a) : 0;
+    float Dc[VEC][6];  // D at (i, j, k0 + e)
 #pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-        float l1 = a.lH[comp * N + c];
-        if (g.pmc && face_zero(g, g.pmc, comp, i, j, k)) l1 = 0.f;
-        if (a.sigH) {
-            const float m = adj_mat(a.im, a.n_mu, a.im_scalar, N, comp, c);
-            const float qh = g.c * adj_mat(a.sigH, a.n_sigH, 0.f, N, comp, c) / g.eta0 * m / 2.f;
-            l1 *= (1.f - qh) / (1.f + qh);
-        }
-        float v = l1 + lh[comp];
-        if (in_hp) {
-            float* hp = a.hp.buf + comp * a.hp.M + q;
-            v += *hp;
-            *hp = 0.f;
-        }
-        a.lH_out[comp * N + c] = v;
+    for (int e = 0; e < VEC; ++e) dcell<false, PML>(a, i0, j, k0 + e, true, Dc[e], sm);
+    Vec<VEC> Hy_m, Hz_m;
+    if (want_grad) {
+        Hy_m = ldv_halo<VEC>(g, H, 1, i0 - 1, j, k0);
+        Hz_m = ldv_halo<VEC>(g, H, 2, i0 - 1, j, k0);
     }
-    float cu[3] = {0.f, 0.f, 0.f};
-    if (a.grad_ie) curl_H_at(a, i, j, k, cu);
-    float gsum = 0.f;
+    for (int i = i0; i < i1; ++i) {
+        const long long c = cell_index(g, i, j, k0);
+        float Dtop[6];
+        dcell<false, PML>(a, i, j, k0 + VEC, false, Dtop, sm);
+        Vec<VEC> lh[3], le[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            lh[comp] = ldv<VEC>(a.lH + comp * N + c);
+            le[comp] = ldv<VEC>(a.lE + comp * N + c);
+        }
+        Vec<VEC> Hx, Hy, Hz, Hz_jm, Hx_jm;
+        float Hy_k = 0.f, Hx_k = 0.f;
+        if (want_grad) {
+            Hx = ldv<VEC>(H + c); Hy = ldv<VEC>(H + N + c); Hz = ldv<VEC>(H + 2 * N + c);
+            Hz_jm = nbv<VEC>(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k0);
+            Hx_jm = nbv<VEC>(g, H, c - sy, j > 0, 0, i, j - 1, k0);
+            Hy_k = nb(g, H, N + c - 1, k0 > 0, 1, i, j, k0 - 1);
+            Hx_k = nb(g, H, c - 1, k0 > 0, 0, i, j, k0 - 1);
+        }
+        Vec<VEC> outH[3], outE[3];
+        float gsum[VEC];
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int k = k0 + e;
+            float Dx[6], Dy[6];
+            dcell<false, PML>(a, i + 1, j, k, i + 1 < i1, Dx, sm);
+            dcell<false, PML>(a, i, j + 1, k, false, Dy, sm);
+            const float* Dz = e + 1 < VEC ? Dc[(e + 1) % VEC] : Dtop;
+            float lht[3];
+            lht[0] = (Dc[e][2] - Dz[2]) + (Dc[e][5] - Dy[5]);
+            lht[1] = (Dc[e][1] - Dz[1]) + (Dc[e][4] - Dx[4]);
+            lht[2] = (Dc[e][0] - Dy[0]) + (Dc[e][3] - Dx[3]);
+            long long q;
+            const bool in_hp = a.hp.buf && box_local(a.hp, i, j, k, q);
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp) {
+                float l1 = lh[comp].v[e];
+                if (g.pmc && face_zero(g, g.pmc, comp, i, j, k)) l1 = 0.f;
+                if (a.sigH) {
+                    const float m = adj_mat(a.im, a.n_mu, a.im_scalar, N, comp, c + e);
+                    const float qh = g.c * adj_mat(a.sigH, a.n_sigH, 0.f, N, comp, c + e) / g.eta0 * m / 2.f;
+                    l1 *= (1.f - qh) / (1.f + qh);
+                }
+                float v = l1 + lht[comp];
+                if (in_hp) {
+                    float* hp = a.hp.buf + comp * a.hp.M + q;
+                    v += *hp;
+                    *hp = 0.f;
+                }
+                outH[comp].v[e] = v;
+            }
+            float cu[3] = {0.f, 0.f, 0.f};
+            if (want_grad) {
+                const float hy_km = e == 0 ? Hy_k : Hy.v[e - 1];
+                const float hx_km = e == 0 ? Hx_k : Hx.v[e - 1];
+                const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
+                                    Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
+                cu[0] = d[0] - d[1];
+                cu[1] = d[2] - d[3];
+                cu[2] = d[4] - d[5];
+                if (PML) curl_H_cpml(a, i, j, k, d, cu, sm);
+            }
+            gsum[e] = 0.f;
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp) {
+                float l1 = le[comp].v[e];
+                if (g.pec && face_zero(g, g.pec, comp, i, j, k)) l1 = 0.f;
+                float lo = l1, dm = g.c * cu[comp];
+                if (a.sigE) {
+                    const float m = adj_mat(a.ie, a.n_eps, 1.f, N, comp, c + e);
+                    const float hs = g.c * adj_mat(a.sigE, a.n_sigE, 0.f, N, comp, c + e) * g.eta0 / 2.f;
+                    const float qe = hs * m;
+                    const float den = 1.f + qe;
+                    lo = l1 * (1.f - qe) / den;
+                    if (want_grad) {
+                        const float e0 = __ldg(a.E + comp * N + c + e);
+                        const float e1 = ((1.f - qe) * e0 + g.c * cu[comp] * m) / den;
+                        dm = (g.c * cu[comp] - hs * (e0 + e1)) / den;
+                    }
+                }
+                outE[comp].v[e] = lo;
+                if (want_grad) {
+                    if (a.n_eps == 3) a.grad_ie[comp * N + c + e] += l1 * dm;
+                    else gsum[e] += l1 * dm;
+                }
+            }
+#pragma unroll
+            for (int q2 = 0; q2 < 6; ++q2) Dc[e][q2] = Dx[q2];
+        }
+        if (want_grad && a.n_eps != 3) {
+            Vec<VEC> gr = ldv_rw<VEC>(a.grad_ie + c);
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) gr.v[e] += gsum[e];
+            stv<VEC>(a.grad_ie + c, gr);
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            stv<VEC>(a.lH_out + comp * N + c, outH[comp]);
+            stv<VEC>(a.lE_out + comp * N + c, outE[comp]);
+        }
+        if (want_grad) {
+            Hy_m = Hy;
+            Hz_m = Hz;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Slab-free core of the transposed half-steps.  Without CPML terms the difference
+// cotangents of a cell are D = (lc0, -lc0, lc1, -lc1, lc2, -lc2), so the transposes are
+// curls of the scaled cotangent field lc:
+//   transposed H-step  lam E3 += curl_H(lcH),  lcH = -c im / e PMC(lam H3)   (backward differences)
+//   transposed E-step  lam H  = (g/e) PMC(lam H3) + curl_E(lcE),  lcE = c ie / d PEC(lam E3)   (forward)
+// i.e. the forward E and H updates with the material moved inside the difference.
+// ---------------------------------------------------------------------------------
+
+// lc of one component at cell c = (i, j, k) from the raw cotangent l there.
+template <bool HSIDE>
+__device__ __forceinline__ float lc_of(const AdjArgs& a, int comp, int i, int j, int k, long long c, float l) {
+    const Geo& g = a.g;
+    const long long N = g.N;
+    const int mask = HSIDE ? g.pmc : g.pec;
+    if (mask && face_zero(g, mask, comp, i, j, k)) return 0.f;
+    if (HSIDE) {
+        const float m = a.im ? __ldg(a.im + (a.n_mu == 3 ? comp * N : 0) + c) : a.im_scalar;
+        float den = 1.f;
+        if (a.sigH) den = 1.f + g.c * __ldg(a.sigH + (a.n_sigH == 3 ? comp * N : 0) + c) / g.eta0 * m / 2.f;
+        return -(g.c * m / den) * l;
+    }
+    const float m = __ldg(a.ie + (a.n_eps == 3 ? comp * N : 0) + c);
+    float den = 1.f;
+    if (a.sigE) den = 1.f + g.c * __ldg(a.sigE + (a.n_sigE == 3 ? comp * N : 0) + c) * g.eta0 * m / 2.f;
+    return (g.c * m / den) * l;
+}
+
+// lc of one component at a neighbour (wrapped with the halo rule; zero in a zero halo).
+template <bool HSIDE>
+__device__ __forceinline__ float lc_nb(const AdjArgs& a, int comp, int i, int j, int k) {
+    if (!wrap_idx(a.g, i, j, k)) return 0.f;
+    const long long c = cell_index(a.g, i, j, k);
+    const float* L = HSIDE ? a.lH : a.lE;
+    return lc_of<HSIDE>(a, comp, i, j, k, c, L[comp * a.g.N + c]);
+}
+
+template <bool HSIDE, int VEC>
+__device__ __forceinline__ Vec<VEC> lc_vec(const AdjArgs& a, int comp, int i, int j, int k0, long long c,
+                                           const Vec<VEC>& l) {
+    Vec<VEC> r;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r.v[e] = lc_of<HSIDE>(a, comp, i, j, k0 + e, c + e, l.v[e]);
+    return r;
+}
+
+// lc of a VEC row one cell away along x or y (all VEC cells share the halo test).
+template <bool HSIDE, int VEC>
+__device__ __forceinline__ Vec<VEC> lc_row(const AdjArgs& a, int comp, int i, int j, int k0) {
+    const Geo& g = a.g;
+    Vec<VEC> r;
+    if (!wrap_idx(g, i, j, k0)) {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) r.v[e] = 0.f;
+        return r;
+    }
+    const long long c = cell_index(g, i, j, k0);
+    const float* L = HSIDE ? a.lH : a.lE;
+    return lc_vec<HSIDE, VEC>(a, comp, i, j, k0, c, ldv<VEC>(L + comp * g.N + c));
+}
+
+// Transposed H-step over the core: lam E3 += curl_H(lcH), in place.
+template <int VEC>
+__global__ void __launch_bounds__(256) k_adj_H_core(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    const long long N = g.N;
+    Vec<VEC> ly_m = lc_row<true, VEC>(a, 1, i0 - 1, j, k0);  // lc1, lc2 at (i - 1)
+    Vec<VEC> lz_m = lc_row<true, VEC>(a, 2, i0 - 1, j, k0);
+    for (int i = i0; i < i1; ++i) {
+        const long long c = cell_index(g, i, j, k0);
+        Vec<VEC> l[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) l[comp] = lc_vec<true, VEC>(a, comp, i, j, k0, c, ldv<VEC>(a.lH + comp * N + c));
+        const Vec<VEC> l0_jm = lc_row<true, VEC>(a, 0, i, j - 1, k0);
+        const Vec<VEC> l2_jm = lc_row<true, VEC>(a, 2, i, j - 1, k0);
+        const float l0_km = lc_nb<true>(a, 0, i, j, k0 - 1);
+        const float l1_km = lc_nb<true>(a, 1, i, j, k0 - 1);
+        Vec<VEC> lE[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) lE[comp] = ldv_rw<VEC>(a.lE + comp * N + c);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const float a0 = e == 0 ? l0_km : l[0].v[e - 1];
+            const float a1 = e == 0 ? l1_km : l[1].v[e - 1];
+            lE[0].v[e] += (l[2].v[e] - l2_jm.v[e]) - (l[1].v[e] - a1);
+            lE[1].v[e] += (l[0].v[e] - a0) - (l[2].v[e] - lz_m.v[e]);
+            lE[2].v[e] += (l[1].v[e] - ly_m.v[e]) - (l[0].v[e] - l0_jm.v[e]);
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) stv<VEC>(a.lE + comp * N + c, lE[comp]);
+        ly_m = l[1];
+        lz_m = l[2];
+    }
+}
+
+// Transposed E-step over the core: lam H(t) = (g/e) PMC(lam H3) + curl_E(lcE) (+ detector
+// part), lam E(t) = (f/d) PEC(lam E3), and the inv_eps cotangent.
+template <int VEC>
+__global__ void __launch_bounds__(256) k_adj_E_core(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    const long long N = g.N;
+    const long long sy = g.nz;
+    const float* __restrict__ H = a.H;
+    const bool want_grad = a.grad_ie != nullptr;
+    Vec<VEC> l[3];  // lcE at (i)
+    {
+        const long long c = cell_index(g, i0, j, k0);
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) l[comp] = lc_vec<false, VEC>(a, comp, i0, j, k0, c, ldv<VEC>(a.lE + comp * N + c));
+    }
+    Vec<VEC> Hy_m, Hz_m;
+    if (want_grad) {
+        Hy_m = ldv_halo<VEC>(g, H, 1, i0 - 1, j, k0);
+        Hz_m = ldv_halo<VEC>(g, H, 2, i0 - 1, j, k0);
+    }
+    for (int i = i0; i < i1; ++i) {
+        const long long c = cell_index(g, i, j, k0);
+        Vec<VEC> ln[3];  // lcE at (i + 1)
+#pragma unroll
+        for (int comp = 1; comp < 3; ++comp) ln[comp] = lc_row<false, VEC>(a, comp, i + 1, j, k0);
+        const Vec<VEC> l0_jp = lc_row<false, VEC>(a, 0, i, j + 1, k0);
+        const Vec<VEC> l2_jp = lc_row<false, VEC>(a, 2, i, j + 1, k0);
+        const float l0_kp = lc_nb<false>(a, 0, i, j, k0 + VEC);
+        const float l1_kp = lc_nb<false>(a, 1, i, j, k0 + VEC);
+        Vec<VEC> le[3], lh[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            le[comp] = ldv<VEC>(a.lE + comp * N + c);
+            lh[comp] = ldv<VEC>(a.lH + comp * N + c);
+        }
+        Vec<VEC> Hx, Hy, Hz, Hz_jm, Hx_jm;
+        float Hy_k = 0.f, Hx_k = 0.f;
+        if (want_grad) {
+            Hx = ldv<VEC>(H + c); Hy = ldv<VEC>(H + N + c); Hz = ldv<VEC>(H + 2 * N + c);
+            Hz_jm = nbv<VEC>(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k0);
+            Hx_jm = nbv<VEC>(g, H, c - sy, j > 0, 0, i, j - 1, k0);
+            Hy_k = nb(g, H, N + c - 1, k0 > 0, 1, i, j, k0 - 1);
+            Hx_k = nb(g, H, c - 1, k0 > 0, 0, i, j, k0 - 1);
+        }
+        Vec<VEC> outH[3], outE[3], gr;
+        if (want_grad && a.n_eps != 3) gr = ldv_rw<VEC>(a.grad_ie + c);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int k = k0 + e;
+            const float b0 = e + 1 < VEC ? l[0].v[(e + 1) % VEC] : l0_kp;
+            const float b1 = e + 1 < VEC ? l[1].v[(e + 1) % VEC] : l1_kp;
+            float lht[3];
+            lht[0] = (l2_jp.v[e] - l[2].v[e]) - (b1 - l[1].v[e]);
+            lht[1] = (b0 - l[0].v[e]) - (ln[2].v[e] - l[2].v[e]);
+            lht[2] = (ln[1].v[e] - l[1].v[e]) - (l0_jp.v[e] - l[0].v[e]);
+            long long q = 0;
+            const bool in_hp = a.hp.buf && box_local(a.hp, i, j, k, q);
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp) {
+                float l1 = lh[comp].v[e];
+                if (g.pmc && face_zero(g, g.pmc, comp, i, j, k)) l1 = 0.f;
+                if (a.sigH) {
+                    const float m = a.im ? __ldg(a.im + (a.n_mu == 3 ? comp * N : 0) + c + e) : a.im_scalar;
+                    const float qh = g.c * __ldg(a.sigH + (a.n_sigH == 3 ? comp * N : 0) + c + e) / g.eta0 * m / 2.f;
+                    l1 *= (1.f - qh) / (1.f + qh);
+                }
+                float v = l1 + lht[comp];
+                if (in_hp) {
+                    float* hp = a.hp.buf + comp * a.hp.M + q;
+                    v += *hp;
+                    *hp = 0.f;
+                }
+                outH[comp].v[e] = v;
+            }
+            float cu[3] = {0.f, 0.f, 0.f};
+            if (want_grad) {
+                const float hy_km = e == 0 ? Hy_k : Hy.v[e - 1];
+                const float hx_km = e == 0 ? Hx_k : Hx.v[e - 1];
+                cu[0] = (Hz.v[e] - Hz_jm.v[e]) - (Hy.v[e] - hy_km);
+                cu[1] = (Hx.v[e] - hx_km) - (Hz.v[e] - Hz_m.v[e]);
+                cu[2] = (Hy.v[e] - Hy_m.v[e]) - (Hx.v[e] - Hx_jm.v[e]);
+            }
+            float gs = 0.f;
+#pragma unroll
+            for (int comp = 0; comp < 3; ++comp) {
+                float l1 = le[comp].v[e];
+                if (g.pec && face_zero(g, g.pec, comp, i, j, k)) l1 = 0.f;
+                float lo = l1, dm = g.c * cu[comp];
+                if (a.sigE) {
+                    const float m = __ldg(a.ie + (a.n_eps == 3 ? comp * N : 0) + c + e);
+                    const float hs = g.c * __ldg(a.sigE + (a.n_sigE == 3 ? comp * N : 0) + c + e) * g.eta0 / 2.f;
+                    const float qe = hs * m;
+                    const float den = 1.f + qe;
+                    lo = l1 * (1.f - qe) / den;
+                    if (want_grad) {
+                        const float e0 = __ldg(a.E + comp * N + c + e);
+                        const float e1 = ((1.f - qe) * e0 + g.c * cu[comp] * m) / den;
+                        dm = (g.c * cu[comp] - hs * (e0 + e1)) / den;
+                    }
+                }
+                outE[comp].v[e] = lo;
+                if (want_grad) {
+                    if (a.n_eps == 3) a.grad_ie[comp * N + c + e] += l1 * dm;
+                    else gs += l1 * dm;
+                }
+            }
+            if (want_grad && a.n_eps != 3) gr.v[e] += gs;
+        }
+        if (want_grad && a.n_eps != 3) stv<VEC>(a.grad_ie + c, gr);
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            stv<VEC>(a.lH_out + comp * N + c, outH[comp]);
+            stv<VEC>(a.lE_out + comp * N + c, outE[comp]);
+        }
+        // lcE at (i + 1) becomes lcE at (i); its x component was not needed above
+        ln[0] = lc_row<false, VEC>(a, 0, i + 1, j, k0);
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) l[comp] = ln[comp];
+        if (want_grad) {
+            Hy_m = Hy;
+            Hz_m = Hz;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Fast forms of the core kernels for the common case: the core box lies strictly inside
+// the grid (no halo), no conductivity, no PEC/PMC faces and (transposed H-step) a scalar
+// inv_mu.  Then lcH = -c im lam H3 is a uniform scale and lcE = c ie lam E3 a pointwise
+// product, and lam E(t) = lam E3.  Addresses advance by one x plane per iteration.
+// ---------------------------------------------------------------------------------
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> vmul(const Vec<VEC>& x, const Vec<VEC>& y) {
+    Vec<VEC> r;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r.v[e] = x.v[e] * y.v[e];
+    return r;
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(256) k_adj_H_core_s(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    const long long N = g.N;
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const float s = -g.c * a.im_scalar;
+    const float* __restrict__ lH = a.lH + cell_index(g, i0, j, k0);
+    float* lE = a.lE + cell_index(g, i0, j, k0);
+    Vec<VEC> y_m = ldv<VEC>(lH + N - sx), z_m = ldv<VEC>(lH + 2 * N - sx);  // lam H3 y, z at (i - 1)
+    for (int i = i0; i < i1; ++i, lH += sx, lE += sx) {
+        const Vec<VEC> x = ldv<VEC>(lH), y = ldv<VEC>(lH + N), z = ldv<VEC>(lH + 2 * N);
+        const Vec<VEC> x_jm = ldv<VEC>(lH - sy), z_jm = ldv<VEC>(lH + 2 * N - sy);
+        const float x_km = __ldg(lH - 1), y_km = __ldg(lH + N - 1);
+        Vec<VEC> e0 = ldv_rw<VEC>(lE), e1 = ldv_rw<VEC>(lE + N), e2 = ldv_rw<VEC>(lE + 2 * N);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const float xk = e == 0 ? x_km : x.v[e - 1];
+            const float yk = e == 0 ? y_km : y.v[e - 1];
+            e0.v[e] += s * ((z.v[e] - z_jm.v[e]) - (y.v[e] - yk));
+            e1.v[e] += s * ((x.v[e] - xk) - (z.v[e] - z_m.v[e]));
+            e2.v[e] += s * ((y.v[e] - y_m.v[e]) - (x.v[e] - x_jm.v[e]));
+        }
+        stv<VEC>(lE, e0);
+        stv<VEC>(lE + N, e1);
+        stv<VEC>(lE + 2 * N, e2);
+        y_m = y;
+        z_m = z;
+    }
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(256, 3) k_adj_E_core_s(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    const long long N = g.N;
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const long long c0 = cell_index(g, i0, j, k0);
+    const bool iso = a.n_eps != 3;
+    const long long mN = iso ? 0 : N;  // component stride of inv_eps
+    const float cc = g.c;
+    const float* __restrict__ lE = a.lE + c0;
+    const float* __restrict__ lH = a.lH + c0;
+    const float* __restrict__ ie = a.ie + c0;
+    const float* __restrict__ H = a.H + c0;
+    float* lEo = a.lE_out + c0;
+    float* lHo = a.lH_out + c0;
+    float* gr = a.grad_ie ? a.grad_ie + c0 : nullptr;
+    // lam E3 and ie lam E3 at (i)
+    Vec<VEC> le[3], lc[3];
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-        float l1 = a.lE[comp * N + c];
-        if (g.pec && face_zero(g, g.pec, comp, i, j, k)) l1 = 0.f;
-        const float m = adj_mat(a.ie, a.n_eps, 1.f, N, comp, c);
-        float le = l1, dm = g.c * cu[comp];
-        if (a.sigE) {
-            const float hs = g.c * adj_mat(a.sigE, a.n_sigE, 0.f, N, comp, c) * g.eta0 / 2.f;
-            const float qe = hs * m;
-            const float den = 1.f + qe;
-            le = l1 * (1.f - qe) / den;
-            if (a.grad_ie) {
-                const float e0 = __ldg(a.E + comp * N + c);
-                const float e1 = ((1.f - qe) * e0 + g.c * cu[comp] * m) / den;
-                dm = (g.c * cu[comp] - hs * (e0 + e1)) / den;
+        le[comp] = ldv<VEC>(lE + comp * N);
+        lc[comp] = vmul<VEC>(le[comp], ldv<VEC>(ie + comp * mN));
+    }
+    Vec<VEC> Hy_m, Hz_m;
+    if (gr) {
+        Hy_m = ldv<VEC>(H + N - sx);
+        Hz_m = ldv<VEC>(H + 2 * N - sx);
+    }
+    for (int i = i0; i < i1; ++i, lE += sx, lH += sx, ie += sx, H += sx, lEo += sx, lHo += sx) {
+        Vec<VEC> len[3], lcn[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            len[comp] = ldv<VEC>(lE + sx + comp * N);
+            lcn[comp] = vmul<VEC>(len[comp], ldv<VEC>(ie + sx + comp * mN));
+        }
+        const Vec<VEC> x_jp = vmul<VEC>(ldv<VEC>(lE + sy), ldv<VEC>(ie + sy));
+        const Vec<VEC> z_jp = vmul<VEC>(ldv<VEC>(lE + 2 * N + sy), ldv<VEC>(ie + 2 * mN + sy));
+        const float x_kp = __ldg(lE + VEC) * __ldg(ie + VEC);
+        const float y_kp = __ldg(lE + N + VEC) * __ldg(ie + mN + VEC);
+        const Vec<VEC> h0 = ldv<VEC>(lH), h1 = ldv<VEC>(lH + N), h2 = ldv<VEC>(lH + 2 * N);
+        Vec<VEC> Hx, Hy, Hz, Hz_jm, Hx_jm;
+        float Hy_k = 0.f, Hx_k = 0.f;
+        Vec<VEC> gv[3];
+        if (gr) {
+            Hx = ldv<VEC>(H); Hy = ldv<VEC>(H + N); Hz = ldv<VEC>(H + 2 * N);
+            Hz_jm = ldv<VEC>(H + 2 * N - sy);
+            Hx_jm = ldv<VEC>(H - sy);
+            Hy_k = __ldg(H + N - 1);
+            Hx_k = __ldg(H - 1);
+            if (iso) gv[0] = ldv_rw<VEC>(gr);
+            else {
+#pragma unroll
+                for (int comp = 0; comp < 3; ++comp) gv[comp] = ldv_rw<VEC>(gr + comp * N);
             }
         }
-        a.lE_out[comp * N + c] = le;
-        if (a.grad_ie) {
-            if (a.n_eps == 3) a.grad_ie[comp * N + c] += l1 * dm;
-            else gsum += l1 * dm;
+        Vec<VEC> o0, o1, o2;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const float b0 = e + 1 < VEC ? lc[0].v[(e + 1) % VEC] : x_kp;
+            const float b1 = e + 1 < VEC ? lc[1].v[(e + 1) % VEC] : y_kp;
+            // curl_E(c ie lam): lc holds ie lam, the factor c is applied to the differences
+            o0.v[e] = h0.v[e] + cc * ((z_jp.v[e] - lc[2].v[e]) - (b1 - lc[1].v[e]));
+            o1.v[e] = h1.v[e] + cc * ((b0 - lc[0].v[e]) - (lcn[2].v[e] - lc[2].v[e]));
+            o2.v[e] = h2.v[e] + cc * ((lcn[1].v[e] - lc[1].v[e]) - (x_jp.v[e] - lc[0].v[e]));
+            if (gr) {
+                const float hy_km = e == 0 ? Hy_k : Hy.v[e - 1];
+                const float hx_km = e == 0 ? Hx_k : Hx.v[e - 1];
+                const float cu0 = (Hz.v[e] - Hz_jm.v[e]) - (Hy.v[e] - hy_km);
+                const float cu1 = (Hx.v[e] - hx_km) - (Hz.v[e] - Hz_m.v[e]);
+                const float cu2 = (Hy.v[e] - Hy_m.v[e]) - (Hx.v[e] - Hx_jm.v[e]);
+                if (iso) {
+                    gv[0].v[e] += cc * (le[0].v[e] * cu0 + le[1].v[e] * cu1 + le[2].v[e] * cu2);
+                } else {
+                    gv[0].v[e] += cc * le[0].v[e] * cu0;
+                    gv[1].v[e] += cc * le[1].v[e] * cu1;
+                    gv[2].v[e] += cc * le[2].v[e] * cu2;
+                }
+            }
+        }
+        if (a.hp.buf) {  // detector part of lam H(t)
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                long long q;
+                if (!box_local(a.hp, i, j, k0 + e, q)) continue;
+                float* hp = a.hp.buf + q;
+                o0.v[e] += hp[0]; hp[0] = 0.f;
+                o1.v[e] += hp[a.hp.M]; hp[a.hp.M] = 0.f;
+                o2.v[e] += hp[2 * a.hp.M]; hp[2 * a.hp.M] = 0.f;
+            }
+        }
+        stv<VEC>(lHo, o0);
+        stv<VEC>(lHo + N, o1);
+        stv<VEC>(lHo + 2 * N, o2);
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) stv<VEC>(lEo + comp * N, le[comp]);
+        if (gr) {
+            if (iso) stv<VEC>(gr, gv[0]);
+            else {
+#pragma unroll
+                for (int comp = 0; comp < 3; ++comp) stv<VEC>(gr + comp * N, gv[comp]);
+            }
+            gr += sx;
+            Hy_m = Hy;
+            Hz_m = Hz;
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            le[comp] = len[comp];
+            lc[comp] = lcn[comp];
         }
     }
-    if (a.grad_ie && a.n_eps != 3) a.grad_ie[c] += gsum;
 }
 
 // ---------------------------------------------------------------------------------

@@ -139,6 +139,73 @@ int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
     return FDTD_OK;
 }
 
+enum class AdjKind { Shell, Core, CoreFast };
+
+template <bool HSIDE, int VEC>
+void launch_adj_kernel(const AdjArgs& a, long long blocks, AdjKind kind, cudaStream_t st) {
+    const unsigned nb = (unsigned)blocks;
+    if (kind == AdjKind::Shell) {
+        if (HSIDE) k_adj_H<VEC, true><<<nb, kUpdBlock, 0, st>>>(a);
+        else k_adj_E<VEC, true><<<nb, kUpdBlock, 0, st>>>(a);
+    } else if (kind == AdjKind::Core) {
+        if (HSIDE) k_adj_H_core<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+        else k_adj_E_core<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+    } else {
+        if (HSIDE) k_adj_H_core_s<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+        else k_adj_E_core_s<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+    }
+}
+
+// Slabs that can reach a box or its one-cell rim (every slab when an axis wraps).
+int box_slab_mask(const FdtdPlan* p, const Box& b) {
+    if (p->g.px || p->g.py || p->g.pz) return 63;
+    int m = 0;
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        const DSlab& sl = p->slab[s];
+        if (sl.lo < b.hi[sl.axis] + 1 && sl.lo + sl.L > b.lo[sl.axis] - 1) m |= 1 << s;
+    }
+    return m;
+}
+
+template <bool HSIDE>
+void launch_adj_boxes(const FdtdPlan* p, AdjArgs a, const Box* boxes, const int* chunks, int n, AdjKind kind,
+                      cudaStream_t st) {
+    const long long blocks = fill_boxes(p, a, boxes, chunks, n);
+    if (blocks <= 0) return;
+    for (int q = 0; q < n; ++q) a.bslab[q] = box_slab_mask(p, boxes[q]);
+    if (p->vec == 4) launch_adj_kernel<HSIDE, 4>(a, blocks, kind, st);
+    else if (p->vec == 2) launch_adj_kernel<HSIDE, 2>(a, blocks, kind, st);
+    else launch_adj_kernel<HSIDE, 1>(a, blocks, kind, st);
+}
+
+// Whether the fast core kernel applies: the box keeps one cell off every face (no halo),
+// no conductivity, no PEC/PMC faces and, for the transposed H-step, a scalar inv_mu.
+bool adj_fast_core(const FdtdPlan* p, const AdjArgs& a, const Box& core, bool hside) {
+    const int n[3] = {p->g.nx, p->g.ny, p->g.nz};
+    for (int x = 0; x < 3; ++x)
+        if (core.lo[x] < 1 || core.hi[x] > n[x] - 1) return false;
+    if (p->g.pec || p->g.pmc || a.sigE || a.sigH) return false;
+    return hside ? a.im == nullptr : true;
+}
+
+// One transposed half-step: a slab-free core (the forward core shrunk by one cell next to
+// every slab, since the transpose reads slab terms at the neighbours) and one launch over
+// the shell boxes.
+template <bool HSIDE>
+void launch_adj(const FdtdPlan* p, const AdjArgs& a, cudaStream_t st) {
+    const Split sp = split_boxes(p, 1);
+    if (!sp.split) {
+        const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
+        launch_adj_boxes<HSIDE>(p, a, &all, &p->chunk, 1, AdjKind::Shell, st);
+        return;
+    }
+    const AdjKind ck = adj_fast_core(p, a, sp.core, HSIDE) ? AdjKind::CoreFast : AdjKind::Core;
+    launch_adj_boxes<HSIDE>(p, a, &sp.core, &p->chunk, 1, ck, st);
+    int chunks[6];
+    for (int q = 0; q < sp.n_shell; ++q) chunks[q] = kShellChunk;
+    launch_adj_boxes<HSIDE>(p, a, sp.shell, chunks, sp.n_shell, AdjKind::Shell, st);
+}
+
 // One step of the backward loop at t = *d_t: snapshot, reconstruction, transposed step.
 void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, const LamSet& cur,
                          const LamSet& nxt, cudaStream_t st) {
@@ -163,9 +230,8 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
         k_adj_det<<<dd.nblocks, kDetBlock, 0, st>>>(a, x, p->d_t);
         if (dd.reduce && dd.kind != FDTD_DET_PHASOR) k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
     }
-    const unsigned blocks = (unsigned)((p->g.N + 255) / 256);
-    k_adj_H<<<blocks, 256, 0, st>>>(a);
-    k_adj_E<<<blocks, 256, 0, st>>>(a);
+    launch_adj<true>(p, a, st);
+    launch_adj<false>(p, a, st);
     k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
 }
 

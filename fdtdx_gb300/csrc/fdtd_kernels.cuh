@@ -181,8 +181,8 @@ __device__ __forceinline__ float material_update(const UpdArgs& a, float u0, flo
 // of one (j) row and marches over the block's `chunk` x planes.
 // The block's box, its column (j, k0) and its x range [i0, i1).  Boxes have VEC-aligned z
 // bounds; the box table is indexed with unrolled static indices (no dynamic param access).
-template <int VEC>
-__device__ __forceinline__ bool column_of(const UpdArgs& a, int& j, int& k0, int& i0, int& i1) {
+template <int VEC, typename Args>
+__device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i0, int& i1) {
     const int b = blockIdx.x;
     int lo0 = 0, lo1 = 0, lo2 = 0, hi0 = 0, hi1 = 0, hi2 = 0, chunk = 1, nbx = 1, start = 0;
 #pragma unroll

@@ -244,7 +244,9 @@ struct Split {
     Box shell[6];
 };
 
-Split split_boxes(const FdtdPlan* p) {
+// `margin` widens every slab by that many cells on its inner side (the adjoint's core must
+// not read slab cells even as neighbours).
+Split split_boxes(const FdtdPlan* p, int margin = 0) {
     Split sp;
     const Geo& g = p->g;
     const int n[3] = {g.nx, g.ny, g.nz};
@@ -252,7 +254,7 @@ Split split_boxes(const FdtdPlan* p) {
     for (int s = 0; s < p->d.n_slabs; ++s) {
         const int ax = p->slab[s].axis, side = p->d.slabs[s].direction > 0 ? 1 : 0;
         if (L[ax][side]) return sp;  // two slabs on one face: no split
-        L[ax][side] = p->slab[s].L;
+        L[ax][side] = p->slab[s].L + margin;
     }
     const int A = g.nz % 4 == 0 ? 4 : p->vec;
     const int zlo = (L[2][0] + A - 1) / A * A, zhi = (n[2] - L[2][1]) / A * A;
@@ -592,7 +594,8 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
 constexpr int kShellChunk = 4;
 
 // Fills the launch's box table; returns the number of blocks of the 1-D grid.
-long long fill_boxes(const FdtdPlan* p, UpdArgs& a, const Box* boxes, const int* chunks, int n) {
+template <typename Args>
+long long fill_boxes(const FdtdPlan* p, Args& a, const Box* boxes, const int* chunks, int n) {
     a.nbox = n;
     long long start = 0;
     for (int q = 0; q < n; ++q) {
