@@ -17,6 +17,8 @@ from fdtdx_gb300.core import (
     TukeyWindow,
     WaveCharacter,
 )
+from fdtdx_gb300.adjoint import reversible_fdtd
+from fdtdx_gb300.batch import SimulationBatch, run_fdtd_batch
 from fdtdx_gb300.fdtd import checkpointed_fdtd, run_fdtd
 from fdtdx_gb300.initialization import apply_params, place_objects
 from fdtdx_gb300.objects import (
@@ -40,12 +42,6 @@ from fdtdx_gb300.objects import (
     UniformPlaneSource,
     boundary_objects_from_config,
 )
-
-
-def reversible_fdtd(*args, **kwargs):
-    from fdtdx_gb300.adjoint import reversible_fdtd as _rf
-
-    return _rf(*args, **kwargs)
 
 
 __all__ = [
@@ -89,5 +85,7 @@ __all__ = [
     "place_objects",
     "reversible_fdtd",
     "run_fdtd",
+    "run_fdtd_batch",
+    "SimulationBatch",
     "wavelength_to_period",
 ]

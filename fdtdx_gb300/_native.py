@@ -156,6 +156,13 @@ SIGNATURES = {
     "fdtd_plan_tune_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "fdtd_plan_uses_tma": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_status": (C.c_int, [C.c_void_p]),
+    "fdtd_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(Buffers), C.c_int32, C.POINTER(C.c_void_p)]),
+    "fdtd_batch_destroy": (None, [C.c_void_p]),
+    "fdtd_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "fdtd_batch_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.c_void_p]),
+    "fdtd_batch_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "fdtd_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "fdtd_batch_launches_per_step": (C.c_int32, [C.c_void_p]),
     "fdtd_detector_sample_noalloc": (
         C.c_int,
         [C.POINTER(DetectorDesc), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_void_p, C.c_void_p,

@@ -1,0 +1,509 @@
+// Host side of the batched forward path (fdtd_batch_*; included by fdtd_plan.cu, which owns
+// the plan type and the launch helpers).
+//
+// A batch holds already-built plans and their buffers.  One batch step runs, for every
+// simulation at once: the E half-step (core and CPML shell of every simulation in one
+// persistent launch), the E-side sources, the H half-step with the fused detectors, the
+// H-side sources, the remaining detectors (+ their reductions) and the step counters:
+// five to six launches per step for the whole batch instead of about eight per
+// simulation.  The step loop is captured in a CUDA graph.  Tile shapes (x planes per core
+// unit, per shell unit, resident blocks per SM) are chosen by an online autotuner that
+// times candidates on real steps of the batch (they change the work partition only, not
+// the arithmetic), so tuning costs no extra simulation work.
+#pragma once
+#include "fdtd_batch_kernels.cuh"
+
+struct FdtdBatch {
+    int n = 0;
+    std::vector<FdtdPlan*> plans;
+    std::vector<FdtdBuffers> bufs;
+    std::vector<int> t;                  // current step of each simulation (host mirror)
+    bool any_hprev = false;
+    int sm_count = 1;
+    // tuning
+    int chunk_scale_num = 1, chunk_scale_den = 1;  // core x-chunk = default chunk * num / den
+    int shell_chunk = kShellChunk;
+    int blocks_per_sm = 8;
+    bool tuned = false;
+    // device tables
+    char* dmem = nullptr;
+    UpdArgs* argsE = nullptr;  // [2 parities][n_args]
+    UpdArgs* argsH = nullptr;
+    BUnit* units = nullptr;
+    int class_start[5] = {0, 0, 0, 0, 0};  // unit ranges of the (vec, pml) classes: (1,0) (1,1) (2,0) (2,1)
+    BSrc* srcE = nullptr;
+    BSrc* srcH = nullptr;
+    int2* src_unitsE = nullptr;
+    int2* src_unitsH = nullptr;
+    BDet* dets = nullptr;
+    int2* det_units = nullptr;
+    int* det_red = nullptr;
+    int** tps = nullptr;
+    int n_args = 0, n_units = 0, n_srcE = 0, n_srcH = 0, n_src_unitsE = 0, n_src_unitsH = 0;
+    int n_dets = 0, n_det_units = 0, n_det_red = 0;
+    int max_args = 0, max_units = 0;
+    // graph of a fixed number of steps
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    int gsteps = 0;
+    cudaStream_t cap_stream = nullptr;
+    std::string err;
+};
+
+namespace {
+
+int bfail(FdtdBatch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+void batch_drop_graph(FdtdBatch* b) {
+    if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    b->gsteps = 0;
+}
+
+int scaled_chunk(const FdtdBatch* b, const FdtdPlan* p) {
+    return std::max(1, p->chunk * b->chunk_scale_num / b->chunk_scale_den);
+}
+
+// The update parts of one simulation: (box list, chunk per box, pml) for the core and the
+// shell, or one CPML part over the whole grid.
+struct BPart {
+    Box boxes[6];
+    int chunks[6];
+    int n;
+    bool pml;
+};
+
+int sim_parts(const FdtdBatch* b, const FdtdPlan* p, BPart parts[2]) {
+    const Split sp = split_boxes(p);
+    if (!sp.split) {
+        parts[0].boxes[0] = Box{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
+        parts[0].chunks[0] = scaled_chunk(b, p);
+        parts[0].n = 1;
+        parts[0].pml = true;
+        return 1;
+    }
+    parts[0].boxes[0] = sp.core;
+    parts[0].chunks[0] = scaled_chunk(b, p);
+    parts[0].n = 1;
+    parts[0].pml = false;
+    if (sp.n_shell == 0) return 1;
+    for (int q = 0; q < sp.n_shell; ++q) {
+        parts[1].boxes[q] = sp.shell[q];
+        parts[1].chunks[q] = b->shell_chunk;
+    }
+    parts[1].n = sp.n_shell;
+    parts[1].pml = true;
+    return 2;
+}
+
+// Rebuilds the update tables and the unit list for the current tile choice and uploads them.
+int batch_build_updates(FdtdBatch* b) {
+    // the tables may be read by steps still in flight on any stream
+    cudaError_t se = cudaDeviceSynchronize();
+    if (se != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("batch rebuild: ") + cudaGetErrorString(se));
+    std::vector<BUnit> units, cunits[4];
+    std::vector<UpdArgs> e0, e1, h0, h1;
+    for (int s = 0; s < b->n; ++s) {
+        FdtdPlan* p = b->plans[s];
+        const FdtdBuffers* bb = &b->bufs[s];
+        float* hc[2] = {bb->H, p->need_hprev ? p->h_twin : bb->H};
+        float* hn[2] = {p->need_hprev ? p->h_twin : bb->H, bb->H};
+        BPart parts[2];
+        const int np = sim_parts(b, p, parts);
+        for (int q = 0; q < np; ++q) {
+            UpdArgs ae[2], ah[2];
+            long long blocks = 0;
+            for (int par = 0; par < 2; ++par) {
+                ae[par] = make_upd(p, bb, true, hc[par], bb->E, bb->E);
+                ah[par] = make_upd_fwd_H(p, bb, hc[par], hn[par]);
+                ae[par].chunk = ah[par].chunk = parts[q].chunks[0];
+                blocks = fill_boxes(p, ae[par], parts[q].boxes, parts[q].chunks, parts[q].n);
+                fill_boxes(p, ah[par], parts[q].boxes, parts[q].chunks, parts[q].n);
+            }
+            const int arg = (int)e0.size();
+            e0.push_back(ae[0]); e1.push_back(ae[1]);
+            h0.push_back(ah[0]); h1.push_back(ah[1]);
+            const int cls = (p->vec == 2 ? 2 : 0) + (parts[q].pml ? 1 : 0);
+            for (long long k = 0; k < blocks; ++k) cunits[cls].push_back(BUnit{arg, (int)k});
+        }
+    }
+    for (int cls = 0; cls < 4; ++cls) {
+        b->class_start[cls] = (int)units.size();
+        units.insert(units.end(), cunits[cls].begin(), cunits[cls].end());
+    }
+    b->class_start[4] = (int)units.size();
+    b->n_args = (int)e0.size();
+    b->n_units = (int)units.size();
+    if (b->n_args > b->max_args || b->n_units > b->max_units) return bfail(b, FDTD_EINVAL, "batch tables overflow");
+    // parity tables are laid out [parity * max_args + arg]
+    cudaError_t e = cudaMemcpy(b->argsE, e0.data(), sizeof(UpdArgs) * b->n_args, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->argsE + b->max_args, e1.data(), sizeof(UpdArgs) * b->n_args, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->argsH, h0.data(), sizeof(UpdArgs) * b->n_args, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->argsH + b->max_args, h1.data(), sizeof(UpdArgs) * b->n_args, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->units, units.data(), sizeof(BUnit) * b->n_units, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("batch table upload: ") + cudaGetErrorString(e));
+    batch_drop_graph(b);
+    return FDTD_OK;
+}
+
+long long sim_update_blocks_upper(const FdtdPlan* p) {
+    // blocks of the finest tiling the tuner may choose (chunk 1): an upper bound for the tables
+    const Split sp = split_boxes(p);
+    auto blocks = [&](const Box& bx) {
+        const long long cols = (long long)(bx.hi[1] - bx.lo[1]) * ((bx.hi[2] - bx.lo[2]) / p->vec);
+        return ((cols + kUpdThreads - 1) / kUpdThreads) * (bx.hi[0] - bx.lo[0]);
+    };
+    if (!sp.split) return blocks(Box{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}});
+    long long n = blocks(sp.core);
+    for (int q = 0; q < sp.n_shell; ++q) n += blocks(sp.shell[q]);
+    return n;
+}
+
+template <bool HSIDE>
+void batch_updates(const FdtdBatch* b, int parity, cudaStream_t st) {
+    const UpdArgs* args = (HSIDE ? b->argsH : b->argsE) + parity * b->max_args;
+    for (int cls = 0; cls < 4; ++cls) {
+        const int n = b->class_start[cls + 1] - b->class_start[cls];
+        if (!n) continue;
+        const BUnit* u = b->units + b->class_start[cls];
+        const int grid = std::max(1, std::min(n, b->blocks_per_sm * b->sm_count));
+        switch (cls) {
+            case 0: k_batch_update<HSIDE, 1, false><<<grid, kUpdBlock, 0, st>>>(u, n, args); break;
+            case 1: k_batch_update<HSIDE, 1, true><<<grid, kUpdBlock, 0, st>>>(u, n, args); break;
+            case 2: k_batch_update<HSIDE, 2, false><<<grid, kUpdBlock, 0, st>>>(u, n, args); break;
+            default: k_batch_update<HSIDE, 2, true><<<grid, kUpdBlock, 0, st>>>(u, n, args); break;
+        }
+    }
+}
+
+void batch_step(const FdtdBatch* b, int parity, cudaStream_t st) {
+    batch_updates<false>(b, parity, st);
+    if (b->n_src_unitsE)
+        k_batch_source<true><<<std::min(b->n_src_unitsE, 4 * b->sm_count), 256, 0, st>>>(b->src_unitsE, b->n_src_unitsE,
+                                                                                       b->srcE, parity);
+    batch_updates<true>(b, parity, st);
+    if (b->n_src_unitsH)
+        k_batch_source<false><<<std::min(b->n_src_unitsH, 4 * b->sm_count), 256, 0, st>>>(b->src_unitsH, b->n_src_unitsH,
+                                                                                        b->srcH, parity);
+    if (b->n_det_units)
+        k_batch_detector<<<std::min(b->n_det_units, 8 * b->sm_count), kDetBlock, 0, st>>>(b->det_units, b->n_det_units,
+                                                                                          b->dets, parity);
+    if (b->n_det_red)
+        k_batch_detector_finalize<<<std::min(b->n_det_red, b->sm_count), kDetBlock, 0, st>>>(b->det_red, b->n_det_red,
+                                                                                            b->dets);
+    k_batch_advance<<<(b->n + 127) / 128, 128, 0, st>>>(b->tps, b->n);
+}
+
+// Runs `steps` steps from `parity` with direct launches; returns the parity after them.
+int batch_run_direct(const FdtdBatch* b, int parity, int steps, cudaStream_t st) {
+    for (int s = 0; s < steps; ++s) {
+        batch_step(b, parity, st);
+        if (b->any_hprev) parity ^= 1;
+    }
+    return parity;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n, FdtdBatch** out) {
+    if (!plans || !bufs || !out || n <= 0) return FDTD_EINVAL;
+    *out = nullptr;
+    FdtdBatch* b = new FdtdBatch();
+    b->n = n;
+    for (int s = 0; s < n; ++s) {
+        FdtdPlan* p = plans[s];
+        if (!p) { delete b; fprintf(stderr, "fdtd_batch_create: plan %d is NULL\n", s); return FDTD_EINVAL; }
+        if (int rc = check_bufs(p, &bufs[s])) {
+            fprintf(stderr, "fdtd_batch_create: simulation %d: %s\n", s, p->err.c_str());
+            delete b;
+            return rc;
+        }
+        if (p->d.record_interfaces) {
+            fprintf(stderr, "fdtd_batch_create: simulation %d records interfaces (the batch runs forward-only plans)\n", s);
+            delete b;
+            return FDTD_EINVAL;
+        }
+        if (p->vec > 2) p->vec = 2;  // the batched kernels carry VEC 1 and 2
+        b->plans.push_back(p);
+        b->bufs.push_back(bufs[s]);
+        b->t.push_back(0);
+        b->any_hprev = b->any_hprev || p->need_hprev;
+    }
+    b->sm_count = plans[0]->sm_count;
+    // table sizes: upper bounds over every tile choice
+    long long units = 0;
+    int args = 0, srcE = 0, srcH = 0, su_E = 0, su_H = 0, dets = 0, du = 0, dred = 0;
+    for (int s = 0; s < n; ++s) {
+        const FdtdPlan* p = plans[s];
+        units += sim_update_blocks_upper(p);
+        args += 2;
+        for (int q = 0; q < p->d.n_sources; ++q) {
+            const DSource& so = p->src[q];
+            const long long P = so.kind == FDTD_SRC_PLANE ? face_cells(p->d.sources[q]) : 1;
+            const int blocks = (int)((P + 255) / 256);
+            const bool onE = !(so.kind == FDTD_SRC_DIPOLE && so.magnetic);
+            const bool onH = !(so.kind == FDTD_SRC_DIPOLE && !so.magnetic);
+            if (onE) { ++srcE; su_E += blocks; }
+            if (onH) { ++srcH; su_H += blocks; }
+        }
+        for (int q = 0; q < p->d.n_detectors; ++q) {
+            if (p->fused[q]) continue;
+            ++dets;
+            du += p->det[q].nblocks;
+            if (p->det[q].reduce) ++dred;
+        }
+    }
+    if (units > (1ll << 30)) { delete b; return FDTD_EINVAL; }
+    b->max_args = args;
+    b->max_units = (int)units;
+    Arena ar;
+    const size_t oE = ar.take(sizeof(UpdArgs) * 2 * args), oH = ar.take(sizeof(UpdArgs) * 2 * args);
+    const size_t oU = ar.take(sizeof(BUnit) * units);
+    const size_t oSE = ar.take(sizeof(BSrc) * std::max(1, srcE)), oSH = ar.take(sizeof(BSrc) * std::max(1, srcH));
+    const size_t oSUE = ar.take(sizeof(int2) * std::max(1, su_E)), oSUH = ar.take(sizeof(int2) * std::max(1, su_H));
+    const size_t oD = ar.take(sizeof(BDet) * std::max(1, dets)), oDU = ar.take(sizeof(int2) * std::max(1, du));
+    const size_t oDR = ar.take(sizeof(int) * std::max(1, dred)), oT = ar.take(sizeof(int*) * n);
+    cudaError_t e = cudaMalloc(&b->dmem, ar.off);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "fdtd_batch_create: cudaMalloc(%zu): %s\n", ar.off, cudaGetErrorString(e));
+        delete b;
+        return FDTD_ENOMEM;
+    }
+    b->argsE = reinterpret_cast<UpdArgs*>(b->dmem + oE);
+    b->argsH = reinterpret_cast<UpdArgs*>(b->dmem + oH);
+    b->units = reinterpret_cast<BUnit*>(b->dmem + oU);
+    b->srcE = reinterpret_cast<BSrc*>(b->dmem + oSE);
+    b->srcH = reinterpret_cast<BSrc*>(b->dmem + oSH);
+    b->src_unitsE = reinterpret_cast<int2*>(b->dmem + oSUE);
+    b->src_unitsH = reinterpret_cast<int2*>(b->dmem + oSUH);
+    b->dets = reinterpret_cast<BDet*>(b->dmem + oD);
+    b->det_units = reinterpret_cast<int2*>(b->dmem + oDU);
+    b->det_red = reinterpret_cast<int*>(b->dmem + oDR);
+    b->tps = reinterpret_cast<int**>(b->dmem + oT);
+    // sources, detectors, step counters (independent of the tile choice)
+    std::vector<BSrc> hsE, hsH;
+    std::vector<int2> huE, huH, hdu;
+    std::vector<BDet> hd;
+    std::vector<int> hdr;
+    std::vector<int*> htp;
+    for (int s = 0; s < n; ++s) {
+        FdtdPlan* p = plans[s];
+        const FdtdBuffers& bb = bufs[s];
+        float* hc[2] = {bb.H, p->need_hprev ? p->h_twin : bb.H};
+        float* hn[2] = {p->need_hprev ? p->h_twin : bb.H, bb.H};
+        htp.push_back(p->d_t);
+        for (int q = 0; q < p->d.n_sources; ++q) {
+            const DSource& so = p->src[q];
+            const long long P = so.kind == FDTD_SRC_PLANE ? face_cells(p->d.sources[q]) : 1;
+            const int blocks = (int)((P + 255) / 256);
+            if (!(so.kind == FDTD_SRC_DIPOLE && so.magnetic)) {
+                BSrc x{};
+                x.g = p->g; x.s = so; x.tp = p->d_t; x.F[0] = x.F[1] = bb.E;
+                x.mat = bb.inv_eps; x.n_mat = p->d.n_eps; x.mat_scalar = 1.f;
+                for (int k = 0; k < blocks; ++k) huE.push_back(make_int2((int)hsE.size(), k));
+                hsE.push_back(x);
+            }
+            if (!(so.kind == FDTD_SRC_DIPOLE && !so.magnetic)) {
+                BSrc x{};
+                x.g = p->g; x.s = so; x.tp = p->d_t; x.F[0] = hn[0]; x.F[1] = hn[1];
+                x.mat = p->d.n_mu ? bb.inv_mu : nullptr; x.n_mat = p->d.n_mu ? p->d.n_mu : 1;
+                x.mat_scalar = p->d.inv_mu_scalar;
+                for (int k = 0; k < blocks; ++k) huH.push_back(make_int2((int)hsH.size(), k));
+                hsH.push_back(x);
+            }
+        }
+        for (int q = 0; q < p->d.n_detectors; ++q) {
+            if (p->fused[q]) continue;
+            BDet x{};
+            x.g = p->g; x.d = p->det[q]; x.tp = p->d_t; x.state = bb.det_state[q];
+            for (int par = 0; par < 2; ++par)
+                x.f[par] = DetFields{bb.E, hc[par], hn[par], bb.inv_eps, p->d.n_eps, p->d.n_mu ? bb.inv_mu : nullptr,
+                                     p->d.n_mu ? p->d.n_mu : 1, p->d.inv_mu_scalar};
+            for (int k = 0; k < p->det[q].nblocks; ++k) hdu.push_back(make_int2((int)hd.size(), k));
+            if (p->det[q].reduce) hdr.push_back((int)hd.size());
+            hd.push_back(x);
+        }
+    }
+    b->n_srcE = (int)hsE.size(); b->n_srcH = (int)hsH.size();
+    b->n_src_unitsE = (int)huE.size(); b->n_src_unitsH = (int)huH.size();
+    b->n_dets = (int)hd.size(); b->n_det_units = (int)hdu.size(); b->n_det_red = (int)hdr.size();
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up(b->srcE, hsE.data(), sizeof(BSrc) * hsE.size());
+    up(b->srcH, hsH.data(), sizeof(BSrc) * hsH.size());
+    up(b->src_unitsE, huE.data(), sizeof(int2) * huE.size());
+    up(b->src_unitsH, huH.data(), sizeof(int2) * huH.size());
+    up(b->dets, hd.data(), sizeof(BDet) * hd.size());
+    up(b->det_units, hdu.data(), sizeof(int2) * hdu.size());
+    up(b->det_red, hdr.data(), sizeof(int) * hdr.size());
+    up(b->tps, htp.data(), sizeof(int*) * htp.size());
+    if (e != cudaSuccess) {
+        fprintf(stderr, "fdtd_batch_create: upload: %s\n", cudaGetErrorString(e));
+        cudaFree(b->dmem);
+        delete b;
+        return FDTD_ECUDA;
+    }
+    if (int rc = batch_build_updates(b)) {
+        fprintf(stderr, "fdtd_batch_create: %s\n", b->err.c_str());
+        cudaFree(b->dmem);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return FDTD_OK;
+}
+
+void fdtd_batch_destroy(FdtdBatch* b) {
+    if (!b) return;
+    batch_drop_graph(b);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    cudaFree(b->dmem);
+    delete b;
+}
+
+const char* fdtd_batch_last_error(const FdtdBatch* b) { return b ? b->err.c_str() : "no batch"; }
+
+int fdtd_batch_tune(FdtdBatch* b, int32_t chunk_num, int32_t chunk_den, int32_t shell_chunk, int32_t blocks_per_sm) {
+    if (!b || chunk_num <= 0 || chunk_den <= 0 || shell_chunk <= 0 || blocks_per_sm <= 0 || blocks_per_sm > 64)
+        return bfail(b, FDTD_EINVAL, "tile parameters must be positive (blocks_per_sm <= 64)");
+    b->chunk_scale_num = chunk_num;
+    b->chunk_scale_den = chunk_den;
+    b->shell_chunk = shell_chunk;
+    b->blocks_per_sm = blocks_per_sm;
+    return batch_build_updates(b);
+}
+
+int fdtd_batch_tuning(const FdtdBatch* b, int32_t* out4) {
+    if (!b || !out4) return FDTD_EINVAL;
+    out4[0] = b->chunk_scale_num;
+    out4[1] = b->chunk_scale_den;
+    out4[2] = b->shell_chunk;
+    out4[3] = b->blocks_per_sm;
+    return FDTD_OK;
+}
+
+int32_t fdtd_batch_launches_per_step(const FdtdBatch* b) {
+    if (!b) return 0;
+    int classes = 0;
+    for (int cls = 0; cls < 4; ++cls) classes += b->class_start[cls + 1] > b->class_start[cls];
+    return 2 * classes + 1 + (b->n_src_unitsE > 0) + (b->n_src_unitsH > 0) + (b->n_det_units > 0) + (b->n_det_red > 0);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Online autotuning: times candidate tile choices on real steps (coordinate search over
+// the core chunk scale, the shell chunk and the resident blocks per SM) and keeps the
+// fastest.  Returns the steps it ran and leaves the parity in *parity.
+int batch_autotune(FdtdBatch* b, int budget, int* parity, cudaStream_t st) {
+    const int per = b->any_hprev ? 4 : 3;  // timed steps per candidate (even with a parity twin)
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int used = 0;
+    auto trial = [&](int num, int den, int shell, int bps) -> float {
+        if (used + per + (b->any_hprev ? 2 : 1) > budget) return -1.f;
+        b->chunk_scale_num = num; b->chunk_scale_den = den; b->shell_chunk = shell; b->blocks_per_sm = bps;
+        if (batch_build_updates(b)) return -1.f;
+        const int warm = b->any_hprev ? 2 : 1;
+        *parity = batch_run_direct(b, *parity, warm, st);
+        cudaEventRecord(e0, st);
+        *parity = batch_run_direct(b, *parity, per, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        used += warm + per;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
+    int best[4] = {1, 1, kShellChunk, 8};
+    float best_ms = trial(best[0], best[1], best[2], best[3]);
+    const int scales[][2] = {{1, 2}, {2, 1}, {4, 1}};
+    for (const auto& sc : scales) {
+        const float ms = trial(sc[0], sc[1], best[2], best[3]);
+        if (ms > 0.f && (best_ms < 0.f || ms < best_ms)) { best_ms = ms; best[0] = sc[0]; best[1] = sc[1]; }
+    }
+    for (int sh : {2, 8}) {
+        const float ms = trial(best[0], best[1], sh, best[3]);
+        if (ms > 0.f && ms < best_ms) { best_ms = ms; best[2] = sh; }
+    }
+    for (int bps : {4, 16}) {
+        const float ms = trial(best[0], best[1], best[2], bps);
+        if (ms > 0.f && ms < best_ms) { best_ms = ms; best[3] = bps; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->chunk_scale_num = best[0]; b->chunk_scale_den = best[1]; b->shell_chunk = best[2]; b->blocks_per_sm = best[3];
+    batch_build_updates(b);
+    b->tuned = true;
+    return used;
+}
+
+}  // namespace
+
+extern "C" int fdtd_batch_forward(FdtdBatch* b, const int32_t* t0, int32_t n_steps, int32_t flags, void* stream) {
+    if (!b) return FDTD_EINVAL;
+    if (n_steps < 0) return bfail(b, FDTD_EINVAL, "n_steps must be >= 0");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    for (int s = 0; s < b->n; ++s) {
+        const int ts = t0 ? t0[s] : b->t[s];
+        if (ts < 0 || (long long)ts + n_steps > (long long)b->plans[s]->d.n_steps_total + 1)
+            return bfail(b, FDTD_EINVAL, "simulation " + std::to_string(s) + ": steps out of the range of its tables");
+    }
+    if (t0)
+        for (int s = 0; s < b->n; ++s) {
+            k_set_step<<<1, 1, 0, st>>>(b->plans[s]->d_t, t0[s]);
+            b->t[s] = t0[s];
+        }
+    if (n_steps == 0) return FDTD_OK;
+    int parity = 0, done = 0;
+    if ((flags & 2) && !b->tuned) done += batch_autotune(b, n_steps / 4, &parity, st);
+    const bool use_graph = (flags & 1) != 0;
+    const int unit = b->any_hprev ? 2 : 1;
+    if (use_graph && n_steps - done >= 8) {
+        if (parity) done += (parity = batch_run_direct(b, parity, 1, st), 1);
+        int G = std::min(n_steps - done, 64);
+        G -= G % unit;
+        if (!b->gexec || b->gsteps != G) {
+            batch_drop_graph(b);
+            if (!b->cap_stream) {
+                cudaError_t e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+                if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, cudaGetErrorString(e));
+            }
+            cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("begin capture: ") + cudaGetErrorString(e));
+            batch_run_direct(b, 0, G, b->cap_stream);
+            e = cudaStreamEndCapture(b->cap_stream, &b->graph);
+            if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("end capture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&b->gexec, b->graph, 0);
+            if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+            b->gsteps = G;
+        }
+        while (n_steps - done >= G) {
+            cudaError_t e = cudaGraphLaunch(b->gexec, st);
+            if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+            done += G;
+        }
+    }
+    parity = batch_run_direct(b, parity, n_steps - done, st);
+    if (parity) {  // H of the parity-twin simulations sits in the twin: bring it back
+        for (int s = 0; s < b->n; ++s) {
+            FdtdPlan* p = b->plans[s];
+            if (!p->need_hprev) continue;
+            cudaError_t e = cudaMemcpyAsync(b->bufs[s].H, p->h_twin, sizeof(float) * 3 * p->g.N,
+                                            cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, cudaGetErrorString(e));
+        }
+    }
+    for (int s = 0; s < b->n; ++s) b->t[s] += n_steps;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+    return FDTD_OK;
+}

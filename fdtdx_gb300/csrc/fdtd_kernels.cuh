@@ -182,8 +182,8 @@ __device__ __forceinline__ float material_update(const UpdArgs& a, float u0, flo
 // The block's box, its column (j, k0) and its x range [i0, i1).  Boxes have VEC-aligned z
 // bounds; the box table is indexed with unrolled static indices (no dynamic param access).
 template <int VEC, typename Args>
-__device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i0, int& i1) {
-    const int b = blockIdx.x;
+__device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i0, int& i1, int blk = -1) {
+    const int b = blk < 0 ? (int)blockIdx.x : blk;
     int lo0 = 0, lo1 = 0, lo2 = 0, hi0 = 0, hi1 = 0, hi2 = 0, chunk = 1, nbx = 1, start = 0;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
@@ -211,10 +211,10 @@ __device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i
 // reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
 // ---------------------------------------------------------------------------------
 template <bool REV, int VEC, bool PML>
-__global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
+__device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
-    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    if (!column_of<VEC>(a, j, k0, i0, i1, blk)) return;
     const long long N = g.N;
     const long long sy = g.nz;
     const float* __restrict__ H = a.F;
@@ -270,6 +270,11 @@ __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArg
         Hy_m = Hy;
         Hz_m = Hz;
     }
+}
+
+template <bool REV, int VEC, bool PML>
+__global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
+    update_E_body<REV, VEC, PML>(a, blockIdx.x);
 }
 
 // Accumulates the fused E-only detectors at cell (i, j, k) from the E values the H
@@ -337,10 +342,10 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
 // fused E-only detectors are accumulated in the same pass (forward only).
 // ---------------------------------------------------------------------------------
 template <bool REV, int VEC, bool PML>
-__global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
+__device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
-    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    if (!column_of<VEC>(a, j, k0, i0, i1, blk)) return;
     const long long N = g.N;
     const long long sy = g.nz, sx = (long long)g.ny * g.nz;
     const float* __restrict__ E = a.F;
@@ -439,6 +444,11 @@ __global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArg
     }
 }
 
+template <bool REV, int VEC, bool PML>
+__global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
+    update_H_body<REV, VEC, PML>(a, blockIdx.x);
+}
+
 // ---------------------------------------------------------------------------------
 // Source injection.  One thread per source cell.  `inverse` flips the sign (the
 // reverse step subtracts what the forward step added).  Positions a conductor
@@ -454,8 +464,8 @@ __device__ __forceinline__ float mat_at(const float* m, int n, float scalar, lon
 }
 
 template <bool ESIDE>
-__global__ void k_source(const Geo g, const DSource s, const int* __restrict__ tp, float* F, const float* mat, int n_mat,
-                         float mat_scalar, int inverse) {
+__device__ __forceinline__ void source_body(const Geo& g, const DSource& s, const int* __restrict__ tp, float* F,
+                                            const float* mat, int n_mat, float mat_scalar, int inverse, int blk) {
     const int t = *tp;
     const int ti = t + 1;
     if (!s.on[ti]) return;
@@ -463,7 +473,7 @@ __global__ void k_source(const Geo g, const DSource s, const int* __restrict__ t
     const float ph0 = ESIDE ? s.phE[ti] : s.phH[ti];
     const int wall = ESIDE ? g.pec : g.pmc;
     if (s.kind == FDTD_SRC_DIPOLE) {
-        if (blockIdx.x != 0 || threadIdx.x != 0) return;
+        if (blk != 0 || threadIdx.x != 0) return;
         if (ESIDE == (bool)s.magnetic) return;
         const int i = s.lo[0], j = s.lo[1], k = s.lo[2];
         if (face_zero(g, wall, s.comp, i, j, k)) return;
@@ -475,7 +485,7 @@ __global__ void k_source(const Geo g, const DSource s, const int* __restrict__ t
     const int n = s.normal, ax = (n + 1) % 3, bx = (n + 2) % 3;
     const int ext[3] = {s.hi[0] - s.lo[0], s.hi[1] - s.lo[1], s.hi[2] - s.lo[2]};
     const long long P = (long long)ext[0] * ext[1] * ext[2];
-    const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long f = (long long)blk * blockDim.x + threadIdx.x;
     if (f >= P) return;
     const int kk = (int)(f % ext[2]);
     const int jj = (int)((f / ext[2]) % ext[1]);
@@ -503,6 +513,12 @@ __global__ void k_source(const Geo g, const DSource s, const int* __restrict__ t
         if (!face_zero(g, wall, ax, i, j, k))
             F[ax * g.N + c] -= sg * (inc_b * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, ax, c));
     }
+}
+
+template <bool ESIDE>
+__global__ void k_source(const Geo g, const DSource s, const int* __restrict__ tp, float* F, const float* mat, int n_mat,
+                         float mat_scalar, int inverse) {
+    source_body<ESIDE>(g, s, tp, F, mat, n_mat, mat_scalar, inverse, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -576,13 +592,13 @@ __device__ __forceinline__ float block_sum(float x, float* sh) {
 
 constexpr int kDetBlock = 256;
 
-__global__ void __launch_bounds__(kDetBlock) k_detector(const Geo g, const DDet d, const int* __restrict__ tp,
-                                                        const DetFields f, void* state) {
+__device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const int* __restrict__ tp,
+                                              const DetFields& f, void* state, int blk) {
     __shared__ float sh[kDetBlock / 32];
     const int t = *tp;
     const int slot = __ldg(d.slot + t + 1);
     if (slot < 0) return;
-    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r = (long long)blk * blockDim.x + threadIdx.x;
     const bool valid = r < d.R;
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int i = 0, j = 0, k = 0;
@@ -652,8 +668,8 @@ __global__ void __launch_bounds__(kDetBlock) k_detector(const Geo g, const DDet 
                 const float re = block_sum<kDetBlock>(valid ? out[q] * w.x : 0.f, sh);
                 const float im = block_sum<kDetBlock>(valid ? out[q] * w.y : 0.f, sh);
                 if (threadIdx.x == 0) {
-                    d.partial[(long long)blockIdx.x * d.ncomp + 2 * (fq * nout + q)] = re;
-                    d.partial[(long long)blockIdx.x * d.ncomp + 2 * (fq * nout + q) + 1] = im;
+                    d.partial[(long long)blk * d.ncomp + 2 * (fq * nout + q)] = re;
+                    d.partial[(long long)blk * d.ncomp + 2 * (fq * nout + q) + 1] = im;
                 }
             }
         }
@@ -667,13 +683,18 @@ __global__ void __launch_bounds__(kDetBlock) k_detector(const Geo g, const DDet 
     }
     for (int q = 0; q < nout; ++q) {
         const float s = block_sum<kDetBlock>(valid ? out[q] : 0.f, sh);
-        if (threadIdx.x == 0) d.partial[(long long)blockIdx.x * d.ncomp + q] = s;
+        if (threadIdx.x == 0) d.partial[(long long)blk * d.ncomp + q] = s;
     }
+}
+
+__global__ void __launch_bounds__(kDetBlock) k_detector(const Geo g, const DDet d, const int* __restrict__ tp,
+                                                        const DetFields f, void* state) {
+    detector_body(g, d, tp, f, state, blockIdx.x);
 }
 
 // Sums the block partials of a reducing detector in a fixed order (deterministic)
 // and writes (field, flux, energy) or accumulates (phasor) the state entry.
-__global__ void __launch_bounds__(kDetBlock) k_detector_finalize(const DDet d, const int* __restrict__ tp, void* state) {
+__device__ __forceinline__ void detector_finalize_body(const DDet& d, const int* __restrict__ tp, void* state) {
     __shared__ float sh[kDetBlock / 32];
     const int t = *tp;
     const int slot = __ldg(d.slot + t + 1);
@@ -694,6 +715,10 @@ __global__ void __launch_bounds__(kDetBlock) k_detector_finalize(const DDet d, c
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(kDetBlock) k_detector_finalize(const DDet d, const int* __restrict__ tp, void* state) {
+    detector_finalize_body(d, tp, state);
 }
 
 // ---------------------------------------------------------------------------------

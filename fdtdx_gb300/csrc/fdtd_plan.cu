@@ -1024,3 +1024,4 @@ extern "C" int fdtd_plan_status(FdtdPlan* p) {
     return FDTD_OK;
 }
 #include "fdtd_noalloc.cuh"
+#include "fdtd_batch.cuh"

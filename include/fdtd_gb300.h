@@ -224,6 +224,33 @@ int32_t fdtd_launches_per_step(const FdtdPlan* plan);
  * [4] detectors, [5] interface recording.  Synchronises the stream. */
 int fdtd_profile_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_steps, float* out_ms, void* stream);
 
+/* ---- Batched forward path: many simulations stepped together --------------------------
+ *
+ * No counterpart in the reference (which runs one simulation per call, fdtdx/fdtd/fdtd.py:
+ * 421-496); it replaces looping that call over a set of simulations.  A batch holds built
+ * plans (forward-only: record_interfaces = 0) with their buffers.  One batch step runs
+ * every simulation's step with one persistent launch per kernel kind (E update, E
+ * sources, H update with fused detectors, H sources, detectors, reductions, step
+ * counters) over a flat list of work units; results equal the per-plan fdtd_forward
+ * (same device bodies).  The plans must stay alive and unused elsewhere while the
+ * batch exists. */
+typedef struct FdtdBatch FdtdBatch;
+int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n, FdtdBatch** out);
+void fdtd_batch_destroy(FdtdBatch* batch);
+const char* fdtd_batch_last_error(const FdtdBatch* batch);
+/* n_steps batch steps.  t0: per-simulation start step (NULL: continue where each
+ * stopped).  flags bit 0: CUDA graph of the step loop; bit 1: autotune the tile shapes
+ * on the first steps of this call (once per batch; at most n_steps / 4 steps, all of
+ * them real simulation steps). */
+int fdtd_batch_forward(FdtdBatch* batch, const int32_t* t0, int32_t n_steps, int32_t flags, void* stream);
+/* Tile shapes: core x-chunk = each plan's default chunk * num / den, shell x-chunk,
+ * resident blocks per SM of the persistent launches.  fdtd_batch_tuning reads them
+ * (out4 = {num, den, shell_chunk, blocks_per_sm}). */
+int fdtd_batch_tune(FdtdBatch* batch, int32_t chunk_num, int32_t chunk_den, int32_t shell_chunk, int32_t blocks_per_sm);
+int fdtd_batch_tuning(const FdtdBatch* batch, int32_t* out4);
+/* Launches of this library's kernels one batch step issues (for the whole batch). */
+int32_t fdtd_batch_launches_per_step(const FdtdBatch* batch);
+
 /* Allocation-free sample of one volume-reducing detector (no counterpart in the
  * reference: there the sample is part of the jitted step, fdtdx/fdtd/update.py:1040-1137).
  *
