@@ -28,7 +28,10 @@ class SimulationBatch:
     ``(time_step, arrays)`` pairs.
     """
 
-    def __init__(self, sims: Sequence[tuple[ArrayContainer, ObjectContainer, SimulationConfig]]):
+    def __init__(self, sims: Sequence[tuple[ArrayContainer, ObjectContainer, SimulationConfig]],
+                 scenes: Sequence[Scene] | None = None, reset: bool = True):
+        """``scenes`` (optional) are already-built scenes of the simulations (e.g. recording
+        ones for gradient jobs); ``reset=False`` steps the given arrays in place."""
         from fdtdx_gb300.fdtd import _materials_detached
 
         if not sims:
@@ -36,9 +39,10 @@ class SimulationBatch:
         self.scenes: list[Scene] = []
         self.arrays: list[ArrayContainer] = []
         self.configs: list[SimulationConfig] = []
-        for arrays, objects, config in sims:
-            work = _materials_detached(arrays).reset()
-            self.scenes.append(Scene(objects, work, config, record_interfaces=False))
+        self._own_scenes = scenes is None
+        for q, (arrays, objects, config) in enumerate(sims):
+            work = _materials_detached(arrays).reset() if reset else arrays
+            self.scenes.append(Scene(objects, work, config, record_interfaces=False) if scenes is None else scenes[q])
             self.arrays.append(work)
             self.configs.append(config)
         n = len(self.scenes)
@@ -98,8 +102,9 @@ class SimulationBatch:
         if getattr(self, "_h", None):
             N.load().fdtd_batch_destroy(self._h)
             self._h = None
-        for s in getattr(self, "scenes", []):
-            s.close()
+        if getattr(self, "_own_scenes", False):
+            for s in self.scenes:
+                s.close()
 
     def __del__(self):
         try:

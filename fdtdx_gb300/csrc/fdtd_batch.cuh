@@ -38,6 +38,9 @@ struct FdtdBatch {
     BDet* dets = nullptr;
     int2* det_units = nullptr;
     int* det_red = nullptr;
+    BIface* ifaces = nullptr;
+    int2* iface_units = nullptr;
+    int iface_start[4] = {0, 0, 0, 0};  // unit ranges per recording dtype (float, bf16, half)
     int** tps = nullptr;
     int n_args = 0, n_units = 0, n_srcE = 0, n_srcH = 0, n_src_unitsE = 0, n_src_unitsH = 0;
     int n_dets = 0, n_det_units = 0, n_det_red = 0;
@@ -188,6 +191,15 @@ void batch_step(const FdtdBatch* b, int parity, cudaStream_t st) {
     if (b->n_src_unitsH)
         k_batch_source<false><<<std::min(b->n_src_unitsH, 4 * b->sm_count), 256, 0, st>>>(b->src_unitsH, b->n_src_unitsH,
                                                                                         b->srcH, parity);
+    for (int dt = 0; dt < 3; ++dt) {
+        const int nu = b->iface_start[dt + 1] - b->iface_start[dt];
+        if (!nu) continue;
+        const int2* u = b->iface_units + b->iface_start[dt];
+        const int grid = std::min(nu, 4 * b->sm_count);
+        if (dt == 0) k_batch_interfaces<float><<<grid, 256, 0, st>>>(u, nu, b->ifaces, parity);
+        else if (dt == 1) k_batch_interfaces<__nv_bfloat16><<<grid, 256, 0, st>>>(u, nu, b->ifaces, parity);
+        else k_batch_interfaces<__half><<<grid, 256, 0, st>>>(u, nu, b->ifaces, parity);
+    }
     if (b->n_det_units)
         k_batch_detector<<<std::min(b->n_det_units, 8 * b->sm_count), kDetBlock, 0, st>>>(b->det_units, b->n_det_units,
                                                                                           b->dets, parity);
@@ -223,8 +235,8 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
             delete b;
             return rc;
         }
-        if (p->d.record_interfaces) {
-            fprintf(stderr, "fdtd_batch_create: simulation %d records interfaces (the batch runs forward-only plans)\n", s);
+        if (p->d.record_interfaces && p->d.n_slabs && !bufs[s].recording) {
+            fprintf(stderr, "fdtd_batch_create: simulation %d records interfaces but has no recording buffer\n", s);
             delete b;
             return FDTD_EINVAL;
         }
@@ -237,7 +249,7 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     b->sm_count = plans[0]->sm_count;
     // table sizes: upper bounds over every tile choice
     long long units = 0;
-    int args = 0, srcE = 0, srcH = 0, su_E = 0, su_H = 0, dets = 0, du = 0, dred = 0;
+    int args = 0, srcE = 0, srcH = 0, su_E = 0, su_H = 0, dets = 0, du = 0, dred = 0, nif = 0, ifu = 0;
     for (int s = 0; s < n; ++s) {
         const FdtdPlan* p = plans[s];
         units += sim_update_blocks_upper(p);
@@ -250,6 +262,10 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
             const bool onH = !(so.kind == FDTD_SRC_DIPOLE && !so.magnetic);
             if (onE) { ++srcE; su_E += blocks; }
             if (onH) { ++srcH; su_H += blocks; }
+        }
+        if (p->d.record_interfaces && p->d.n_slabs) {
+            ++nif;
+            ifu += (int)((p->ifc.total + 255) / 256);
         }
         for (int q = 0; q < p->d.n_detectors; ++q) {
             if (p->fused[q]) continue;
@@ -268,6 +284,7 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     const size_t oSUE = ar.take(sizeof(int2) * std::max(1, su_E)), oSUH = ar.take(sizeof(int2) * std::max(1, su_H));
     const size_t oD = ar.take(sizeof(BDet) * std::max(1, dets)), oDU = ar.take(sizeof(int2) * std::max(1, du));
     const size_t oDR = ar.take(sizeof(int) * std::max(1, dred)), oT = ar.take(sizeof(int*) * n);
+    const size_t oI = ar.take(sizeof(BIface) * std::max(1, nif)), oIU = ar.take(sizeof(int2) * std::max(1, ifu));
     cudaError_t e = cudaMalloc(&b->dmem, ar.off);
     if (e != cudaSuccess) {
         fprintf(stderr, "fdtd_batch_create: cudaMalloc(%zu): %s\n", ar.off, cudaGetErrorString(e));
@@ -285,18 +302,30 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     b->det_units = reinterpret_cast<int2*>(b->dmem + oDU);
     b->det_red = reinterpret_cast<int*>(b->dmem + oDR);
     b->tps = reinterpret_cast<int**>(b->dmem + oT);
+    b->ifaces = reinterpret_cast<BIface*>(b->dmem + oI);
+    b->iface_units = reinterpret_cast<int2*>(b->dmem + oIU);
     // sources, detectors, step counters (independent of the tile choice)
     std::vector<BSrc> hsE, hsH;
     std::vector<int2> huE, huH, hdu;
     std::vector<BDet> hd;
     std::vector<int> hdr;
     std::vector<int*> htp;
+    std::vector<BIface> hif;
+    std::vector<int2> hifu[3];
     for (int s = 0; s < n; ++s) {
         FdtdPlan* p = plans[s];
         const FdtdBuffers& bb = bufs[s];
         float* hc[2] = {bb.H, p->need_hprev ? p->h_twin : bb.H};
         float* hn[2] = {p->need_hprev ? p->h_twin : bb.H, bb.H};
         htp.push_back(p->d_t);
+        if (p->d.record_interfaces && p->d.n_slabs) {
+            BIface x{};
+            x.g = p->g; x.ifc = p->ifc; x.tp = p->d_t; x.n_slots = p->d.n_steps_total;
+            x.E = bb.E; x.H[0] = hn[0]; x.H[1] = hn[1]; x.rec = bb.recording;
+            const int dt = p->d.recording_dtype >= 0 && p->d.recording_dtype <= 2 ? p->d.recording_dtype : 0;
+            for (long long k = 0; k < (p->ifc.total + 255) / 256; ++k) hifu[dt].push_back(make_int2((int)hif.size(), (int)k));
+            hif.push_back(x);
+        }
         for (int q = 0; q < p->d.n_sources; ++q) {
             const DSource& so = p->src[q];
             const long long P = so.kind == FDTD_SRC_PLANE ? face_cells(p->d.sources[q]) : 1;
@@ -343,6 +372,16 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     up(b->det_units, hdu.data(), sizeof(int2) * hdu.size());
     up(b->det_red, hdr.data(), sizeof(int) * hdr.size());
     up(b->tps, htp.data(), sizeof(int*) * htp.size());
+    {
+        std::vector<int2> all;
+        for (int dt = 0; dt < 3; ++dt) {
+            b->iface_start[dt] = (int)all.size();
+            all.insert(all.end(), hifu[dt].begin(), hifu[dt].end());
+        }
+        b->iface_start[3] = (int)all.size();
+        up(b->ifaces, hif.data(), sizeof(BIface) * hif.size());
+        up(b->iface_units, all.data(), sizeof(int2) * all.size());
+    }
     if (e != cudaSuccess) {
         fprintf(stderr, "fdtd_batch_create: upload: %s\n", cudaGetErrorString(e));
         cudaFree(b->dmem);
@@ -392,7 +431,10 @@ int32_t fdtd_batch_launches_per_step(const FdtdBatch* b) {
     if (!b) return 0;
     int classes = 0;
     for (int cls = 0; cls < 4; ++cls) classes += b->class_start[cls + 1] > b->class_start[cls];
-    return 2 * classes + 1 + (b->n_src_unitsE > 0) + (b->n_src_unitsH > 0) + (b->n_det_units > 0) + (b->n_det_red > 0);
+    int ifc = 0;
+    for (int dt = 0; dt < 3; ++dt) ifc += b->iface_start[dt + 1] > b->iface_start[dt];
+    return 2 * classes + 1 + ifc + (b->n_src_unitsE > 0) + (b->n_src_unitsH > 0) + (b->n_det_units > 0) +
+           (b->n_det_red > 0);
 }
 
 }  // extern "C"

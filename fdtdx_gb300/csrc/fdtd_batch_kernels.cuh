@@ -73,6 +73,27 @@ __global__ void __launch_bounds__(kDetBlock) k_batch_detector_finalize(const int
     }
 }
 
+// PML-interface recording of one simulation (dtype per group).
+struct BIface {
+    Geo g;
+    IfaceDev ifc;
+    const int* tp;
+    int n_slots;
+    float* E;
+    float* H[2];
+    void* rec;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_interfaces(const int2* __restrict__ units, int n_units,
+                                                          const BIface* __restrict__ args, int parity) {
+    for (int u = blockIdx.x; u < n_units; u += gridDim.x) {
+        const int2 bu = units[u];
+        const BIface& b = args[bu.x];
+        interfaces_body<T, false>(b.g, b.ifc, b.tp, b.n_slots, b.E, b.H[parity], reinterpret_cast<T*>(b.rec), bu.y);
+    }
+}
+
 __global__ void k_batch_advance(int* const* __restrict__ tps, int n) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) *tps[q] += 1;

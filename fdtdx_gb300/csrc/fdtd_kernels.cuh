@@ -735,9 +735,9 @@ struct IfaceDev {
 };
 
 template <typename T, bool RESTORE>
-__global__ void k_interfaces(const Geo g, const IfaceDev ifc, const int* __restrict__ tp, int n_slots, float* E, float* H,
-                             T* rec) {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& ifc, const int* __restrict__ tp,
+                                                int n_slots, float* E, float* H, T* rec, int blk) {
+    const long long q = (long long)blk * blockDim.x + threadIdx.x;
     if (q >= ifc.total) return;
     int t = *tp;
     if (t < 0) t += n_slots;  // a negative step index wraps like a JAX index
@@ -762,6 +762,12 @@ __global__ void k_interfaces(const Geo g, const IfaceDev ifc, const int* __restr
             else base[comp * P + pidx] = to_storage<T>(F[comp * g.N + c]);
         }
     }
+}
+
+template <typename T, bool RESTORE>
+__global__ void k_interfaces(const Geo g, const IfaceDev ifc, const int* __restrict__ tp, int n_slots, float* E, float* H,
+                             T* rec) {
+    interfaces_body<T, RESTORE>(g, ifc, tp, n_slots, E, H, rec, blockIdx.x);
 }
 
 __global__ void k_set_step(int* tp, int t) { *tp = t; }

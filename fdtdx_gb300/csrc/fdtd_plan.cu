@@ -879,12 +879,16 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
     const long long N = (long long)d->nx * d->ny * d->nz;
     long long bytes = 4ll * N * (3 + 3 + d->n_eps + d->n_mu + d->n_sigma_E + d->n_sigma_H);
     const int n3[3] = {d->nx, d->ny, d->nz};
-    long long iface = 0;
+    long long iface = 0, psi = 0;
     for (int s = 0; s < d->n_slabs; ++s) {
         const FdtdSlabDesc& sl = d->slabs[s];
-        bytes += 4ll * 4 * (N / n3[sl.axis]) * sl.thickness;  // psi_E and psi_H pairs
+        psi += 4ll * 4 * (N / n3[sl.axis]) * sl.thickness;  // psi_E and psi_H pairs
         iface += N / n3[sl.axis];
     }
+    bytes += psi;
+    // a recording plan is a reversible-gradient job: the state's cotangents, their twins, a
+    // reconstruction copy of the state and the inv_eps gradient
+    if (d->record_interfaces) bytes += 3 * (24ll * N + psi) + 4ll * d->n_eps * N;
     bool hprev = false;
     for (int q = 0; q < d->n_detectors; ++q) {
         const FdtdDetectorDesc& dd = d->detectors[q];

@@ -177,3 +177,39 @@ def strip(shape=(128, 128, 96), width_um: float = 0.5, steps: int = 2000, dx: fl
                                            direction="+", wave_characters=(WaveCharacter(wavelength=WL),),
                                            scaling_mode="pulse"))
     return place_objects(objs, cfg, device=device)
+
+
+def serving_job(shape=(64, 64, 64), steps: int = 1000, seed: int = 0, anisotropic: bool = False,
+                gradient: bool = False, with_recorder: bool = True, n_boxes: int = 20, pml: int = 10,
+                dx: float = 50e-9, device=None):
+    """A request of the serving stream: random boxes (isotropic eps from {2.1025, 12.11}, or
+    per-axis eps uniform in [2, 12]), a pulsed z dipole at the centre and an E phasor plane
+    near the +z face whose sum |phasor|^2 is the gradient jobs' objective."""
+    rng = np.random.default_rng(seed)
+    pml = min(pml, max(2, min(shape) // 4))
+    cfg = _config(dx, steps, gradient=gradient and with_recorder)
+    vol = SimulationVolume(shape=shape)
+    objs = [vol]
+    objs += list(boundary_objects_from_config(BoundaryConfig.from_uniform_bound(thickness=pml), vol).values())
+    lo, hi = [pml] * 3, [n - pml for n in shape]
+    for b in range(n_boxes):
+        st = []
+        for a in range(3):
+            span = hi[a] - lo[a]
+            side = min(int(rng.integers(3, min(15, max(3, span - 1)) + 1)), span)
+            start = int(rng.integers(lo[a], hi[a] - side + 1))
+            st.append((start, start + side))
+        if anisotropic:
+            eps = tuple(float(x) for x in rng.uniform(2.0, 12.0, size=3))
+        else:
+            eps = float(rng.choice([EPS_SIO2, EPS_SI]))
+        objs.append(UniformMaterialObject(name=f"box{b}", grid_slice_tuple=tuple(st),
+                                          material=Material(permittivity=eps), placement_order=b))
+    c = [n // 2 for n in shape]
+    objs.append(PointDipoleSource(name="dipole", grid_slice_tuple=tuple((x, x + 1) for x in c), polarization=2,
+                                  wave_character=WaveCharacter(wavelength=WL), temporal_profile=pulse_5fs()))
+    zd = max(c[2] + 1, shape[2] - pml - 2)
+    objs.append(PhasorDetector(name="objective", grid_slice_tuple=((lo[0], hi[0]), (lo[1], hi[1]), (zd, zd + 1)),
+                               wave_characters=(WaveCharacter(wavelength=WL),), components=("Ex", "Ey", "Ez"),
+                               scaling_mode="pulse"))
+    return place_objects(objs, cfg, device=device)

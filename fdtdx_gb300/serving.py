@@ -1,0 +1,409 @@
+"""Serving loop: forward and gradient jobs admitted by HBM footprint, continuously batched.
+
+There is no serving layer in fdtdx; this module is the GB300 runtime around the native
+path for a stream of independent simulation requests:
+
+* admission by HBM footprint (``fdtd_footprint_bytes``, which counts fields, materials,
+  psi, detector states, the interface recording and, for gradient jobs, the adjoint
+  buffers) against a budget, plus a slot limit; FIFO with bounded backfill (a job that
+  does not fit may be overtaken by later ones at most ``max_bypass`` times);
+* every admitted job keeps its state on the device until it completes;
+* continuous batching: all jobs in their forward phase advance together through one
+  ``fdtd_batch_forward`` call per chunk (the batch is rebuilt whenever a job joins or
+  leaves), while gradient jobs in their adjoint phase run ``fdtd_adjoint`` chunks on a
+  second stream, so the two kinds of work overlap on the GPU;
+* per-job latency (arrival to completion) and aggregate throughput are recorded.
+
+The scheduling logic (``Scheduler``) is host-only and unit-tested without a GPU.
+"""
+
+from __future__ import annotations
+
+import collections
+import math
+import time
+from dataclasses import dataclass
+from typing import Callable
+
+import torch
+
+from fdtdx_gb300.config import SimulationConfig
+from fdtdx_gb300.container import ArrayContainer, ObjectContainer
+
+
+def phasor_power_loss(name: str) -> Callable[[dict], torch.Tensor]:
+    """Objective sum |phasor|^2 of detector ``name`` (the inverse-design form)."""
+
+    def loss(det: dict) -> torch.Tensor:
+        return (det[name]["phasor"].abs() ** 2).sum()
+
+    return loss
+
+
+# build(device, with_recorder) -> (objects, arrays, config): places the job's simulation on
+# `device`; gradient jobs are built with an interface recorder on the GPU.
+Builder = Callable[[str, bool], tuple[ObjectContainer, ArrayContainer, SimulationConfig]]
+
+
+@dataclass
+class Job:
+    """One request: how to place its simulation and what to compute."""
+
+    build: Builder
+    kind: str = "forward"                       # "forward" or "gradient"
+    loss: Callable[[dict], torch.Tensor] | None = None  # gradient jobs: scalar of the detector states
+    arrival: float = 0.0                        # seconds after the stream start
+    # filled in by estimate_footprint / the server
+    id: int = -1
+    footprint: int = 0
+    n_cells: int = 0
+    steps: int = 0
+    objects: ObjectContainer | None = None
+    arrays: ArrayContainer | None = None
+    config: SimulationConfig | None = None
+    detectors: dict | None = None               # gradient jobs: the final detector states
+    phase: str = "queued"                       # queued, forward, adjoint, done
+    t_fwd: int = 0                              # forward steps done
+    t_adj: int = 0                              # adjoint steps left
+    bypassed: int = 0
+    t_admit: float = math.nan
+    t_done: float = math.nan
+    result: ArrayContainer | None = None
+    grad: torch.Tensor | None = None
+    loss_value: float | None = None
+    scene: object = None
+    state: ArrayContainer | None = None
+    lam: dict | None = None
+
+    @property
+    def cells(self) -> int:
+        return self.n_cells
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+def random_boxes_job(shape, steps: int, seed: int, kind: str = "forward", anisotropic: bool = False,
+                     arrival: float = 0.0, **kw) -> Job:
+    """A serving request over ``scenes.serving_job`` (random boxes, dipole, E phasor plane)."""
+    from fdtdx_gb300 import scenes
+
+    def build(device: str, with_recorder: bool):
+        o, a, _p, c, _i = scenes.serving_job(shape=tuple(shape), steps=steps, seed=seed, anisotropic=anisotropic,
+                                             gradient=kind == "gradient", with_recorder=with_recorder,
+                                             device=device, **kw)
+        return o, a, c
+
+    loss = phasor_power_loss("objective") if kind == "gradient" else None
+    return Job(build=build, kind=kind, loss=loss, arrival=arrival)
+
+
+def estimate_footprint(job: Job) -> int:
+    """The job's device footprint from a host-side build of its description (no device
+    memory is touched): ``fdtd_footprint_bytes`` of its plan description."""
+    from fdtdx_gb300.engine import Scene
+
+    objects, arrays, config = job.build("cpu", False)
+    scene = Scene(objects, arrays, config, record_interfaces=job.kind == "gradient")
+    job.footprint = scene.footprint_bytes()
+    n = objects.volume.grid_shape
+    job.n_cells = n[0] * n[1] * n[2]
+    job.steps = config.time_steps_total
+    return job.footprint
+
+
+class Scheduler:
+    """Admission and phase bookkeeping of the serving loop (host only)."""
+
+    def __init__(self, budget_bytes: int, max_slots: int = 64, max_bypass: int = 8):
+        self.budget = int(budget_bytes)
+        self.max_slots = int(max_slots)
+        self.max_bypass = int(max_bypass)
+        self.queue: collections.deque[Job] = collections.deque()
+        self.active: list[Job] = []
+        self.used = 0
+        self.done: list[Job] = []
+
+    def arrive(self, job: Job) -> None:
+        if job.footprint > self.budget:
+            raise ValueError(f"job {job.id} needs {job.footprint} bytes, more than the whole budget {self.budget}")
+        job.phase = "queued"
+        self.queue.append(job)
+
+    def admit(self, now: float) -> list[Job]:
+        """Admit queued jobs that fit, in arrival order; a job that does not fit lets later
+        ones pass at most ``max_bypass`` times, after which admission waits for it."""
+        admitted = []
+        blocked = False
+        for job in list(self.queue):
+            if len(self.active) >= self.max_slots:
+                break
+            fits = self.used + job.footprint <= self.budget
+            if fits and not blocked:
+                self.queue.remove(job)
+                self.active.append(job)
+                self.used += job.footprint
+                job.phase = "forward"
+                job.t_admit = now
+                admitted.append(job)
+            elif not fits:
+                job.bypassed += 1
+                if job.bypassed > self.max_bypass:
+                    blocked = True  # reserve: nothing behind it is admitted until it fits
+        return admitted
+
+    def forward_jobs(self) -> list[Job]:
+        return [j for j in self.active if j.phase == "forward"]
+
+    def adjoint_jobs(self) -> list[Job]:
+        return [j for j in self.active if j.phase == "adjoint"]
+
+    def forward_chunk(self, cap: int) -> int:
+        """Steps the forward batch can advance: at most ``cap`` and no job past its end."""
+        fw = self.forward_jobs()
+        if not fw:
+            return 0
+        return max(1, min(cap, min(j.steps - j.t_fwd for j in fw)))
+
+    def advanced(self, job: Job, n: int) -> None:
+        job.t_fwd += n
+
+    def forward_finished(self, job: Job) -> bool:
+        return job.t_fwd >= job.steps
+
+    def start_adjoint(self, job: Job) -> None:
+        job.phase = "adjoint"
+        job.t_adj = job.steps + 1  # the reference's backward loop runs t = T-1 .. -1
+
+    def complete(self, job: Job, now: float) -> None:
+        job.phase = "done"
+        job.t_done = now
+        self.active.remove(job)
+        self.used -= job.footprint
+        self.done.append(job)
+
+    def idle(self) -> bool:
+        return not self.queue and not self.active
+
+
+class Server:
+    """The GPU serving loop over a list of timed jobs (``Job.arrival`` in seconds)."""
+
+    def __init__(self, budget_bytes: int = 160 * 10**9, max_slots: int = 64, target_chunk_s: float = 0.05,
+                 autotune: bool = True):
+        self.sched = Scheduler(budget_bytes, max_slots)
+        self.target = float(target_chunk_s)
+        self.autotune = autotune
+        self._tile = None
+        self._batch = None
+        self._members: tuple = ()
+        self.rate = 2.0e10  # cell-updates/s estimate, refined online
+        self.adj_rate = 6.0e9
+        self.forward_cell_updates = 0
+        self.adjoint_cell_updates = 0
+        self.makespan = 0.0
+
+    # ---- job lifecycle on the device
+    def _prepare(self, job: Job) -> None:
+        """Places an admitted job on the device and builds its plan."""
+        from fdtdx_gb300.engine import Scene
+        from fdtdx_gb300.fdtd import _materials_detached
+
+        rec = job.kind == "gradient"
+        job.objects, job.arrays, job.config = job.build("cuda", rec)
+        job.state = _materials_detached(job.arrays).reset()
+        job.scene = Scene(job.objects, job.state, job.config, record_interfaces=rec)
+        job.steps = job.config.time_steps_total
+
+    def _batch_for(self, jobs: list[Job]):
+        from fdtdx_gb300.batch import SimulationBatch
+
+        key = tuple(j.id for j in jobs)
+        if key == self._members and self._batch is not None:
+            return self._batch, False
+        if self._batch is not None:
+            self._batch.close()
+            self._batch = None
+        self._members = key
+        b = SimulationBatch([(j.state, j.objects, j.config) for j in jobs], scenes=[j.scene for j in jobs], reset=False)
+        if self._tile is not None:
+            b.tune(*self._tile)
+        self._batch = b
+        return b, True
+
+    def _start_adjoint(self, job: Job) -> None:
+        st = job.state
+        det = {n: {k: v.detach().clone().requires_grad_(True) for k, v in s.items()}
+               for n, s in st.detector_states.items()}
+        with torch.enable_grad():
+            loss = job.loss(det)
+            leaves = [v for s in det.values() for v in s.values()]
+            grads = torch.autograd.grad(loss, leaves, allow_unused=True)
+        job.loss_value = float(loss.detach())
+        job.detectors = {n: {k: v.detach().clone() for k, v in s.items()} for n, s in st.detector_states.items()}
+        lam_det, q = {}, 0
+        for n, s in det.items():
+            for _k, v in s.items():
+                g = grads[q]
+                q += 1
+                if g is not None:
+                    lam_det[n] = g.detach().contiguous()
+        f = st.fields
+        job.lam = {
+            "E": torch.zeros_like(f.E), "H": torch.zeros_like(f.H),
+            "psi_E": {k: (torch.zeros_like(a), torch.zeros_like(b)) for k, (a, b) in f.psi_E.items()},
+            "psi_H": {k: (torch.zeros_like(a), torch.zeros_like(b)) for k, (a, b) in f.psi_H.items()},
+            "det": lam_det,
+            "grad_inv_eps": torch.zeros_like(st.inv_permittivities),
+        }
+        self.sched.start_adjoint(job)
+
+    def _finish(self, job: Job, now: float) -> None:
+        job.scene.status()
+        if job.kind == "gradient":
+            job.grad = job.lam["grad_inv_eps"]
+            job.lam = None
+            job.state = None  # reconstructed back to the start: nothing to return
+        else:
+            job.result = job.state
+        job.scene.close()
+        job.scene = None
+        job.arrays = None
+        self.sched.complete(job, now)
+
+    # ---- the loop
+    def run(self, jobs: list[Job], realtime: bool = True) -> list[Job]:
+        """Serve ``jobs`` (arrivals replayed in real time when ``realtime``); returns them done."""
+        dev = torch.device("cuda")
+        s_fwd = torch.cuda.Stream(dev)
+        s_adj = torch.cuda.Stream(dev)
+        for i, j in enumerate(jobs):
+            j.id = i
+            if not j.footprint:
+                estimate_footprint(j)
+        pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
+        t0 = time.perf_counter()
+        clock = (lambda: time.perf_counter() - t0) if realtime else None
+        vnow = 0.0
+        while pending or not self.sched.idle():
+            now = clock() if realtime else vnow
+            while pending and pending[0].arrival <= now:
+                self.sched.arrive(pending.popleft())
+            for job in self.sched.admit(now):
+                self._prepare(job)
+            fw, adj = self.sched.forward_jobs(), self.sched.adjoint_jobs()
+            if not fw and not adj:
+                if pending:
+                    if realtime:
+                        time.sleep(max(0.0, min(0.01, pending[0].arrival - now)))
+                    else:
+                        vnow = max(vnow, pending[0].arrival)
+                continue
+            # one chunk of forward batch work and one of each adjoint job, overlapping
+            ev = []
+            n_f = 0
+            if fw:
+                cells = sum(j.cells for j in fw)
+                cap = max(8, min(1000, int(self.target * self.rate / cells)))
+                n_f = self.sched.forward_chunk(cap)
+                b, fresh = self._batch_for(fw)
+                with torch.cuda.stream(s_fwd):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(s_fwd)
+                    b.advance(n_f, t0=[j.t_fwd for j in fw] if fresh else None, graph=True,
+                              autotune=self.autotune and self._tile is None, stream=s_fwd)
+                    e1.record(s_fwd)
+                    ev.append(("f", e0, e1, cells * n_f))
+            n_adj = {}
+            for j in adj:
+                n = min(j.t_adj, max(8, int(self.target * self.adj_rate / j.cells)))
+                n_adj[j.id] = n
+                with torch.cuda.stream(s_adj):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(s_adj)
+                    j.scene.adjoint(j.state, j.lam, j.t_adj - 1, n, stream=s_adj)
+                    e1.record(s_adj)
+                    ev.append(("a", e0, e1, j.cells * n))
+            s_fwd.synchronize()
+            s_adj.synchronize()
+            for kind, e0, e1, work in ev:
+                ms = e0.elapsed_time(e1)
+                if ms > 0:
+                    r = work / (ms * 1e-3)
+                    if kind == "f":
+                        self.rate = 0.7 * self.rate + 0.3 * r
+                    else:
+                        self.adj_rate = 0.7 * self.adj_rate + 0.3 * r
+            if fw and self._tile is None and self.autotune:
+                t = self._batch.tuning()
+                self._tile = (t["chunk_scale"][0], t["chunk_scale"][1], t["shell_chunk"], t["blocks_per_sm"])
+            if not realtime:
+                vnow += max([e0.elapsed_time(e1) * 1e-3 for _k, e0, e1, _w in ev] + [0.0])
+            now = clock() if realtime else vnow
+            for j in fw:
+                self.sched.advanced(j, n_f)
+                self.forward_cell_updates += j.cells * n_f
+                if self.sched.forward_finished(j):
+                    if j.kind == "gradient":
+                        self._start_adjoint(j)
+                    else:
+                        self._finish(j, now)
+            for j in adj:
+                n = n_adj[j.id]
+                j.t_adj -= n
+                self.adjoint_cell_updates += j.cells * n
+                if j.t_adj <= 0:
+                    self._finish(j, now)
+        if self._batch is not None:
+            self._batch.close()
+            self._batch = None
+        self.makespan = (time.perf_counter() - t0) if realtime else vnow
+        return jobs
+
+
+def run_one_at_a_time(jobs: list[Job], realtime: bool = True) -> list[Job]:
+    """The plain path: each job alone through run_fdtd / reversible_fdtd, in arrival order."""
+    from fdtdx_gb300.adjoint import reversible_fdtd
+    from fdtdx_gb300.fdtd import run_fdtd
+
+    t0 = time.perf_counter()
+    for i, j in enumerate(sorted(jobs, key=lambda j: j.arrival)):
+        j.id = i
+        if realtime:
+            wait = j.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        j.t_admit = time.perf_counter() - t0
+        objects, arrays, config = j.build("cuda", j.kind == "gradient")
+        j.steps = config.time_steps_total
+        n = objects.volume.grid_shape
+        j.n_cells = n[0] * n[1] * n[2]
+        if j.kind == "gradient":
+            ie = arrays.inv_permittivities.detach().clone().requires_grad_(True)
+            _, out = reversible_fdtd(arrays.aset("inv_permittivities", ie), objects, config)
+            loss = j.loss(out.detector_states)
+            (g,) = torch.autograd.grad(loss, [ie])
+            j.grad, j.loss_value = g.detach(), float(loss.detach())
+            j.detectors = {dn: {k: v.detach().clone() for k, v in st.items()} for dn, st in out.detector_states.items()}
+        else:
+            _, j.result = run_fdtd(arrays, objects, config)
+        torch.cuda.synchronize()
+        j.t_done = time.perf_counter() - t0
+        j.phase = "done"
+        del objects, arrays
+    return jobs
+
+
+def latency_stats(jobs: list[Job]) -> dict:
+    lat = sorted(j.latency for j in jobs)
+    if not lat:
+        return {"p50_s": None, "p99_s": None, "mean_s": None}
+
+    def pct(p):
+        k = min(len(lat) - 1, max(0, int(math.ceil(p / 100.0 * len(lat))) - 1))
+        return lat[k]
+
+    return {"p50_s": pct(50), "p99_s": pct(99), "mean_s": sum(lat) / len(lat)}

@@ -177,7 +177,9 @@ int64_t fdtd_interface_floats(const FdtdPlan* plan);
 /* Device bytes the plan itself holds (tables + scratch). */
 int64_t fdtd_plan_device_bytes(const FdtdPlan* plan);
 /* Device bytes one simulation of this description needs (fields, materials, psi,
- * detector states, recording, plan tables and scratch): serving admission. */
+ * detector states, recording, plan tables and scratch; with record_interfaces also the
+ * reversible gradient's cotangents, twins, reconstruction copy and gradient): serving
+ * admission. */
 int64_t fdtd_footprint_bytes(const FdtdDesc* desc);
 
 /* Forward steps t0 .. t0+n_steps-1.  flags bit 0: use a CUDA graph for the loop. */
@@ -228,10 +230,10 @@ int fdtd_profile_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, in
  *
  * No counterpart in the reference (which runs one simulation per call, fdtdx/fdtd/fdtd.py:
  * 421-496); it replaces looping that call over a set of simulations.  A batch holds built
- * plans (forward-only: record_interfaces = 0) with their buffers.  One batch step runs
- * every simulation's step with one persistent launch per kernel kind (E update, E
- * sources, H update with fused detectors, H sources, detectors, reductions, step
- * counters) over a flat list of work units; results equal the per-plan fdtd_forward
+ * plans with their buffers.  One batch step runs every simulation's forward step with
+ * one persistent launch per kernel kind (E update, E sources, H update with fused
+ * detectors, H sources, interface recording, detectors, reductions, step counters)
+ * over a flat list of work units; results equal the per-plan fdtd_forward
  * (same device bodies).  The plans must stay alive and unused elsewhere while the
  * batch exists. */
 typedef struct FdtdBatch FdtdBatch;
