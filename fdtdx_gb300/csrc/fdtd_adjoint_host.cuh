@@ -240,6 +240,8 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
 extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, int32_t t_end,
                             int32_t n_steps, void* stream) {
     if (!p) return FDTD_EINVAL;
+    if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
+        return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_adjoint)");
     if (int rc = check_bufs(p, b)) return rc;
     if (int rc = check_adj(p, adj)) return rc;
     if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)

@@ -492,6 +492,9 @@ int batch_autotune(FdtdBatch* b, int budget, int* parity, cudaStream_t st) {
 
 extern "C" int fdtd_batch_forward(FdtdBatch* b, const int32_t* t0, int32_t n_steps, int32_t flags, void* stream) {
     if (!b) return FDTD_EINVAL;
+    if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
+        return bfail(b, FDTD_ECUDA, std::string("error left pending by an earlier CUDA call (before fdtd_batch_forward): ") +
+                                        cudaGetErrorString(pre));
     if (n_steps < 0) return bfail(b, FDTD_EINVAL, "n_steps must be >= 0");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     for (int s = 0; s < b->n; ++s) {
@@ -508,11 +511,10 @@ extern "C" int fdtd_batch_forward(FdtdBatch* b, const int32_t* t0, int32_t n_ste
     int parity = 0, done = 0;
     if ((flags & 2) && !b->tuned) done += batch_autotune(b, n_steps / 4, &parity, st);
     const bool use_graph = (flags & 1) != 0;
-    const int unit = b->any_hprev ? 2 : 1;
-    if (use_graph && n_steps - done >= 8) {
+    // one fixed graph length, so calls with different step counts reuse the same graph
+    constexpr int G = 32;
+    if (use_graph && n_steps - done >= G + 1) {
         if (parity) done += (parity = batch_run_direct(b, parity, 1, st), 1);
-        int G = std::min(n_steps - done, 64);
-        G -= G % unit;
         if (!b->gexec || b->gsteps != G) {
             batch_drop_graph(b);
             if (!b->cap_stream) {

@@ -297,8 +297,17 @@ void configure_tma(FdtdPlan* p) {
     const size_t smE = tma_smem(tma_cfg(tz, ty, ns, false, nmE, nsE, nullptr));
     const size_t smH = tma_smem(tma_cfg(tz, ty, ns, true, nmH, nsH, nullptr, staged_planes(p)));
     int occ = 1 << 30;
+    // The attribute is per kernel function and process-wide, shared by every plan: raise it
+    // once to the device's opt-in maximum (a smaller plan built later must not shrink the
+    // limit a larger plan's launches rely on); occupancy below uses this plan's own size.
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 0;
     auto setup = [&](const void* fn, size_t sm) {
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if ((int)sm > optin || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+            occ = 0;
+            return;
+        }
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, sm) != cudaSuccess) nb = 0;
         occ = std::min(occ, nb);
@@ -792,6 +801,8 @@ int32_t fdtd_launches_per_step(const FdtdPlan* p) {
 
 int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, int32_t flags, void* stream) {
     if (!p) return FDTD_EINVAL;
+    if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
+        return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_forward)");
     if (int rc = check_bufs(p, b)) return rc;
     if (n_steps < 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)
         return fail(p, FDTD_EINVAL, "time steps out of the range covered by the plan's tables");
@@ -855,6 +866,8 @@ int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps,
 // psi frozen), reverse E.
 int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_steps, void* stream) {
     if (!p) return FDTD_EINVAL;
+    if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
+        return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_reverse)");
     if (int rc = check_bufs(p, b)) return rc;
     if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)
         return fail(p, FDTD_EINVAL, "reverse steps out of the range covered by the plan's tables");

@@ -271,6 +271,8 @@ class Server:
         job.scene = None
         job.arrays = None
         self.sched.complete(job, now)
+        if job.footprint > 2**30:
+            torch.cuda.empty_cache()  # hand large blocks back so the next large job can be placed
 
     # ---- the loop
     def run(self, jobs: list[Job], realtime: bool = True) -> list[Job]:

@@ -274,3 +274,22 @@ def test_tma_kernels_match_register_kernels(tile):
         for q in range(2):
             assert rel_l2(outs[0].fields.psi_E[n][q], outs[1].fields.psi_E[n][q]) < 1e-6
             assert rel_l2(outs[0].fields.psi_H[n][q], outs[1].fields.psi_H[n][q]) < 1e-6
+
+
+def test_plans_of_different_tile_memory_coexist():
+    """A plan built after another must not break it: the TMA kernels' shared-memory limit is a
+    process-wide function attribute (an anisotropic plan stages three material planes, an
+    isotropic one fewer)."""
+    o1, a1, _, c1, _ = scenes.serving_job(shape=(40, 36, 32), steps=30, seed=1, anisotropic=True, device="cuda")
+    o2, a2, _, c2, _ = scenes.serving_job(shape=(40, 36, 32), steps=30, seed=2, anisotropic=False, device="cuda")
+    s1 = Scene(o1, a1.reset(), c1)
+    w1 = a1.reset()
+    s1.plan  # build the large-tile plan first
+    s2 = Scene(o2, a2.reset(), c2)
+    w2 = a2.reset()
+    s2.plan
+    s1.forward(w1, 0, 30)
+    s2.forward(w2, 0, 30)
+    torch.cuda.synchronize()
+    assert torch.isfinite(w1.fields.E).all() and torch.isfinite(w2.fields.E).all()
+    assert s1.uses_tma
