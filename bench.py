@@ -106,19 +106,37 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _fused(dd) -> bool:
+    """E-only phasor / field detectors without volume reduction ride in the H half-step."""
+    return dd.kind in (1, 0) and (dd.comp_mask & 56) == 0 and not dd.reduce_volume
+
+
 def algorithmic_bytes(scene) -> dict:
-    """Compulsory float32 bytes per launch of each kernel class (see the design notes)."""
+    """Compulsory float32 bytes per launch group: E update (E r/w, H, inv_eps, sigma, psi_E
+    r/w on slab cells), H update (H r/w, E, inv_mu, sigma, psi_H r/w, plus the read-modify-
+    write of the detectors fused into it), detectors (the other detectors' samples)."""
+    import fdtdx_gb300._native as NATIVE
+
     d = scene.desc
     N = d.nx * d.ny * d.nz
     slab = sum((N // (d.nx, d.ny, d.nz)[d.slabs[s].axis]) * d.slabs[s].thickness for s in range(d.n_slabs))
     e = N * (24 + 12 + 4 * d.n_eps + 4 * d.n_sigma_E) + slab * 16
     h = N * (24 + 12 + 4 * d.n_mu + 4 * d.n_sigma_H) + slab * 16
     det = 0
+    n_fused = 0
     for q in range(d.n_detectors):
         dd = d.detectors[q]
         R = (dd.hi[0] - dd.lo[0]) * (dd.hi[1] - dd.lo[1]) * (dd.hi[2] - dd.lo[2])
         C_ = bin(dd.comp_mask).count("1")
-        det += R * (4 * C_ + 16 * C_ * max(1, dd.n_freq))
+        if dd.kind == NATIVE.DET_PHASOR:
+            b = R * 16 * C_ * max(1, dd.n_freq)  # complex64 read + write per component and frequency
+        else:
+            b = R * 4 * C_
+        if _fused(dd) and n_fused < 2:
+            h += b
+            n_fused += 1
+        else:
+            det += b + R * 4 * C_  # samples gathered from the fields
     return {"E update": e, "H update": h, "detectors": det}
 
 
@@ -182,10 +200,12 @@ def run_gpu(args):
     dom = max(("E update", "H update", "detectors"), key=lambda k: times[k])
     peak, peak_kind = _peaks()
     achieved = alg[dom] / (times[dom] / 1e3) / 1e9
-    traffic_file = ROOT / "profiles" / "traffic.json"
     traffic = None
-    if traffic_file.exists():
-        traffic = json.loads(traffic_file.read_text()).get(dom)
+    traffic_file = ROOT / "profiles" / "coupler_traffic.txt"
+    if traffic_file.exists() and shape == SHAPE:
+        for ln in traffic_file.read_text().splitlines():
+            if ln.startswith(dom + " "):
+                traffic = int(ln.split()[-1])
 
     # end to end through run_fdtd: permittivity from pinned host memory, flux phasors read back
     cfg_e2e = fx.SimulationConfig(time=K * cfg.time_step_duration, grid=cfg.grid, courant_factor=cfg.courant_factor)
@@ -282,7 +302,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def bench_gradient(dev) -> dict:
+def bench_gradient(dev, steps: int = 3000) -> dict:
     """Inverse-design gradient: 200x200x100 @25 nm, 10-cell CPML, 3000 steps, 120x120x9 design
     region, pulsed plane source, sum |phasor|^2 over a 40x40 plane; d loss / d params through
     reversible_fdtd (forward with interface recording, then the T+1-step adjoint)."""
@@ -290,7 +310,7 @@ def bench_gradient(dev) -> dict:
     from fdtdx_gb300 import scenes
     from fdtdx_gb300.fdtd import _materials_detached, get_scene
 
-    objects, arrays, params, cfg, _ = scenes.inverse_design(device=dev)
+    objects, arrays, params, cfg, _ = scenes.inverse_design(steps=steps, device=dev)
     T = cfg.time_steps_total
     N = 200 * 200 * 100
 
@@ -318,7 +338,7 @@ def bench_gradient(dev) -> dict:
     torch.cuda.synchronize()
     fwd = e0.elapsed_time(e1) / 1e3
     return {
-        "workload": "inverse design 200x200x100 @25nm, 10-cell CPML, 3000 steps, 120x120x9 design, plane pulse, "
+        "workload": f"inverse design 200x200x100 @25nm, 10-cell CPML, {T} steps, 120x120x9 design, plane pulse, "
                     "|phasor|^2 on a 40x40 plane; gradient via reversible_fdtd (T+1 adjoint steps)",
         "gradient_s": round(total, 4),
         "forward_s": round(fwd, 4),
@@ -547,11 +567,24 @@ def main():
     ap.add_argument("--batch-sims", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2000)
     ap.add_argument("--serve-jobs", type=int, default=32)
+    ap.add_argument("--case", default="all", choices=["all", "gradient", "batch", "serving"],
+                    help="run one secondary measurement alone and print its record (profiling)")
+    ap.add_argument("--grad-steps", type=int, default=3000, help="steps of the gradient case (profiling: fewer)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.case != "all":
+        torch.cuda.set_device(0)
+        dev = torch.device("cuda", 0)
+        if args.case == "gradient":
+            out = bench_gradient(dev, args.grad_steps)
+        elif args.case == "batch":
+            out = bench_batch(dev, args.batch_sims, args.batch_steps)
+        else:
+            out = bench_serving(2.0e10, args.serve_jobs)
+        print(json.dumps({"case": args.case, **out}))
     else:
         run_gpu(args)
 
