@@ -189,13 +189,16 @@ def run_gpu(args):
     value = ncell * K * ws / (ms / 1e3)
 
     # per-kernel device times (CUDA events around each launch group, same stream, same workload)
-    prof = (C.c_float * 6)()
+    prof = (C.c_float * 8)()
     lib = NATIVE.load()
     b = scene.buffers(arrays)
     rc = lib.fdtd_profile_forward(scene.plan, C.byref(b), W + K, 5, prof, C.c_void_p(stream.cuda_stream))
     NATIVE.check(rc, scene.plan, "fdtd_profile_forward")
-    groups = ["E update", "E sources", "H update", "H sources", "detectors", "interfaces"]
-    times = dict(zip(groups, [float(x) for x in prof]))
+    parts = ["E core", "E shell", "E sources", "H core", "H shell", "H sources", "detectors", "interfaces"]
+    split = dict(zip(parts, [float(x) for x in prof]))
+    times = {"E update": split["E core"] + split["E shell"], "E sources": split["E sources"],
+             "H update": split["H core"] + split["H shell"], "H sources": split["H sources"],
+             "detectors": split["detectors"], "interfaces": split["interfaces"]}
     alg = algorithmic_bytes(scene)
     dom = max(("E update", "H update", "detectors"), key=lambda k: times[k])
     peak, peak_kind = _peaks()
@@ -288,6 +291,7 @@ def run_gpu(args):
             "traffic": traffic,
             "alg_bytes_per_launch": alg[dom],
             "kernel_ms": {k: round(v, 4) for k, v in times.items()},
+            "launch_ms": {k: round(v, 4) for k, v in split.items()},
         },
         "e2e": e2e,
         "gpu_launches": launches,

@@ -156,23 +156,11 @@ void launch_adj_kernel(const AdjArgs& a, long long blocks, AdjKind kind, cudaStr
     }
 }
 
-// Slabs that can reach a box or its one-cell rim (every slab when an axis wraps).
-int box_slab_mask(const FdtdPlan* p, const Box& b) {
-    if (p->g.px || p->g.py || p->g.pz) return 63;
-    int m = 0;
-    for (int s = 0; s < p->d.n_slabs; ++s) {
-        const DSlab& sl = p->slab[s];
-        if (sl.lo < b.hi[sl.axis] + 1 && sl.lo + sl.L > b.lo[sl.axis] - 1) m |= 1 << s;
-    }
-    return m;
-}
-
 template <bool HSIDE>
 void launch_adj_boxes(const FdtdPlan* p, AdjArgs a, const Box* boxes, const int* chunks, int n, AdjKind kind,
                       cudaStream_t st) {
     const long long blocks = fill_boxes(p, a, boxes, chunks, n);
     if (blocks <= 0) return;
-    for (int q = 0; q < n; ++q) a.bslab[q] = box_slab_mask(p, boxes[q]);
     if (p->vec == 4) launch_adj_kernel<HSIDE, 4>(a, blocks, kind, st);
     else if (p->vec == 2) launch_adj_kernel<HSIDE, 2>(a, blocks, kind, st);
     else launch_adj_kernel<HSIDE, 1>(a, blocks, kind, st);

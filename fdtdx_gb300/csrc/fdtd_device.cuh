@@ -68,6 +68,7 @@ struct UpdArgs {
     // blocks, box b owning blocks [bstart[b], bstart[b+1]) laid out as (nbx[b] columns) x (x chunks)
     int nbox;
     int blo[6][3], bhi[6][3], bchunk[6], nbx[6], bstart[7];
+    int bslab[6];               // per box: bit s set when slab s can reach the box or its one-cell rim
     const int* tp;              // device time-step counter
     int n_fuse;
     DFuse fuse[kMaxFuse];

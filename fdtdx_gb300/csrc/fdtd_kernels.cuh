@@ -28,13 +28,13 @@ __device__ __forceinline__ long long psi_offset(const DSlab& sl, int i, int j, i
            (k - (sl.axis == 2 ? sl.lo : 0));
 }
 
-__device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k, PsiPre& pr) {
+__device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k, PsiPre& pr, int active = 63) {
     const int idx3[3] = {i, j, k};
 #pragma unroll
     for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
         pr.v[s][0] = 0.f;
         pr.v[s][1] = 0.f;
-        if (s >= a.n_slab) continue;
+        if (s >= a.n_slab || !(active >> s & 1)) continue;
         const DSlab& sl = a.slab[s];
         const int l = idx3[sl.axis] - sl.lo;
         if ((unsigned)l >= (unsigned)sl.L) continue;
@@ -47,11 +47,12 @@ __device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k,
 // cpml_correct with the psi values taken from a prefetch.
 template <bool REV, bool HSIDE>
 __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k, const float d[6], float cu[3],
-                                           const PsiPre& pr) {
+                                           const PsiPre& pr, int active = 63) {
     const int idx3[3] = {i, j, k};
 #pragma unroll
     for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
         if (s >= a.n_slab) break;
+        if (!(active >> s & 1)) continue;
         const DSlab& sl = a.slab[s];
         const int l = idx3[sl.axis] - sl.lo;
         if ((unsigned)l >= (unsigned)sl.L) continue;
@@ -158,6 +159,42 @@ __device__ __forceinline__ bool maybe_slab(const UpdArgs& a, int i, int j, int k
     return false;
 }
 
+// The slab mask of block `blk`'s box.
+template <typename Args>
+__device__ __forceinline__ int box_slab_mask_of(const Args& a, int blk) {
+    int m = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        if (q < a.nbox && blk >= a.bstart[q]) m = a.bslab[q];
+    return m;
+}
+
+// Slabs of the box mask that can hold this thread's column: a y or z slab is fixed along the
+// x-march (decided once), an x slab is tested per plane (slab_active).
+__device__ __forceinline__ int column_slabs(const UpdArgs& a, int box_mask, int j, int k0, int vec) {
+    int m = 0;
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (s >= a.n_slab || !(box_mask >> s & 1)) continue;
+        const DSlab& sl = a.slab[s];
+        if (sl.axis == 1 && (unsigned)(j - sl.lo) >= (unsigned)sl.L) continue;
+        if (sl.axis == 2 && (k0 + vec - 1 < sl.lo || k0 >= sl.lo + sl.L)) continue;
+        m |= 1 << s;
+    }
+    return m;
+}
+
+__device__ __forceinline__ int slab_active(const UpdArgs& a, int col_mask, int i) {
+    int m = col_mask;
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (!(col_mask >> s & 1)) continue;
+        const DSlab& sl = a.slab[s];
+        if (sl.axis == 0 && (unsigned)(i - sl.lo) >= (unsigned)sl.L) m &= ~(1 << s);
+    }
+    return m;
+}
+
 // The material update of one component of one cell.
 template <bool REV, bool HSIDE>
 __device__ __forceinline__ float material_update(const UpdArgs& a, float u0, float cu, float m, const float* sig_p,
@@ -218,6 +255,7 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     const long long N = g.N;
     const long long sy = g.nz;
     const float* __restrict__ H = a.F;
+    const int col = PML && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
     Vec<VEC> Hy_m = ldv_halo<VEC>(g, H, 1, i0 - 1, j, k0);
     Vec<VEC> Hz_m = ldv_halo<VEC>(g, H, 2, i0 - 1, j, k0);
     for (int i = i0; i < i1; ++i) {
@@ -242,11 +280,12 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
         Vec<VEC> Eo[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) Eo[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
-        const bool pml = PML && a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        const int act = PML && col ? slab_active(a, col, i) : 0;
+        const bool pml = act != 0;
         PsiPre pre[VEC];
         if (pml) {  // issued with the field loads, so both round trips overlap
 #pragma unroll
-            for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e]);
+            for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e], act);
         }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
@@ -256,7 +295,7 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
             const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
                                 Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
             float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-            if (pml) cpml_apply<REV, false>(a, i, j, k, d, cu, pre[e]);
+            if (pml) cpml_apply<REV, false>(a, i, j, k, d, cu, pre[e], act);
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
@@ -287,7 +326,7 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
                                                 const float2 w[kMaxFuse][kMaxFuseFreq], int i, int j, int k,
                                                 float Ex, float Ex_kp, float Ex_im, float Exkp_im, float Ey, float Ey_kp,
                                                 float Ey_jm, float Eykp_jm, float Ez, const float* staged = nullptr,
-                                                int staged_stride = 0) {
+                                                int staged_stride = 0, const float2* pref = nullptr) {
 #pragma unroll
     for (int q = 0; q < kMaxFuse; ++q) {
         if (q >= a.n_fuse) break;
@@ -319,6 +358,8 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
                     if (q == 0 && staged) {
                         const float* sp = staged + (f * d.nout + o) * staged_stride;
                         z = make_float2(sp[0], sp[1]);
+                    } else if (q == 0 && pref) {
+                        z = pref[comp];  // prefetched with the field loads (one frequency)
                     } else {
                         z = *pp;
                     }
@@ -350,6 +391,7 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     const long long sy = g.nz, sx = (long long)g.ny * g.nz;
     const float* __restrict__ E = a.F;
     const bool kin = k0 + VEC < g.nz;
+    const int col = PML && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
 
     int slot[kMaxFuse];
     float2 w[kMaxFuse][kMaxFuseFreq];
@@ -400,17 +442,42 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
         Vec<VEC> Ho[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) Ho[comp] = ldv_rw<VEC>(a.Uin + comp * N + c);
-        const bool pml = PML && a.n_slab > 0 && maybe_slab(a, i, j, k0, VEC);
+        const int act = PML && col ? slab_active(a, col, i) : 0;
+        const bool pml = act != 0;
         PsiPre pre[VEC];
         if (pml) {
 #pragma unroll
-            for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e]);
+            for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e], act);
         }
         Vec<VEC> Ey_jm{};
         float Eyk_jm = 0.f;
         if (!REV && any) {
             Ey_jm = nbv<VEC>(g, E, N + c - sy, j > 0, 1, i, j - 1, k0);
             Eyk_jm = ld_halo(g, E, 1, i, j - 1, k0 + VEC);
+        }
+        // the first fused phasor's previous values (one frequency), loaded with the fields so
+        // its read-modify-write does not add a second round trip after the update
+        float2 pf[VEC][3];
+        bool pfo = false;
+        if (!REV && a.n_fuse > 0 && slot[0] >= 0 && a.fuse[0].kind == FDTD_DET_PHASOR && a.fuse[0].nfreq == 1) {
+            const DFuse& d = a.fuse[0];
+            pfo = true;
+            const bool row = i >= d.lo[0] && i < d.hi[0] && j >= d.lo[1] && j < d.hi[1];
+            const float2* st = reinterpret_cast<const float2*>(d.state);
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                const int k = k0 + e;
+                const bool in = row && k >= d.lo[2] && k < d.hi[2];
+                const long long r = ((long long)(i - d.lo[0]) * d.ry + (j - d.lo[1])) * d.rz + (k - d.lo[2]);
+                int o = 0;
+#pragma unroll
+                for (int comp = 0; comp < 3; ++comp) {
+                    pf[e][comp] = make_float2(0.f, 0.f);
+                    if (!(d.mask >> comp & 1)) continue;
+                    if (in) pf[e][comp] = st[(long long)o * d.R + r];
+                    ++o;
+                }
+            }
         }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
@@ -420,7 +487,7 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
             const float d[6] = {Ez_jp.v[e] - Ez.v[e], ey_kp - Ey.v[e], ex_kp - Ex.v[e],
                                 Ez_ip.v[e] - Ez.v[e], Ey_ip.v[e] - Ey.v[e], Ex_jp.v[e] - Ex.v[e]};
             float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-            if (pml) cpml_apply<REV, true>(a, i, j, k, d, cu, pre[e]);
+            if (pml) cpml_apply<REV, true>(a, i, j, k, d, cu, pre[e], act);
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
@@ -432,7 +499,7 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
                 const float exkp_im = e + 1 < VEC ? Ex_im.v[e + 1] : Exk_im;
                 const float eykp_jm = e + 1 < VEC ? Ey_jm.v[e + 1] : Eyk_jm;
                 fused_detectors(a, slot, w, i, j, k, Ex.v[e], ex_kp, Ex_im.v[e], exkp_im, Ey.v[e], ey_kp, Ey_jm.v[e],
-                                eykp_jm, Ez.v[e]);
+                                eykp_jm, Ez.v[e], nullptr, 0, pfo ? pf[e] : nullptr);
             }
         }
 #pragma unroll
@@ -445,7 +512,7 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
 }
 
 template <bool REV, int VEC, bool PML>
-__global__ void __launch_bounds__(256) k_update_H(const __grid_constant__ UpdArgs a) {
+__global__ void __launch_bounds__(256, 3) k_update_H(const __grid_constant__ UpdArgs a) {
     update_H_body<REV, VEC, PML>(a, blockIdx.x);
 }
 

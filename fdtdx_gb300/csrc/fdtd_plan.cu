@@ -602,6 +602,17 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
 
 constexpr int kShellChunk = 4;
 
+// Slabs that can reach a box or its one-cell rim (every slab when an axis wraps).
+int box_slab_mask(const FdtdPlan* p, const Box& b) {
+    if (p->g.px || p->g.py || p->g.pz) return 63;
+    int m = 0;
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        const DSlab& sl = p->slab[s];
+        if (sl.lo < b.hi[sl.axis] + 1 && sl.lo + sl.L > b.lo[sl.axis] - 1) m |= 1 << s;
+    }
+    return m;
+}
+
 // Fills the launch's box table; returns the number of blocks of the 1-D grid.
 template <typename Args>
 long long fill_boxes(const FdtdPlan* p, Args& a, const Box* boxes, const int* chunks, int n) {
@@ -616,6 +627,7 @@ long long fill_boxes(const FdtdPlan* p, Args& a, const Box* boxes, const int* ch
         a.bchunk[q] = chunks[q];
         a.nbx[q] = nbx;
         a.bstart[q] = (int)start;
+        a.bslab[q] = box_slab_mask(p, b);
         start += (long long)nbx * nby;
     }
     a.bstart[n] = (int)start;
@@ -638,17 +650,20 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
     }
 }
 
+// `mid` (optional) is recorded between the core and the shell launches (profiling).
 template <bool REV, bool HSIDE>
-void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent_t mid = nullptr) {
     const Split sp = split_boxes(p);
     if (!sp.split) {
         const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
+        if (mid) cudaEventRecord(mid, st);
         launch_plain_boxes<REV, HSIDE, true>(p, a, &all, &p->chunk, 1, st);
         return;
     }
     UpdArgs ac = a;
     for (int x = 0; x < 3; ++x) { ac.lo[x] = sp.core.lo[x]; ac.hi[x] = sp.core.hi[x]; }
     if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
+    if (mid) cudaEventRecord(mid, st);
     int chunks[6];
     for (int q = 0; q < sp.n_shell; ++q) chunks[q] = kShellChunk;
     launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st);
@@ -932,22 +947,22 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     if (n_steps <= 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)
         return fail(p, FDTD_EINVAL, "time steps out of range");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    cudaEvent_t ev[7];
+    cudaEvent_t ev[9];
     for (auto& e : ev) cudaEventCreate(&e);
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
     float* Hcur = b->H;
     float* Hnext = p->need_hprev ? p->h_twin : b->H;
     for (int s = 0; s < n_steps; ++s) {
         cudaEventRecord(ev[0], st);
-        launch_E<false>(p, make_upd(p, b, true, Hcur, b->E, b->E), st);
-        cudaEventRecord(ev[1], st);
-        launch_sources(p, b, true, b->E, 0, st);
+        launch_half<false, false>(p, make_upd(p, b, true, Hcur, b->E, b->E), st, ev[1]);
         cudaEventRecord(ev[2], st);
-        launch_H<false>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st);
+        launch_sources(p, b, true, b->E, 0, st);
         cudaEventRecord(ev[3], st);
+        launch_half<false, true>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st, ev[4]);
+        cudaEventRecord(ev[5], st);
         launch_sources(p, b, false, Hnext, 0, st);
-        cudaEventRecord(ev[4], st);
+        cudaEventRecord(ev[6], st);
         DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
                     p->d.inv_mu_scalar};
         for (int q = 0; q < p->d.n_detectors; ++q) {
@@ -956,16 +971,16 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
             k_detector<<<dd.nblocks, kDetBlock, 0, st>>>(p->g, dd, p->d_t, f, b->det_state[q]);
             if (dd.reduce) k_detector_finalize<<<1, kDetBlock, 0, st>>>(dd, p->d_t, b->det_state[q]);
         }
-        cudaEventRecord(ev[5], st);
+        cudaEventRecord(ev[7], st);
         if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
         k_advance<<<1, 1, 0, st>>>(p->d_t, 1);
-        cudaEventRecord(ev[6], st);
-        cudaError_t e = cudaEventSynchronize(ev[6]);
+        cudaEventRecord(ev[8], st);
+        cudaError_t e = cudaEventSynchronize(ev[8]);
         if (e != cudaSuccess) {
             for (auto& x : ev) cudaEventDestroy(x);
             return cuda_fail(p, e, "fdtd_profile_forward");
         }
-        for (int k = 0; k < 6; ++k) {
+        for (int k = 0; k < 8; ++k) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
             acc[k] += ms;
@@ -975,7 +990,7 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     if (p->need_hprev && Hcur != b->H)
         cudaMemcpyAsync(b->H, Hcur, sizeof(float) * 3 * p->g.N, cudaMemcpyDeviceToDevice, st);
     for (auto& x : ev) cudaEventDestroy(x);
-    for (int k = 0; k < 6; ++k) out_ms[k] = (float)(acc[k] / n_steps);
+    for (int k = 0; k < 8; ++k) out_ms[k] = (float)(acc[k] / n_steps);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_profile_forward");
     return FDTD_OK;

@@ -221,9 +221,11 @@ int fdtd_plan_status(FdtdPlan* plan);
 int32_t fdtd_launches_per_step(const FdtdPlan* plan);
 
 /* Benchmark helper: runs forward steps t0 .. t0+n_steps-1 with CUDA events on `stream`
- * around each launch group and writes the mean device time per step, in ms, of:
- * out_ms[0] E update, [1] E-side sources, [2] H update, [3] H-side sources,
- * [4] detectors, [5] interface recording.  Synchronises the stream. */
+ * around each launch and writes the mean device time per step, in ms, of:
+ * out_ms[0] E core, [1] E CPML shell, [2] E-side sources, [3] H core (with the fused
+ * detectors), [4] H CPML shell, [5] H-side sources, [6] detectors, [7] interface
+ * recording (a grid that does not split reports its whole update as the shell).
+ * Synchronises the stream. */
 int fdtd_profile_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_steps, float* out_ms, void* stream);
 
 /* ---- Batched forward path: many simulations stepped together --------------------------
