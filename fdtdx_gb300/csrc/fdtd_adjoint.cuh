@@ -71,6 +71,7 @@ struct AdjArgs {
     int nbox;
     int blo[6][3], bhi[6][3], bchunk[6], nbx[6], bstart[7];
     int bslab[6];          // per box: bit s set when slab s can reach the box or its one-cell rim
+    int ax_slab[3][2];     // the slab on each axis' low / high face (-1: none)
 };
 
 // The slab mask of this block's box.
@@ -386,6 +387,65 @@ __global__ void __launch_bounds__(256) k_adj_E(const __grid_constant__ AdjArgs a
 // i.e. the forward E and H updates with the material moved inside the difference.
 // ---------------------------------------------------------------------------------
 
+// CPML term of the slab on `axis` at cell (i, j, k) (in range), given the base curl
+// cotangents lci = lc[(axis+1)%3] and lcj = lc[(axis+2)%3] there: the slab adds d1 to the
+// difference cotangent of d_axis F_j and d2 to that of d_axis F_i, which is the same as
+// differencing along `axis` the effective cotangents lc_ci - d1 and lc_cj + d2.  With
+// `out` the psi cotangent of step t is written (the cell is the caller's own).
+template <bool HSIDE>
+__device__ __forceinline__ void slab_term(const AdjArgs& a, int axis, int i, int j, int k, float lci, float lcj,
+                                          bool out, float& d1, float& d2) {
+    d1 = 0.f;
+    d2 = 0.f;
+    const int x = axis == 0 ? i : (axis == 1 ? j : k);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const int s = a.ax_slab[axis][side];
+        if (s < 0) continue;
+        const DSlab& sl = a.slab[s];
+        const int l = x - sl.lo;
+        if ((unsigned)l >= (unsigned)sl.L) continue;
+        const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
+        const long long p = psi_offset(sl, i, j, k);
+        const float* lp0 = HSIDE ? a.lpH[s][0] : a.lpE[s][0];
+        const float* lp1 = HSIDE ? a.lpH[s][1] : a.lpE[s][1];
+        const float t1 = lp0[p] - lci;
+        const float t2 = lp1[p] + lcj;
+        const float ca = __ldg(co + l);
+        float e1 = ca * t1, e2 = ca * t2;
+        if (!sl.kappa_one) {
+            const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+            e1 -= ikm1 * lci;
+            e2 += ikm1 * lcj;
+        }
+        d1 += e1;
+        d2 += e2;
+        if (out) {
+            const float cb = __ldg(co + sl.L + l);
+            float* o0 = HSIDE ? a.lpH_out[s][0] : a.lpE_out[s][0];
+            float* o1 = HSIDE ? a.lpH_out[s][1] : a.lpE_out[s][1];
+            o0[p] = cb * t1;
+            o1[p] = cb * t2;
+        }
+    }
+}
+
+// Effective cotangents along `axis` of a VEC row at (i, j, k0) (wrapped with the halo rule;
+// rows in a zero halo hold zeros): lci -= d1, lcj += d2 per cell.
+template <bool HSIDE, int VEC>
+__device__ __forceinline__ void axis_terms(const AdjArgs& a, int axis, int i, int j, int k0, Vec<VEC>& lci,
+                                          Vec<VEC>& lcj, bool out) {
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+        int ii = i, jj = j, kk = k0 + e;
+        if (!wrap_idx(a.g, ii, jj, kk)) continue;
+        float d1, d2;
+        slab_term<HSIDE>(a, axis, ii, jj, kk, lci.v[e], lcj.v[e], out, d1, d2);
+        lci.v[e] -= d1;
+        lcj.v[e] += d2;
+    }
+}
+
 // lc of one component at cell c = (i, j, k) from the raw cotangent l there.
 template <bool HSIDE>
 __device__ __forceinline__ float lc_of(const AdjArgs& a, int comp, int i, int j, int k, long long c, float l) {
@@ -438,45 +498,63 @@ __device__ __forceinline__ Vec<VEC> lc_row(const AdjArgs& a, int comp, int i, in
     return lc_vec<HSIDE, VEC>(a, comp, i, j, k0, c, ldv<VEC>(L + comp * g.N + c));
 }
 
-// Transposed H-step over the core: lam E3 += curl_H(lcH), in place.
-template <int VEC>
+// Transposed H-step: lam E3 += curl_H(lcH), in place.  PML: the differences along each axis
+// use the effective cotangents of that axis' slab (slab_term), so a neighbour needs one
+// slab lookup; the psi cotangents of step t are written at the thread's own cells.
+template <int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_adj_H_core(const __grid_constant__ AdjArgs a) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
     if (!column_of<VEC>(a, j, k0, i0, i1)) return;
     const long long N = g.N;
-    Vec<VEC> ly_m = lc_row<true, VEC>(a, 1, i0 - 1, j, k0);  // lc1, lc2 at (i - 1)
+    Vec<VEC> ly_m = lc_row<true, VEC>(a, 1, i0 - 1, j, k0);  // lc1, lc2 along x at (i - 1)
     Vec<VEC> lz_m = lc_row<true, VEC>(a, 2, i0 - 1, j, k0);
+    if (PML) axis_terms<true, VEC>(a, 0, i0 - 1, j, k0, ly_m, lz_m, false);
     for (int i = i0; i < i1; ++i) {
         const long long c = cell_index(g, i, j, k0);
         Vec<VEC> l[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) l[comp] = lc_vec<true, VEC>(a, comp, i, j, k0, c, ldv<VEC>(a.lH + comp * N + c));
-        const Vec<VEC> l0_jm = lc_row<true, VEC>(a, 0, i, j - 1, k0);
-        const Vec<VEC> l2_jm = lc_row<true, VEC>(a, 2, i, j - 1, k0);
-        const float l0_km = lc_nb<true>(a, 0, i, j, k0 - 1);
-        const float l1_km = lc_nb<true>(a, 1, i, j, k0 - 1);
+        Vec<VEC> l0_jm = lc_row<true, VEC>(a, 0, i, j - 1, k0);
+        Vec<VEC> l2_jm = lc_row<true, VEC>(a, 2, i, j - 1, k0);
+        float l0_km = lc_nb<true>(a, 0, i, j, k0 - 1);
+        float l1_km = lc_nb<true>(a, 1, i, j, k0 - 1);
+        // effective cotangents along x (l1x, l2x), y (l2y, l0y), z (l0z, l1z)
+        Vec<VEC> l1x = l[1], l2x = l[2], l2y = l[2], l0y = l[0], l0z = l[0], l1z = l[1];
+        if (PML) {
+            axis_terms<true, VEC>(a, 0, i, j, k0, l1x, l2x, true);
+            axis_terms<true, VEC>(a, 1, i, j, k0, l2y, l0y, true);
+            axis_terms<true, VEC>(a, 2, i, j, k0, l0z, l1z, true);
+            axis_terms<true, VEC>(a, 1, i, j - 1, k0, l2_jm, l0_jm, false);
+            Vec<1> z0, z1;
+            z0.v[0] = l0_km;
+            z1.v[0] = l1_km;
+            axis_terms<true, 1>(a, 2, i, j, k0 - 1, z0, z1, false);
+            l0_km = z0.v[0];
+            l1_km = z1.v[0];
+        }
         Vec<VEC> lE[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) lE[comp] = ldv_rw<VEC>(a.lE + comp * N + c);
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
-            const float a0 = e == 0 ? l0_km : l[0].v[e - 1];
-            const float a1 = e == 0 ? l1_km : l[1].v[e - 1];
-            lE[0].v[e] += (l[2].v[e] - l2_jm.v[e]) - (l[1].v[e] - a1);
-            lE[1].v[e] += (l[0].v[e] - a0) - (l[2].v[e] - lz_m.v[e]);
-            lE[2].v[e] += (l[1].v[e] - ly_m.v[e]) - (l[0].v[e] - l0_jm.v[e]);
+            const float a0 = e == 0 ? l0_km : l0z.v[e - 1];
+            const float a1 = e == 0 ? l1_km : l1z.v[e - 1];
+            lE[0].v[e] += (l2y.v[e] - l2_jm.v[e]) - (l1z.v[e] - a1);
+            lE[1].v[e] += (l0z.v[e] - a0) - (l2x.v[e] - lz_m.v[e]);
+            lE[2].v[e] += (l1x.v[e] - ly_m.v[e]) - (l0y.v[e] - l0_jm.v[e]);
         }
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) stv<VEC>(a.lE + comp * N + c, lE[comp]);
-        ly_m = l[1];
-        lz_m = l[2];
+        ly_m = l1x;
+        lz_m = l2x;
     }
 }
 
-// Transposed E-step over the core: lam H(t) = (g/e) PMC(lam H3) + curl_E(lcE) (+ detector
-// part), lam E(t) = (f/d) PEC(lam E3), and the inv_eps cotangent.
-template <int VEC>
+// Transposed E-step: lam H(t) = (g/e) PMC(lam H3) + curl_E(lcE) (+ detector part),
+// lam E(t) = (f/d) PEC(lam E3), and the inv_eps cotangent.  PML: effective cotangents per
+// axis as in k_adj_H_core, and curl_H of the gradient with the frozen psi advanced once.
+template <int VEC, bool PML>
 __global__ void __launch_bounds__(256) k_adj_E_core(const __grid_constant__ AdjArgs a) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
@@ -485,6 +563,7 @@ __global__ void __launch_bounds__(256) k_adj_E_core(const __grid_constant__ AdjA
     const long long sy = g.nz;
     const float* __restrict__ H = a.H;
     const bool want_grad = a.grad_ie != nullptr;
+    const int sm = PML ? block_slab_mask(a) : 0;
     Vec<VEC> l[3];  // lcE at (i)
     {
         const long long c = cell_index(g, i0, j, k0);
@@ -501,10 +580,26 @@ __global__ void __launch_bounds__(256) k_adj_E_core(const __grid_constant__ AdjA
         Vec<VEC> ln[3];  // lcE at (i + 1)
 #pragma unroll
         for (int comp = 1; comp < 3; ++comp) ln[comp] = lc_row<false, VEC>(a, comp, i + 1, j, k0);
-        const Vec<VEC> l0_jp = lc_row<false, VEC>(a, 0, i, j + 1, k0);
-        const Vec<VEC> l2_jp = lc_row<false, VEC>(a, 2, i, j + 1, k0);
-        const float l0_kp = lc_nb<false>(a, 0, i, j, k0 + VEC);
-        const float l1_kp = lc_nb<false>(a, 1, i, j, k0 + VEC);
+        Vec<VEC> l0_jp = lc_row<false, VEC>(a, 0, i, j + 1, k0);
+        Vec<VEC> l2_jp = lc_row<false, VEC>(a, 2, i, j + 1, k0);
+        float l0_kp = lc_nb<false>(a, 0, i, j, k0 + VEC);
+        float l1_kp = lc_nb<false>(a, 1, i, j, k0 + VEC);
+        // effective cotangents: along x at (i) and (i+1), along y at (j) and (j+1), along z
+        Vec<VEC> l1x = l[1], l2x = l[2], l2y = l[2], l0y = l[0], l0z = l[0], l1z = l[1];
+        Vec<VEC> n1x = ln[1], n2x = ln[2];
+        if (PML) {
+            axis_terms<false, VEC>(a, 0, i, j, k0, l1x, l2x, true);
+            axis_terms<false, VEC>(a, 1, i, j, k0, l2y, l0y, true);
+            axis_terms<false, VEC>(a, 2, i, j, k0, l0z, l1z, true);
+            axis_terms<false, VEC>(a, 0, i + 1, j, k0, n1x, n2x, false);
+            axis_terms<false, VEC>(a, 1, i, j + 1, k0, l2_jp, l0_jp, false);
+            Vec<1> z0, z1;
+            z0.v[0] = l0_kp;
+            z1.v[0] = l1_kp;
+            axis_terms<false, 1>(a, 2, i, j, k0 + VEC, z0, z1, false);
+            l0_kp = z0.v[0];
+            l1_kp = z1.v[0];
+        }
         Vec<VEC> le[3], lh[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) {
@@ -525,12 +620,12 @@ __global__ void __launch_bounds__(256) k_adj_E_core(const __grid_constant__ AdjA
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
             const int k = k0 + e;
-            const float b0 = e + 1 < VEC ? l[0].v[(e + 1) % VEC] : l0_kp;
-            const float b1 = e + 1 < VEC ? l[1].v[(e + 1) % VEC] : l1_kp;
+            const float b0 = e + 1 < VEC ? l0z.v[(e + 1) % VEC] : l0_kp;
+            const float b1 = e + 1 < VEC ? l1z.v[(e + 1) % VEC] : l1_kp;
             float lht[3];
-            lht[0] = (l2_jp.v[e] - l[2].v[e]) - (b1 - l[1].v[e]);
-            lht[1] = (b0 - l[0].v[e]) - (ln[2].v[e] - l[2].v[e]);
-            lht[2] = (ln[1].v[e] - l[1].v[e]) - (l0_jp.v[e] - l[0].v[e]);
+            lht[0] = (l2_jp.v[e] - l2y.v[e]) - (b1 - l1z.v[e]);
+            lht[1] = (b0 - l0z.v[e]) - (n2x.v[e] - l2x.v[e]);
+            lht[2] = (n1x.v[e] - l1x.v[e]) - (l0_jp.v[e] - l0y.v[e]);
             long long q = 0;
             const bool in_hp = a.hp.buf && box_local(a.hp, i, j, k, q);
 #pragma unroll
@@ -554,9 +649,12 @@ __global__ void __launch_bounds__(256) k_adj_E_core(const __grid_constant__ AdjA
             if (want_grad) {
                 const float hy_km = e == 0 ? Hy_k : Hy.v[e - 1];
                 const float hx_km = e == 0 ? Hx_k : Hx.v[e - 1];
-                cu[0] = (Hz.v[e] - Hz_jm.v[e]) - (Hy.v[e] - hy_km);
-                cu[1] = (Hx.v[e] - hx_km) - (Hz.v[e] - Hz_m.v[e]);
-                cu[2] = (Hy.v[e] - Hy_m.v[e]) - (Hx.v[e] - Hx_jm.v[e]);
+                const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
+                                    Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
+                cu[0] = d[0] - d[1];
+                cu[1] = d[2] - d[3];
+                cu[2] = d[4] - d[5];
+                if (PML) curl_H_cpml(a, i, j, k, d, cu, sm);
             }
             float gs = 0.f;
 #pragma unroll
@@ -746,6 +844,215 @@ __global__ void __launch_bounds__(256, 3) k_adj_E_core_s(const __grid_constant__
         for (int comp = 0; comp < 3; ++comp) stv<VEC>(lEo + comp * N, le[comp]);
         if (gr) {
             if (iso) stv<VEC>(gr, gv[0]);
+            else {
+#pragma unroll
+                for (int comp = 0; comp < 3; ++comp) stv<VEC>(gr + comp * N, gv[comp]);
+            }
+            gr += sx;
+            Hy_m = Hy;
+            Hz_m = Hz;
+        }
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            le[comp] = len[comp];
+            lc[comp] = lcn[comp];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Fast forms of the CPML-shell kernels (same conditions as the fast core, except that the
+// boxes touch the grid faces: neighbours outside the grid read as the zero halo, the
+// reference's CPML boundary; no periodic axis).  The slab terms are the per-axis ones of
+// k_adj_H_core / k_adj_E_core.
+// ---------------------------------------------------------------------------------
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> vscale(const Vec<VEC>& x, float s) {
+    Vec<VEC> r;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r.v[e] = x.v[e] * s;
+    return r;
+}
+
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> vzero() {
+    Vec<VEC> r;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r.v[e] = 0.f;
+    return r;
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(256) k_adj_H_shell_s(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    const long long N = g.N;
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const float s = -g.c * a.im_scalar;
+    const bool jm = j > 0, km = k0 > 0;
+    const float* __restrict__ lH = a.lH + cell_index(g, i0, j, k0);
+    float* lE = a.lE + cell_index(g, i0, j, k0);
+    // lc1, lc2 along x at (i - 1)
+    Vec<VEC> y_m = vzero<VEC>(), z_m = vzero<VEC>();
+    if (i0 > 0) {
+        y_m = vscale<VEC>(ldv<VEC>(lH + N - sx), s);
+        z_m = vscale<VEC>(ldv<VEC>(lH + 2 * N - sx), s);
+        axis_terms<true, VEC>(a, 0, i0 - 1, j, k0, y_m, z_m, false);
+    }
+    for (int i = i0; i < i1; ++i, lH += sx, lE += sx) {
+        const Vec<VEC> x = vscale<VEC>(ldv<VEC>(lH), s), y = vscale<VEC>(ldv<VEC>(lH + N), s);
+        const Vec<VEC> z = vscale<VEC>(ldv<VEC>(lH + 2 * N), s);
+        Vec<VEC> x_jm = vzero<VEC>(), z_jm = vzero<VEC>();
+        if (jm) {
+            x_jm = vscale<VEC>(ldv<VEC>(lH - sy), s);
+            z_jm = vscale<VEC>(ldv<VEC>(lH + 2 * N - sy), s);
+        }
+        Vec<1> x_km, y_km;
+        x_km.v[0] = km ? s * __ldg(lH - 1) : 0.f;
+        y_km.v[0] = km ? s * __ldg(lH + N - 1) : 0.f;
+        Vec<VEC> l1x = y, l2x = z, l2y = z, l0y = x, l0z = x, l1z = y;
+        axis_terms<true, VEC>(a, 0, i, j, k0, l1x, l2x, true);
+        axis_terms<true, VEC>(a, 1, i, j, k0, l2y, l0y, true);
+        axis_terms<true, VEC>(a, 2, i, j, k0, l0z, l1z, true);
+        if (jm) axis_terms<true, VEC>(a, 1, i, j - 1, k0, z_jm, x_jm, false);
+        if (km) axis_terms<true, 1>(a, 2, i, j, k0 - 1, x_km, y_km, false);
+        Vec<VEC> e0 = ldv_rw<VEC>(lE), e1 = ldv_rw<VEC>(lE + N), e2 = ldv_rw<VEC>(lE + 2 * N);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const float a0 = e == 0 ? x_km.v[0] : l0z.v[e - 1];
+            const float a1 = e == 0 ? y_km.v[0] : l1z.v[e - 1];
+            e0.v[e] += (l2y.v[e] - z_jm.v[e]) - (l1z.v[e] - a1);
+            e1.v[e] += (l0z.v[e] - a0) - (l2x.v[e] - z_m.v[e]);
+            e2.v[e] += (l1x.v[e] - y_m.v[e]) - (l0y.v[e] - x_jm.v[e]);
+        }
+        stv<VEC>(lE, e0);
+        stv<VEC>(lE + N, e1);
+        stv<VEC>(lE + 2 * N, e2);
+        y_m = l1x;
+        z_m = l2x;
+    }
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(256) k_adj_E_shell_s(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    int j, k0, i0, i1;
+    if (!column_of<VEC>(a, j, k0, i0, i1)) return;
+    const long long N = g.N;
+    const long long sy = g.nz, sx = (long long)g.ny * g.nz;
+    const long long c0 = cell_index(g, i0, j, k0);
+    const long long mN = a.n_eps == 3 ? N : 0;
+    const float cc = g.c;
+    const bool jm = j > 0, jp = j + 1 < g.ny, km = k0 > 0, kp = k0 + VEC < g.nz;
+    const int sm = block_slab_mask(a);
+    const float* __restrict__ lE = a.lE + c0;
+    const float* __restrict__ lH = a.lH + c0;
+    const float* __restrict__ ie = a.ie + c0;
+    const float* __restrict__ H = a.H + c0;
+    float* lEo = a.lE_out + c0;
+    float* lHo = a.lH_out + c0;
+    float* gr = a.grad_ie ? a.grad_ie + c0 : nullptr;
+    // lam E3 and lcE = c ie lam E3 at (i)
+    Vec<VEC> le[3], lc[3];
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+        le[comp] = ldv<VEC>(lE + comp * N);
+        lc[comp] = vscale<VEC>(vmul<VEC>(le[comp], ldv<VEC>(ie + comp * mN)), cc);
+    }
+    Vec<VEC> Hy_m = vzero<VEC>(), Hz_m = vzero<VEC>();
+    if (gr && i0 > 0) {
+        Hy_m = ldv<VEC>(H + N - sx);
+        Hz_m = ldv<VEC>(H + 2 * N - sx);
+    }
+    for (int i = i0; i < i1; ++i, lE += sx, lH += sx, ie += sx, H += sx, lEo += sx, lHo += sx) {
+        const bool ip = i + 1 < g.nx;
+        Vec<VEC> len[3], lcn[3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            len[comp] = ip ? ldv<VEC>(lE + sx + comp * N) : vzero<VEC>();
+            lcn[comp] = ip ? vscale<VEC>(vmul<VEC>(len[comp], ldv<VEC>(ie + sx + comp * mN)), cc) : vzero<VEC>();
+        }
+        Vec<VEC> x_jp = vzero<VEC>(), z_jp = vzero<VEC>();
+        if (jp) {
+            x_jp = vscale<VEC>(vmul<VEC>(ldv<VEC>(lE + sy), ldv<VEC>(ie + sy)), cc);
+            z_jp = vscale<VEC>(vmul<VEC>(ldv<VEC>(lE + 2 * N + sy), ldv<VEC>(ie + 2 * mN + sy)), cc);
+        }
+        Vec<1> x_kp, y_kp;
+        x_kp.v[0] = kp ? cc * __ldg(lE + VEC) * __ldg(ie + VEC) : 0.f;
+        y_kp.v[0] = kp ? cc * __ldg(lE + N + VEC) * __ldg(ie + mN + VEC) : 0.f;
+        // effective cotangents per axis (centre: psi cotangents of step t written)
+        Vec<VEC> l1x = lc[1], l2x = lc[2], l2y = lc[2], l0y = lc[0], l0z = lc[0], l1z = lc[1];
+        Vec<VEC> n1x = lcn[1], n2x = lcn[2];
+        axis_terms<false, VEC>(a, 0, i, j, k0, l1x, l2x, true);
+        axis_terms<false, VEC>(a, 1, i, j, k0, l2y, l0y, true);
+        axis_terms<false, VEC>(a, 2, i, j, k0, l0z, l1z, true);
+        if (ip) axis_terms<false, VEC>(a, 0, i + 1, j, k0, n1x, n2x, false);
+        if (jp) axis_terms<false, VEC>(a, 1, i, j + 1, k0, z_jp, x_jp, false);
+        if (kp) axis_terms<false, 1>(a, 2, i, j, k0 + VEC, x_kp, y_kp, false);
+        const Vec<VEC> h0 = ldv<VEC>(lH), h1 = ldv<VEC>(lH + N), h2 = ldv<VEC>(lH + 2 * N);
+        Vec<VEC> Hx, Hy, Hz, Hz_jm = vzero<VEC>(), Hx_jm = vzero<VEC>();
+        float Hy_k = 0.f, Hx_k = 0.f;
+        Vec<VEC> gv[3];
+        if (gr) {
+            Hx = ldv<VEC>(H); Hy = ldv<VEC>(H + N); Hz = ldv<VEC>(H + 2 * N);
+            if (jm) {
+                Hz_jm = ldv<VEC>(H + 2 * N - sy);
+                Hx_jm = ldv<VEC>(H - sy);
+            }
+            if (km) {
+                Hy_k = __ldg(H + N - 1);
+                Hx_k = __ldg(H - 1);
+            }
+            if (!mN) gv[0] = ldv_rw<VEC>(gr);
+            else {
+#pragma unroll
+                for (int comp = 0; comp < 3; ++comp) gv[comp] = ldv_rw<VEC>(gr + comp * N);
+            }
+        }
+        Vec<VEC> o0, o1, o2;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+            const int k = k0 + e;
+            const float b0 = e + 1 < VEC ? l0z.v[(e + 1) % VEC] : x_kp.v[0];
+            const float b1 = e + 1 < VEC ? l1z.v[(e + 1) % VEC] : y_kp.v[0];
+            o0.v[e] = h0.v[e] + ((z_jp.v[e] - l2y.v[e]) - (b1 - l1z.v[e]));
+            o1.v[e] = h1.v[e] + ((b0 - l0z.v[e]) - (n2x.v[e] - l2x.v[e]));
+            o2.v[e] = h2.v[e] + ((n1x.v[e] - l1x.v[e]) - (x_jp.v[e] - l0y.v[e]));
+            if (gr) {
+                const float hy_km = e == 0 ? Hy_k : Hy.v[e - 1];
+                const float hx_km = e == 0 ? Hx_k : Hx.v[e - 1];
+                const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
+                                    Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
+                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+                curl_H_cpml(a, i, j, k, d, cu, sm);
+                if (!mN) {
+                    gv[0].v[e] += cc * (le[0].v[e] * cu[0] + le[1].v[e] * cu[1] + le[2].v[e] * cu[2]);
+                } else {
+                    gv[0].v[e] += cc * le[0].v[e] * cu[0];
+                    gv[1].v[e] += cc * le[1].v[e] * cu[1];
+                    gv[2].v[e] += cc * le[2].v[e] * cu[2];
+                }
+            }
+        }
+        if (a.hp.buf) {  // detector part of lam H(t)
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                long long q;
+                if (!box_local(a.hp, i, j, k0 + e, q)) continue;
+                float* hp = a.hp.buf + q;
+                o0.v[e] += hp[0]; hp[0] = 0.f;
+                o1.v[e] += hp[a.hp.M]; hp[a.hp.M] = 0.f;
+                o2.v[e] += hp[2 * a.hp.M]; hp[2 * a.hp.M] = 0.f;
+            }
+        }
+        stv<VEC>(lHo, o0);
+        stv<VEC>(lHo + N, o1);
+        stv<VEC>(lHo + 2 * N, o2);
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) stv<VEC>(lEo + comp * N, le[comp]);
+        if (gr) {
+            if (!mN) stv<VEC>(gr, gv[0]);
             else {
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) stv<VEC>(gr + comp * N, gv[comp]);

@@ -128,7 +128,21 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
     a.lH_out = nxt.H;
     a.grad_ie = adj->grad_inv_eps;
     a.hp = p->hp;
+    for (int x = 0; x < 3; ++x) a.ax_slab[x][0] = a.ax_slab[x][1] = -1;
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        const int side = p->d.slabs[s].direction > 0 ? 1 : 0;
+        int& slot = a.ax_slab[p->slab[s].axis][side];
+        slot = slot < 0 ? s : -2;  // -2: two slabs on one face (the per-axis kernels do not apply)
+    }
     return a;
+}
+
+// Whether every face holds at most one slab (the per-axis shell kernels apply).
+bool axis_table_ok(const AdjArgs& a) {
+    for (int x = 0; x < 3; ++x)
+        for (int side = 0; side < 2; ++side)
+            if (a.ax_slab[x][side] == -2) return false;
+    return true;
 }
 
 int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
@@ -139,17 +153,23 @@ int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
     return FDTD_OK;
 }
 
-enum class AdjKind { Shell, Core, CoreFast };
+enum class AdjKind { Shell, ShellGeneric, ShellFast, Core, CoreFast };
 
 template <bool HSIDE, int VEC>
 void launch_adj_kernel(const AdjArgs& a, long long blocks, AdjKind kind, cudaStream_t st) {
     const unsigned nb = (unsigned)blocks;
-    if (kind == AdjKind::Shell) {
+    if (kind == AdjKind::ShellGeneric) {
         if (HSIDE) k_adj_H<VEC, true><<<nb, kUpdBlock, 0, st>>>(a);
         else k_adj_E<VEC, true><<<nb, kUpdBlock, 0, st>>>(a);
+    } else if (kind == AdjKind::ShellFast) {
+        if (HSIDE) k_adj_H_shell_s<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+        else k_adj_E_shell_s<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+    } else if (kind == AdjKind::Shell) {
+        if (HSIDE) k_adj_H_core<VEC, true><<<nb, kUpdBlock, 0, st>>>(a);
+        else k_adj_E_core<VEC, true><<<nb, kUpdBlock, 0, st>>>(a);
     } else if (kind == AdjKind::Core) {
-        if (HSIDE) k_adj_H_core<VEC><<<nb, kUpdBlock, 0, st>>>(a);
-        else k_adj_E_core<VEC><<<nb, kUpdBlock, 0, st>>>(a);
+        if (HSIDE) k_adj_H_core<VEC, false><<<nb, kUpdBlock, 0, st>>>(a);
+        else k_adj_E_core<VEC, false><<<nb, kUpdBlock, 0, st>>>(a);
     } else {
         if (HSIDE) k_adj_H_core_s<VEC><<<nb, kUpdBlock, 0, st>>>(a);
         else k_adj_E_core_s<VEC><<<nb, kUpdBlock, 0, st>>>(a);
@@ -182,16 +202,21 @@ bool adj_fast_core(const FdtdPlan* p, const AdjArgs& a, const Box& core, bool hs
 template <bool HSIDE>
 void launch_adj(const FdtdPlan* p, const AdjArgs& a, cudaStream_t st) {
     const Split sp = split_boxes(p, 1);
+    AdjKind shell = axis_table_ok(a) ? AdjKind::Shell : AdjKind::ShellGeneric;
+    // fast shell: zero halo (no periodic axis), no conductivity, no PEC/PMC, scalar inv_mu (H)
+    if (shell == AdjKind::Shell && !p->g.px && !p->g.py && !p->g.pz && !p->g.pec && !p->g.pmc && !a.sigE &&
+        !a.sigH && (!HSIDE || a.im == nullptr))
+        shell = AdjKind::ShellFast;
     if (!sp.split) {
         const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
-        launch_adj_boxes<HSIDE>(p, a, &all, &p->chunk, 1, AdjKind::Shell, st);
+        launch_adj_boxes<HSIDE>(p, a, &all, &p->chunk, 1, shell, st);
         return;
     }
     const AdjKind ck = adj_fast_core(p, a, sp.core, HSIDE) ? AdjKind::CoreFast : AdjKind::Core;
     launch_adj_boxes<HSIDE>(p, a, &sp.core, &p->chunk, 1, ck, st);
     int chunks[6];
     for (int q = 0; q < sp.n_shell; ++q) chunks[q] = kShellChunk;
-    launch_adj_boxes<HSIDE>(p, a, sp.shell, chunks, sp.n_shell, AdjKind::Shell, st);
+    launch_adj_boxes<HSIDE>(p, a, sp.shell, chunks, sp.n_shell, shell, st);
 }
 
 // One step of the backward loop at t = *d_t: snapshot, reconstruction, transposed step.
