@@ -179,10 +179,13 @@ void launch_adj_kernel(const AdjArgs& a, long long blocks, AdjKind kind, cudaStr
 template <bool HSIDE>
 void launch_adj_boxes(const FdtdPlan* p, AdjArgs a, const Box* boxes, const int* chunks, int n, AdjKind kind,
                       cudaStream_t st) {
-    const long long blocks = fill_boxes(p, a, boxes, chunks, n);
+    // CPML shells run one z cell per thread (more warps for their latency-bound slab loads)
+    const bool shell = kind == AdjKind::Shell || kind == AdjKind::ShellFast || kind == AdjKind::ShellGeneric;
+    const int vec = shell ? 1 : p->vec;
+    const long long blocks = fill_boxes(p, a, boxes, chunks, n, vec);
     if (blocks <= 0) return;
-    if (p->vec == 4) launch_adj_kernel<HSIDE, 4>(a, blocks, kind, st);
-    else if (p->vec == 2) launch_adj_kernel<HSIDE, 2>(a, blocks, kind, st);
+    if (vec == 4) launch_adj_kernel<HSIDE, 4>(a, blocks, kind, st);
+    else if (vec == 2) launch_adj_kernel<HSIDE, 2>(a, blocks, kind, st);
     else launch_adj_kernel<HSIDE, 1>(a, blocks, kind, st);
 }
 
