@@ -163,6 +163,8 @@ SIGNATURES = {
     "fdtd_batch_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "fdtd_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "fdtd_batch_launches_per_step": (C.c_int32, [C.c_void_p]),
+    "fdtd_batch_set_mode": (C.c_int, [C.c_void_p, C.c_int32]),
+    "fdtd_batch_mode": (C.c_int32, [C.c_void_p]),
     "fdtd_detector_sample_noalloc": (
         C.c_int,
         [C.POINTER(DetectorDesc), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_void_p, C.c_void_p,

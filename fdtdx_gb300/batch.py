@@ -89,11 +89,19 @@ class SimulationBatch:
     def tuning(self) -> dict:
         out = (C.c_int32 * 4)()
         self._check(N.load().fdtd_batch_tuning(self._h, out), "fdtd_batch_tuning")
-        return {"chunk_scale": (out[0], out[1]), "shell_chunk": out[2], "blocks_per_sm": out[3]}
+        return {"chunk_scale": (out[0], out[1]), "shell_chunk": out[2], "blocks_per_sm": out[3], "mode": self.mode}
 
     def tune(self, chunk_num: int = 1, chunk_den: int = 1, shell_chunk: int = 4, blocks_per_sm: int = 8) -> None:
         rc = N.load().fdtd_batch_tune(self._h, chunk_num, chunk_den, shell_chunk, blocks_per_sm)
         self._check(rc, "fdtd_batch_tune")
+
+    @property
+    def mode(self) -> str:
+        return {0: "persistent", 1: "branches"}[int(N.load().fdtd_batch_mode(self._h))]
+
+    def set_mode(self, mode: str) -> None:
+        rc = N.load().fdtd_batch_set_mode(self._h, {"persistent": 0, "branches": 1}[mode])
+        self._check(rc, "fdtd_batch_set_mode")
 
     def launches_per_step(self) -> int:
         return int(N.load().fdtd_batch_launches_per_step(self._h))

@@ -50,6 +50,12 @@ struct FdtdBatch {
     cudaGraph_t graph = nullptr;
     int gsteps = 0;
     cudaStream_t cap_stream = nullptr;
+    // mode 1 ("branches"): each simulation's own launch chain (TMA cores) on its own stream,
+    // forked from and joined to the caller's stream -- parallel branches of one graph
+    int mode = 0;
+    std::vector<cudaStream_t> sim_streams;
+    std::vector<cudaEvent_t> join_ev;
+    cudaEvent_t fork_ev = nullptr;
     std::string err;
 };
 
@@ -209,8 +215,46 @@ void batch_step(const FdtdBatch* b, int parity, cudaStream_t st) {
     k_batch_advance<<<(b->n + 127) / 128, 128, 0, st>>>(b->tps, b->n);
 }
 
+// The branch mode's streams and events (created on first use).
+bool batch_branch_streams(FdtdBatch* b) {
+    if (b->fork_ev) return true;
+    if (cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess) return false;
+    b->sim_streams.assign(b->n, nullptr);
+    b->join_ev.assign(b->n, nullptr);
+    for (int s = 0; s < b->n; ++s)
+        if (cudaStreamCreateWithFlags(&b->sim_streams[s], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join_ev[s], cudaEventDisableTiming) != cudaSuccess)
+            return false;
+    return true;
+}
+
+// `steps` steps of every simulation on its own stream (its per-plan launches, TMA cores
+// included), forked from and joined back to `st`.
+void batch_run_branches(const FdtdBatch* b, int parity, int steps, cudaStream_t st) {
+    cudaEventRecord(b->fork_ev, st);
+    for (int s = 0; s < b->n; ++s) {
+        const FdtdPlan* p = b->plans[s];
+        const FdtdBuffers* bb = &b->bufs[s];
+        cudaStream_t ss = b->sim_streams[s];
+        cudaStreamWaitEvent(ss, b->fork_ev, 0);
+        int par = parity;
+        for (int k = 0; k < steps; ++k) {
+            float* hc = p->need_hprev && par ? p->h_twin : bb->H;
+            float* hn = p->need_hprev ? (par ? bb->H : p->h_twin) : bb->H;
+            launch_forward_step(p, bb, hc, hn, ss);
+            if (b->any_hprev) par ^= 1;
+        }
+        cudaEventRecord(b->join_ev[s], ss);
+        cudaStreamWaitEvent(st, b->join_ev[s], 0);
+    }
+}
+
 // Runs `steps` steps from `parity` with direct launches; returns the parity after them.
 int batch_run_direct(const FdtdBatch* b, int parity, int steps, cudaStream_t st) {
+    if (b->mode == 1) {
+        batch_run_branches(b, parity, steps, st);
+        return b->any_hprev ? parity ^ (steps & 1) : parity;
+    }
     for (int s = 0; s < steps; ++s) {
         batch_step(b, parity, st);
         if (b->any_hprev) parity ^= 1;
@@ -402,6 +446,11 @@ void fdtd_batch_destroy(FdtdBatch* b) {
     if (!b) return;
     batch_drop_graph(b);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    for (cudaStream_t x : b->sim_streams)
+        if (x) cudaStreamDestroy(x);
+    for (cudaEvent_t x : b->join_ev)
+        if (x) cudaEventDestroy(x);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     cudaFree(b->dmem);
     delete b;
 }
@@ -427,8 +476,24 @@ int fdtd_batch_tuning(const FdtdBatch* b, int32_t* out4) {
     return FDTD_OK;
 }
 
+int fdtd_batch_set_mode(FdtdBatch* b, int32_t mode) {
+    if (!b || (mode != 0 && mode != 1)) return bfail(b, FDTD_EINVAL, "mode must be 0 (persistent) or 1 (branches)");
+    if (mode == 1 && !batch_branch_streams(b)) return bfail(b, FDTD_ECUDA, "branch streams could not be created");
+    cudaDeviceSynchronize();
+    b->mode = mode;
+    batch_drop_graph(b);
+    return FDTD_OK;
+}
+
+int32_t fdtd_batch_mode(const FdtdBatch* b) { return b ? b->mode : -1; }
+
 int32_t fdtd_batch_launches_per_step(const FdtdBatch* b) {
     if (!b) return 0;
+    if (b->mode == 1) {
+        int n = 0;
+        for (const FdtdPlan* p : b->plans) n += fdtd_launches_per_step(p);
+        return n;
+    }
     int classes = 0;
     for (int cls = 0; cls < 4; ++cls) classes += b->class_start[cls + 1] > b->class_start[cls];
     int ifc = 0;
@@ -480,10 +545,25 @@ int batch_autotune(FdtdBatch* b, int budget, int* parity, cudaStream_t st) {
         const float ms = trial(best[0], best[1], best[2], bps);
         if (ms > 0.f && ms < best_ms) { best_ms = ms; best[3] = bps; }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     b->chunk_scale_num = best[0]; b->chunk_scale_den = best[1]; b->shell_chunk = best[2]; b->blocks_per_sm = best[3];
     batch_build_updates(b);
+    // the branch mode (each simulation's own kernels, overlapped across simulations)
+    const int warm = b->any_hprev ? 2 : 1;
+    if (used + warm + per <= budget && batch_branch_streams(b)) {
+        b->mode = 1;
+        *parity = batch_run_direct(b, *parity, warm, st);
+        cudaEventRecord(e0, st);
+        *parity = batch_run_direct(b, *parity, per, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        used += warm + per;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (!(ms > 0.f && (best_ms < 0.f || ms < best_ms))) b->mode = 0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    batch_drop_graph(b);
     b->tuned = true;
     return used;
 }

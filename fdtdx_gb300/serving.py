@@ -228,7 +228,8 @@ class Server:
         self._members = key
         b = SimulationBatch([(j.state, j.objects, j.config) for j in jobs], scenes=[j.scene for j in jobs], reset=False)
         if self._tile is not None:
-            b.tune(*self._tile)
+            b.tune(*self._tile[:4])
+            b.set_mode(self._tile[4])
         self._batch = b
         return b, True
 
@@ -341,7 +342,7 @@ class Server:
                         self.adj_rate = 0.7 * self.adj_rate + 0.3 * r
             if fw and self._tile is None and self.autotune:
                 t = self._batch.tuning()
-                self._tile = (t["chunk_scale"][0], t["chunk_scale"][1], t["shell_chunk"], t["blocks_per_sm"])
+                self._tile = (t["chunk_scale"][0], t["chunk_scale"][1], t["shell_chunk"], t["blocks_per_sm"], t["mode"])
             if not realtime:
                 vnow += max([e0.elapsed_time(e1) * 1e-3 for _k, e0, e1, _w in ev] + [0.0])
             now = clock() if realtime else vnow

@@ -252,6 +252,12 @@ int fdtd_batch_forward(FdtdBatch* batch, const int32_t* t0, int32_t n_steps, int
  * (out4 = {num, den, shell_chunk, blocks_per_sm}). */
 int fdtd_batch_tune(FdtdBatch* batch, int32_t chunk_num, int32_t chunk_den, int32_t shell_chunk, int32_t blocks_per_sm);
 int fdtd_batch_tuning(const FdtdBatch* batch, int32_t* out4);
+/* Execution mode: 0 = persistent launches over the unit lists (default), 1 = each
+ * simulation's own per-plan launch chain on its own stream, forked from and joined to the
+ * caller's stream (parallel branches of one CUDA graph).  The autotuner (fdtd_batch_forward
+ * flag bit 1) times both and keeps the faster. */
+int fdtd_batch_set_mode(FdtdBatch* batch, int32_t mode);
+int32_t fdtd_batch_mode(const FdtdBatch* batch);
 /* Launches of this library's kernels one batch step issues (for the whole batch). */
 int32_t fdtd_batch_launches_per_step(const FdtdBatch* batch);
 

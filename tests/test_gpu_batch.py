@@ -89,7 +89,25 @@ def test_batch_matches_single_runs(graph, autotune):
     if autotune:
         t = batch.tuning()
         assert t["shell_chunk"] in (2, 4, 8) and t["blocks_per_sm"] in (4, 8, 16)
-    assert batch.launches_per_step() <= 13
+        assert t["mode"] in ("persistent", "branches")
+    else:
+        assert batch.launches_per_step() <= 13
+    batch.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_branch_mode_matches_single_runs(graph):
+    """Mode 'branches': every simulation's own launch chain on its own stream; bitwise equal
+    to the single runs (the same kernels, TMA cores included)."""
+    sims = _sims()
+    batch = SimulationBatch(sims)
+    batch.set_mode("branches")
+    batch.advance(STEPS, t0=[0] * len(sims), graph=graph, autotune=False)
+    torch.cuda.synchronize()
+    for q, (arrays, objects, config) in enumerate(sims):
+        ref = _alone(arrays, objects, config, STEPS)
+        for k, v in _states(batch.arrays[q]).items():
+            assert torch.equal(v, _states(ref)[k]), (q, k)
     batch.close()
 
 
