@@ -6,7 +6,14 @@ The public names mirror ``fdtdx`` (``run_fdtd``, ``reversible_fdtd``,
 ``libfdtd_gb300.so`` (C ABI in ``include/fdtd_gb300.h``); there is no CPU path.
 """
 
-from fdtdx_gb300.config import DtypeConversion, GradientConfig, Recorder, SimulationConfig, UniformGrid
+from fdtdx_gb300.config import (
+    DtypeConversion,
+    GradientConfig,
+    LinearReconstructEveryK,
+    Recorder,
+    SimulationConfig,
+    UniformGrid,
+)
 from fdtdx_gb300.constants import wavelength_to_period
 from fdtdx_gb300.container import ArrayContainer, FieldState, ObjectContainer, ParameterContainer, RecordingState
 from fdtdx_gb300.core import (
@@ -50,6 +57,7 @@ __all__ = [
     "BoundaryConfig",
     "Device",
     "DtypeConversion",
+    "LinearReconstructEveryK",
     "EnergyDetector",
     "FieldDetector",
     "FieldState",

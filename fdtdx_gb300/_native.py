@@ -101,6 +101,11 @@ class Desc(C.Structure):
         ("detectors", DetectorDesc * MAX_DETECTORS),
         ("record_interfaces", C.c_int32),
         ("recording_dtype", C.c_int32),
+        ("rec_slots", C.c_int32),
+        ("rec_store", C.c_void_p),
+        ("rec_a", C.c_void_p),
+        ("rec_b", C.c_void_p),
+        ("rec_w", C.c_void_p),
     ]
 
 

@@ -38,25 +38,100 @@ class DtypeConversion:
         self.exclude_filter = tuple(exclude_filter)
 
 
+class LinearReconstructEveryK:
+    """Interface-recorder time filter: store every k-th step, interpolate linearly between.
+
+    fdtdx/interfaces/time_filter.py:140-257.  The stored steps are ``start_recording_after``,
+    then every ``k`` steps, plus the last step T-1.  A stored step reads its own slot; any
+    other step t reads ``prev + f * (next - prev)`` between the slot a at or before t and
+    slot a + 1, with f = (t - t_a) / (t_{a+1} - t_a) and t_a the first step mapped to slot a.
+    """
+
+    def __init__(self, k: int, start_recording_after: int = 0):
+        if k < 1:
+            raise ValueError("k must be >= 1")
+        self.k = int(k)
+        self.start_recording_after = int(start_recording_after)
+
+    def save_steps(self, T: int) -> list[int]:
+        steps = list(range(self.start_recording_after, T, self.k))
+        if not steps or steps[-1] != T - 1:
+            steps.append(T - 1)
+        return steps
+
+    def time_to_slot(self, T: int) -> list[int]:
+        """Slot of the last stored step at or before t (time_filter.py:180-191)."""
+        idx = [0] * T
+        for a, t in enumerate(self.save_steps(T)):
+            idx[t] = a
+        for _ in range(self.k - 1):  # each pass copies a slot one step to the right
+            rolled = [idx[-1]] + idx[:-1]
+            idx = [r if v == 0 else v for v, r in zip(idx, rolled)]
+            for t in range(min(self.k, T)):
+                idx[t] = 0
+        return idx
+
+    def tables(self, T: int) -> tuple[list[int], list[int], list[int], list[float]]:
+        """Per step t = -1 .. T (entry t + 1): store slot (-1: not stored), and the restore
+        slots a, b and weight w of ``v = v_a + w (v_b - v_a)``."""
+        S = self.save_steps(T)
+        Sset = set(S)
+        m = self.time_to_slot(T)
+        first = {}
+        for t, a in enumerate(m):
+            first.setdefault(a, t)
+        A = len(S)
+        store, sa, sb, w = [], [], [], []
+        for t in range(-1, T + 1):
+            tj = min(max(t + T if t < 0 else t, 0), T - 1)  # a JAX gather: -1 wraps, T clamps
+            store.append(m[tj] if t in Sset else -1)
+            a = m[tj]
+            if tj in Sset:
+                sa.append(a), sb.append(a), w.append(0.0)
+                continue
+            b = min(a + 1, A - 1)
+            t_prev = first.get(a, 0)
+            t_next = first.get(a + 1, 0)  # no step maps to a + 1: the first index (argmax of no match)
+            f = (t - t_prev) / (t_next - t_prev) if t_next != t_prev else 0.0
+            sa.append(a), sb.append(b), w.append(f)
+        return store, sa, sb, w
+
+
 class Recorder:
     """Records the PML-interface planes of E and H after every forward step.
 
     fdtdx/interfaces/recorder.py:14-199.  The identity recorder (no modules) keeps
-    float32 planes; a ``DtypeConversion`` module narrows the storage.
+    float32 planes; a ``DtypeConversion`` module narrows the storage; a
+    ``LinearReconstructEveryK`` time filter stores every k-th step only.
     """
 
     def __init__(self, modules: Sequence[object] = ()):
         self.modules = list(modules)
         for m in self.modules:
-            if not isinstance(m, DtypeConversion):
+            if not isinstance(m, (DtypeConversion, LinearReconstructEveryK)):
                 raise NotImplementedError(f"recorder module {type(m).__name__} is not supported")
+        if sum(isinstance(m, LinearReconstructEveryK) for m in self.modules) > 1:
+            raise NotImplementedError("at most one time filter per recorder")
 
     @property
     def storage_dtype(self) -> torch.dtype:
         dt = torch.float32
         for m in self.modules:
-            dt = m.dtype
+            if isinstance(m, DtypeConversion):
+                dt = m.dtype
         return dt
+
+    @property
+    def time_filter(self) -> LinearReconstructEveryK | None:
+        for m in self.modules:
+            if isinstance(m, LinearReconstructEveryK):
+                return m
+        return None
+
+    def slots(self, T: int) -> int:
+        """Recording rows for a run of T steps."""
+        tf = self.time_filter
+        return T if tf is None else len(tf.save_steps(T))
 
 
 @dataclass

@@ -364,7 +364,7 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
         htp.push_back(p->d_t);
         if (p->d.record_interfaces && p->d.n_slabs) {
             BIface x{};
-            x.g = p->g; x.ifc = p->ifc; x.tp = p->d_t; x.n_slots = p->d.n_steps_total;
+            x.g = p->g; x.ifc = p->ifc; x.tp = p->d_t; x.n_slots = rec_rows(p->d);
             x.E = bb.E; x.H[0] = hn[0]; x.H[1] = hn[1]; x.rec = bb.recording;
             const int dt = p->d.recording_dtype >= 0 && p->d.recording_dtype <= 2 ? p->d.recording_dtype : 0;
             for (long long k = 0; k < (p->ifc.total + 255) / 256; ++k) hifu[dt].push_back(make_int2((int)hif.size(), (int)k));

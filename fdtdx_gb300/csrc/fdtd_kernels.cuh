@@ -799,6 +799,11 @@ struct IfaceDev {
     int layer[FDTD_MAX_SLABS];
     long long start[FDTD_MAX_SLABS + 1];  // prefix sums of plane sizes
     long long total;                     // sum of plane sizes
+    // recorder time filter (nullptr: one slot per step): store slot, restore slots a, b, weight
+    const int* store;
+    const int* ra;
+    const int* rb;
+    const float* rw;
 };
 
 template <typename T, bool RESTORE>
@@ -806,9 +811,23 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
                                                 int n_slots, float* E, float* H, T* rec, int blk) {
     const long long q = (long long)blk * blockDim.x + threadIdx.x;
     if (q >= ifc.total) return;
-    int t = *tp;
-    if (t < 0) t += n_slots;  // a negative step index wraps like a JAX index
-    if (t < 0 || t >= n_slots) return;
+    int t = *tp, tb = t;
+    float w = 0.f;
+    if (ifc.store) {  // time filter: store every k-th step, restore by linear interpolation
+        const int ti = t + 1;
+        if (RESTORE) {
+            tb = __ldg(ifc.rb + ti);
+            w = __ldg(ifc.rw + ti);
+            t = __ldg(ifc.ra + ti);
+        } else {
+            t = tb = __ldg(ifc.store + ti);
+            if (t < 0) return;
+        }
+    } else {
+        if (t < 0) t += n_slots;  // a negative step index wraps like a JAX index
+        tb = t;
+    }
+    if (t < 0 || t >= n_slots || tb < 0 || tb >= n_slots) return;
     int s = 0;
     while (s + 1 < ifc.n && q >= ifc.start[s + 1]) ++s;
     const long long pidx = q - ifc.start[s];
@@ -819,14 +838,19 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
     const long long c = cell_index(g, i, j, k);
     const long long P = ifc.start[s + 1] - ifc.start[s];
     T* slotp = rec + (long long)t * 6 * ifc.total;
+    const long long db = ((long long)tb - t) * 6 * ifc.total;  // slot b relative to slot a
 #pragma unroll
     for (int fld = 0; fld < 2; ++fld) {
         float* F = fld == 0 ? E : H;
         T* base = slotp + fld * 3 * ifc.total + 3 * ifc.start[s];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) {
-            if (RESTORE) F[comp * g.N + c] = from_storage(base[comp * P + pidx]);
-            else base[comp * P + pidx] = to_storage<T>(F[comp * g.N + c]);
+            if (RESTORE) {
+                const float va = from_storage(base[comp * P + pidx]);
+                F[comp * g.N + c] = w != 0.f ? va + w * (from_storage(base[db + comp * P + pidx]) - va) : va;
+            } else {
+                base[comp * P + pidx] = to_storage<T>(F[comp * g.N + c]);
+            }
         }
     }
 }

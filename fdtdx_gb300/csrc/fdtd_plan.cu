@@ -80,6 +80,9 @@ struct Arena {
     }
 };
 
+// Rows of the interface recording: one per step, or the time filter's stored steps.
+int rec_rows(const FdtdDesc& d) { return d.rec_slots > 0 ? d.rec_slots : d.n_steps_total; }
+
 long long face_cells(const FdtdSourceDesc& s) {
     return (long long)(s.hi[0] - s.lo[0]) * (s.hi[1] - s.lo[1]) * (s.hi[2] - s.lo[2]);
 }
@@ -179,6 +182,17 @@ int validate(const FdtdDesc* d, std::string& why) {
     if (d->n_sigma_E < 0 || d->n_sigma_E > 3 || d->n_sigma_E == 2) { why = "n_sigma_E must be 0, 1 or 3"; return FDTD_EINVAL; }
     if (d->n_sigma_H < 0 || d->n_sigma_H > 3 || d->n_sigma_H == 2) { why = "n_sigma_H must be 0, 1 or 3"; return FDTD_EINVAL; }
     if (d->n_slabs < 0 || d->n_slabs > FDTD_MAX_SLABS) { why = "too many slabs"; return FDTD_EINVAL; }
+    if (d->rec_slots < 0 || (d->rec_slots > 0 && (!d->rec_store || !d->rec_a || !d->rec_b || !d->rec_w))) {
+        why = "a recorder time filter needs rec_slots > 0 and all four tables";
+        return FDTD_EINVAL;
+    }
+    if (d->rec_slots > 0)
+        for (int t = 0; t < d->n_steps_total + 2; ++t)
+            if (d->rec_store[t] >= d->rec_slots || d->rec_a[t] < 0 || d->rec_a[t] >= d->rec_slots || d->rec_b[t] < 0 ||
+                d->rec_b[t] >= d->rec_slots) {
+                why = "recorder time-filter tables reference slots outside [0, rec_slots)";
+                return FDTD_EINVAL;
+            }
     if (d->n_sources < 0 || d->n_sources > FDTD_MAX_SOURCES) { why = "too many sources"; return FDTD_EINVAL; }
     if (d->n_detectors < 0 || d->n_detectors > FDTD_MAX_DETECTORS) { why = "too many detectors"; return FDTD_EINVAL; }
     const int n[3] = {d->nx, d->ny, d->nz};
@@ -400,6 +414,9 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     }
     size_t o_twin = 0;
     if (p->need_hprev) o_twin = ar.take(sizeof(float) * 3 * (size_t)p->g.N);
+    size_t o_rec[4] = {0, 0, 0, 0};
+    if (d.rec_slots > 0)
+        for (int q = 0; q < 4; ++q) o_rec[q] = ar.take(4 * tbl);
     p->dmem_bytes = ar.off;
 
     cudaError_t e = cudaMalloc(&p->dmem, p->dmem_bytes);
@@ -492,6 +509,16 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         if (e == cudaSuccess && dd.kind == FDTD_DET_PHASOR) e = up(o.w, dd.weights, 8 * tbl * dd.n_freq);
     }
     if (p->need_hprev) p->h_twin = reinterpret_cast<float*>(p->dmem + o_twin);
+    if (d.rec_slots > 0 && e == cudaSuccess) {
+        e = up(o_rec[0], d.rec_store, 4 * tbl);
+        if (e == cudaSuccess) e = up(o_rec[1], d.rec_a, 4 * tbl);
+        if (e == cudaSuccess) e = up(o_rec[2], d.rec_b, 4 * tbl);
+        if (e == cudaSuccess) e = up(o_rec[3], d.rec_w, 4 * tbl);
+        p->ifc.store = reinterpret_cast<const int*>(p->dmem + o_rec[0]);
+        p->ifc.ra = reinterpret_cast<const int*>(p->dmem + o_rec[1]);
+        p->ifc.rb = reinterpret_cast<const int*>(p->dmem + o_rec[2]);
+        p->ifc.rw = reinterpret_cast<const float*>(p->dmem + o_rec[3]);
+    }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         fprintf(stderr, "fdtd_plan_create: %s\n", cudaGetErrorString(e));
@@ -510,6 +537,8 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         p->d.detectors[q].slot = nullptr;
         p->d.detectors[q].weights = nullptr;
     }
+    p->d.rec_store = p->d.rec_a = p->d.rec_b = nullptr;
+    p->d.rec_w = nullptr;
     {
         const Split sp = split_boxes(p);
         p->tma_tz = pick_tz(sp.split ? sp.core.hi[2] - sp.core.lo[2] : p->g.nz);
@@ -757,7 +786,7 @@ int sources_launched(const FdtdPlan* p, bool eside) {
 template <typename T, bool RESTORE>
 void launch_ifaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t st) {
     const int blocks = (int)((p->ifc.total + 255) / 256);
-    k_interfaces<T, RESTORE><<<blocks, 256, 0, st>>>(p->g, p->ifc, p->d_t, p->d.n_steps_total, b->E, H,
+    k_interfaces<T, RESTORE><<<blocks, 256, 0, st>>>(p->g, p->ifc, p->d_t, rec_rows(p->d), b->E, H,
                                                      reinterpret_cast<T*>(b->recording));
 }
 
@@ -936,7 +965,7 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
         if (det_needs_h(dd)) hprev = true;
     }
     if (hprev) bytes += 12ll * N;
-    if (d->record_interfaces) bytes += (long long)rec_elem_bytes(d->recording_dtype) * 6 * iface * d->n_steps_total;
+    if (d->record_interfaces) bytes += (long long)rec_elem_bytes(d->recording_dtype) * 6 * iface * rec_rows(*d);
     bytes += 1ll << 20;  // tables and scratch
     return bytes;
 }

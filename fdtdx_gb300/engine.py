@@ -347,6 +347,16 @@ class Scene:
         if gc is not None and gc.recorder is not None:
             rec_dtype = gc.recorder.storage_dtype
         d.recording_dtype = {torch.float32: 0, torch.bfloat16: 1, torch.float16: 2}[rec_dtype]
+        tf = gc.recorder.time_filter if gc is not None and gc.recorder is not None else None
+        d.rec_slots = 0
+        if tf is not None and record_interfaces:
+            T = config.time_steps_total
+            store, ra, rb, rw = tf.tables(T)
+            tabs = [np.asarray(store, dtype=np.int32), np.asarray(ra, dtype=np.int32),
+                    np.asarray(rb, dtype=np.int32), np.asarray(rw, dtype=np.float32)]
+            self._keep.extend(tabs)
+            d.rec_slots = len(tf.save_steps(T))
+            d.rec_store, d.rec_a, d.rec_b, d.rec_w = (x.ctypes.data for x in tabs)
         self._plan: int | None = None
 
     # ---- plan lifecycle

@@ -128,7 +128,8 @@ def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None)
     gc = config.gradient_config
     if gc is not None and gc.recorder is not None:
         per_step = 6 * sum(int(torch.tensor(p.grid_shape).prod()) // p.thickness for p in objects.pml_objects)
-        data = torch.zeros((config.time_steps_total, per_step), dtype=gc.recorder.storage_dtype, device=device)
+        data = torch.zeros((gc.recorder.slots(config.time_steps_total), per_step), dtype=gc.recorder.storage_dtype,
+                           device=device)
         rec = RecordingState(data={"interfaces": data})
 
     return ArrayContainer(

@@ -138,6 +138,15 @@ typedef struct {
     FdtdDetectorDesc detectors[FDTD_MAX_DETECTORS];
     int32_t record_interfaces; /* 1: record E, H on each slab's innermost layer after every step */
     int32_t recording_dtype;   /* 0: float32, 1: bfloat16, 2: float16 */
+    /* Recorder time filter (fdtdx/interfaces/time_filter.py:140-257), or rec_slots = 0 for one
+     * slot per step.  Tables of n_steps_total + 2 entries (entry t + 1 for step t): the slot
+     * step t is stored in (-1: not stored), and the two slots and the weight a reverse step
+     * restores from: v = v[rec_a] + rec_w (v[rec_b] - v[rec_a]).  Host pointers, copied. */
+    int32_t rec_slots;
+    const int32_t* rec_store;
+    const int32_t* rec_a;
+    const int32_t* rec_b;
+    const float* rec_w;
 } FdtdDesc;
 
 typedef struct {
@@ -150,7 +159,7 @@ typedef struct {
     float* psi_E[FDTD_MAX_SLABS][2];  /* slab-shaped psi pairs (psi_1, psi_2) */
     float* psi_H[FDTD_MAX_SLABS][2];
     void* det_state[FDTD_MAX_DETECTORS];
-    void* recording;            /* (T, fdtd_interface_floats(plan)) in recording_dtype, or NULL */
+    void* recording;            /* (T or rec_slots, fdtd_interface_floats(plan)) in recording_dtype, or NULL */
 } FdtdBuffers;
 
 /* Cotangent (adjoint) buffers of the reversible gradient. */

@@ -330,6 +330,44 @@ class OracleScene:
         self.periodic = tuple(self.periodic)
         self.sources = [self._setup_source(s) for s in objects.sources]
         self.detectors = [self._setup_detector(d) for d in objects.detectors if not d.inverse]
+        self._setup_time_filter(config)
+
+    # ---- recorder time filter (fdtdx/interfaces/time_filter.py:140-257)
+    def _setup_time_filter(self, config):
+        self.tf_save, self.tf_map = None, None
+        gc = getattr(config, "gradient_config", None)
+        rec = getattr(gc, "recorder", None) if gc is not None else None
+        for m in getattr(rec, "modules", []) if rec is not None else []:
+            if type(m).__name__ != "LinearReconstructEveryK":
+                continue
+            T, k = self.T, m.k
+            save = list(range(m.start_recording_after, T, k))  # time_filter.py:168-171
+            if save[-1] != T - 1:
+                save.append(T - 1)
+            idx = np.zeros(T, dtype=np.int64)  # time_filter.py:176-187
+            idx[save] = np.arange(len(save))
+            for _ in range(k - 1):
+                rolled = np.roll(idx, 1)
+                idx = np.where(idx == 0, rolled, idx)
+                idx[:k] = 0
+            self.tf_save, self.tf_map = save, idx
+
+    def recorded(self, rec: list, t: int) -> dict:
+        """Interface values the reverse step at t re-imposes (time_filter.py:218-257)."""
+        if self.tf_save is None:
+            return rec[t]  # a Python list wraps t = -1 like the JAX gather
+        tj = t + self.T if t < 0 else t
+        a = int(self.tf_map[tj])
+        if tj in self.tf_save:
+            return rec[a]
+        nxt = min(a + 1, len(rec) - 1)  # a JAX gather clamps the index
+        t_prev = int(np.argmax(self.tf_map == a))  # index_1d_array: first step mapped to the slot
+        t_next = int(np.argmax(self.tf_map == a + 1))
+        f = (t - t_prev) / (t_next - t_prev)
+        return {key: v + f * (rec[nxt][key] - v) for key, v in rec[a].items()}
+
+    def records(self, t: int) -> bool:
+        return self.tf_save is None or t in self.tf_save
 
     # ---- sources
     def _switch_tables(self, sw):
@@ -767,7 +805,7 @@ def forward(sc: OracleScene, st: OState, inv_eps=None, inv_mu=None, record_detec
     E, psi_E = update_E(sc, t, st.E, st.H, st.psi_E, inv_eps, simulate_boundaries)
     H, psi_H = update_H(sc, t, E, st.H, st.psi_H, inv_mu, simulate_boundaries)
     rec = st.rec
-    if record_boundaries:
+    if record_boundaries and sc.records(t):
         rec = rec + [collect_interfaces(sc, E, H)]
     det = update_detectors(sc, t, E, H, H_prev, st.det, inv_eps, inv_mu) if record_detectors else st.det
     return OState(t + 1, E, H, psi_E, psi_H, det, rec)
@@ -778,7 +816,7 @@ def backward(sc: OracleScene, st: OState) -> OState:
     t = st.t - 1
     E, H = st.E, st.H
     if st.rec:
-        E, H = add_interfaces(sc, E, H, st.rec[t])  # a Python list wraps t = -1 like the JAX gather
+        E, H = add_interfaces(sc, E, H, sc.recorded(st.rec, t))
     H = update_H_reverse(sc, t, E, H, st.psi_H, sc.inv_mu)
     E = update_E_reverse(sc, t, E, H, st.psi_E, sc.inv_eps)
     return OState(t, E, H, st.psi_E, st.psi_H, st.det, st.rec)

@@ -100,11 +100,11 @@ def test_adjoint_periodic_lossy_slab_fields_loss():
     _check("adjoint_periodic_lossy", g, sc32, sc64, f32, f64, {}, {}, cot_E=lambda f: 2 * f.E)
 
 
-def _cpml_phasor_scene(shape=(26, 24, 24), pml=5, steps=90):
+def _cpml_phasor_scene(shape=(26, 24, 24), pml=5, steps=90, recorder=None):
     dx = 50e-9
     dt = 0.99 / math.sqrt(3) * dx / C0
     cfg = fx.SimulationConfig(time=steps * dt, grid=fx.UniformGrid(dx),
-                              gradient_config=fx.GradientConfig(recorder=fx.Recorder()))
+                              gradient_config=fx.GradientConfig(recorder=recorder or fx.Recorder()))
     vol = fx.SimulationVolume(shape=shape)
     objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(pml), vol).values())
     objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((10, 16), (9, 15), (9, 15)),
@@ -129,6 +129,32 @@ def test_adjoint_cpml_plane_source_phasor_objective():
     f32, f64 = O.run(sc32, T, record_boundaries=True), O.run(sc64, T, record_boundaries=True)
     _check("adjoint_cpml_phasor", g, sc32, sc64, f32, f64,
            {"ph": {"phasor": 2 * f32.det["ph"]["phasor"]}}, {"ph": {"phasor": 2 * f64.det["ph"]["phasor"]}})
+
+
+@pytest.mark.parametrize("modules", [
+    [fx.LinearReconstructEveryK(k=3)],
+    [fx.LinearReconstructEveryK(k=4, start_recording_after=5), fx.DtypeConversion(torch.float16)],
+])
+def test_adjoint_recorder_time_filter(modules):
+    """Interfaces stored every k-th step and interpolated in the reverse steps (the recording
+    holds the filter's stored steps only), against the oracle with the same recorder."""
+    objects, arrays, cfg = _cpml_phasor_scene(recorder=fx.Recorder(modules))
+    assert arrays.recording_state.data["interfaces"].shape[0] == cfg.gradient_config.recorder.slots(
+        cfg.time_steps_total) < cfg.time_steps_total
+    out, g = _gpu_grad(objects, arrays, cfg, lambda o: (o.detector_states["ph"]["phasor"].abs() ** 2).sum())
+    sc32, sc64 = O.OracleScene(objects, arrays, cfg, torch.float32), O.OracleScene(objects, arrays, cfg, torch.float64)
+    T = cfg.time_steps_total
+    f32, f64 = O.run(sc32, T, record_boundaries=True), O.run(sc64, T, record_boundaries=True)
+    if any(isinstance(m, fx.DtypeConversion) for m in modules):
+        # the stored planes are rounded to the storage dtype: so are the oracle's
+        for f in (f32, f64):
+            f.rec[:] = [{k: v.to(torch.float16).to(v.dtype) for k, v in r.items()} for r in f.rec]
+    tol = "f16" if any(isinstance(m, fx.DtypeConversion) for m in modules) else "f32"
+    g32 = O.reversible_gradient(sc32, f32, {"ph": {"phasor": 2 * f32.det["ph"]["phasor"]}})
+    g64 = O.reversible_gradient(sc64, f64, {"ph": {"phasor": 2 * f64.det["ph"]["phasor"]}})
+    e32, e64 = rel_l2(g, g32), rel_l2(g, g64)
+    log_result(f"adjoint_time_filter_{tol}", grad_rel_l2_vs_fp32=e32, grad_rel_l2_vs_fp64=e64)
+    assert e32 <= GTOL, (e32, e64)
 
 
 def _all_detectors_scene(steps=70):
