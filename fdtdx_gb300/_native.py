@@ -132,6 +132,7 @@ class AdjointBuffers(C.Structure):
         ("lam_psi_H", (C.c_void_p * 2) * MAX_SLABS),
         ("lam_det", C.c_void_p * MAX_DETECTORS),
         ("grad_inv_eps", C.c_void_p),
+        ("grad_inv_mu", C.c_void_p),
     ]
 
 

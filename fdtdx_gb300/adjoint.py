@@ -4,7 +4,8 @@ The forward pass runs on the native library and records the PML-interface planes
 (``record_boundaries=config.invertible_optimization``).  The backward pass is the
 reference's custom VJP: for t = T-1 down to -1, reconstruct the state at t by a
 reverse step (interfaces re-imposed, psi frozen) and apply the transpose of the
-forward step at t, accumulating d/d inv_permittivities.  Both run in one native call
+forward step at t, accumulating d/d inv_permittivities and d/d inv_permeabilities
+(the latter when the permeability is an array).  Both run in one native call
 (``fdtd_adjoint``); here the cotangents are marshalled and the call is wrapped as a
 ``torch.autograd.Function``, the PyTorch counterpart of ``jax.custom_vjp``.
 
@@ -13,9 +14,9 @@ stores the full field state at the interior slice boundaries during the forward 
 and resets the reconstruction to it when the backward loop reaches that step.
 
 As in the reference only the materials receive a gradient (fdtd.py:324-333); the
-initial fields, psi, detector states and recording get none.  The inv_permeability
-gradient of the reference is not provided: a magnetic-material input that requires a
-gradient raises.
+initial fields, psi, detector states and recording get none.  A scalar (float)
+inv_permeabilities carries no gradient here: make it a (1 | 3, nx, ny, nz) tensor to
+differentiate it.
 """
 
 from __future__ import annotations
@@ -83,10 +84,10 @@ class _Layout:
 
 
 class _ReversibleRun(torch.autograd.Function):
-    """Forward run + reversible backward; the only differentiable input is inv_permittivities."""
+    """Forward run + reversible backward; the differentiable inputs are the materials."""
 
     @staticmethod
-    def forward(ctx, ctl: dict, inv_eps: torch.Tensor):
+    def forward(ctx, ctl: dict, inv_eps: torch.Tensor, inv_mu: torch.Tensor | None):
         scene, arrays, T = ctl["scene"], ctl["arrays"], ctl["T"]
         bounds = ctl["bounds"]
         checkpoints = []
@@ -133,9 +134,15 @@ class _ReversibleRun(torch.autograd.Function):
             if grads[i] is not None:
                 lam["det"][n] = cot(i)
             i += 1
-        ie = ctl["inv_eps"]
-        grad = torch.zeros_like(ie, dtype=torch.float32).contiguous()
-        lam["grad_inv_eps"] = grad
+        ie, im = ctl["inv_eps"], ctl["inv_mu"]
+        want_eps, want_mu = ctx.needs_input_grad[1], ctx.needs_input_grad[2]
+        grad = grad_mu = None
+        if want_eps:
+            grad = torch.zeros_like(ie, dtype=torch.float32).contiguous()
+            lam["grad_inv_eps"] = grad
+        if want_mu:
+            grad_mu = torch.zeros_like(im, dtype=torch.float32).contiguous()
+            lam["grad_inv_mu"] = grad_mu
         # slices from the last to the first; the last call runs down to t = -1
         k = len(bounds) - 1
         for seg in range(k - 1, -1, -1):
@@ -146,7 +153,8 @@ class _ReversibleRun(torch.autograd.Function):
                 _copy_fields(f, checkpoints[seg - 1])
         scene.status()
         ctl["checkpoints"] = []
-        return None, grad.to(ie.dtype)
+        return (None, None if grad is None else grad.to(ie.dtype),
+                None if grad_mu is None else grad_mu.to(im.dtype))
 
 
 def reversible_fdtd(
@@ -159,18 +167,15 @@ def reversible_fdtd(
 ) -> SimulationState:
     """Differentiable forward run with the time-reversal gradient (fdtd.py:39-418).
 
-    Returns ``(T, arrays)`` like the reference.  When ``arrays.inv_permittivities``
-    requires a gradient, the returned fields and detector states are connected to it
-    through the reversible backward pass.
+    Returns ``(T, arrays)`` like the reference.  When ``arrays.inv_permittivities`` or an
+    array ``arrays.inv_permeabilities`` requires a gradient, the returned fields and
+    detector states are connected to it through the reversible backward pass.
     """
     del key, show_progress
     from fdtdx_gb300.fdtd import _materials_detached, get_scene
 
     if arrays.inv_permittivities.shape[0] not in (1, 3):
         raise NotImplementedError("fully anisotropic (9-component) materials are not supported")
-    mu = arrays.inv_permeabilities
-    if isinstance(mu, torch.Tensor) and mu.requires_grad:
-        raise NotImplementedError("the inv_permeabilities gradient is not provided by the reversible path")
     gc = config.gradient_config
     num_ckpt = 0 if gc is None else gc.num_checkpoints_reversible
     T = config.time_steps_total
@@ -182,20 +187,30 @@ def reversible_fdtd(
         )
     bounds = reversible_slice_boundaries(T, num_slices)
     ie_in = arrays.inv_permittivities
+    mu_in = arrays.inv_permeabilities
+    if isinstance(mu_in, torch.Tensor) and mu_in.dim() == 0:
+        if mu_in.requires_grad:
+            raise NotImplementedError("a 0-d inv_permeabilities has no gradient here: pass a (1|3, nx, ny, nz) array")
+        mu_in = float(mu_in)
+        arrays = arrays.aset("inv_permeabilities", mu_in)
+    mu_t = mu_in if isinstance(mu_in, torch.Tensor) else None
     work = _materials_detached(arrays).reset()
     if work.recording_state is None and config.invertible_optimization and objects.pml_objects:
         raise ValueError("the reversible gradient needs a recording state (init_arrays with a recorder)")
     scene = get_scene(objects, work, config, record_interfaces=config.invertible_optimization)
     layout = _Layout(work)
     ctl = {"scene": scene, "arrays": work, "T": T, "bounds": bounds, "layout": layout,
-           "inv_eps": work.inv_permittivities}
-    if not (torch.is_grad_enabled() and ie_in.requires_grad):
-        _ReversibleRun.forward(_NoCtx(), ctl, work.inv_permittivities)
+           "inv_eps": work.inv_permittivities, "inv_mu": work.inv_permeabilities}
+    wants = ie_in.requires_grad or (mu_t is not None and mu_t.requires_grad)
+    if not (torch.is_grad_enabled() and wants):
+        _ReversibleRun.forward(_NoCtx(), ctl, work.inv_permittivities, None)
         out = work
     else:
-        flat = _ReversibleRun.apply(ctl, ie_in)
+        flat = _ReversibleRun.apply(ctl, ie_in, mu_t)
         out = layout.unflatten(work, list(flat))
         out = out.aset("inv_permittivities", ie_in)
+        if mu_t is not None:
+            out = out.aset("inv_permeabilities", mu_t)
     if progress_callback is not None:
         progress_callback(T, T)
     return T, out

@@ -15,7 +15,8 @@
 // transposed detector samples (k_adj_det, a scatter over the detector region).  Sources
 // add constants (the reference stops their gradient, tfsf.py:286-304) and drop out.
 // d/d inv_eps is taken in k_adj_E from the E-step with curl_H evaluated at the
-// reconstructed H and the frozen psi, as jax.vjp evaluates it there.
+// reconstructed H and the frozen psi, as jax.vjp evaluates it there; d/d inv_mu in
+// k_grad_mu from the H-step with curl_E evaluated at the recomputed E3.
 //
 // Cotangents of complex detector states follow torch's convention: for a real loss L the
 // cotangent of z is dL/dRe z + i dL/dIm z, so a real sample x entering z as x * w has
@@ -57,6 +58,8 @@ struct AdjArgs {
     DSlab slab[FDTD_MAX_SLABS];
     const float* psiE1[FDTD_MAX_SLABS];  // frozen psi_E of the reconstructed state
     const float* psiE2[FDTD_MAX_SLABS];
+    const float* psiH1[FDTD_MAX_SLABS];  // frozen psi_H (read by the inv_mu cotangent only)
+    const float* psiH2[FDTD_MAX_SLABS];
     float* lE;             // in: lam E(t+1) (+ detector part); k_adj_H turns it into lam E3 in place
     float* lH;             // lam H(t+1) (+ detector part)
     float* lE_out;         // lam E(t)
@@ -66,6 +69,7 @@ struct AdjArgs {
     float* lpE_out[FDTD_MAX_SLABS][2];    // lam psi_E(t), lam psi_H(t)
     float* lpH_out[FDTD_MAX_SLABS][2];
     float* grad_ie;        // (n_eps, N), accumulated; nullptr: not wanted
+    float* grad_im;        // (n_mu, N), accumulated; nullptr: not wanted
     DBox hp;               // detector cotangents of H before the H update (added to lam H(t), then cleared)
     // the boxes a launch covers (the layout of UpdArgs' box table, read by column_of)
     int nbox;
@@ -1260,7 +1264,7 @@ __global__ void __launch_bounds__(kDetBlock) k_adj_det(const __grid_constant__ A
             gv[5] = gS[0] * v[1] - gS[1] * v[0];
         } else {  // energy 0.5 sum E^2 / ie + 0.5 sum H^2 / im
             const long long c = cell_index(g, i, j, k);
-            float gsum = 0.f;
+            float gsum = 0.f, msum = 0.f;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 const float ie = adj_mat(a.ie, a.n_eps, 1.f, g.N, q, c);
@@ -1272,11 +1276,129 @@ __global__ void __launch_bounds__(kDetBlock) k_adj_det(const __grid_constant__ A
                     if (a.n_eps == 3) atomicAdd(a.grad_ie + q * g.N + c, ge);
                     else gsum += ge;
                 }
+                const float gm = -0.5f * L[0] * v[3 + q] * v[3 + q] / (im * im);
+                if (a.grad_im) {
+                    if (a.n_mu == 3) atomicAdd(a.grad_im + q * g.N + c, gm);
+                    else msum += gm;
+                }
             }
             if (a.grad_ie && a.n_eps != 3) atomicAdd(a.grad_ie + c, gsum);
+            if (a.grad_im && a.n_mu != 3) atomicAdd(a.grad_im + c, msum);
         }
     }
     colocate_T(a, d.exact, i, j, k, gv);
+}
+
+// ---------------------------------------------------------------------------------
+// inv_mu cotangent of one forward H-step, H1 = (g H - c im curl_E(E3', psiH')) / e, taken
+// as jax.vjp takes it at the reconstructed state (fdtdx/fdtd/fdtd.py:228-249, cotangent
+// cot[6] returned at :331): E3' is the E-step recomputed from the reconstructed (E, H)
+// and psiH' = bH psiH + aH dE3' is advanced from the frozen psi_H.  The reverse E-step
+// inverted the E-step with the frozen psi_E, so E3' equals the state's E3 outside the
+// E-slabs and, inside them, E3 + (c ie / d)(psiE' - psiE) on each corrected component
+// (psiE' = bE psiE + aE dH, the kappa terms cancel; PEC components stay zero).
+// k_grad_mu runs between the reverse H-step (H holds H(t)) and the reverse E-step (E
+// still holds E3), after the detector cotangents have been added to lam H3:
+//   d im += PMC(lam H3) . dH1/d im,  dH1/d im = (-c curl - (c sigma_H / 2 eta0)(H + H1)) / e.
+// ---------------------------------------------------------------------------------
+
+// E3' at (i, j, k) (halo rule: zero in a zero halo).
+template <bool PML>
+__device__ __forceinline__ float e3_recomputed(const AdjArgs& a, int i, int j, int k, int comp) {
+    const Geo& g = a.g;
+    if (!wrap_idx(g, i, j, k)) return 0.f;
+    const long long N = g.N;
+    const long long c = cell_index(g, i, j, k);
+    const float v = __ldg(a.E + comp * N + c);
+    if (!PML) return v;
+    float dc = 0.f;
+#pragma unroll
+    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+        if (s >= a.n_slab) break;
+        const DSlab& sl = a.slab[s];
+        const int ax = sl.axis;
+        const int ci = (ax + 1) % 3, cj = (ax + 2) % 3;
+        if (comp != ci && comp != cj) continue;
+        const int l = slab_layer(sl, i, j, k);
+        if (l < 0) continue;
+        const int pi = i - (ax == 0), pj = j - (ax == 1), pk = k - (ax == 2);
+        const float ca = __ldg(sl.coef + l), cb = __ldg(sl.coef + sl.L + l);
+        const long long p = psi_offset(sl, i, j, k);
+        if (comp == ci) {  // curl[ci] -= c1, c1 from psi1 and d1 = d_ax H[cj]
+            const float d1 = __ldg(a.H + cj * N + c) - ld_halo(g, a.H, cj, pi, pj, pk);
+            dc -= (cb - 1.f) * __ldg(a.psiE1[s] + p) + ca * d1;
+        } else {           // curl[cj] += c2, c2 from psi2 and d2 = d_ax H[ci]
+            const float d2 = __ldg(a.H + ci * N + c) - ld_halo(g, a.H, ci, pi, pj, pk);
+            dc += (cb - 1.f) * __ldg(a.psiE2[s] + p) + ca * d2;
+        }
+    }
+    if (dc == 0.f || (g.pec && face_zero(g, g.pec, comp, i, j, k))) return v;
+    const float m = adj_mat(a.ie, a.n_eps, 1.f, N, comp, c);
+    float den = 1.f;
+    if (a.sigE) den = 1.f + g.c * adj_mat(a.sigE, a.n_sigE, 0.f, N, comp, c) * g.eta0 * m / 2.f;
+    return v + g.c * m / den * dc;
+}
+
+// One thread per cell (z fastest).
+template <bool PML>
+__global__ void __launch_bounds__(256) k_grad_mu(const __grid_constant__ AdjArgs a) {
+    const Geo& g = a.g;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.N) return;
+    const long long N = g.N;
+    const int k = (int)(c % g.nz);
+    const int j = (int)((c / g.nz) % g.ny);
+    const int i = (int)(c / ((long long)g.nz * g.ny));
+    const float Ex = e3_recomputed<PML>(a, i, j, k, 0);
+    const float Ey = e3_recomputed<PML>(a, i, j, k, 1);
+    const float Ez = e3_recomputed<PML>(a, i, j, k, 2);
+    // raw forward differences in the order (dy Ez, dz Ey, dz Ex, dx Ez, dx Ey, dy Ex)
+    const float d[6] = {e3_recomputed<PML>(a, i, j + 1, k, 2) - Ez, e3_recomputed<PML>(a, i, j, k + 1, 1) - Ey,
+                        e3_recomputed<PML>(a, i, j, k + 1, 0) - Ex, e3_recomputed<PML>(a, i + 1, j, k, 2) - Ez,
+                        e3_recomputed<PML>(a, i + 1, j, k, 1) - Ey, e3_recomputed<PML>(a, i, j + 1, k, 0) - Ex};
+    float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+    if (PML) {
+#pragma unroll
+        for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
+            if (s >= a.n_slab) break;
+            const DSlab& sl = a.slab[s];
+            const int l = slab_layer(sl, i, j, k);
+            if (l < 0) continue;
+            const float d1 = sl.axis == 0 ? d[3] : (sl.axis == 1 ? d[5] : d[1]);
+            const float d2 = sl.axis == 0 ? d[4] : (sl.axis == 1 ? d[0] : d[2]);
+            const float* co = sl.coef + 3 * sl.L;
+            const long long p = psi_offset(sl, i, j, k);
+            const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
+            float c1 = cb * __ldg(a.psiH1[s] + p) + ca * d1;
+            float c2 = cb * __ldg(a.psiH2[s] + p) + ca * d2;
+            if (!sl.kappa_one) {
+                const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+                c1 += ikm1 * d1;
+                c2 += ikm1 * d2;
+            }
+            if (sl.axis == 0) { cu[1] -= c1; cu[2] += c2; }
+            else if (sl.axis == 1) { cu[2] -= c1; cu[0] += c2; }
+            else { cu[0] -= c1; cu[1] += c2; }
+        }
+    }
+    float gsum = 0.f;
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+        float l3 = a.lH[comp * N + c];
+        if (g.pmc && face_zero(g, g.pmc, comp, i, j, k)) l3 = 0.f;
+        float dm = -g.c * cu[comp];
+        if (a.sigH) {
+            const float m = adj_mat(a.im, a.n_mu, a.im_scalar, N, comp, c);
+            const float hs = g.c * adj_mat(a.sigH, a.n_sigH, 0.f, N, comp, c) / g.eta0 / 2.f;
+            const float qh = hs * m;
+            const float h0 = __ldg(a.H + comp * N + c);
+            const float h1 = ((1.f - qh) * h0 - g.c * m * cu[comp]) / (1.f + qh);
+            dm = (-g.c * cu[comp] - hs * (h0 + h1)) / (1.f + qh);
+        }
+        if (a.n_mu == 3) a.grad_im[comp * N + c] += l3 * dm;
+        else gsum += l3 * dm;
+    }
+    if (a.n_mu != 3) a.grad_im[c] += gsum;
 }
 
 // Clears the cotangent entry a reducing field / flux / energy detector overwrote at step t

@@ -117,6 +117,8 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
         a.slab[s] = p->slab[s];
         a.psiE1[s] = b->psi_E[s][0];
         a.psiE2[s] = b->psi_E[s][1];
+        a.psiH1[s] = b->psi_H[s][0];
+        a.psiH2[s] = b->psi_H[s][1];
         a.lpE[s][0] = cur.psi[s][0]; a.lpE[s][1] = cur.psi[s][1];
         a.lpH[s][0] = cur.psi[s][2]; a.lpH[s][1] = cur.psi[s][3];
         a.lpE_out[s][0] = nxt.psi[s][0]; a.lpE_out[s][1] = nxt.psi[s][1];
@@ -127,6 +129,7 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
     a.lE_out = nxt.E;
     a.lH_out = nxt.H;
     a.grad_ie = adj->grad_inv_eps;
+    a.grad_im = adj->grad_inv_mu;
     a.hp = p->hp;
     for (int x = 0; x < 3; ++x) a.ax_slab[x][0] = a.ax_slab[x][1] = -1;
     for (int s = 0; s < p->d.n_slabs; ++s) {
@@ -150,6 +153,8 @@ int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
     for (int s = 0; s < p->d.n_slabs; ++s)
         if (!adj->lam_psi_E[s][0] || !adj->lam_psi_E[s][1] || !adj->lam_psi_H[s][0] || !adj->lam_psi_H[s][1])
             return fail(p, FDTD_EINVAL, "psi cotangent buffers required for every slab");
+    if (adj->grad_inv_mu && p->d.n_mu == 0)
+        return fail(p, FDTD_EINVAL, "grad_inv_mu needs an inv_mu array (n_mu 1 or 3), not a scalar inv_mu");
     return FDTD_OK;
 }
 
@@ -233,8 +238,8 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
     interfaces<true>(p, b, b->H, st);
     launch_sources(p, b, false, b->H, 1, st);
     launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H), st);
-    launch_sources(p, b, true, b->E, 1, st);
-    launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E), st);
+    // here H holds H(t) and E still E3: the detector cotangents (which read H(t) for exact
+    // interpolation) complete lam H3, and the inv_mu cotangent needs E3 and H(t)
     const AdjArgs a = make_adj(p, b, adj, cur, nxt);
     for (int q = 0; q < p->d.n_detectors; ++q) {
         if (!adj->lam_det[q]) continue;
@@ -246,6 +251,13 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
         k_adj_det<<<dd.nblocks, kDetBlock, 0, st>>>(a, x, p->d_t);
         if (dd.reduce && dd.kind != FDTD_DET_PHASOR) k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
     }
+    if (a.grad_im) {
+        const unsigned nb = (unsigned)((p->g.N + 255) / 256);
+        if (a.n_slab) k_grad_mu<true><<<nb, 256, 0, st>>>(a);
+        else k_grad_mu<false><<<nb, 256, 0, st>>>(a);
+    }
+    launch_sources(p, b, true, b->E, 1, st);
+    launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E), st);
     launch_adj<true>(p, a, st);
     launch_adj<false>(p, a, st);
     k_advance<<<1, 1, 0, st>>>(p->d_t, -1);

@@ -449,8 +449,8 @@ class Scene:
         ``arrays`` holds the forward state at ``t_end`` and is reconstructed in place down to
         ``t_end - n_steps``.  ``lam`` holds the cotangents of that state: ``"E"``, ``"H"``,
         ``"psi_E"`` / ``"psi_H"`` (name -> (psi1, psi2)), ``"det"`` (detector name -> tensor
-        of the state's layout, complex states with torch's convention) and ``"grad_inv_eps"``
-        (accumulated); all are updated in place.
+        of the state's layout, complex states with torch's convention), ``"grad_inv_eps"`` and
+        ``"grad_inv_mu"`` (accumulated; either may be absent); all are updated in place.
         """
         st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
         b = self.buffers(arrays)
@@ -470,6 +470,7 @@ class Scene:
                 raise ValueError("detector cotangents must be contiguous CUDA tensors")
             a.lam_det[q] = N.ptr(t)
         a.grad_inv_eps = N.ptr(lam.get("grad_inv_eps"))
+        a.grad_inv_mu = N.ptr(lam.get("grad_inv_mu"))
         rc = N.load().fdtd_adjoint(self.plan, C.byref(b), C.byref(a), int(t_end), int(n_steps),
                                    C.c_void_p(st.cuda_stream))
         N.check(rc, self.plan, "fdtd_adjoint")

@@ -173,6 +173,9 @@ typedef struct {
      * step overwrote (field, flux, energy slots) are cleared as the loop passes them. */
     void* lam_det[FDTD_MAX_DETECTORS];
     float* grad_inv_eps;        /* (n_eps, nx, ny, nz), accumulated (+=), or NULL */
+    /* (n_mu, nx, ny, nz), accumulated (+=), or NULL; needs an inv_mu array (n_mu 1 or 3).
+     * The reference's custom VJP returns this cotangent as cot[6] (fdtdx/fdtd/fdtd.py:331). */
+    float* grad_inv_mu;
 } FdtdAdjointBuffers;
 
 typedef struct FdtdPlan FdtdPlan;
@@ -202,7 +205,8 @@ int fdtd_reverse(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t_end, int32_t
  * (t = -1 is admitted, as the reference's loop runs one step there): reverse step
  * t+1 -> t on bufs (interfaces re-imposed, psi frozen), then the transposed forward
  * step at t.  On entry adj holds the cotangents of the state at t_end, on return
- * those of the state at t_end - n_steps; grad_inv_eps accumulates.  The first call
+ * those of the state at t_end - n_steps; grad_inv_eps and grad_inv_mu accumulate
+ * (fdtdx/fdtd/fdtd.py:324-333 returns both material cotangents).  The first call
  * allocates the plan's adjoint scratch (cotangent twins, detector snapshots);
  * fdtd_plan_device_bytes counts it from then on. */
 int fdtd_adjoint(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t_end,

@@ -831,13 +831,15 @@ def run(sc: OracleScene, n_steps: int | None = None, record_boundaries=False, st
     return st
 
 
-def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=None, cot_H=None) -> torch.Tensor:
+def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=None, cot_H=None, with_mu=False):
     """d loss / d inv_eps by the reference's custom VJP (fdtdx/fdtd/fdtd.py:215-333).
 
     Reverse-reconstructs the state step by step (psi frozen, interfaces re-imposed) and
     applies the VJP of one forward step at each reconstructed state, from t = T-1 down to
     t = -1 (the reference's loop condition ``time_step >= 0`` admits one step at t = -1).
-    Cotangents follow torch's convention for complex detector states.
+    Cotangents follow torch's convention for complex detector states.  With ``with_mu``
+    (an inv_mu array) returns ``(d/d inv_eps, d/d inv_mu)``, the reference's cot[5] and
+    cot[6] (fdtd.py:330-331).
     """
     zE = torch.zeros_like(final.E)
     lam = {
@@ -849,6 +851,9 @@ def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=Non
                 for k, v in final.det.items()},
     }
     grad = torch.zeros_like(sc.inv_eps)
+    if with_mu and not isinstance(sc.inv_mu, torch.Tensor):
+        raise ValueError("with_mu needs an inv_mu array")
+    grad_mu = torch.zeros_like(sc.inv_mu) if with_mu else None
     st = final
     while st.t >= 0:
         st = backward(sc, st)
@@ -858,7 +863,8 @@ def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=Non
         pH = {k: (a.clone().requires_grad_(True), b.clone().requires_grad_(True)) for k, (a, b) in st.psi_H.items()}
         det_in = {k: {k2: v2.clone().requires_grad_(True) for k2, v2 in v.items()} for k, v in st.det.items()}
         ie = sc.inv_eps.clone().requires_grad_(True)
-        out = forward(sc, OState(st.t, E, H, pE, pH, det_in, []), inv_eps=ie, record_detectors=True)
+        im = sc.inv_mu.clone().requires_grad_(True) if with_mu else None
+        out = forward(sc, OState(st.t, E, H, pE, pH, det_in, []), inv_eps=ie, inv_mu=im, record_detectors=True)
         outs, cots, ins = [out.E, out.H], [lam["E"], lam["H"]], [E, H, ie]
         for k in pE:
             outs += [out.psi_E[k][0], out.psi_E[k][1], out.psi_H[k][0], out.psi_H[k][1]]
@@ -869,6 +875,8 @@ def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=Non
             outs.append(out.det[k][k2])
             cots.append(lam["det"][k][k2])
             ins.append(det_in[k][k2])
+        if with_mu:
+            ins.append(im)
         pairs = [(o, c) for o, c in zip(outs, cots) if o.requires_grad]
         g = torch.autograd.grad([o for o, _ in pairs], ins, grad_outputs=[c for _, c in pairs], allow_unused=True)
         g = [torch.zeros_like(x) if gi is None else gi for gi, x in zip(g, ins)]
@@ -882,16 +890,19 @@ def reversible_gradient(sc: OracleScene, final: OState, cot_det: dict, cot_E=Non
         for k, k2 in dkeys:
             lam["det"][k][k2] = g[q]
             q += 1
-    return grad
+        if with_mu:
+            grad_mu = grad_mu + g[q]
+    return (grad, grad_mu) if with_mu else grad
 
 
-def autograd_gradient(sc: OracleScene, loss_fn, n_steps: int | None = None) -> torch.Tensor:
-    """Exact gradient of loss_fn(final detector states) by autograd through the whole forward run."""
-    ie = sc.inv_eps.clone().requires_grad_(True)
+def autograd_gradient(sc: OracleScene, loss_fn, n_steps: int | None = None, wrt: str = "eps") -> torch.Tensor:
+    """Exact gradient of loss_fn(final detector states) by autograd through the whole forward run
+    with respect to inv_eps (``wrt="eps"``) or the inv_mu array (``wrt="mu"``)."""
+    x = (sc.inv_eps if wrt == "eps" else sc.inv_mu).clone().requires_grad_(True)
     st = sc.init_state()
     n = sc.T if n_steps is None else n_steps
     for _ in range(n):
-        st = forward(sc, st, inv_eps=ie)
+        st = forward(sc, st, inv_eps=x) if wrt == "eps" else forward(sc, st, inv_mu=x)
     loss = loss_fn(st.det)
-    (g,) = torch.autograd.grad(loss, [ie])
+    (g,) = torch.autograd.grad(loss, [x])
     return g

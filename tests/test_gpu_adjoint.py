@@ -282,3 +282,87 @@ def test_adjoint_params_chain_and_finite_differences():
     e = rel_l2(ad, fd)
     log_result("adjoint_fd_16_voxels", rel_l2=e, fd=fd.tolist(), adjoint=ad.tolist())
     assert e <= 2e-2, (e, fd, ad)
+
+
+def _gpu_grads_eps_mu(objects, arrays, cfg, cot_fn):
+    """d <cot, outputs> / d (inv_eps, inv_mu) through the public reversible_fdtd."""
+    ga = _to_cuda(objects, arrays)
+    ie = ga.inv_permittivities.clone().requires_grad_(True)
+    im = ga.inv_permeabilities.clone().requires_grad_(True)
+    _, out = fx.reversible_fdtd(ga.aset("inv_permittivities", ie).aset("inv_permeabilities", im), objects, cfg)
+    cot_fn(out).backward()
+    torch.cuda.synchronize()
+    return ie.grad.detach().cpu(), im.grad.detach().cpu()
+
+
+def _check_eps_mu(name, ge, gm, objects, arrays, cfg, cots, cot_E=None, cot_H=None):
+    T = cfg.time_steps_total
+    res = {}
+    for dt in (torch.float32, torch.float64):
+        sc = O.OracleScene(objects, arrays, cfg, dt)
+        f = O.run(sc, T, record_boundaries=True)
+        res[dt] = O.reversible_gradient(sc, f, cots(f), None if cot_E is None else cot_E(f),
+                                        None if cot_H is None else cot_H(f), with_mu=True)
+    (e32, m32), (e64, m64) = res[torch.float32], res[torch.float64]
+    err = dict(eps_vs_fp32=rel_l2(ge, e32), eps_vs_fp64=rel_l2(ge, e64), mu_vs_fp32=rel_l2(gm, m32),
+               mu_vs_fp64=rel_l2(gm, m64), fp32_oracle_mu_vs_fp64=rel_l2(m32, m64))
+    log_result(name, **err)
+    assert torch.linalg.vector_norm(m64).item() > 0
+    assert err["eps_vs_fp32"] <= GTOL and err["mu_vs_fp32"] <= GTOL, err
+
+
+@pytest.mark.parametrize("permeability", [1.5, (1.5, 1.2, 2.0)])
+def test_adjoint_inv_mu_periodic_magnetic_slab(permeability):
+    """d/d inv_permeabilities (cot[6] of the reference's custom VJP, fdtd.py:331) with magnetic
+    conductivity, isotropic (n_mu 1) and diagonal (n_mu 3); loss sum(E^2) + sum(H^2)."""
+    n, dx = 8, 50e-9
+    cfg = fx.SimulationConfig(time=30e-15, grid=fx.UniformGrid(dx),
+                              gradient_config=fx.GradientConfig(recorder=fx.Recorder()))
+    vol = fx.SimulationVolume(shape=(n, n, n))
+    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(4, "periodic"),
+                                                        vol).values())
+    objs.append(fx.UniformMaterialObject(
+        name="slab", grid_slice_tuple=((0, n), (0, n), (n // 4, n // 4 + n // 2)),
+        material=fx.Material(permittivity=2.0, permeability=permeability, electric_conductivity=1e2,
+                             magnetic_conductivity=3e7)))
+    objs.append(fx.PointDipoleSource(name="dip", grid_slice_tuple=((n // 2, n // 2 + 1),) * 3, polarization=0,
+                                     wave_character=fx.WaveCharacter(frequency=C0 / 800e-9)))
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    ge, gm = _gpu_grads_eps_mu(objects, arrays, cfg, lambda o: (o.fields.E**2).sum() + (o.fields.H**2).sum())
+    _check_eps_mu(f"adjoint_inv_mu_periodic_n{arrays.inv_permeabilities.shape[0]}", ge, gm, objects, arrays, cfg,
+                  lambda f: {}, cot_E=lambda f: 2 * f.E, cot_H=lambda f: 2 * f.H)
+
+
+def test_adjoint_inv_mu_cpml_detectors():
+    """inv_mu cotangent with CPML (kappa != 1) on all faces, a magnetic block, a TFSF plane source,
+    a phasor detector on E and H components and an energy detector (its 1/inv_mu term)."""
+    dx = 50e-9
+    steps = 70
+    dt = 0.99 / math.sqrt(3) * dx / C0
+    cfg = fx.SimulationConfig(time=steps * dt, grid=fx.UniformGrid(dx),
+                              gradient_config=fx.GradientConfig(recorder=fx.Recorder()))
+    shape, pml = (26, 24, 24), 5
+    vol = fx.SimulationVolume(shape=shape)
+    bc = fx.BoundaryConfig.from_uniform_bound(pml, "pml", kappa_end=1.5)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((10, 16), (9, 15), (9, 15)),
+                                         material=fx.Material(permittivity=3.0, permeability=(1.8, 1.3, 2.2))))
+    wc = fx.WaveCharacter(wavelength=1.55e-6)
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((pml + 1, pml + 2), (pml, shape[1] - pml),
+                                                                    (pml, shape[2] - pml)),
+                                      direction="+", fixed_E_polarization_vector=(0, 1, 0), wave_character=wc,
+                                      temporal_profile=scenes.pulse_5fs()))
+    objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((18, 19), (8, 16), (8, 16)), wave_characters=(wc,),
+                                  components=("Ey", "Hx", "Hz"), scaling_mode="pulse"))
+    objs.append(fx.EnergyDetector(name="en", grid_slice_tuple=((11, 15), (10, 14), (10, 14)), reduce_volume=True))
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    assert arrays.inv_permeabilities.shape[0] == 3
+    w_en = 1e3
+
+    def loss(o):
+        return (o.detector_states["ph"]["phasor"].abs() ** 2).sum() + w_en * o.detector_states["en"]["energy"].sum()
+
+    ge, gm = _gpu_grads_eps_mu(objects, arrays, cfg, loss)
+    _check_eps_mu("adjoint_inv_mu_cpml", ge, gm, objects, arrays, cfg,
+                  lambda f: {"ph": {"phasor": 2 * f.det["ph"]["phasor"]},
+                             "en": {"energy": w_en * torch.ones_like(f.det["en"]["energy"])}})
