@@ -163,6 +163,8 @@ def run_gpu(args):
         scene.tune_tma(True, args.tz, args.ty, args.stages, args.tchunk)
     if args.chunk or args.vec:
         scene.tune(args.chunk, args.vec)
+    if args.shell_chunk or args.shell_vec:
+        scene.tune_shell(args.shell_chunk, args.shell_vec)
     ncell = shape[0] * shape[1] * shape[2]
     W, K = args.warmup, args.steps
     if W + K + 8 > T_TOTAL:
@@ -558,6 +560,8 @@ def main():
     ap.add_argument("--shape", default="", help="grid override nx,ny,nz (profiling cases)")
     ap.add_argument("--chunk", type=int, default=0, help="x planes per update block (0: plan default)")
     ap.add_argument("--vec", type=int, default=0, help="z cells per thread (0: plan default)")
+    ap.add_argument("--shell-chunk", type=int, default=0, help="x planes per CPML shell block (0: plan default)")
+    ap.add_argument("--shell-vec", type=int, default=0, help="z cells per CPML shell thread (0: plan default)")
     ap.add_argument("--tma", default="auto", choices=["auto", "0", "1"], help="TMA-pipelined update kernels")
     ap.add_argument("--tz", type=int, default=0)
     ap.add_argument("--ty", type=int, default=0)

@@ -157,6 +157,7 @@ SIGNATURES = {
     ),
     "fdtd_launches_per_step": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "fdtd_plan_tune_shell": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "fdtd_plan_chunk": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_vec": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_tune_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),

@@ -69,6 +69,12 @@ struct UpdArgs {
     int nbox;
     int blo[6][3], bhi[6][3], bchunk[6], nbx[6], bstart[7];
     int bslab[6];               // per box: bit s set when slab s can reach the box or its one-cell rim
+    // per-axis slab table, valid when axt = 1 (every face holds at most one slab and the two
+    // slabs of an axis do not overlap): the slab on each axis' low / high face (L = 0: none)
+    // and its psi pair, so a cell's CPML terms are found with compile-time axes
+    int axt;
+    DSlab axs[3][2];
+    float* axp[3][2][2];
     const int* tp;              // device time-step counter
     int n_fuse;
     DFuse fuse[kMaxFuse];

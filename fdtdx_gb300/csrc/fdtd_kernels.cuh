@@ -80,6 +80,84 @@ __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k
     }
 }
 
+// ---------------------------------------------------------------------------------
+// The same CPML terms through the per-axis slab table (UpdArgs::axt): the axis of every
+// term is a compile-time constant, a cell lies in at most one slab per axis, and a psi
+// offset is two 32-bit multiply-adds.  The y and z lookups of a column are fixed along
+// the x-march (AxCol); the x lookup is made per plane.
+// ---------------------------------------------------------------------------------
+template <int AX>
+__device__ __forceinline__ int ax_find(const UpdArgs& a, int x, int& l) {
+    l = x - a.axs[AX][0].lo;
+    if ((unsigned)l < (unsigned)a.axs[AX][0].L) return 0;
+    l = x - a.axs[AX][1].lo;
+    if ((unsigned)l < (unsigned)a.axs[AX][1].L) return 1;
+    return -1;
+}
+
+// Offset of (i, j, k) in a slab's psi array for a slab on axis AX (lo, dims sy, sz).
+template <int AX>
+__device__ __forceinline__ int ax_off(int lo, int sy, int sz, int i, int j, int k) {
+    if (AX == 0) return ((i - lo) * sy + j) * sz + k;
+    if (AX == 1) return (i * sy + (j - lo)) * sz + k;
+    return (i * sy + j) * sz + (k - lo);
+}
+
+template <int VEC>
+struct AxCol {
+    int ys, yl;             // y face of the column (0 / 1, -1: none) and its layer
+    int zs[VEC], zl[VEC];   // z face and layer of each of its cells
+};
+
+template <int VEC>
+__device__ __forceinline__ void ax_column(const UpdArgs& a, int j, int k0, AxCol<VEC>& c) {
+    c.ys = ax_find<1>(a, j, c.yl);
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) c.zs[e] = ax_find<2>(a, k0 + e, c.zl[e]);
+}
+
+// Field-wise selection of the slab on face `side` (0 / 1) of axis AX: the table is read
+// with static indices only.
+#define FDTD_AX_SEL(AX, side, f) ((side) ? a.axs[AX][1].f : a.axs[AX][0].f)
+#define FDTD_AX_PSI(AX, side, q) ((side) ? a.axp[AX][1][q] : a.axp[AX][0][q])
+
+// psi pair of the slab on face `side` of axis AX at (i, j, k) (zero when side < 0).
+template <int AX>
+__device__ __forceinline__ float2 ax_psi(const UpdArgs& a, int side, int i, int j, int k) {
+    if (side < 0) return make_float2(0.f, 0.f);
+    const int o = ax_off<AX>(FDTD_AX_SEL(AX, side, lo), FDTD_AX_SEL(AX, side, sy), FDTD_AX_SEL(AX, side, sz), i, j, k);
+    return make_float2(FDTD_AX_PSI(AX, side, 0)[o], FDTD_AX_PSI(AX, side, 1)[o]);
+}
+
+// One slab's CPML term at a cell (cpml_apply for the slab on face `side` of axis AX).
+template <bool REV, bool HSIDE, int AX>
+__device__ __forceinline__ void ax_term(const UpdArgs& a, int side, int l, int i, int j, int k, const float d[6],
+                                        float cu[3], float2 pv) {
+    if (side < 0) return;
+    const int L = FDTD_AX_SEL(AX, side, L);
+    const float d1 = AX == 0 ? d[3] : (AX == 1 ? d[5] : d[1]);
+    const float d2 = AX == 0 ? d[4] : (AX == 1 ? d[0] : d[2]);
+    const float* co = FDTD_AX_SEL(AX, side, coef) + (HSIDE ? 3 * L : 0);
+    float p1 = pv.x, p2 = pv.y;
+    if (!REV) {
+        const float ca = __ldg(co + l), cb = __ldg(co + L + l);
+        p1 = cb * p1 + ca * d1;
+        p2 = cb * p2 + ca * d2;
+        const int o = ax_off<AX>(FDTD_AX_SEL(AX, side, lo), FDTD_AX_SEL(AX, side, sy), FDTD_AX_SEL(AX, side, sz), i, j, k);
+        FDTD_AX_PSI(AX, side, 0)[o] = p1;
+        FDTD_AX_PSI(AX, side, 1)[o] = p2;
+    }
+    float c1 = p1, c2 = p2;
+    if (!FDTD_AX_SEL(AX, side, kappa_one)) {
+        const float ikm1 = __ldg(co + 2 * L + l) - 1.f;
+        c1 = ikm1 * d1 + p1;
+        c2 = ikm1 * d2 + p2;
+    }
+    if (AX == 0) { cu[1] -= c1; cu[2] += c2; }
+    else if (AX == 1) { cu[2] -= c1; cu[0] += c2; }
+    else { cu[0] -= c1; cu[1] += c2; }
+}
+
 // Neighbour on one axis with the halo rule (wrap on a periodic axis, else zero).
 __device__ __forceinline__ float nb(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp, int i,
                                     int j, int k) {
@@ -247,7 +325,7 @@ __device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i
 // E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
 // reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
 // ---------------------------------------------------------------------------------
-template <bool REV, int VEC, bool PML>
+template <bool REV, int VEC, bool PML, bool AXT = false>
 __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
@@ -255,7 +333,9 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     const long long N = g.N;
     const long long sy = g.nz;
     const float* __restrict__ H = a.F;
-    const int col = PML && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
+    const int col = PML && !AXT && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
+    AxCol<VEC> axc;
+    if (AXT) ax_column<VEC>(a, j, k0, axc);
     Vec<VEC> Hy_m = ldv_halo<VEC>(g, H, 1, i0 - 1, j, k0);
     Vec<VEC> Hz_m = ldv_halo<VEC>(g, H, 2, i0 - 1, j, k0);
     for (int i = i0; i < i1; ++i) {
@@ -287,6 +367,17 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e], act);
         }
+        int xs = -1, xl = 0;
+        float2 px[VEC], py[VEC], pz[VEC];
+        if (AXT) {
+            xs = ax_find<0>(a, i, xl);
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                px[e] = ax_psi<0>(a, xs, i, j, k0 + e);
+                py[e] = ax_psi<1>(a, axc.ys, i, j, k0 + e);
+                pz[e] = ax_psi<2>(a, axc.zs[e], i, j, k0 + e);
+            }
+        }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
             const int k = k0 + e;
@@ -296,6 +387,11 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
                                 Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
             float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
             if (pml) cpml_apply<REV, false>(a, i, j, k, d, cu, pre[e], act);
+            if (AXT) {
+                ax_term<REV, false, 0>(a, xs, xl, i, j, k, d, cu, px[e]);
+                ax_term<REV, false, 1>(a, axc.ys, axc.yl, i, j, k, d, cu, py[e]);
+                ax_term<REV, false, 2>(a, axc.zs[e], axc.zl[e], i, j, k, d, cu, pz[e]);
+            }
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
@@ -311,9 +407,9 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     }
 }
 
-template <bool REV, int VEC, bool PML>
+template <bool REV, int VEC, bool PML, bool AXT = false>
 __global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
-    update_E_body<REV, VEC, PML>(a, blockIdx.x);
+    update_E_body<REV, VEC, PML, AXT>(a, blockIdx.x);
 }
 
 // Accumulates the fused E-only detectors at cell (i, j, k) from the E values the H
@@ -382,7 +478,7 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
 // Marches along +x keeping E(i+1) (the next iteration's E(i)) and Ex(i-1) in registers;
 // fused E-only detectors are accumulated in the same pass (forward only).
 // ---------------------------------------------------------------------------------
-template <bool REV, int VEC, bool PML>
+template <bool REV, int VEC, bool PML, bool AXT = false>
 __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
@@ -391,7 +487,9 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     const long long sy = g.nz, sx = (long long)g.ny * g.nz;
     const float* __restrict__ E = a.F;
     const bool kin = k0 + VEC < g.nz;
-    const int col = PML && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
+    const int col = PML && !AXT && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
+    AxCol<VEC> axc;
+    if (AXT) ax_column<VEC>(a, j, k0, axc);
 
     int slot[kMaxFuse];
     float2 w[kMaxFuse][kMaxFuseFreq];
@@ -449,6 +547,17 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) psi_fetch(a, i, j, k0 + e, pre[e], act);
         }
+        int xs = -1, xl = 0;
+        float2 px[VEC], py[VEC], pz[VEC];
+        if (AXT) {
+            xs = ax_find<0>(a, i, xl);
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+                px[e] = ax_psi<0>(a, xs, i, j, k0 + e);
+                py[e] = ax_psi<1>(a, axc.ys, i, j, k0 + e);
+                pz[e] = ax_psi<2>(a, axc.zs[e], i, j, k0 + e);
+            }
+        }
         Vec<VEC> Ey_jm{};
         float Eyk_jm = 0.f;
         if (!REV && any) {
@@ -488,6 +597,11 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
                                 Ez_ip.v[e] - Ez.v[e], Ey_ip.v[e] - Ey.v[e], Ex_jp.v[e] - Ex.v[e]};
             float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
             if (pml) cpml_apply<REV, true>(a, i, j, k, d, cu, pre[e], act);
+            if (AXT) {
+                ax_term<REV, true, 0>(a, xs, xl, i, j, k, d, cu, px[e]);
+                ax_term<REV, true, 1>(a, axc.ys, axc.yl, i, j, k, d, cu, py[e]);
+                ax_term<REV, true, 2>(a, axc.zs[e], axc.zl[e], i, j, k, d, cu, pz[e]);
+            }
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* sp = a.sig ? a.sig + (a.n_sig == 3 ? comp * N : 0) : nullptr;
@@ -511,9 +625,9 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     }
 }
 
-template <bool REV, int VEC, bool PML>
+template <bool REV, int VEC, bool PML, bool AXT = false>
 __global__ void __launch_bounds__(256, 3) k_update_H(const __grid_constant__ UpdArgs a) {
-    update_H_body<REV, VEC, PML>(a, blockIdx.x);
+    update_H_body<REV, VEC, PML, AXT>(a, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------------

@@ -34,6 +34,8 @@ struct FdtdPlan {
     int n_fused = 0;
     int chunk = 1;                        // x planes per update block
     int vec = 1;                          // z cells per thread (4, 2 or 1: nz % vec == 0)
+    int shell_chunk = 4;                  // the same two for the CPML shell boxes of a split grid
+    int shell_vec = 1;
     int sm_count = 1;
     // TMA-pipelined update kernels (non-periodic scenes with nz % 4 == 0)
     bool tma_ok = false;                  // the scene admits the TMA kernels
@@ -671,6 +673,18 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
     const long long blocks = fill_boxes(p, a, boxes, chunks, n, vec);
     if (blocks <= 0) return;
     const dim3 grid((unsigned)blocks, 1, 1);
+    if (PML && a.axt) {  // CPML terms through the per-axis slab table
+        if (HSIDE) {
+            if (vec == 2) k_update_H<REV, 2, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+            else if (vec == 1) k_update_H<REV, 1, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+            else k_update_H<REV, 4, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+        } else {
+            if (vec == 2) k_update_E<REV, 2, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+            else if (vec == 1) k_update_E<REV, 1, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+            else k_update_E<REV, 4, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+        }
+        return;
+    }
     if (HSIDE) {
         if (vec == 4) k_update_H<REV, 4, PML><<<grid, kUpdBlock, 0, st>>>(a);
         else if (vec == 2) k_update_H<REV, 2, PML><<<grid, kUpdBlock, 0, st>>>(a);
@@ -697,10 +711,11 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
     if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
     if (mid) cudaEventRecord(mid, st);
     int chunks[6];
-    for (int q = 0; q < sp.n_shell; ++q) chunks[q] = kShellChunk;
-    // the H shell runs one z cell per thread: half the registers per thread, more warps in
-    // flight for its latency-bound CPML and phasor loads (measured 14% faster than two)
-    launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st, HSIDE ? 1 : 0);
+    for (int q = 0; q < sp.n_shell; ++q) chunks[q] = p->shell_chunk;
+    // the shells run one z cell per thread by default: fewer registers per thread, more
+    // warps in flight for their latency-bound CPML and phasor loads (measured 14% (H) and
+    // 24% (E) faster than two)
+    launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st, p->shell_vec);
 }
 
 int half_step_launches(const FdtdPlan* p) {
@@ -732,6 +747,22 @@ UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const floa
         a.slab[s] = p->slab[s];
         a.psi1[s] = eside ? b->psi_E[s][0] : b->psi_H[s][0];
         a.psi2[s] = eside ? b->psi_E[s][1] : b->psi_H[s][1];
+    }
+    // per-axis slab table: one slab per face, the two slabs of an axis disjoint
+    a.axt = 1;
+    for (int s = 0; s < p->d.n_slabs && a.axt; ++s) {
+        const DSlab& sl = p->slab[s];
+        const int side = p->d.slabs[s].direction > 0 ? 1 : 0;
+        if (a.axs[sl.axis][side].L) { a.axt = 0; break; }
+        a.axs[sl.axis][side] = sl;
+        a.axp[sl.axis][side][0] = a.psi1[s];
+        a.axp[sl.axis][side][1] = a.psi2[s];
+        if ((long long)sl.sx * sl.sy * sl.sz >= (1LL << 31)) a.axt = 0;  // 32-bit psi offsets
+    }
+    for (int x = 0; x < 3 && a.axt; ++x) {
+        const DSlab& lo = a.axs[x][0];
+        const DSlab& hi = a.axs[x][1];
+        if (lo.L && hi.L && lo.lo < hi.lo + hi.L && hi.lo < lo.lo + lo.L) a.axt = 0;
     }
     a.chunk = p->chunk;
     a.tp = p->d_t;
@@ -1039,6 +1070,22 @@ extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk, int32_t vec) {
     if (chunk != p->chunk || vec != p->vec) {
         p->chunk = chunk;
         p->vec = vec;
+        if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+        if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+        p->gsteps = 0;
+    }
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_plan_tune_shell(FdtdPlan* p, int32_t chunk, int32_t vec) {
+    if (!p) return FDTD_EINVAL;
+    if (chunk <= 0) chunk = kShellChunk;
+    if (vec <= 0) vec = 1;
+    if ((vec != 1 && vec != 2 && vec != 4) || (vec > 1 && p->g.nz % 4))
+        return fail(p, FDTD_EINVAL, "shell vec must be 1, or 2 / 4 with nz % 4 == 0");
+    if (chunk != p->shell_chunk || vec != p->shell_vec) {
+        p->shell_chunk = chunk;
+        p->shell_vec = vec;
         if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
         if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
         p->gsteps = 0;

@@ -394,6 +394,10 @@ class Scene:
         """Launch shape of the register-queue update kernels (0 keeps the default)."""
         N.check(N.load().fdtd_plan_tune(self.plan, int(chunk), int(vec)), self.plan, "fdtd_plan_tune")
 
+    def tune_shell(self, chunk: int = 0, vec: int = 0) -> None:
+        """x planes per block and z cells per thread of the CPML shell kernels (0: default)."""
+        N.check(N.load().fdtd_plan_tune_shell(self.plan, int(chunk), int(vec)), self.plan, "fdtd_plan_tune_shell")
+
     def tune_tma(self, enable: bool = True, tz: int = 0, ty: int = 0, stages: int = 0, chunk: int = 0) -> None:
         """Select the TMA-pipelined update kernels and their tile (0 keeps a default)."""
         N.check(N.load().fdtd_plan_tune_tma(self.plan, 1 if enable else 0, int(tz), int(ty), int(stages), int(chunk)),

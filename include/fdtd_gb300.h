@@ -218,6 +218,10 @@ int fdtd_adjoint(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffe
 int fdtd_plan_tune(FdtdPlan* plan, int32_t chunk, int32_t vec);
 int32_t fdtd_plan_chunk(const FdtdPlan* plan);
 int32_t fdtd_plan_vec(const FdtdPlan* plan);
+/* The same for the CPML shell boxes of a grid split into a slab-free core and its shell:
+ * `chunk` x planes per block (default 4), `vec` z cells per thread (default 1; 2 or 4 need
+ * nz % 4 == 0).  Invalidates a cached CUDA graph. */
+int fdtd_plan_tune_shell(FdtdPlan* plan, int32_t chunk, int32_t vec);
 
 /* Selects the TMA-pipelined update kernels (enable=1; scenes without periodic axes and
  * with nz % 4 == 0) or the register-queue kernels (enable=0), with a (y, z) tile of
