@@ -223,6 +223,41 @@ __device__ __forceinline__ Vec<VEC> nbv(const Geo& g, const float* __restrict__ 
     return inside ? ldv<VEC>(f + off) : ldv_halo<VEC>(g, f, comp, i, j, k0);
 }
 
+// The halo loads with the halo rule fixed at compile time: ZH (zero halo, no periodic
+// axis) reduces a neighbour outside the grid to a bounds test.
+template <bool ZH>
+__device__ __forceinline__ float ld_halo_t(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k) {
+    if (!ZH) return ld_halo(g, f, comp, i, j, k);
+    const bool in = (unsigned)i < (unsigned)g.nx && (unsigned)j < (unsigned)g.ny && (unsigned)k < (unsigned)g.nz;
+    return in ? __ldg(f + comp * g.N + cell_index(g, i, j, k)) : 0.f;
+}
+
+template <bool ZH>
+__device__ __forceinline__ float nb_t(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp,
+                                      int i, int j, int k) {
+    if (!ZH) return nb(g, f, off, inside, comp, i, j, k);
+    return inside ? __ldg(f + off) : 0.f;
+}
+
+template <int VEC, bool ZH>
+__device__ __forceinline__ Vec<VEC> ldv_halo_t(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k0) {
+    Vec<VEC> r;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) r.v[e] = ld_halo_t<ZH>(g, f, comp, i, j, k0 + e);
+    return r;
+}
+
+template <int VEC, bool ZH>
+__device__ __forceinline__ Vec<VEC> nbv_t(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp,
+                                          int i, int j, int k0) {
+    if (!ZH) return nbv<VEC>(g, f, off, inside, comp, i, j, k0);
+    if (inside) return ldv<VEC>(f + off);
+    Vec<VEC> z;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) z.v[e] = 0.f;
+    return z;
+}
+
 // Whether (i, j, k0 .. k0+VEC-1) can lie in any CPML slab.
 __device__ __forceinline__ bool maybe_slab(const UpdArgs& a, int i, int j, int k0, int vec) {
     const int idx[3] = {i, j, k0};
@@ -325,8 +360,9 @@ __device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i
 // E half-step: E <- (f E + c curl_H(H) inv_eps) / d  (fdtdx/fdtd/update.py:281-354)
 // reverse:     E <- (E (1+q) - c curl_H(H) inv_eps) / (1-q)  (update.py:586-609)
 // ---------------------------------------------------------------------------------
-template <bool REV, int VEC, bool PML, bool AXT = false>
+template <bool REV, int VEC, bool PML, int AXT = 0>
 __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
+    constexpr bool ZH = AXT == 2;
     const Geo& g = a.g;
     int j, k0, i0, i1;
     if (!column_of<VEC>(a, j, k0, i0, i1, blk)) return;
@@ -336,15 +372,15 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     const int col = PML && !AXT && a.n_slab > 0 ? column_slabs(a, box_slab_mask_of(a, blk < 0 ? (int)blockIdx.x : blk), j, k0, VEC) : 0;
     AxCol<VEC> axc;
     if (AXT) ax_column<VEC>(a, j, k0, axc);
-    Vec<VEC> Hy_m = ldv_halo<VEC>(g, H, 1, i0 - 1, j, k0);
-    Vec<VEC> Hz_m = ldv_halo<VEC>(g, H, 2, i0 - 1, j, k0);
+    Vec<VEC> Hy_m = ldv_halo_t<VEC, ZH>(g, H, 1, i0 - 1, j, k0);
+    Vec<VEC> Hz_m = ldv_halo_t<VEC, ZH>(g, H, 2, i0 - 1, j, k0);
     for (int i = i0; i < i1; ++i) {
         const long long c = cell_index(g, i, j, k0);
         const Vec<VEC> Hx = ldv<VEC>(H + c), Hy = ldv<VEC>(H + N + c), Hz = ldv<VEC>(H + 2 * N + c);
-        const Vec<VEC> Hz_jm = nbv<VEC>(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k0);
-        const Vec<VEC> Hx_jm = nbv<VEC>(g, H, c - sy, j > 0, 0, i, j - 1, k0);
-        const float Hy_k = nb(g, H, N + c - 1, k0 > 0, 1, i, j, k0 - 1);   // z neighbour below the vector
-        const float Hx_k = nb(g, H, c - 1, k0 > 0, 0, i, j, k0 - 1);
+        const Vec<VEC> Hz_jm = nbv_t<VEC, ZH>(g, H, 2 * N + c - sy, j > 0, 2, i, j - 1, k0);
+        const Vec<VEC> Hx_jm = nbv_t<VEC, ZH>(g, H, c - sy, j > 0, 0, i, j - 1, k0);
+        const float Hy_k = nb_t<ZH>(g, H, N + c - 1, k0 > 0, 1, i, j, k0 - 1);   // z neighbour below the vector
+        const float Hx_k = nb_t<ZH>(g, H, c - 1, k0 > 0, 0, i, j, k0 - 1);
         Vec<VEC> ie[3];
         if (a.mat) {
 #pragma unroll
@@ -407,8 +443,8 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
     }
 }
 
-template <bool REV, int VEC, bool PML, bool AXT = false>
-__global__ void __launch_bounds__(256) k_update_E(const __grid_constant__ UpdArgs a) {
+template <bool REV, int VEC, bool PML, int AXT = 0>
+__global__ void __launch_bounds__(256, AXT && VEC == 1 ? 4 : 1) k_update_E(const __grid_constant__ UpdArgs a) {
     update_E_body<REV, VEC, PML, AXT>(a, blockIdx.x);
 }
 
@@ -478,8 +514,9 @@ __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot
 // Marches along +x keeping E(i+1) (the next iteration's E(i)) and Ex(i-1) in registers;
 // fused E-only detectors are accumulated in the same pass (forward only).
 // ---------------------------------------------------------------------------------
-template <bool REV, int VEC, bool PML, bool AXT = false>
+template <bool REV, int VEC, bool PML, int AXT = 0>
 __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
+    constexpr bool ZH = AXT == 2;
     const Geo& g = a.g;
     int j, k0, i0, i1;
     if (!column_of<VEC>(a, j, k0, i0, i1, blk)) return;
@@ -513,18 +550,18 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     Vec<VEC> Ex_im{};
     float Exk_im = 0.f;
     if (any) {
-        Ex_im = ldv_halo<VEC>(g, E, 0, i0 - 1, j, k0);
-        Exk_im = ld_halo(g, E, 0, i0 - 1, j, k0 + VEC);
+        Ex_im = ldv_halo_t<VEC, ZH>(g, E, 0, i0 - 1, j, k0);
+        Exk_im = ld_halo_t<ZH>(g, E, 0, i0 - 1, j, k0 + VEC);
     }
     for (int i = i0; i < i1; ++i) {
         const long long c = cell_index(g, i, j, k0);
         const Vec<VEC> Ex = ldv<VEC>(E + c);
-        const Vec<VEC> Ey_ip = nbv<VEC>(g, E, N + c + sx, i < g.nx - 1, 1, i + 1, j, k0);
-        const Vec<VEC> Ez_ip = nbv<VEC>(g, E, 2 * N + c + sx, i < g.nx - 1, 2, i + 1, j, k0);
-        const Vec<VEC> Ez_jp = nbv<VEC>(g, E, 2 * N + c + sy, j < g.ny - 1, 2, i, j + 1, k0);
-        const Vec<VEC> Ex_jp = nbv<VEC>(g, E, c + sy, j < g.ny - 1, 0, i, j + 1, k0);
-        const float Ey_k = nb(g, E, N + c + VEC, kin, 1, i, j, k0 + VEC);  // z neighbour above the vector
-        const float Ex_k = nb(g, E, c + VEC, kin, 0, i, j, k0 + VEC);
+        const Vec<VEC> Ey_ip = nbv_t<VEC, ZH>(g, E, N + c + sx, i < g.nx - 1, 1, i + 1, j, k0);
+        const Vec<VEC> Ez_ip = nbv_t<VEC, ZH>(g, E, 2 * N + c + sx, i < g.nx - 1, 2, i + 1, j, k0);
+        const Vec<VEC> Ez_jp = nbv_t<VEC, ZH>(g, E, 2 * N + c + sy, j < g.ny - 1, 2, i, j + 1, k0);
+        const Vec<VEC> Ex_jp = nbv_t<VEC, ZH>(g, E, c + sy, j < g.ny - 1, 0, i, j + 1, k0);
+        const float Ey_k = nb_t<ZH>(g, E, N + c + VEC, kin, 1, i, j, k0 + VEC);  // z neighbour above the vector
+        const float Ex_k = nb_t<ZH>(g, E, c + VEC, kin, 0, i, j, k0 + VEC);
         Vec<VEC> im[3];
         if (a.mat) {
 #pragma unroll
@@ -561,8 +598,8 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
         Vec<VEC> Ey_jm{};
         float Eyk_jm = 0.f;
         if (!REV && any) {
-            Ey_jm = nbv<VEC>(g, E, N + c - sy, j > 0, 1, i, j - 1, k0);
-            Eyk_jm = ld_halo(g, E, 1, i, j - 1, k0 + VEC);
+            Ey_jm = nbv_t<VEC, ZH>(g, E, N + c - sy, j > 0, 1, i, j - 1, k0);
+            Eyk_jm = ld_halo_t<ZH>(g, E, 1, i, j - 1, k0 + VEC);
         }
         // the first fused phasor's previous values (one frequency), loaded with the fields so
         // its read-modify-write does not add a second round trip after the update
@@ -625,8 +662,8 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     }
 }
 
-template <bool REV, int VEC, bool PML, bool AXT = false>
-__global__ void __launch_bounds__(256, 3) k_update_H(const __grid_constant__ UpdArgs a) {
+template <bool REV, int VEC, bool PML, int AXT = 0>
+__global__ void __launch_bounds__(256, AXT && VEC == 1 ? 4 : 3) k_update_H(const __grid_constant__ UpdArgs a) {
     update_H_body<REV, VEC, PML, AXT>(a, blockIdx.x);
 }
 

@@ -673,15 +673,21 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
     const long long blocks = fill_boxes(p, a, boxes, chunks, n, vec);
     if (blocks <= 0) return;
     const dim3 grid((unsigned)blocks, 1, 1);
-    if (PML && a.axt) {  // CPML terms through the per-axis slab table
-        if (HSIDE) {
-            if (vec == 2) k_update_H<REV, 2, true, true><<<grid, kUpdBlock, 0, st>>>(a);
-            else if (vec == 1) k_update_H<REV, 1, true, true><<<grid, kUpdBlock, 0, st>>>(a);
-            else k_update_H<REV, 4, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+    if (PML && a.axt && vec <= 2) {  // CPML terms through the per-axis slab table
+        if (a.axt == 2) {            // no periodic axis: zero-halo neighbour loads
+            if (HSIDE) {
+                if (vec == 2) k_update_H<REV, 2, true, 2><<<grid, kUpdBlock, 0, st>>>(a);
+                else k_update_H<REV, 1, true, 2><<<grid, kUpdBlock, 0, st>>>(a);
+            } else {
+                if (vec == 2) k_update_E<REV, 2, true, 2><<<grid, kUpdBlock, 0, st>>>(a);
+                else k_update_E<REV, 1, true, 2><<<grid, kUpdBlock, 0, st>>>(a);
+            }
+        } else if (HSIDE) {
+            if (vec == 2) k_update_H<REV, 2, true, 1><<<grid, kUpdBlock, 0, st>>>(a);
+            else k_update_H<REV, 1, true, 1><<<grid, kUpdBlock, 0, st>>>(a);
         } else {
-            if (vec == 2) k_update_E<REV, 2, true, true><<<grid, kUpdBlock, 0, st>>>(a);
-            else if (vec == 1) k_update_E<REV, 1, true, true><<<grid, kUpdBlock, 0, st>>>(a);
-            else k_update_E<REV, 4, true, true><<<grid, kUpdBlock, 0, st>>>(a);
+            if (vec == 2) k_update_E<REV, 2, true, 1><<<grid, kUpdBlock, 0, st>>>(a);
+            else k_update_E<REV, 1, true, 1><<<grid, kUpdBlock, 0, st>>>(a);
         }
         return;
     }
@@ -764,6 +770,7 @@ UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const floa
         const DSlab& hi = a.axs[x][1];
         if (lo.L && hi.L && lo.lo < hi.lo + hi.L && hi.lo < lo.lo + lo.L) a.axt = 0;
     }
+    if (a.axt && !p->g.px && !p->g.py && !p->g.pz) a.axt = 2;  // and a zero halo on every axis
     a.chunk = p->chunk;
     a.tp = p->d_t;
     a.n_fuse = 0;
