@@ -344,13 +344,14 @@ __device__ __forceinline__ bool column_of(const Args& a, int& j, int& k0, int& i
         }
     }
     const int lb = b - start;
-    const int bx = lb % nbx, by = lb / nbx;
+    const int by = lb / nbx, bx = lb - by * nbx;
     const int nq = (hi2 - lo2) / VEC;
-    const long long q = (long long)bx * blockDim.x + threadIdx.x;
-    if (q >= (long long)(hi1 - lo1) * nq) return false;
-    const int jj = (int)(q / nq);
+    // 32-bit column index: a y-z plane holds fewer than 2^31 cells (checked at plan creation)
+    const int q = bx * (int)blockDim.x + (int)threadIdx.x;
+    if (q >= (hi1 - lo1) * nq) return false;
+    const int jj = q / nq;
     j = lo1 + jj;
-    k0 = lo2 + (int)(q - (long long)jj * nq) * VEC;
+    k0 = lo2 + (q - jj * nq) * VEC;
     i0 = lo0 + by * chunk;
     i1 = min(i0 + chunk, hi0);
     return i0 < i1;
