@@ -454,14 +454,16 @@ __global__ void __launch_bounds__(256, AXT && VEC == 1 ? 4 : 1) k_update_E(const
 // Ex <- (avg_x(Ex)(k) + avg_x(Ex)(k+1)) / 2, Ey <- (avg_y(Ey)(k) + avg_y(Ey)(k+1)) / 2, Ez.
 // `staged` (optional) points at this cell's previous phasor values of detector 0 in a
 // shared-memory tile (complex planes `staged_stride` floats apart), so the read half of
-// its read-modify-write comes from the TMA pipeline instead of HBM.
+// its read-modify-write comes from the TMA pipeline instead of HBM.  Detectors before `q0`
+// are left to the caller.
 __device__ __forceinline__ void fused_detectors(const UpdArgs& a, const int slot[kMaxFuse],
                                                 const float2 w[kMaxFuse][kMaxFuseFreq], int i, int j, int k,
                                                 float Ex, float Ex_kp, float Ex_im, float Exkp_im, float Ey, float Ey_kp,
                                                 float Ey_jm, float Eykp_jm, float Ez, const float* staged = nullptr,
-                                                int staged_stride = 0, const float2* pref = nullptr) {
+                                                int staged_stride = 0, const float2* pref = nullptr, int q0 = 0) {
 #pragma unroll
     for (int q = 0; q < kMaxFuse; ++q) {
+        if (q < q0) continue;
         if (q >= a.n_fuse) break;
         if (slot[q] < 0) continue;
         const DFuse& d = a.fuse[q];
@@ -604,8 +606,10 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
         }
         // the first fused phasor's previous values (one frequency), loaded with the fields so
         // its read-modify-write does not add a second round trip after the update
+        // (AXT kernels: its update is made here too, from the same region test and index)
         float2 pf[VEC][3];
-        bool pfo = false;
+        bool pfo = false, pin[VEC];
+        long long pr[VEC];
         if (!REV && a.n_fuse > 0 && slot[0] >= 0 && a.fuse[0].kind == FDTD_DET_PHASOR && a.fuse[0].nfreq == 1) {
             const DFuse& d = a.fuse[0];
             pfo = true;
@@ -616,6 +620,8 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
                 const int k = k0 + e;
                 const bool in = row && k >= d.lo[2] && k < d.hi[2];
                 const long long r = ((long long)(i - d.lo[0]) * d.ry + (j - d.lo[1])) * d.rz + (k - d.lo[2]);
+                pin[e] = in;
+                pr[e] = r;
                 int o = 0;
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
@@ -650,8 +656,38 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
             if (!REV && any) {
                 const float exkp_im = e + 1 < VEC ? Ex_im.v[e + 1] : Exk_im;
                 const float eykp_jm = e + 1 < VEC ? Ey_jm.v[e + 1] : Eyk_jm;
-                fused_detectors(a, slot, w, i, j, k, Ex.v[e], ex_kp, Ex_im.v[e], exkp_im, Ey.v[e], ey_kp, Ey_jm.v[e],
-                                eykp_jm, Ez.v[e], nullptr, 0, pfo ? pf[e] : nullptr);
+                if (AXT && pfo) {  // the first fused phasor, inline
+                    const DFuse& d = a.fuse[0];
+                    if (pin[e]) {
+                        float v[3];
+                        if (d.exact) {
+                            v[0] = (0.5f * (Ex.v[e] + Ex_im.v[e]) + 0.5f * (ex_kp + exkp_im)) / 2.f;
+                            v[1] = (0.5f * (Ey.v[e] + Ey_jm.v[e]) + 0.5f * (ey_kp + eykp_jm)) / 2.f;
+                        } else {
+                            v[0] = Ex.v[e];
+                            v[1] = Ey.v[e];
+                        }
+                        v[2] = Ez.v[e];
+                        float2* st = reinterpret_cast<float2*>(d.state);
+                        const float2 w0 = w[0][0];
+                        int o = 0;
+#pragma unroll
+                        for (int comp = 0; comp < 3; ++comp) {
+                            if (!(d.mask >> comp & 1)) continue;
+                            float2 z = pf[e][comp];
+                            if (d.inverse) { z.x -= v[comp] * w0.x; z.y -= v[comp] * w0.y; }
+                            else { z.x += v[comp] * w0.x; z.y += v[comp] * w0.y; }
+                            st[(long long)o * d.R + pr[e]] = z;
+                            ++o;
+                        }
+                    }
+                    if (a.n_fuse > 1)
+                        fused_detectors(a, slot, w, i, j, k, Ex.v[e], ex_kp, Ex_im.v[e], exkp_im, Ey.v[e], ey_kp,
+                                        Ey_jm.v[e], eykp_jm, Ez.v[e], nullptr, 0, nullptr, 1);
+                } else {
+                    fused_detectors(a, slot, w, i, j, k, Ex.v[e], ex_kp, Ex_im.v[e], exkp_im, Ey.v[e], ey_kp, Ey_jm.v[e],
+                                    eykp_jm, Ez.v[e], nullptr, 0, pfo ? pf[e] : nullptr);
+                }
             }
         }
 #pragma unroll
