@@ -320,8 +320,42 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                     const float Ey_jm = E[(1 * EY + r0 - 1) * EZ + kk];
                     const float Eykp_jm = E[(1 * EY + r0 - 1) * EZ + kk + 1];
                     const float* staged = tc.nd ? E + tc.off_D + ty * 2 * TZ + 2 * cz : nullptr;
-                    fused_detectors(a, slot, w, i, j, k0 + e, Ex, Ex_kp, Exm[e], Exm[e + 1], Ey, Ey_kp, Ey_jm, Eykp_jm,
-                                    Ez, staged, TY * 2 * TZ);
+                    if (staged && a.fuse[0].nfreq == 1 && slot[0] >= 0) {
+                        // the staged phasor (one frequency) inline: its tile row is the cell's
+                        const DFuse& d = a.fuse[0];
+                        const int kc = k0 + e;
+                        if (i >= d.lo[0] && i < d.hi[0] && j >= d.lo[1] && j < d.hi[1] && kc >= d.lo[2] && kc < d.hi[2]) {
+                            float v[3];
+                            if (d.exact) {
+                                v[0] = (0.5f * (Ex + Exm[e]) + 0.5f * (Ex_kp + Exm[e + 1])) / 2.f;
+                                v[1] = (0.5f * (Ey + Ey_jm) + 0.5f * (Ey_kp + Eykp_jm)) / 2.f;
+                            } else {
+                                v[0] = Ex;
+                                v[1] = Ey;
+                            }
+                            v[2] = Ez;
+                            const long long r =
+                                ((long long)(i - d.lo[0]) * d.ry + (j - d.lo[1])) * d.rz + (kc - d.lo[2]);
+                            float2* st = reinterpret_cast<float2*>(d.state);
+                            const float2 w0 = w[0][0];
+                            int o = 0;
+#pragma unroll
+                            for (int comp = 0; comp < 3; ++comp) {
+                                if (!(d.mask >> comp & 1)) continue;
+                                float2 z = make_float2(staged[o * TY * 2 * TZ], staged[o * TY * 2 * TZ + 1]);
+                                if (d.inverse) { z.x -= v[comp] * w0.x; z.y -= v[comp] * w0.y; }
+                                else { z.x += v[comp] * w0.x; z.y += v[comp] * w0.y; }
+                                st[(long long)o * d.R + r] = z;
+                                ++o;
+                            }
+                        }
+                        if (a.n_fuse > 1)
+                            fused_detectors(a, slot, w, i, j, k0 + e, Ex, Ex_kp, Exm[e], Exm[e + 1], Ey, Ey_kp, Ey_jm,
+                                            Eykp_jm, Ez, nullptr, 0, nullptr, 1);
+                    } else {
+                        fused_detectors(a, slot, w, i, j, k0 + e, Ex, Ex_kp, Exm[e], Exm[e + 1], Ey, Ey_kp, Ey_jm,
+                                        Eykp_jm, Ez, staged, TY * 2 * TZ);
+                    }
                 }
             }
 #pragma unroll
