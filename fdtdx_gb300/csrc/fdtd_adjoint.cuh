@@ -76,6 +76,12 @@ struct AdjArgs {
     int blo[6][3], bhi[6][3], bchunk[6], nbx[6], bstart[7];
     int bslab[6];          // per box: bit s set when slab s can reach the box or its one-cell rim
     int ax_slab[3][2];     // the slab on each axis' low / high face (-1: none)
+    // copies of those slabs (L = 0: none) and their arrays, read with static indices by the
+    // fast shell kernels: frozen psi_E, and [H side][axis][face][psi1 / psi2] cotangents
+    DSlab axs[3][2];
+    const float* axpE[3][2][2];
+    const float* axlp[2][3][2][2];
+    float* axlpo[2][3][2][2];
 };
 
 // The slab mask of this block's box.
@@ -430,6 +436,86 @@ __device__ __forceinline__ void slab_term(const AdjArgs& a, int axis, int i, int
             float* o1 = HSIDE ? a.lpH_out[s][1] : a.lpE_out[s][1];
             o0[p] = cb * t1;
             o1[p] = cb * t2;
+        }
+    }
+}
+
+// slab_term for the slab table copies: the axis is a compile-time constant, the slab and
+// its arrays are read with static indices and psi offsets are 32-bit (same arithmetic).
+template <bool HSIDE, int AX>
+__device__ __forceinline__ void slab_term_ax(const AdjArgs& a, int i, int j, int k, float lci, float lcj, bool out,
+                                             float& d1, float& d2) {
+    d1 = 0.f;
+    d2 = 0.f;
+    const int x = AX == 0 ? i : (AX == 1 ? j : k);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const DSlab& sl = a.axs[AX][side];
+        const int l = x - sl.lo;
+        if ((unsigned)l >= (unsigned)sl.L) continue;
+        const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
+        const int p = ax_off<AX>(sl.lo, sl.sy, sl.sz, i, j, k);
+        const float t1 = a.axlp[HSIDE][AX][side][0][p] - lci;
+        const float t2 = a.axlp[HSIDE][AX][side][1][p] + lcj;
+        const float ca = __ldg(co + l);
+        float e1 = ca * t1, e2 = ca * t2;
+        if (!sl.kappa_one) {
+            const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+            e1 -= ikm1 * lci;
+            e2 += ikm1 * lcj;
+        }
+        d1 += e1;
+        d2 += e2;
+        if (out) {
+            const float cb = __ldg(co + sl.L + l);
+            a.axlpo[HSIDE][AX][side][0][p] = cb * t1;
+            a.axlpo[HSIDE][AX][side][1][p] = cb * t2;
+        }
+    }
+}
+
+// axis_terms through the slab table copies, for a grid without periodic axes (zero halo).
+template <bool HSIDE, int VEC, int AX>
+__device__ __forceinline__ void axis_terms_ax(const AdjArgs& a, int i, int j, int k0, Vec<VEC>& lci, Vec<VEC>& lcj,
+                                              bool out) {
+    const Geo& g = a.g;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+        const int kk = k0 + e;
+        if ((unsigned)i >= (unsigned)g.nx || (unsigned)j >= (unsigned)g.ny || (unsigned)kk >= (unsigned)g.nz) continue;
+        float d1, d2;
+        slab_term_ax<HSIDE, AX>(a, i, j, kk, lci.v[e], lcj.v[e], out, d1, d2);
+        lci.v[e] -= d1;
+        lcj.v[e] += d2;
+    }
+}
+
+// curl_H_cpml through the slab table copies.
+__device__ __forceinline__ void curl_H_cpml_ax(const AdjArgs& a, int i, int j, int k, const float d[6], float cu[3]) {
+    const int idx[3] = {i, j, k};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const DSlab& sl = a.axs[ax][side];
+            const int l = idx[ax] - sl.lo;
+            if ((unsigned)l >= (unsigned)sl.L) continue;
+            const float d1 = ax == 0 ? d[3] : (ax == 1 ? d[5] : d[1]);
+            const float d2 = ax == 0 ? d[4] : (ax == 1 ? d[0] : d[2]);
+            const int p = ax == 0 ? ax_off<0>(sl.lo, sl.sy, sl.sz, i, j, k)
+                                  : (ax == 1 ? ax_off<1>(sl.lo, sl.sy, sl.sz, i, j, k) : ax_off<2>(sl.lo, sl.sy, sl.sz, i, j, k));
+            const float* co = sl.coef;
+            const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
+            float c1 = cb * __ldg(a.axpE[ax][side][0] + p) + ca * d1;
+            float c2 = cb * __ldg(a.axpE[ax][side][1] + p) + ca * d2;
+            if (!sl.kappa_one) {
+                const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+                c1 += ikm1 * d1;
+                c2 += ikm1 * d2;
+            }
+            if (ax == 0) { cu[1] -= c1; cu[2] += c2; }
+            else if (ax == 1) { cu[2] -= c1; cu[0] += c2; }
+            else { cu[0] -= c1; cu[1] += c2; }
         }
     }
 }
@@ -887,7 +973,7 @@ __device__ __forceinline__ Vec<VEC> vzero() {
 }
 
 template <int VEC>
-__global__ void __launch_bounds__(256) k_adj_H_shell_s(const __grid_constant__ AdjArgs a) {
+__global__ void __launch_bounds__(256, VEC == 1 ? 4 : 1) k_adj_H_shell_s(const __grid_constant__ AdjArgs a) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
     if (!column_of<VEC>(a, j, k0, i0, i1)) return;
@@ -902,7 +988,7 @@ __global__ void __launch_bounds__(256) k_adj_H_shell_s(const __grid_constant__ A
     if (i0 > 0) {
         y_m = vscale<VEC>(ldv<VEC>(lH + N - sx), s);
         z_m = vscale<VEC>(ldv<VEC>(lH + 2 * N - sx), s);
-        axis_terms<true, VEC>(a, 0, i0 - 1, j, k0, y_m, z_m, false);
+        axis_terms_ax<true, VEC, 0>(a, i0 - 1, j, k0, y_m, z_m, false);
     }
     for (int i = i0; i < i1; ++i, lH += sx, lE += sx) {
         const Vec<VEC> x = vscale<VEC>(ldv<VEC>(lH), s), y = vscale<VEC>(ldv<VEC>(lH + N), s);
@@ -916,11 +1002,11 @@ __global__ void __launch_bounds__(256) k_adj_H_shell_s(const __grid_constant__ A
         x_km.v[0] = km ? s * __ldg(lH - 1) : 0.f;
         y_km.v[0] = km ? s * __ldg(lH + N - 1) : 0.f;
         Vec<VEC> l1x = y, l2x = z, l2y = z, l0y = x, l0z = x, l1z = y;
-        axis_terms<true, VEC>(a, 0, i, j, k0, l1x, l2x, true);
-        axis_terms<true, VEC>(a, 1, i, j, k0, l2y, l0y, true);
-        axis_terms<true, VEC>(a, 2, i, j, k0, l0z, l1z, true);
-        if (jm) axis_terms<true, VEC>(a, 1, i, j - 1, k0, z_jm, x_jm, false);
-        if (km) axis_terms<true, 1>(a, 2, i, j, k0 - 1, x_km, y_km, false);
+        axis_terms_ax<true, VEC, 0>(a, i, j, k0, l1x, l2x, true);
+        axis_terms_ax<true, VEC, 1>(a, i, j, k0, l2y, l0y, true);
+        axis_terms_ax<true, VEC, 2>(a, i, j, k0, l0z, l1z, true);
+        if (jm) axis_terms_ax<true, VEC, 1>(a, i, j - 1, k0, z_jm, x_jm, false);
+        if (km) axis_terms_ax<true, 1, 2>(a, i, j, k0 - 1, x_km, y_km, false);
         Vec<VEC> e0 = ldv_rw<VEC>(lE), e1 = ldv_rw<VEC>(lE + N), e2 = ldv_rw<VEC>(lE + 2 * N);
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
@@ -939,7 +1025,7 @@ __global__ void __launch_bounds__(256) k_adj_H_shell_s(const __grid_constant__ A
 }
 
 template <int VEC>
-__global__ void __launch_bounds__(256) k_adj_E_shell_s(const __grid_constant__ AdjArgs a) {
+__global__ void __launch_bounds__(256, VEC == 1 ? 4 : 1) k_adj_E_shell_s(const __grid_constant__ AdjArgs a) {
     const Geo& g = a.g;
     int j, k0, i0, i1;
     if (!column_of<VEC>(a, j, k0, i0, i1)) return;
@@ -949,7 +1035,6 @@ __global__ void __launch_bounds__(256) k_adj_E_shell_s(const __grid_constant__ A
     const long long mN = a.n_eps == 3 ? N : 0;
     const float cc = g.c;
     const bool jm = j > 0, jp = j + 1 < g.ny, km = k0 > 0, kp = k0 + VEC < g.nz;
-    const int sm = block_slab_mask(a);
     const float* __restrict__ lE = a.lE + c0;
     const float* __restrict__ lH = a.lH + c0;
     const float* __restrict__ ie = a.ie + c0;
@@ -988,12 +1073,12 @@ __global__ void __launch_bounds__(256) k_adj_E_shell_s(const __grid_constant__ A
         // effective cotangents per axis (centre: psi cotangents of step t written)
         Vec<VEC> l1x = lc[1], l2x = lc[2], l2y = lc[2], l0y = lc[0], l0z = lc[0], l1z = lc[1];
         Vec<VEC> n1x = lcn[1], n2x = lcn[2];
-        axis_terms<false, VEC>(a, 0, i, j, k0, l1x, l2x, true);
-        axis_terms<false, VEC>(a, 1, i, j, k0, l2y, l0y, true);
-        axis_terms<false, VEC>(a, 2, i, j, k0, l0z, l1z, true);
-        if (ip) axis_terms<false, VEC>(a, 0, i + 1, j, k0, n1x, n2x, false);
-        if (jp) axis_terms<false, VEC>(a, 1, i, j + 1, k0, z_jp, x_jp, false);
-        if (kp) axis_terms<false, 1>(a, 2, i, j, k0 + VEC, x_kp, y_kp, false);
+        axis_terms_ax<false, VEC, 0>(a, i, j, k0, l1x, l2x, true);
+        axis_terms_ax<false, VEC, 1>(a, i, j, k0, l2y, l0y, true);
+        axis_terms_ax<false, VEC, 2>(a, i, j, k0, l0z, l1z, true);
+        if (ip) axis_terms_ax<false, VEC, 0>(a, i + 1, j, k0, n1x, n2x, false);
+        if (jp) axis_terms_ax<false, VEC, 1>(a, i, j + 1, k0, z_jp, x_jp, false);
+        if (kp) axis_terms_ax<false, 1, 2>(a, i, j, k0 + VEC, x_kp, y_kp, false);
         const Vec<VEC> h0 = ldv<VEC>(lH), h1 = ldv<VEC>(lH + N), h2 = ldv<VEC>(lH + 2 * N);
         Vec<VEC> Hx, Hy, Hz, Hz_jm = vzero<VEC>(), Hx_jm = vzero<VEC>();
         float Hy_k = 0.f, Hx_k = 0.f;
@@ -1029,7 +1114,7 @@ __global__ void __launch_bounds__(256) k_adj_E_shell_s(const __grid_constant__ A
                 const float d[6] = {Hz.v[e] - Hz_jm.v[e], Hy.v[e] - hy_km, Hx.v[e] - hx_km,
                                     Hz.v[e] - Hz_m.v[e], Hy.v[e] - Hy_m.v[e], Hx.v[e] - Hx_jm.v[e]};
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                curl_H_cpml(a, i, j, k, d, cu, sm);
+                curl_H_cpml_ax(a, i, j, k, d, cu);
                 if (!mN) {
                     gv[0].v[e] += cc * (le[0].v[e] * cu[0] + le[1].v[e] * cu[1] + le[2].v[e] * cu[2]);
                 } else {

@@ -137,7 +137,27 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
         int& slot = a.ax_slab[p->slab[s].axis][side];
         slot = slot < 0 ? s : -2;  // -2: two slabs on one face (the per-axis kernels do not apply)
     }
+    for (int x = 0; x < 3; ++x)
+        for (int side = 0; side < 2; ++side) {
+            const int s = a.ax_slab[x][side];
+            if (s < 0) continue;
+            a.axs[x][side] = p->slab[s];
+            for (int q = 0; q < 2; ++q) {
+                a.axpE[x][side][q] = b->psi_E[s][q];
+                a.axlp[0][x][side][q] = cur.psi[s][q];
+                a.axlp[1][x][side][q] = cur.psi[s][2 + q];
+                a.axlpo[0][x][side][q] = nxt.psi[s][q];
+                a.axlpo[1][x][side][q] = nxt.psi[s][2 + q];
+            }
+        }
     return a;
+}
+
+// Whether every slab's psi array is indexable with 32-bit offsets (the fast shell kernels).
+bool psi_offsets_32bit(const FdtdPlan* p) {
+    for (int s = 0; s < p->d.n_slabs; ++s)
+        if ((long long)p->slab[s].sx * p->slab[s].sy * p->slab[s].sz >= (1LL << 31)) return false;
+    return true;
 }
 
 // Whether every face holds at most one slab (the per-axis shell kernels apply).
@@ -213,7 +233,7 @@ void launch_adj(const FdtdPlan* p, const AdjArgs& a, cudaStream_t st) {
     AdjKind shell = axis_table_ok(a) ? AdjKind::Shell : AdjKind::ShellGeneric;
     // fast shell: zero halo (no periodic axis), no conductivity, no PEC/PMC, scalar inv_mu (H)
     if (shell == AdjKind::Shell && !p->g.px && !p->g.py && !p->g.pz && !p->g.pec && !p->g.pmc && !a.sigE &&
-        !a.sigH && (!HSIDE || a.im == nullptr))
+        !a.sigH && (!HSIDE || a.im == nullptr) && psi_offsets_32bit(p))
         shell = AdjKind::ShellFast;
     if (!sp.split) {
         const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
