@@ -721,20 +721,19 @@ __device__ __forceinline__ float mat_at(const float* m, int n, float scalar, lon
 template <bool ESIDE>
 __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, const int* __restrict__ tp, float* F,
                                             const float* mat, int n_mat, float mat_scalar, int inverse, int blk) {
-    const int t = *tp;
-    const int ti = t + 1;
-    if (!s.on[ti]) return;
-    const float teff = s.teff[ti] + (ESIDE ? 0.f : 0.5f);
-    const float ph0 = ESIDE ? s.phE[ti] : s.phH[ti];
     const int wall = ESIDE ? g.pec : g.pmc;
     if (s.kind == FDTD_SRC_DIPOLE) {
         if (blk != 0 || threadIdx.x != 0) return;
         if (ESIDE == (bool)s.magnetic) return;
         const int i = s.lo[0], j = s.lo[1], k = s.lo[2];
         if (face_zero(g, wall, s.comp, i, j, k)) return;
-        const float amp = profile_amp(s, teff, ph0);
+        float* fp = F + s.comp * g.N + cell_index(g, i, j, k);
+        const float f0 = *fp;  // issued before the step-dependent loads
+        const int ti = *tp + 1;
+        if (!s.on[ti]) return;
+        const float amp = profile_amp(s, s.teff[ti] + (ESIDE ? 0.f : 0.5f), ESIDE ? s.phE[ti] : s.phH[ti]);
         const float sg = inverse ? 1.f : -1.f;
-        F[s.comp * g.N + cell_index(g, i, j, k)] += sg * (s.coef * amp);
+        *fp = f0 + sg * (s.coef * amp);
         return;
     }
     const int n = s.normal, ax = (n + 1) % 3, bx = (n + 2) % 3;
@@ -750,23 +749,28 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
     const float sg = inverse ? -s.sign : s.sign;
     const float* inc = ESIDE ? s.incH : s.incE;
     const float* off = ESIDE ? s.offH : s.offE;
+    // every load that does not depend on the time step is issued before the step counter's,
+    // so the kernel waits on two memory round trips instead of five
     const float oa = __ldg(off + ax * P + f), ob = __ldg(off + bx * P + f);
+    const float ia = __ldg(inc + ax * P + f), ib = __ldg(inc + bx * P + f);
+    const float ma = mat_at(mat, n_mat, mat_scalar, g.N, ax, c), mb = mat_at(mat, n_mat, mat_scalar, g.N, bx, c);
+    const float fa = F[ax * g.N + c], fb = F[bx * g.N + c];
+    const int ti = *tp + 1;
+    if (!s.on[ti]) return;
+    const float teff = s.teff[ti] + (ESIDE ? 0.f : 0.5f);
+    const float ph0 = ESIDE ? s.phE[ti] : s.phH[ti];
     const float amp_a = profile_amp(s, teff + oa, ph0 + s.omega_dt * oa);
     const float amp_b = profile_amp(s, teff + ob, ph0 + s.omega_dt * ob);
-    const float inc_a = __ldg(inc + ax * P + f) * amp_a;
-    const float inc_b = __ldg(inc + bx * P + f) * amp_b;
+    const float inc_a = ia * amp_a;
+    const float inc_b = ib * amp_b;
     if (ESIDE) {
         // E[a] += sign c inv_eps[a] H_inc,b ;  E[b] -= sign c inv_eps[b] H_inc,a
-        if (!face_zero(g, wall, ax, i, j, k))
-            F[ax * g.N + c] += sg * (inc_b * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, ax, c));
-        if (!face_zero(g, wall, bx, i, j, k))
-            F[bx * g.N + c] -= sg * (inc_a * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, bx, c));
+        if (!face_zero(g, wall, ax, i, j, k)) F[ax * g.N + c] = fa + sg * (inc_b * s.coef * ma);
+        if (!face_zero(g, wall, bx, i, j, k)) F[bx * g.N + c] = fb - sg * (inc_a * s.coef * mb);
     } else {
         // H[b] += sign c inv_mu[b] E_inc,a ;  H[a] -= sign c inv_mu[a] E_inc,b
-        if (!face_zero(g, wall, bx, i, j, k))
-            F[bx * g.N + c] += sg * (inc_a * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, bx, c));
-        if (!face_zero(g, wall, ax, i, j, k))
-            F[ax * g.N + c] -= sg * (inc_b * s.coef * mat_at(mat, n_mat, mat_scalar, g.N, ax, c));
+        if (!face_zero(g, wall, bx, i, j, k)) F[bx * g.N + c] = fb + sg * (inc_a * s.coef * mb);
+        if (!face_zero(g, wall, ax, i, j, k)) F[ax * g.N + c] = fa - sg * (inc_b * s.coef * ma);
     }
 }
 
@@ -999,6 +1003,24 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
                                                 int n_slots, float* E, float* H, T* rec, int blk) {
     const long long q = (long long)blk * blockDim.x + threadIdx.x;
     if (q >= ifc.total) return;
+    int s = 0;
+    while (s + 1 < ifc.n && q >= ifc.start[s + 1]) ++s;
+    const long long pidx = q - ifc.start[s];
+    int i, j, k;
+    if (ifc.axis[s] == 0) { i = ifc.layer[s]; j = (int)(pidx / g.nz); k = (int)(pidx % g.nz); }
+    else if (ifc.axis[s] == 1) { j = ifc.layer[s]; i = (int)(pidx / g.nz); k = (int)(pidx % g.nz); }
+    else { k = ifc.layer[s]; i = (int)(pidx / g.ny); j = (int)(pidx % g.ny); }
+    const long long c = cell_index(g, i, j, k);
+    // recording: the field values do not depend on the step, so they are loaded before the
+    // step counter and its table (one memory round trip less on the critical path)
+    float v[6];
+    if (!RESTORE) {
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            v[comp] = E[comp * g.N + c];
+            v[3 + comp] = H[comp * g.N + c];
+        }
+    }
     int t = *tp, tb = t;
     float w = 0.f;
     if (ifc.store) {  // time filter: store every k-th step, restore by linear interpolation
@@ -1016,14 +1038,6 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
         tb = t;
     }
     if (t < 0 || t >= n_slots || tb < 0 || tb >= n_slots) return;
-    int s = 0;
-    while (s + 1 < ifc.n && q >= ifc.start[s + 1]) ++s;
-    const long long pidx = q - ifc.start[s];
-    int i, j, k;
-    if (ifc.axis[s] == 0) { i = ifc.layer[s]; j = (int)(pidx / g.nz); k = (int)(pidx % g.nz); }
-    else if (ifc.axis[s] == 1) { j = ifc.layer[s]; i = (int)(pidx / g.nz); k = (int)(pidx % g.nz); }
-    else { k = ifc.layer[s]; i = (int)(pidx / g.ny); j = (int)(pidx % g.ny); }
-    const long long c = cell_index(g, i, j, k);
     const long long P = ifc.start[s + 1] - ifc.start[s];
     T* slotp = rec + (long long)t * 6 * ifc.total;
     const long long db = ((long long)tb - t) * 6 * ifc.total;  // slot b relative to slot a
@@ -1037,7 +1051,7 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
                 const float va = from_storage(base[comp * P + pidx]);
                 F[comp * g.N + c] = w != 0.f ? va + w * (from_storage(base[db + comp * P + pidx]) - va) : va;
             } else {
-                base[comp * P + pidx] = to_storage<T>(F[comp * g.N + c]);
+                base[comp * P + pidx] = to_storage<T>(v[3 * fld + comp]);
             }
         }
     }
