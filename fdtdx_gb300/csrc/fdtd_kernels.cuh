@@ -606,7 +606,8 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
         }
         // the first fused phasor's previous values (one frequency), loaded with the fields so
         // its read-modify-write does not add a second round trip after the update
-        // (AXT kernels: its update is made here too, from the same region test and index)
+        // (the per-axis-table kernels also make its update here, from the same region test
+        // and index)
         float2 pf[VEC][3];
         bool pfo = false, pin[VEC];
         long long pr[VEC];
@@ -1043,11 +1044,11 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
     const long long db = ((long long)tb - t) * 6 * ifc.total;  // slot b relative to slot a
 #pragma unroll
     for (int fld = 0; fld < 2; ++fld) {
-        float* F = fld == 0 ? E : H;
         T* base = slotp + fld * 3 * ifc.total + 3 * ifc.start[s];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) {
             if (RESTORE) {
+                float* F = fld == 0 ? E : H;
                 const float va = from_storage(base[comp * P + pidx]);
                 F[comp * g.N + c] = w != 0.f ? va + w * (from_storage(base[db + comp * P + pidx]) - va) : va;
             } else {

@@ -233,6 +233,30 @@ def test_vec_and_chunk_variants_agree(nz):
                     assert torch.equal(x, y), (vec, chunk)
 
 
+def test_shell_tiling_variants_agree():
+    """CPML shell launch shapes (fdtd_plan_tune_shell): x chunks and one or two z cells per
+    thread give bit-identical results (same per-cell arithmetic through the per-axis slab
+    table); four z cells per thread take the generic six-slab form, whose CPML terms are
+    summed in slab order instead of axis order (agreement to rounding)."""
+    objects, arrays, _, cfg, _ = scenes.coupler(shape=(36, 32, 40), steps=40, scale=0.15, pml=5)
+    outs = {}
+    for chunk, vec in ((4, 1), (1, 1), (9, 2), (3, 4)):
+        a = arrays.reset()
+        s = Scene(objects, a, cfg)
+        s.tune_shell(chunk, vec)
+        s.forward(a, 0, 40)
+        torch.cuda.synchronize()
+        outs[(chunk, vec)] = [a.fields.E.clone(), a.fields.H.clone()] + [
+            v.clone() for st in a.detector_states.values() for v in st.values()]
+        s.close()
+    ref = outs[(4, 1)]
+    for key in ((1, 1), (9, 2)):
+        for x, y in zip(outs[key], ref):
+            assert torch.equal(x, y), key
+    for x, y in zip(outs[(3, 4)], ref):
+        assert rel_l2(x, y) < 1e-6
+
+
 @pytest.mark.parametrize("tile", [(0, 0, 0, 0), (16, 8, 2, 3), (24, 4, 3, 7), (64, 8, 6, 0)])
 def test_tma_kernels_match_register_kernels(tile):
     """The TMA-pipelined half-steps agree with the register-queue half-steps (every tile shape,
