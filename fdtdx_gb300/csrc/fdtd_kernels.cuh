@@ -728,13 +728,11 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
         if (ESIDE == (bool)s.magnetic) return;
         const int i = s.lo[0], j = s.lo[1], k = s.lo[2];
         if (face_zero(g, wall, s.comp, i, j, k)) return;
-        float* fp = F + s.comp * g.N + cell_index(g, i, j, k);
-        const float f0 = *fp;  // issued before the step-dependent loads
         const int ti = *tp + 1;
         if (!s.on[ti]) return;
         const float amp = profile_amp(s, s.teff[ti] + (ESIDE ? 0.f : 0.5f), ESIDE ? s.phE[ti] : s.phH[ti]);
         const float sg = inverse ? 1.f : -1.f;
-        *fp = f0 + sg * (s.coef * amp);
+        atomicAdd(F + s.comp * g.N + cell_index(g, i, j, k), sg * (s.coef * amp));
         return;
     }
     const int n = s.normal, ax = (n + 1) % 3, bx = (n + 2) % 3;
@@ -751,11 +749,12 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
     const float* inc = ESIDE ? s.incH : s.incE;
     const float* off = ESIDE ? s.offH : s.offE;
     // every load that does not depend on the time step is issued before the step counter's,
-    // so the kernel waits on two memory round trips instead of five
+    // and the field is updated by atomic adds (no read of it; sources that overlap, which a
+    // batched launch runs together, add up in any order), so the kernel waits on two memory
+    // round trips instead of five
     const float oa = __ldg(off + ax * P + f), ob = __ldg(off + bx * P + f);
     const float ia = __ldg(inc + ax * P + f), ib = __ldg(inc + bx * P + f);
     const float ma = mat_at(mat, n_mat, mat_scalar, g.N, ax, c), mb = mat_at(mat, n_mat, mat_scalar, g.N, bx, c);
-    const float fa = F[ax * g.N + c], fb = F[bx * g.N + c];
     const int ti = *tp + 1;
     if (!s.on[ti]) return;
     const float teff = s.teff[ti] + (ESIDE ? 0.f : 0.5f);
@@ -766,12 +765,12 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
     const float inc_b = ib * amp_b;
     if (ESIDE) {
         // E[a] += sign c inv_eps[a] H_inc,b ;  E[b] -= sign c inv_eps[b] H_inc,a
-        if (!face_zero(g, wall, ax, i, j, k)) F[ax * g.N + c] = fa + sg * (inc_b * s.coef * ma);
-        if (!face_zero(g, wall, bx, i, j, k)) F[bx * g.N + c] = fb - sg * (inc_a * s.coef * mb);
+        if (!face_zero(g, wall, ax, i, j, k)) atomicAdd(F + ax * g.N + c, sg * (inc_b * s.coef * ma));
+        if (!face_zero(g, wall, bx, i, j, k)) atomicAdd(F + bx * g.N + c, -(sg * (inc_a * s.coef * mb)));
     } else {
         // H[b] += sign c inv_mu[b] E_inc,a ;  H[a] -= sign c inv_mu[a] E_inc,b
-        if (!face_zero(g, wall, bx, i, j, k)) F[bx * g.N + c] = fb + sg * (inc_a * s.coef * mb);
-        if (!face_zero(g, wall, ax, i, j, k)) F[ax * g.N + c] = fa - sg * (inc_b * s.coef * ma);
+        if (!face_zero(g, wall, bx, i, j, k)) atomicAdd(F + bx * g.N + c, sg * (inc_a * s.coef * mb));
+        if (!face_zero(g, wall, ax, i, j, k)) atomicAdd(F + ax * g.N + c, -(sg * (inc_b * s.coef * ma)));
     }
 }
 
