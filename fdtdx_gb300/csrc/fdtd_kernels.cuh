@@ -854,9 +854,6 @@ constexpr int kDetBlock = 256;
 __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const int* __restrict__ tp,
                                               const DetFields& f, void* state, int blk) {
     __shared__ float sh[kDetBlock / 32];
-    const int t = *tp;
-    const int slot = __ldg(d.slot + t + 1);
-    if (slot < 0) return;
     const long long r = (long long)blk * blockDim.x + threadIdx.x;
     const bool valid = r < d.R;
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -868,7 +865,12 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
     }
     int need = d.comp_mask;
     if (d.kind == FDTD_DET_FLUX || d.kind == FDTD_DET_ENERGY) need = 63;
+    // the samples do not depend on the step: their loads are issued before the step
+    // counter's and the slot table's, which then overlap them
     if (valid) colocate(g, f, d.exact, need, i, j, k, v);
+    const int t = *tp;
+    const int slot = __ldg(d.slot + t + 1);
+    if (slot < 0) return;
 
     // gather the recorded values of this cell
     float out[6];
