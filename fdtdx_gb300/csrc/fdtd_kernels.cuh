@@ -445,7 +445,7 @@ __device__ __forceinline__ void update_E_body(const UpdArgs& a, int blk) {
 }
 
 template <bool REV, int VEC, bool PML, int AXT = 0>
-__global__ void __launch_bounds__(256, AXT && VEC == 1 ? 4 : 1) k_update_E(const __grid_constant__ UpdArgs a) {
+__global__ void __launch_bounds__(256, AXT && VEC == 1 ? 5 : 1) k_update_E(const __grid_constant__ UpdArgs a) {
     update_E_body<REV, VEC, PML, AXT>(a, blockIdx.x);
 }
 
@@ -701,7 +701,7 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
 }
 
 template <bool REV, int VEC, bool PML, int AXT = 0>
-__global__ void __launch_bounds__(256, AXT && VEC == 1 ? 4 : 3) k_update_H(const __grid_constant__ UpdArgs a) {
+__global__ void __launch_bounds__(256, AXT && VEC == 1 ? (REV ? 5 : 4) : 3) k_update_H(const __grid_constant__ UpdArgs a) {
     update_H_body<REV, VEC, PML, AXT>(a, blockIdx.x);
 }
 
