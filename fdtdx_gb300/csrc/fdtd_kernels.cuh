@@ -157,6 +157,8 @@ __device__ __forceinline__ void ax_term(const UpdArgs& a, int side, int l, int i
     else if (AX == 1) { cu[2] -= c1; cu[0] += c2; }
     else { cu[0] -= c1; cu[1] += c2; }
 }
+#undef FDTD_AX_SEL
+#undef FDTD_AX_PSI
 
 // Neighbour on one axis with the halo rule (wrap on a periodic axis, else zero).
 __device__ __forceinline__ float nb(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp, int i,
@@ -256,20 +258,6 @@ __device__ __forceinline__ Vec<VEC> nbv_t(const Geo& g, const float* __restrict_
 #pragma unroll
     for (int e = 0; e < VEC; ++e) z.v[e] = 0.f;
     return z;
-}
-
-// Whether (i, j, k0 .. k0+VEC-1) can lie in any CPML slab.
-__device__ __forceinline__ bool maybe_slab(const UpdArgs& a, int i, int j, int k0, int vec) {
-    const int idx[3] = {i, j, k0};
-#pragma unroll
-    for (int s = 0; s < FDTD_MAX_SLABS; ++s) {
-        if (s >= a.n_slab) break;
-        const DSlab& sl = a.slab[s];
-        const int lo = idx[sl.axis] - sl.lo;
-        const int hi = lo + (sl.axis == 2 ? vec - 1 : 0);
-        if (hi >= 0 && lo < sl.L) return true;
-    }
-    return false;
 }
 
 // The slab mask of block `blk`'s box.
