@@ -1245,7 +1245,7 @@ __device__ void colocate_snap(const AdjArgs& a, const AdjDet& x, int i, int j, i
         for (int q = 0; q < 6; ++q) v[q] = S(q, i, j, k);
         return;
     }
-    auto hav = [&](int comp, int ii, int jj, int kk) { return (ld_halo(g, a.H, comp, ii, jj, kk) + S(3 + comp, ii, jj, kk)) / 2.f; };
+    auto hav = [&](int comp, int ii, int jj, int kk) { return (ld_halo_sel(g, a.H, comp, ii, jj, kk) + S(3 + comp, ii, jj, kk)) / 2.f; };
     v[0] = (0.5f * (S(0, i, j, k) + S(0, i - 1, j, k)) + 0.5f * (S(0, i, j, k + 1) + S(0, i - 1, j, k + 1))) / 2.f;
     v[1] = (0.5f * (S(1, i, j, k) + S(1, i, j - 1, k)) + 0.5f * (S(1, i, j, k + 1) + S(1, i, j - 1, k + 1))) / 2.f;
     v[2] = S(2, i, j, k);

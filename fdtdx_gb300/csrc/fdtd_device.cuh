@@ -124,6 +124,19 @@ __device__ __forceinline__ float ld_halo(const Geo& g, const float* __restrict__
     return __ldg(f + comp * g.N + cell_index(g, i, j, k));
 }
 
+// ld_halo without branches: the wrapped index is formed with selects and the load always
+// issues from a valid address (a one-cell excursion wraps into the grid), so every load of
+// a caller can be in flight at once; a zero-halo neighbour reads 0.
+__device__ __forceinline__ float ld_halo_sel(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k) {
+    const bool li = i < 0, ui = i >= g.nx, lj = j < 0, uj = j >= g.ny, lk = k < 0, uk = k >= g.nz;
+    const bool ok = (!(li || ui) || g.px) && (!(lj || uj) || g.py) && (!(lk || uk) || g.pz);
+    const int ii = li ? i + g.nx : (ui ? i - g.nx : i);
+    const int jj = lj ? j + g.ny : (uj ? j - g.ny : j);
+    const int kk = lk ? k + g.nz : (uk ? k - g.nz : k);
+    const float v = __ldg(f + comp * g.N + cell_index(g, ok ? ii : 0, ok ? jj : 0, ok ? kk : 0));
+    return ok ? v : 0.f;
+}
+
 // Whether component `comp` at (i, j, k) is zeroed by a conductor face in `mask`
 // (PEC for E: fdtdx/objects/boundaries/pec.py:71-77; PMC for H: pmc.py:62-76).
 __device__ __forceinline__ bool face_zero(const Geo& g, int mask, int comp, int i, int j, int k) {

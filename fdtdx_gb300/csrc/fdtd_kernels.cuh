@@ -785,7 +785,7 @@ struct DetFields {
 };
 
 __device__ __forceinline__ float hav(const Geo& g, const DetFields& f, int comp, int i, int j, int k) {
-    return (ld_halo(g, f.Hp, comp, i, j, k) + ld_halo(g, f.H, comp, i, j, k)) / 2.f;
+    return (ld_halo_sel(g, f.Hp, comp, i, j, k) + ld_halo_sel(g, f.H, comp, i, j, k)) / 2.f;
 }
 
 __device__ void colocate(const Geo& g, const DetFields& f, int exact, int mask, int i, int j, int k, float v[6]) {
@@ -799,13 +799,13 @@ __device__ void colocate(const Geo& g, const DetFields& f, int exact, int mask, 
         return;
     }
     if (mask & 1) {
-        const float lo = 0.5f * (ld_halo(g, f.E, 0, i, j, k) + ld_halo(g, f.E, 0, i - 1, j, k));
-        const float up = 0.5f * (ld_halo(g, f.E, 0, i, j, k + 1) + ld_halo(g, f.E, 0, i - 1, j, k + 1));
+        const float lo = 0.5f * (ld_halo_sel(g, f.E, 0, i, j, k) + ld_halo_sel(g, f.E, 0, i - 1, j, k));
+        const float up = 0.5f * (ld_halo_sel(g, f.E, 0, i, j, k + 1) + ld_halo_sel(g, f.E, 0, i - 1, j, k + 1));
         v[0] = (lo + up) / 2.f;
     }
     if (mask & 2) {
-        const float lo = 0.5f * (ld_halo(g, f.E, 1, i, j, k) + ld_halo(g, f.E, 1, i, j - 1, k));
-        const float up = 0.5f * (ld_halo(g, f.E, 1, i, j, k + 1) + ld_halo(g, f.E, 1, i, j - 1, k + 1));
+        const float lo = 0.5f * (ld_halo_sel(g, f.E, 1, i, j, k) + ld_halo_sel(g, f.E, 1, i, j - 1, k));
+        const float up = 0.5f * (ld_halo_sel(g, f.E, 1, i, j, k + 1) + ld_halo_sel(g, f.E, 1, i, j - 1, k + 1));
         v[1] = (lo + up) / 2.f;
     }
     if (mask & 4) v[2] = __ldg(f.E + 2 * g.N + c);
