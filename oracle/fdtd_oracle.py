@@ -20,6 +20,9 @@ torch autograd for per-step vector-Jacobian products), the reference files:
 * fdtdx/objects/detectors/{detector,phasor,field,poynting_flux,energy}.py  detectors
 * fdtdx/fdtd/update.py:1040-1222, fdtdx/fdtd/misc.py:10-66     detectors, interfaces
 * fdtdx/fdtd/forward.py:83-156, backward.py:62-135, fdtd.py:39-418  step and VJP loop
+* fdtdx/fdtd/update.py:356-523, 641-676, 751-807, 956-995, fdtdx/fdtd/misc.py:69-213,
+  fdtdx/core/misc.py:557-611   full 3x3 anisotropic update branch (uniform grid); the
+  GB300 library does not build this branch yet, the oracle states it for its pins
 
 Parity status: the reference is JAX and JAX cannot be installed on these machines,
 so the reference itself cannot be run.  The reference's tests hold no stored field
@@ -642,6 +645,86 @@ def _walls(sc, F, walls):
 
 
 # --------------------------------------------------------------------------------------------
+# full 3x3 anisotropic branch (uniform grid)
+# --------------------------------------------------------------------------------------------
+
+
+def expand_to_3x3(arr):
+    """fdtdx/core/misc.py:557-611: (1 | 3 | 9, *grid) or a scalar -> (3, 3, *grid)."""
+    if arr is None:
+        return None
+    if not isinstance(arr, torch.Tensor) or arr.dim() == 0:
+        a = torch.as_tensor(arr, dtype=torch.float64)
+        return (torch.eye(3, dtype=a.dtype) * a)[:, :, None, None, None]
+    n = arr.shape[0]
+    if n == 9:
+        return arr.reshape(3, 3, *arr.shape[1:])
+    z = torch.zeros(arr.shape[1:], dtype=arr.dtype)
+    d = [arr[0], arr[0], arr[0]] if n == 1 else [arr[0], arr[1], arr[2]]
+    return torch.stack([torch.stack([d[r] if q == r else z for q in range(3)]) for r in range(3)])
+
+
+def aniso_update_matrices(inv, sigma, c: float, eta_factor: float, reverse: bool = False):
+    """fdtdx/fdtd/misc.py:69-129: A, B of E^(n+1) = A E^n + B curl (forward) or of the reverse
+    update; M1 = I + (c eta / 2) inv sigma, M2 = I - (c eta / 2) inv sigma, forward A = M1^-1 M2,
+    B = c M1^-1 inv, reverse A = M2^-1 M1, B = c M2^-1 inv."""
+    grid = inv.shape[2:]
+    eye = torch.eye(3, dtype=inv.dtype).reshape(3, 3, 1, 1, 1).expand(3, 3, *grid)
+    M1, M2 = eye.clone(), eye.clone()
+    if sigma is not None:
+        f = c * eta_factor / 2 * torch.einsum("ijxyz,jkxyz->ikxyz", inv, sigma.expand(3, 3, *grid))
+        M1 = M1 + f
+        M2 = M2 - f
+    to_last = (2, 3, 4, 0, 1)
+    back = (3, 4, 0, 1, 2)
+    lhs, rhs = (M2, M1) if reverse else (M1, M2)
+    A = torch.linalg.solve(lhs.permute(to_last), rhs.permute(to_last)).permute(back)
+    B = c * torch.linalg.solve(lhs.permute(to_last), inv.expand(3, 3, *grid).permute(to_last)).permute(back)
+    return A, B
+
+
+def avg_aniso_E(field_pad, component: int, location: int):
+    """fdtdx/fdtd/misc.py:132-171 (uniform grid): component `component` of a padded E-type field
+    averaged onto the Yee location of `location`."""
+    s = field_pad[component]
+    la, ca = location, component
+    out = (s + torch.roll(s, -1, dims=la) + torch.roll(s, 1, dims=ca)
+           + torch.roll(torch.roll(s, -1, dims=la), 1, dims=ca)) / 4
+    return out[1:-1, 1:-1, 1:-1]
+
+
+def avg_aniso_H(field_pad, component: int, location: int):
+    """fdtdx/fdtd/misc.py:174-213 (uniform grid), the H-type stencil."""
+    s = field_pad[component]
+    la, ca = location, component
+    out = (s + torch.roll(s, 1, dims=la) + torch.roll(s, -1, dims=ca)
+           + torch.roll(torch.roll(s, 1, dims=la), -1, dims=ca)) / 4
+    return out[1:-1, 1:-1, 1:-1]
+
+
+def aniso_apply(A, B, F, curl, periodic, avg, sign: float):
+    """Rows of update.py:474-492 / 791-807: F_i = sum_j A_ij F_j@i + sign sum_j B_ij curl_j@i,
+    the diagonal terms local, the off-diagonal ones averaged onto component i's location."""
+    F_pad, K_pad = pad_fields(F, periodic), pad_fields(curl, periodic)
+    rows = []
+    for i in range(3):
+        acc_a = A[i, i] * F[i]
+        acc_b = B[i, i] * curl[i]
+        for j in range(3):
+            if j == i:
+                continue
+            acc_a = acc_a + A[i, j] * avg(F_pad, j, i)
+            acc_b = acc_b + B[i, j] * avg(K_pad, j, i)
+        rows.append(acc_a + sign * acc_b)
+    return torch.stack(rows)
+
+
+def _full_tensor(inv, sigma) -> bool:
+    return (isinstance(inv, torch.Tensor) and inv.dim() > 0 and inv.shape[0] == 9) or (
+        sigma is not None and sigma.shape[0] == 9)
+
+
+# --------------------------------------------------------------------------------------------
 # updates
 # --------------------------------------------------------------------------------------------
 
@@ -651,6 +734,11 @@ def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=
     c = sc.courant
     curl, psi_E = curl_H(pad_fields(H, sc.periodic), psi_E, sc.pmls, simulate_boundaries)
     sig = sc.sigma_E
+    if _full_tensor(inv_eps, sig):  # update.py:356-492
+        A, B = aniso_update_matrices(expand_to_3x3(inv_eps), expand_to_3x3(sig), c, ETA0)
+        E = aniso_apply(A, B, E, curl, sc.periodic, avg_aniso_E, 1.0)
+        E = _apply_sources(sc, E, inv_eps, t, True, False)
+        return _walls(sc, E, sc.pec), psi_E
     factor = 1
     if sig is not None:
         factor = 1 - c * sig * ETA0 * inv_eps / 2
@@ -666,6 +754,11 @@ def update_H(sc: OracleScene, t: int, E, H, psi_H, inv_mu, simulate_boundaries=T
     c = sc.courant
     curl, psi_H = curl_E(pad_fields(E, sc.periodic), psi_H, sc.pmls, simulate_boundaries)
     sig = sc.sigma_H
+    if _full_tensor(inv_mu, sig):  # update.py:751-807
+        A, B = aniso_update_matrices(expand_to_3x3(inv_mu), expand_to_3x3(sig), c, 1 / ETA0)
+        H = aniso_apply(A, B, H, curl, sc.periodic, avg_aniso_H, -1.0)
+        H = _apply_sources(sc, H, inv_mu, t, False, False)
+        return _walls(sc, H, sc.pmc), psi_H
     factor = 1
     if sig is not None:
         factor = 1 - c * sig / ETA0 * inv_mu / 2
@@ -682,6 +775,9 @@ def update_E_reverse(sc: OracleScene, t: int, E, H, psi_E, inv_eps):
     E = _apply_sources(sc, E, inv_eps, t, True, True)
     curl, _ = curl_H(pad_fields(H, sc.periodic), psi_E, sc.pmls, False)
     sig = sc.sigma_E
+    if _full_tensor(inv_eps, sig):  # update.py:641-676
+        A, B = aniso_update_matrices(expand_to_3x3(inv_eps), expand_to_3x3(sig), c, ETA0, reverse=True)
+        return _walls(sc, aniso_apply(A, B, E, curl, sc.periodic, avg_aniso_E, -1.0), sc.pec)
     factor = 1
     if sig is not None:
         E = E * (1 + c * sig * ETA0 * inv_eps / 2)
@@ -696,6 +792,9 @@ def update_H_reverse(sc: OracleScene, t: int, E, H, psi_H, inv_mu):
     H = _apply_sources(sc, H, inv_mu, t, False, True)
     curl, _ = curl_E(pad_fields(E, sc.periodic), psi_H, sc.pmls, False)
     sig = sc.sigma_H
+    if _full_tensor(inv_mu, sig):  # update.py:956-995
+        A, B = aniso_update_matrices(expand_to_3x3(inv_mu), expand_to_3x3(sig), c, 1 / ETA0, reverse=True)
+        return _walls(sc, aniso_apply(A, B, H, curl, sc.periodic, avg_aniso_H, 1.0), sc.pmc)
     factor = 1
     if sig is not None:
         H = H * (1 + c * sig / ETA0 * inv_mu / 2)
