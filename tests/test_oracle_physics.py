@@ -1,0 +1,101 @@
+"""Analytic physics on the oracle (CPU, float32): the reference's simulation-tier checks
+replayed on the restatement, so its physics is pinned beyond internal consistency.
+
+* plane-wave wavenumber k = 2 pi n / lambda from the phasor phase between two planes, and
+  the wave impedance |Ex| / |Hy| = 1 / n in fdtdx's normalised units (E is stored as
+  E_SI / eta0), in vacuum and in eps_r = 4
+  (tests/simulation/physics/test_plane_wave.py:185-241, 5%);
+* Fresnel power transmission at normal incidence T = 4 n1 n2 / (n1 + n2)^2 from the
+  time-averaged Poynting flux behind a vacuum / eps_r = 4 interface, normalised by a vacuum
+  run (tests/simulation/physics/test_fresnel.py:150-244, 5%).
+
+Both use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a
++z uniform plane source with Ex polarisation and the default CW profile, 120 fs.
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import fdtdx_gb300 as fx
+from oracle import fdtd_oracle as O
+
+C0 = 299792458.0
+WL = 1e-6
+TOL = 0.05
+
+
+def _domain(dx: float, nz: int, eps_fill: float | None = None, eps_half_from: int | None = None):
+    cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(3, 3, nz))
+    bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                           boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                           thickness_grid_minz=10, thickness_grid_maxz=10)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    if eps_fill is not None:
+        objs.append(fx.UniformMaterialObject(name="fill", grid_slice_tuple=((0, 3), (0, 3), (0, nz)),
+                                             material=fx.Material(permittivity=eps_fill)))
+    if eps_half_from is not None:
+        objs.append(fx.UniformMaterialObject(name="half", grid_slice_tuple=((0, 3), (0, 3), (eps_half_from, nz)),
+                                             material=fx.Material(permittivity=4.0)))
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 3), (0, 3), (12, 13)), direction="+",
+                                      fixed_E_polarization_vector=(1, 0, 0),
+                                      wave_character=fx.WaveCharacter(wavelength=WL)))
+    return cfg, objs
+
+
+def _run(cfg, objs):
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    sc = O.OracleScene(objects, arrays, cfg, torch.float32)
+    return sc, O.run(sc, sc.T)
+
+
+@pytest.mark.parametrize("eps_r,sep", [(1.0, 5), (4.0, 3)])
+def test_plane_wave_wavenumber_and_impedance(eps_r, sep):
+    dx = 50e-9
+    cfg, objs = _domain(dx, 80, eps_fill=eps_r if eps_r != 1.0 else None)
+    wc = fx.WaveCharacter(wavelength=WL)
+    for name, z in (("d1", 17), ("d2", 17 + sep)):
+        objs.append(fx.PhasorDetector(name=name, grid_slice_tuple=((1, 2), (1, 2), (z, z + 1)), wave_characters=(wc,),
+                                      components=("Ex", "Hy"), reduce_volume=True))
+    sc, st = _run(cfg, objs)
+    p1 = st.det["d1"]["phasor"].reshape(-1)
+    p2 = st.det["d2"]["phasor"].reshape(-1)
+    ex1, hy1, ex2 = complex(p1[0]), complex(p1[1]), complex(p2[0])
+    assert abs(ex1) > 0 and abs(ex2) > 0
+    n = math.sqrt(eps_r)
+    dphi = (np.angle(ex2) - np.angle(ex1)) % (2 * math.pi)  # exp(+i w t) weights: the phase grows along +z
+    k = dphi / (sep * dx)
+    k_ref = 2 * math.pi * n / WL
+    assert abs(k - k_ref) / k_ref < TOL, (k, k_ref)
+    z = abs(ex1) / abs(hy1)
+    assert abs(z - 1 / n) / (1 / n) < TOL, (z, 1 / n)
+
+
+def _mean_flux(st, steps_per_period: int) -> float:
+    f = st.det["flux"]["poynting_flux"][:, 0].double().numpy()
+    return float(f[-10 * steps_per_period:].mean())
+
+
+def test_fresnel_normal_incidence_transmission():
+    dx = 25e-9
+    nz = 200
+    out = []
+    for half in (None, 100):
+        cfg, objs = _domain(dx, nz, eps_half_from=half)
+        objs.append(fx.PoyntingFluxDetector(name="flux", grid_slice_tuple=((0, 3), (0, 3), (140, 141)), direction="+",
+                                            reduce_volume=True))
+        sc, st = _run(cfg, objs)
+        spp = round(WL / (C0 * sc.dt))
+        out.append(_mean_flux(st, spp))
+    s0, st_ = out
+    assert s0 > 0 and st_ > 0
+    n1, n2 = 1.0, 2.0
+    t_ref = 4 * n1 * n2 / (n1 + n2) ** 2
+    t = st_ / s0
+    assert abs(t - t_ref) / t_ref < TOL, (t, t_ref)
+    r = 1 - t
+    r_ref = ((n1 - n2) / (n1 + n2)) ** 2
+    assert abs(r - r_ref) / r_ref < TOL, (r, r_ref)
