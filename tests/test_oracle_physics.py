@@ -10,7 +10,10 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   run (tests/simulation/physics/test_fresnel.py:150-244, 5%);
 * a phasor flux plane equals the time-averaged time-domain flux over the same gated window
   (tests/simulation/physics/test_phasor_poynting_flux.py:90-138, 2%; the reference reports
-  about 0.02%, the oracle gives 0.018%).
+  about 0.02%, the oracle gives 0.018%);
+* the skin-depth attenuation in a sigma = 1e4 S/m conductor from the exact complex
+  dispersion relation (tests/simulation/physics/test_skin_depth.py:60-276, 10%; the oracle
+  gives 3.5%).
 
 Both use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a
 +z uniform plane source with Ex polarisation and the default CW profile, 120 fs.
@@ -128,3 +131,28 @@ def test_phasor_flux_equals_time_averaged_flux():
     fd = float(fd_obj.compute_poynting_flux({"phasor": st.det["fd"]["phasor"]}, dx)[0])
     assert abs(td) > 0
     assert abs(fd - td) / abs(td) < 0.02, (fd, td)
+
+
+def test_skin_depth_in_a_conductor():
+    """A plane wave entering a sigma = 1e4 S/m, eps_r = 1 conductor decays with the attenuation
+    alpha = Im((w / c0) sqrt(eps_r - i sigma / (w eps0))): the Ex phasor amplitude ratio of two
+    planes 1 um apart inside it (tests/simulation/physics/test_skin_depth.py:60-276, 10%)."""
+    dx = 50e-9
+    nz = 90
+    cfg = fx.SimulationConfig(time=80e-15, grid=fx.UniformGrid(dx))
+    cfg_objs = _domain(dx, nz)[1]
+    cfg_objs.append(fx.UniformMaterialObject(name="cond", grid_slice_tuple=((0, 3), (0, 3), (30, 80)),
+                                             material=fx.Material(permittivity=1.0, electric_conductivity=1e4)))
+    wc = fx.WaveCharacter(wavelength=WL)
+    for name, z in (("d1", 35), ("d2", 55)):
+        cfg_objs.append(fx.PhasorDetector(name=name, grid_slice_tuple=((1, 2), (1, 2), (z, z + 1)),
+                                          wave_characters=(wc,), components=("Ex",), reduce_volume=True))
+    sc, st = _run(cfg, cfg_objs)
+    p1 = complex(st.det["d1"]["phasor"].reshape(-1)[0])
+    p2 = complex(st.det["d2"]["phasor"].reshape(-1)[0])
+    assert abs(p1) > 0 and abs(p2) > 0
+    omega = 2 * math.pi * C0 / WL
+    k = omega / C0 * np.sqrt(1.0 - 1j * 1e4 / (omega * O.EPS0))
+    alpha_ref = abs(k.imag)
+    alpha = -math.log(abs(p2) / abs(p1)) / (20 * dx)
+    assert abs(alpha - alpha_ref) / alpha_ref < 0.10, (alpha, alpha_ref)
