@@ -13,7 +13,10 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   about 0.02%, the oracle gives 0.018%);
 * the skin-depth attenuation in a sigma = 1e4 S/m conductor from the exact complex
   dispersion relation (tests/simulation/physics/test_skin_depth.py:60-276, 10%; the oracle
-  gives 3.5%).
+  gives 3.5%);
+* total reflection from a PEC or PMC wall: zero net time-averaged flux of the standing wave
+  against a PML-terminated run (tests/simulation/physics/boundaries/test_pec_reflection.py,
+  test_pmc_reflection.py, 5%).
 
 Both use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a
 +z uniform plane source with Ex polarisation and the default CW profile, 120 fs.
@@ -156,3 +159,30 @@ def test_skin_depth_in_a_conductor():
     alpha_ref = abs(k.imag)
     alpha = -math.log(abs(p2) / abs(p1)) / (20 * dx)
     assert abs(alpha - alpha_ref) / alpha_ref < 0.10, (alpha, alpha_ref)
+
+
+@pytest.mark.parametrize("wall", ["pec", "pmc"])
+def test_conductor_wall_total_reflection(wall):
+    """A PEC (or PMC) wall at z-max reflects all the power: the time-averaged flux of the
+    standing wave in front of it vanishes against a PML-terminated run, R = 1 within 5%
+    (tests/simulation/physics/boundaries/test_pec_reflection.py:150-175, test_pmc_reflection.py)."""
+    dx = 50e-9
+    flux = []
+    for zmax in ("pml", wall):
+        cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(dx))
+        vol = fx.SimulationVolume(shape=(3, 3, 80))
+        bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                               boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                               boundary_type_maxz=zmax, thickness_grid_minz=10, thickness_grid_maxz=10)
+        objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+        objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 3), (0, 3), (12, 13)), direction="+",
+                                          fixed_E_polarization_vector=(1, 0, 0),
+                                          wave_character=fx.WaveCharacter(wavelength=WL)))
+        objs.append(fx.PoyntingFluxDetector(name="flux", grid_slice_tuple=((0, 3), (0, 3), (40, 41)), direction="+",
+                                            reduce_volume=True))
+        sc, st = _run(cfg, objs)
+        flux.append(_mean_flux(st, round(WL / (C0 * sc.dt))))
+    s_ref, s_wall = flux
+    assert s_ref > 0
+    r = 1.0 - s_wall / s_ref
+    assert abs(r - 1.0) < 0.05, r
