@@ -4,13 +4,15 @@ from __future__ import annotations
 
 import json
 import os
+import tempfile
 from pathlib import Path
 
 import torch
 
 from oracle import fdtd_oracle as O
 
-RESULTS = Path(os.environ.get("FDTD_PARITY_LOG", "gpurun_out/parity.jsonl"))
+# parity records (measured errors per case); FDTD_PARITY_LOG chooses the file
+RESULTS = Path(os.environ.get("FDTD_PARITY_LOG", os.path.join(tempfile.gettempdir(), "fdtd_parity.jsonl")))
 
 
 def rel_l2(a, b) -> float:
