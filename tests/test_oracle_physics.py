@@ -16,10 +16,12 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   gives 3.5%);
 * total reflection from a PEC or PMC wall: zero net time-averaged flux of the standing wave
   against a PML-terminated run (tests/simulation/physics/boundaries/test_pec_reflection.py,
-  test_pmc_reflection.py, 5%).
+  test_pmc_reflection.py, 5%);
+* a broadband pulse's stack transmission against single-frequency runs at three wavelengths
+  (tests/simulation/fdtd/test_pulsed_vs_cw.py, 5%; the oracle gives 1.8-2.6%).
 
-Both use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a
-+z uniform plane source with Ex polarisation and the default CW profile, 120 fs.
+All use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a +z
+uniform plane source with Ex polarisation (the default CW profile unless stated).
 """
 
 import math
@@ -186,3 +188,41 @@ def test_conductor_wall_total_reflection(wall):
     assert s_ref > 0
     r = 1.0 - s_wall / s_ref
     assert abs(r - 1.0) < 0.05, r
+
+
+def _stack_run(profile, wave, wavelengths, with_stack: bool):
+    dx = 25e-9
+    cfg = fx.SimulationConfig(time=200e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(3, 3, 200))
+    bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                           boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                           thickness_grid_minz=10, thickness_grid_maxz=10)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    if with_stack:
+        for name, (z0, z1), eps in (("l1", (80, 100), 2.25), ("l2", (100, 115), 6.25), ("l3", (115, 135), 4.0)):
+            objs.append(fx.UniformMaterialObject(name=name, grid_slice_tuple=((0, 3), (0, 3), (z0, z1)),
+                                                 material=fx.Material(permittivity=eps)))
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 3), (0, 3), (12, 13)), direction="+",
+                                      fixed_E_polarization_vector=(1, 0, 0), wave_character=wave,
+                                      temporal_profile=profile))
+    objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((1, 2), (1, 2), (160, 161)),
+                                  wave_characters=tuple(fx.WaveCharacter(wavelength=w) for w in wavelengths),
+                                  components=("Ex",), reduce_volume=True))
+    _, st = _run(cfg, objs)
+    return st.det["ph"]["phasor"].reshape(-1).abs().double().numpy()
+
+
+def test_pulsed_spectrum_matches_cw_transmission():
+    """The transmission of a three-layer stack from one broadband pulse (normalised by a run
+    without the stack) matches single-frequency runs at 0.85, 1.0 and 1.15 um
+    (tests/simulation/fdtd/test_pulsed_vs_cw.py:1-248, 5%)."""
+    wls = [0.85e-6, 1.0e-6, 1.15e-6]
+    pulse = fx.GaussianPulseProfile(spectral_width=fx.WaveCharacter(wavelength=3e-6),
+                                    center_wave=fx.WaveCharacter(wavelength=1e-6))
+    w0 = fx.WaveCharacter(wavelength=1e-6)
+    t_pulse = _stack_run(pulse, w0, wls, True) / _stack_run(pulse, w0, wls, False)
+    for q, wl in enumerate(wls):
+        w = fx.WaveCharacter(wavelength=wl)
+        cw = fx.SingleFrequencyProfile()
+        t_cw = _stack_run(cw, w, [wl], True)[0] / _stack_run(cw, w, [wl], False)[0]
+        assert abs(t_pulse[q] - t_cw) / t_cw < 0.05, (wl, t_pulse[q], t_cw)
