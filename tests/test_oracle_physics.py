@@ -18,7 +18,9 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   against a PML-terminated run (tests/simulation/physics/boundaries/test_pec_reflection.py,
   test_pmc_reflection.py, 5%);
 * a broadband pulse's stack transmission against single-frequency runs at three wavelengths
-  (tests/simulation/fdtd/test_pulsed_vs_cw.py, 5%; the oracle gives 1.8-2.6%).
+  (tests/simulation/fdtd/test_pulsed_vs_cw.py, 5%; the oracle gives 1.8-2.6%);
+* a uniform plane source is linear in its amplitude factor and uniform across the periodic
+  cross-section (tests/simulation/physics/sources/test_plane_source.py:108-146).
 
 All use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a +z
 uniform plane source with Ex polarisation (the default CW profile unless stated).
@@ -226,3 +228,33 @@ def test_pulsed_spectrum_matches_cw_transmission():
         cw = fx.SingleFrequencyProfile()
         t_cw = _stack_run(cw, w, [wl], True)[0] / _stack_run(cw, w, [wl], False)[0]
         assert abs(t_pulse[q] - t_cw) / t_cw < 0.05, (wl, t_pulse[q], t_cw)
+
+
+def test_uniform_plane_source_linearity_and_uniformity():
+    """Doubling a uniform plane source's static amplitude factor doubles the transmitted phasor
+    (5%), and across a 5 x 5 periodic cross-section the phasor's amplitude and phase are uniform
+    (1% and 0.02 rad) (tests/simulation/physics/sources/test_plane_source.py:108-146)."""
+    dx = 50e-9
+    wc = fx.WaveCharacter(wavelength=WL)
+    amps = []
+    for factor in (1.0, 2.0):
+        cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(dx))
+        vol = fx.SimulationVolume(shape=(5, 5, 80))
+        bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                               boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                               thickness_grid_minz=10, thickness_grid_maxz=10)
+        objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+        objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 5), (0, 5), (12, 13)), direction="+",
+                                          fixed_E_polarization_vector=(1, 0, 0), wave_character=wc,
+                                          static_amplitude_factor=factor))
+        objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((0, 5), (0, 5), (22, 23)), wave_characters=(wc,),
+                                      components=("Ex",)))
+        _, st = _run(cfg, objs)
+        amps.append(st.det["ph"]["phasor"].reshape(5, 5).to(torch.complex128))
+    a1, a2 = amps
+    ratio = float(a2.abs().mean() / a1.abs().mean())
+    assert abs(ratio - 2.0) / 2.0 < 0.05, ratio
+    mag = a1.abs()
+    assert float((mag - mag.mean()).abs().max() / mag.mean()) < 0.01
+    ph = torch.angle(a1 / a1[0, 0])
+    assert float(ph.abs().max()) < 0.02
