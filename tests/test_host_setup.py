@@ -88,3 +88,16 @@ def test_material_painting_in_placement_order():
     assert arrays.inv_permeabilities == 1.0
     sig = arrays.electric_conductivity[0, :, 0, 0]
     assert torch.allclose(sig, torch.tensor([0.0] * 6 + [10.0 * 50e-9] * 4))
+
+
+def test_reversible_fdtd_rejects_unsupported_material_inputs():
+    """Inputs the reversible path does not take are refused before any device work: a full
+    3x3 (9-component) permittivity, and a 0-d permeability tensor that asks for a gradient
+    (a permeability gradient needs a (1 | 3, nx, ny, nz) array)."""
+    objects, arrays, _, cfg, _ = scenes.dipole_boxes(shape=(12, 12, 12), steps=4, n_boxes=1, pml=3, device="cpu")
+    full = arrays.aset("inv_permittivities", torch.ones((9, 12, 12, 12)))
+    with pytest.raises(NotImplementedError):
+        fx.reversible_fdtd(full, objects, cfg)
+    mu0 = arrays.aset("inv_permeabilities", torch.tensor(1.0, requires_grad=True))
+    with pytest.raises(NotImplementedError):
+        fx.reversible_fdtd(mu0, objects, cfg)
