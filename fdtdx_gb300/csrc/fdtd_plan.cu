@@ -1002,8 +1002,9 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
     }
     bytes += psi;
     // a recording plan is a reversible-gradient job: the state's cotangents, their twins, a
-    // reconstruction copy of the state and the inv_eps gradient
-    if (d->record_interfaces) bytes += 3 * (24ll * N + psi) + 4ll * d->n_eps * N;
+    // reconstruction copy of the state and the material gradients (inv_eps, and inv_mu when
+    // the permeability is an array)
+    if (d->record_interfaces) bytes += 3 * (24ll * N + psi) + 4ll * (d->n_eps + d->n_mu) * N;
     bool hprev = false;
     for (int q = 0; q < d->n_detectors; ++q) {
         const FdtdDetectorDesc& dd = d->detectors[q];

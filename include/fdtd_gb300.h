@@ -190,8 +190,8 @@ int64_t fdtd_interface_floats(const FdtdPlan* plan);
 int64_t fdtd_plan_device_bytes(const FdtdPlan* plan);
 /* Device bytes one simulation of this description needs (fields, materials, psi,
  * detector states, recording, plan tables and scratch; with record_interfaces also the
- * reversible gradient's cotangents, twins, reconstruction copy and gradient): serving
- * admission. */
+ * reversible gradient's cotangents, twins, reconstruction copy and material gradients):
+ * serving admission.  Computed on the host; needs no GPU. */
 int64_t fdtd_footprint_bytes(const FdtdDesc* desc);
 
 /* Forward steps t0 .. t0+n_steps-1.  flags bit 0: use a CUDA graph for the loop. */

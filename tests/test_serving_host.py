@@ -74,3 +74,38 @@ def test_latency_percentiles():
         jobs.append(j)
     st = latency_stats(jobs)
     assert st["p50_s"] == 3.0 and st["p99_s"] == 100.0 and abs(st["mean_s"] - 22.0) < 1e-12
+
+
+def test_footprint_counts_gradient_buffers():
+    """fdtd_footprint_bytes (host only): a gradient job needs more than its forward run, and a
+    magnetic-array scene's gradient footprint covers the permeability array and its gradient
+    (4 n_mu bytes per cell each) beyond the same scene with a scalar permeability."""
+    import ctypes as C
+
+    import fdtdx_gb300 as fx
+    from fdtdx_gb300 import _native as N
+    from fdtdx_gb300.build import build
+    from fdtdx_gb300.engine import Scene
+
+    build()  # no-op when the library is up to date
+
+    def scene(permeability):
+        cfg = fx.SimulationConfig(time=20 * 5e-17, grid=fx.UniformGrid(50e-9),
+                                  gradient_config=fx.GradientConfig(recorder=fx.Recorder()))
+        vol = fx.SimulationVolume(shape=(24, 20, 16))
+        objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(4), vol).values())
+        objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((6, 12), (6, 12), (6, 10)),
+                                             material=fx.Material(permittivity=3.0, permeability=permeability)))
+        return fx.place_objects(objs, cfg, device="cpu")
+
+    lib = N.load()
+    sizes = {}
+    for mu in (1.0, (1.5, 1.2, 2.0)):
+        objects, arrays, _, cfg, _ = scene(mu)
+        for rec in (False, True):
+            s = Scene(objects, arrays, cfg, record_interfaces=rec)
+            sizes[(mu, rec)] = lib.fdtd_footprint_bytes(C.byref(s.desc))
+    n = 24 * 20 * 16
+    for mu in (1.0, (1.5, 1.2, 2.0)):
+        assert sizes[(mu, True)] > sizes[(mu, False)] > 0
+    assert sizes[((1.5, 1.2, 2.0), True)] - sizes[(1.0, True)] >= 2 * 4 * 3 * n
