@@ -91,7 +91,9 @@ def source_time_tables(src, config: SimulationConfig) -> tuple[np.ndarray, np.nd
     return on, teff
 
 
-def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> SourceTables:
+def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> list[SourceTables]:
+    """The source records of one source object: one per plane source, one per injected
+    component of a point dipole."""
     dt = config.time_step_duration
     c = config.courant_number
     kind, omega, phase0, ramp_inv, t0s, inv2s2 = _profile_params(src.temporal_profile, src.wave_character, dt)
@@ -113,20 +115,26 @@ def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> Sourc
     d.teff = keep[2].ctypes.data
     d.on = on.ctypes.data
     if isinstance(src, PointDipoleSource):
-        d.kind = N.SRC_DIPOLE
-        d.component = src.polarization
-        d.magnetic = 1 if src.source_type == "magnetic" else 0
-        i, j, k = (st[0][0], st[1][0], st[2][0])
         if src.grid_shape != (1, 1, 1):
             raise ValueError("a point dipole occupies exactly one cell")
-        if d.magnetic:
-            m = arrays.inv_permeabilities
-            local = float(m) if not isinstance(m, torch.Tensor) else float(m[min(src.polarization, m.shape[0] - 1), i, j, k])
-        else:
-            m = arrays.inv_permittivities
-            local = float(m[min(src.polarization, m.shape[0] - 1), i, j, k])
-        d.coef = c * src.amplitude * src.static_amplitude_factor * local
-        return SourceTables(d, keep)
+        i, j, k = (st[0][0], st[1][0], st[2][0])
+        magnetic = src.source_type == "magnetic"
+        m = arrays.inv_permeabilities if magnetic else arrays.inv_permittivities
+        # one record per injected component: the polarization axis alone for an axis-aligned
+        # dipole, every axis the tilted orientation reaches otherwise (dipole.py:219-232), each
+        # scaled by c * amplitude * inv_material[axis] * orientation[axis]
+        orient = src.orientation
+        axes = [src.polarization] if not src.is_tilted else [a for a in range(3) if orient[a] != 0.0]
+        out = []
+        for a in axes:
+            local = float(m) if not isinstance(m, torch.Tensor) else float(m[min(a, m.shape[0] - 1), i, j, k])
+            da = N.SourceDesc.from_buffer_copy(d)
+            da.kind = N.SRC_DIPOLE
+            da.component = a
+            da.magnetic = 1 if magnetic else 0
+            da.coef = c * src.amplitude * src.static_amplitude_factor * local * (1.0 if not src.is_tilted else orient[a])
+            out.append(SourceTables(da, keep))
+        return out
     if isinstance(src, LinearlyPolarizedPlaneSource):
         d.kind = N.SRC_PLANE
         d.normal_axis = src.propagation_axis
@@ -135,7 +143,7 @@ def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> Sourc
         incE, incH, offE, offH = plane_source_profiles(src, arrays, config)
         keep += [incE, incH, offE, offH]
         d.inc_E, d.inc_H, d.off_E, d.off_H = (x.ctypes.data for x in (incE, incH, offE, offH))
-        return SourceTables(d, keep)
+        return [SourceTables(d, keep)]
     raise NotImplementedError(f"source type {type(src).__name__} is not supported")
 
 
@@ -147,6 +155,8 @@ def plane_source_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContai
     H / sqrt(inv_eps / inv_mu) -> offsets = -(k . r) n / (c dt) with r the Yee position of
     each component relative to the plane (calculate_time_offset_yee, fdtdx/core/grid.py:720-880).
     """
+    if src.is_tilted:
+        return _tilted_plane_profiles(src, arrays, config)
     n = src.propagation_axis
     h_ax, v_ax = src.horizontal_axis, src.vertical_axis
     shape = src.grid_shape
@@ -177,6 +187,89 @@ def plane_source_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContai
     kn = k[n]
     offE = np.stack([np.broadcast_to(-(stag_E[q] * dx * kn) * scale, shape) for q in range(3)])
     offH = np.stack([np.broadcast_to(-(stag_H[q] * dx * kn) * scale, shape) for q in range(3)])
+    P = int(np.prod(shape))
+    f32 = lambda x: np.ascontiguousarray(np.broadcast_to(x, (3, *shape)).reshape(3, P), dtype=np.float32)  # noqa: E731
+    return f32(E), f32(Hf), f32(offE), f32(offH)
+
+
+def _interp_renormalised(arr: np.ndarray, pu: np.ndarray, pv: np.ndarray) -> np.ndarray:
+    """Bilinear sampling of a 2-D array at fractional indices (fdtdx/core/misc.py:363-390): the
+    floor / ceil neighbours, weights prod(1 - |index - point|), neighbours outside the array
+    dropped, and the sum divided by (sum of the kept weights + 1e-8)."""
+    acc = np.zeros_like(pu)
+    wsum = np.zeros_like(pu)
+    for iu in (np.floor(pu), np.ceil(pu)):
+        for iv in (np.floor(pv), np.ceil(pv)):
+            ok = (iu >= 0) & (iu < arr.shape[0]) & (iv >= 0) & (iv < arr.shape[1])
+            wgt = np.where(ok, (1.0 - np.abs(iu - pu)) * (1.0 - np.abs(iv - pv)), 0.0)
+            acc += wgt * arr[np.where(ok, iu, 0).astype(np.int64), np.where(ok, iv, 0).astype(np.int64)]
+            wsum += wgt
+    return acc / (wsum + 1e-8)
+
+
+def _tilted_plane_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContainer, config: SimulationConfig):
+    """Incident profiles and Yee time offsets of a plane source tilted by azimuth / elevation.
+
+    Restates LinearlyPolarizedPlaneSource.apply (linear_polarization.py:168-330) on a uniform
+    grid: the plane's cells, taken relative to its centre, are projected onto the plane normal
+    to the tilted wave vector k, written in the in-plane basis u = (e_h - (e_h.k) k) / |...| and
+    v = sign k x u, and the transverse profile is sampled there bilinearly.  The offsets are
+    -(r . k) n / (c dt) with r the Yee position of each component relative to the plane's
+    centre (calculate_time_offset_yee, fdtdx/core/grid.py:720-880), so they vary across the
+    plane.  The kernels read per-cell profiles and offsets, so a tilted source needs no other
+    device path than an untilted one.
+    """
+    n = src.propagation_axis
+    h_ax, v_ax = src.horizontal_axis, src.vertical_axis
+    shape = src.grid_shape
+    dx, dt = config.uniform_spacing(), config.time_step_duration
+    W, Hn = shape[h_ax], shape[v_ax]
+    ch, cv = 0.5 * (W - 1), 0.5 * (Hn - 1)
+    e_pol, h_pol, k = src.polarization_vectors()
+    e_h = np.zeros(3)
+    e_h[h_ax] = 1.0
+    ub = e_h - (e_h @ k) * k
+    ub = ub / np.linalg.norm(ub)
+    vb = (1.0 if src.direction == "+" else -1.0) * np.cross(k, ub)
+    w, hh = np.meshgrid(np.arange(W, dtype=np.float64), np.arange(Hn, dtype=np.float64), indexing="ij")
+    pts = np.zeros((W, Hn, 3))
+    pts[..., h_ax] = w - ch
+    pts[..., v_ax] = hh - cv
+    proj = pts - (pts @ k)[..., None] * k
+    prof_hv = _interp_renormalised(src.amplitude_raw_hv(dx), proj @ ub + ch, proj @ vb + cv)
+    prof = prof_hv.T if h_ax > v_ax else prof_hv
+    amp = np.expand_dims(prof, axis=n)
+    E = amp[None] * e_pol[:, None, None, None]
+    Hf = amp[None] * h_pol[:, None, None, None]
+    sl = (slice(None), *src.grid_slice)
+    ie = arrays.inv_permittivities[sl].detach().double().cpu().numpy()
+    mu = arrays.inv_permeabilities
+    im = mu[sl].detach().double().cpu().numpy() if isinstance(mu, torch.Tensor) else float(mu)
+    if src.normalize_by_energy:
+        energy = (0.5 * (1.0 / ie) * E**2).sum(axis=0) + (0.5 * (1.0 / im) * Hf**2).sum(axis=0)
+        root = math.sqrt(float(energy.sum()))
+        E = E / root
+        Hf = Hf / root
+    Hf = Hf / np.sqrt(ie / im)
+    # Yee positions in the plane's frame: component q of E sits half a cell along axis q, of H
+    # half a cell along the other two axes; the plane's centre is (ch, cv) cells across, 0 along n
+    centre = np.zeros(3)
+    centre[h_ax], centre[v_ax] = ch, cv
+    idx = np.stack(np.meshgrid(*(np.arange(m, dtype=np.float64) for m in shape), indexing="ij"), axis=-1)
+    ie0 = ie[0]
+    im0 = im[0] if isinstance(im, np.ndarray) else im
+    scale = (1.0 / np.sqrt(ie0 * im0)) / (constants.c * dt)
+
+    def offsets(half_along):
+        out = []
+        for q in range(3):
+            stag = np.array([0.5 if half_along(q, a) else 0.0 for a in range(3)])
+            r = (idx + stag - centre) * dx
+            out.append(-(r @ k) * scale)
+        return np.stack(out)
+
+    offE = offsets(lambda q, a: a == q)
+    offH = offsets(lambda q, a: a != q)
     P = int(np.prod(shape))
     f32 = lambda x: np.ascontiguousarray(np.broadcast_to(x, (3, *shape)).reshape(3, P), dtype=np.float32)  # noqa: E731
     return f32(E), f32(Hf), f32(offE), f32(offH)
@@ -326,11 +419,11 @@ class Scene:
             sd.kappa_is_one = 1 if p.kappa_is_one else 0
             sd.coef = tbl.ctypes.data
         self.sources = list(objects.sources)
-        if len(self.sources) > N.MAX_SOURCES:
-            raise ValueError(f"at most {N.MAX_SOURCES} sources")
-        d.n_sources = len(self.sources)
-        for s, src in enumerate(self.sources):
-            tb = build_source(src, arrays, config)
+        records = [tb for src in self.sources for tb in build_source(src, arrays, config)]
+        if len(records) > N.MAX_SOURCES:
+            raise ValueError(f"at most {N.MAX_SOURCES} source records (a tilted point dipole takes up to three)")
+        d.n_sources = len(records)
+        for s, tb in enumerate(records):
             self._keep.append(tb)
             d.sources[s] = tb.desc
         self.detectors = list(objects.forward_detectors)

@@ -361,6 +361,27 @@ def boundary_objects_from_config(config: BoundaryConfig, volume: SimulationVolum
 # --------------------------------------------------------------------------------------------
 
 
+def tilt_vector(vector, azimuth: float, elevation: float, axes: tuple[int, int, int]) -> np.ndarray:
+    """Tilt a vector by azimuth / elevation (radians) in the frame ``axes`` = (horizontal,
+    vertical, propagation) (fdtdx/core/linalg.py:90-160).
+
+    The frame's tilted rows are u = (cos az, 0, sin az) (the horizontal axis turned about the
+    vertical one), v = (0, cos el, sin el) (the vertical axis turned about the horizontal one)
+    and w = u x v / |u x v|.  The vector's frame coordinates go through those rows and back to
+    the global axes, and the result is rescaled to the input's norm: u and v are not orthogonal
+    when both angles are set, so the map is not a rotation and the rescaling is part of it.
+    """
+    vec = np.asarray(vector, dtype=np.float64)
+    frame = np.eye(3)[list(axes)]  # rows: global -> frame coordinates
+    ca, sa, ce, se = math.cos(azimuth), math.sin(azimuth), math.cos(elevation), math.sin(elevation)
+    u = np.array([ca, 0.0, sa])
+    v = np.array([0.0, ce, se])
+    w = np.cross(u, v)
+    w = w / np.linalg.norm(w)
+    out = frame.T @ (np.stack([u, v, w]) @ (frame @ vec))
+    return out / np.linalg.norm(out) * np.linalg.norm(vec)
+
+
 @dataclass(eq=False)
 class Source(SimulationObject):
     wave_character: WaveCharacter = field(default_factory=lambda: WaveCharacter(wavelength=1.55e-6))
@@ -371,7 +392,9 @@ class Source(SimulationObject):
 
 @dataclass(eq=False)
 class PointDipoleSource(Source):
-    """Soft point dipole: E[p] += -c * amp * s(t) * inv_eps[p] at one cell (dipole.py:195-234)."""
+    """Soft point dipole: E[i] += -c * amp * s(t) * inv_eps[i] * p[i] at one cell for the unit
+    orientation p (dipole.py:195-277); axis-aligned (p = e_polarization) unless tilted by
+    ``azimuth_angle`` / ``elevation_angle`` (degrees)."""
 
     polarization: int = 2
     azimuth_angle: float = 0.0
@@ -384,8 +407,21 @@ class PointDipoleSource(Source):
             raise ValueError(f"source_type must be electric or magnetic, got {self.source_type}")
         if self.polarization not in (0, 1, 2):
             raise ValueError(f"polarization must be 0, 1, or 2, got {self.polarization}")
-        if self.azimuth_angle != 0.0 or self.elevation_angle != 0.0:
-            raise NotImplementedError("tilted point dipoles are not supported")
+
+    @property
+    def is_tilted(self) -> bool:
+        return self.azimuth_angle != 0.0 or self.elevation_angle != 0.0
+
+    @property
+    def orientation(self) -> np.ndarray:
+        """Unit orientation: e_polarization tilted in the frame (p+1, p+2, p) (dipole.py:130-148)."""
+        base = np.zeros(3)
+        base[self.polarization] = 1.0
+        if not self.is_tilted:
+            return base
+        p = self.polarization
+        return tilt_vector(base, math.radians(self.azimuth_angle), math.radians(self.elevation_angle),
+                           ((p + 1) % 3, (p + 2) % 3, p))
 
 
 @dataclass(eq=False)
@@ -403,8 +439,8 @@ class LinearlyPolarizedPlaneSource(Source):
     max_horizontal_offset: float = 0.0
 
     def __post_init__(self):
-        if self.azimuth_angle or self.elevation_angle or self.max_angle_random_offset:
-            raise NotImplementedError("tilted plane sources are not supported")
+        if self.max_angle_random_offset:
+            raise NotImplementedError("random plane-source angle offsets are not supported")
         if self.max_vertical_offset or self.max_horizontal_offset:
             raise NotImplementedError("random plane-source offsets are not supported")
 
@@ -420,8 +456,14 @@ class LinearlyPolarizedPlaneSource(Source):
     def vertical_axis(self) -> int:
         return (self.propagation_axis + 2) % 3
 
+    @property
+    def is_tilted(self) -> bool:
+        return self.azimuth_angle != 0.0 or self.elevation_angle != 0.0
+
     def polarization_vectors(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-        """E/H polarization unit vectors and wave vector (fdtdx/core/misc.py:471-553, core/linalg.py:7-47)."""
+        """E/H polarization unit vectors and wave vector (fdtdx/core/misc.py:471-553, core/linalg.py:7-47),
+        all three tilted by the azimuth / elevation angles in the frame (horizontal, vertical,
+        propagation) when the source is tilted."""
         k = np.zeros(3)
         k[self.propagation_axis] = 1.0 if self.direction == "+" else -1.0
         e = None if self.fixed_E_polarization_vector is None else np.asarray(self.fixed_E_polarization_vector, float)
@@ -436,6 +478,10 @@ class LinearlyPolarizedPlaneSource(Source):
             e = np.cross(h, k)
         if h is None:
             h = np.cross(k, e)
+        if self.is_tilted:
+            axes = (self.horizontal_axis, self.vertical_axis, self.propagation_axis)
+            az, el = math.radians(self.azimuth_angle), math.radians(self.elevation_angle)
+            e, h, k = (tilt_vector(x, az, el, axes) for x in (e, h, k))
         return e, h, k
 
     def amplitude_raw_hv(self, spacing: float) -> np.ndarray:

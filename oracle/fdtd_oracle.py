@@ -271,6 +271,47 @@ def profile_amplitude(profile, time: torch.Tensor, period: float, phase_shift: f
 # --------------------------------------------------------------------------------------------
 
 
+def tilt_vector(vec: torch.Tensor, azimuth: float, elevation: float, axes: tuple[int, int, int]) -> torch.Tensor:
+    """rotate_vector (fdtdx/core/linalg.py:90-160, rotation matrices :50-87): global -> raw
+    basis (rows e_h, e_v, e_p), through the rows u = R_1(azimuth) e1, v = R_0(elevation) e2,
+    w = u x v / |u x v|, back to global, rescaled to the input's norm."""
+    dt_ = vec.dtype
+    h_ax, v_ax, p_ax = axes
+    eye = torch.eye(3, dtype=dt_)
+    to_raw = torch.stack((eye[h_ax], eye[v_ax], eye[p_ax]), 0)
+    ca, sa = math.cos(azimuth), math.sin(azimuth)
+    ce, se = math.cos(elevation), math.sin(elevation)
+    az_m = torch.tensor([[ca, 0.0, -sa], [0.0, 1.0, 0.0], [sa, 0.0, ca]], dtype=dt_)
+    el_m = torch.tensor([[1.0, 0.0, 0.0], [0.0, ce, -se], [0.0, se, ce]], dtype=dt_)
+    u = az_m @ torch.tensor([1.0, 0.0, 0.0], dtype=dt_)
+    v = el_m @ torch.tensor([0.0, 1.0, 0.0], dtype=dt_)
+    w = torch.linalg.cross(u, v)
+    w = w / torch.linalg.norm(w)
+    rotated = torch.stack((u, v, w), 0) @ (to_raw @ vec)
+    out = to_raw.T @ rotated
+    return out / torch.linalg.norm(out) * torch.linalg.norm(vec)
+
+
+def linear_interpolated_indexing(points: torch.Tensor, arr: torch.Tensor) -> torch.Tensor:
+    """fdtdx/core/misc.py:363-390 for a batch of 2-D points (P, 2): the floor / ceil corners,
+    weights prod(1 - |corner - point|), corners outside ``arr`` weighted 0 (and read at 0), and
+    sum(w v) / (sum(w) + 1e-8)."""
+    fl, ce = torch.floor(points), torch.ceil(points)
+    num = torch.zeros(points.shape[0], dtype=arr.dtype)
+    den = torch.zeros(points.shape[0], dtype=arr.dtype)
+    for c0 in (fl[:, 0], ce[:, 0]):
+        for c1 in (fl[:, 1], ce[:, 1]):
+            corner = torch.stack((c0, c1), -1)
+            wgt = (1 - (corner - points).abs()).prod(-1)
+            bad = (c0 < 0) | (c0 >= arr.shape[0]) | (c1 < 0) | (c1 >= arr.shape[1])
+            wgt = torch.where(bad, torch.zeros_like(wgt), wgt)
+            i0 = torch.where(bad, torch.zeros_like(c0), c0).long()
+            i1 = torch.where(bad, torch.zeros_like(c1), c1).long()
+            num = num + wgt * arr[i0, i1]
+            den = den + wgt
+    return num / (den + 1e-8)
+
+
 @dataclass
 class OSource:
     obj: Any
@@ -280,6 +321,7 @@ class OSource:
     default_on: bool
     # dipole
     inv_local: torch.Tensor | None = None
+    orient: torch.Tensor | None = None
     # plane
     E_inc: torch.Tensor | None = None
     H_inc: torch.Tensor | None = None
@@ -388,14 +430,22 @@ class OracleScene:
                 local = inv[(slice(None), *s.grid_slice)]
             else:
                 local = torch.tensor(inv, dtype=self.dtype)
-            return OSource(s, "dipole", on, idx, default_on, inv_local=local)
+            # _orientation (dipole.py:130-148)
+            orient = torch.zeros(3, dtype=self.dtype)
+            orient[s.polarization] = 1.0
+            if s.azimuth_angle != 0.0 or s.elevation_angle != 0.0:
+                p = s.polarization
+                orient = tilt_vector(orient, float(np.deg2rad(s.azimuth_angle)), float(np.deg2rad(s.elevation_angle)),
+                                     ((p + 1) % 3, (p + 2) % 3, p))
+            return OSource(s, "dipole", on, idx, default_on, inv_local=local, orient=orient)
         if name in ("GaussianPlaneSource", "UniformPlaneSource"):
             E, H, oE, oH = self._plane_apply(s)
             return OSource(s, "plane", on, idx, default_on, E_inc=E, H_inc=H, off_E=oE, off_H=oH)
         raise NotImplementedError(name)
 
     def _plane_apply(self, s):
-        """LinearlyPolarizedPlaneSource.apply for normal incidence (linear_polarization.py:168-358)."""
+        """LinearlyPolarizedPlaneSource.apply on a uniform grid, normal or tilted incidence
+        (linear_polarization.py:168-358); no random centre or angle offsets."""
         dt_ = self.dtype
         gs = s.grid_shape
         n = gs.index(1)
@@ -415,6 +465,12 @@ class OracleScene:
             e = torch.linalg.cross(h, k)
         if h is None:
             h = torch.linalg.cross(k, e)
+        tilted = s.azimuth_angle != 0.0 or s.elevation_angle != 0.0
+        if getattr(s, "max_angle_random_offset", 0.0):
+            raise NotImplementedError("random angle offsets")
+        if tilted:  # tilted_polarization_vectors (core/misc.py:508-553)
+            az, el = float(np.deg2rad(s.azimuth_angle)), float(np.deg2rad(s.elevation_angle))
+            e, h, k = (tilt_vector(x, az, el, (h_ax, v_ax, n)) for x in (e, h, k))
         # raw amplitude (linear_polarization.py:392-482)
         if type(s).__name__ == "GaussianPlaneSource":
             r = s.radius / self.dx
@@ -425,9 +481,25 @@ class OracleScene:
             prof_hv = prof / prof.sum()
         else:
             prof_hv = s.amplitude * torch.ones((W, Hh), dtype=dt_)
-        # projection of the untilted plane is the identity; linear_interpolated_indexing at an
-        # integer point returns 4 v / (4 + 1e-8) (core/misc.py:363-390)
-        interp = (4.0 * prof_hv) / (4.0 + 1e-8)
+        if tilted:
+            # projection onto the plane normal to k in the basis (u, v) (linear_polarization.py:241-286)
+            e_h = torch.zeros(3, dtype=dt_)
+            e_h[h_ax] = 1.0
+            ub = e_h - torch.dot(e_h, k) * k
+            ub = ub / torch.linalg.norm(ub)
+            vb = (1.0 if s.direction == "+" else -1.0) * torch.linalg.cross(k, ub)
+            w_, h_ = torch.meshgrid(torch.arange(W, dtype=dt_), torch.arange(Hh, dtype=dt_), indexing="ij")
+            wh = (torch.stack([w_, h_], -1) - center).reshape(-1, 2)
+            pt = torch.zeros(wh.shape[0], 3, dtype=dt_)
+            pt[:, h_ax] = wh[:, 0]
+            pt[:, v_ax] = wh[:, 1]
+            proj = pt - (pt @ k)[:, None] * k
+            fp = torch.stack([proj @ ub, proj @ vb], -1) + center
+            interp = linear_interpolated_indexing(fp, prof_hv).reshape(prof_hv.shape)
+        else:
+            # projection of the untilted plane is the identity; linear_interpolated_indexing at an
+            # integer point returns 4 v / (4 + 1e-8) (core/misc.py:363-390)
+            interp = (4.0 * prof_hv) / (4.0 + 1e-8)
         prof2 = interp.T if h_ax > v_ax else interp
         amp = prof2.unsqueeze(n)[None]
         E = amp * e[:, None, None, None]
@@ -562,11 +634,12 @@ def _source_update_E(sc: OracleScene, s: OSource, E, inv_eps, t: float, inverse:
                                 o.wave_character.get_period(), o.wave_character.phase_shift)
         sign = -1.0 if not inverse else 1.0
         scale = c * o.amplitude * o.static_amplitude_factor * amp
-        orient = torch.zeros(3, dtype=dt_)
-        orient[o.polarization] = 1.0
-        oriented = s.inv_local * orient.reshape(3, 1, 1, 1)
-        inj = scale * oriented[o.polarization]
-        return _add_at(E, (o.polarization, *o.grid_slice), sign * inj)
+        oriented = s.inv_local * s.orient.reshape(3, 1, 1, 1)
+        if o.azimuth_angle == 0.0 and o.elevation_angle == 0.0:
+            return _add_at(E, (o.polarization, *o.grid_slice), sign * (scale * oriented[o.polarization]))
+        for axis in range(3):
+            E = _add_at(E, (axis, *o.grid_slice), sign * (scale * oriented[axis]))
+        return E
     # TFSF plane E-side (tfsf.py:193-308, 739-771)
     n = o.grid_shape.index(1)
     a_ax, b_ax = (n + 1) % 3, (n + 2) % 3
@@ -597,11 +670,12 @@ def _source_update_H(sc: OracleScene, s: OSource, H, inv_mu, t: float, inverse: 
                                 o.wave_character.get_period(), o.wave_character.phase_shift)
         sign = -1.0 if not inverse else 1.0
         scale = c * o.amplitude * o.static_amplitude_factor * amp
-        orient = torch.zeros(3, dtype=dt_)
-        orient[o.polarization] = 1.0
-        oriented = s.inv_local * orient.reshape(3, 1, 1, 1)
-        inj = scale * oriented[o.polarization]
-        return _add_at(H, (o.polarization, *o.grid_slice), sign * inj)
+        oriented = s.inv_local * s.orient.reshape(3, 1, 1, 1)
+        if o.azimuth_angle == 0.0 and o.elevation_angle == 0.0:
+            return _add_at(H, (o.polarization, *o.grid_slice), sign * (scale * oriented[o.polarization]))
+        for axis in range(3):
+            H = _add_at(H, (axis, *o.grid_slice), sign * (scale * oriented[axis]))
+        return H
     n = o.grid_shape.index(1)
     a_ax, b_ax = (n + 1) % 3, (n + 2) % 3
     sign = 1 if o.direction == "+" else -1
