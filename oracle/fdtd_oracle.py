@@ -17,6 +17,8 @@ torch autograd for per-step vector-Jacobian products), the reference files:
 * fdtdx/objects/sources/profile.py:253-345, core/window.py:16-30  temporal profiles
 * fdtdx/objects/sources/linear_polarization.py:168-468, tfsf.py:144-409, 739-806,
   fdtdx/core/grid.py:720-880                                   TFSF plane source
+* fdtdx/core/linalg.py:50-160, core/misc.py:363-390, 508-553   source tilt (dipole
+  orientation, tilted plane polarisation, projection and bilinear sampling)
 * fdtdx/objects/detectors/{detector,phasor,field,poynting_flux,energy}.py  detectors
 * fdtdx/fdtd/update.py:1040-1222, fdtdx/fdtd/misc.py:10-66     detectors, interfaces
 * fdtdx/fdtd/forward.py:83-156, backward.py:62-135, fdtd.py:39-418  step and VJP loop
