@@ -389,6 +389,10 @@ class Scene:
         for b in objects.boundary_objects:
             side = 1 if b.direction == "+" else 0
             if isinstance(b, PeriodicBoundary):
+                if b.needs_complex_fields:
+                    raise NotImplementedError(
+                        f"Bloch boundary '{b.name}' has a non-zero Bloch vector along its axis; that needs complex "
+                        "fields, which the GB300 kernels do not carry (a zero vector runs as a periodic boundary)")
                 d.periodic[b.axis] = 1
             elif isinstance(b, PerfectElectricConductor):
                 d.pec_faces |= 1 << (2 * b.axis + side)

@@ -22,6 +22,7 @@ profiles and Yee time offsets, per-step tables) is computed on the host in
 
 from __future__ import annotations
 
+import cmath
 import math
 from dataclasses import dataclass, field
 from typing import Literal, Sequence
@@ -298,8 +299,27 @@ class PeriodicBoundary(BaseBoundary):
     def uses_wrap_padding(self) -> bool:
         return True
 
+    @property
+    def needs_complex_fields(self) -> bool:
+        return False
 
-BlochBoundary = PeriodicBoundary
+
+@dataclass(eq=False)
+class BlochBoundary(PeriodicBoundary):
+    """Wrap halo whose ghost layers carry the Bloch phase F(x + L) = F(x) exp(i k L)
+    (fdtdx/objects/boundaries/bloch.py:13-155): the '+' ghost layer is multiplied by
+    exp(i k L), the '-' one by its conjugate, k the vector's component along the axis.  A zero
+    component is a plain periodic boundary; a non-zero one needs complex fields."""
+
+    bloch_vector: tuple[float, float, float] = (0.0, 0.0, 0.0)
+
+    @property
+    def needs_complex_fields(self) -> bool:
+        return self.bloch_vector[self.axis] != 0.0
+
+    def get_bloch_phase(self, volume_shape, resolution: float) -> complex:
+        """exp(i k L), L = the volume's extent along the axis (uniform grid)."""
+        return cmath.exp(1j * self.bloch_vector[self.axis] * volume_shape[self.axis] * resolution)
 
 
 @dataclass
@@ -319,14 +339,19 @@ class BoundaryConfig:
     thickness_grid_minz: int = 10
     thickness_grid_maxz: int = 10
     pml_kwargs: dict = field(default_factory=dict)
+    bloch_vector: tuple[float, float, float] = (0.0, 0.0, 0.0)
 
     @classmethod
-    def from_uniform_bound(cls, thickness: int = 10, boundary_type: str = "pml", **pml_kwargs) -> "BoundaryConfig":
+    def from_uniform_bound(cls, thickness: int = 10, boundary_type: str = "pml", override_types: dict | None = None,
+                           bloch_vector: tuple[float, float, float] = (0.0, 0.0, 0.0), **pml_kwargs) -> "BoundaryConfig":
+        """One type and thickness on every face, ``override_types`` ({"min_x": "bloch", ...})
+        replacing the type of single faces (initialization.py:444-553)."""
+        override_types = {} if override_types is None else override_types
         kw = {}
         for side in ("minx", "maxx", "miny", "maxy", "minz", "maxz"):
-            kw[f"boundary_type_{side}"] = boundary_type
+            kw[f"boundary_type_{side}"] = override_types.get(f"{side[:3]}_{side[3]}", boundary_type)
             kw[f"thickness_grid_{side}"] = thickness
-        return cls(**kw, pml_kwargs=dict(pml_kwargs))
+        return cls(**kw, pml_kwargs=dict(pml_kwargs), bloch_vector=tuple(float(k) for k in bloch_vector))
 
 
 def boundary_objects_from_config(config: BoundaryConfig, volume: SimulationVolume) -> dict[str, BaseBoundary]:
@@ -343,8 +368,10 @@ def boundary_objects_from_config(config: BoundaryConfig, volume: SimulationVolum
         st[axis] = (0, thick) if direction == "-" else (shape[axis] - thick, shape[axis])
         if btype == "pml":
             obj: BaseBoundary = PerfectlyMatchedLayer(name=kind, axis=axis, direction=direction, **config.pml_kwargs)
-        elif btype in ("periodic", "bloch"):
+        elif btype == "periodic":
             obj = PeriodicBoundary(name=kind, axis=axis, direction=direction)
+        elif btype == "bloch":
+            obj = BlochBoundary(name=kind, axis=axis, direction=direction, bloch_vector=config.bloch_vector)
         elif btype == "pec":
             obj = PerfectElectricConductor(name=kind, axis=axis, direction=direction)
         elif btype == "pmc":

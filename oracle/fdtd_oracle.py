@@ -11,6 +11,8 @@ torch autograd for per-step vector-Jacobian products), the reference files:
 * fdtdx/fdtd/update.py:256-1007       update_E / update_H and their reverses
 * fdtdx/core/physics/curl.py:86-397   curls with CPML corrections, co-location
 * fdtdx/core/misc.py:615-641          halo padding
+* fdtdx/fdtd/update.py:92-136, objects/boundaries/bloch.py:13-155, fdtd/initialization.py:581-594
+                                      Bloch ghost-layer phases and complex fields
 * fdtdx/objects/boundaries/perfectly_matched_layer.py:69-275   CPML coefficients
 * fdtdx/objects/boundaries/pec.py:71-77, pmc.py:62-76          conductor walls
 * fdtdx/objects/sources/dipole.py:150-277                      point dipole
@@ -66,8 +68,12 @@ def jax_index(n: int, t: int) -> int:
 # --------------------------------------------------------------------------------------------
 
 
-def pad_fields(f: torch.Tensor, periodic: tuple[bool, bool, bool]) -> torch.Tensor:
-    """One-cell halo per axis, wrap or zero, applied axis by axis (fdtdx/core/misc.py:615-641)."""
+def pad_fields(f: torch.Tensor, periodic: tuple[bool, bool, bool], bloch=()) -> torch.Tensor:
+    """One-cell halo per axis, wrap or zero, applied axis by axis (fdtdx/core/misc.py:615-641),
+    then the Bloch ghost-cell phases (fdtdx/fdtd/update.py:92-136,
+    objects/boundaries/bloch.py:59-94): for each (axis, direction, phase) of a Bloch boundary
+    with a non-zero vector, the '-' ghost layer (wrapped from the far end) is multiplied by
+    conj(phase) and the '+' ghost layer by phase, phase = exp(i k L)."""
     for ax, per in enumerate(periodic):
         d = ax + 1
         n = f.shape[d]
@@ -77,6 +83,11 @@ def pad_fields(f: torch.Tensor, periodic: tuple[bool, bool, bool]) -> torch.Tens
             z = torch.zeros_like(f.narrow(d, 0, 1))
             lo, hi = z, z
         f = torch.cat([lo, f, hi], dim=d)
+    for ax, direction, phase in bloch:
+        f = f.clone()
+        idx = [slice(None)] * f.dim()
+        idx[ax + 1] = 0 if direction == "-" else -1
+        f[tuple(idx)] = f[tuple(idx)] * (phase.conj() if direction == "-" else phase)
     return f
 
 
@@ -360,10 +371,16 @@ class OracleScene:
         self.sigma_H = sh.detach().to("cpu", dtype) if sh is not None else None
         self.periodic = [False, False, False]
         self.pec, self.pmc, self.pmls = [], [], []
+        self.bloch = []  # (axis, direction, exp(i k L)) of Bloch boundaries with k != 0
+        cdt = torch.complex128 if dtype == torch.float64 else torch.complex64
         for b in objects.boundary_objects:
             name = type(b).__name__
             if name in ("PeriodicBoundary", "BlochBoundary"):
                 self.periodic[b.axis] = True
+                k = float(getattr(b, "bloch_vector", (0.0, 0.0, 0.0))[b.axis])
+                if k != 0.0:  # get_bloch_phase (bloch.py:133-155), uniform grid
+                    L = self.shape[b.axis] * self.dx
+                    self.bloch.append((b.axis, b.direction, torch.exp(torch.tensor(1j * k * L, dtype=cdt))))
             elif name == "PerfectElectricConductor":
                 self.pec.append(b)
             elif name == "PerfectMagneticConductor":
@@ -375,6 +392,8 @@ class OracleScene:
                          co["inv_kappa_E"], co["a_H"], co["b_H"], co["inv_kappa_H"])
                 )
         self.periodic = tuple(self.periodic)
+        # complex fields exactly when a Bloch vector is non-zero (fdtd/initialization.py:581-594)
+        self.field_dtype = cdt if self.bloch else dtype
         self.sources = [self._setup_source(s) for s in objects.sources]
         self.detectors = [self._setup_detector(d) for d in objects.detectors if not d.inverse]
         self._setup_time_filter(config)
@@ -557,11 +576,16 @@ class OracleScene:
         kind = {"FieldDetector": "field", "PoyntingFluxDetector": "flux", "EnergyDetector": "energy"}[name]
         return ODetector(d, kind, on, idx)
 
+    def pad(self, f: torch.Tensor) -> torch.Tensor:
+        """pad_fields_for_boundaries (fdtdx/fdtd/update.py:92-136) without symmetry planes."""
+        return pad_fields(f, self.periodic, self.bloch)
+
     # ---- state
     def init_state(self) -> "OState":
-        z = torch.zeros((3, *self.shape), dtype=self.dtype)
-        psi_E = {p.name: (torch.zeros(_slab_shape(self.shape, p), dtype=self.dtype),) * 2 for p in self.pmls}
-        psi_H = {p.name: (torch.zeros(_slab_shape(self.shape, p), dtype=self.dtype),) * 2 for p in self.pmls}
+        fdt = self.field_dtype
+        z = torch.zeros((3, *self.shape), dtype=fdt)
+        psi_E = {p.name: (torch.zeros(_slab_shape(self.shape, p), dtype=fdt),) * 2 for p in self.pmls}
+        psi_H = {p.name: (torch.zeros(_slab_shape(self.shape, p), dtype=fdt),) * 2 for p in self.pmls}
         det = {}
         for od in self.detectors:
             d = od.obj
@@ -778,10 +802,11 @@ def avg_aniso_H(field_pad, component: int, location: int):
     return out[1:-1, 1:-1, 1:-1]
 
 
-def aniso_apply(A, B, F, curl, periodic, avg, sign: float):
+def aniso_apply(A, B, F, curl, pad, avg, sign: float):
     """Rows of update.py:474-492 / 791-807: F_i = sum_j A_ij F_j@i + sign sum_j B_ij curl_j@i,
-    the diagonal terms local, the off-diagonal ones averaged onto component i's location."""
-    F_pad, K_pad = pad_fields(F, periodic), pad_fields(curl, periodic)
+    the diagonal terms local, the off-diagonal ones averaged onto component i's location
+    (``pad`` is the scene's halo, Bloch phases included)."""
+    F_pad, K_pad = pad(F), pad(curl)
     rows = []
     for i in range(3):
         acc_a = A[i, i] * F[i]
@@ -808,11 +833,11 @@ def _full_tensor(inv, sigma) -> bool:
 def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=True):
     """fdtdx/fdtd/update.py:256-523 (isotropic / diagonal branch)."""
     c = sc.courant
-    curl, psi_E = curl_H(pad_fields(H, sc.periodic), psi_E, sc.pmls, simulate_boundaries)
+    curl, psi_E = curl_H(sc.pad(H), psi_E, sc.pmls, simulate_boundaries)
     sig = sc.sigma_E
     if _full_tensor(inv_eps, sig):  # update.py:356-492
         A, B = aniso_update_matrices(expand_to_3x3(inv_eps), expand_to_3x3(sig), c, ETA0)
-        E = aniso_apply(A, B, E, curl, sc.periodic, avg_aniso_E, 1.0)
+        E = aniso_apply(A, B, E, curl, sc.pad, avg_aniso_E, 1.0)
         E = _apply_sources(sc, E, inv_eps, t, True, False)
         return _walls(sc, E, sc.pec), psi_E
     factor = 1
@@ -828,11 +853,11 @@ def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=
 def update_H(sc: OracleScene, t: int, E, H, psi_H, inv_mu, simulate_boundaries=True):
     """fdtdx/fdtd/update.py:689-853 (isotropic / diagonal branch)."""
     c = sc.courant
-    curl, psi_H = curl_E(pad_fields(E, sc.periodic), psi_H, sc.pmls, simulate_boundaries)
+    curl, psi_H = curl_E(sc.pad(E), psi_H, sc.pmls, simulate_boundaries)
     sig = sc.sigma_H
     if _full_tensor(inv_mu, sig):  # update.py:751-807
         A, B = aniso_update_matrices(expand_to_3x3(inv_mu), expand_to_3x3(sig), c, 1 / ETA0)
-        H = aniso_apply(A, B, H, curl, sc.periodic, avg_aniso_H, -1.0)
+        H = aniso_apply(A, B, H, curl, sc.pad, avg_aniso_H, -1.0)
         H = _apply_sources(sc, H, inv_mu, t, False, False)
         return _walls(sc, H, sc.pmc), psi_H
     factor = 1
@@ -849,11 +874,11 @@ def update_E_reverse(sc: OracleScene, t: int, E, H, psi_E, inv_eps):
     """fdtdx/fdtd/update.py:526-686."""
     c = sc.courant
     E = _apply_sources(sc, E, inv_eps, t, True, True)
-    curl, _ = curl_H(pad_fields(H, sc.periodic), psi_E, sc.pmls, False)
+    curl, _ = curl_H(sc.pad(H), psi_E, sc.pmls, False)
     sig = sc.sigma_E
     if _full_tensor(inv_eps, sig):  # update.py:641-676
         A, B = aniso_update_matrices(expand_to_3x3(inv_eps), expand_to_3x3(sig), c, ETA0, reverse=True)
-        return _walls(sc, aniso_apply(A, B, E, curl, sc.periodic, avg_aniso_E, -1.0), sc.pec)
+        return _walls(sc, aniso_apply(A, B, E, curl, sc.pad, avg_aniso_E, -1.0), sc.pec)
     factor = 1
     if sig is not None:
         E = E * (1 + c * sig * ETA0 * inv_eps / 2)
@@ -866,11 +891,11 @@ def update_H_reverse(sc: OracleScene, t: int, E, H, psi_H, inv_mu):
     """fdtdx/fdtd/update.py:856-1007."""
     c = sc.courant
     H = _apply_sources(sc, H, inv_mu, t, False, True)
-    curl, _ = curl_E(pad_fields(E, sc.periodic), psi_H, sc.pmls, False)
+    curl, _ = curl_E(sc.pad(E), psi_H, sc.pmls, False)
     sig = sc.sigma_H
     if _full_tensor(inv_mu, sig):  # update.py:956-995
         A, B = aniso_update_matrices(expand_to_3x3(inv_mu), expand_to_3x3(sig), c, 1 / ETA0, reverse=True)
-        return _walls(sc, aniso_apply(A, B, H, curl, sc.periodic, avg_aniso_H, 1.0), sc.pmc)
+        return _walls(sc, aniso_apply(A, B, H, curl, sc.pad, avg_aniso_H, 1.0), sc.pmc)
     factor = 1
     if sig is not None:
         H = H * (1 + c * sig / ETA0 * inv_mu / 2)
@@ -895,7 +920,7 @@ def update_detectors(sc: OracleScene, t: int, E, H, H_prev, det: dict, inv_eps, 
         gs = (slice(None), *d.grid_slice)
         if d.exact_interpolation:
             if full is None:
-                full = interpolate_fields(pad_fields(E, sc.periodic), pad_fields((H_prev + H) / 2, sc.periodic))
+                full = interpolate_fields(sc.pad(E), sc.pad((H_prev + H) / 2))
             Er, Hr = full[0][gs], full[1][gs]
         else:
             Er, Hr = E[gs], H[gs]
@@ -916,14 +941,19 @@ def update_detectors(sc: OracleScene, t: int, E, H, H_prev, det: dict, inv_eps, 
         elif od.kind == "field":
             if d.reduce_volume:
                 EH = EH.mean(dim=(1, 2, 3))
+            if EH.is_complex() and not st["fields"].is_complex():
+                EH = EH.real  # a real state keeps the real part (JAX's complex -> float cast)
             idx = od.arr_idx[jax_index(sc.T, t)]
             out[d.name] = {"fields": _set_at(st["fields"], idx, EH)}
         elif od.kind == "flux":
+            Hc = Hr.conj() if Hr.is_complex() else Hr  # Re(E x conj(H)) (core/physics/metrics.py:99-117)
             S = torch.stack([
-                Er[1] * Hr[2] - Er[2] * Hr[1],
-                Er[2] * Hr[0] - Er[0] * Hr[2],
-                Er[0] * Hr[1] - Er[1] * Hr[0],
+                Er[1] * Hc[2] - Er[2] * Hc[1],
+                Er[2] * Hc[0] - Er[0] * Hc[2],
+                Er[0] * Hc[1] - Er[1] * Hc[0],
             ], 0)
+            if S.is_complex():
+                S = S.real
             pf = S if d.keep_all_components else S[d.propagation_axis]
             if d.direction == "-":
                 pf = -pf
@@ -935,7 +965,10 @@ def update_detectors(sc: OracleScene, t: int, E, H, H_prev, det: dict, inv_eps, 
         else:  # energy
             ie = inv_eps[gs]
             im = inv_mu[gs] if isinstance(inv_mu, torch.Tensor) else inv_mu
-            e = (0.5 * (1 / ie) * Er**2).sum(0) + (0.5 * (1 / im) * Hr**2).sum(0)
+            if Er.is_complex():  # |E|^2 (core/physics/metrics.py:15-60)
+                e = (0.5 * (1 / ie) * Er.abs() ** 2).sum(0) + (0.5 * (1 / im) * Hr.abs() ** 2).sum(0)
+            else:
+                e = (0.5 * (1 / ie) * Er**2).sum(0) + (0.5 * (1 / im) * Hr**2).sum(0)
             if d.reduce_volume:
                 e = (e * sc.dx**3).sum().reshape(1)
             idx = od.arr_idx[jax_index(sc.T, t)]
