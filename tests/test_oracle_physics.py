@@ -20,10 +20,17 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
 * a broadband pulse's stack transmission against single-frequency runs at three wavelengths
   (tests/simulation/fdtd/test_pulsed_vs_cw.py, 5%; the oracle gives 1.8-2.6%);
 * a uniform plane source is linear in its amplitude factor and uniform across the periodic
-  cross-section (tests/simulation/physics/sources/test_plane_source.py:108-146).
+  cross-section (tests/simulation/physics/sources/test_plane_source.py:108-146);
+* birefringence in eps = diag(2.25, 4, 1): k and impedance 1/n of the ordinary (x) and
+  extraordinary (y) polarisations (tests/simulation/physics/test_birefringence.py, 5%);
+* point-dipole radiation: outward flux through six planes, x / y symmetry and a weaker axial
+  flux for a z-dipole, the minimum along x for an x-dipole, and a 45-degree tilted dipole's
+  x = z, y > x pattern at equal total power
+  (tests/simulation/physics/sources/test_dipole_radiation.py:138-312, 10%, 40^3 box).
 
-All use the reference's quasi-1D domains: 3 x 3 periodic cells across, CPML along z, a +z
-uniform plane source with Ex polarisation (the default CW profile unless stated).
+The plane-wave checks use the reference's quasi-1D domains: 3 x 3 periodic cells across,
+CPML along z, a +z uniform plane source with Ex polarisation (the default CW profile unless
+stated).
 """
 
 import math
@@ -258,3 +265,81 @@ def test_uniform_plane_source_linearity_and_uniformity():
     assert float((mag - mag.mean()).abs().max() / mag.mean()) < 0.01
     ph = torch.angle(a1 / a1[0, 0])
     assert float(ph.abs().max()) < 0.02
+
+
+@pytest.mark.parametrize("pol", [0, 1])
+def test_birefringence_wavenumber_and_impedance(pol):
+    """A diagonally anisotropic fill eps = diag(2.25, 4, 1): an x-polarised wave travels with
+    k_o = 2 pi 1.5 / lambda and |Ex| / |Hy| = 1 / 1.5, a y-polarised one with k_e = 2 pi 2 /
+    lambda and |Ey| / |Hx| = 1 / 2 (tests/simulation/physics/test_birefringence.py:1-300, 5%)."""
+    dx, nz, sep = 50e-9, 80, 3
+    cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(3, 3, nz))
+    bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                           boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                           thickness_grid_minz=10, thickness_grid_maxz=10)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    objs.append(fx.UniformMaterialObject(name="fill", grid_slice_tuple=((0, 3), (0, 3), (0, nz)),
+                                         material=fx.Material(permittivity=(2.25, 4.0, 1.0))))
+    e_pol = (1, 0, 0) if pol == 0 else (0, 1, 0)
+    wc = fx.WaveCharacter(wavelength=WL)
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 3), (0, 3), (12, 13)), direction="+",
+                                      fixed_E_polarization_vector=e_pol, wave_character=wc))
+    comps = ("Ex", "Hy") if pol == 0 else ("Ey", "Hx")
+    for name, z in (("d1", 17), ("d2", 17 + sep)):
+        objs.append(fx.PhasorDetector(name=name, grid_slice_tuple=((1, 2), (1, 2), (z, z + 1)), wave_characters=(wc,),
+                                      components=comps, reduce_volume=True))
+    _, st = _run(cfg, objs)
+    p1 = st.det["d1"]["phasor"].reshape(-1)
+    p2 = st.det["d2"]["phasor"].reshape(-1)
+    e1, h1, e2 = complex(p1[0]), complex(p1[1]), complex(p2[0])
+    assert abs(e1) > 0 and abs(e2) > 0
+    n = 1.5 if pol == 0 else 2.0
+    k = ((np.angle(e2) - np.angle(e1)) % (2 * math.pi)) / (sep * dx)
+    k_ref = 2 * math.pi * n / WL
+    assert abs(k - k_ref) / k_ref < TOL, (k, k_ref)
+    z = abs(e1) / abs(h1)
+    assert abs(z - 1 / n) / (1 / n) < TOL, (z, 1 / n)
+
+
+def _dipole_fluxes(pol: int, azimuth: float = 0.0) -> dict:
+    """Time-averaged flux through six full-width planes 8 cells from a CW point dipole at the
+    centre of a 40^3 CPML box (50 nm cells)."""
+    n, off = 40, 8
+    cfg = fx.SimulationConfig(time=60e-15, grid=fx.UniformGrid(50e-9))
+    vol = fx.SimulationVolume(shape=(n, n, n))
+    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(8), vol).values())
+    c = n // 2
+    objs.append(fx.PointDipoleSource(name="dip", grid_slice_tuple=((c, c + 1),) * 3, polarization=pol,
+                                     azimuth_angle=azimuth, wave_character=fx.WaveCharacter(wavelength=WL)))
+    for ax in range(3):
+        for side in "+-":
+            st = [(0, n)] * 3
+            pos = c + off if side == "+" else c - off
+            st[ax] = (pos, pos + 1)
+            objs.append(fx.PoyntingFluxDetector(name=f"{'xyz'[ax]}{side}", grid_slice_tuple=tuple(st), direction=side,
+                                                fixed_propagation_axis=ax, reduce_volume=True))
+    sc, st = _run(cfg, objs)
+    spp = round(WL / (C0 * sc.dt))
+    return {k: float(v["poynting_flux"][:, 0].double()[-10 * spp:].mean()) for k, v in st.det.items()}
+
+
+def test_dipole_radiation_pattern():
+    """A z-dipole radiates outward through all six planes, equally through +-x and +-y and less
+    along its axis; an x-dipole radiates least along x and the same total power; a z-dipole
+    tilted 45 degrees in azimuth sends equal power through the x and z planes, more through y,
+    and the same total (tests/simulation/physics/sources/test_dipole_radiation.py:138-312, 10%,
+    on a 40^3 box instead of 60^3)."""
+    fz = _dipole_fluxes(2)
+    total = sum(fz.values())
+    assert all(v > 0 for v in fz.values()) and total > 0
+    assert abs(fz["x+"] - fz["x-"]) / fz["x+"] < 0.1 and abs(fz["x+"] - fz["y+"]) / fz["x+"] < 0.1
+    assert fz["z+"] < fz["x+"]
+    fx_ = _dipole_fluxes(0)
+    per_axis = [fx_[f"{a}+"] + fx_[f"{a}-"] for a in "xyz"]
+    assert int(np.argmin(per_axis)) == 0
+    assert abs(sum(fx_.values()) - total) / total < 0.1
+    ft = _dipole_fluxes(2, azimuth=45.0)
+    sx, sy, sz = (abs(ft[f"{a}+"]) + abs(ft[f"{a}-"]) for a in "xyz")
+    assert abs(sx - sz) / sx < 0.1 and sy > sx
+    assert abs(sum(ft.values()) - total) / total < 0.1
