@@ -25,8 +25,10 @@ torch autograd for per-step vector-Jacobian products), the reference files:
 * fdtdx/fdtd/update.py:1040-1222, fdtdx/fdtd/misc.py:10-66     detectors, interfaces
 * fdtdx/fdtd/forward.py:83-156, backward.py:62-135, fdtd.py:39-418  step and VJP loop
 * fdtdx/fdtd/update.py:356-523, 641-676, 751-807, 956-995, fdtdx/fdtd/misc.py:69-213,
-  fdtdx/core/misc.py:557-611   full 3x3 anisotropic update branch (uniform grid); the
-  GB300 library does not build this branch yet, the oracle states it for its pins
+  fdtdx/core/misc.py:557-611   full 3x3 anisotropic update branch (uniform grid), with
+  the tensor branches of the sources (dipole.py:15-37, tfsf.py:144-190, 287-299, 384-393)
+  and of the energy detector (core/physics/metrics.py:34-51); the GB300 library does not
+  build this branch yet, the oracle states it for its pins
 
 Parity status: the reference is JAX and JAX cannot be installed on these machines,
 so the reference itself cannot be run.  The reference's tests hold no stored field
@@ -528,12 +530,29 @@ class OracleScene:
         sl = (slice(None), *s.grid_slice)
         ie = self.inv_eps[sl]
         im = self.inv_mu[sl] if isinstance(self.inv_mu, torch.Tensor) else self.inv_mu
+        full = _is9(ie) or _is9(im)
+        if full:  # tensor media: eps = inv(inv_eps) per cell (core/physics/metrics.py:34-51, tfsf.py:144-190)
+            eps_t = _tensor_inverse(expand_to_3x3(ie)).to(dt_).expand(3, 3, *gs)
+            mu_t = _tensor_inverse(expand_to_3x3(im)).to(dt_).expand(3, 3, *gs)
         if s.normalize_by_energy:
-            energy = (0.5 * (1 / ie) * E.abs() ** 2).sum(0) + (0.5 * (1 / im) * H.abs() ** 2).sum(0)
+            if full:
+                energy = 0.5 * torch.einsum("ixyz,ijxyz,jxyz->xyz", E.conj(), eps_t.to(E.dtype), E).real \
+                    + 0.5 * torch.einsum("ixyz,ijxyz,jxyz->xyz", H.conj(), mu_t.to(H.dtype), H).real
+            else:
+                energy = (0.5 * (1 / ie) * E.abs() ** 2).sum(0) + (0.5 * (1 / im) * H.abs() ** 2).sum(0)
             root = torch.sqrt(energy.sum())
             E = E / root
             H = H / root
-        H = H / torch.sqrt(ie / im)
+        if full:
+            eps_eff = torch.einsum("i,ijxyz,j->xyz", e, eps_t, e)
+            mu_eff = torch.einsum("i,ijxyz,j->xyz", h, mu_t, h)
+            H = H / torch.sqrt(mu_eff / eps_eff)
+            for m in (ie, im):  # grid.py:781-861: tensor media must be isotropic here
+                if _is9(m) and not (torch.allclose(m[0], m[4]) and torch.allclose(m[4], m[8]) and all(
+                        torch.allclose(m[q], torch.zeros_like(m[q])) for q in (1, 2, 3, 5, 6, 7))):
+                    raise NotImplementedError("Gaussian or planewave sources within anisotropic materials")
+        else:
+            H = H / torch.sqrt(ie / im)
         # calculate_time_offset_yee (fdtdx/core/grid.py:720-880), uniform edges
         edges = [torch.arange(gs[ax] + 1, dtype=dt_) * self.dx for ax in range(3)]
         cphys = torch.zeros(3, dtype=dt_)
@@ -649,6 +668,29 @@ def _src_time(sc: OracleScene, s: OSource, t: float, eside: bool):
     return on, adj + half
 
 
+def _is9(m) -> bool:
+    return isinstance(m, torch.Tensor) and m.dim() > 0 and m.shape[0] == 9
+
+
+def contract_orientation(inv_local, orient: torch.Tensor) -> torch.Tensor:
+    """_contract_orientation (dipole.py:15-37): sum_j inv_ij p_j for a 9-component tensor,
+    inv_i p_i for the isotropic / diagonal forms (a scalar or 1-component value broadcasts)."""
+    if _is9(inv_local):
+        return torch.einsum("ij...,j->i...", inv_local.reshape(3, 3, *inv_local.shape[1:]), orient.to(inv_local.dtype))
+    return inv_local * orient.reshape(3, 1, 1, 1)
+
+
+def _dipole_inject(F, o, s: OSource, scale, sign):
+    """dipole.py:219-232 / 260-273: one component for an untilted dipole in an isotropic or
+    diagonal medium, every component otherwise (tilted, or a full-tensor medium)."""
+    oriented = contract_orientation(s.inv_local, s.orient)
+    if o.azimuth_angle == 0.0 and o.elevation_angle == 0.0 and not _is9(s.inv_local):
+        return _add_at(F, (o.polarization, *o.grid_slice), sign * (scale * oriented[o.polarization]))
+    for axis in range(3):
+        F = _add_at(F, (axis, *o.grid_slice), sign * (scale * oriented[axis]))
+    return F
+
+
 def _source_update_E(sc: OracleScene, s: OSource, E, inv_eps, t: float, inverse: bool):
     o = s.obj
     c = sc.courant
@@ -660,12 +702,7 @@ def _source_update_E(sc: OracleScene, s: OSource, E, inv_eps, t: float, inverse:
                                 o.wave_character.get_period(), o.wave_character.phase_shift)
         sign = -1.0 if not inverse else 1.0
         scale = c * o.amplitude * o.static_amplitude_factor * amp
-        oriented = s.inv_local * s.orient.reshape(3, 1, 1, 1)
-        if o.azimuth_angle == 0.0 and o.elevation_angle == 0.0:
-            return _add_at(E, (o.polarization, *o.grid_slice), sign * (scale * oriented[o.polarization]))
-        for axis in range(3):
-            E = _add_at(E, (axis, *o.grid_slice), sign * (scale * oriented[axis]))
-        return E
+        return _dipole_inject(E, o, s, scale, sign)
     # TFSF plane E-side (tfsf.py:193-308, 739-771)
     n = o.grid_shape.index(1)
     a_ax, b_ax = (n + 1) % 3, (n + 2) % 3
@@ -678,6 +715,12 @@ def _source_update_E(sc: OracleScene, s: OSource, E, inv_eps, t: float, inverse:
         time_H = (t + s.off_H[ax]) * sc.dt
         amp[ax] = profile_amplitude(o.temporal_profile, time_H, o.wave_character.get_period(),
                                     o.wave_character.phase_shift) * o.static_amplitude_factor
+    if _is9(ies):  # fully anisotropic face (tfsf.py:287-299): every row picks up both tangential terms
+        Hb_inc, Ha_inc = s.H_inc[b_ax] * amp[b_ax], s.H_inc[a_ax] * amp[a_ax]
+        for row in (n, a_ax, b_ax):
+            corr = c * (ies[row * 3 + a_ax] * Hb_inc + ies[row * 3 + b_ax] * (-Ha_inc))
+            E = _add_at(E, (row, *o.grid_slice), sign * corr)
+        return E
     Hb = s.H_inc[b_ax] * amp[b_ax] * c * ies[min(a_ax, ies.shape[0] - 1)]
     Ha = s.H_inc[a_ax] * amp[a_ax] * c * ies[min(b_ax, ies.shape[0] - 1)]
     E = _add_at(E, (a_ax, *o.grid_slice), sign * Hb)
@@ -696,27 +739,29 @@ def _source_update_H(sc: OracleScene, s: OSource, H, inv_mu, t: float, inverse: 
                                 o.wave_character.get_period(), o.wave_character.phase_shift)
         sign = -1.0 if not inverse else 1.0
         scale = c * o.amplitude * o.static_amplitude_factor * amp
-        oriented = s.inv_local * s.orient.reshape(3, 1, 1, 1)
-        if o.azimuth_angle == 0.0 and o.elevation_angle == 0.0:
-            return _add_at(H, (o.polarization, *o.grid_slice), sign * (scale * oriented[o.polarization]))
-        for axis in range(3):
-            H = _add_at(H, (axis, *o.grid_slice), sign * (scale * oriented[axis]))
-        return H
+        return _dipole_inject(H, o, s, scale, sign)
     n = o.grid_shape.index(1)
     a_ax, b_ax = (n + 1) % 3, (n + 2) % 3
     sign = 1 if o.direction == "+" else -1
     if inverse:
         sign = -sign
-    if isinstance(inv_mu, torch.Tensor):
-        ims = inv_mu.detach()[(slice(None), *o.grid_slice)]
-        im_a, im_b = ims[min(a_ax, ims.shape[0] - 1)], ims[min(b_ax, ims.shape[0] - 1)]
-    else:
-        im_a = im_b = inv_mu
     amp = {}
     for ax in (a_ax, b_ax):
         time_E = (t + s.off_E[ax]) * sc.dt
         amp[ax] = profile_amplitude(o.temporal_profile, time_E, o.wave_character.get_period(),
                                     o.wave_character.phase_shift) * o.static_amplitude_factor
+    if _is9(inv_mu):  # fully anisotropic face (tfsf.py:384-393)
+        ims = inv_mu.detach()[(slice(None), *o.grid_slice)]
+        Ea_inc, Eb_inc = s.E_inc[a_ax] * amp[a_ax], s.E_inc[b_ax] * amp[b_ax]
+        for row in (n, a_ax, b_ax):
+            corr = c * (ims[row * 3 + a_ax] * (-Eb_inc) + ims[row * 3 + b_ax] * Ea_inc)
+            H = _add_at(H, (row, *o.grid_slice), sign * corr)
+        return H
+    if isinstance(inv_mu, torch.Tensor):
+        ims = inv_mu.detach()[(slice(None), *o.grid_slice)]
+        im_a, im_b = ims[min(a_ax, ims.shape[0] - 1)], ims[min(b_ax, ims.shape[0] - 1)]
+    else:
+        im_a = im_b = inv_mu
     Ea = s.E_inc[a_ax] * amp[a_ax] * c * im_b
     Eb = s.E_inc[b_ax] * amp[b_ax] * c * im_a
     H = _add_at(H, (b_ax, *o.grid_slice), sign * Ea)
@@ -762,6 +807,14 @@ def expand_to_3x3(arr):
     z = torch.zeros(arr.shape[1:], dtype=arr.dtype)
     d = [arr[0], arr[0], arr[0]] if n == 1 else [arr[0], arr[1], arr[2]]
     return torch.stack([torch.stack([d[r] if q == r else z for q in range(3)]) for r in range(3)])
+
+
+def _tensor_inverse(m: torch.Tensor) -> torch.Tensor:
+    """Per-cell inverse of a (3, 3, ...) tensor field (3 x 3 blocks moved last and back)."""
+    k = m.dim() - 2
+    perm = tuple(range(2, 2 + k)) + (0, 1)
+    back = (k, k + 1) + tuple(range(k))
+    return torch.linalg.inv(m.permute(perm)).permute(back)
 
 
 def aniso_update_matrices(inv, sigma, c: float, eta_factor: float, reverse: bool = False):
@@ -965,7 +1018,12 @@ def update_detectors(sc: OracleScene, t: int, E, H, H_prev, det: dict, inv_eps, 
         else:  # energy
             ie = inv_eps[gs]
             im = inv_mu[gs] if isinstance(inv_mu, torch.Tensor) else inv_mu
-            if Er.is_complex():  # |E|^2 (core/physics/metrics.py:15-60)
+            if _is9(ie) or _is9(im):  # 0.5 Re(E* eps E) + 0.5 Re(H* mu H) (core/physics/metrics.py:34-51)
+                eps_t = _tensor_inverse(expand_to_3x3(ie)).to(sc.dtype).expand(3, 3, *Er.shape[1:])
+                mu_t = _tensor_inverse(expand_to_3x3(im)).to(sc.dtype).expand(3, 3, *Er.shape[1:])
+                e = 0.5 * torch.einsum("ixyz,ijxyz,jxyz->xyz", Er.conj(), eps_t.to(Er.dtype), Er).real \
+                    + 0.5 * torch.einsum("ixyz,ijxyz,jxyz->xyz", Hr.conj(), mu_t.to(Hr.dtype), Hr).real
+            elif Er.is_complex():  # |E|^2 (core/physics/metrics.py:15-60)
                 e = (0.5 * (1 / ie) * Er.abs() ** 2).sum(0) + (0.5 * (1 / im) * Hr.abs() ** 2).sum(0)
             else:
                 e = (0.5 * (1 / ie) * Er**2).sum(0) + (0.5 * (1 / im) * Hr**2).sum(0)

@@ -101,3 +101,6 @@ def test_reversible_fdtd_rejects_unsupported_material_inputs():
     mu0 = arrays.aset("inv_permeabilities", torch.tensor(1.0, requires_grad=True))
     with pytest.raises(NotImplementedError):
         fx.reversible_fdtd(mu0, objects, cfg)
+    # the forward path refuses a full tensor on the host too, before its source tables are built
+    with pytest.raises(NotImplementedError, match="9-component"):
+        fx.run_fdtd(full, objects, cfg)

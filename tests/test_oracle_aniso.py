@@ -4,8 +4,12 @@ The reference's own known-answer tests for the averaging stencils and the update
 (tests/unit/fdtd/test_fdtd_misc.py:158-395) are replayed on the oracle's restatement, and
 the branch is checked to reduce to the diagonal update when the off-diagonal entries are
 zero (the reference takes the diagonal branch for (1 | 3)-component arrays and the tensor
-branch for 9-component ones; both must agree on a diagonal tensor).  The GB300 library does
-not build this branch yet; these pins keep the oracle ready for it.
+branch for 9-component ones; both must agree on a diagonal tensor).  The same holds for the
+tensor branches of the sources (dipole contraction, TFSF faces, plane impedance and energy
+normalisation) and of the energy detector, and the reference's full-tensor dipole check
+(tests/unit/objects/sources/test_dipole.py:178-193) is replayed.  The GB300 library does not
+build the tensor branch yet (it refuses 9-component arrays); these pins keep the oracle
+ready for it.
 """
 
 import math
@@ -115,7 +119,6 @@ def test_tensor_branch_reduces_to_diagonal_branch(periodic):
              for k, (a, b) in st.psi_H.items()}
     ie3, im3 = sc.inv_eps, sc.inv_mu
     assert ie3.shape[0] == 3 and im3.shape[0] == 3
-    sc.sources = []  # the sources' tensor-material handling is not part of this branch's pin
     e_diag, pe_diag = O.update_E(sc, 0, E, H, psi_E, ie3)
     e_full, pe_full = O.update_E(sc, 0, E, H, psi_E, _as9(ie3))
     h_diag, ph_diag = O.update_H(sc, 0, E, H, psi_H, im3)
@@ -154,3 +157,86 @@ def test_tensor_branch_off_diagonal_coupling_is_stable():
         H, _ = O.update_H(sc, t, E, H, st.psi_H, 1.0)
         peak = max(peak, float((E**2).sum()))
     assert torch.isfinite(E).all() and peak < 100 * e0
+
+
+def test_full_tensor_dipole_keeps_coupled_components():
+    """An x-dipole in a medium whose inverse permittivity has the column (1, 2, 3) injects
+    (1, 2, 3) times the same scalar (tests/unit/objects/sources/test_dipole.py:178-193)."""
+    dx = 50e-9
+    cfg = fx.SimulationConfig(time=20 * 0.99 / math.sqrt(3) * dx / C0, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(8, 8, 8))
+    objs = [vol, fx.PointDipoleSource(name="d", grid_slice_tuple=((4, 5), (4, 5), (4, 5)), polarization=0,
+                                      wave_character=fx.WaveCharacter(wavelength=1e-6))]
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    inv = torch.zeros((9, 8, 8, 8))
+    inv[0], inv[3], inv[6] = 1.0, 2.0, 3.0
+    sc = O.OracleScene(objects, arrays.aset("inv_permittivities", inv), cfg, torch.float32)
+    E = O._source_update_E(sc, sc.sources[0], torch.zeros((3, 8, 8, 8)), sc.inv_eps, 10.0, False)
+    v = E[:, 4, 4, 4]
+    assert v[0] != 0 and torch.allclose(v[1], 2 * v[0], atol=1e-6) and torch.allclose(v[2], 3 * v[0], atol=1e-6)
+    rest = E.clone()
+    rest[:, 4, 4, 4] = 0
+    assert torch.count_nonzero(rest) == 0
+
+
+def test_tensor_sources_and_detectors_reduce_to_diagonal():
+    """Six forward steps of a scene with a tilted electric dipole and a magnetic dipole inside a
+    diagonal (eps, mu) block, a TFSF plane in vacuum, and energy / flux / phasor detectors: the
+    9-component form of the same tensors gives the diagonal form's fields and detector states
+    (the full-tensor source branches dipole.py:15-37, 219-232, tfsf.py:287-299, 384-393, the
+    tensor impedance and energy of tfsf.py:144-190 and metrics.py:34-51; float64, 1e-11)."""
+    dx = 50e-9
+    steps = 6
+    cfg = fx.SimulationConfig(time=steps * 0.99 / math.sqrt(3) * dx / C0, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(16, 12, 10))
+    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(3), vol).values())
+    blk = ((7, 12), (2, 9), (2, 8))
+    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=blk, material=fx.Material(
+        permittivity=(2.0, 3.0, 4.0), permeability=(1.5, 1.2, 1.8), electric_conductivity=(1e4, 2e4, 0.0))))
+    wc = fx.WaveCharacter(wavelength=1e-6)
+    objs += [
+        fx.PointDipoleSource(name="de", grid_slice_tuple=((9, 10), (5, 6), (4, 5)), polarization=2, azimuth_angle=35.0,
+                             elevation_angle=20.0, wave_character=wc),
+        fx.PointDipoleSource(name="dm", grid_slice_tuple=((8, 9), (4, 5), (5, 6)), polarization=1,
+                             source_type="magnetic", wave_character=wc),
+        fx.UniformPlaneSource(name="pl", grid_slice_tuple=((4, 5), (3, 9), (3, 7)), direction="+",
+                              fixed_E_polarization_vector=(0, 1, 1), wave_character=wc),
+        fx.EnergyDetector(name="en", grid_slice_tuple=blk),
+        fx.PoyntingFluxDetector(name="fl", grid_slice_tuple=((10, 11), (3, 9), (3, 7)), direction="+"),
+        fx.PhasorDetector(name="ph", grid_slice_tuple=blk, wave_characters=(wc,)),
+    ]
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    a9 = arrays.aset("inv_permittivities", _as9(arrays.inv_permittivities)).aset(
+        "inv_permeabilities", _as9(arrays.inv_permeabilities))
+    sc3 = O.OracleScene(objects, arrays, cfg, torch.float64)
+    sc9 = O.OracleScene(objects, a9, cfg, torch.float64)
+    assert sc9.inv_eps.shape[0] == 9 and sc9.inv_mu.shape[0] == 9
+    for s3, s9 in zip(sc3.sources, sc9.sources):
+        if s3.kind == "plane":
+            for a, b in ((s3.E_inc, s9.E_inc), (s3.H_inc, s9.H_inc), (s3.off_E, s9.off_E), (s3.off_H, s9.off_H)):
+                assert torch.allclose(a, b, rtol=1e-12, atol=1e-15)
+    st3 = O.run(sc3, steps)
+    st9 = O.run(sc9, steps)
+    assert st3.E.abs().max() > 0 and st3.H.abs().max() > 0
+    assert torch.allclose(st3.E, st9.E, rtol=1e-11, atol=1e-11 * st3.E.abs().max().item())
+    assert torch.allclose(st3.H, st9.H, rtol=1e-11, atol=1e-11 * st3.H.abs().max().item())
+    for name in ("en", "fl", "ph"):
+        for k, v in st3.det[name].items():
+            w = st9.det[name][k]
+            assert torch.allclose(v, w, rtol=1e-10, atol=1e-10 * v.abs().max().item()), name
+    assert st3.det["en"]["energy"].abs().max() > 0
+
+
+def test_tensor_plane_source_in_anisotropic_medium_is_refused():
+    """A plane source inside a genuinely anisotropic tensor medium is refused, as the reference's
+    time-offset computation refuses it (fdtdx/core/grid.py:781-861)."""
+    dx = 50e-9
+    cfg = fx.SimulationConfig(time=4 * 0.99 / math.sqrt(3) * dx / C0, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(8, 8, 8))
+    objs = [vol, fx.UniformPlaneSource(name="pl", grid_slice_tuple=((4, 5), (0, 8), (0, 8)), direction="+",
+                                       fixed_E_polarization_vector=(0, 1, 0))]
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    eps = torch.tensor([[3.0, 0.6, 0.2], [0.6, 2.5, 0.3], [0.2, 0.3, 2.0]], dtype=torch.float64)
+    inv9 = torch.linalg.inv(eps).reshape(9, 1, 1, 1).expand(9, 8, 8, 8).clone().float()
+    with pytest.raises(NotImplementedError):
+        O.OracleScene(objects, arrays.aset("inv_permittivities", inv9), cfg, torch.float32)
