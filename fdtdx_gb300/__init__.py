@@ -16,6 +16,7 @@ from fdtdx_gb300.config import (
 )
 from fdtdx_gb300.constants import wavelength_to_period
 from fdtdx_gb300.container import ArrayContainer, FieldState, ObjectContainer, ParameterContainer, RecordingState
+from fdtdx_gb300.dispersion import DispersionModel, DrudePole, LorentzPole
 from fdtdx_gb300.core import (
     GaussianPulseProfile,
     GaussianWindow,
@@ -56,8 +57,11 @@ __all__ = [
     "BlochBoundary",
     "BoundaryConfig",
     "Device",
+    "DispersionModel",
+    "DrudePole",
     "DtypeConversion",
     "LinearReconstructEveryK",
+    "LorentzPole",
     "EnergyDetector",
     "FieldDetector",
     "FieldState",

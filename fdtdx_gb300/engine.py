@@ -386,6 +386,8 @@ class Scene:
         d.inv_mu_scalar = 1.0 if isinstance(mu, torch.Tensor) else float(mu)
         if d.n_eps not in (1, 3) or d.n_mu not in (0, 1, 3):
             raise NotImplementedError("fully anisotropic (9-component) materials are not supported by the GB300 kernels")
+        if any(getattr(o.material, "is_dispersive", False) for o in objects.static_material_objects):
+            raise NotImplementedError("dispersive (ADE) materials are not supported by the GB300 kernels")
         d.n_sigma_E = arrays.electric_conductivity.shape[0] if arrays.electric_conductivity is not None else 0
         d.n_sigma_H = arrays.magnetic_conductivity.shape[0] if arrays.magnetic_conductivity is not None else 0
         for b in objects.boundary_objects:

@@ -106,6 +106,8 @@ class Material:
     permeability: tuple[float, ...] | float = 1.0
     electric_conductivity: tuple[float, ...] | float = 0.0
     magnetic_conductivity: tuple[float, ...] | float = 0.0
+    #: optional ``DispersionModel``; ``permittivity`` is then eps_infinity (fdtdx/materials.py:138-142)
+    dispersion: object | None = None
 
     def __post_init__(self):
         for f in ("permittivity", "permeability", "electric_conductivity", "magnetic_conductivity"):
@@ -134,6 +136,10 @@ class Material:
     @property
     def is_diagonal_permeability(self) -> bool:
         return self._diag(self.permeability)
+
+    @property
+    def is_dispersive(self) -> bool:
+        return self.dispersion is not None and self.dispersion.num_poles > 0
 
     @property
     def is_magnetic(self) -> bool:

@@ -19,6 +19,9 @@ torch autograd for per-step vector-Jacobian products), the reference files:
 * fdtdx/objects/sources/profile.py:253-345, core/window.py:16-30  temporal profiles
 * fdtdx/objects/sources/linear_polarization.py:168-468, tfsf.py:144-409, 739-806,
   fdtdx/core/grid.py:720-880                                   TFSF plane source
+* fdtdx/fdtd/update.py:316-350, dispersion.py:789-857, 988-1066, 1067-1251, 1254-1307,
+  fdtd/initialization.py:686-1000, tfsf.py:21-141, 256-261   dispersive (ADE) Lorentz / Drude
+  poles: coefficients, update, carrier-frequency sources and the H-side impedance filter
 * fdtdx/core/linalg.py:50-160, core/misc.py:363-390, 508-553   source tilt (dipole
   orientation, tilted plane polarisation, projection and bilinear sampling)
 * fdtdx/objects/detectors/{detector,phasor,field,poynting_flux,energy}.py  detectors
@@ -327,6 +330,22 @@ def linear_interpolated_indexing(points: torch.Tensor, arr: torch.Tensor) -> tor
     return num / (den + 1e-8)
 
 
+def _chi_from_coefficients(c1, c2, c3, omega: float, dt: float) -> torch.Tensor:
+    """susceptibility_from_coefficients (dispersion.py:988-1066) without the dE/dt coupling,
+    summed over the pole axis; cells whose coefficients are all zero give 0."""
+    mask = (c1 != 0) | (c3 != 0)
+    omc2 = 1.0 - c2
+    gdt = torch.where(mask, 2.0 * (1.0 + c2) / torch.where(omc2 == 0, torch.ones_like(omc2), omc2),
+                      torch.zeros_like(c2))
+    half = 1.0 + 0.5 * gdt
+    w0dt2 = torch.where(mask, 2.0 - c1 * half, torch.zeros_like(c1))
+    adt2 = torch.where(mask, c3 * half, torch.zeros_like(c3))
+    wdt = omega * dt
+    den = w0dt2 - wdt * wdt - 1j * gdt * wdt
+    chi = torch.where(mask, adt2 / torch.where(mask, den, torch.ones_like(den)), torch.zeros_like(den))
+    return chi.sum(0)
+
+
 @dataclass
 class OSource:
     obj: Any
@@ -342,6 +361,7 @@ class OSource:
     H_inc: torch.Tensor | None = None
     off_E: torch.Tensor | None = None
     off_H: torch.Tensor | None = None
+    h_filter: np.ndarray | None = None  # H-side profile at integer steps in dispersive scenes
 
 
 @dataclass
@@ -396,6 +416,7 @@ class OracleScene:
         self.periodic = tuple(self.periodic)
         # complex fields exactly when a Bloch vector is non-zero (fdtd/initialization.py:581-594)
         self.field_dtype = cdt if self.bloch else dtype
+        self.disp = self._setup_dispersion(objects)
         self.sources = [self._setup_source(s) for s in objects.sources]
         self.detectors = [self._setup_detector(d) for d in objects.detectors if not d.inverse]
         self._setup_time_filter(config)
@@ -437,6 +458,88 @@ class OracleScene:
     def records(self, t: int) -> bool:
         return self.tf_save is None or t in self.tf_save
 
+    # ---- dispersion
+    def _setup_dispersion(self, objects):
+        """Per-cell ADE coefficients (c1, c2, c3), each (poles, 1 | 3, *grid), or None without
+        dispersive materials (fdtd/initialization.py:686-700, 795-830, 955-1000): every painted
+        material, the volume first and then the material objects in placement order, writes its
+        pole stack over its slice, zero-padded to the scene's pole count (zeros for a material
+        without poles); one component when every pole is isotropic, else three.  Coefficients
+        of dispersion.py:789-857; stored in the scene dtype."""
+        painted = [objects.volume] + sorted(objects.static_material_objects, key=lambda o: o.placement_order)
+        mats = [(o, getattr(o, "material", None)) for o in painted]
+        models = [m.dispersion for _, m in mats
+                  if m is not None and getattr(m, "dispersion", None) is not None and m.dispersion.num_poles > 0]
+        if not models:
+            return None
+        n_poles = max(d.num_poles for d in models)
+        nc = 1 if all(d.is_isotropic for d in models) else 3
+        cs = [torch.zeros((n_poles, nc, *self.shape), dtype=torch.float64) for _ in range(3)]
+        for o, m in mats:
+            if m is None:
+                continue
+            poles = m.dispersion.poles if getattr(m, "dispersion", None) is not None else ()
+            block = [torch.zeros((n_poles, nc), dtype=torch.float64) for _ in range(3)]
+            for i, p in enumerate(poles):
+                if getattr(p, "orientation", None) is not None or any(getattr(p, "coupling_edot_axes", (0.0,) * 3)):
+                    raise NotImplementedError("oriented and CCPR poles")
+                w0, g, k = p.omega_0_axes, p.gamma_axes, p.coupling_sq_axes
+                for ax in range(nc):
+                    if k[ax] != 0.0 and w0[ax] * self.dt >= 2.0:
+                        raise ValueError("omega_0 * dt >= 2: the ADE recurrence is unstable")
+                    den = 1.0 + 0.5 * g[ax] * self.dt
+                    block[0][i, ax] = (2.0 - w0[ax] ** 2 * self.dt**2) / den
+                    block[1][i, ax] = -(1.0 - 0.5 * g[ax] * self.dt) / den
+                    block[2][i, ax] = k[ax] * self.dt**2 / den
+            for c, b in zip(cs, block):
+                c[(slice(None), slice(None), *o.grid_slice)] = b[:, :, None, None, None]
+        return tuple(c.to(self.dtype) for c in cs)
+
+    def _eff_inv_eps(self, inv_eps_slice, sl, omega: float):
+        """effective_inv_permittivity (dispersion.py:988-1066, 1254-1307): 1 / (eps_inf +
+        Re chi(omega)) per cell, chi from the stored coefficients by inverting the recurrence
+        (gamma dt = 2 (1 + c2) / (1 - c2), omega_0^2 dt^2 = 2 - c1 D, K dt^2 = c3 D), cells
+        without a pole unchanged."""
+        if self.disp is None:
+            return inv_eps_slice
+        c1, c2, c3 = (c[(slice(None), slice(None), *sl)].to(torch.float64) for c in self.disp)
+        chi = _chi_from_coefficients(c1, c2, c3, omega, self.dt)  # (1 | 3, *slice)
+        return (1.0 / (1.0 / inv_eps_slice.to(torch.float64) + chi.real)).to(inv_eps_slice.dtype)
+
+    def _h_filter(self, s) -> np.ndarray:
+        """_build_dispersive_H_filter (tfsf.py:21-141) with
+        compute_eps_spectrum_from_coefficients (dispersion.py:1067-1177) and
+        compute_impedance_corrected_temporal_profile (dispersion.py:1180-1251): the raw profile
+        sampled at every integer step; unless the source cells hold no pole, filtered by
+        G = sqrt(eps(omega) / eps(omega_c)) (slice-averaged eps, G = 1 at DC, real at Nyquist)
+        over a zero-padded FFT of length M = the power of two >= 2 T."""
+        T = self.T
+        raw = np.array([float(profile_amplitude(s.temporal_profile, torch.tensor(n * self.dt, dtype=torch.float64),
+                                                s.wave_character.get_period(), s.wave_character.phase_shift))
+                        for n in range(T)])
+        cs = [c[(slice(None), slice(None), *s.grid_slice)].to(torch.float64) for c in self.disp]
+        if not bool(torch.any(cs[2] != 0)):
+            return raw
+        m = 1
+        while m < 2 * T:
+            m *= 2
+        inv_inf = self.inv_eps[(slice(None), *s.grid_slice)].to(torch.float64)
+        eps_inf = (1.0 / inv_inf).mean(0)
+
+        def eps_mean(omega):
+            chi = _chi_from_coefficients(cs[0], cs[1], cs[2], omega, self.dt)  # (C, *slice)
+            return complex((eps_inf + chi.mean(0)).mean())
+
+        omegas = 2 * np.pi * np.fft.rfftfreq(m, d=self.dt)
+        spectrum_eps = np.array([eps_mean(float(w)) for w in omegas])
+        eps_c = eps_mean(2 * np.pi * s.wave_character.get_frequency())
+        padded = np.zeros(m)
+        padded[:T] = raw
+        G = np.sqrt(spectrum_eps / eps_c)
+        G[0] = 1.0
+        G[-1] = complex(G[-1].real, 0.0)
+        return np.fft.irfft(np.fft.rfft(padded) * G, n=m)[:T]
+
     # ---- sources
     def _switch_tables(self, sw):
         on = sw.calculate_on_list(self.T, self.dt)
@@ -451,6 +554,8 @@ class OracleScene:
             inv = self.inv_eps if s.source_type == "electric" else self.inv_mu
             if isinstance(inv, torch.Tensor):
                 local = inv[(slice(None), *s.grid_slice)]
+                if s.source_type == "electric":  # sampled at the carrier in dispersive media (dipole.py:168-180)
+                    local = self._eff_inv_eps(local, s.grid_slice, 2 * math.pi * s.wave_character.get_frequency())
             else:
                 local = torch.tensor(inv, dtype=self.dtype)
             # _orientation (dipole.py:130-148)
@@ -463,7 +568,8 @@ class OracleScene:
             return OSource(s, "dipole", on, idx, default_on, inv_local=local, orient=orient)
         if name in ("GaussianPlaneSource", "UniformPlaneSource"):
             E, H, oE, oH = self._plane_apply(s)
-            return OSource(s, "plane", on, idx, default_on, E_inc=E, H_inc=H, off_E=oE, off_H=oH)
+            return OSource(s, "plane", on, idx, default_on, E_inc=E, H_inc=H, off_E=oE, off_H=oH,
+                           h_filter=self._h_filter(s) if self.disp is not None else None)
         raise NotImplementedError(name)
 
     def _plane_apply(self, s):
@@ -528,7 +634,8 @@ class OracleScene:
         E = amp * e[:, None, None, None]
         H = amp * h[:, None, None, None]
         sl = (slice(None), *s.grid_slice)
-        ie = self.inv_eps[sl]
+        # impedance, energy and offsets see the medium at the carrier (linear_polarization.py:186-211)
+        ie = self._eff_inv_eps(self.inv_eps[sl], s.grid_slice, 2 * math.pi * s.wave_character.get_frequency())
         im = self.inv_mu[sl] if isinstance(self.inv_mu, torch.Tensor) else self.inv_mu
         full = _is9(ie) or _is9(im)
         if full:  # tensor media: eps = inv(inv_eps) per cell (core/physics/metrics.py:34-51, tfsf.py:144-190)
@@ -626,7 +733,11 @@ class OracleScene:
                 det[d.name] = {"poynting_flux": torch.zeros(shp, dtype=self.dtype)}
             else:
                 det[d.name] = {"energy": torch.zeros((n_on, 1) if d.reduce_volume else (n_on, *gs), dtype=self.dtype)}
-        return OState(0, z.clone(), z.clone(), psi_E, psi_H, det, [])
+        P = None
+        if self.disp is not None:
+            zp = torch.zeros((self.disp[0].shape[0], 3, *self.shape), dtype=fdt)
+            P = (zp, zp.clone())
+        return OState(0, z.clone(), z.clone(), psi_E, psi_H, det, [], P)
 
 
 class _ConfigShim:
@@ -650,6 +761,7 @@ class OState:
     psi_H: dict
     det: dict
     rec: list = field(default_factory=list)
+    P: tuple | None = None  # (P_curr, P_prev) of the dispersive poles, (poles, 3, *grid)
 
 
 # --------------------------------------------------------------------------------------------
@@ -712,6 +824,12 @@ def _source_update_E(sc: OracleScene, s: OSource, E, inv_eps, t: float, inverse:
     ies = inv_eps.detach()[(slice(None), *o.grid_slice)]
     amp = {}
     for ax in (a_ax, b_ax):
+        if s.h_filter is not None:  # linear interpolation of the filtered profile, 0 outside (tfsf.py:256-261)
+            idx = (t + s.off_H[ax]).to(torch.float64)
+            xs = np.arange(len(s.h_filter), dtype=np.float64)
+            vals = np.interp(idx.numpy().ravel(), xs, s.h_filter, left=0.0, right=0.0).reshape(tuple(idx.shape))
+            amp[ax] = torch.from_numpy(vals).to(sc.dtype) * o.static_amplitude_factor
+            continue
         time_H = (t + s.off_H[ax]) * sc.dt
         amp[ax] = profile_amplitude(o.temporal_profile, time_H, o.wave_character.get_period(),
                                     o.wave_character.phase_shift) * o.static_amplitude_factor
@@ -883,12 +1001,17 @@ def _full_tensor(inv, sigma) -> bool:
 # --------------------------------------------------------------------------------------------
 
 
-def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=True):
-    """fdtdx/fdtd/update.py:256-523 (isotropic / diagonal branch)."""
+def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=True, P=None):
+    """fdtdx/fdtd/update.py:256-523 (isotropic / diagonal branch).  With dispersive poles and
+    their polarisation ``P`` = (P_curr, P_prev) given, the ADE correction of update.py:316-350
+    is applied and (E, psi_E, P_new) returned."""
     c = sc.courant
+    E_old = E
     curl, psi_E = curl_H(sc.pad(H), psi_E, sc.pmls, simulate_boundaries)
     sig = sc.sigma_E
     if _full_tensor(inv_eps, sig):  # update.py:356-492
+        if P is not None:
+            raise NotImplementedError("dispersion with full-tensor materials")
         A, B = aniso_update_matrices(expand_to_3x3(inv_eps), expand_to_3x3(sig), c, ETA0)
         E = aniso_apply(A, B, E, curl, sc.pad, avg_aniso_E, 1.0)
         E = _apply_sources(sc, E, inv_eps, t, True, False)
@@ -897,9 +1020,18 @@ def update_E(sc: OracleScene, t: int, E, H, psi_E, inv_eps, simulate_boundaries=
     if sig is not None:
         factor = 1 - c * sig * ETA0 * inv_eps / 2
     E = factor * E + c * curl * inv_eps
+    if P is not None:
+        # P_hat = c1 P^n + c2 P^{n-1} + c3 E^n;  E += inv_eps sum_poles (P^n - P_hat)
+        c1, c2, c3 = sc.disp
+        P_curr, P_prev = P
+        P_hat = c1 * P_curr + c2 * P_prev + c3 * E_old
+        E = E + inv_eps * (P_curr - P_hat).sum(0)
+        P = (P_hat, P_curr)
     if sig is not None:
         E = E / (1 + c * sig * ETA0 * inv_eps / 2)
     E = _apply_sources(sc, E, inv_eps, t, True, False)
+    if P is not None:
+        return _walls(sc, E, sc.pec), psi_E, P
     return _walls(sc, E, sc.pec), psi_E
 
 
@@ -1068,17 +1200,23 @@ def forward(sc: OracleScene, st: OState, inv_eps=None, inv_mu=None, record_detec
     inv_mu = sc.inv_mu if inv_mu is None else inv_mu
     t = st.t
     H_prev = st.H
-    E, psi_E = update_E(sc, t, st.E, st.H, st.psi_E, inv_eps, simulate_boundaries)
+    P = st.P
+    if sc.disp is not None:
+        E, psi_E, P = update_E(sc, t, st.E, st.H, st.psi_E, inv_eps, simulate_boundaries, P=st.P)
+    else:
+        E, psi_E = update_E(sc, t, st.E, st.H, st.psi_E, inv_eps, simulate_boundaries)
     H, psi_H = update_H(sc, t, E, st.H, st.psi_H, inv_mu, simulate_boundaries)
     rec = st.rec
     if record_boundaries and sc.records(t):
         rec = rec + [collect_interfaces(sc, E, H)]
     det = update_detectors(sc, t, E, H, H_prev, st.det, inv_eps, inv_mu) if record_detectors else st.det
-    return OState(t + 1, E, H, psi_E, psi_H, det, rec)
+    return OState(t + 1, E, H, psi_E, psi_H, det, rec, P)
 
 
 def backward(sc: OracleScene, st: OState) -> OState:
     """One reverse step with reset_fields=False and no detectors (fdtdx/fdtd/backward.py:62-135)."""
+    if sc.disp is not None:  # fdtd/initialization.py:674-685: the ADE recurrence is not reversed
+        raise NotImplementedError("dispersive materials have no time-reversed step")
     t = st.t - 1
     E, H = st.E, st.H
     if st.rec:
