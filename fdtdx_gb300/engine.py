@@ -299,7 +299,9 @@ def detector_tables(det, config: SimulationConfig) -> tuple[np.ndarray, np.ndarr
             window = det.apodization.get_window(np.arange(T) * dt) * on_arr
         wsum = float(window.sum())
         if not math.isfinite(wsum) or wsum <= 0.0:
-            raise Exception(f"Detector '{det.name}': the apodization window sums to {wsum} over the recorded time steps")
+            raise Exception(f"Detector '{det.name}': the apodization window sums to {wsum} over the recorded "
+                            "time steps; it must be finite and positive. Check that the window's support overlaps "
+                            "the detector's active interval.")
         if det.scaling_mode == "continuous":
             scale = 2.0 / wsum
         elif det.scaling_mode == "pulse":

@@ -618,6 +618,11 @@ class PhasorDetector(Detector):
     dft_subsample: int | Literal["auto"] = 1
     apodization: TemporalWindow | None = None
 
+    def __post_init__(self):
+        if self.apodization is not None and not isinstance(self.apodization, TemporalWindow):
+            raise Exception(f"apodization must be a TemporalWindow, got {type(self.apodization).__name__}. "
+                            "Source temporal profiles are not valid windows.")
+
     @property
     def recorded_components(self) -> tuple[str, ...]:
         return tuple(c for c in COMPONENTS if c in self.components)
@@ -673,6 +678,7 @@ class PhasorPoyntingFluxDetector(PhasorDetector):
     keep_all_components: bool = False
 
     def __post_init__(self):
+        super().__post_init__()
         self.components = COMPONENTS
         self.reduce_volume = False
 
