@@ -47,6 +47,21 @@ def _dist():
     return ws, rank, local
 
 
+def _max_over_ranks(ms: float, dev) -> float:
+    """The slowest rank's timed-region length: the job's steps are done when the last rank's are."""
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _job_rate(ncell: int, steps: int, ws: int, ms: float) -> float:
+    """Whole-job cell-updates/s: every rank advances its own replica of ``ncell`` cells by
+    ``steps`` steps within the slowest rank's ``ms``."""
+    return ncell * steps * ws / (ms / 1e3)
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -184,11 +199,9 @@ def run_gpu(args):
     scene.status()
     ms = ev0.elapsed_time(ev1)
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = _max_over_ranks(ms, dev)
         dist.barrier()
-    value = ncell * K * ws / (ms / 1e3)
+    value = _job_rate(ncell, K, ws, ms)
 
     # per-kernel device times (CUDA events around each launch group, same stream, same workload)
     prof = (C.c_float * 8)()
