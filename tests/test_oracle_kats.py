@@ -222,3 +222,40 @@ def test_phasor_semantics():
     assert torch.allclose(p0.abs(), 2 * p1.abs())
     w = 2 * math.pi * 299792458.0 / 1.55e-6 * sc.dt
     assert torch.allclose(p2, p1 * (1 + complex(math.cos(w), math.sin(w))))
+
+
+def test_flux_and_energy_reduce_to_physical_integrals():
+    """Uniform Ex = 1, Hy = 1 in a periodic box: a reduced flux plane of 2 x 2 cells is the
+    surface integral 4 dx^2 ('-' flips it; all components give (0, 0, 4 dx^2)); Ex = 1 alone
+    gives 0.5 |E|^2 = 0.5 per cell and the volume integral 4 x 0.5 dx^3 over the 4 cells, and
+    eps_r = 2 doubles it (tests/unit/objects/detectors/test_poynting_flux.py:306-326,
+    test_energy.py:243-262)."""
+    dx = 2e-7
+    cfg = fx.SimulationConfig(time=3 * 0.99 / math.sqrt(3) * dx / 299792458.0, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(4, 4, 4))
+    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(1, "periodic"),
+                                                        vol).values())
+    plane = ((1, 3), (1, 3), (2, 3))
+    objs += [fx.PoyntingFluxDetector(name="fp", grid_slice_tuple=plane, direction="+"),
+             fx.PoyntingFluxDetector(name="fm", grid_slice_tuple=plane, direction="-"),
+             fx.PoyntingFluxDetector(name="fa", grid_slice_tuple=plane, direction="+", keep_all_components=True),
+             fx.EnergyDetector(name="en", grid_slice_tuple=plane, reduce_volume=True),
+             fx.EnergyDetector(name="ec", grid_slice_tuple=plane)]
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    sc = O.OracleScene(objects, arrays, cfg, torch.float64)
+    st = sc.init_state()
+    E = torch.zeros(3, 4, 4, 4, dtype=torch.float64)
+    H = torch.zeros_like(E)
+    E[0], H[1] = 1.0, 1.0
+    det = O.update_detectors(sc, 0, E, H, H, st.det, sc.inv_eps, sc.inv_mu)
+    assert math.isclose(float(det["fp"]["poynting_flux"][0, 0]), 4 * dx**2, rel_tol=1e-12)
+    assert math.isclose(float(det["fm"]["poynting_flux"][0, 0]), -4 * dx**2, rel_tol=1e-12)
+    assert torch.allclose(det["fa"]["poynting_flux"][0], torch.tensor([0.0, 0.0, 4 * dx**2], dtype=torch.float64))
+    Eonly = O.update_detectors(sc, 0, E, torch.zeros_like(E), torch.zeros_like(E), st.det, sc.inv_eps, sc.inv_mu)
+    assert math.isclose(float(Eonly["en"]["energy"][0, 0]), 4 * 0.5 * dx**3, rel_tol=1e-12)
+    assert torch.allclose(Eonly["ec"]["energy"][0], torch.full((2, 2, 1), 0.5, dtype=torch.float64))
+    sc2 = O.OracleScene(objects, arrays.aset("inv_permittivities", torch.full((1, 4, 4, 4), 0.5)), cfg,
+                        torch.float64)
+    E2 = O.update_detectors(sc2, 0, E, torch.zeros_like(E), torch.zeros_like(E), sc2.init_state().det, sc2.inv_eps,
+                            sc2.inv_mu)
+    assert math.isclose(float(E2["en"]["energy"][0, 0]), 4 * 1.0 * dx**3, rel_tol=1e-12)
