@@ -162,7 +162,7 @@ def reversible_fdtd(
     objects: ObjectContainer,
     config: SimulationConfig,
     key=None,
-    show_progress: bool = False,
+    show_progress: bool = True,
     progress_callback: Callable[[int, int], None] | None = None,
 ) -> SimulationState:
     """Differentiable forward run with the time-reversal gradient (fdtd.py:39-418).

@@ -67,7 +67,7 @@ def checkpointed_fdtd(
     config: SimulationConfig,
     key=None,
     stopping_condition=None,
-    show_progress: bool = False,
+    show_progress: bool = True,
     progress_callback: Callable[[int, int], None] | None = None,
 ) -> SimulationState:
     """Forward run of ``config.time_steps_total`` steps from a reset state (fdtd.py:421-496)."""
@@ -92,7 +92,7 @@ def run_fdtd(
     config: SimulationConfig,
     key=None,
     stopping_condition=None,
-    show_progress: bool = False,
+    show_progress: bool = True,
     progress_callback: Callable[[int, int], None] | None = None,
 ) -> SimulationState:
     """Run the simulation; dispatches like fdtdx/fdtd/wrapper.py:14-63."""
