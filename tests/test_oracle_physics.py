@@ -26,7 +26,9 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
 * point-dipole radiation: outward flux through six planes, x / y symmetry and a weaker axial
   flux for a z-dipole, the minimum along x for an x-dipole, and a 45-degree tilted dipole's
   x = z, y > x pattern at equal total power
-  (tests/simulation/physics/sources/test_dipole_radiation.py:138-312, 10%, 40^3 box).
+  (tests/simulation/physics/sources/test_dipole_radiation.py:138-312, 10%, 40^3 box);
+* the paraxial width of a Gaussian plane source's beam four cells downstream
+  (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%).
 
 The plane-wave checks use the reference's quasi-1D domains: 3 x 3 periodic cells across,
 CPML along z, a +z uniform plane source with Ex polarisation (the default CW profile unless
@@ -343,3 +345,30 @@ def test_dipole_radiation_pattern():
     sx, sy, sz = (abs(ft[f"{a}+"]) + abs(ft[f"{a}-"]) for a in "xyz")
     assert abs(sx - sz) / sx < 0.1 and sy > sx
     assert abs(sum(ft.values()) - total) / total < 0.1
+
+
+def test_gaussian_plane_source_beam_width():
+    """A Gaussian plane source of radius 1.5 um (sigma_0 = radius / 3 = 500 nm) in a 100 x 100
+    CPML box: four cells downstream, the RMS width of |Ex|^2 across the beam is the paraxial
+    sigma(z) / sqrt(2) with sigma(z)^2 = sigma_0^2 + (lambda z / (2 pi sigma_0))^2, within 10%
+    (tests/simulation/physics/sources/test_gaussian_source.py:148-219; a 40-cell z extent and
+    60 fs instead of 80 cells and 120 fs; the oracle gives 3.6%)."""
+    dx, n = 50e-9, 100
+    cfg = fx.SimulationConfig(time=60e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(n, n, 40))
+    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(10), vol).values())
+    wc = fx.WaveCharacter(wavelength=WL)
+    objs.append(fx.GaussianPlaneSource(name="g", grid_slice_tuple=((0, n), (0, n), (12, 13)), direction="+",
+                                       fixed_E_polarization_vector=(1, 0, 0), radius=1.5e-6, wave_character=wc))
+    objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((0, n), (0, n), (16, 17)), wave_characters=(wc,),
+                                  components=("Ex",)))
+    _, st = _run(cfg, objs)
+    ex = st.det["ph"]["phasor"].reshape(n, n).abs().double().numpy()
+    c = n // 2
+    prof = ex[:, c]
+    assert prof[c] > 0
+    x = (np.arange(n) - c) * dx
+    rms = math.sqrt(float((x**2 * prof**2).sum() / (prof**2).sum()))
+    s0 = 1.5e-6 / 3
+    sigma = math.sqrt(s0**2 + (WL * 4 * dx / (2 * math.pi * s0)) ** 2)
+    assert abs(rms - sigma / math.sqrt(2)) / (sigma / math.sqrt(2)) < 0.10, (rms, sigma / math.sqrt(2))
