@@ -28,7 +28,9 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   x = z, y > x pattern at equal total power
   (tests/simulation/physics/sources/test_dipole_radiation.py:138-312, 10%, 40^3 box);
 * the paraxial width of a Gaussian plane source's beam four cells downstream
-  (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%).
+  (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%);
+* mixed boundaries (PEC on x, PMC on y, both) with CPML along z keep free-space k and
+  impedance (tests/simulation/physics/boundaries/test_mixed_boundaries.py, 5%).
 
 The plane-wave checks use the reference's quasi-1D domains: 3 x 3 periodic cells across,
 CPML along z, a +z uniform plane source with Ex polarisation (the default CW profile unless
@@ -372,3 +374,36 @@ def test_gaussian_plane_source_beam_width():
     s0 = 1.5e-6 / 3
     sigma = math.sqrt(s0**2 + (WL * 4 * dx / (2 * math.pi * s0)) ** 2)
     assert abs(rms - sigma / math.sqrt(2)) / (sigma / math.sqrt(2)) < 0.10, (rms, sigma / math.sqrt(2))
+
+
+@pytest.mark.parametrize("walls", ["pec_x", "pmc_y", "pec_x_pmc_y"])
+def test_mixed_boundaries_keep_free_space_propagation(walls):
+    """PEC walls on x, PMC walls on y, or both, with CPML along z: an x-polarised plane wave
+    (Ex, Hy, neither constrained by those walls) keeps k = k0 between two planes 5 cells apart
+    and, with PMC walls, the impedance |Ex| / |Hy| = 1 (tests/simulation/physics/boundaries/
+    test_mixed_boundaries.py:194-268, 384-430, 5%)."""
+    dx, nz, wide, narrow = 50e-9, 80, 40, 3
+    nx = wide if "pec" in walls else narrow
+    ny = wide if "pmc" in walls else narrow
+    types = {"min_x": "pec" if "pec" in walls else "periodic", "max_x": "pec" if "pec" in walls else "periodic",
+             "min_y": "pmc" if "pmc" in walls else "periodic", "max_y": "pmc" if "pmc" in walls else "periodic"}
+    cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(nx, ny, nz))
+    objs = [vol] + list(fx.boundary_objects_from_config(
+        fx.BoundaryConfig.from_uniform_bound(10, override_types=types), vol).values())
+    wc = fx.WaveCharacter(wavelength=WL)
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, nx), (0, ny), (12, 13)), direction="+",
+                                      fixed_E_polarization_vector=(1, 0, 0), wave_character=wc))
+    for name, z in (("d1", 17), ("d2", 22)):
+        objs.append(fx.PhasorDetector(name=name, grid_slice_tuple=((0, nx), (0, ny), (z, z + 1)), wave_characters=(wc,),
+                                      reduce_volume=True))
+    _, st = _run(cfg, objs)
+    p1 = st.det["d1"]["phasor"].reshape(-1)
+    p2 = st.det["d2"]["phasor"].reshape(-1)
+    ex1, hy1, ex2 = complex(p1[0]), complex(p1[4]), complex(p2[0])
+    assert abs(ex1) > 0 and abs(ex2) > 0
+    k = ((np.angle(ex2) - np.angle(ex1)) % (2 * math.pi)) / (5 * dx)
+    k0 = 2 * math.pi / WL
+    assert abs(k - k0) / k0 < TOL, (k, k0)
+    if "pmc" in walls:
+        assert abs(hy1) > 0 and abs(abs(ex1) / abs(hy1) - 1.0) < TOL
