@@ -30,7 +30,8 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
 * the paraxial width of a Gaussian plane source's beam four cells downstream
   (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%);
 * mixed boundaries (PEC on x, PMC on y, both) with CPML along z keep free-space k and
-  impedance (tests/simulation/physics/boundaries/test_mixed_boundaries.py, 5%).
+  impedance (tests/simulation/physics/boundaries/test_mixed_boundaries.py, 5%);
+* a TFSF plane injects one way: flux behind it below 1e-3 of the flux ahead.
 
 The plane-wave checks use the reference's quasi-1D domains: 3 x 3 periodic cells across,
 CPML along z, a +z uniform plane source with Ex polarisation (the default CW profile unless
@@ -407,3 +408,36 @@ def test_mixed_boundaries_keep_free_space_propagation(walls):
     assert abs(k - k0) / k0 < TOL, (k, k0)
     if "pmc" in walls:
         assert abs(hy1) > 0 and abs(abs(ex1) / abs(hy1) - 1.0) < TOL
+
+
+@pytest.mark.parametrize("direction,eps", [("+", 1.0), ("-", 1.0), ("+", 2.25)])
+def test_tfsf_plane_injects_one_way(direction, eps):
+    """A TFSF plane inside a uniform medium sends its wave one way only: the time-averaged flux
+    behind it is below 1e-3 of the flux ahead, in vacuum and in eps_r = 2.25, for both
+    directions (the property tests/simulation/physics/test_dispersion.py:329-360 checks in a
+    dispersive medium, here in non-dispersive ones; the oracle gives 1.4e-9 to 2.3e-8)."""
+    dx, nz = 25e-9, 200
+    cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(3, 3, nz))
+    bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                           boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                           thickness_grid_minz=10, thickness_grid_maxz=10)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    if eps != 1.0:
+        objs.append(fx.UniformMaterialObject(name="fill", grid_slice_tuple=((0, 3), (0, 3), (0, nz)),
+                                             material=fx.Material(permittivity=eps)))
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 3), (0, 3), (100, 101)), direction=direction,
+                                      fixed_E_polarization_vector=(1, 0, 0), wave_character=fx.WaveCharacter(wavelength=WL)))
+    for name, z in (("lo", 50), ("hi", 150)):
+        objs.append(fx.PoyntingFluxDetector(name=name, grid_slice_tuple=((0, 3), (0, 3), (z, z + 1)), direction="+",
+                                            reduce_volume=True))
+    sc, st = _run(cfg, objs)
+    spp = round(WL / (C0 * sc.dt))
+    lo, hi = _mean_flux_named(st, "lo", spp), _mean_flux_named(st, "hi", spp)
+    ahead, behind = (hi, lo) if direction == "+" else (-lo, hi)
+    assert ahead > 0 and abs(behind) < 1e-3 * ahead, (ahead, behind)
+
+
+def _mean_flux_named(st, name: str, steps_per_period: int) -> float:
+    f = st.det[name]["poynting_flux"][:, 0].double().numpy()
+    return float(f[-10 * steps_per_period:].mean())
