@@ -24,9 +24,10 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
 * birefringence in eps = diag(2.25, 4, 1): k and impedance 1/n of the ordinary (x) and
   extraordinary (y) polarisations (tests/simulation/physics/test_birefringence.py, 5%);
 * point-dipole radiation: outward flux through six planes, x / y symmetry and a weaker axial
-  flux for a z-dipole, the minimum along x for an x-dipole, and a 45-degree tilted dipole's
-  x = z, y > x pattern at equal total power
-  (tests/simulation/physics/sources/test_dipole_radiation.py:138-312, 10%, 40^3 box);
+  flux for a z-dipole, the minimum along x for an x-dipole, a 45-degree tilted dipole's
+  x = z, y > x pattern at equal total power, and the magnetic dipole's dual pattern
+  (tests/simulation/physics/sources/test_dipole_radiation.py:138-312,
+  test_dipole_magnetic.py:131-190, 10%, 40^3 box);
 * the paraxial width of a Gaussian plane source's beam four cells downstream
   (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%);
 * mixed boundaries (PEC on x, PMC on y, both) with CPML along z keep free-space k and
@@ -307,7 +308,7 @@ def test_birefringence_wavenumber_and_impedance(pol):
     assert abs(z - 1 / n) / (1 / n) < TOL, (z, 1 / n)
 
 
-def _dipole_fluxes(pol: int, azimuth: float = 0.0) -> dict:
+def _dipole_fluxes(pol: int, azimuth: float = 0.0, source_type: str = "electric") -> dict:
     """Time-averaged flux through six full-width planes 8 cells from a CW point dipole at the
     centre of a 40^3 CPML box (50 nm cells)."""
     n, off = 40, 8
@@ -316,7 +317,8 @@ def _dipole_fluxes(pol: int, azimuth: float = 0.0) -> dict:
     objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(8), vol).values())
     c = n // 2
     objs.append(fx.PointDipoleSource(name="dip", grid_slice_tuple=((c, c + 1),) * 3, polarization=pol,
-                                     azimuth_angle=azimuth, wave_character=fx.WaveCharacter(wavelength=WL)))
+                                     azimuth_angle=azimuth, source_type=source_type,
+                                     wave_character=fx.WaveCharacter(wavelength=WL)))
     for ax in range(3):
         for side in "+-":
             st = [(0, n)] * 3
@@ -348,6 +350,14 @@ def test_dipole_radiation_pattern():
     sx, sy, sz = (abs(ft[f"{a}+"]) + abs(ft[f"{a}-"]) for a in "xyz")
     assert abs(sx - sz) / sx < 0.1 and sy > sx
     assert abs(sum(ft.values()) - total) / total < 0.1
+    # a magnetic z-dipole: the same pattern (E <-> H duality) and power within a factor of 10
+    # (tests/simulation/physics/sources/test_dipole_magnetic.py:131-190)
+    fm = _dipole_fluxes(2, source_type="magnetic")
+    assert all(v > 0 for v in fm.values())
+    assert abs(fm["x+"] - fm["x-"]) / fm["x+"] < 0.1 and abs(fm["x+"] - fm["y+"]) / fm["x+"] < 0.1
+    assert fm["z+"] < fm["x+"]
+    ratio = max(total, sum(fm.values())) / min(total, sum(fm.values()))
+    assert ratio < 10
 
 
 def test_gaussian_plane_source_beam_width():
