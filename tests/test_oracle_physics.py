@@ -25,9 +25,10 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   extraordinary (y) polarisations (tests/simulation/physics/test_birefringence.py, 5%);
 * point-dipole radiation: outward flux through six planes, x / y symmetry and a weaker axial
   flux for a z-dipole, the minimum along x for an x-dipole, a 45-degree tilted dipole's
-  x = z, y > x pattern at equal total power, and the magnetic dipole's dual pattern
+  x = z, y > x pattern at equal total power, the magnetic dipole's dual pattern, and n times
+  the vacuum power in a uniform dielectric
   (tests/simulation/physics/sources/test_dipole_radiation.py:138-312,
-  test_dipole_magnetic.py:131-190, 10%, 40^3 box);
+  test_dipole_magnetic.py:131-190, test_dipole_green_function.py:175-208, 40^3 box);
 * the paraxial width of a Gaussian plane source's beam four cells downstream
   (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%);
 * mixed boundaries (PEC on x, PMC on y, both) with CPML along z keep free-space k and
@@ -308,7 +309,7 @@ def test_birefringence_wavenumber_and_impedance(pol):
     assert abs(z - 1 / n) / (1 / n) < TOL, (z, 1 / n)
 
 
-def _dipole_fluxes(pol: int, azimuth: float = 0.0, source_type: str = "electric") -> dict:
+def _dipole_fluxes(pol: int, azimuth: float = 0.0, source_type: str = "electric", eps: float = 1.0) -> dict:
     """Time-averaged flux through six full-width planes 8 cells from a CW point dipole at the
     centre of a 40^3 CPML box (50 nm cells)."""
     n, off = 40, 8
@@ -316,6 +317,9 @@ def _dipole_fluxes(pol: int, azimuth: float = 0.0, source_type: str = "electric"
     vol = fx.SimulationVolume(shape=(n, n, n))
     objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(8), vol).values())
     c = n // 2
+    if eps != 1.0:
+        objs.append(fx.UniformMaterialObject(name="fill", grid_slice_tuple=((0, n),) * 3,
+                                             material=fx.Material(permittivity=eps)))
     objs.append(fx.PointDipoleSource(name="dip", grid_slice_tuple=((c, c + 1),) * 3, polarization=pol,
                                      azimuth_angle=azimuth, source_type=source_type,
                                      wave_character=fx.WaveCharacter(wavelength=WL)))
@@ -358,6 +362,11 @@ def test_dipole_radiation_pattern():
     assert fm["z+"] < fm["x+"]
     ratio = max(total, sum(fm.values())) / min(total, sum(fm.values()))
     assert ratio < 10
+    # in a uniform eps_r = 2.25 the same dipole radiates n = 1.5 times the vacuum power
+    # (tests/simulation/physics/sources/test_dipole_green_function.py:175-208, 5%; the oracle
+    # gives 1.507)
+    fd = _dipole_fluxes(2, eps=2.25)
+    assert abs(sum(fd.values()) / total - 1.5) / 1.5 < 0.05, sum(fd.values()) / total
 
 
 def test_gaussian_plane_source_beam_width():
