@@ -139,38 +139,6 @@ def test_plane_sources_and_all_detectors():
     assert rel_l2(g, r) <= TOL
 
 
-def test_tilted_sources():
-    """A tilted Gaussian plane source (per-cell Yee time offsets across the plane) and tilted
-    electric and magnetic point dipoles (one source record per injected component) in a
-    diagonally anisotropic, magnetic block, against the oracle."""
-    cfg = _cfg(120, dx=25e-9)
-    vol = fx.SimulationVolume(shape=(36, 32, 30))
-    objs = [vol] + list(fx.boundary_objects_from_config(fx.BoundaryConfig.from_uniform_bound(6), vol).values())
-    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((14, 26), (10, 22), (12, 20)),
-                                         material=fx.Material(permittivity=(2.0, 3.0, 2.5), permeability=(1.2, 1.0, 1.4))))
-    wc = fx.WaveCharacter(wavelength=1.0e-6)
-    objs.append(fx.GaussianPlaneSource(name="g", grid_slice_tuple=((7, 29), (7, 25), (9, 10)), direction="+",
-                                       radius=7 * 25e-9, fixed_E_polarization_vector=(1, 0, 0), azimuth_angle=25.0,
-                                       elevation_angle=-10.0, wave_character=wc))
-    objs.append(fx.PointDipoleSource(name="de", grid_slice_tuple=((18, 19), (15, 16), (16, 17)), polarization=2,
-                                     azimuth_angle=35.0, elevation_angle=20.0, wave_character=wc,
-                                     temporal_profile=scenes.pulse_5fs()))
-    objs.append(fx.PointDipoleSource(name="dm", grid_slice_tuple=((22, 23), (12, 13), (14, 15)), polarization=0,
-                                     azimuth_angle=-30.0, elevation_angle=15.0, source_type="magnetic",
-                                     amplitude=0.7, wave_character=wc))
-    R = ((10, 26), (9, 23), (11, 22))
-    objs += [
-        fx.PhasorDetector(name="ph", grid_slice_tuple=R, wave_characters=(wc,)),
-        fx.PoyntingFluxDetector(name="flux", grid_slice_tuple=((8, 28), (8, 24), (22, 23)), direction="+"),
-    ]
-    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
-    _, out = fx.run_fdtd(arrays, objects, cfg)
-    torch.cuda.synchronize()
-    _, r32 = oracle_run(objects, arrays, cfg, torch.float32)
-    _, r64 = oracle_run(objects, arrays, cfg, torch.float64)
-    compare_states("tilted_sources", out, r32, r64, TOL)
-
-
 def test_graph_and_direct_paths_agree():
     objects, arrays, _, cfg, _ = scenes.coupler(shape=(60, 60, 40), steps=100, scale=0.2, pml=6)
     a = arrays.reset()
