@@ -6,8 +6,9 @@ scene written for fdtdx reads the same here:
 * ``SimulationVolume``, ``UniformMaterialObject``   fdtdx/objects/static_material/static.py
 * ``PerfectlyMatchedLayer``                         fdtdx/objects/boundaries/perfectly_matched_layer.py:12-275
 * ``PerfectElectricConductor`` / ``PerfectMagneticConductor``  fdtdx/objects/boundaries/pec.py, pmc.py
-* ``PeriodicBoundary`` (a Bloch boundary with k = 0) fdtdx/objects/boundaries/bloch.py
-* ``PointDipoleSource``                             fdtdx/objects/sources/dipole.py:51-277
+* ``PeriodicBoundary``, ``BlochBoundary``           fdtdx/objects/boundaries/bloch.py (the kernels run
+  a zero Bloch vector, i.e. a periodic boundary; a non-zero one needs complex fields)
+* ``PointDipoleSource`` (axis-aligned or tilted)    fdtdx/objects/sources/dipole.py:51-277
 * ``GaussianPlaneSource`` / ``UniformPlaneSource``  fdtdx/objects/sources/linear_polarization.py:414-482
 * ``FieldDetector``, ``PhasorDetector``, ``PoyntingFluxDetector``,
   ``PhasorPoyntingFluxDetector``, ``EnergyDetector``  fdtdx/objects/detectors/*.py
