@@ -12,6 +12,8 @@
   (linear_polarization.py:168-330), on every propagation axis and direction, Gaussian and
   uniform, isotropic and diagonal media; the tilted formula reduces to the untilted tables at
   zero angles, and a tilted uniform source keeps a constant profile;
+* in vacuum the tables are energy-normalised with equal E and H norms, tilted or not, and
+  the raw Gaussian profile sums to 1 around its central peak;
 * physics: a 30-degree TE plane wave, in a periodic cell two wavelengths of the transverse
   period wide (k_x L = 2 pi, so plain wrap halos carry it exactly), crosses a vacuum /
   eps_r = 4 interface with the Fresnel power transmission T = 0.854 (5%), and its phasor phase
@@ -228,3 +230,29 @@ def test_oblique_fresnel_te_and_transverse_phase():
     tt = math.asin(math.sin(th) / 2.0)
     t_ref = (2.0 * math.cos(tt)) / math.cos(th) * (2.0 * math.cos(th) / (math.cos(th) + 2.0 * math.cos(tt))) ** 2
     assert abs(s1 / s0 - t_ref) / t_ref < 0.05, (s1 / s0, t_ref)
+
+
+@pytest.mark.parametrize("n", [0, 1, 2])
+@pytest.mark.parametrize("az,el", [(0.0, 0.0), (30.0, -15.0)])
+def test_plane_tables_in_vacuum_are_energy_normalised(n, az, el):
+    """In vacuum the incident H table has the E table's norm (impedance 1) and, with
+    ``normalize_by_energy``, sum 0.5 (|E|^2 + |H|^2) over the plane is 1; the raw Gaussian
+    profile sums to 1 and peaks at the centre (tests/unit/objects/sources/
+    test_linear_polarization.py:102-164, 215-238)."""
+    dx = 25e-9
+    cfg = fx.SimulationConfig(time=10 * 0.99 / math.sqrt(3) * dx / C0, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(24, 22, 20))
+    st = [(2, 22), (3, 20), (2, 18)]
+    st[n] = (9, 10)
+    src = fx.GaussianPlaneSource(name="g", grid_slice_tuple=tuple(st), direction="+", radius=0.15e-6,
+                                 fixed_E_polarization_vector=tuple(1 if a == (n + 1) % 3 else 0 for a in range(3)),
+                                 azimuth_angle=az, elevation_angle=el, wave_character=fx.WaveCharacter(wavelength=1e-6))
+    objects, arrays, _, cfg, _ = fx.place_objects([vol, src], cfg, device="cpu")
+    src = objects.sources[0]
+    raw = src.amplitude_raw_hv(dx)
+    W, H = raw.shape
+    assert math.isclose(float(raw.sum()), 1.0, rel_tol=1e-12) and raw[W // 2, H // 2] == raw.max() > raw[0, 0]
+    E, Hh, _, _ = engine.plane_source_profiles(src, arrays, cfg)
+    E, Hh = E.astype(np.float64), Hh.astype(np.float64)
+    assert math.isclose(np.linalg.norm(E), np.linalg.norm(Hh), rel_tol=1e-6)
+    assert math.isclose(float(0.5 * ((E**2).sum() + (Hh**2).sum())), 1.0, rel_tol=1e-6)
