@@ -38,7 +38,12 @@ so the reference itself cannot be run.  The reference's tests hold no stored fie
 or detector values; what they hold are known-answer tests and invariants (curl of
 a linear field, CPML scatter signs, update formulas, forward/backward round trips,
 PML profile values, phasor semantics), and those are replayed against this oracle
-in tests/test_oracle_kats.py.  Beyond those, field-level parity is unpinned.
+in tests/test_oracle_kats.py, together with the reference's simulation-tier physics
+checks (analytic wavenumbers, impedances, Fresnel coefficients, skin depth, radiation
+patterns, dispersion, Bloch oblique incidence) in tests/test_oracle_physics.py,
+test_tilted_sources.py, test_oracle_bloch.py, test_oracle_dispersion.py and
+test_oracle_aniso.py, and its gradient checks in tests/test_oracle_gradient.py.  Beyond
+those, field-level parity is unpinned.
 
 Objects are read through their fdtdx attribute names (duck typing), so a scene
 built with ``fdtdx_gb300`` objects drives this oracle without using any of that
