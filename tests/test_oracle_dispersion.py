@@ -19,6 +19,8 @@ carrier frequency (dipole.py:150-193, linear_polarization.py:186-211, tfsf.py:21
   fraction 1 - R within 10% (7.0% at 25 nm cells against a 16 nm power decay length);
 * a plane source inside a uniform Lorentz medium injects the medium's impedance at the
   carrier: backward / forward flux < 2% (test_dispersion.py:329-360; the oracle gives 7e-7);
+* the broadband H-side filter leaks less of a Gaussian pulse's energy backwards than the
+  carrier-only impedance (ratio below 0.85, test_dispersive_source.py:192-225);
 * the library refuses a dispersive scene before any device work, and the oracle has no
   reversed step for one (fdtd/initialization.py:674-685).
 """
@@ -172,3 +174,42 @@ def test_library_refuses_dispersion_and_oracle_has_no_reverse():
     st = O.run(sc, 2)
     with pytest.raises(NotImplementedError):
         O.backward(sc, st)
+
+
+def test_broadband_filter_reduces_backward_leakage():
+    """A Gaussian pulse (15% bandwidth) from a plane source inside a strongly dispersive Lorentz
+    medium: the H-side profile filtered by sqrt(eps(omega) / eps(omega_c)) leaks less
+    pulse energy backwards (time-integrated |flux| behind / ahead) than the carrier-only
+    impedance, by the reference's margin (ratio < 0.85;
+    tests/simulation/physics/test_dispersive_source.py:192-225)."""
+    nz = 200
+    pulse = fx.GaussianPulseProfile(spectral_width=fx.WaveCharacter(frequency=0.15 * C0 / WL),
+                                    center_wave=fx.WaveCharacter(wavelength=WL))
+    model = fx.DispersionModel(poles=(fx.LorentzPole(resonance_frequency=1.4 * OMEGA, damping=5e12,
+                                                     delta_epsilon=1.5),))
+    cfg = fx.SimulationConfig(time=180e-15, grid=fx.UniformGrid(25e-9))
+    vol = fx.SimulationVolume(shape=(3, 3, nz))
+    bc = fx.BoundaryConfig.from_uniform_bound(10, override_types={"min_x": "periodic", "max_x": "periodic",
+                                                                  "min_y": "periodic", "max_y": "periodic"})
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    objs.append(fx.UniformMaterialObject(name="m", grid_slice_tuple=((0, 3), (0, 3), (0, nz)),
+                                         material=fx.Material(permittivity=1.0, dispersion=model)))
+    objs.append(fx.UniformPlaneSource(name="s", grid_slice_tuple=((0, 3), (0, 3), (60, 61)), direction="+",
+                                      fixed_E_polarization_vector=(1, 0, 0), temporal_profile=pulse,
+                                      wave_character=fx.WaveCharacter(wavelength=WL)))
+    for name, z in (("fwd", 90), ("bwd", 30)):
+        objs.append(fx.PoyntingFluxDetector(name=name, grid_slice_tuple=((0, 3), (0, 3), (z, z + 1)), direction="+",
+                                            reduce_volume=True))
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    leak = []
+    for filtered in (True, False):
+        sc = O.OracleScene(objects, arrays, cfg, torch.float32)
+        assert sc.sources[0].h_filter is not None
+        if not filtered:
+            sc.sources[0].h_filter = None  # the carrier-only impedance path
+        st = O.run(sc)
+        fwd = float(st.det["fwd"]["poynting_flux"][:, 0].double().abs().sum())
+        bwd = float(st.det["bwd"]["poynting_flux"][:, 0].double().abs().sum())
+        assert fwd > 0 and bwd > 0
+        leak.append(bwd / fwd)
+    assert leak[0] / leak[1] < 0.85, leak
