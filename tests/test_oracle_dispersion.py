@@ -19,6 +19,9 @@ carrier frequency (dipole.py:150-193, linear_polarization.py:186-211, tfsf.py:21
   fraction 1 - R within 10% (7.0% at 25 nm cells against a 16 nm power decay length);
 * a plane source inside a uniform Lorentz medium injects the medium's impedance at the
   carrier: backward / forward flux < 2% (test_dispersion.py:329-360; the oracle gives 7e-7);
+* per-axis Lorentz poles act on their own axis only: each polarisation matches the isotropic
+  run with that axis' pole and its own Fresnel transmission
+  (test_anisotropic_dispersion.py:203-244);
 * the broadband H-side filter leaks less of a Gaussian pulse's energy backwards than the
   carrier-only impedance (ratio below 0.85, test_dispersive_source.py:192-225);
 * the library refuses a dispersive scene before any device work, and the oracle has no
@@ -124,7 +127,7 @@ def test_ade_update_formula():
     assert torch.equal(Pn, P_hat) and torch.equal(Pc1, Pc)
 
 
-def _flux_run(mat, half=True, src_z=12, dets=(("t", 140),)):
+def _flux_run(mat, half=True, src_z=12, dets=(("t", 140),), e_pol=(1, 0, 0)):
     nz = 200
     cfg = fx.SimulationConfig(time=120e-15, grid=fx.UniformGrid(25e-9))
     vol = fx.SimulationVolume(shape=(3, 3, nz))
@@ -135,7 +138,7 @@ def _flux_run(mat, half=True, src_z=12, dets=(("t", 140),)):
         objs.append(fx.UniformMaterialObject(name="m", grid_slice_tuple=((0, 3), (0, 3), (100 if half else 0, nz)),
                                              material=mat))
     objs.append(fx.UniformPlaneSource(name="s", grid_slice_tuple=((0, 3), (0, 3), (src_z, src_z + 1)), direction="+",
-                                      fixed_E_polarization_vector=(1, 0, 0), wave_character=fx.WaveCharacter(wavelength=WL)))
+                                      fixed_E_polarization_vector=e_pol, wave_character=fx.WaveCharacter(wavelength=WL)))
     for n, z in dets:
         objs.append(fx.PoyntingFluxDetector(name=n, grid_slice_tuple=((0, 3), (0, 3), (z, z + 1)), direction="+",
                                             reduce_volume=True))
@@ -213,3 +216,25 @@ def test_broadband_filter_reduces_backward_leakage():
         assert fwd > 0 and bwd > 0
         leak.append(bwd / fwd)
     assert leak[0] / leak[1] < 0.85, leak
+
+
+def test_per_axis_lorentz_half_space():
+    """Per-axis Lorentz poles (delta_eps 2.25 on x, 0.75 on y and z): an x-polarised wave sees
+    only chi_x and a y-polarised one only chi_y, so each run equals the isotropic run with that
+    axis' pole (rel 1e-4) and transmits the Fresnel power of its own eps(omega) (5%), and the
+    two transmissions differ (tests/simulation/physics/test_anisotropic_dispersion.py:203-244)."""
+    w0 = 2.0 * OMEGA
+    per_axis = fx.DispersionModel(poles=(fx.LorentzPole(resonance_frequency=w0, damping=1e13,
+                                                        delta_epsilon=(2.25, 0.75, 0.75)),))
+    s0 = _flux_run(None)["t"]
+    chi = per_axis.susceptibility_axes(OMEGA)
+    t = {}
+    for pol, de, e_pol in ((0, 2.25, (1, 0, 0)), (1, 0.75, (0, 1, 0))):
+        iso = fx.DispersionModel(poles=(fx.LorentzPole(resonance_frequency=w0, damping=1e13, delta_epsilon=de),))
+        s_axis = _flux_run(fx.Material(permittivity=1.0, dispersion=per_axis), e_pol=e_pol)["t"]
+        s_iso = _flux_run(fx.Material(permittivity=1.0, dispersion=iso), e_pol=e_pol)["t"]
+        assert s_iso > 0 and abs(s_axis - s_iso) / s_iso < 1e-4
+        t[pol] = s_axis / s0
+        t_ref = _fresnel_t(1.0 + chi[pol])
+        assert abs(t[pol] - t_ref) / t_ref < 0.05, (pol, t[pol], t_ref)
+    assert abs(t[0] - t[1]) > 0.02
