@@ -21,7 +21,8 @@ carrier frequency (dipole.py:150-193, linear_polarization.py:186-211, tfsf.py:21
   carrier: backward / forward flux < 2% (test_dispersion.py:329-360; the oracle gives 7e-7);
 * per-axis Lorentz poles act on their own axis only: each polarisation matches the isotropic
   run with that axis' pole and its own Fresnel transmission
-  (test_anisotropic_dispersion.py:203-244);
+  (test_anisotropic_dispersion.py:203-244), and a Drude pole on x alone makes a hyperbolic
+  medium that reflects x and passes y (test_anisotropic_dispersion.py:247-280);
 * the broadband H-side filter leaks less of a Gaussian pulse's energy backwards than the
   carrier-only impedance (ratio below 0.85, test_dispersive_source.py:192-225);
 * the library refuses a dispersive scene before any device work, and the oracle has no
@@ -238,3 +239,18 @@ def test_per_axis_lorentz_half_space():
         t_ref = _fresnel_t(1.0 + chi[pol])
         assert abs(t[pol] - t_ref) / t_ref < 0.05, (pol, t[pol], t_ref)
     assert abs(t[0] - t[1]) > 0.02
+
+
+def test_hyperbolic_drude_medium_is_polarisation_selective():
+    """A Drude pole on x only (omega_p = 5 omega, gamma = 0.05 omega): Re eps_x < 0 < eps_y, so
+    the x polarisation reflects like a metal and the y polarisation passes, each at its Fresnel
+    value within 0.05, and T_y - T_x > 0.8 (test_anisotropic_dispersion.py:247-280)."""
+    model = fx.DispersionModel(poles=(fx.DrudePole(plasma_frequency=(5 * OMEGA, 0.0, 0.0), damping=0.05 * OMEGA),))
+    chi = model.susceptibility_axes(OMEGA)
+    assert (1.0 + chi[0]).real < 0 < (1.0 + chi[1]).real
+    mat = fx.Material(permittivity=1.0, dispersion=model)
+    s0 = _flux_run(None)["t"]
+    t_x = _flux_run(mat, e_pol=(1, 0, 0))["t"] / s0
+    t_y = _flux_run(mat, e_pol=(0, 1, 0))["t"] / s0
+    assert abs(t_x - _fresnel_t(1.0 + chi[0])) < 0.05 and abs(t_y - _fresnel_t(1.0 + chi[1])) < 0.05
+    assert t_y - t_x > 0.8
