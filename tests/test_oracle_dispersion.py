@@ -254,3 +254,41 @@ def test_hyperbolic_drude_medium_is_polarisation_selective():
     t_y = _flux_run(mat, e_pol=(0, 1, 0))["t"] / s0
     assert abs(t_x - _fresnel_t(1.0 + chi[0])) < 0.05 and abs(t_y - _fresnel_t(1.0 + chi[1])) < 0.05
     assert t_y - t_x > 0.8
+
+
+def test_pole_model_kats():
+    """The pole models' closed forms and coefficient rules (tests/unit/test_dispersion.py:48-200)."""
+    lor = fx.DispersionModel(poles=(fx.LorentzPole(resonance_frequency=2e15, damping=1e13, delta_epsilon=3.5),))
+    chi0 = lor.susceptibility(0.0)
+    assert abs(chi0.imag) < 1e-18 and math.isclose(chi0.real, 3.5, rel_tol=1e-12)
+    m = fx.DispersionModel(poles=(fx.LorentzPole(resonance_frequency=1.5e15, damping=5e13, delta_epsilon=1.7),))
+    for w in (0.3e15, 0.9e15, 1.4e15, 2.5e15):
+        want = 1.7 * 1.5e15**2 / (1.5e15**2 - w**2 - 1j * 5e13 * w)
+        assert abs(m.susceptibility(w) - want) <= 1e-12 * abs(want)
+    d = fx.DispersionModel(poles=(fx.DrudePole(plasma_frequency=9e15, damping=1.5e13),))
+    for w in (0.5e15, 2e15, 5e15):
+        want = -(9e15**2) / (w**2 + 1j * 1.5e13 * w)
+        assert abs(d.susceptibility(w) - want) <= 1e-12 * abs(want)
+    p = fx.LorentzPole(resonance_frequency=2e15, damping=3e13, delta_epsilon=1.5)
+    c1, c2, c3 = compute_pole_coefficients_per_axis((p,), 5e-18)
+    den = 1.0 + 0.5 * 3e13 * 5e-18
+    assert np.allclose(c1[0], (2.0 - (2e15 * 5e-18) ** 2) / den, rtol=1e-12)
+    assert np.allclose(c2[0], -(1.0 - 0.5 * 3e13 * 5e-18) / den, rtol=1e-12)
+    assert np.allclose(c3[0], 1.5 * 2e15**2 * (5e-18) ** 2 / den, rtol=1e-12)
+    q = fx.DrudePole(plasma_frequency=1e16, damping=1e14)
+    c1, _, c3 = compute_pole_coefficients_per_axis((q,), 2e-18)
+    den = 1.0 + 0.5 * 1e14 * 2e-18
+    assert np.allclose(c1[0], 2.0 / den, rtol=1e-12) and np.allclose(c3[0], 1e32 * 4e-36 / den, rtol=1e-12)
+    _, c2, _ = compute_pole_coefficients_per_axis((fx.LorentzPole(resonance_frequency=1e15, damping=1e13,
+                                                                  delta_epsilon=2.0),), 1e-17)
+    assert abs(c2[0, 0] + 1.0) < 2e-4
+    slow = fx.LorentzPole(resonance_frequency=1e15, damping=1e10, delta_epsilon=2.0)
+    with pytest.raises(ValueError, match=r"omega_0 \* dt"):
+        compute_pole_coefficients_per_axis((slow,), 2.0 / 1e15)
+    assert np.isfinite(compute_pole_coefficients_per_axis((slow,), 1.9 / 1e15)[0]).all()
+    inert = fx.LorentzPole(resonance_frequency=3e17, damping=3e17, delta_epsilon=0.0)
+    c1, c2, c3 = compute_pole_coefficients_per_axis((inert,), 1e-17)
+    assert (c3 == 0).all() and np.isfinite(c1).all() and np.isfinite(c2).all()
+    assert not fx.Material(permittivity=2.25).is_dispersive
+    assert not fx.Material(dispersion=fx.DispersionModel()).is_dispersive
+    assert fx.Material(dispersion=m).is_dispersive
