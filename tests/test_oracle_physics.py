@@ -33,7 +33,9 @@ replayed on the restatement, so its physics is pinned beyond internal consistenc
   (tests/simulation/physics/sources/test_gaussian_source.py:148-219, 10%);
 * mixed boundaries (PEC on x, PMC on y, both) with CPML along z keep free-space k and
   impedance (tests/simulation/physics/boundaries/test_mixed_boundaries.py, 5%);
-* a TFSF plane injects one way: flux behind it below 1e-3 of the flux ahead.
+* a TFSF plane injects one way: flux behind it below 1e-3 of the flux ahead;
+* PEC walls put the standing wave's E node at the wall, PMC walls its antinode
+  (tests/simulation/physics/boundaries/test_pec_pmc_symmetry.py:168-215).
 
 The plane-wave checks use the reference's quasi-1D domains: 3 x 3 periodic cells across,
 CPML along z, a +z uniform plane source with Ex polarisation (the default CW profile unless
@@ -460,3 +462,31 @@ def test_tfsf_plane_injects_one_way(direction, eps):
 def _mean_flux_named(st, name: str, steps_per_period: int) -> float:
     f = st.det[name]["poynting_flux"][:, 0].double().numpy()
     return float(f[-10 * steps_per_period:].mean())
+
+
+@pytest.mark.parametrize("wall", ["pec", "pmc"])
+def test_conductor_wall_standing_wave_nodes(wall):
+    """A plane wave reflected by a PEC wall has its E node at the wall and an antinode a quarter
+    wavelength away (|Ex| one cell from the wall / |Ex| at lambda / 4 below 0.2); a PMC wall
+    swaps them (ratio above 5) (tests/simulation/physics/boundaries/test_pec_pmc_symmetry.py:
+    168-215, 12.5 nm cells, 100 fs instead of 150 fs)."""
+    dx, nz = 12.5e-9, 400
+    cfg = fx.SimulationConfig(time=100e-15, grid=fx.UniformGrid(dx))
+    vol = fx.SimulationVolume(shape=(3, 3, nz))
+    bc = fx.BoundaryConfig(boundary_type_minx="periodic", boundary_type_maxx="periodic",
+                           boundary_type_miny="periodic", boundary_type_maxy="periodic",
+                           thickness_grid_minz=10, boundary_type_maxz=wall)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    wc = fx.WaveCharacter(wavelength=WL)
+    objs.append(fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, 3), (0, 3), (12, 13)), direction="+",
+                                      fixed_E_polarization_vector=(1, 0, 0), wave_character=wc))
+    for name, z in (("near", nz - 2), ("far", nz - 21)):
+        objs.append(fx.PhasorDetector(name=name, grid_slice_tuple=((0, 3), (0, 3), (z, z + 1)), wave_characters=(wc,),
+                                      components=("Ex",), reduce_volume=True))
+    _, st = _run(cfg, objs)
+    near = float(st.det["near"]["phasor"].abs().max())
+    far = float(st.det["far"]["phasor"].abs().max())
+    if wall == "pec":
+        assert far > 0 and near / far < 0.2, (near, far)
+    else:
+        assert near > 0 and (far == 0 or near / far > 5.0), (near, far)
