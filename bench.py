@@ -121,6 +121,13 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_name(shape=SHAPE) -> str:
+    """The workload string both arms print (the reference arm times a bounded x-slab sample of
+    this same scene; its ``cpu_baseline.sample`` says which)."""
+    return (f"coupler {shape[0]}x{shape[1]}x{shape[2]} @20nm, 10-cell CPML, CW Gaussian TFSF source, full-volume "
+            "Ex/Ey/Ez phasor + 2 phasor-flux planes (8000-step run; K consecutive steps timed)")
+
+
 def _fused(dd) -> bool:
     """E-only phasor / field detectors without volume reduction ride in the H half-step."""
     return dd.kind in (1, 0) and (dd.comp_mask & 56) == 0 and not dd.reduce_volume
@@ -180,6 +187,8 @@ def run_gpu(args):
         scene.tune(args.chunk, args.vec)
     if args.shell_chunk or args.shell_vec:
         scene.tune_shell(args.shell_chunk, args.shell_vec)
+    if args.zshell != "auto" or args.zs_ty or args.zs_chunk:
+        scene.tune_zshell(args.zshell != "0", args.zs_ty, args.zs_chunk)
     ncell = shape[0] * shape[1] * shape[2]
     W, K = args.warmup, args.steps
     if W + K + 8 > T_TOTAL:
@@ -261,6 +270,8 @@ def run_gpu(args):
     scene.close()
     del arrays, base, host_eps
     torch.cuda.empty_cache()
+    if ws > 1:  # the secondary measurements are single-GPU workloads: the headline alone scales
+        args.no_gradient = args.no_batch = args.no_serving = True
     if not args.no_gradient:
         extra["gradient"] = bench_gradient(dev)
         torch.cuda.empty_cache()
@@ -285,14 +296,14 @@ def run_gpu(args):
         "dtype": "f32",
         "data": "synthetic (seeded scene builder)",
         "config": {
-            "workload": f"coupler {shape[0]}x{shape[1]}x{shape[2]} @20nm, 10-cell CPML, CW Gaussian TFSF source, full-volume Ex/Ey/Ez "
-                        "phasor + 2 phasor-flux planes (8000-step run; K consecutive steps timed)",
+            "workload": workload_name(shape),
             "cells": ncell,
             "l2": "inputs larger than L2 (fields 384 MB, phasor 768 MB)",
             "parallelism": f"replicas x{ws}",
             "chunk": int(NATIVE.load().fdtd_plan_chunk(scene.plan)),
             "vec": int(NATIVE.load().fdtd_plan_vec(scene.plan)),
             "tma": scene.uses_tma,
+            "zshell_tma": scene.uses_zshell,
             "hbm_gbs_effective": round(sum(alg.values()) / (ms / K / 1e3) / 1e9, 1),
         },
         "roofline": {
@@ -368,7 +379,8 @@ def bench_gradient(dev, steps: int = 3000) -> dict:
         }
 
 
-def _strip_sims(n: int, steps: int, dev, seed: int = 0):
+def _strip_sims(n: int, steps: int, dev, seed: int = 0, lo=(64, 64, 64), hi=(256, 256, 128), pml: int = 10):
+    """Seeded strips (uniform integer sizes per axis in [lo, hi], width uniform in 0.30-0.80 um)."""
     import numpy as np
 
     from fdtdx_gb300 import scenes
@@ -376,61 +388,124 @@ def _strip_sims(n: int, steps: int, dev, seed: int = 0):
     rng = np.random.default_rng(seed)
     sims, cells = [], 0
     for _ in range(n):
-        nx, ny = (int(x) for x in rng.integers(64, 257, size=2))
-        nz = int(rng.integers(64, 129))
+        nx, ny = (int(x) for x in rng.integers((lo[0], lo[1]), (hi[0] + 1, hi[1] + 1)))
+        nz = int(rng.integers(lo[2], hi[2] + 1))
         w = float(rng.uniform(0.30, 0.80))
-        o, a, _, c, _ = scenes.strip(shape=(nx, ny, nz), width_um=w, steps=steps, device=dev)
+        o, a, _, c, _ = scenes.strip(shape=(nx, ny, nz), width_um=w, steps=steps, device=dev, pml=pml)
         sims.append((a, o, c))
         cells += nx * ny * nz
     return sims, cells
 
 
-def bench_batch(dev, n_sims: int = 64, steps: int = 2000) -> dict:
-    """64 Si strips of seeded uneven grids (64..256 x 64..256 x 64..128 @25 nm, 10-cell CPML,
-    2000 steps, pulsed Gaussian source, transmitted phasor flux): one batch (persistent
-    launches, CUDA graph, autotuned tiles) against the same runs one at a time."""
+def _zero_state(arrays) -> None:
+    """Fields, psi and detector states back to zero in place (a fresh run on the same buffers,
+    so captured CUDA graphs stay valid)."""
+    f = arrays.fields
+    f.E.zero_()
+    f.H.zero_()
+    for n in f.psi_E:
+        for t in (*f.psi_E[n], *f.psi_H[n]):
+            t.zero_()
+    for st in arrays.detector_states.values():
+        for v in st.values():
+            v.zero_()
+
+
+def _batch_case(sims, cells, steps: int) -> dict:
+    """One batch of ``sims`` against the same runs one at a time, plans, batch tables, tile
+    tuning and CUDA-graph capture all done before either timer starts."""
     from fdtdx_gb300.batch import SimulationBatch
     from fdtdx_gb300.engine import Scene
     from fdtdx_gb300.fdtd import _materials_detached
 
-    sims, cells = _strip_sims(n_sims, steps, dev)
     work = cells * steps
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for a, o, c in sims:  # plain path, one at a time (plan per run, graph-replayed steps)
+    # one at a time: every plan built and its graph captured first, then the runs back to back
+    seq = []
+    for a, o, c in sims:
         w = _materials_detached(a).reset()
-        s = Scene(o, w, c)
-        s.forward(w, 0, steps)
-        s.close()
+        sc = Scene(o, w, c)
+        sc.forward(w, 0, 64)
+        _zero_state(w)
+        seq.append((sc, w))
     torch.cuda.synchronize()
-    seq = time.perf_counter() - t0
     t0 = time.perf_counter()
+    for sc, w in seq:
+        sc.forward(w, 0, steps)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    for sc, _ in seq:
+        sc.close()
+    del seq
+    torch.cuda.empty_cache()
+    # batched: tiles tuned on real steps and the graph captured, then the state zeroed
     b = SimulationBatch(sims)
-    b.advance(steps, t0=[0] * n_sims, graph=True, autotune=True)
+    b.advance(min(400, steps), t0=[0] * len(sims), graph=True, autotune=True)
+    b.advance(64, graph=True, autotune=False)
+    for w in b.arrays:
+        _zero_state(w)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.advance(steps, t0=[0] * len(sims), graph=True, autotune=False)
     torch.cuda.synchronize()
     bt = time.perf_counter() - t0
     tune = b.tuning()
     launches = b.launches_per_step()
     b.close()
     return {
-        "workload": f"{n_sims} Si strips, seeded grids 64-256 x 64-256 x 64-128 @25nm, 10-cell CPML, {steps} steps, "
-                    "pulsed Gaussian source, transmitted phasor flux",
         "cells_total": cells,
         "batched_cell_updates_per_s": work / bt,
-        "sequential_cell_updates_per_s": work / seq,
-        "speedup_vs_sequential": seq / bt,
+        "sequential_cell_updates_per_s": work / seq_s,
+        "speedup_vs_sequential": seq_s / bt,
         "batched_s": round(bt, 3),
-        "sequential_s": round(seq, 3),
+        "sequential_s": round(seq_s, 3),
         "launches_per_batch_step": launches,
         "tiles": tune,
     }
 
 
-def bench_serving(capacity: float, n_jobs: int = 32, seed: int = 0) -> dict:
+def _strip_bytes_per_step(sims) -> float:
+    """Algorithmic bytes of one step of every simulation (the per-launch-group formula summed)."""
+    from fdtdx_gb300.engine import Scene
+
+    tot = 0
+    for a, o, c in sims:
+        sc = Scene(o, a, c)
+        tot += sum(algorithmic_bytes(sc).values())
+    return float(tot)
+
+
+def bench_batch(dev, n_sims: int = 64, steps: int = 2000) -> dict:
+    """64 Si strips of seeded uneven grids (64..256 x 64..256 x 64..128 @25 nm, 10-cell CPML,
+    2000 steps, pulsed Gaussian source, transmitted phasor flux): one batch (CUDA graph,
+    autotuned tiles) against the same runs one at a time; and the same for 64 small strips
+    (32..96 per axis, 8-cell CPML), where a run alone is bound by launches, not bandwidth.
+    Setup (plans, batch tables, tuning, graph capture) is outside both timers."""
+    peak, _ = _peaks()
+    sims, cells = _strip_sims(n_sims, steps, dev)
+    out = {"workload": f"{n_sims} Si strips, seeded grids 64-256 x 64-256 x 64-128 @25nm, 10-cell CPML, {steps} steps, "
+                       "pulsed Gaussian source, transmitted phasor flux"}
+    bps = _strip_bytes_per_step(sims)
+    r = _batch_case(sims, cells, steps)
+    r["batched_roofline_frac"] = round(bps * steps / r["batched_s"] / 1e9 / peak, 4)
+    out.update(r)
+    del sims
+    torch.cuda.empty_cache()
+    small, scells = _strip_sims(n_sims, steps, dev, seed=1, lo=(32, 32, 32), hi=(96, 96, 96), pml=8)
+    sb = _strip_bytes_per_step(small)
+    rs = _batch_case(small, scells, steps)
+    rs["batched_roofline_frac"] = round(sb * steps / rs["batched_s"] / 1e9 / peak, 4)
+    rs["sequential_roofline_frac"] = round(sb * steps / rs["sequential_s"] / 1e9 / peak, 4)
+    rs["workload"] = f"{n_sims} small Si strips, seeded grids 32-96 per axis @25nm, 8-cell CPML, {steps} steps"
+    out["small_grids"] = rs
+    return out
+
+
+def bench_serving(capacity: float, n_jobs: int = 200, seed: int = 0, load: float = 1.5) -> dict:
     """Poisson stream: grids log-uniform in [32,384]x[32,384]x[32,192] @50 nm, steps uniform
     in [500, 10000], 70% forward / 30% forward+gradient, random boxes (20% diagonal-
-    anisotropic, per-axis eps in [2, 12]), 160 GB admission budget; rate = 0.8 x the
-    measured batched capacity.  Served (continuous batching) against one at a time."""
+    anisotropic, per-axis eps in [2, 12]), 160 GB admission budget.  The offered load is
+    ``load`` x the measured batched capacity, so both arms run saturated and their aggregate
+    throughputs and latencies compare; served (continuous batching) against one at a time."""
     import numpy as np
 
     from fdtdx_gb300.serving import Server, estimate_footprint, latency_stats, random_boxes_job, run_one_at_a_time
@@ -439,25 +514,20 @@ def bench_serving(capacity: float, n_jobs: int = 32, seed: int = 0) -> dict:
 
     def make():
         rng = np.random.default_rng(seed)
-        jobs, t = [], 0.0
         specs = []
-        for q in range(n_jobs):
+        for _ in range(n_jobs):
             shp = [int(round(math.exp(rng.uniform(math.log(32), math.log(hi))))) for hi in (384, 384, 192)]
             steps = int(rng.integers(500, 10001))
             kind = "gradient" if rng.uniform() < 0.3 else "forward"
             aniso = bool(rng.uniform() < 0.2)
             specs.append((shp, steps, kind, aniso))
-        for q, (shp, steps, kind, aniso) in enumerate(specs):
-            jobs.append(random_boxes_job(shp, steps, seed=seed * 1000 + q, kind=kind, anisotropic=aniso))
-        return jobs, specs
+        return [random_boxes_job(shp, steps, seed=seed * 1000 + q, kind=kind, anisotropic=aniso)
+                for q, (shp, steps, kind, aniso) in enumerate(specs)]
 
-    jobs, specs = make()
-    keep = []
-    for j in jobs:
-        if estimate_footprint(j) <= budget:
-            keep.append(j)
+    jobs = make()
+    keep = [j for j in jobs if estimate_footprint(j) <= budget]
     work = sum(j.cells * j.steps * (4.5 if j.kind == "gradient" else 1.0) for j in keep)
-    rate = 0.8 * capacity / (work / len(keep))  # jobs per second
+    rate = load * capacity / (work / len(keep))  # jobs per second
     rng = np.random.default_rng(seed + 1)
     t = 0.0
     arrivals = []
@@ -470,10 +540,9 @@ def bench_serving(capacity: float, n_jobs: int = 32, seed: int = 0) -> dict:
     server.run(keep, realtime=True)
     served = latency_stats(keep)
     served_work = server.forward_cell_updates + server.adjoint_cell_updates
-    served_tp = served_work / server.makespan
+    torch.cuda.empty_cache()
     # the same stream one at a time
-    jobs2, _ = make()
-    keep2 = [j for j in jobs2 if estimate_footprint(j) <= budget]
+    keep2 = [j for j in make() if estimate_footprint(j) <= budget]
     for j, a in zip(keep2, arrivals):
         j.arrival = a
     t0 = time.perf_counter()
@@ -483,10 +552,10 @@ def bench_serving(capacity: float, n_jobs: int = 32, seed: int = 0) -> dict:
     return {
         "workload": f"{len(keep)} jobs (of {n_jobs}; larger than the budget dropped), grids log-uniform 32-384 x 32-384 "
                     "x 32-192 @50nm, steps 500-10000, 70% forward / 30% gradient, 20% diagonal-anisotropic, "
-                    "160 GB budget, Poisson arrivals",
+                    f"160 GB budget, Poisson arrivals at {load}x the batched capacity",
         "rate_jobs_per_s": rate,
         "served": {"p50_s": served["p50_s"], "p99_s": served["p99_s"], "mean_s": served["mean_s"],
-                   "makespan_s": server.makespan, "cell_updates_per_s": served_tp},
+                   "makespan_s": server.makespan, "cell_updates_per_s": served_work / server.makespan},
         "one_at_a_time": {"p50_s": plain["p50_s"], "p99_s": plain["p99_s"], "mean_s": plain["mean_s"],
                           "makespan_s": plain_s, "cell_updates_per_s": served_work / plain_s},
         "gradient_jobs": sum(1 for j in keep if j.kind == "gradient"),
@@ -552,7 +621,8 @@ def run_reference(args):
         "metric": METRIC, "value": val, "unit": "cell-updates/s", "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene builder)", "impl": "reference",
-        "config": {"workload": "coupler 400x400x200 @20nm (x-slab sample on the host CPU)", "cells": nx * SHAPE[1] * SHAPE[2]},
+        "config": {"workload": workload_name(), "cells": SHAPE[0] * SHAPE[1] * SHAPE[2],
+                   "sample_cells": nx * SHAPE[1] * SHAPE[2]},
         "cpu_baseline": {"value": val, "unit": "cell-updates/s", "cores": torch.get_num_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -576,6 +646,10 @@ def main():
     ap.add_argument("--shell-chunk", type=int, default=0, help="x planes per CPML shell block (0: plan default)")
     ap.add_argument("--shell-vec", type=int, default=0, help="z cells per CPML shell thread (0: plan default)")
     ap.add_argument("--tma", default="auto", choices=["auto", "0", "1"], help="TMA-pipelined update kernels")
+    ap.add_argument("--zshell", default="auto", choices=["auto", "0", "1"],
+                    help="z-slab CPML shell boxes on the TMA kernels")
+    ap.add_argument("--zs-ty", type=int, default=0, help="rows of the z-shell TMA tile (0: default)")
+    ap.add_argument("--zs-chunk", type=int, default=0, help="x planes per z-shell TMA block (0: default)")
     ap.add_argument("--tz", type=int, default=0)
     ap.add_argument("--ty", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)
@@ -587,7 +661,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream measurement")
     ap.add_argument("--batch-sims", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2000)
-    ap.add_argument("--serve-jobs", type=int, default=32)
+    ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--case", default="all", choices=["all", "gradient", "batch", "serving"],
                     help="run one secondary measurement alone and print its record (profiling)")
     ap.add_argument("--grad-steps", type=int, default=3000, help="steps of the gradient case (profiling: fewer)")

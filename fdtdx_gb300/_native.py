@@ -16,6 +16,8 @@ MAX_DETECTORS = 32
 MAX_FREQS = 16
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENONFINITE = range(6)
+FWD_GRAPH, FWD_CHECK_FINITE = 1, 2
+INJECT_ALLOC, INJECT_WAIT_EXPIRY = 1, 2
 PROFILE_CW, PROFILE_GAUSSIAN = 0, 1
 SRC_DIPOLE, SRC_PLANE = 0, 1
 DET_FIELD, DET_PHASOR, DET_FLUX, DET_ENERGY = 0, 1, 2, 3
@@ -162,7 +164,10 @@ SIGNATURES = {
     "fdtd_plan_vec": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_tune_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "fdtd_plan_uses_tma": (C.c_int32, [C.c_void_p]),
+    "fdtd_plan_tune_zshell": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "fdtd_plan_uses_zshell": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_status": (C.c_int, [C.c_void_p]),
+    "fdtd_debug_inject": (C.c_int, [C.c_int32, C.c_int32]),
     "fdtd_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(Buffers), C.c_int32, C.POINTER(C.c_void_p)]),
     "fdtd_batch_destroy": (None, [C.c_void_p]),
     "fdtd_batch_last_error": (C.c_char_p, [C.c_void_p]),
@@ -209,7 +214,11 @@ def load(build_if_missing: bool = False) -> C.CDLL:
 
 
 class NativeError(RuntimeError):
-    pass
+    """A status code other than FDTD_OK from the native library (``code`` holds it)."""
+
+    def __init__(self, message: str, code: int | None = None):
+        super().__init__(message)
+        self.code = code
 
 
 def check(rc: int, plan: int | None = None, what: str = "") -> None:
@@ -221,7 +230,7 @@ def check(rc: int, plan: int | None = None, what: str = "") -> None:
         msg = m.decode() if m else ""
     names = {EINVAL: "FDTD_EINVAL", ENOMEM: "FDTD_ENOMEM", ECUDA: "FDTD_ECUDA", ETIMEOUT: "FDTD_ETIMEOUT",
              ENONFINITE: "FDTD_ENONFINITE"}
-    raise NativeError(f"{what}: {names.get(rc, rc)} {msg}".strip())
+    raise NativeError(f"{what}: {names.get(rc, rc)} {msg}".strip(), rc)
 
 
 def ptr(t) -> int | None:

@@ -92,10 +92,12 @@ class _ReversibleRun(torch.autograd.Function):
         bounds = ctl["bounds"]
         checkpoints = []
         for seg in range(len(bounds) - 1):
-            scene.forward(arrays, bounds[seg], bounds[seg + 1] - bounds[seg])
+            scene.forward(arrays, bounds[seg], bounds[seg + 1] - bounds[seg], check_finite=seg == len(bounds) - 2)
             if seg < len(bounds) - 2:
                 checkpoints.append(_clone_fields(arrays.fields))
-        scene.status()
+        from fdtdx_gb300.fdtd import finite_status
+
+        finite_status(scene)
         ctl["checkpoints"] = checkpoints
         ctl["final"] = arrays
         ctx.ctl = ctl

@@ -57,7 +57,7 @@ class SimulationBatch:
     def _check(self, rc: int, what: str) -> None:
         if rc != N.OK:
             msg = N.load().fdtd_batch_last_error(self._h)
-            raise N.NativeError(f"{what}: {rc} {msg.decode() if msg else ''}")
+            raise N.NativeError(f"{what}: {rc} {msg.decode() if msg else ''}", rc)
 
     def advance(self, n_steps: int, t0: Sequence[int] | None = None, graph: bool = True, autotune: bool = True,
                 stream=None) -> None:

@@ -329,7 +329,7 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     const size_t oD = ar.take(sizeof(BDet) * std::max(1, dets)), oDU = ar.take(sizeof(int2) * std::max(1, du));
     const size_t oDR = ar.take(sizeof(int) * std::max(1, dred)), oT = ar.take(sizeof(int*) * n);
     const size_t oI = ar.take(sizeof(BIface) * std::max(1, nif)), oIU = ar.take(sizeof(int2) * std::max(1, ifu));
-    cudaError_t e = cudaMalloc(&b->dmem, ar.off);
+    cudaError_t e = dev_alloc(reinterpret_cast<void**>(&b->dmem), ar.off);
     if (e != cudaSuccess) {
         fprintf(stderr, "fdtd_batch_create: cudaMalloc(%zu): %s\n", ar.off, cudaGetErrorString(e));
         delete b;
@@ -571,6 +571,7 @@ int batch_autotune(FdtdBatch* b, int budget, int* parity, cudaStream_t st) {
 }  // namespace
 
 extern "C" int fdtd_batch_forward(FdtdBatch* b, const int32_t* t0, int32_t n_steps, int32_t flags, void* stream) {
+    NvtxRange nvtx_range("fdtd_batch_forward");
     if (!b) return FDTD_EINVAL;
     if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
         return bfail(b, FDTD_ECUDA, std::string("error left pending by an earlier CUDA call (before fdtd_batch_forward): ") +

@@ -1056,4 +1056,14 @@ __global__ void k_interfaces(const Geo g, const IfaceDev ifc, const int* __restr
 __global__ void k_set_step(int* tp, int t) { *tp = t; }
 __global__ void k_advance(int* tp, int delta) { *tp += delta; }
 
+// Sets *err to FDTD_ENONFINITE when any of the n floats at f is a NaN or an infinity
+// (grid-stride, one flag per block).  Reads only; the fields are left as they are.
+__global__ void __launch_bounds__(256) k_check_finite(const float* __restrict__ f, long long n, int* err) {
+    bool bad = false;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
+        bad |= !isfinite(__ldg(f + q));
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(err, FDTD_ENONFINITE);
+}
+
 }  // namespace fdtd

@@ -46,7 +46,12 @@ extern "C" int fdtd_detector_sample_noalloc(const FdtdDetectorDesc* det, int32_t
             return noalloc_reject("detector region must be non-empty and inside the grid");
     if (det->kind == FDTD_DET_FIELD && ((det->comp_mask & 63) == 0 || (det->comp_mask & ~63)))
         return noalloc_reject("comp_mask must select components among Ex..Hz");
-    if (det->exact_interpolation && !H_prev) return noalloc_reject("H_prev is required with exact interpolation");
+    // H before the step's H update is read only where the plan's detectors read it too: exact
+    // interpolation of a FLUX or ENERGY sample, or of a FIELD sample recording H components
+    const bool needs_hprev = det->exact_interpolation &&
+                             (det->kind != FDTD_DET_FIELD || (det->comp_mask & 56) != 0);
+    if (needs_hprev && !H_prev)
+        return noalloc_reject("H_prev is required with exact interpolation of H components");
     if (n_eps != 1 && n_eps != 3) return noalloc_reject("n_eps must be 1 or 3");
     if (n_mu != 0 && n_mu != 1 && n_mu != 3) return noalloc_reject("n_mu must be 0, 1 or 3");
     if (det->kind == FDTD_DET_ENERGY && (!inv_eps || (n_mu && !inv_mu)))
@@ -87,10 +92,19 @@ extern "C" int fdtd_detector_sample_noalloc(const FdtdDetectorDesc* det, int32_t
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_reject(cudaGetErrorString(e));
     if (dev < 0 || dev >= kNoAllocDevices) return noalloc_reject("device ordinal beyond the scratch address table");
+    // The scratch address is looked up again on every call made outside stream capture, so
+    // a device reset (which reloads the module and may move the array) is picked up by the
+    // next call; inside a capture the address of the last call on this device is used.
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
     float* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
+        if (!g_noalloc_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
             void* ptr = nullptr;
             e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
             if (e != cudaSuccess) {
@@ -111,8 +125,7 @@ extern "C" int fdtd_detector_sample_noalloc(const FdtdDetectorDesc* det, int32_t
     g.nx = nx; g.ny = ny; g.nz = nz;
     g.N = (long long)nx * ny * nz;
     g.px = periodic[0] != 0; g.py = periodic[1] != 0; g.pz = periodic[2] != 0;
-    DetFields f{E, d.exact ? H_prev : H, H, inv_eps, n_eps, n_mu ? inv_mu : nullptr, n_mu ? n_mu : 1, inv_mu_scalar};
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    DetFields f{E, needs_hprev ? H_prev : H, H, inv_eps, n_eps, n_mu ? inv_mu : nullptr, n_mu ? n_mu : 1, inv_mu_scalar};
     k_detector<<<d.nblocks, kDetBlock, 0, st>>>(g, d, tp, f, out);
     k_detector_finalize<<<1, kDetBlock, 0, st>>>(d, tp, out);
     e = cudaGetLastError();

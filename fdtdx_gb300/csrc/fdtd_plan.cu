@@ -2,6 +2,7 @@
 // (device copies of the small per-scene tables), the per-step launch sequence,
 // CUDA-graph capture of the step loop and the reverse (time-reversed) loop.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,7 @@
 #include "fdtd_tma.cuh"
 
 #include <cudaTypedefs.h>
+#include <nvtx3/nvToolsExt.h>
 
 using namespace fdtd;
 
@@ -43,6 +45,12 @@ struct FdtdPlan {
     int tma_tz = 32, tma_ty = 8, tma_ns = 4;
     int tma_chunk = 1;                    // x planes per block of the H kernel
     int tma_chunk_e = 1;                  // and of the E kernel
+    // the two z-slab shell boxes through the TMA kernels with their CPML terms (ZP kernels)
+    bool zs_ok = false;                   // the split admits them (core on TMA, z boxes of <= 64 cells)
+    bool zs_on = true;                    // selected (fdtd_plan_tune_zshell)
+    int zs_tz = 0, zs_ty = 16;            // tile: the thicker z box's extent x zs_ty rows
+    int zs_chunk = 1, zs_chunk_e = 1;     // x planes per block (H, E)
+    int zs_sides = 0, zs_lo = 0, zs_hi = 0;
     int* d_err = nullptr;                 // kernel error word (FDTD_ETIMEOUT on a wait that ran out)
     // graph cache for the forward loop
     cudaGraphExec_t gexec = nullptr;
@@ -50,6 +58,12 @@ struct FdtdPlan {
     FdtdBuffers gbufs{};
     int gsteps = 0;
     cudaStream_t cap_stream = nullptr;
+    // graph cache for the adjoint loop (an even number of steps: the cotangents ping-pong)
+    cudaGraphExec_t agexec = nullptr;
+    cudaGraph_t agraph = nullptr;
+    FdtdBuffers agbufs{};
+    FdtdAdjointBuffers agadj{};
+    int agsteps = 0;
     // reversible-gradient scratch, allocated by the first fdtd_adjoint call
     char* amem = nullptr;
     size_t amem_bytes = 0;
@@ -64,6 +78,36 @@ namespace {
 
 size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
+// An NVTX range over one entry point (shown by Nsight tools when one is attached; a few
+// nanoseconds otherwise).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+// Injected failures still to deliver (fdtd_debug_inject): process-wide counters.
+std::atomic<int> g_inject_alloc{0};
+std::atomic<int> g_inject_expiry{0};
+
+bool take_injected(std::atomic<int>& counter) {
+    int v = counter.load();
+    while (v > 0)
+        if (counter.compare_exchange_weak(v, v - 1)) return true;
+    return false;
+}
+
+// Every device allocation of the library goes through here, so an injected allocation failure
+// reaches each caller's out-of-memory path without exhausting the device.
+cudaError_t dev_alloc(void** ptr, size_t bytes) {
+    if (take_injected(g_inject_alloc)) {
+        *ptr = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(ptr, bytes);
+}
+
 int fail(FdtdPlan* p, int code, const std::string& msg) {
     if (p) p->err = msg;
     return code;
@@ -71,6 +115,17 @@ int fail(FdtdPlan* p, int code, const std::string& msg) {
 
 int cuda_fail(FdtdPlan* p, cudaError_t e, const char* where) {
     return fail(p, FDTD_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Drops the cached CUDA graphs of the forward and adjoint loops (a tuning change alters the
+// launches they hold).
+void drop_graphs(FdtdPlan* p) {
+    if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    p->gsteps = 0;
+    if (p->agexec) { cudaGraphExecDestroy(p->agexec); p->agexec = nullptr; }
+    if (p->agraph) { cudaGraphDestroy(p->agraph); p->agraph = nullptr; }
+    p->agsteps = 0;
 }
 
 // Layout of the plan's single device allocation.
@@ -310,6 +365,65 @@ int staged_planes(const FdtdPlan* p) {
     return 0;
 }
 
+// The z-slab shell boxes ([0, zlo) and [zhi, nz) over the core's x and y range: their cells
+// lie in no x or y slab, so the ZP TMA kernels update them with the z terms alone.  Tile: the
+// thicker box's z extent (a multiple of 4) x zs_ty rows; x chunks of about four waves.
+void configure_zshell(FdtdPlan* p, const Split& sp, int optin) {
+    p->zs_ok = false;
+    if (!sp.split || p->d.n_slabs == 0) return;
+    const int nz = p->g.nz, zlo = sp.core.lo[2], zhi = sp.core.hi[2];
+    const int sides = (zlo > 0 ? 1 : 0) | (zhi < nz ? 2 : 0);
+    if (!sides) return;
+    // every z slab must lie inside its box, one slab per z face (the per-axis table), 32-bit psi offsets
+    int faces = 0;
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        const DSlab& sl = p->slab[s];
+        if ((long long)sl.sx * sl.sy * sl.sz >= (1LL << 31)) return;
+        if (sl.axis != 2) continue;
+        const int side = p->d.slabs[s].direction > 0 ? 1 : 0;
+        if (faces >> side & 1) return;
+        faces |= 1 << side;
+        if (side == 0 ? sl.lo + sl.L > zlo : sl.lo < zhi) return;
+    }
+    const int tz = std::max(zlo, nz - zhi);
+    const int ty = p->zs_ty;
+    if (tz % 4 || tz > 64 || ty < 1 || ty * tz / 2 > 256 || ty * tz / 2 < 32) return;
+    const int threads = ty * tz / 2;
+    const size_t smE = tma_smem(tma_cfg(tz, ty, p->tma_ns, false, p->d.n_eps, p->d.n_sigma_E, nullptr));
+    const size_t smH = tma_smem(tma_cfg(tz, ty, p->tma_ns, true, p->d.n_mu, p->d.n_sigma_H, nullptr, staged_planes(p)));
+    int occ_e = 1 << 30, occ_h = 1 << 30;
+    bool ok = true;
+    auto setup = [&](const void* fn, size_t sm, int& o) {
+        if ((int)sm > optin || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+            ok = false;
+            return;
+        }
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, sm) != cudaSuccess) nb = 0;
+        o = std::min(o, nb);
+    };
+    setup((const void*)k_tma_E<false, true>, smE, occ_e);
+    setup((const void*)k_tma_E<true, true>, smE, occ_e);
+    setup((const void*)k_tma_H<false, true>, smH, occ_h);
+    setup((const void*)k_tma_H<true, true>, smH, occ_h);
+    cudaGetLastError();
+    if (!ok || occ_e <= 0 || occ_h <= 0) return;
+    const int cx = sp.core.hi[0] - sp.core.lo[0], cy = sp.core.hi[1] - sp.core.lo[1];
+    const long long tiles = (long long)((sides & 1) + (sides >> 1)) * ((cy + ty - 1) / ty);
+    auto chunk_for = [&](int waves, int o) {
+        long long n = std::max(1ll, (long long)waves * o * p->sm_count / tiles);
+        n = std::min<long long>(n, std::max(1, cx / 4));
+        return (int)((cx + n - 1) / n);
+    };
+    p->zs_tz = tz;
+    p->zs_sides = sides;
+    p->zs_lo = zlo;
+    p->zs_hi = zhi;
+    p->zs_chunk_e = chunk_for(4, occ_e);
+    p->zs_chunk = chunk_for(4, occ_h);
+    p->zs_ok = true;
+}
+
 // Shared memory, occupancy and the x-chunk of the TMA kernels for the current tile choice.
 void configure_tma(FdtdPlan* p) {
     p->use_tma = false;
@@ -343,6 +457,7 @@ void configure_tma(FdtdPlan* p) {
     cudaGetLastError();
     if (occ <= 0 || threads > 256 || threads < 32) return;
     const Split sp = split_boxes(p);
+    configure_zshell(p, sp, optin);
     const Box core = sp.split ? sp.core : Box{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
     const int cx = core.hi[0] - core.lo[0], cy = core.hi[1] - core.lo[1], cz = core.hi[2] - core.lo[2];
     const long long tiles = (long long)((cz + tz - 1) / tz) * ((cy + ty - 1) / ty);
@@ -365,6 +480,7 @@ void configure_tma(FdtdPlan* p) {
 extern "C" {
 
 int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
+    NvtxRange nvtx_range("fdtd_plan_create");
     if (!desc || !out) return FDTD_EINVAL;
     *out = nullptr;
     std::string why;
@@ -436,7 +552,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         for (int q = 0; q < 4; ++q) o_rec[q] = ar.take(4 * tbl);
     p->dmem_bytes = ar.off;
 
-    cudaError_t e = cudaMalloc(&p->dmem, p->dmem_bytes);
+    cudaError_t e = dev_alloc(reinterpret_cast<void**>(&p->dmem), p->dmem_bytes);
     if (e != cudaSuccess) {
         delete p;
         fprintf(stderr, "fdtd_plan_create: cudaMalloc(%zu) failed: %s\n", ar.off, cudaGetErrorString(e));
@@ -567,8 +683,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
 
 void fdtd_plan_destroy(FdtdPlan* p) {
     if (!p) return;
-    if (p->gexec) cudaGraphExecDestroy(p->gexec);
-    if (p->graph) cudaGraphDestroy(p->graph);
+    drop_graphs(p);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
     cudaFree(p->dmem);
     cudaFree(p->amem);
@@ -602,12 +717,13 @@ bool make_map(CUtensorMap* m, const float* base, int ncomp, const Geo& g, int bz
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Launch of a TMA-pipelined half-step; false when a tensor map cannot be built (the caller
-// then uses the register-queue kernel).
-template <bool REV, bool HSIDE>
+// Launch of a TMA-pipelined half-step over the core box, or (ZP) over the z-slab shell boxes
+// with their CPML terms; false when a tensor map cannot be built (the caller then uses the
+// register-queue kernel).
+template <bool REV, bool HSIDE, bool ZP = false>
 bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     const Geo& g = p->g;
-    const int tz = p->tma_tz, ty = p->tma_ty;
+    const int tz = ZP ? p->zs_tz : p->tma_tz, ty = ZP ? p->zs_ty : p->tma_ty;
     const int nm = a.mat ? a.n_mat : 0, nsig = a.sig ? a.n_sig : 0;
     // the staged phasor tile of the first fused detector (forward H step only)
     int nd = 0;
@@ -627,6 +743,14 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
             nd = planes;
     }
     TmaCfg c = tma_cfg(tz, ty, p->tma_ns, HSIDE, nm, nsig, p->d_err, nd);
+    if (ZP) {
+        c.zsides = p->zs_sides;
+        c.zlo = p->zs_lo;
+        c.zhi = p->zs_hi;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (g_inject_expiry.load() > 0 && cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+        c.expire = take_injected(g_inject_expiry) ? 1 : 0;  // direct launches only: a graph keeps no injected node
     if (nd)
         for (int x = 0; x < 3; ++x) c.dlo[x] = a.fuse[0].lo[x];
     CUtensorMap mF, mU, mM, mS;
@@ -637,12 +761,13 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     if (nm && !make_map(&mM, a.mat, nm, g, tz, ty, nm)) return false;
     if (nsig && !make_map(&mS, a.sig, nsig, g, tz, ty, nsig)) return false;
     UpdArgs aa = a;
-    aa.chunk = HSIDE ? p->tma_chunk : p->tma_chunk_e;
+    aa.chunk = ZP ? (HSIDE ? p->zs_chunk : p->zs_chunk_e) : (HSIDE ? p->tma_chunk : p->tma_chunk_e);
     const int bx = aa.hi[0] - aa.lo[0], by = aa.hi[1] - aa.lo[1], bz = aa.hi[2] - aa.lo[2];
-    const dim3 grid((bz + tz - 1) / tz, (by + ty - 1) / ty, (bx + aa.chunk - 1) / aa.chunk);
+    const int gz = ZP ? (p->zs_sides & 1) + (p->zs_sides >> 1) : (bz + tz - 1) / tz;
+    const dim3 grid(gz, (by + ty - 1) / ty, (bx + aa.chunk - 1) / aa.chunk);
     const dim3 block(ty * tz / 2);
-    if (HSIDE) k_tma_H<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
-    else k_tma_E<REV><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
+    if (HSIDE) k_tma_H<REV, ZP><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
+    else k_tma_E<REV, ZP><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
     return true;
 }
 
@@ -731,17 +856,38 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
     for (int x = 0; x < 3; ++x) { ac.lo[x] = sp.core.lo[x]; ac.hi[x] = sp.core.hi[x]; }
     if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
     if (mid) cudaEventRecord(mid, st);
+    // the z-slab boxes (short z rows: the CPML cells with the worst coalescing) through the
+    // TMA pipeline with their z terms, when the per-axis slab table holds
+    Box shell[6];
+    int n_shell = 0;
+    const bool zs = p->use_tma && p->zs_ok && p->zs_on && a.axt == 2 && launch_tma<REV, HSIDE, true>(p, ac, st);
+    for (int q = 0; q < sp.n_shell; ++q) {
+        const Box& b = sp.shell[q];
+        const bool zbox = b.lo[0] == sp.core.lo[0] && b.hi[0] == sp.core.hi[0] && b.lo[1] == sp.core.lo[1] &&
+                          b.hi[1] == sp.core.hi[1];
+        if (!(zs && zbox)) shell[n_shell++] = b;
+    }
     int chunks[6];
-    for (int q = 0; q < sp.n_shell; ++q) chunks[q] = p->shell_chunk;
+    for (int q = 0; q < n_shell; ++q) chunks[q] = p->shell_chunk;
     // the shells run one z cell per thread by default: fewer registers per thread, more
     // warps in flight for their latency-bound CPML and phasor loads (measured 14% (H) and
     // 24% (E) faster than two)
-    launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st, p->shell_vec);
+    launch_plain_boxes<REV, HSIDE, true>(p, a, shell, chunks, n_shell, st, p->shell_vec);
 }
 
 int half_step_launches(const FdtdPlan* p) {
     const Split sp = split_boxes(p);
-    return sp.split ? 1 + (sp.n_shell > 0) : 1;
+    if (!sp.split) return 1;
+    int rest = sp.n_shell;
+    const bool zs = p->use_tma && p->zs_ok && p->zs_on;
+    if (zs)
+        for (int q = 0; q < sp.n_shell; ++q) {
+            const Box& b = sp.shell[q];
+            if (b.lo[0] == sp.core.lo[0] && b.hi[0] == sp.core.hi[0] && b.lo[1] == sp.core.lo[1] &&
+                b.hi[1] == sp.core.hi[1])
+                --rest;
+        }
+    return 1 + (zs ? 1 : 0) + (rest > 0 ? 1 : 0);
 }
 
 template <bool REV>
@@ -902,6 +1048,7 @@ int32_t fdtd_launches_per_step(const FdtdPlan* p) {
 }
 
 int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, int32_t flags, void* stream) {
+    NvtxRange nvtx_range("fdtd_forward");
     if (!p) return FDTD_EINVAL;
     if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
         return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_forward)");
@@ -909,13 +1056,13 @@ int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps,
     if (n_steps < 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)
         return fail(p, FDTD_EINVAL, "time steps out of the range covered by the plan's tables");
     if (p->d.record_interfaces && p->d.n_slabs && !b->recording) return fail(p, FDTD_EINVAL, "recording buffer required");
-    if (n_steps == 0) return FDTD_OK;
+    if (n_steps == 0 && !(flags & FDTD_FWD_CHECK_FINITE)) return FDTD_OK;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
+    if (n_steps > 0) k_set_step<<<1, 1, 0, st>>>(p->d_t, t0);
     float* Hcur = b->H;
     float* Hnext = p->need_hprev ? p->h_twin : b->H;
     int done = 0;
-    const bool use_graph = (flags & 1) != 0;
+    const bool use_graph = (flags & FDTD_FWD_GRAPH) != 0;
     const int unit = p->need_hprev ? 2 : 1;
     if (use_graph && n_steps >= 8) {
         int G = std::min(n_steps, 64);
@@ -957,6 +1104,11 @@ int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps,
         cudaError_t e = cudaMemcpyAsync(b->H, Hcur, sizeof(float) * 3 * p->g.N, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return cuda_fail(p, e, "cudaMemcpyAsync");
     }
+    if (flags & FDTD_FWD_CHECK_FINITE) {
+        const int blocks = std::max(1, std::min(p->sm_count * 8, (int)((3 * p->g.N + 255) / 256)));
+        k_check_finite<<<blocks, 256, 0, st>>>(b->E, 3 * p->g.N, p->d_err);
+        k_check_finite<<<blocks, 256, 0, st>>>(b->H, 3 * p->g.N, p->d_err);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_forward launch");
     return FDTD_OK;
@@ -967,6 +1119,7 @@ int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps,
 // re-impose the recorded interfaces of step t, reverse H (sources subtracted first,
 // psi frozen), reverse E.
 int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_steps, void* stream) {
+    NvtxRange nvtx_range("fdtd_reverse");
     if (!p) return FDTD_EINVAL;
     if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
         return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_reverse)");
@@ -1093,9 +1246,7 @@ extern "C" int fdtd_plan_tune(FdtdPlan* p, int32_t chunk, int32_t vec) {
     if (chunk != p->chunk || vec != p->vec) {
         p->chunk = chunk;
         p->vec = vec;
-        if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
-        if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
-        p->gsteps = 0;
+        drop_graphs(p);
     }
     return FDTD_OK;
 }
@@ -1109,9 +1260,7 @@ extern "C" int fdtd_plan_tune_shell(FdtdPlan* p, int32_t chunk, int32_t vec) {
     if (chunk != p->shell_chunk || vec != p->shell_vec) {
         p->shell_chunk = chunk;
         p->shell_vec = vec;
-        if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
-        if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
-        p->gsteps = 0;
+        drop_graphs(p);
     }
     return FDTD_OK;
 }
@@ -1140,13 +1289,29 @@ extern "C" int fdtd_plan_tune_tma(FdtdPlan* p, int32_t enable, int32_t tz, int32
     } else {
         p->use_tma = false;
     }
-    if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
-    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
-    p->gsteps = 0;
+    drop_graphs(p);
     return FDTD_OK;
 }
 
 extern "C" int32_t fdtd_plan_uses_tma(const FdtdPlan* p) { return p && p->use_tma ? 1 : 0; }
+
+extern "C" int fdtd_plan_tune_zshell(FdtdPlan* p, int32_t enable, int32_t ty, int32_t chunk) {
+    if (!p) return FDTD_EINVAL;
+    if (ty < 0 || ty > 256 || chunk < 0) return fail(p, FDTD_EINVAL, "invalid z-shell tile");
+    p->zs_on = enable != 0;
+    p->zs_ty = ty > 0 ? ty : 16;
+    configure_tma(p);
+    if (enable && !(p->use_tma && p->zs_ok)) {
+        p->zs_on = false;
+        return fail(p, FDTD_EINVAL, "the z-slab shell boxes cannot run on the TMA kernels here (no TMA core, "
+                                    "no z slab, a z box thicker than 64 cells or a tile that does not fit)");
+    }
+    if (chunk > 0) p->zs_chunk = p->zs_chunk_e = std::min(chunk, p->g.nx);
+    drop_graphs(p);
+    return FDTD_OK;
+}
+
+extern "C" int32_t fdtd_plan_uses_zshell(const FdtdPlan* p) { return p && p->use_tma && p->zs_ok && p->zs_on ? 1 : 0; }
 
 extern "C" int fdtd_plan_status(FdtdPlan* p) {
     if (!p) return FDTD_EINVAL;
@@ -1155,8 +1320,19 @@ extern "C" int fdtd_plan_status(FdtdPlan* p) {
     if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_plan_status");
     if (h) {
         cudaMemset(p->d_err, 0, sizeof(int));
+        if (h == FDTD_ENONFINITE)
+            return fail(p, h, "a field holds a NaN or an infinity after the steps (check the materials, the sources "
+                              "and the Courant number)");
         return fail(p, h, "a pipeline wait in a kernel ran out (the step's results are invalid)");
     }
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_debug_inject(int32_t kind, int32_t count) {
+    if (count < 0) return FDTD_EINVAL;
+    if (kind == FDTD_INJECT_ALLOC) g_inject_alloc.store(count);
+    else if (kind == FDTD_INJECT_WAIT_EXPIRY) g_inject_expiry.store(count);
+    else return FDTD_EINVAL;
     return FDTD_OK;
 }
 #include "fdtd_noalloc.cuh"

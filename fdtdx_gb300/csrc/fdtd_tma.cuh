@@ -33,7 +33,79 @@ struct TmaCfg {
     int off_U, off_M, off_S, off_D, stage_floats;
     uint32_t stage_bytes;  // bytes the TMA loads of one stage deliver
     int* err;
+    int expire;            // test hook: take the bounded-wait error exit before issuing any copy
+    // z-slab shell launches (ZP kernels): which z boxes (bit 0: low, bit 1: high; blockIdx.x
+    // picks one), the low box's end and the high box's start
+    int zsides, zlo, zhi;
 };
+
+// ---------------------------------------------------------------------------------
+// CPML z-slab terms inside the TMA half-steps (ZP kernels, launched over the two z-slab
+// shell boxes of a split grid, whose cells lie in no x or y slab): a thread's two cells
+// have a fixed layer of the slab along the whole x-march, so the slab coefficients are
+// read once and the psi offset grows by ny * L per plane.  psi is read with plain loads
+// issued before the plane's pipeline wait.  Same arithmetic as ax_term on axis 2
+// (fdtdx/core/physics/curl.py:284-308, perfectly_matched_layer.py:138-190).
+// ---------------------------------------------------------------------------------
+struct ZCol {
+    int o[2];              // psi offset of each cell at plane 0 (-1: the cell has no z term)
+    int stride;            // psi floats per x plane
+    float ca[2], cb[2], km[2];
+    int kone;
+    float* p1;
+    float* p2;
+};
+
+template <bool HSIDE>
+__device__ __forceinline__ void zcol_init(const UpdArgs& a, int side, int j, int k0, bool valid, ZCol& z) {
+    const int L = side ? a.axs[2][1].L : a.axs[2][0].L;
+    const int lo = side ? a.axs[2][1].lo : a.axs[2][0].lo;
+    const float* co = (side ? a.axs[2][1].coef : a.axs[2][0].coef) + (HSIDE ? 3 * L : 0);
+    z.kone = side ? a.axs[2][1].kappa_one : a.axs[2][0].kappa_one;
+    z.p1 = side ? a.axp[2][1][0] : a.axp[2][0][0];
+    z.p2 = side ? a.axp[2][1][1] : a.axp[2][0][1];
+    z.stride = a.g.ny * L;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int l = k0 + e - lo;
+        z.o[e] = -1;
+        z.ca[e] = z.cb[e] = z.km[e] = 0.f;
+        if (valid && L > 0 && (unsigned)l < (unsigned)L) {
+            z.o[e] = j * L + l;
+            z.ca[e] = __ldg(co + l);
+            z.cb[e] = __ldg(co + L + l);
+            z.km[e] = z.kone ? 0.f : __ldg(co + 2 * L + l) - 1.f;
+        }
+    }
+}
+
+// psi pair of cell e at plane i (zero without a term), loaded ahead of the plane's wait.
+__device__ __forceinline__ float2 zcol_load(const ZCol& z, int e, int i) {
+    if (z.o[e] < 0) return make_float2(0.f, 0.f);
+    const int o = z.o[e] + i * z.stride;
+    return make_float2(z.p1[o], z.p2[o]);
+}
+
+// The z term of cell e: d1 = d_z F_y, d2 = d_z F_x; curl_x -= c1, curl_y += c2.
+template <bool REV>
+__device__ __forceinline__ void zcol_apply(const ZCol& z, int e, int i, float2 pv, float d1, float d2, float cu[3]) {
+    if (z.o[e] < 0) return;
+    float p1 = pv.x, p2 = pv.y;
+    if (!REV) {
+        p1 = z.cb[e] * p1 + z.ca[e] * d1;
+        p2 = z.cb[e] * p2 + z.ca[e] * d2;
+        const int o = z.o[e] + i * z.stride;
+        z.p1[o] = p1;
+        z.p2[o] = p2;
+    }
+    float c1 = p1, c2 = p2;
+    if (!z.kone) {
+        c1 = z.km[e] * d1 + p1;
+        c2 = z.km[e] * d2 + p2;
+    }
+    cu[0] -= c1;
+    cu[1] += c2;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -92,7 +164,7 @@ __device__ __forceinline__ void drain(uint64_t* bar, int ns, int from, int to) {
 //   E, inv_eps, sigma_E on the tile
 // Loads cover planes i0-1 .. i1-1; the first only seeds H(i-1) of each column.
 // ---------------------------------------------------------------------------------
-template <bool REV>
+template <bool REV, bool ZP = false>
 __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -105,12 +177,21 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    // ZP: blockIdx.x picks the z-slab box (low box [0, zlo), high box [zhi, nz))
+    const int zside = ZP ? (tc.zsides == 3 ? (int)blockIdx.x : tc.zsides >> 1) : 0;
+    const int kt = ZP ? (zside ? tc.zhi : 0) : a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int kend = ZP ? (zside ? g.nz : tc.zlo) : a.hi[2];
     const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < a.hi[2] && j < a.hi[1];
+    const bool valid = k0 < kend && j < a.hi[1];
     const long long N = g.N;
+    ZCol zc{};
+    if (ZP) zcol_init<false>(a, zside, j, k0, valid, zc);
+    if (tc.expire) {  // injected wait expiry: the error path, with no copy issued
+        if (tid == 0) atomicExch(tc.err, FDTD_ETIMEOUT);
+        return;
+    }
 
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
@@ -133,9 +214,14 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
     float Hy_m[2] = {0.f, 0.f}, Hz_m[2] = {0.f, 0.f};
     for (int p = 0; p < P; ++p) {
         const int s = p % NS;
+        const int i = i0 - 1 + p;
+        float2 zv[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (ZP && p > 0) {
+            zv[0] = zcol_load(zc, 0, i);
+            zv[1] = zcol_load(zc, 1, i);
+        }
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
         const float* F = sm + s * tc.stage_floats;
-        const int i = i0 - 1 + p;
         if (ok && p == 0) {
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
@@ -162,7 +248,8 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 const float d[6] = {Hz - Hz_jm, Hy - Hy_km, Hx - Hx_km, Hz - Hz_m[e], Hy - Hy_m[e], Hx - Hx_jm};
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
-                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+                if (ZP) zcol_apply<REV>(zc, e, i, zv[e], d[1], d[2], cu);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -205,7 +292,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 //   H, inv_mu, sigma_H on the tile
 // Loads cover planes i0 .. i1; plane i is computed once the loads of i and i+1 landed.
 // ---------------------------------------------------------------------------------
-template <bool REV>
+template <bool REV, bool ZP = false>
 __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -219,12 +306,16 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int zside = ZP ? (tc.zsides == 3 ? (int)blockIdx.x : tc.zsides >> 1) : 0;
+    const int kt = ZP ? (zside ? tc.zhi : 0) : a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
+    const int kend = ZP ? (zside ? g.nz : tc.zlo) : a.hi[2];
     const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < a.hi[2] && j < a.hi[1];
+    const bool valid = k0 < kend && j < a.hi[1];
     const long long N = g.N;
+    ZCol zc{};
+    if (ZP) zcol_init<true>(a, zside, j, k0, valid, zc);
 
     int slot[kMaxFuse];
     float2 w[kMaxFuse][kMaxFuseFreq];
@@ -243,6 +334,10 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                           : make_float2(0.f, 0.f);
     }
 
+    if (tc.expire) {  // injected wait expiry: the error path, with no copy issued
+        if (tid == 0) atomicExch(tc.err, FDTD_ETIMEOUT);
+        return;
+    }
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
         mbar_fence_init();
@@ -271,8 +366,13 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
     }
     for (int p = 0; p + 1 < P; ++p) {
         const int s = p % NS, s1 = (p + 1) % NS;
-        ok = ok && mbar_wait_bounded(&bar[s1], (uint32_t)(((p + 1) / NS) & 1));
         const int i = i0 + p;
+        float2 zv[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (ZP) {
+            zv[0] = zcol_load(zc, 0, i);
+            zv[1] = zcol_load(zc, 1, i);
+        }
+        ok = ok && mbar_wait_bounded(&bar[s1], (uint32_t)(((p + 1) / NS) & 1));
         if (ok && valid) {
             const float* E = sm + s * tc.stage_floats;
             const float* E1 = sm + s1 * tc.stage_floats;
@@ -299,7 +399,8 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ez_ip = E1[(2 * EY + r0) * EZ + kk];
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
-                const float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+                float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
+                if (ZP) zcol_apply<REV>(zc, e, i, zv[e], d[1], d[2], cu);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];

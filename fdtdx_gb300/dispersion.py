@@ -111,11 +111,13 @@ class DispersionModel:
         return self.susceptibility_axes(omega)[0]
 
 
-def compute_pole_coefficients_per_axis(poles, dt: float) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-    """(c1, c2, c3), each (len(poles), 3), of the ADE recurrence (dispersion.py:789-857); a
-    coupled axis needs omega_0 dt < 2 for the recurrence to stay stable."""
+def compute_pole_coefficients_per_axis(poles, dt: float) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+    """(c1, c2, c3, c4), each (len(poles), 3), of the ADE recurrence (dispersion.py:789-857),
+    the reference's four arrays; c4 (the term of a pole with a numerator coefficient b) is
+    zero for the Lorentz and Drude poles here.  A coupled axis needs omega_0 dt < 2 for the
+    recurrence to stay stable."""
     n = len(poles)
-    c1, c2, c3 = (np.zeros((n, 3)) for _ in range(3))
+    c1, c2, c3, c4 = (np.zeros((n, 3)) for _ in range(4))
     for i, p in enumerate(poles):
         w0, g, k = p.omega_0_axes, p.gamma_axes, p.coupling_sq_axes
         for ax in range(3):
@@ -125,4 +127,4 @@ def compute_pole_coefficients_per_axis(poles, dt: float) -> tuple[np.ndarray, np
             c1[i, ax] = (2.0 - w0[ax] ** 2 * dt**2) / d
             c2[i, ax] = -(1.0 - 0.5 * g[ax] * dt) / d
             c3[i, ax] = k[ax] * dt**2 / d
-    return c1, c2, c3
+    return c1, c2, c3, c4

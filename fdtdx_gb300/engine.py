@@ -510,6 +510,15 @@ class Scene:
     def uses_tma(self) -> bool:
         return bool(N.load().fdtd_plan_uses_tma(self.plan))
 
+    def tune_zshell(self, enable: bool = True, ty: int = 0, chunk: int = 0) -> None:
+        """The z-slab CPML shell boxes on the TMA kernels (enable) or the register-queue shell."""
+        N.check(N.load().fdtd_plan_tune_zshell(self.plan, 1 if enable else 0, int(ty), int(chunk)), self.plan,
+                "fdtd_plan_tune_zshell")
+
+    @property
+    def uses_zshell(self) -> bool:
+        return bool(N.load().fdtd_plan_uses_zshell(self.plan))
+
     def status(self) -> None:
         """Raise if a kernel reported an error (a bounded pipeline wait that ran out)."""
         N.check(N.load().fdtd_plan_status(self.plan), self.plan, "fdtd_plan_status")
@@ -537,10 +546,15 @@ class Scene:
             b.recording = N.ptr(arrays.recording_state.data["interfaces"])
         return b
 
-    def forward(self, arrays: ArrayContainer, t0: int, n_steps: int, graph: bool = True, stream=None) -> None:
+    def forward(self, arrays: ArrayContainer, t0: int, n_steps: int, graph: bool = True, stream=None,
+                check_finite: bool = False) -> None:
+        """Forward steps t0 .. t0+n_steps-1 in place.  ``check_finite`` scans E and H once after
+        the last step; ``status()`` then raises ``NativeError`` (FDTD_ENONFINITE) when either
+        holds a NaN or an infinity."""
         st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
         b = self.buffers(arrays)
-        rc = N.load().fdtd_forward(self.plan, C.byref(b), int(t0), int(n_steps), 1 if graph else 0,
+        flags = (N.FWD_GRAPH if graph else 0) | (N.FWD_CHECK_FINITE if check_finite else 0)
+        rc = N.load().fdtd_forward(self.plan, C.byref(b), int(t0), int(n_steps), flags,
                                    C.c_void_p(st.cuda_stream))
         N.check(rc, self.plan, "fdtd_forward")
 

@@ -7,6 +7,7 @@ the Python side only builds the plan once per scene and hands over buffers.
 
 from __future__ import annotations
 
+import warnings
 from typing import Callable
 
 import torch
@@ -54,6 +55,20 @@ def get_scene(objects: ObjectContainer, arrays: ArrayContainer, config: Simulati
     return scene
 
 
+def finite_status(scene: Scene) -> None:
+    """Reads the plan's error word after a run that ended with a finite check.  A NaN or an
+    infinity in the fields is reported with a ``RuntimeWarning`` and the arrays are still
+    returned, as the reference returns a diverged run's arrays; any other error raises."""
+    from fdtdx_gb300 import _native as N
+
+    try:
+        scene.status()
+    except N.NativeError as e:
+        if e.code != N.ENONFINITE:
+            raise
+        warnings.warn(f"the FDTD run diverged: {e}", RuntimeWarning, stacklevel=3)
+
+
 def _materials_detached(arrays: ArrayContainer) -> ArrayContainer:
     mu = arrays.inv_permeabilities
     return arrays.aset("inv_permittivities", arrays.inv_permittivities.detach().contiguous()).aset(
@@ -79,8 +94,8 @@ def checkpointed_fdtd(
     arrays = _materials_detached(arrays).reset()
     scene = get_scene(objects, arrays, config, record_interfaces=config.invertible_optimization)
     T = config.time_steps_total
-    scene.forward(arrays, 0, T)
-    scene.status()
+    scene.forward(arrays, 0, T, check_finite=True)
+    finite_status(scene)
     if progress_callback is not None:
         progress_callback(T, T)
     return T, arrays

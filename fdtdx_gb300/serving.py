@@ -10,8 +10,12 @@ path for a stream of independent simulation requests:
 * every admitted job keeps its state on the device until it completes;
 * continuous batching: all jobs in their forward phase advance together through one
   ``fdtd_batch_forward`` call per chunk (the batch is rebuilt whenever a job joins or
-  leaves), while gradient jobs in their adjoint phase run ``fdtd_adjoint`` chunks on a
-  second stream, so the two kinds of work overlap on the GPU;
+  leaves), while gradient jobs in their adjoint phase run ``fdtd_adjoint`` chunks on
+  adjoint lanes (streams of their own), so the kinds of work overlap on the GPU; every lane
+  gets its next chunk when its CUDA event says the last one finished, with no device-wide
+  wait, and admitted jobs are placed by a worker thread on a side stream meanwhile;
+* cancellation of queued and running jobs, host snapshots of a running job's state, and
+  per-job divergence detection (a non-finite job fails alone);
 * per-job latency (arrival to completion) and aggregate throughput are recorded.
 
 The scheduling logic (``Scheduler``) is host-only and unit-tested without a GPU.
@@ -62,7 +66,7 @@ class Job:
     arrays: ArrayContainer | None = None
     config: SimulationConfig | None = None
     detectors: dict | None = None               # gradient jobs: the final detector states
-    phase: str = "queued"                       # queued, forward, adjoint, done
+    phase: str = "queued"                       # queued, forward, adjoint, done, cancelled, failed
     t_fwd: int = 0                              # forward steps done
     t_adj: int = 0                              # adjoint steps left
     bypassed: int = 0
@@ -74,6 +78,9 @@ class Job:
     scene: object = None
     state: ArrayContainer | None = None
     lam: dict | None = None
+    cancel_requested: bool = False
+    error: str | None = None                    # why a failed job failed
+    inflight: int = 0                           # steps of a chunk issued and not yet accounted
 
     @property
     def cells(self) -> int:
@@ -176,12 +183,23 @@ class Scheduler:
         job.phase = "adjoint"
         job.t_adj = job.steps + 1  # the reference's backward loop runs t = T-1 .. -1
 
-    def complete(self, job: Job, now: float) -> None:
-        job.phase = "done"
+    def complete(self, job: Job, now: float, phase: str = "done") -> None:
+        """A job leaves the active set ("done", "cancelled" or "failed") and frees its budget."""
+        job.phase = phase
         job.t_done = now
         self.active.remove(job)
         self.used -= job.footprint
         self.done.append(job)
+
+    def withdraw(self, job: Job, now: float) -> bool:
+        """Removes a queued job (cancellation before admission); False when it is not queued."""
+        if job not in self.queue:
+            return False
+        self.queue.remove(job)
+        job.phase = "cancelled"
+        job.t_done = now
+        self.done.append(job)
+        return True
 
     def idle(self) -> bool:
         return not self.queue and not self.active
@@ -191,8 +209,9 @@ class Server:
     """The GPU serving loop over a list of timed jobs (``Job.arrival`` in seconds)."""
 
     def __init__(self, budget_bytes: int = 160 * 10**9, max_slots: int = 64, target_chunk_s: float = 0.05,
-                 autotune: bool = True):
+                 autotune: bool = True, adjoint_lanes: int = 4):
         self.sched = Scheduler(budget_bytes, max_slots)
+        self.adjoint_lanes = max(1, int(adjoint_lanes))
         self.target = float(target_chunk_s)
         self.autotune = autotune
         self._tile = None
@@ -205,15 +224,20 @@ class Server:
         self.makespan = 0.0
 
     # ---- job lifecycle on the device
-    def _prepare(self, job: Job) -> None:
-        """Places an admitted job on the device and builds its plan."""
+    def _prepare(self, job: Job, stream=None) -> None:
+        """Places an admitted job on the device and builds its plan (run by the placement
+        worker, its uploads on ``stream``, which it drains before the job is handed over)."""
         from fdtdx_gb300.engine import Scene
         from fdtdx_gb300.fdtd import _materials_detached
 
         rec = job.kind == "gradient"
-        job.objects, job.arrays, job.config = job.build("cuda", rec)
-        job.state = _materials_detached(job.arrays).reset()
-        job.scene = Scene(job.objects, job.state, job.config, record_interfaces=rec)
+        st = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(st):
+            job.objects, job.arrays, job.config = job.build("cuda", rec)
+            job.state = _materials_detached(job.arrays).reset()
+            job.scene = Scene(job.objects, job.state, job.config, record_interfaces=rec)
+            job.scene.plan  # the plan's tables are built and uploaded here, off the loop thread
+        st.synchronize()
         job.steps = job.config.time_steps_total
 
     def _batch_for(self, jobs: list[Job]):
@@ -260,6 +284,49 @@ class Server:
         }
         self.sched.start_adjoint(job)
 
+    def cancel(self, job: Job) -> None:
+        """Cancels a job: one not yet arrived is dropped when it arrives, a queued one leaves the
+        queue, a running one stops at the next chunk boundary and releases its device state."""
+        job.cancel_requested = True
+
+    def snapshot(self, job: Job) -> dict:
+        """Host copy of a running job's device state: the step it holds, E, H and the detector
+        states (during the adjoint phase, the reconstructed state and its step).  Waits for
+        the job's chunk in flight, if any."""
+        if job.state is None:
+            raise ValueError(f"job {job.id} holds no device state (phase {job.phase})")
+        torch.cuda.synchronize()
+        st = job.state
+        t = job.t_fwd + job.inflight if job.phase == "forward" else job.t_adj - 1 - job.inflight
+        return {"t": t, "phase": job.phase, "E": st.fields.E.detach().cpu(), "H": st.fields.H.detach().cpu(),
+                "detectors": {n: {k: v.detach().cpu() for k, v in d.items()} for n, d in st.detector_states.items()}}
+
+    def _release(self, job: Job, now: float, phase: str, error: str | None = None) -> None:
+        """Ends a job without a result (cancelled or failed) and frees its device state."""
+        if self._batch is not None and job.id in self._members:
+            self._batch.close()  # it references the job's plan and buffers
+            self._batch = None
+            self._members = ()
+        if job.scene is not None:
+            job.scene.close()
+        job.scene = job.state = job.arrays = job.lam = None
+        job.error = error
+        self.sched.complete(job, now, phase)
+
+    def _diverged(self, job: Job) -> str | None:
+        """The native finite check of the job's fields (E and H read once): the error message
+        when they hold a NaN or an infinity, else None."""
+        from fdtdx_gb300 import _native as N
+
+        job.scene.forward(job.state, job.t_fwd, 0, graph=False, check_finite=True)
+        try:
+            job.scene.status()
+        except N.NativeError as e:
+            if e.code == N.ENONFINITE:
+                return str(e)
+            raise
+        return None
+
     def _finish(self, job: Job, now: float) -> None:
         job.scene.status()
         if job.kind == "gradient":
@@ -276,95 +343,187 @@ class Server:
             torch.cuda.empty_cache()  # hand large blocks back so the next large job can be placed
 
     # ---- the loop
-    def run(self, jobs: list[Job], realtime: bool = True) -> list[Job]:
-        """Serve ``jobs`` (arrivals replayed in real time when ``realtime``); returns them done."""
+    def run(self, jobs: list[Job], realtime: bool = True,
+            on_chunk: Callable[["Server", float], None] | None = None) -> list[Job]:
+        """Serve ``jobs`` (arrivals replayed in real time when ``realtime``, else idle gaps
+        before an arrival are skipped); returns them done, cancelled or failed.
+
+        The loop never waits for the whole device: the forward batch and every adjoint lane are
+        polled through their CUDA events, and each gets its next chunk as soon as its last one
+        has finished.  Admitted jobs are placed and their plans built by a worker thread on a
+        side stream while the device runs the others.  ``on_chunk(server, now)`` runs after
+        every finished chunk; ``cancel`` and ``snapshot`` may be called there.  A job whose
+        fields turn non-finite fails alone (phase "failed", ``error`` set)."""
+        import concurrent.futures as cf
+
         dev = torch.device("cuda")
         s_fwd = torch.cuda.Stream(dev)
-        s_adj = torch.cuda.Stream(dev)
+        s_prep = torch.cuda.Stream(dev)
+        lanes = [torch.cuda.Stream(dev) for _ in range(self.adjoint_lanes)]
         for i, j in enumerate(jobs):
             j.id = i
             if not j.footprint:
                 estimate_footprint(j)
         pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
-        t0 = time.perf_counter()
-        clock = (lambda: time.perf_counter() - t0) if realtime else None
-        vnow = 0.0
-        while pending or not self.sched.idle():
-            now = clock() if realtime else vnow
-            while pending and pending[0].arrival <= now:
-                self.sched.arrive(pending.popleft())
-            for job in self.sched.admit(now):
-                self._prepare(job)
-            fw, adj = self.sched.forward_jobs(), self.sched.adjoint_jobs()
-            if not fw and not adj:
-                if pending:
-                    if realtime:
-                        time.sleep(max(0.0, min(0.01, pending[0].arrival - now)))
-                    else:
-                        vnow = max(vnow, pending[0].arrival)
-                continue
-            # one chunk of forward batch work and one of each adjoint job, overlapping
-            ev = []
-            n_f = 0
-            if fw:
-                cells = sum(j.cells for j in fw)
-                cap = max(8, min(1000, int(self.target * self.rate / cells)))
-                n_f = self.sched.forward_chunk(cap)
-                b, fresh = self._batch_for(fw)
-                with torch.cuda.stream(s_fwd):
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record(s_fwd)
-                    b.advance(n_f, t0=[j.t_fwd for j in fw] if fresh else None, graph=True,
-                              autotune=self.autotune and self._tile is None, stream=s_fwd)
-                    e1.record(s_fwd)
-                    ev.append(("f", e0, e1, cells * n_f))
-            n_adj = {}
-            for j in adj:
-                n = min(j.t_adj, max(8, int(self.target * self.adj_rate / j.cells)))
-                n_adj[j.id] = n
-                with torch.cuda.stream(s_adj):
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record(s_adj)
-                    j.scene.adjoint(j.state, j.lam, j.t_adj - 1, n, stream=s_adj)
-                    e1.record(s_adj)
-                    ev.append(("a", e0, e1, j.cells * n))
-            s_fwd.synchronize()
-            s_adj.synchronize()
-            for kind, e0, e1, work in ev:
-                ms = e0.elapsed_time(e1)
-                if ms > 0:
-                    r = work / (ms * 1e-3)
-                    if kind == "f":
-                        self.rate = 0.7 * self.rate + 0.3 * r
-                    else:
-                        self.adj_rate = 0.7 * self.adj_rate + 0.3 * r
-            if fw and self._tile is None and self.autotune:
-                t = self._batch.tuning()
-                self._tile = (t["chunk_scale"][0], t["chunk_scale"][1], t["shell_chunk"], t["blocks_per_sm"], t["mode"])
-            if not realtime:
-                vnow += max([e0.elapsed_time(e1) * 1e-3 for _k, e0, e1, _w in ev] + [0.0])
-            now = clock() if realtime else vnow
-            for j in fw:
-                self.sched.advanced(j, n_f)
-                self.forward_cell_updates += j.cells * n_f
-                if self.sched.forward_finished(j):
-                    if j.kind == "gradient":
-                        self._start_adjoint(j)
-                    else:
-                        self._finish(j, now)
-            for j in adj:
-                n = n_adj[j.id]
-                j.t_adj -= n
-                self.adjoint_cell_updates += j.cells * n
-                if j.t_adj <= 0:
-                    self._finish(j, now)
-        if self._batch is not None:
-            self._batch.close()
-            self._batch = None
-        self.makespan = (time.perf_counter() - t0) if realtime else vnow
+        t_start = time.perf_counter()
+        skipped = [0.0]  # idle time jumped over when not replaying arrivals in real time
+
+        def clock() -> float:
+            return time.perf_counter() - t_start + skipped[0]
+
+        pool = cf.ThreadPoolExecutor(max_workers=1, thread_name_prefix="fdtd-serve-prep")
+        preparing: dict[int, cf.Future] = {}
+        ready: set[int] = set()
+        fwd = None              # in-flight forward chunk: (start event, end event, jobs, steps)
+        adj: dict[int, tuple] = {}  # job id -> (lane, start event, end event, steps)
+        lane_of: dict[int, int] = {}
+        try:
+            while pending or not self.sched.idle():
+                progressed = False
+                now = clock()
+                while pending and pending[0].arrival <= now:
+                    job = pending.popleft()
+                    if job.cancel_requested:
+                        job.phase, job.t_done = "cancelled", now
+                        self.sched.done.append(job)
+                        continue
+                    self.sched.arrive(job)
+                for job in list(self.sched.queue):
+                    if job.cancel_requested:
+                        self.sched.withdraw(job, now)
+                for job in list(self.sched.active):
+                    busy = job.id in adj or job.id in preparing or (fwd is not None and job in fwd[2])
+                    if job.cancel_requested and not busy:
+                        ready.discard(job.id)
+                        self._release(job, now, "cancelled")
+                for job in self.sched.admit(now):
+                    preparing[job.id] = pool.submit(self._prepare, job, s_prep)
+                for jid, fut in list(preparing.items()):
+                    if fut.done():
+                        fut.result()  # a placement error ends the loop with its exception
+                        del preparing[jid]
+                        ready.add(jid)
+                        progressed = True
+                # forward lane: account the finished chunk, issue the next one
+                if fwd is not None and fwd[1].query():
+                    self._forward_done(fwd, clock())
+                    fwd = None
+                    progressed = True
+                if fwd is None:
+                    fw = [j for j in self.sched.forward_jobs() if j.id in ready and not j.cancel_requested]
+                    if fw:
+                        fwd = self._issue_forward(fw, s_fwd)
+                        progressed = True
+                # adjoint lanes: one chunk per lane in flight
+                for job in list(self.sched.adjoint_jobs()):
+                    rec = adj.get(job.id)
+                    if rec is not None and rec[2].query():
+                        del adj[job.id]
+                        self._adjoint_done(job, rec, clock())
+                        progressed = True
+                busy_lanes = {rec[0] for rec in adj.values()}
+                for job in self.sched.adjoint_jobs():
+                    if job.id in adj:
+                        continue
+                    if job.cancel_requested:
+                        self._release(job, clock(), "cancelled")
+                        progressed = True
+                        continue
+                    lane = lane_of.setdefault(job.id, len(lane_of) % len(lanes))
+                    if lane in busy_lanes:
+                        continue
+                    adj[job.id] = self._issue_adjoint(job, lanes[lane], lane)
+                    busy_lanes.add(lane)
+                    progressed = True
+                if progressed:
+                    if on_chunk is not None:
+                        on_chunk(self, clock())
+                    continue
+                if fwd is not None or adj:
+                    time.sleep(2e-4)
+                elif preparing:
+                    cf.wait(list(preparing.values()), timeout=0.01, return_when=cf.FIRST_COMPLETED)
+                elif pending:
+                    wait = pending[0].arrival - clock()
+                    if wait > 0:
+                        if realtime:
+                            time.sleep(min(wait, 0.01))
+                        else:
+                            skipped[0] += wait
+        finally:
+            pool.shutdown(wait=True)
+            torch.cuda.synchronize()
+            if self._batch is not None:
+                self._batch.close()
+                self._batch = None
+                self._members = ()
+        self.makespan = clock()
         return jobs
+
+    def _issue_forward(self, fw: list[Job], stream) -> tuple:
+        """One chunk of the forward batch of ``fw`` on ``stream`` (about target_chunk_s of work)."""
+        cells = sum(j.cells for j in fw)
+        cap = max(8, min(1000, int(self.target * self.rate / cells)))
+        n = max(1, min(cap, min(j.steps - j.t_fwd for j in fw)))
+        b, fresh = self._batch_for(fw)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            b.advance(n, t0=[j.t_fwd for j in fw] if fresh else None, graph=True,
+                      autotune=self.autotune and self._tile is None, stream=stream)
+            e1.record(stream)
+        for j in fw:
+            j.inflight = n
+        return (e0, e1, fw, n)
+
+    def _forward_done(self, rec: tuple, now: float) -> None:
+        e0, e1, fw, n = rec
+        ms = e0.elapsed_time(e1)
+        cells = sum(j.cells for j in fw)
+        if ms > 0:
+            self.rate = 0.7 * self.rate + 0.3 * cells * n / (ms * 1e-3)
+        if self._tile is None and self.autotune and self._batch is not None:
+            t = self._batch.tuning()
+            self._tile = (t["chunk_scale"][0], t["chunk_scale"][1], t["shell_chunk"], t["blocks_per_sm"], t["mode"])
+        for j in fw:
+            j.inflight = 0
+            self.sched.advanced(j, n)
+            self.forward_cell_updates += j.cells * n
+            if j.cancel_requested:
+                self._release(j, now, "cancelled")
+            elif self.sched.forward_finished(j):
+                err = self._diverged(j)
+                if err is not None:
+                    self._release(j, now, "failed", err)
+                elif j.kind == "gradient":
+                    self._start_adjoint(j)
+                else:
+                    self._finish(j, now)
+
+    def _issue_adjoint(self, job: Job, stream, lane: int) -> tuple:
+        """One chunk of ``job``'s adjoint loop on its lane's stream."""
+        n = min(job.t_adj, max(8, int(self.target * self.adj_rate / job.cells)))
+        stream.wait_stream(torch.cuda.current_stream())  # its cotangents were zeroed there
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            job.scene.adjoint(job.state, job.lam, job.t_adj - 1, n, stream=stream)
+            e1.record(stream)
+        job.inflight = n
+        return (lane, e0, e1, n)
+
+    def _adjoint_done(self, job: Job, rec: tuple, now: float) -> None:
+        _lane, e0, e1, n = rec
+        ms = e0.elapsed_time(e1)
+        if ms > 0:
+            self.adj_rate = 0.7 * self.adj_rate + 0.3 * job.cells * n / (ms * 1e-3)
+        job.inflight = 0
+        job.t_adj -= n
+        self.adjoint_cell_updates += job.cells * n
+        if job.cancel_requested:
+            self._release(job, now, "cancelled")
+        elif job.t_adj <= 0:
+            self._finish(job, now)
 
 
 def run_one_at_a_time(jobs: list[Job], realtime: bool = True) -> list[Job]:

@@ -194,7 +194,13 @@ int64_t fdtd_plan_device_bytes(const FdtdPlan* plan);
  * serving admission.  Computed on the host; needs no GPU. */
 int64_t fdtd_footprint_bytes(const FdtdDesc* desc);
 
-/* Forward steps t0 .. t0+n_steps-1.  flags bit 0: use a CUDA graph for the loop. */
+/* Forward steps t0 .. t0+n_steps-1.  flags: FDTD_FWD_GRAPH replays the loop from a CUDA graph;
+ * FDTD_FWD_CHECK_FINITE scans E and H once after the last step (one read of both fields) and
+ * makes the next fdtd_plan_status return FDTD_ENONFINITE when either holds a NaN or an
+ * infinity (n_steps = 0 with this flag runs the check alone).  The reference raises no such
+ * error: a diverging JAX run returns the non-finite arrays (fdtdx/fdtd/fdtd.py:482-496). */
+#define FDTD_FWD_GRAPH 1
+#define FDTD_FWD_CHECK_FINITE 2
 int fdtd_forward(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t0, int32_t n_steps, int32_t flags, void* stream);
 
 /* Reverse steps: state at t_end is taken back to t_end - n_steps.  Uses the
@@ -230,9 +236,31 @@ int fdtd_plan_tune_shell(FdtdPlan* plan, int32_t chunk, int32_t vec);
 int fdtd_plan_tune_tma(FdtdPlan* plan, int32_t enable, int32_t tz, int32_t ty, int32_t stages, int32_t chunk);
 int32_t fdtd_plan_uses_tma(const FdtdPlan* plan);
 
-/* Reads and clears the kernels' error word (synchronises the device): FDTD_OK, or
- * FDTD_ETIMEOUT when a bounded pipeline wait ran out during an earlier call. */
+/* The two z-slab CPML shell boxes of a split grid (the slab cells whose z rows are shortest)
+ * run on the TMA kernels with their CPML z terms when the core does (the default), else on
+ * the register-queue shell kernel: enable = 1 / 0, `ty` rows of the (box z extent) x ty tile
+ * and `chunk` x planes per block (0 picks a default).  fdtd_plan_uses_zshell reports it. */
+int fdtd_plan_tune_zshell(FdtdPlan* plan, int32_t enable, int32_t ty, int32_t chunk);
+int32_t fdtd_plan_uses_zshell(const FdtdPlan* plan);
+
+/* Reads and clears the kernels' error word (synchronises the device): FDTD_OK,
+ * FDTD_ETIMEOUT when a bounded pipeline wait ran out during an earlier call, or
+ * FDTD_ENONFINITE when a finite check (FDTD_FWD_CHECK_FINITE) found a NaN or an infinity. */
 int fdtd_plan_status(FdtdPlan* plan);
+
+/* Failure injection for tests of the error paths (no counterpart in the reference, whose
+ * errors are Python exceptions at trace time).  No GPU fault is involved in either kind:
+ *   FDTD_INJECT_ALLOC        the next `count` device allocations of the library (plan tables,
+ *                            adjoint scratch, batch tables) report out-of-memory without
+ *                            calling cudaMalloc: the call returns FDTD_ENOMEM;
+ *   FDTD_INJECT_WAIT_EXPIRY  the next `count` TMA half-step launches issued outside stream
+ *                            capture take their bounded-wait error exit before issuing any
+ *                            copy: they update nothing, and the plan's next fdtd_plan_status
+ *                            returns FDTD_ETIMEOUT.
+ * count = 0 clears a kind.  Process-wide; returns FDTD_EINVAL for an unknown kind. */
+#define FDTD_INJECT_ALLOC 1
+#define FDTD_INJECT_WAIT_EXPIRY 2
+int fdtd_debug_inject(int32_t kind, int32_t count);
 
 /* Number of launches of this library's kernels one forward step issues. */
 int32_t fdtd_launches_per_step(const FdtdPlan* plan);
@@ -284,7 +312,8 @@ int32_t fdtd_batch_launches_per_step(const FdtdBatch* batch);
  * Evaluates the reduced value a FIELD (component mean), FLUX (Poynting flux summed over
  * the region times cell_weight) or ENERGY (energy summed times cell_weight) detector
  * records at one step, from the fields E (after the step), H_prev (H before the step's H
- * update; read only when det->exact_interpolation) and H, and writes its ncomp floats to
+ * update; read, and required, only when det->exact_interpolation and the sample reads H: a
+ * FLUX or ENERGY sample, or a FIELD sample of H components) and H, and writes its ncomp floats to
  * the device buffer `out` (ncomp: the recorded components for FIELD, 3 or 1 for FLUX,
  * 1 for ENERGY).  det->slot, det->weights and det->reduce_volume are ignored.
  *
@@ -295,7 +324,9 @@ int32_t fdtd_batch_launches_per_step(const FdtdBatch* batch);
  * written before it is read, and the step word and slot table it also holds are
  * zero-initialised with the library and never written.  The first call on a device
  * looks up the scratch address (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture.  The scratch is shared by all calls on a
+ * that first call before any stream capture.  Every later call made outside a capture
+ * looks it up again (a device reset may move the array); a call inside a capture uses the
+ * address of the last call on that device.  The scratch is shared by all calls on a
  * device: calls that overlap (other streams, other host threads) race on it and must be
  * serialised by the caller.  Same arithmetic as the plan's detector kernels. */
 #define FDTD_NOALLOC_SCRATCH_FLOATS 65536

@@ -71,3 +71,65 @@ def test_struct_layout_matches_c(tmp_path):
             assert getattr(m[t], f).offset == int(val), key
         else:
             assert C.sizeof(m[key]) == int(val), key
+
+
+def _valid_desc(nx=8, ny=8, nz=8):
+    d = N.Desc()
+    d.nx, d.ny, d.nz = nx, ny, nz
+    d.n_steps_total = 4
+    d.courant = 0.99 / 3**0.5
+    d.n_eps = 1
+    d.inv_mu_scalar = 1.0
+    return d
+
+
+@pytest.mark.parametrize("what", ["dims", "slab", "too_many_sources", "detector_box", "dipole_axis", "rec_dtype"])
+def test_bad_descriptors_are_rejected_before_any_device_work(lib, what):
+    """fdtd_plan_create validates the description on the host: an invalid one returns
+    FDTD_EINVAL and no plan, before any CUDA call (so this runs without a GPU)."""
+    import numpy as np
+
+    d = _valid_desc()
+    keep = []
+    if what == "dims":
+        d.nz = 0
+    elif what == "slab":
+        coef = np.zeros(6 * 20, np.float32)
+        keep.append(coef)
+        d.n_slabs = 1
+        d.slabs[0].axis, d.slabs[0].direction, d.slabs[0].thickness = 0, -1, 20  # thicker than nx
+        d.slabs[0].coef = coef.ctypes.data
+    elif what == "too_many_sources":
+        d.n_sources = N.MAX_SOURCES + 1
+    elif what == "detector_box":
+        slot = np.zeros(6, np.int32)
+        keep.append(slot)
+        d.n_detectors = 1
+        dd = d.detectors[0]
+        dd.kind, dd.comp_mask, dd.slot = N.DET_FIELD, 4, slot.ctypes.data
+        for a in range(3):
+            dd.lo[a], dd.hi[a] = 0, 8
+        dd.hi[2] = 9  # one cell past the grid
+    elif what == "dipole_axis":
+        tab = np.zeros(6, np.float32)
+        on = np.ones(6, np.uint8)
+        keep += [tab, on]
+        d.n_sources = 1
+        so = d.sources[0]
+        so.kind, so.component = N.SRC_DIPOLE, 3
+        for a in range(3):
+            so.lo[a], so.hi[a] = 4, 5
+        so.phase_E = so.phase_H = so.teff = tab.ctypes.data
+        so.on = on.ctypes.data
+    elif what == "rec_dtype":
+        d.recording_dtype = 7
+    h = C.c_void_p(12345)
+    rc = lib.fdtd_plan_create(C.byref(d), C.byref(h))
+    assert rc == N.EINVAL and h.value is None
+
+
+def test_debug_inject_rejects_unknown_kinds(lib):
+    assert lib.fdtd_debug_inject(99, 1) == N.EINVAL
+    assert lib.fdtd_debug_inject(N.INJECT_ALLOC, -1) == N.EINVAL
+    assert lib.fdtd_debug_inject(N.INJECT_ALLOC, 0) == N.OK
+    assert lib.fdtd_debug_inject(N.INJECT_WAIT_EXPIRY, 0) == N.OK

@@ -317,3 +317,46 @@ def test_plans_of_different_tile_memory_coexist():
     torch.cuda.synchronize()
     assert torch.isfinite(w1.fields.E).all() and torch.isfinite(w2.fields.E).all()
     assert s1.uses_tma
+
+
+@pytest.mark.parametrize("ty,chunk", [(0, 0), (10, 3)])
+def test_zshell_tma_matches_register_shell(ty, chunk):
+    """The z-slab CPML shell boxes on the TMA kernels with their z terms (the default when the
+    core runs on TMA) against the register-queue shell: forward steps with kappa != 1, a
+    conductor in the slab and a fused full-volume phasor, then time-reversed steps with the
+    recorded interfaces (psi frozen)."""
+    cfg = _cfg(60, record=True)
+    vol = fx.SimulationVolume(shape=(30, 27, 44))
+    bc = fx.BoundaryConfig.from_uniform_bound(6, "pml", kappa_end=1.8)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((8, 22), (6, 20), (2, 40)),
+                                         material=fx.Material(permittivity=(4.0, 3.0, 5.0), electric_conductivity=1e4)))
+    objs.append(fx.PointDipoleSource(name="d", grid_slice_tuple=((15, 16), (13, 14), (5, 6)), polarization=1,
+                                     wave_character=fx.WaveCharacter(wavelength=1.55e-6),
+                                     temporal_profile=scenes.pulse_5fs()))
+    objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((0, 30), (0, 27), (0, 44)),
+                                  wave_characters=(fx.WaveCharacter(wavelength=1.55e-6),), components=("Ex", "Ey", "Ez")))
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
+    assert arrays.recording_state is not None
+    outs = []
+    for zs in (True, False):
+        a = arrays.reset()
+        s = Scene(objects, a, cfg, record_interfaces=True)
+        if zs:
+            s.tune_zshell(True, ty, chunk)
+            assert s.uses_tma and s.uses_zshell
+        else:
+            s.tune_zshell(False)
+            assert not s.uses_zshell
+        s.forward(a, 0, 60)
+        s.status()
+        torch.cuda.synchronize()
+        fwd = [a.fields.E.clone(), a.fields.H.clone(), a.detector_states["ph"]["phasor"].clone()]
+        fwd += [t.clone() for n in a.fields.psi_E for t in (*a.fields.psi_E[n], *a.fields.psi_H[n])]
+        s.reverse(a, 60, 30)
+        s.status()
+        torch.cuda.synchronize()
+        outs.append((fwd, [a.fields.E.clone(), a.fields.H.clone()]))
+        s.close()
+    for x, y in zip(outs[0][0] + outs[0][1], outs[1][0] + outs[1][1]):
+        assert rel_l2(x, y) < 1e-6

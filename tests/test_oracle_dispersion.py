@@ -65,7 +65,8 @@ def test_lorentz_permittivity_and_discrete_susceptibility():
                                                         damping=(1e13, 3e13, 0.0), delta_epsilon=(2.25, 1.0, 0.5)),
                                          fx.DrudePole(plasma_frequency=(5 * OMEGA, 0.0, 2 * OMEGA), damping=0.05 * OMEGA)))
     for model in (_lorentz(), _drude(), per_axis):
-        c1, c2, c3 = (torch.from_numpy(a) for a in compute_pole_coefficients_per_axis(model.poles, dt))
+        c1, c2, c3, c4 = (torch.from_numpy(a) for a in compute_pole_coefficients_per_axis(model.poles, dt))
+        assert torch.count_nonzero(c4) == 0  # no pole here has a numerator term
         for w in (0.6 * OMEGA, OMEGA, 1.7 * OMEGA):
             chi = O._chi_from_coefficients(c1, c2, c3, w, dt)  # (3,)
             want = model.susceptibility_axes(w)
@@ -270,16 +271,17 @@ def test_pole_model_kats():
         want = -(9e15**2) / (w**2 + 1j * 1.5e13 * w)
         assert abs(d.susceptibility(w) - want) <= 1e-12 * abs(want)
     p = fx.LorentzPole(resonance_frequency=2e15, damping=3e13, delta_epsilon=1.5)
-    c1, c2, c3 = compute_pole_coefficients_per_axis((p,), 5e-18)
+    c1, c2, c3, c4 = compute_pole_coefficients_per_axis((p,), 5e-18)
+    assert c4.shape == c1.shape and (c4 == 0).all()
     den = 1.0 + 0.5 * 3e13 * 5e-18
     assert np.allclose(c1[0], (2.0 - (2e15 * 5e-18) ** 2) / den, rtol=1e-12)
     assert np.allclose(c2[0], -(1.0 - 0.5 * 3e13 * 5e-18) / den, rtol=1e-12)
     assert np.allclose(c3[0], 1.5 * 2e15**2 * (5e-18) ** 2 / den, rtol=1e-12)
     q = fx.DrudePole(plasma_frequency=1e16, damping=1e14)
-    c1, _, c3 = compute_pole_coefficients_per_axis((q,), 2e-18)
+    c1, _, c3, _ = compute_pole_coefficients_per_axis((q,), 2e-18)
     den = 1.0 + 0.5 * 1e14 * 2e-18
     assert np.allclose(c1[0], 2.0 / den, rtol=1e-12) and np.allclose(c3[0], 1e32 * 4e-36 / den, rtol=1e-12)
-    _, c2, _ = compute_pole_coefficients_per_axis((fx.LorentzPole(resonance_frequency=1e15, damping=1e13,
+    _, c2, _, _ = compute_pole_coefficients_per_axis((fx.LorentzPole(resonance_frequency=1e15, damping=1e13,
                                                                   delta_epsilon=2.0),), 1e-17)
     assert abs(c2[0, 0] + 1.0) < 2e-4
     slow = fx.LorentzPole(resonance_frequency=1e15, damping=1e10, delta_epsilon=2.0)
@@ -287,7 +289,7 @@ def test_pole_model_kats():
         compute_pole_coefficients_per_axis((slow,), 2.0 / 1e15)
     assert np.isfinite(compute_pole_coefficients_per_axis((slow,), 1.9 / 1e15)[0]).all()
     inert = fx.LorentzPole(resonance_frequency=3e17, damping=3e17, delta_epsilon=0.0)
-    c1, c2, c3 = compute_pole_coefficients_per_axis((inert,), 1e-17)
+    c1, c2, c3, _ = compute_pole_coefficients_per_axis((inert,), 1e-17)
     assert (c3 == 0).all() and np.isfinite(c1).all() and np.isfinite(c2).all()
     assert not fx.Material(permittivity=2.25).is_dispersive
     assert not fx.Material(dispersion=fx.DispersionModel()).is_dispersive

@@ -109,3 +109,19 @@ def test_footprint_counts_gradient_buffers():
     for mu in (1.0, (1.5, 1.2, 2.0)):
         assert sizes[(mu, True)] > sizes[(mu, False)] > 0
     assert sizes[((1.5, 1.2, 2.0), True)] - sizes[(1.0, True)] >= 2 * 4 * 3 * n
+
+
+def test_withdraw_and_release_phases():
+    """A queued job is withdrawn without touching the budget; an active one leaves as
+    "cancelled" or "failed" and frees its footprint."""
+    s = Scheduler(budget_bytes=100, max_slots=8)
+    a, b, c = _job(0, 60), _job(1, 30), _job(2, 50)
+    for j in (a, b, c):
+        s.arrive(j)
+    assert [j.id for j in s.admit(0.0)] == [0, 1]
+    assert s.withdraw(c, 0.5) and c.phase == "cancelled" and s.used == 90
+    assert not s.withdraw(c, 0.6)  # no longer queued
+    s.complete(a, 1.0, "cancelled")
+    s.complete(b, 1.0, "failed")
+    assert s.used == 0 and s.idle()
+    assert [j.phase for j in s.done] == ["cancelled", "cancelled", "failed"]
