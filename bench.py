@@ -187,8 +187,8 @@ def run_gpu(args):
         scene.tune(args.chunk, args.vec)
     if args.shell_chunk or args.shell_vec:
         scene.tune_shell(args.shell_chunk, args.shell_vec)
-    if args.zshell != "auto" or args.zs_ty or args.zs_chunk:
-        scene.tune_zshell(args.zshell != "0", args.zs_ty, args.zs_chunk)
+    if args.shell_tma >= 0:
+        scene.tune_shell_tma(args.shell_tma, args.pml_tz, args.pml_chunk)
     ncell = shape[0] * shape[1] * shape[2]
     W, K = args.warmup, args.steps
     if W + K + 8 > T_TOTAL:
@@ -303,7 +303,7 @@ def run_gpu(args):
             "chunk": int(NATIVE.load().fdtd_plan_chunk(scene.plan)),
             "vec": int(NATIVE.load().fdtd_plan_vec(scene.plan)),
             "tma": scene.uses_tma,
-            "zshell_tma": scene.uses_zshell,
+            "shell_tma": scene.shell_tma,
             "hbm_gbs_effective": round(sum(alg.values()) / (ms / K / 1e3) / 1e9, 1),
         },
         "roofline": {
@@ -646,10 +646,10 @@ def main():
     ap.add_argument("--shell-chunk", type=int, default=0, help="x planes per CPML shell block (0: plan default)")
     ap.add_argument("--shell-vec", type=int, default=0, help="z cells per CPML shell thread (0: plan default)")
     ap.add_argument("--tma", default="auto", choices=["auto", "0", "1"], help="TMA-pipelined update kernels")
-    ap.add_argument("--zshell", default="auto", choices=["auto", "0", "1"],
-                    help="z-slab CPML shell boxes on the TMA kernels")
-    ap.add_argument("--zs-ty", type=int, default=0, help="rows of the z-shell TMA tile (0: default)")
-    ap.add_argument("--zs-chunk", type=int, default=0, help="x planes per z-shell TMA block (0: default)")
+    ap.add_argument("--shell-tma", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="CPML slab cells on the TMA kernels: 0 none, 1 x and y slabs, 2 all (-1: default)")
+    ap.add_argument("--pml-tz", type=int, default=0, help="z extent of the whole-grid TMA tile (shell mode 2)")
+    ap.add_argument("--pml-chunk", type=int, default=0, help="x planes per block of the slab-cell TMA launch")
     ap.add_argument("--tz", type=int, default=0)
     ap.add_argument("--ty", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)

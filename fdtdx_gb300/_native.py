@@ -164,8 +164,8 @@ SIGNATURES = {
     "fdtd_plan_vec": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_tune_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "fdtd_plan_uses_tma": (C.c_int32, [C.c_void_p]),
-    "fdtd_plan_tune_zshell": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
-    "fdtd_plan_uses_zshell": (C.c_int32, [C.c_void_p]),
+    "fdtd_plan_tune_shell_tma": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "fdtd_plan_shell_tma": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_status": (C.c_int, [C.c_void_p]),
     "fdtd_debug_inject": (C.c_int, [C.c_int32, C.c_int32]),
     "fdtd_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(Buffers), C.c_int32, C.POINTER(C.c_void_p)]),

@@ -45,12 +45,16 @@ struct FdtdPlan {
     int tma_tz = 32, tma_ty = 8, tma_ns = 4;
     int tma_chunk = 1;                    // x planes per block of the H kernel
     int tma_chunk_e = 1;                  // and of the E kernel
-    // the two z-slab shell boxes through the TMA kernels with their CPML terms (ZP kernels)
-    bool zs_ok = false;                   // the split admits them (core on TMA, z boxes of <= 64 cells)
-    bool zs_on = true;                    // selected (fdtd_plan_tune_zshell)
-    int zs_tz = 0, zs_ty = 16;            // tile: the thicker z box's extent x zs_ty rows
-    int zs_chunk = 1, zs_chunk_e = 1;     // x planes per block (H, E)
-    int zs_sides = 0, zs_lo = 0, zs_hi = 0;
+    // CPML slab cells on the TMA kernels with in-kernel slab terms (fdtd_plan_tune_shell_tma):
+    // mode 1 widens the core to the whole x and y extent (the x and y slab terms in the PML
+    // kernels) and leaves the two z boxes to the register-queue shell kernel; mode 2 runs the
+    // whole grid in one PML launch per half-step (z terms too); mode 0 runs all six slab boxes
+    // on the shell kernel
+    int shell_tma = 0;                    // requested mode
+    bool m1_ok = false, m2_ok = false;    // admissible
+    int m1_chunk = 1, m1_chunk_e = 1;     // x planes per block (H, E), mode 1
+    int m2_tz = 0;                        // z extent of the mode-2 tile (the core's ty rows)
+    int m2_chunk = 1, m2_chunk_e = 1;
     int* d_err = nullptr;                 // kernel error word (FDTD_ETIMEOUT on a wait that ran out)
     // graph cache for the forward loop
     cudaGraphExec_t gexec = nullptr;
@@ -365,63 +369,71 @@ int staged_planes(const FdtdPlan* p) {
     return 0;
 }
 
-// The z-slab shell boxes ([0, zlo) and [zhi, nz) over the core's x and y range: their cells
-// lie in no x or y slab, so the ZP TMA kernels update them with the z terms alone.  Tile: the
-// thicker box's z extent (a multiple of 4) x zs_ty rows; x chunks of about four waves.
-void configure_zshell(FdtdPlan* p, const Split& sp, int optin) {
-    p->zs_ok = false;
+// The CPML slab cells on the TMA kernels.  Mode 1: the PML kernels over the whole x and y
+// extent and the core's z range (x and y terms), the z boxes on the shell kernel.  Mode 2:
+// the PML kernels over the whole grid, with the z extent of their tile picked for nz.  x
+// chunks of about ten (E) and six (H) waves of resident blocks, as for the core.
+void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
+    p->m1_ok = p->m2_ok = false;
     if (!sp.split || p->d.n_slabs == 0) return;
-    const int nz = p->g.nz, zlo = sp.core.lo[2], zhi = sp.core.hi[2];
-    const int sides = (zlo > 0 ? 1 : 0) | (zhi < nz ? 2 : 0);
-    if (!sides) return;
-    // every z slab must lie inside its box, one slab per z face (the per-axis table), 32-bit psi offsets
-    int faces = 0;
+    // one slab per face (the per-axis table) and 32-bit psi offsets
+    int faces[3] = {0, 0, 0};
     for (int s = 0; s < p->d.n_slabs; ++s) {
         const DSlab& sl = p->slab[s];
         if ((long long)sl.sx * sl.sy * sl.sz >= (1LL << 31)) return;
-        if (sl.axis != 2) continue;
         const int side = p->d.slabs[s].direction > 0 ? 1 : 0;
-        if (faces >> side & 1) return;
-        faces |= 1 << side;
-        if (side == 0 ? sl.lo + sl.L > zlo : sl.lo < zhi) return;
+        if (faces[sl.axis] >> side & 1) return;
+        faces[sl.axis] |= 1 << side;
     }
-    const int tz = std::max(zlo, nz - zhi);
-    const int ty = p->zs_ty;
-    if (tz % 4 || tz > 64 || ty < 1 || ty * tz / 2 > 256 || ty * tz / 2 < 32) return;
-    const int threads = ty * tz / 2;
-    const size_t smE = tma_smem(tma_cfg(tz, ty, p->tma_ns, false, p->d.n_eps, p->d.n_sigma_E, nullptr));
-    const size_t smH = tma_smem(tma_cfg(tz, ty, p->tma_ns, true, p->d.n_mu, p->d.n_sigma_H, nullptr, staged_planes(p)));
-    int occ_e = 1 << 30, occ_h = 1 << 30;
-    bool ok = true;
-    auto setup = [&](const void* fn, size_t sm, int& o) {
-        if ((int)sm > optin || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
-            ok = false;
-            return;
-        }
+    auto occ_of = [&](const void* fn, int threads, size_t sm) {
         int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, sm) != cudaSuccess) nb = 0;
-        o = std::min(o, nb);
+        if ((int)sm > optin || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, sm) != cudaSuccess)
+            nb = 0;
+        return nb;
     };
-    setup((const void*)k_tma_E<false, true>, smE, occ_e);
-    setup((const void*)k_tma_E<true, true>, smE, occ_e);
-    setup((const void*)k_tma_H<false, true>, smH, occ_h);
-    setup((const void*)k_tma_H<true, true>, smH, occ_h);
-    cudaGetLastError();
-    if (!ok || occ_e <= 0 || occ_h <= 0) return;
-    const int cx = sp.core.hi[0] - sp.core.lo[0], cy = sp.core.hi[1] - sp.core.lo[1];
-    const long long tiles = (long long)((sides & 1) + (sides >> 1)) * ((cy + ty - 1) / ty);
-    auto chunk_for = [&](int waves, int o) {
-        long long n = std::max(1ll, (long long)waves * o * p->sm_count / tiles);
+    auto occ_pair = [&](int tz, int ty, int& oe, int& oh) {
+        const int threads = ty * tz / 2;
+        const size_t smE = tma_smem(tma_cfg(tz, ty, p->tma_ns, false, p->d.n_eps, p->d.n_sigma_E, nullptr));
+        const size_t smH = tma_smem(tma_cfg(tz, ty, p->tma_ns, true, p->d.n_mu, p->d.n_sigma_H, nullptr, staged_planes(p)));
+        oe = std::min(occ_of((const void*)k_tma_E<false, true>, threads, smE), occ_of((const void*)k_tma_E<true, true>, threads, smE));
+        oh = std::min(occ_of((const void*)k_tma_H<false, true>, threads, smH), occ_of((const void*)k_tma_H<true, true>, threads, smH));
+    };
+    auto chunk_for = [&](int waves, int o, long long tiles, int cx) {
+        long long n = std::max(1ll, (long long)waves * o * p->sm_count / std::max(1ll, tiles));
         n = std::min<long long>(n, std::max(1, cx / 4));
         return (int)((cx + n - 1) / n);
     };
-    p->zs_tz = tz;
-    p->zs_sides = sides;
-    p->zs_lo = zlo;
-    p->zs_hi = zhi;
-    p->zs_chunk_e = chunk_for(4, occ_e);
-    p->zs_chunk = chunk_for(4, occ_h);
-    p->zs_ok = true;
+    const int nx = p->g.nx, ny = p->g.ny, nz = p->g.nz, ty = p->tma_ty;
+    int oe = 0, oh = 0;
+    occ_pair(p->tma_tz, ty, oe, oh);
+    if (oe > 0 && oh > 0) {
+        const int cz = sp.core.hi[2] - sp.core.lo[2];
+        const long long tiles = (long long)((cz + p->tma_tz - 1) / p->tma_tz) * ((ny + ty - 1) / ty);
+        p->m1_chunk_e = chunk_for(10, oe, tiles, nx);
+        p->m1_chunk = chunk_for(6, oh, tiles, nx);
+        p->m1_ok = true;
+    }
+    const int tz2 = p->m2_tz > 0 ? p->m2_tz : pick_tz(nz);
+    if (tz2 % 4 == 0 && ty * tz2 / 2 <= 256 && ty * tz2 / 2 >= 32) {
+        occ_pair(tz2, ty, oe, oh);
+        if (oe > 0 && oh > 0) {
+            const long long tiles = (long long)((nz + tz2 - 1) / tz2) * ((ny + ty - 1) / ty);
+            p->m2_tz = tz2;
+            p->m2_chunk_e = chunk_for(10, oe, tiles, nx);
+            p->m2_chunk = chunk_for(6, oh, tiles, nx);
+            p->m2_ok = true;
+        }
+    }
+    cudaGetLastError();
+}
+
+// The shell mode the launches use: the requested one, lowered to what the scene admits.
+int shell_tma_mode(const FdtdPlan* p) {
+    if (!p->use_tma) return 0;
+    if (p->shell_tma == 2 && p->m2_ok) return 2;
+    if (p->shell_tma == 1 && p->m1_ok) return 1;
+    return 0;
 }
 
 // Shared memory, occupancy and the x-chunk of the TMA kernels for the current tile choice.
@@ -457,7 +469,7 @@ void configure_tma(FdtdPlan* p) {
     cudaGetLastError();
     if (occ <= 0 || threads > 256 || threads < 32) return;
     const Split sp = split_boxes(p);
-    configure_zshell(p, sp, optin);
+    configure_shell_tma(p, sp, optin);
     const Box core = sp.split ? sp.core : Box{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
     const int cx = core.hi[0] - core.lo[0], cy = core.hi[1] - core.lo[1], cz = core.hi[2] - core.lo[2];
     const long long tiles = (long long)((cz + tz - 1) / tz) * ((cy + ty - 1) / ty);
@@ -720,10 +732,10 @@ bool make_map(CUtensorMap* m, const float* base, int ncomp, const Geo& g, int bz
 // Launch of a TMA-pipelined half-step over the core box, or (ZP) over the z-slab shell boxes
 // with their CPML terms; false when a tensor map cannot be built (the caller then uses the
 // register-queue kernel).
-template <bool REV, bool HSIDE, bool ZP = false>
-bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
+template <bool REV, bool HSIDE, bool PML = false>
+bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, int tz, int chunk) {
     const Geo& g = p->g;
-    const int tz = ZP ? p->zs_tz : p->tma_tz, ty = ZP ? p->zs_ty : p->tma_ty;
+    const int ty = p->tma_ty;
     const int nm = a.mat ? a.n_mat : 0, nsig = a.sig ? a.n_sig : 0;
     // the staged phasor tile of the first fused detector (forward H step only)
     int nd = 0;
@@ -743,11 +755,6 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
             nd = planes;
     }
     TmaCfg c = tma_cfg(tz, ty, p->tma_ns, HSIDE, nm, nsig, p->d_err, nd);
-    if (ZP) {
-        c.zsides = p->zs_sides;
-        c.zlo = p->zs_lo;
-        c.zhi = p->zs_hi;
-    }
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (g_inject_expiry.load() > 0 && cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
         c.expire = take_injected(g_inject_expiry) ? 1 : 0;  // direct launches only: a graph keeps no injected node
@@ -761,13 +768,12 @@ bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) {
     if (nm && !make_map(&mM, a.mat, nm, g, tz, ty, nm)) return false;
     if (nsig && !make_map(&mS, a.sig, nsig, g, tz, ty, nsig)) return false;
     UpdArgs aa = a;
-    aa.chunk = ZP ? (HSIDE ? p->zs_chunk : p->zs_chunk_e) : (HSIDE ? p->tma_chunk : p->tma_chunk_e);
+    aa.chunk = chunk;
     const int bx = aa.hi[0] - aa.lo[0], by = aa.hi[1] - aa.lo[1], bz = aa.hi[2] - aa.lo[2];
-    const int gz = ZP ? (p->zs_sides & 1) + (p->zs_sides >> 1) : (bz + tz - 1) / tz;
-    const dim3 grid(gz, (by + ty - 1) / ty, (bx + aa.chunk - 1) / aa.chunk);
+    const dim3 grid((bz + tz - 1) / tz, (by + ty - 1) / ty, (bx + aa.chunk - 1) / aa.chunk);
     const dim3 block(ty * tz / 2);
-    if (HSIDE) k_tma_H<REV, ZP><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
-    else k_tma_E<REV, ZP><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
+    if (HSIDE) k_tma_H<REV, PML><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, mD, c);
+    else k_tma_E<REV, PML><<<grid, block, tma_smem(c), st>>>(aa, mF, mU, mM, mS, c);
     return true;
 }
 
@@ -852,42 +858,51 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
         launch_plain_boxes<REV, HSIDE, true>(p, a, &all, &p->chunk, 1, st);
         return;
     }
+    const int mode = a.axt == 2 ? shell_tma_mode(p) : 0;
+    if (mode == 2) {
+        // the whole grid in one launch of the PML kernels (every slab term in the tiles)
+        UpdArgs ax = a;
+        for (int x = 0; x < 3; ++x) { ax.lo[x] = 0; ax.hi[x] = x == 0 ? p->g.nx : x == 1 ? p->g.ny : p->g.nz; }
+        if (mid) cudaEventRecord(mid, st);
+        if (launch_tma<REV, HSIDE, true>(p, ax, st, p->m2_tz, HSIDE ? p->m2_chunk : p->m2_chunk_e)) return;
+    }
+    if (mode == 1) {
+        // the core widened over the x and y slabs (their terms in the PML kernels), then the two
+        // z boxes (over the whole x and y extent) on the shell kernel
+        UpdArgs ax = a;
+        ax.lo[0] = 0; ax.lo[1] = 0; ax.lo[2] = sp.core.lo[2];
+        ax.hi[0] = p->g.nx; ax.hi[1] = p->g.ny; ax.hi[2] = sp.core.hi[2];
+        if (launch_tma<REV, HSIDE, true>(p, ax, st, p->tma_tz, HSIDE ? p->m1_chunk : p->m1_chunk_e)) {
+            if (mid) cudaEventRecord(mid, st);
+            Box zb[2];
+            int nzb = 0;
+            if (sp.core.lo[2] > 0) zb[nzb++] = Box{{0, 0, 0}, {p->g.nx, p->g.ny, sp.core.lo[2]}};
+            if (sp.core.hi[2] < p->g.nz) zb[nzb++] = Box{{0, 0, sp.core.hi[2]}, {p->g.nx, p->g.ny, p->g.nz}};
+            const int zc[2] = {p->shell_chunk, p->shell_chunk};
+            if (nzb) launch_plain_boxes<REV, HSIDE, true>(p, a, zb, zc, nzb, st, p->shell_vec);
+            return;
+        }
+    }
     UpdArgs ac = a;
     for (int x = 0; x < 3; ++x) { ac.lo[x] = sp.core.lo[x]; ac.hi[x] = sp.core.hi[x]; }
-    if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st))) launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
+    if (!(p->use_tma && launch_tma<REV, HSIDE>(p, ac, st, p->tma_tz, HSIDE ? p->tma_chunk : p->tma_chunk_e)))
+        launch_plain_boxes<REV, HSIDE, false>(p, a, &sp.core, &p->chunk, 1, st);
     if (mid) cudaEventRecord(mid, st);
-    // the z-slab boxes (short z rows: the CPML cells with the worst coalescing) through the
-    // TMA pipeline with their z terms, when the per-axis slab table holds
-    Box shell[6];
-    int n_shell = 0;
-    const bool zs = p->use_tma && p->zs_ok && p->zs_on && a.axt == 2 && launch_tma<REV, HSIDE, true>(p, ac, st);
-    for (int q = 0; q < sp.n_shell; ++q) {
-        const Box& b = sp.shell[q];
-        const bool zbox = b.lo[0] == sp.core.lo[0] && b.hi[0] == sp.core.hi[0] && b.lo[1] == sp.core.lo[1] &&
-                          b.hi[1] == sp.core.hi[1];
-        if (!(zs && zbox)) shell[n_shell++] = b;
-    }
     int chunks[6];
-    for (int q = 0; q < n_shell; ++q) chunks[q] = p->shell_chunk;
+    for (int q = 0; q < sp.n_shell; ++q) chunks[q] = p->shell_chunk;
     // the shells run one z cell per thread by default: fewer registers per thread, more
     // warps in flight for their latency-bound CPML and phasor loads (measured 14% (H) and
     // 24% (E) faster than two)
-    launch_plain_boxes<REV, HSIDE, true>(p, a, shell, chunks, n_shell, st, p->shell_vec);
+    launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st, p->shell_vec);
 }
 
 int half_step_launches(const FdtdPlan* p) {
     const Split sp = split_boxes(p);
     if (!sp.split) return 1;
-    int rest = sp.n_shell;
-    const bool zs = p->use_tma && p->zs_ok && p->zs_on;
-    if (zs)
-        for (int q = 0; q < sp.n_shell; ++q) {
-            const Box& b = sp.shell[q];
-            if (b.lo[0] == sp.core.lo[0] && b.hi[0] == sp.core.hi[0] && b.lo[1] == sp.core.lo[1] &&
-                b.hi[1] == sp.core.hi[1])
-                --rest;
-        }
-    return 1 + (zs ? 1 : 0) + (rest > 0 ? 1 : 0);
+    const int mode = shell_tma_mode(p);
+    if (mode == 2) return 1;
+    if (mode == 1) return 1 + ((sp.core.lo[2] > 0 || sp.core.hi[2] < p->g.nz) ? 1 : 0);
+    return 1 + (sp.n_shell > 0);
 }
 
 template <bool REV>
@@ -1295,23 +1310,27 @@ extern "C" int fdtd_plan_tune_tma(FdtdPlan* p, int32_t enable, int32_t tz, int32
 
 extern "C" int32_t fdtd_plan_uses_tma(const FdtdPlan* p) { return p && p->use_tma ? 1 : 0; }
 
-extern "C" int fdtd_plan_tune_zshell(FdtdPlan* p, int32_t enable, int32_t ty, int32_t chunk) {
+extern "C" int fdtd_plan_tune_shell_tma(FdtdPlan* p, int32_t mode, int32_t tz, int32_t chunk) {
     if (!p) return FDTD_EINVAL;
-    if (ty < 0 || ty > 256 || chunk < 0) return fail(p, FDTD_EINVAL, "invalid z-shell tile");
-    p->zs_on = enable != 0;
-    p->zs_ty = ty > 0 ? ty : 16;
+    if (mode < 0 || mode > 2 || tz < 0 || tz % 4 || tz > 120 || chunk < 0)
+        return fail(p, FDTD_EINVAL, "invalid slab-cell mode (0, 1 or 2) or tile (tz a multiple of 4, <= 120)");
+    p->shell_tma = mode;
+    p->m2_tz = tz;
     configure_tma(p);
-    if (enable && !(p->use_tma && p->zs_ok)) {
-        p->zs_on = false;
-        return fail(p, FDTD_EINVAL, "the z-slab shell boxes cannot run on the TMA kernels here (no TMA core, "
-                                    "no z slab, a z box thicker than 64 cells or a tile that does not fit)");
+    if (shell_tma_mode(p) != mode) {
+        p->shell_tma = shell_tma_mode(p);
+        return fail(p, FDTD_EINVAL, "the CPML slab cells cannot run on the TMA kernels in this mode here (no TMA "
+                                    "core, two slabs on a face or a tile that does not fit)");
     }
-    if (chunk > 0) p->zs_chunk = p->zs_chunk_e = std::min(chunk, p->g.nx);
+    if (chunk > 0) {
+        if (mode == 1) p->m1_chunk = p->m1_chunk_e = std::min(chunk, p->g.nx);
+        if (mode == 2) p->m2_chunk = p->m2_chunk_e = std::min(chunk, p->g.nx);
+    }
     drop_graphs(p);
     return FDTD_OK;
 }
 
-extern "C" int32_t fdtd_plan_uses_zshell(const FdtdPlan* p) { return p && p->use_tma && p->zs_ok && p->zs_on ? 1 : 0; }
+extern "C" int32_t fdtd_plan_shell_tma(const FdtdPlan* p) { return p ? shell_tma_mode(p) : 0; }
 
 extern "C" int fdtd_plan_status(FdtdPlan* p) {
     if (!p) return FDTD_EINVAL;

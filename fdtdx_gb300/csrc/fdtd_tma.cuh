@@ -34,22 +34,22 @@ struct TmaCfg {
     uint32_t stage_bytes;  // bytes the TMA loads of one stage deliver
     int* err;
     int expire;            // test hook: take the bounded-wait error exit before issuing any copy
-    // z-slab shell launches (ZP kernels): which z boxes (bit 0: low, bit 1: high; blockIdx.x
-    // picks one), the low box's end and the high box's start
-    int zsides, zlo, zhi;
 };
 
 // ---------------------------------------------------------------------------------
-// CPML z-slab terms inside the TMA half-steps (ZP kernels, launched over the two z-slab
-// shell boxes of a split grid, whose cells lie in no x or y slab): a thread's two cells
-// have a fixed layer of the slab along the whole x-march, so the slab coefficients are
-// read once and the psi offset grows by ny * L per plane.  psi is read with plain loads
-// issued before the plane's pipeline wait.  Same arithmetic as ax_term on axis 2
-// (fdtdx/core/physics/curl.py:284-308, perfectly_matched_layer.py:138-190).
+// CPML terms inside the TMA half-steps (PML kernels: a box that may hold slab cells, up to
+// the whole grid).  The layer of a thread's column in a y or z slab is fixed along the whole
+// x-march (YCol, ZCol: coefficients read once, the psi offset grows by a constant per plane);
+// the x layer is the same for every thread of a plane (XPlane, block-uniform loads).  psi is
+// read a plane ahead of its use (PsiPf) with plain loads, one 8-byte access per psi array for
+// a thread's two cells.  The terms are those of ax_term (fdtdx/core/physics/curl.py:284-308,
+// perfectly_matched_layer.py:138-190), applied in axis order x, y, z as the shell kernel
+// applies them.  psi offsets: x slab (L, ny, nz) -> (l ny + j) nz + k; y slab (nx, L, nz) ->
+// (i L + l) nz + k; z slab (nx, ny, L) -> (i ny + j) L + l.
 // ---------------------------------------------------------------------------------
 struct ZCol {
     int o[2];              // psi offset of each cell at plane 0 (-1: the cell has no z term)
-    int stride;            // psi floats per x plane
+    int stride;            // psi floats per x plane (ny L)
     float ca[2], cb[2], km[2];
     int kone;
     float* p1;
@@ -57,54 +57,194 @@ struct ZCol {
 };
 
 template <bool HSIDE>
-__device__ __forceinline__ void zcol_init(const UpdArgs& a, int side, int j, int k0, bool valid, ZCol& z) {
-    const int L = side ? a.axs[2][1].L : a.axs[2][0].L;
-    const int lo = side ? a.axs[2][1].lo : a.axs[2][0].lo;
-    const float* co = (side ? a.axs[2][1].coef : a.axs[2][0].coef) + (HSIDE ? 3 * L : 0);
-    z.kone = side ? a.axs[2][1].kappa_one : a.axs[2][0].kappa_one;
-    z.p1 = side ? a.axp[2][1][0] : a.axp[2][0][0];
-    z.p2 = side ? a.axp[2][1][1] : a.axp[2][0][1];
-    z.stride = a.g.ny * L;
+__device__ __forceinline__ void zcol_init(const UpdArgs& a, int j, int k0, bool valid, ZCol& z) {
+    z.o[0] = z.o[1] = -1;
+    z.stride = 0;
+    z.kone = 1;
+    z.p1 = z.p2 = nullptr;
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
-        const int l = k0 + e - lo;
-        z.o[e] = -1;
         z.ca[e] = z.cb[e] = z.km[e] = 0.f;
-        if (valid && L > 0 && (unsigned)l < (unsigned)L) {
-            z.o[e] = j * L + l;
-            z.ca[e] = __ldg(co + l);
-            z.cb[e] = __ldg(co + L + l);
-            z.km[e] = z.kone ? 0.f : __ldg(co + 2 * L + l) - 1.f;
-        }
+        int l = 0;
+        const int side = valid ? ax_find<2>(a, k0 + e, l) : -1;
+        if (side < 0) continue;
+        // two adjacent cells cannot lie in the two different z slabs: one side per thread
+        const int L = side ? a.axs[2][1].L : a.axs[2][0].L;
+        const float* co = (side ? a.axs[2][1].coef : a.axs[2][0].coef) + (HSIDE ? 3 * L : 0);
+        z.kone = side ? a.axs[2][1].kappa_one : a.axs[2][0].kappa_one;
+        z.p1 = side ? a.axp[2][1][0] : a.axp[2][0][0];
+        z.p2 = side ? a.axp[2][1][1] : a.axp[2][0][1];
+        z.stride = a.g.ny * L;
+        z.o[e] = j * L + l;
+        z.ca[e] = __ldg(co + l);
+        z.cb[e] = __ldg(co + L + l);
+        z.km[e] = z.kone ? 0.f : __ldg(co + 2 * L + l) - 1.f;
     }
 }
 
-// psi pair of cell e at plane i (zero without a term), loaded ahead of the plane's wait.
-__device__ __forceinline__ float2 zcol_load(const ZCol& z, int e, int i) {
-    if (z.o[e] < 0) return make_float2(0.f, 0.f);
-    const int o = z.o[e] + i * z.stride;
-    return make_float2(z.p1[o], z.p2[o]);
+struct YCol {
+    int o[2];              // psi offset of each cell at plane 0 (-1: no y term)
+    int stride;            // psi floats per x plane (L nz)
+    float ca, cb, km;
+    int kone;
+    float* p1;
+    float* p2;
+};
+
+template <bool HSIDE>
+__device__ __forceinline__ void ycol_init(const UpdArgs& a, int j, int k0, bool valid, YCol& y) {
+    y.o[0] = y.o[1] = -1;
+    y.ca = y.cb = y.km = 0.f;
+    y.kone = 1;
+    y.stride = 0;
+    y.p1 = y.p2 = nullptr;
+    int l = 0;
+    const int side = ax_find<1>(a, j, l);
+    if (!valid || side < 0) return;
+    const int L = side ? a.axs[1][1].L : a.axs[1][0].L;
+    const float* co = (side ? a.axs[1][1].coef : a.axs[1][0].coef) + (HSIDE ? 3 * L : 0);
+    y.kone = side ? a.axs[1][1].kappa_one : a.axs[1][0].kappa_one;
+    y.p1 = side ? a.axp[1][1][0] : a.axp[1][0][0];
+    y.p2 = side ? a.axp[1][1][1] : a.axp[1][0][1];
+    y.ca = __ldg(co + l);
+    y.cb = __ldg(co + L + l);
+    y.km = y.kone ? 0.f : __ldg(co + 2 * L + l) - 1.f;
+    y.stride = L * a.g.nz;
+    y.o[0] = l * a.g.nz + k0;
+    y.o[1] = y.o[0] + 1;
 }
 
-// The z term of cell e: d1 = d_z F_y, d2 = d_z F_x; curl_x -= c1, curl_y += c2.
-template <bool REV>
-__device__ __forceinline__ void zcol_apply(const ZCol& z, int e, int i, float2 pv, float d1, float d2, float cu[3]) {
-    if (z.o[e] < 0) return;
-    float p1 = pv.x, p2 = pv.y;
+struct XPlane {
+    int side, l;           // face of the x slab holding the plane (-1: none) and its layer
+    float ca, cb, km;
+    int kone;
+    float* p1;
+    float* p2;
+};
+
+template <bool HSIDE>
+__device__ __forceinline__ void xplane_init(const UpdArgs& a, int i, XPlane& x) {
+    x.side = ax_find<0>(a, i, x.l);
+    x.ca = x.cb = x.km = 0.f;
+    x.kone = 1;
+    x.p1 = x.p2 = nullptr;
+    if (x.side < 0) return;
+    const int L = x.side ? a.axs[0][1].L : a.axs[0][0].L;
+    const float* co = (x.side ? a.axs[0][1].coef : a.axs[0][0].coef) + (HSIDE ? 3 * L : 0);
+    x.kone = x.side ? a.axs[0][1].kappa_one : a.axs[0][0].kappa_one;
+    x.p1 = x.side ? a.axp[0][1][0] : a.axp[0][0][0];
+    x.p2 = x.side ? a.axp[0][1][1] : a.axp[0][0][1];
+    x.ca = __ldg(co + x.l);
+    x.cb = __ldg(co + L + x.l);
+    x.km = x.kone ? 0.f : __ldg(co + 2 * L + x.l) - 1.f;
+}
+
+__device__ __forceinline__ int xplane_off(const UpdArgs& a, const XPlane& x, int j, int k) {
+    return (x.l * a.g.ny + j) * a.g.nz + k;
+}
+
+// psi offsets of a thread's two cells at plane i (-1: no term there).
+__device__ __forceinline__ void zcol_off(const ZCol& z, int i, int& o0, int& o1) {
+    o0 = z.o[0] >= 0 ? z.o[0] + i * z.stride : -1;
+    o1 = z.o[1] >= 0 ? z.o[1] + i * z.stride : -1;
+}
+
+__device__ __forceinline__ void ycol_off(const YCol& y, int i, int& o0, int& o1) {
+    o0 = y.o[0] >= 0 ? y.o[0] + i * y.stride : -1;
+    o1 = y.o[1] >= 0 ? y.o[1] + i * y.stride : -1;
+}
+
+// psi pairs (psi1, psi2) of a thread's two cells at offsets o0, o1 (-1: no term): one 8-byte
+// load or store per psi array when the cells are adjacent and the offset even.
+__device__ __forceinline__ void psi_load_pair(const float* p1, const float* p2, int o0, int o1, float2& c0, float2& c1) {
+    c0 = c1 = make_float2(0.f, 0.f);
+    if (o0 >= 0 && o1 == o0 + 1 && !(o0 & 1)) {
+        const float2 u = *reinterpret_cast<const float2*>(p1 + o0);
+        const float2 v = *reinterpret_cast<const float2*>(p2 + o0);
+        c0 = make_float2(u.x, v.x);
+        c1 = make_float2(u.y, v.y);
+        return;
+    }
+    if (o0 >= 0) c0 = make_float2(p1[o0], p2[o0]);
+    if (o1 >= 0) c1 = make_float2(p1[o1], p2[o1]);
+}
+
+__device__ __forceinline__ void psi_store_pair(float* p1, float* p2, int o0, int o1, float2 c0, float2 c1) {
+    if (o0 >= 0 && o1 == o0 + 1 && !(o0 & 1)) {
+        *reinterpret_cast<float2*>(p1 + o0) = make_float2(c0.x, c1.x);
+        *reinterpret_cast<float2*>(p2 + o0) = make_float2(c0.y, c1.y);
+        return;
+    }
+    if (o0 >= 0) { p1[o0] = c0.x; p2[o0] = c0.y; }
+    if (o1 >= 0) { p1[o1] = c1.x; p2[o1] = c1.y; }
+}
+
+// The psi pairs of a thread's two cells at one plane, fetched a plane ahead of their use so
+// the loads overlap the previous plane's work (the field tiles arrive through the pipeline).
+struct PsiPf {
+    float2 x[2], y[2], z[2];
+    XPlane xp;
+};
+
+template <bool HSIDE>
+__device__ __forceinline__ void pml_fetch(const UpdArgs& a, const ZCol& zc, const YCol& yc, int i, int j, int k0,
+                                          bool valid, PsiPf& f) {
+    int o0, o1;
+    zcol_off(zc, i, o0, o1);
+    psi_load_pair(zc.p1, zc.p2, o0, o1, f.z[0], f.z[1]);
+    ycol_off(yc, i, o0, o1);
+    psi_load_pair(yc.p1, yc.p2, o0, o1, f.y[0], f.y[1]);
+    xplane_init<HSIDE>(a, i, f.xp);
+    o0 = f.xp.side >= 0 && valid ? xplane_off(a, f.xp, j, k0) : -1;
+    psi_load_pair(f.xp.p1, f.xp.p2, o0, o0 >= 0 ? o0 + 1 : -1, f.x[0], f.x[1]);
+}
+
+// One slab term on axis AX at a cell (ax_term's arithmetic): the differences of the slab
+// axis (AX 0: d_x F_z, d_x F_y; AX 1: d_y F_x, d_y F_z; AX 2: d_z F_y, d_z F_x) advance the
+// psi pair (reverse steps keep it frozen) and correct two curl components; returns the pair
+// a forward step stores.
+template <bool REV, int AX>
+__device__ __forceinline__ float2 tma_slab_term(float ca, float cb, float km, int kone, float2 pv, const float d[6],
+                                                float cu[3]) {
+    const float d1 = AX == 0 ? d[3] : (AX == 1 ? d[5] : d[1]);
+    const float d2 = AX == 0 ? d[4] : (AX == 1 ? d[0] : d[2]);
+    float q1 = pv.x, q2 = pv.y;
     if (!REV) {
-        p1 = z.cb[e] * p1 + z.ca[e] * d1;
-        p2 = z.cb[e] * p2 + z.ca[e] * d2;
-        const int o = z.o[e] + i * z.stride;
-        z.p1[o] = p1;
-        z.p2[o] = p2;
+        q1 = cb * q1 + ca * d1;
+        q2 = cb * q2 + ca * d2;
     }
-    float c1 = p1, c2 = p2;
-    if (!z.kone) {
-        c1 = z.km[e] * d1 + p1;
-        c2 = z.km[e] * d2 + p2;
+    float c1 = q1, c2 = q2;
+    if (!kone) {
+        c1 = km * d1 + q1;
+        c2 = km * d2 + q2;
     }
-    cu[0] -= c1;
-    cu[1] += c2;
+    if (AX == 0) { cu[1] -= c1; cu[2] += c2; }
+    else if (AX == 1) { cu[2] -= c1; cu[0] += c2; }
+    else { cu[0] -= c1; cu[1] += c2; }
+    return make_float2(q1, q2);
+}
+
+// The slab terms of cell e (axis order x, y, z); q holds the psi pairs to store.
+template <bool REV>
+__device__ __forceinline__ void pml_terms(const PsiPf& f, const YCol& yc, const ZCol& zc, int e, const float d[6],
+                                          float cu[3], float2 q[3]) {
+    if (f.xp.side >= 0) q[0] = tma_slab_term<REV, 0>(f.xp.ca, f.xp.cb, f.xp.km, f.xp.kone, f.x[e], d, cu);
+    if (yc.o[e] >= 0) q[1] = tma_slab_term<REV, 1>(yc.ca, yc.cb, yc.km, yc.kone, f.y[e], d, cu);
+    if (zc.o[e] >= 0) q[2] = tma_slab_term<REV, 2>(zc.ca[e], zc.cb[e], zc.km[e], zc.kone, f.z[e], d, cu);
+}
+
+// The forward step's psi stores of both cells at plane i.
+__device__ __forceinline__ void pml_store(const UpdArgs& a, const PsiPf& f, const YCol& yc, const ZCol& zc, int i, int j,
+                                          int k0, const float2 q[2][3]) {
+    int o0, o1;
+    if (f.xp.side >= 0) {
+        o0 = xplane_off(a, f.xp, j, k0);
+        psi_store_pair(f.xp.p1, f.xp.p2, o0, o0 + 1, q[0][0], q[1][0]);
+    }
+    ycol_off(yc, i, o0, o1);
+    psi_store_pair(yc.p1, yc.p2, o0, o1, q[0][1], q[1][1]);
+    zcol_off(zc, i, o0, o1);
+    psi_store_pair(zc.p1, zc.p2, o0, o1, q[0][2], q[1][2]);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -164,7 +304,7 @@ __device__ __forceinline__ void drain(uint64_t* bar, int ns, int from, int to) {
 //   E, inv_eps, sigma_E on the tile
 // Loads cover planes i0-1 .. i1-1; the first only seeds H(i-1) of each column.
 // ---------------------------------------------------------------------------------
-template <bool REV, bool ZP = false>
+template <bool REV, bool PML = false>
 __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -177,17 +317,18 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    // ZP: blockIdx.x picks the z-slab box (low box [0, zlo), high box [zhi, nz))
-    const int zside = ZP ? (tc.zsides == 3 ? (int)blockIdx.x : tc.zsides >> 1) : 0;
-    const int kt = ZP ? (zside ? tc.zhi : 0) : a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
-    const int kend = ZP ? (zside ? g.nz : tc.zlo) : a.hi[2];
+    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
     const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < kend && j < a.hi[1];
+    const bool valid = k0 < a.hi[2] && j < a.hi[1];
     const long long N = g.N;
     ZCol zc{};
-    if (ZP) zcol_init<false>(a, zside, j, k0, valid, zc);
+    YCol yc{};
+    if (PML) {
+        zcol_init<false>(a, j, k0, valid, zc);
+        ycol_init<false>(a, j, k0, valid, yc);
+    }
     if (tc.expire) {  // injected wait expiry: the error path, with no copy issued
         if (tid == 0) atomicExch(tc.err, FDTD_ETIMEOUT);
         return;
@@ -212,13 +353,13 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
         for (int p = 0; p < min(NS, P); ++p) issue(p);
 
     float Hy_m[2] = {0.f, 0.f}, Hz_m[2] = {0.f, 0.f};
+    PsiPf pf{}, pn{};  // psi of the plane being updated and of the next one
     for (int p = 0; p < P; ++p) {
         const int s = p % NS;
         const int i = i0 - 1 + p;
-        float2 zv[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        if (ZP && p > 0) {
-            zv[0] = zcol_load(zc, 0, i);
-            zv[1] = zcol_load(zc, 1, i);
+        if (PML) {
+            pf = pn;
+            if (p + 1 < P) pml_fetch<false>(a, zc, yc, i + 1, j, k0, valid, pn);
         }
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
         const float* F = sm + s * tc.stage_floats;
@@ -234,6 +375,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
             const float* S = F + tc.off_S;
             const long long c = cell_index(g, i, j, k0);
             float out[3][2];
+            float2 qn[2][3];  // the psi pairs a forward step stores
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int kk = 4 + 2 * tz + e;
@@ -249,7 +391,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (ZP) zcol_apply<REV>(zc, e, i, zv[e], d[1], d[2], cu);
+                if (PML) pml_terms<REV>(pf, yc, zc, e, d, cu, qn[e]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -270,6 +412,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
+            if (PML && !REV) pml_store(a, pf, yc, zc, i, j, k0, qn);
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -292,7 +435,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 //   H, inv_mu, sigma_H on the tile
 // Loads cover planes i0 .. i1; plane i is computed once the loads of i and i+1 landed.
 // ---------------------------------------------------------------------------------
-template <bool REV, bool ZP = false>
+template <bool REV, bool PML = false>
 __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -306,16 +449,18 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
     const int tid = threadIdx.x;
     const int half = TZ / 2;
     const int tz = tid % half, ty = tid / half;
-    const int zside = ZP ? (tc.zsides == 3 ? (int)blockIdx.x : tc.zsides >> 1) : 0;
-    const int kt = ZP ? (zside ? tc.zhi : 0) : a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
-    const int kend = ZP ? (zside ? g.nz : tc.zlo) : a.hi[2];
+    const int kt = a.lo[2] + blockIdx.x * TZ, jt = a.lo[1] + blockIdx.y * TY;
     const int i0 = a.lo[0] + blockIdx.z * a.chunk, i1 = min(i0 + a.chunk, a.hi[0]);
     const int P = i1 - i0 + 1;
     const int k0 = kt + 2 * tz, j = jt + ty;
-    const bool valid = k0 < kend && j < a.hi[1];
+    const bool valid = k0 < a.hi[2] && j < a.hi[1];
     const long long N = g.N;
     ZCol zc{};
-    if (ZP) zcol_init<true>(a, zside, j, k0, valid, zc);
+    YCol yc{};
+    if (PML) {
+        zcol_init<true>(a, j, k0, valid, zc);
+        ycol_init<true>(a, j, k0, valid, yc);
+    }
 
     int slot[kMaxFuse];
     float2 w[kMaxFuse][kMaxFuseFreq];
@@ -364,13 +509,14 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
         for (int e = 0; e < 3; ++e) Exm[e] = ld_halo(g, a.F, 0, i0 - 1, j, k0 + e);
     }
+    PsiPf pf{}, pn{};  // psi of the plane being updated and of the next one
+    if (PML && P > 1) pml_fetch<true>(a, zc, yc, i0, j, k0, valid, pn);
     for (int p = 0; p + 1 < P; ++p) {
         const int s = p % NS, s1 = (p + 1) % NS;
         const int i = i0 + p;
-        float2 zv[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        if (ZP) {
-            zv[0] = zcol_load(zc, 0, i);
-            zv[1] = zcol_load(zc, 1, i);
+        if (PML) {
+            pf = pn;
+            if (p + 2 < P) pml_fetch<true>(a, zc, yc, i + 1, j, k0, valid, pn);
         }
         ok = ok && mbar_wait_bounded(&bar[s1], (uint32_t)(((p + 1) / NS) & 1));
         if (ok && valid) {
@@ -382,6 +528,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
             const long long c = cell_index(g, i, j, k0);
             const int r0 = ty + 1;
             float out[3][2];
+            float2 qn[2][3];  // the psi pairs a forward step stores
             float Exc[3];
 #pragma unroll
             for (int e = 0; e < 3; ++e) Exc[e] = E[(0 * EY + r0) * EZ + 4 + 2 * tz + e];
@@ -400,7 +547,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (ZP) zcol_apply<REV>(zc, e, i, zv[e], d[1], d[2], cu);
+                if (PML) pml_terms<REV>(pf, yc, zc, e, d, cu, qn[e]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -464,6 +611,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
+            if (PML && !REV) pml_store(a, pf, yc, zc, i, j, k0, qn);
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {

@@ -510,14 +510,16 @@ class Scene:
     def uses_tma(self) -> bool:
         return bool(N.load().fdtd_plan_uses_tma(self.plan))
 
-    def tune_zshell(self, enable: bool = True, ty: int = 0, chunk: int = 0) -> None:
-        """The z-slab CPML shell boxes on the TMA kernels (enable) or the register-queue shell."""
-        N.check(N.load().fdtd_plan_tune_zshell(self.plan, 1 if enable else 0, int(ty), int(chunk)), self.plan,
-                "fdtd_plan_tune_zshell")
+    def tune_shell_tma(self, mode: int = 2, tz: int = 0, chunk: int = 0) -> None:
+        """Where the CPML slab cells run with a TMA core: 0 the register-queue shell kernel, 1 the
+        x and y slabs in the TMA kernels (z boxes on the shell kernel), 2 the whole grid in one
+        TMA launch (tile z extent ``tz``, 0: picked for nz)."""
+        N.check(N.load().fdtd_plan_tune_shell_tma(self.plan, int(mode), int(tz), int(chunk)), self.plan,
+                "fdtd_plan_tune_shell_tma")
 
     @property
-    def uses_zshell(self) -> bool:
-        return bool(N.load().fdtd_plan_uses_zshell(self.plan))
+    def shell_tma(self) -> int:
+        return int(N.load().fdtd_plan_shell_tma(self.plan))
 
     def status(self) -> None:
         """Raise if a kernel reported an error (a bounded pipeline wait that ran out)."""

@@ -236,12 +236,14 @@ int fdtd_plan_tune_shell(FdtdPlan* plan, int32_t chunk, int32_t vec);
 int fdtd_plan_tune_tma(FdtdPlan* plan, int32_t enable, int32_t tz, int32_t ty, int32_t stages, int32_t chunk);
 int32_t fdtd_plan_uses_tma(const FdtdPlan* plan);
 
-/* The two z-slab CPML shell boxes of a split grid (the slab cells whose z rows are shortest)
- * run on the TMA kernels with their CPML z terms when the core does (the default), else on
- * the register-queue shell kernel: enable = 1 / 0, `ty` rows of the (box z extent) x ty tile
- * and `chunk` x planes per block (0 picks a default).  fdtd_plan_uses_zshell reports it. */
-int fdtd_plan_tune_zshell(FdtdPlan* plan, int32_t enable, int32_t ty, int32_t chunk);
-int32_t fdtd_plan_uses_zshell(const FdtdPlan* plan);
+/* Where the CPML slab cells of a grid split into a slab-free core and its shell run, when the
+ * core runs on the TMA kernels: mode 0, the register-queue shell kernel over the six slab
+ * boxes; mode 1, the TMA kernels with in-tile slab terms over the whole x and y extent (the x
+ * and y slabs) and the shell kernel over the two z boxes; mode 2, the whole grid in one launch
+ * of the TMA kernels with every slab term in the tiles (tile z extent `tz`, 0: picked for nz).
+ * `chunk` x planes per block (0: a default).  fdtd_plan_shell_tma returns the mode in use. */
+int fdtd_plan_tune_shell_tma(FdtdPlan* plan, int32_t mode, int32_t tz, int32_t chunk);
+int32_t fdtd_plan_shell_tma(const FdtdPlan* plan);
 
 /* Reads and clears the kernels' error word (synchronises the device): FDTD_OK,
  * FDTD_ETIMEOUT when a bounded pipeline wait ran out during an earlier call, or

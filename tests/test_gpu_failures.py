@@ -138,7 +138,7 @@ def test_serving_cancellation_and_divergence_are_isolated():
     seen = {}
 
     def on_chunk(srv, now):
-        if "snap" not in seen and jobs[2].phase == "forward":
+        if "snap" not in seen and jobs[2].phase == "forward" and jobs[2].t_fwd > 0:
             seen["snap"] = srv.snapshot(jobs[2])
             srv.cancel(jobs[2])
             srv.cancel(jobs[4])
@@ -146,7 +146,7 @@ def test_serving_cancellation_and_divergence_are_isolated():
     server.run(jobs, realtime=False, on_chunk=on_chunk)
     assert [j.phase for j in jobs] == ["done", "done", "cancelled", "failed", "cancelled"]
     assert "NaN" in jobs[3].error or "infinity" in jobs[3].error
-    assert seen["snap"]["E"].shape == (3, 40, 36, 32) and 0 < seen["snap"]["t"] < 400
+    assert seen["snap"]["E"].shape == (3, 40, 36, 32) and 0 < seen["snap"]["t"] <= 400
     assert jobs[2].result is None and jobs[4].t_admit != jobs[4].t_admit  # never admitted (NaN)
     assert server.sched.used == 0
     alone = run_one_at_a_time(mix()[:2], realtime=False)

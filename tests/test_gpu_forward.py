@@ -319,19 +319,23 @@ def test_plans_of_different_tile_memory_coexist():
     assert s1.uses_tma
 
 
-@pytest.mark.parametrize("ty,chunk", [(0, 0), (10, 3)])
-def test_zshell_tma_matches_register_shell(ty, chunk):
-    """The z-slab CPML shell boxes on the TMA kernels with their z terms (the default when the
-    core runs on TMA) against the register-queue shell: forward steps with kappa != 1, a
-    conductor in the slab and a fused full-volume phasor, then time-reversed steps with the
-    recorded interfaces (psi frozen)."""
+@pytest.mark.parametrize("mode,tz,chunk", [(1, 0, 0), (2, 0, 0), (2, 20, 3)])
+def test_shell_tma_matches_register_shell(mode, tz, chunk):
+    """The CPML slab cells on the TMA kernels with in-tile slab terms (mode 1: the x and y
+    slabs, the core widened over them; mode 2: the whole grid in one launch) against the
+    register-queue shell kernel: forward steps with kappa != 1, a conductor and a dipole inside
+    the slabs and a fused full-volume phasor, then time-reversed steps with the recorded
+    interfaces (psi frozen)."""
     cfg = _cfg(60, record=True)
     vol = fx.SimulationVolume(shape=(30, 27, 44))
     bc = fx.BoundaryConfig.from_uniform_bound(6, "pml", kappa_end=1.8)
     objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
-    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((8, 22), (6, 20), (2, 40)),
+    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((3, 22), (2, 20), (2, 40)),
                                          material=fx.Material(permittivity=(4.0, 3.0, 5.0), electric_conductivity=1e4)))
     objs.append(fx.PointDipoleSource(name="d", grid_slice_tuple=((15, 16), (13, 14), (5, 6)), polarization=1,
+                                     wave_character=fx.WaveCharacter(wavelength=1.55e-6),
+                                     temporal_profile=scenes.pulse_5fs()))
+    objs.append(fx.PointDipoleSource(name="d2", grid_slice_tuple=((2, 3), (3, 4), (20, 21)), polarization=2,
                                      wave_character=fx.WaveCharacter(wavelength=1.55e-6),
                                      temporal_profile=scenes.pulse_5fs()))
     objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((0, 30), (0, 27), (0, 44)),
@@ -339,15 +343,11 @@ def test_zshell_tma_matches_register_shell(ty, chunk):
     objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
     assert arrays.recording_state is not None
     outs = []
-    for zs in (True, False):
+    for m in (mode, 0):
         a = arrays.reset()
         s = Scene(objects, a, cfg, record_interfaces=True)
-        if zs:
-            s.tune_zshell(True, ty, chunk)
-            assert s.uses_tma and s.uses_zshell
-        else:
-            s.tune_zshell(False)
-            assert not s.uses_zshell
+        s.tune_shell_tma(m, tz if m == 2 else 0, chunk if m else 0)
+        assert s.uses_tma and s.shell_tma == m
         s.forward(a, 0, 60)
         s.status()
         torch.cuda.synchronize()
