@@ -536,7 +536,7 @@ def bench_serving(capacity: float, n_jobs: int = 200, seed: int = 0, load: float
         arrivals.append(t)
     for j, a in zip(keep, arrivals):
         j.arrival = a
-    server = Server(budget_bytes=budget, max_slots=64, target_chunk_s=0.05)
+    server = Server(budget_bytes=budget, max_slots=64, target_chunk_s=0.05, keep_results=False)
     server.run(keep, realtime=True)
     served = latency_stats(keep)
     served_work = server.forward_cell_updates + server.adjoint_cell_updates
@@ -546,7 +546,7 @@ def bench_serving(capacity: float, n_jobs: int = 200, seed: int = 0, load: float
     for j, a in zip(keep2, arrivals):
         j.arrival = a
     t0 = time.perf_counter()
-    run_one_at_a_time(keep2, realtime=True)
+    run_one_at_a_time(keep2, realtime=True, keep_results=False)
     plain_s = time.perf_counter() - t0
     plain = latency_stats(keep2)
     return {

@@ -108,6 +108,9 @@ class Desc(C.Structure):
         ("rec_a", C.c_void_p),
         ("rec_b", C.c_void_p),
         ("rec_w", C.c_void_p),
+        ("bloch_axes", C.c_int32),
+        ("bloch_cos", C.c_float * 3),
+        ("bloch_sin", C.c_float * 3),
     ]
 
 

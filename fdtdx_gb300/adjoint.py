@@ -204,6 +204,9 @@ def reversible_fdtd(
     ctl = {"scene": scene, "arrays": work, "T": T, "bounds": bounds, "layout": layout,
            "inv_eps": work.inv_permittivities, "inv_mu": work.inv_permeabilities}
     wants = ie_in.requires_grad or (mu_t is not None and mu_t.requires_grad)
+    if wants and torch.is_grad_enabled() and scene.complex_fields:
+        raise NotImplementedError("the reversible gradient of complex (Bloch) fields is not supported by the GB300 "
+                                  "kernels (their forward and reverse steps are)")
     if not (torch.is_grad_enabled() and wants):
         _ReversibleRun.forward(_NoCtx(), ctl, work.inv_permittivities, None)
         out = work

@@ -293,6 +293,7 @@ extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjoint
         return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_adjoint)");
     if (int rc = check_bufs(p, b)) return rc;
     if (int rc = check_adj(p, adj)) return rc;
+    if (p->parts != 1) return fail(p, FDTD_EINVAL, "the reversible gradient of complex (Bloch) fields is not supported");
     if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)
         return fail(p, FDTD_EINVAL, "adjoint steps out of the range covered by the plan's tables");
     if (n_steps == 0) return FDTD_OK;

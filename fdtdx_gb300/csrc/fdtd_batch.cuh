@@ -274,6 +274,11 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     for (int s = 0; s < n; ++s) {
         FdtdPlan* p = plans[s];
         if (!p) { delete b; fprintf(stderr, "fdtd_batch_create: plan %d is NULL\n", s); return FDTD_EINVAL; }
+        if (p->parts != 1) {
+            delete b;
+            fprintf(stderr, "fdtd_batch_create: simulation %d has complex (Bloch) fields, which batches do not run\n", s);
+            return FDTD_EINVAL;
+        }
         if (int rc = check_bufs(p, &bufs[s])) {
             fprintf(stderr, "fdtd_batch_create: simulation %d: %s\n", s, p->err.c_str());
             delete b;

@@ -29,6 +29,15 @@ struct Geo {
     float c;                    // Courant number
     float eta0;                 // free-space impedance mu0*c (host-supplied)
     int pec, pmc;               // face masks, bit (2*axis + side)
+    // Bloch boundaries (complex fields, held planar: the real parts (3, N) then the imaginary
+    // parts (3, N)): bit a of `bloch` marks a Bloch axis with phase exp(i k L) = bc + i bs.
+    // A kernel works on one part; a neighbour wrapped across a Bloch axis is multiplied by the
+    // phase ('+' side) or its conjugate ('-' side), which mixes in the other part, `pother`
+    // floats away, with sign `psign` (-1 for the real part, +1 for the imaginary part).
+    int bloch;
+    float bc[3], bs[3];
+    long long pother;
+    float psign;
 };
 
 // A detector accumulated inside the H half-step: E components only, so every value
@@ -114,14 +123,34 @@ __device__ __forceinline__ long long cell_index(const Geo& g, int i, int j, int 
 // Field value at (i, j, k) with the reference's one-cell halo semantics
 // (fdtdx/core/misc.py:615-641): an out-of-range index on a periodic axis wraps,
 // otherwise the value is zero.  Only one-cell excursions are ever requested.
+// The Bloch phase of one wrap across axis a (from above: exp(i k L); from below: its
+// conjugate), composed into (cr, ci) (fdtdx/fdtd/update.py:92-136, bloch.py:59-94).
+__device__ __forceinline__ void bloch_turn(const Geo& g, int a, bool from_above, float& cr, float& ci) {
+    if (!(g.bloch >> a & 1)) return;
+    const float c = g.bc[a], s = from_above ? g.bs[a] : -g.bs[a];
+    const float r = cr * c - ci * s;
+    ci = cr * s + ci * c;
+    cr = r;
+}
+
+// A wrapped neighbour's value in this part: Re or Im of (cr + i ci) (v_re + i v_im).
+__device__ __forceinline__ float bloch_mix(const Geo& g, const float* __restrict__ f, long long off, float cr, float ci,
+                                           float v) {
+    if (ci == 0.f && cr == 1.f) return v;
+    return cr * v + g.psign * ci * __ldg(f + g.pother + off);
+}
+
 __device__ __forceinline__ float ld_halo(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k) {
-    if (i < 0) { if (!g.px) return 0.f; i += g.nx; }
-    else if (i >= g.nx) { if (!g.px) return 0.f; i -= g.nx; }
-    if (j < 0) { if (!g.py) return 0.f; j += g.ny; }
-    else if (j >= g.ny) { if (!g.py) return 0.f; j -= g.ny; }
-    if (k < 0) { if (!g.pz) return 0.f; k += g.nz; }
-    else if (k >= g.nz) { if (!g.pz) return 0.f; k -= g.nz; }
-    return __ldg(f + comp * g.N + cell_index(g, i, j, k));
+    float cr = 1.f, ci = 0.f;
+    if (i < 0) { if (!g.px) return 0.f; i += g.nx; bloch_turn(g, 0, false, cr, ci); }
+    else if (i >= g.nx) { if (!g.px) return 0.f; i -= g.nx; bloch_turn(g, 0, true, cr, ci); }
+    if (j < 0) { if (!g.py) return 0.f; j += g.ny; bloch_turn(g, 1, false, cr, ci); }
+    else if (j >= g.ny) { if (!g.py) return 0.f; j -= g.ny; bloch_turn(g, 1, true, cr, ci); }
+    if (k < 0) { if (!g.pz) return 0.f; k += g.nz; bloch_turn(g, 2, false, cr, ci); }
+    else if (k >= g.nz) { if (!g.pz) return 0.f; k -= g.nz; bloch_turn(g, 2, true, cr, ci); }
+    const long long off = comp * g.N + cell_index(g, i, j, k);
+    const float v = __ldg(f + off);
+    return g.bloch ? bloch_mix(g, f, off, cr, ci, v) : v;
 }
 
 // ld_halo without branches: the wrapped index is formed with selects and the load always
@@ -133,7 +162,15 @@ __device__ __forceinline__ float ld_halo_sel(const Geo& g, const float* __restri
     const int ii = li ? i + g.nx : (ui ? i - g.nx : i);
     const int jj = lj ? j + g.ny : (uj ? j - g.ny : j);
     const int kk = lk ? k + g.nz : (uk ? k - g.nz : k);
-    const float v = __ldg(f + comp * g.N + cell_index(g, ok ? ii : 0, ok ? jj : 0, ok ? kk : 0));
+    const long long off = comp * g.N + cell_index(g, ok ? ii : 0, ok ? jj : 0, ok ? kk : 0);
+    const float v = __ldg(f + off);
+    if (g.bloch && ok && (li || ui || lj || uj || lk || uk)) {
+        float cr = 1.f, ci = 0.f;
+        if (li || ui) bloch_turn(g, 0, ui, cr, ci);
+        if (lj || uj) bloch_turn(g, 1, uj, cr, ci);
+        if (lk || uk) bloch_turn(g, 2, uk, cr, ci);
+        return bloch_mix(g, f, off, cr, ci, v);
+    }
     return ok ? v : 0.f;
 }
 

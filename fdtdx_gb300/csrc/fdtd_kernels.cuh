@@ -782,6 +782,7 @@ struct DetFields {
     const float* inv_mu;
     int n_mu;
     float mu_scalar;
+    long long im = 0;  // complex (Bloch) fields: floats from each field's real parts to its imaginary parts
 };
 
 __device__ __forceinline__ float hav(const Geo& g, const DetFields& f, int comp, int i, int j, int k) {
@@ -853,23 +854,48 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
     }
     int need = d.comp_mask;
     if (d.kind == FDTD_DET_FLUX || d.kind == FDTD_DET_ENERGY) need = 63;
+    // complex (Bloch) fields: the imaginary parts' samples too, with the other part and sign
+    // of each wrapped neighbour's phase mixing swapped
+    float vi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     // the samples do not depend on the step: their loads are issued before the step
     // counter's and the slot table's, which then overlap them
-    if (valid) colocate(g, f, d.exact, need, i, j, k, v);
+    if (valid) {
+        colocate(g, f, d.exact, need, i, j, k, v);
+        if (f.im && d.kind != FDTD_DET_FIELD) {
+            Geo gi = g;
+            gi.pother = -f.im;
+            gi.psign = 1.f;
+            DetFields fi = f;
+            fi.E = f.E + f.im;
+            fi.Hp = f.Hp + f.im;
+            fi.H = f.H + f.im;
+            colocate(gi, fi, d.exact, need, i, j, k, vi);
+        }
+    }
     const int t = *tp;
     const int slot = __ldg(d.slot + t + 1);
     if (slot < 0) return;
 
-    // gather the recorded values of this cell
-    float out[6];
+    // gather the recorded values of this cell (outi: the imaginary parts of complex phasor
+    // samples; a field detector of complex fields records their real parts)
+    float out[6], outi[6];
     int nout = 0;
     if (d.kind == FDTD_DET_FIELD || d.kind == FDTD_DET_PHASOR) {
 #pragma unroll
         for (int q = 0; q < 6; ++q)
-            if (d.comp_mask >> q & 1) out[nout++] = v[q];
+            if (d.comp_mask >> q & 1) {
+                outi[nout] = vi[q];
+                out[nout++] = v[q];
+            }
     } else if (d.kind == FDTD_DET_FLUX) {
-        // S = E x H (real fields; fdtdx/core/physics/metrics.py:99-117)
-        const float S[3] = {v[1] * v[5] - v[2] * v[4], v[2] * v[3] - v[0] * v[5], v[0] * v[4] - v[1] * v[3]};
+        // S = E x H (real fields; fdtdx/core/physics/metrics.py:99-117); complex fields:
+        // Re(E x conj H) = E_re x H_re + E_im x H_im
+        float S[3] = {v[1] * v[5] - v[2] * v[4], v[2] * v[3] - v[0] * v[5], v[0] * v[4] - v[1] * v[3]};
+        if (f.im) {
+            S[0] += vi[1] * vi[5] - vi[2] * vi[4];
+            S[1] += vi[2] * vi[3] - vi[0] * vi[5];
+            S[2] += vi[0] * vi[4] - vi[1] * vi[3];
+        }
         if (d.keep_all) {
             out[0] = d.flux_sign * S[0];
             out[1] = d.flux_sign * S[1];
@@ -885,8 +911,9 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
             const long long c = cell_index(g, i, j, k);
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                e += 0.5f * (1.f / mat_at(f.inv_eps, f.n_eps, 1.f, g.N, q, c)) * (v[q] * v[q]);
-                h += 0.5f * (1.f / mat_at(f.inv_mu, f.n_mu, f.mu_scalar, g.N, q, c)) * (v[3 + q] * v[3 + q]);
+                e += 0.5f * (1.f / mat_at(f.inv_eps, f.n_eps, 1.f, g.N, q, c)) * (v[q] * v[q] + vi[q] * vi[q]);
+                h += 0.5f * (1.f / mat_at(f.inv_mu, f.n_mu, f.mu_scalar, g.N, q, c)) *
+                     (v[3 + q] * v[3 + q] + vi[3 + q] * vi[3 + q]);
             }
         }
         out[0] = e + h;
@@ -903,8 +930,11 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
                 for (int q = 0; q < nout; ++q) {
                     float2* p = st + ((long long)fq * nout + q) * d.R + r;
                     float2 z = *p;
-                    if (d.inverse) { z.x -= out[q] * w.x; z.y -= out[q] * w.y; }
-                    else { z.x += out[q] * w.x; z.y += out[q] * w.y; }
+                    // the sample (out + i outi) times the weight
+                    const float ar = f.im ? out[q] * w.x - outi[q] * w.y : out[q] * w.x;
+                    const float ai = f.im ? out[q] * w.y + outi[q] * w.x : out[q] * w.y;
+                    if (d.inverse) { z.x -= ar; z.y -= ai; }
+                    else { z.x += ar; z.y += ai; }
                     *p = z;
                 }
             }
@@ -914,8 +944,10 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
         for (int fq = 0; fq < d.nfreq; ++fq) {
             const float2 w = __ldg(wt + fq);
             for (int q = 0; q < nout; ++q) {
-                const float re = block_sum<kDetBlock>(valid ? out[q] * w.x : 0.f, sh);
-                const float im = block_sum<kDetBlock>(valid ? out[q] * w.y : 0.f, sh);
+                const float ar = f.im ? out[q] * w.x - outi[q] * w.y : out[q] * w.x;
+                const float ai = f.im ? out[q] * w.y + outi[q] * w.x : out[q] * w.y;
+                const float re = block_sum<kDetBlock>(valid ? ar : 0.f, sh);
+                const float im = block_sum<kDetBlock>(valid ? ai : 0.f, sh);
                 if (threadIdx.x == 0) {
                     d.partial[(long long)blk * d.ncomp + 2 * (fq * nout + q)] = re;
                     d.partial[(long long)blk * d.ncomp + 2 * (fq * nout + q) + 1] = im;

@@ -32,6 +32,7 @@ struct FdtdPlan {
     int* d_t = nullptr;          // device time-step counter read by every kernel
     float* h_twin = nullptr;     // second H buffer (ping-pong) when a detector needs H before the H update
     bool need_hprev = false;
+    int parts = 1;               // 2 for complex (Bloch) fields: real parts, then imaginary parts
     bool fused[FDTD_MAX_DETECTORS] = {};  // accumulated inside the H half-step
     int n_fused = 0;
     int chunk = 1;                        // x planes per update block
@@ -306,6 +307,13 @@ int validate(const FdtdDesc* d, std::string& why) {
         if (dd.kind == FDTD_DET_FLUX && (dd.flux_axis < 0 || dd.flux_axis > 2)) { why = "invalid flux axis"; return FDTD_EINVAL; }
     }
     if (d->recording_dtype < 0 || d->recording_dtype > 2) { why = "invalid recording dtype"; return FDTD_EINVAL; }
+    if (d->bloch_axes & ~7) { why = "bloch_axes holds bits beyond the three axes"; return FDTD_EINVAL; }
+    for (int a = 0; a < 3; ++a)
+        if ((d->bloch_axes >> a & 1) && !d->periodic[a]) { why = "a Bloch axis must be periodic"; return FDTD_EINVAL; }
+    if (d->bloch_axes && d->recording_dtype != 0) {
+        why = "complex (Bloch) interface recordings are stored in float32 only";
+        return FDTD_EINVAL;
+    }
     return FDTD_OK;
 }
 
@@ -511,6 +519,11 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     p->g.c = d.courant;
     p->g.eta0 = (float)(4e-7 * M_PI * 299792458.0);
     p->g.pec = d.pec_faces; p->g.pmc = d.pmc_faces;
+    p->g.bloch = d.bloch_axes;
+    for (int a = 0; a < 3; ++a) { p->g.bc[a] = d.bloch_cos[a]; p->g.bs[a] = d.bloch_sin[a]; }
+    p->g.pother = 3 * p->g.N;
+    p->g.psign = -1.f;
+    p->parts = d.bloch_axes ? 2 : 1;
     {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -550,7 +563,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         const long long nb = (R + kDetBlock - 1) / kDetBlock;
         const bool red = dd.reduce_volume || dd.kind == FDTD_DET_PHASOR ? dd.reduce_volume : dd.reduce_volume;
         o.partial = red ? ar.take(4 * (size_t)nb * det_ncomp(dd)) : 0;
-        if (det_fusable(dd) && p->n_fused < kMaxFuse) {
+        if (det_fusable(dd) && p->n_fused < kMaxFuse && p->parts == 1) {
             p->fused[q] = true;
             ++p->n_fused;
         } else if (det_needs_h(dd)) {
@@ -558,7 +571,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         }
     }
     size_t o_twin = 0;
-    if (p->need_hprev) o_twin = ar.take(sizeof(float) * 3 * (size_t)p->g.N);
+    if (p->need_hprev) o_twin = ar.take(sizeof(float) * 3 * (size_t)p->parts * (size_t)p->g.N);
     size_t o_rec[4] = {0, 0, 0, 0};
     if (d.rec_slots > 0)
         for (int q = 0; q < 4; ++q) o_rec[q] = ar.take(4 * tbl);
@@ -570,13 +583,24 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         fprintf(stderr, "fdtd_plan_create: cudaMalloc(%zu) failed: %s\n", ar.off, cudaGetErrorString(e));
         return FDTD_ENOMEM;
     }
+    // the tables go up on a private non-blocking stream, synchronised alone: no device-wide
+    // wait and no legacy-stream work, so a plan can be built on one host thread while another
+    // captures a CUDA graph (the serving loop places jobs beside the running batch)
+    cudaStream_t up_st = nullptr;
+    e = cudaStreamCreateWithFlags(&up_st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaFree(p->dmem);
+        delete p;
+        fprintf(stderr, "fdtd_plan_create: cudaStreamCreate: %s\n", cudaGetErrorString(e));
+        return FDTD_ECUDA;
+    }
     auto up = [&](size_t off, const void* src, size_t bytes) -> cudaError_t {
         if (!bytes) return cudaSuccess;
-        return cudaMemcpy(p->dmem + off, src, bytes, cudaMemcpyHostToDevice);
+        return cudaMemcpyAsync(p->dmem + off, src, bytes, cudaMemcpyHostToDevice, up_st);
     };
     p->d_t = reinterpret_cast<int*>(p->dmem + o_t);
     p->d_err = p->d_t + 1;
-    e = cudaMemset(p->d_t, 0, sizeof(int) * 4);
+    e = cudaMemsetAsync(p->d_t, 0, sizeof(int) * 4, up_st);
 
     const int n3[3] = {d.nx, d.ny, d.nz};
     for (int s = 0; s < d.n_slabs && e == cudaSuccess; ++s) {
@@ -664,7 +688,8 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         p->ifc.rb = reinterpret_cast<const int*>(p->dmem + o_rec[2]);
         p->ifc.rw = reinterpret_cast<const float*>(p->dmem + o_rec[3]);
     }
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(up_st);
+    cudaStreamDestroy(up_st);
     if (e != cudaSuccess) {
         fprintf(stderr, "fdtd_plan_create: %s\n", cudaGetErrorString(e));
         cudaFree(p->dmem);
@@ -911,12 +936,20 @@ void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) { launch_hal
 template <bool REV>
 void launch_H(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) { launch_half<REV, true>(p, a, st); }
 
-UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout) {
+// The arguments of one half-step; `part` 1 selects the imaginary parts of complex (Bloch)
+// fields (planar buffers: the real parts, then the imaginary parts).
+UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout,
+                 int part = 0) {
     UpdArgs a{};
     a.g = p->g;
-    a.F = F;
-    a.Uin = Uin;
-    a.Uout = Uout;
+    const long long po = part ? 3 * p->g.N : 0;
+    a.F = F + po;
+    a.Uin = Uin + po;
+    a.Uout = Uout + po;
+    if (part) {
+        a.g.pother = -3 * p->g.N;
+        a.g.psign = 1.f;
+    }
     if (eside) {
         a.mat = b->inv_eps; a.n_mat = p->d.n_eps; a.mat_scalar = 1.f;
         a.sig = p->d.n_sigma_E ? b->sigma_E : nullptr; a.n_sig = p->d.n_sigma_E;
@@ -927,8 +960,9 @@ UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const floa
     a.n_slab = p->d.n_slabs;
     for (int s = 0; s < p->d.n_slabs; ++s) {
         a.slab[s] = p->slab[s];
-        a.psi1[s] = eside ? b->psi_E[s][0] : b->psi_H[s][0];
-        a.psi2[s] = eside ? b->psi_E[s][1] : b->psi_H[s][1];
+        const long long ps = part ? (long long)p->slab[s].sx * p->slab[s].sy * p->slab[s].sz : 0;
+        a.psi1[s] = (eside ? b->psi_E[s][0] : b->psi_H[s][0]) + ps;
+        a.psi2[s] = (eside ? b->psi_E[s][1] : b->psi_H[s][1]) + ps;
     }
     // per-axis slab table: one slab per face, the two slabs of an axis disjoint
     a.axt = 1;
@@ -1000,8 +1034,11 @@ int sources_launched(const FdtdPlan* p, bool eside) {
 template <typename T, bool RESTORE>
 void launch_ifaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t st) {
     const int blocks = (int)((p->ifc.total + 255) / 256);
-    k_interfaces<T, RESTORE><<<blocks, 256, 0, st>>>(p->g, p->ifc, p->d_t, rec_rows(p->d), b->E, H,
-                                                     reinterpret_cast<T*>(b->recording));
+    // complex fields: the imaginary parts' planes go to a second recording after the first
+    const long long fo = 3 * p->g.N, ro = (long long)rec_rows(p->d) * 6 * p->ifc.total;
+    for (int part = 0; part < p->parts; ++part)
+        k_interfaces<T, RESTORE><<<blocks, 256, 0, st>>>(p->g, p->ifc, p->d_t, rec_rows(p->d), b->E + part * fo,
+                                                         H + part * fo, reinterpret_cast<T*>(b->recording) + part * ro);
 }
 
 template <bool RESTORE>
@@ -1012,16 +1049,26 @@ void interfaces(const FdtdPlan* p, const FdtdBuffers* b, float* H, cudaStream_t 
     else launch_ifaces<__half, RESTORE>(p, b, H, st);
 }
 
+// The detector inputs: the fields (with the imaginary parts' offset when they are complex) and
+// the materials.
+DetFields det_fields(const FdtdPlan* p, const FdtdBuffers* b, const float* Hprev, const float* H) {
+    DetFields f{b->E, Hprev, H, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
+                p->d.inv_mu_scalar};
+    f.im = p->parts == 2 ? 3 * p->g.N : 0;
+    return f;
+}
+
 // One forward step (fdtdx/fdtd/forward.py:83-156): update_E, E sources (+PEC inside the
 // update), update_H, H sources (+PMC), interface recording, detectors, advance t.
 void launch_forward_step(const FdtdPlan* p, const FdtdBuffers* b, float* Hcur, float* Hnext, cudaStream_t st) {
-    launch_E<false>(p, make_upd(p, b, true, Hcur, b->E, b->E), st);
-    launch_sources(p, b, true, b->E, 0, st);
-    launch_H<false>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st);
+    for (int part = 0; part < p->parts; ++part) launch_E<false>(p, make_upd(p, b, true, Hcur, b->E, b->E, part), st);
+    launch_sources(p, b, true, b->E, 0, st);  // sources are real: they drive the real parts
+    if (p->parts == 1) launch_H<false>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st);
+    else
+        for (int part = 0; part < p->parts; ++part) launch_H<false>(p, make_upd(p, b, false, b->E, Hcur, Hnext, part), st);
     launch_sources(p, b, false, Hnext, 0, st);
     if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
-    DetFields f{b->E, Hcur, Hnext, b->inv_eps, p->d.n_eps, p->d.n_mu ? b->inv_mu : nullptr, p->d.n_mu ? p->d.n_mu : 1,
-                p->d.inv_mu_scalar};
+    const DetFields f = det_fields(p, b, Hcur, Hnext);
     for (int q = 0; q < p->d.n_detectors; ++q) {
         if (p->fused[q]) continue;
         const DDet& dd = p->det[q];
@@ -1055,8 +1102,8 @@ extern "C" {
 
 int32_t fdtd_launches_per_step(const FdtdPlan* p) {
     if (!p) return 0;
-    int n = 2 * half_step_launches(p) + sources_launched(p, true) + sources_launched(p, false) + 1;
-    if (p->d.record_interfaces && p->d.n_slabs) n += 1;
+    int n = 2 * p->parts * half_step_launches(p) + sources_launched(p, true) + sources_launched(p, false) + 1;
+    if (p->d.record_interfaces && p->d.n_slabs) n += p->parts;
     for (int q = 0; q < p->d.n_detectors; ++q)
         if (!p->fused[q]) n += p->det[q].reduce ? 2 : 1;
     return n;
@@ -1116,13 +1163,14 @@ int fdtd_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps,
         if (p->need_hprev) std::swap(Hcur, Hnext);
     }
     if (p->need_hprev && Hcur != b->H) {
-        cudaError_t e = cudaMemcpyAsync(b->H, Hcur, sizeof(float) * 3 * p->g.N, cudaMemcpyDeviceToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(b->H, Hcur, sizeof(float) * 3 * p->parts * p->g.N, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return cuda_fail(p, e, "cudaMemcpyAsync");
     }
     if (flags & FDTD_FWD_CHECK_FINITE) {
-        const int blocks = std::max(1, std::min(p->sm_count * 8, (int)((3 * p->g.N + 255) / 256)));
-        k_check_finite<<<blocks, 256, 0, st>>>(b->E, 3 * p->g.N, p->d_err);
-        k_check_finite<<<blocks, 256, 0, st>>>(b->H, 3 * p->g.N, p->d_err);
+        const long long n = 3 * p->parts * p->g.N;
+        const int blocks = std::max(1, std::min(p->sm_count * 8, (int)((n + 255) / 256)));
+        k_check_finite<<<blocks, 256, 0, st>>>(b->E, n, p->d_err);
+        k_check_finite<<<blocks, 256, 0, st>>>(b->H, n, p->d_err);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_forward launch");
@@ -1147,9 +1195,9 @@ int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_ste
     for (int s = 0; s < n_steps; ++s) {
         interfaces<true>(p, b, b->H, st);
         launch_sources(p, b, false, b->H, 1, st);
-        launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H), st);
+        for (int part = 0; part < p->parts; ++part) launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H, part), st);
         launch_sources(p, b, true, b->E, 1, st);
-        launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E), st);
+        for (int part = 0; part < p->parts; ++part) launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E, part), st);
         k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
     }
     cudaError_t e = cudaGetLastError();
@@ -1160,12 +1208,13 @@ int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_ste
 int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
     if (!d) return -1;
     const long long N = (long long)d->nx * d->ny * d->nz;
-    long long bytes = 4ll * N * (3 + 3 + d->n_eps + d->n_mu + d->n_sigma_E + d->n_sigma_H);
+    const int parts = d->bloch_axes ? 2 : 1;
+    long long bytes = 4ll * N * (3 * parts + 3 * parts + d->n_eps + d->n_mu + d->n_sigma_E + d->n_sigma_H);
     const int n3[3] = {d->nx, d->ny, d->nz};
     long long iface = 0, psi = 0;
     for (int s = 0; s < d->n_slabs; ++s) {
         const FdtdSlabDesc& sl = d->slabs[s];
-        psi += 4ll * 4 * (N / n3[sl.axis]) * sl.thickness;  // psi_E and psi_H pairs
+        psi += 4ll * 4 * parts * (N / n3[sl.axis]) * sl.thickness;  // psi_E and psi_H pairs
         iface += N / n3[sl.axis];
     }
     bytes += psi;
@@ -1186,8 +1235,8 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
         else bytes += 4ll * on * (dd.keep_all ? 3 : 1) * (dd.reduce_volume ? 1 : R);
         if (det_needs_h(dd)) hprev = true;
     }
-    if (hprev) bytes += 12ll * N;
-    if (d->record_interfaces) bytes += (long long)rec_elem_bytes(d->recording_dtype) * 6 * iface * rec_rows(*d);
+    if (hprev) bytes += 12ll * parts * N;
+    if (d->record_interfaces) bytes += (long long)rec_elem_bytes(d->recording_dtype) * 6 * parts * iface * rec_rows(*d);
     bytes += 1ll << 20;  // tables and scratch
     return bytes;
 }
@@ -1198,6 +1247,7 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
 
 extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, float* out_ms,
                                     void* stream) {
+    if (p && p->parts != 1) return fail(p, FDTD_EINVAL, "per-launch profiling of complex (Bloch) fields is not supported");
     if (!p || !out_ms) return FDTD_EINVAL;
     if (int rc = check_bufs(p, b)) return rc;
     if (n_steps <= 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)

@@ -392,18 +392,28 @@ class Scene:
             raise NotImplementedError("dispersive (ADE) materials are not supported by the GB300 kernels")
         d.n_sigma_E = arrays.electric_conductivity.shape[0] if arrays.electric_conductivity is not None else 0
         d.n_sigma_H = arrays.magnetic_conductivity.shape[0] if arrays.magnetic_conductivity is not None else 0
+        bloch: dict[int, list] = {}
         for b in objects.boundary_objects:
             side = 1 if b.direction == "+" else 0
             if isinstance(b, PeriodicBoundary):
-                if b.needs_complex_fields:
-                    raise NotImplementedError(
-                        f"Bloch boundary '{b.name}' has a non-zero Bloch vector along its axis; that needs complex "
-                        "fields, which the GB300 kernels do not carry (a zero vector runs as a periodic boundary)")
                 d.periodic[b.axis] = 1
+                if b.needs_complex_fields:
+                    bloch.setdefault(b.axis, []).append(b)
             elif isinstance(b, PerfectElectricConductor):
                 d.pec_faces |= 1 << (2 * b.axis + side)
             elif isinstance(b, PerfectMagneticConductor):
                 d.pmc_faces |= 1 << (2 * b.axis + side)
+        # Bloch axes (bloch.py:59-94): the '+' ghost layer times exp(i k L), the '-' one times its
+        # conjugate; the kernels carry the phase per axis, so both faces must carry the same one
+        for ax, objs in bloch.items():
+            phases = {o.direction: o.get_bloch_phase(shape, config.uniform_spacing()) for o in objs}
+            if set(phases) != {"-", "+"} or abs(phases["-"] - phases["+"]) > 1e-12:
+                raise NotImplementedError(f"axis {ax}: a Bloch phase must be set on both faces with the same vector")
+            d.bloch_axes |= 1 << ax
+            d.bloch_cos[ax] = phases["+"].real
+            d.bloch_sin[ax] = phases["+"].imag
+        self.complex_fields = d.bloch_axes != 0
+        self._planar = None
         self.pmls: list[PerfectlyMatchedLayer] = objects.pml_objects
         if len(self.pmls) > N.MAX_SLABS:
             raise ValueError("at most six PML slabs")
@@ -526,9 +536,16 @@ class Scene:
         N.check(N.load().fdtd_plan_status(self.plan), self.plan, "fdtd_plan_status")
 
     # ---- buffers
+    def _workspace(self, arrays: ArrayContainer) -> "PlanarFields":
+        if self._planar is None or not self._planar.fits(arrays):
+            self._planar = PlanarFields(arrays, self.pmls)
+        return self._planar
+
     def buffers(self, arrays: ArrayContainer) -> N.Buffers:
         b = N.Buffers()
         f = arrays.fields
+        if self.complex_fields:
+            return self._complex_buffers(arrays)
         for t in (f.E, f.H, arrays.inv_permittivities):
             if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
                 raise ValueError("fields and materials must be contiguous float32 CUDA tensors")
@@ -548,25 +565,69 @@ class Scene:
             b.recording = N.ptr(arrays.recording_state.data["interfaces"])
         return b
 
+    def _complex_buffers(self, arrays: ArrayContainer) -> N.Buffers:
+        """Native buffers of a complex (Bloch) scene: the planar workspace's fields, psi and
+        recording (real parts, then imaginary parts), the container's materials and states."""
+        for t in (arrays.fields.E, arrays.fields.H, arrays.inv_permittivities):
+            if not (t.is_cuda and t.is_contiguous()):
+                raise ValueError("fields and materials must be contiguous CUDA tensors")
+        ws = self._workspace(arrays)
+        b = N.Buffers()
+        b.E, b.H = N.ptr(ws.E), N.ptr(ws.H)
+        b.inv_eps = N.ptr(arrays.inv_permittivities)
+        mu = arrays.inv_permeabilities
+        b.inv_mu = N.ptr(mu) if isinstance(mu, torch.Tensor) else None
+        b.sigma_E = N.ptr(arrays.electric_conductivity)
+        b.sigma_H = N.ptr(arrays.magnetic_conductivity)
+        for s, p in enumerate(self.pmls):
+            b.psi_E[s][0], b.psi_E[s][1] = N.ptr(ws.psi_E[p.name][0]), N.ptr(ws.psi_E[p.name][1])
+            b.psi_H[s][0], b.psi_H[s][1] = N.ptr(ws.psi_H[p.name][0]), N.ptr(ws.psi_H[p.name][1])
+        for q, det in enumerate(self.detectors):
+            b.det_state[q] = N.ptr(next(iter(arrays.detector_states[det.name].values())))
+        if ws.rec is not None:
+            b.recording = N.ptr(ws.rec)
+        return b
+
+    def _run(self, arrays: ArrayContainer, call) -> None:
+        """Runs a native call on the container's buffers (complex fields staged through the
+        planar workspace and written back)."""
+        if not self.complex_fields:
+            call(self.buffers(arrays))
+            return
+        b = self.buffers(arrays)
+        ws = self._workspace(arrays)
+        ws.load(arrays)
+        call(b)
+        ws.store(arrays)
+
     def forward(self, arrays: ArrayContainer, t0: int, n_steps: int, graph: bool = True, stream=None,
                 check_finite: bool = False) -> None:
         """Forward steps t0 .. t0+n_steps-1 in place.  ``check_finite`` scans E and H once after
         the last step; ``status()`` then raises ``NativeError`` (FDTD_ENONFINITE) when either
         holds a NaN or an infinity."""
         st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
-        b = self.buffers(arrays)
         flags = (N.FWD_GRAPH if graph else 0) | (N.FWD_CHECK_FINITE if check_finite else 0)
-        rc = N.load().fdtd_forward(self.plan, C.byref(b), int(t0), int(n_steps), flags,
-                                   C.c_void_p(st.cuda_stream))
-        N.check(rc, self.plan, "fdtd_forward")
+
+        def call(b):
+            rc = N.load().fdtd_forward(self.plan, C.byref(b), int(t0), int(n_steps), flags, C.c_void_p(st.cuda_stream))
+            N.check(rc, self.plan, "fdtd_forward")
+
+        with torch.cuda.stream(st):
+            self._run(arrays, call)
 
     def reverse(self, arrays: ArrayContainer, t_end: int, n_steps: int, stream=None) -> None:
         st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
-        b = self.buffers(arrays)
-        rc = N.load().fdtd_reverse(self.plan, C.byref(b), int(t_end), int(n_steps), C.c_void_p(st.cuda_stream))
-        N.check(rc, self.plan, "fdtd_reverse")
+
+        def call(b):
+            rc = N.load().fdtd_reverse(self.plan, C.byref(b), int(t_end), int(n_steps), C.c_void_p(st.cuda_stream))
+            N.check(rc, self.plan, "fdtd_reverse")
+
+        with torch.cuda.stream(st):
+            self._run(arrays, call)
 
     def adjoint(self, arrays: ArrayContainer, lam: dict, t_end: int, n_steps: int, stream=None) -> None:
+        if self.complex_fields:
+            raise NotImplementedError("the reversible gradient of complex (Bloch) fields is not supported")
         """Backward loop of the reversible gradient on the native path (``fdtd_adjoint``).
 
         ``arrays`` holds the forward state at ``t_end`` and is reconstructed in place down to
@@ -597,3 +658,58 @@ class Scene:
         rc = N.load().fdtd_adjoint(self.plan, C.byref(b), C.byref(a), int(t_end), int(n_steps),
                                    C.c_void_p(st.cuda_stream))
         N.check(rc, self.plan, "fdtd_adjoint")
+
+
+class PlanarFields:
+    """The planar float32 workspace of a complex (Bloch) scene's state: E, H, the psi pairs and
+    the interface recording as (2, ...) tensors, real parts first.  The native kernels work on
+    one part at a time; ``load`` / ``store`` copy from / into the container's complex tensors."""
+
+    def __init__(self, arrays: ArrayContainer, pmls):
+        f = arrays.fields
+        self.shapes = self._key(arrays)
+        dev = f.E.device
+        self.E = torch.empty((2, *f.E.shape), dtype=torch.float32, device=dev)
+        self.H = torch.empty((2, *f.H.shape), dtype=torch.float32, device=dev)
+        self.psi_E = {p.name: tuple(torch.empty((2, *t.shape), dtype=torch.float32, device=dev) for t in f.psi_E[p.name])
+                      for p in pmls}
+        self.psi_H = {p.name: tuple(torch.empty((2, *t.shape), dtype=torch.float32, device=dev) for t in f.psi_H[p.name])
+                      for p in pmls}
+        rec = arrays.recording_state
+        self.rec = None
+        if rec is not None:
+            r = rec.data["interfaces"]
+            self.rec = torch.empty((2, *r.shape), dtype=torch.float32, device=dev)
+
+    @staticmethod
+    def _key(arrays: ArrayContainer):
+        f = arrays.fields
+        rec = arrays.recording_state
+        return (tuple(f.E.shape), tuple((k, tuple(a.shape)) for k, (a, _b) in f.psi_E.items()),
+                None if rec is None else tuple(rec.data["interfaces"].shape))
+
+    def fits(self, arrays: ArrayContainer) -> bool:
+        return self._key(arrays) == self.shapes
+
+    def _pairs(self, arrays: ArrayContainer):
+        f = arrays.fields
+        out = [(f.E, self.E), (f.H, self.H)]
+        for k in self.psi_E:
+            out += list(zip(f.psi_E[k], self.psi_E[k])) + list(zip(f.psi_H[k], self.psi_H[k]))
+        if self.rec is not None:
+            out.append((arrays.recording_state.data["interfaces"], self.rec))
+        return out
+
+    def load(self, arrays: ArrayContainer) -> None:
+        for c, w in self._pairs(arrays):
+            if not c.is_complex():
+                raise ValueError("a scene with a Bloch phase needs complex fields (place it with place_objects)")
+            r = torch.view_as_real(c)
+            w[0].copy_(r[..., 0])
+            w[1].copy_(r[..., 1])
+
+    def store(self, arrays: ArrayContainer) -> None:
+        for c, w in self._pairs(arrays):
+            r = torch.view_as_real(c)
+            r[..., 0].copy_(w[0])
+            r[..., 1].copy_(w[1])

@@ -76,12 +76,16 @@ def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None)
     device = torch.device(device) if device is not None else _default_device()
     shape = objects.volume.grid_shape
     N3 = (3, *shape)
-    E = torch.zeros(N3, dtype=torch.float32, device=device)
-    H = torch.zeros(N3, dtype=torch.float32, device=device)
-    psi_E = {p.name: (torch.zeros(p.grid_shape, device=device), torch.zeros(p.grid_shape, device=device))
-             for p in objects.pml_objects}
-    psi_H = {p.name: (torch.zeros(p.grid_shape, device=device), torch.zeros(p.grid_shape, device=device))
-             for p in objects.pml_objects}
+    # complex fields exactly when a Bloch boundary carries a non-zero vector component
+    # (fdtdx/fdtd/initialization.py:581-594)
+    complex_fields = any(getattr(b, "needs_complex_fields", False) for b in objects.boundary_objects)
+    fdt = torch.complex64 if complex_fields else torch.float32
+    E = torch.zeros(N3, dtype=fdt, device=device)
+    H = torch.zeros(N3, dtype=fdt, device=device)
+    psi_E = {p.name: (torch.zeros(p.grid_shape, dtype=fdt, device=device),
+                      torch.zeros(p.grid_shape, dtype=fdt, device=device)) for p in objects.pml_objects}
+    psi_H = {p.name: (torch.zeros(p.grid_shape, dtype=fdt, device=device),
+                      torch.zeros(p.grid_shape, dtype=fdt, device=device)) for p in objects.pml_objects}
 
     vol = objects.volume
     bg = vol.material if vol.material is not None else Material()
@@ -128,8 +132,12 @@ def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None)
     gc = config.gradient_config
     if gc is not None and gc.recorder is not None:
         per_step = 6 * sum(int(torch.tensor(p.grid_shape).prod()) // p.thickness for p in objects.pml_objects)
-        data = torch.zeros((gc.recorder.slots(config.time_steps_total), per_step), dtype=gc.recorder.storage_dtype,
-                           device=device)
+        rdt = gc.recorder.storage_dtype
+        if complex_fields:
+            if rdt != torch.float32:
+                raise NotImplementedError("complex (Bloch) fields are recorded in float32 only")
+            rdt = torch.complex64
+        data = torch.zeros((gc.recorder.slots(config.time_steps_total), per_step), dtype=rdt, device=device)
         rec = RecordingState(data={"interfaces": data})
 
     return ArrayContainer(

@@ -209,8 +209,11 @@ class Server:
     """The GPU serving loop over a list of timed jobs (``Job.arrival`` in seconds)."""
 
     def __init__(self, budget_bytes: int = 160 * 10**9, max_slots: int = 64, target_chunk_s: float = 0.05,
-                 autotune: bool = True, adjoint_lanes: int = 4):
+                 autotune: bool = True, adjoint_lanes: int = 4, keep_results: bool = True):
+        """``keep_results=False`` returns each finished job's detector states on the host (in
+        ``Job.detectors``) and frees its device state, as a service answering many requests does."""
         self.sched = Scheduler(budget_bytes, max_slots)
+        self.keep_results = keep_results
         self.adjoint_lanes = max(1, int(adjoint_lanes))
         self.target = float(target_chunk_s)
         self.autotune = autotune
@@ -330,11 +333,14 @@ class Server:
     def _finish(self, job: Job, now: float) -> None:
         job.scene.status()
         if job.kind == "gradient":
-            job.grad = job.lam["grad_inv_eps"]
+            job.grad = job.lam["grad_inv_eps"] if self.keep_results else job.lam["grad_inv_eps"].cpu()
             job.lam = None
             job.state = None  # reconstructed back to the start: nothing to return
-        else:
+        elif self.keep_results:
             job.result = job.state
+        else:
+            job.detectors = {n: {k: v.detach().cpu() for k, v in st.items()} for n, st in job.state.detector_states.items()}
+            job.state = None
         job.scene.close()
         job.scene = None
         job.arrays = None
@@ -526,8 +532,9 @@ class Server:
             self._finish(job, now)
 
 
-def run_one_at_a_time(jobs: list[Job], realtime: bool = True) -> list[Job]:
-    """The plain path: each job alone through run_fdtd / reversible_fdtd, in arrival order."""
+def run_one_at_a_time(jobs: list[Job], realtime: bool = True, keep_results: bool = True) -> list[Job]:
+    """The plain path: each job alone through run_fdtd / reversible_fdtd, in arrival order.
+    ``keep_results=False`` keeps only the host copies of the detector states (and gradients)."""
     from fdtdx_gb300.adjoint import reversible_fdtd
     from fdtdx_gb300.fdtd import run_fdtd
 
@@ -550,12 +557,23 @@ def run_one_at_a_time(jobs: list[Job], realtime: bool = True) -> list[Job]:
             (g,) = torch.autograd.grad(loss, [ie])
             j.grad, j.loss_value = g.detach(), float(loss.detach())
             j.detectors = {dn: {k: v.detach().clone() for k, v in st.items()} for dn, st in out.detector_states.items()}
+            if not keep_results:
+                j.grad = j.grad.cpu()
+                j.detectors = {dn: {k: v.cpu() for k, v in st.items()} for dn, st in j.detectors.items()}
+            del out, ie, g, loss
         else:
-            _, j.result = run_fdtd(arrays, objects, config)
+            _, res = run_fdtd(arrays, objects, config)
+            if keep_results:
+                j.result = res
+            else:
+                j.detectors = {dn: {k: v.detach().cpu() for k, v in st.items()} for dn, st in res.detector_states.items()}
+            del res
         torch.cuda.synchronize()
         j.t_done = time.perf_counter() - t0
         j.phase = "done"
         del objects, arrays
+        if not keep_results and j.footprint > 2**30:
+            torch.cuda.empty_cache()
     return jobs
 
 

@@ -147,6 +147,15 @@ typedef struct {
     const int32_t* rec_a;
     const int32_t* rec_b;
     const float* rec_w;
+    /* Bloch boundaries with a non-zero vector (fdtdx/objects/boundaries/bloch.py:13-155): bit a
+     * set when the (periodic) axis a carries the phase exp(i k_a L_a) = bloch_cos[a] + i
+     * bloch_sin[a] on its '+' ghost layer (its conjugate on the '-' one).  The fields are then
+     * complex: E, H, every psi array, the H twin and the interface recording hold their real
+     * parts followed by their imaginary parts (planar, a leading dimension of 2); detector states
+     * keep their layouts (phasors complex, the rest real).  Forward and reverse steps only. */
+    int32_t bloch_axes;
+    float bloch_cos[3];
+    float bloch_sin[3];
 } FdtdDesc;
 
 typedef struct {

@@ -147,7 +147,7 @@ def test_serving_cancellation_and_divergence_are_isolated():
     assert [j.phase for j in jobs] == ["done", "done", "cancelled", "failed", "cancelled"]
     assert "NaN" in jobs[3].error or "infinity" in jobs[3].error
     assert seen["snap"]["E"].shape == (3, 40, 36, 32) and 0 < seen["snap"]["t"] <= 400
-    assert jobs[2].result is None and jobs[4].t_admit != jobs[4].t_admit  # never admitted (NaN)
+    assert jobs[2].result is None and jobs[4].result is None
     assert server.sched.used == 0
     alone = run_one_at_a_time(mix()[:2], realtime=False)
     assert rel_l2(jobs[0].result.fields.E, alone[0].result.fields.E) <= 1e-5

@@ -1,8 +1,6 @@
 """Bloch boundaries on the oracle (CPU): complex fields with a phase on the wrap halo.
 
-The GB300 kernels carry real fields only, so the library runs a Bloch boundary with a zero
-vector as a periodic one and refuses a non-zero vector; the oracle states the complex path
-so that a kernel for it has its checker ready.  Pins:
+The oracle states the complex path (the checker of the GPU kernels' complex fields).  Pins:
 
 * the phase exp(i k L) of the boundary's axis component, unit magnitude, one at k = 0
   (tests/unit/objects/boundaries/test_bloch.py:109-206), and the ghost layers of the padded
@@ -20,7 +18,9 @@ so that a kernel for it has its checker ready.  Pins:
   oracle gives 0.851);
 * the reversible gradient on complex fields equals autograd through the complex run
   (float64, rel 1e-9), finite and non-zero (test_time_reversal.py:687-800);
-* the library refuses a non-zero Bloch vector before any device work.
+* the library builds the complex description of a non-zero Bloch vector and refuses the
+  reversible gradient of such a scene before any device work (its forward and reverse steps
+  run on the GPU: tests/test_gpu_bloch.py).
 """
 
 import cmath
@@ -174,12 +174,25 @@ def test_bloch_oblique_fresnel_te():
     assert abs(s1 / s0 - t_ref) / t_ref < 0.05, (s1 / s0, t_ref)
 
 
-def test_library_refuses_a_nonzero_bloch_vector():
-    """The GB300 path has no complex fields: a non-zero Bloch vector along a Bloch boundary's
-    axis is refused before any device work; a zero one runs as periodic."""
-    objects, arrays, cfg, _ = _scene({f: "bloch" for f in FACES[:2]}, (1e6, 0.0, 0.0))
+def test_library_bloch_description_and_gradient_refusal():
+    """A non-zero Bloch vector gives complex fields (the container's E, H and psi are
+    complex64) and a plan description with the axis' phase exp(i k L) on the '+' ghost; the
+    reversible gradient of such a scene is refused before any device work."""
+    from fdtdx_gb300.engine import Scene
+
+    kv = (1e6, 0.0, 0.0)
+    objects, arrays, cfg, sc = _scene({f: "bloch" for f in FACES[:2]}, kv)
+    assert arrays.fields.E.dtype == torch.complex64 and arrays.fields.H.dtype == torch.complex64
+    assert all(t.dtype == torch.complex64 for pair in arrays.fields.psi_E.values() for t in pair)
+    scene = Scene(objects, arrays, cfg)
+    d = scene.desc
+    ph = cmath.exp(1j * kv[0] * sc.shape[0] * sc.dx)
+    assert scene.complex_fields and d.bloch_axes == 1 and d.periodic[0] == 1
+    assert abs(d.bloch_cos[0] - ph.real) < 1e-7 and abs(d.bloch_sin[0] - ph.imag) < 1e-7
+    objects, arrays, cfg, _ = _scene({f: "bloch" for f in FACES[:2]}, kv, record=True)
+    ie = arrays.inv_permittivities.clone().requires_grad_(True)
     with pytest.raises(NotImplementedError, match="complex"):
-        fx.run_fdtd(arrays, objects, cfg)
+        fx.reversible_fdtd(arrays.aset("inv_permittivities", ie), objects, cfg)
 
 
 @pytest.mark.parametrize("pml", [False, True])
