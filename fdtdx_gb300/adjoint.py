@@ -101,8 +101,9 @@ class _ReversibleRun(torch.autograd.Function):
         ctl["checkpoints"] = checkpoints
         ctl["final"] = arrays
         ctx.ctl = ctl
-        flat = ctl["layout"].flatten(arrays)
-        return tuple(flat)
+        # the outputs are aliases of the final state: autograd attaches its node to the aliases,
+        # so the state held by the node's context does not point back at the node (no cycle)
+        return tuple(t.detach() for t in ctl["layout"].flatten(arrays))
 
     @staticmethod
     def backward(ctx, *grads):
@@ -204,9 +205,9 @@ def reversible_fdtd(
     ctl = {"scene": scene, "arrays": work, "T": T, "bounds": bounds, "layout": layout,
            "inv_eps": work.inv_permittivities, "inv_mu": work.inv_permeabilities}
     wants = ie_in.requires_grad or (mu_t is not None and mu_t.requires_grad)
-    if wants and torch.is_grad_enabled() and scene.complex_fields:
-        raise NotImplementedError("the reversible gradient of complex (Bloch) fields is not supported by the GB300 "
-                                  "kernels (their forward and reverse steps are)")
+    if wants and torch.is_grad_enabled() and scene.complex_fields and mu_t is not None and mu_t.requires_grad:
+        raise NotImplementedError("the inv_permeabilities gradient of complex (Bloch) fields is not supported by the "
+                                  "GB300 kernels (the inv_permittivities gradient is)")
     if not (torch.is_grad_enabled() and wants):
         _ReversibleRun.forward(_NoCtx(), ctl, work.inv_permittivities, None)
         out = work

@@ -31,6 +31,7 @@ struct DBox {
     int lo[3], n[3];
     long long M;       // cells in the box
     float* buf;        // nullptr: empty box
+    long long other;   // complex (Bloch) fields: floats from this part's box to the other part's
 };
 
 __device__ __forceinline__ bool box_local(const DBox& b, int i, int j, int k, long long& q) {
@@ -82,6 +83,11 @@ struct AdjArgs {
     const float* axpE[3][2][2];
     const float* axlp[2][3][2][2];
     float* axlpo[2][3][2][2];
+    // complex (Bloch) fields: the part this launch transposes (0 real, 1 imaginary), the number
+    // of parts, and per slab the floats from this part's psi cotangents to the other part's
+    // (the lam fields' offset is g.pother)
+    int part, nparts;
+    long long lpother[FDTD_MAX_SLABS];
 };
 
 // The slab mask of this block's box.
@@ -106,6 +112,30 @@ __device__ __forceinline__ bool wrap_idx(const Geo& g, int& i, int& j, int& k) {
     return true;
 }
 
+// wrap_idx that also returns the Bloch rotation (cr, ci) of the wrap ((1, 0) when no Bloch
+// axis is crossed).  The transposed steps gather across a Bloch face with the same rule the
+// forward halo loads use (a wrap from below takes the conjugate phase, from above the phase):
+// the adjoint of the phase-shifted wrap read is the conjugate-shifted read the other way.
+__device__ __forceinline__ bool wrap_turn(const Geo& g, int& i, int& j, int& k, float& cr, float& ci) {
+    cr = 1.f;
+    ci = 0.f;
+    if (i < 0) { if (!g.px) return false; i += g.nx; bloch_turn(g, 0, false, cr, ci); }
+    else if (i >= g.nx) { if (!g.px) return false; i -= g.nx; bloch_turn(g, 0, true, cr, ci); }
+    if (j < 0) { if (!g.py) return false; j += g.ny; bloch_turn(g, 1, false, cr, ci); }
+    else if (j >= g.ny) { if (!g.py) return false; j -= g.ny; bloch_turn(g, 1, true, cr, ci); }
+    if (k < 0) { if (!g.pz) return false; k += g.nz; bloch_turn(g, 2, false, cr, ci); }
+    else if (k >= g.nz) { if (!g.pz) return false; k -= g.nz; bloch_turn(g, 2, true, cr, ci); }
+    return true;
+}
+
+// A value of this part's array at `off` seen through a wrap with rotation (cr, ci): the other
+// part, `pother` floats away, mixed in with this part's sign.
+__device__ __forceinline__ float mix_at(const float* f, long long off, long long pother, float psign, float cr, float ci) {
+    const float v = f[off];
+    if (ci == 0.f && cr == 1.f) return v;
+    return cr * v + psign * ci * f[off + pother];
+}
+
 // The slab a cell lies in along one axis: its layer index l (out: -1 when outside).
 __device__ __forceinline__ int slab_layer(const DSlab& sl, int i, int j, int k) {
     const int x = sl.axis == 0 ? i : (sl.axis == 1 ? j : k);
@@ -126,7 +156,8 @@ __device__ __forceinline__ void dcell(const AdjArgs& a, int i, int j, int k, boo
     const Geo& g = a.g;
 #pragma unroll
     for (int q = 0; q < 6; ++q) D[q] = 0.f;
-    if (!wrap_idx(g, i, j, k)) return;
+    float cr, ci;
+    if (!wrap_turn(g, i, j, k, cr, ci)) return;
     const long long N = g.N;
     const long long c = cell_index(g, i, j, k);
     const float* L = HSIDE ? a.lH : a.lE;
@@ -134,7 +165,7 @@ __device__ __forceinline__ void dcell(const AdjArgs& a, int i, int j, int k, boo
     float lc[3];
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-        float l1 = L[comp * N + c];
+        float l1 = mix_at(L, comp * N + c, g.pother, g.psign, cr, ci);
         if (mask && face_zero(g, mask, comp, i, j, k)) l1 = 0.f;
         float m, den = 1.f;
         if (HSIDE) {
@@ -162,8 +193,8 @@ __device__ __forceinline__ void dcell(const AdjArgs& a, int i, int j, int k, boo
         const float lcj = sl.axis == 0 ? lc[2] : (sl.axis == 1 ? lc[0] : lc[1]);  // curl[(a+2)%3]
         const float* lp0 = HSIDE ? a.lpH[s][0] : a.lpE[s][0];
         const float* lp1 = HSIDE ? a.lpH[s][1] : a.lpE[s][1];
-        const float t1 = lp0[p] - lci;  // cotangent of psi1' (state output + correction c1)
-        const float t2 = lp1[p] + lcj;
+        const float t1 = mix_at(lp0, p, a.lpother[s], g.psign, cr, ci) - lci;  // cotangent of psi1' (+ correction c1)
+        const float t2 = mix_at(lp1, p, a.lpother[s], g.psign, cr, ci) + lcj;
         const float ca = __ldg(co + l);
         float d1 = ca * t1, d2 = ca * t2;
         if (!sl.kappa_one) {
@@ -404,7 +435,7 @@ __global__ void __launch_bounds__(256) k_adj_E(const __grid_constant__ AdjArgs a
 // `out` the psi cotangent of step t is written (the cell is the caller's own).
 template <bool HSIDE>
 __device__ __forceinline__ void slab_term(const AdjArgs& a, int axis, int i, int j, int k, float lci, float lcj,
-                                          bool out, float& d1, float& d2) {
+                                          bool out, float& d1, float& d2, float cr = 1.f, float ci = 0.f) {
     d1 = 0.f;
     d2 = 0.f;
     const int x = axis == 0 ? i : (axis == 1 ? j : k);
@@ -419,8 +450,8 @@ __device__ __forceinline__ void slab_term(const AdjArgs& a, int axis, int i, int
         const long long p = psi_offset(sl, i, j, k);
         const float* lp0 = HSIDE ? a.lpH[s][0] : a.lpE[s][0];
         const float* lp1 = HSIDE ? a.lpH[s][1] : a.lpE[s][1];
-        const float t1 = lp0[p] - lci;
-        const float t2 = lp1[p] + lcj;
+        const float t1 = mix_at(lp0, p, a.lpother[s], a.g.psign, cr, ci) - lci;
+        const float t2 = mix_at(lp1, p, a.lpother[s], a.g.psign, cr, ci) + lcj;
         const float ca = __ldg(co + l);
         float e1 = ca * t1, e2 = ca * t2;
         if (!sl.kappa_one) {
@@ -528,9 +559,10 @@ __device__ __forceinline__ void axis_terms(const AdjArgs& a, int axis, int i, in
 #pragma unroll
     for (int e = 0; e < VEC; ++e) {
         int ii = i, jj = j, kk = k0 + e;
-        if (!wrap_idx(a.g, ii, jj, kk)) continue;
+        float cr, ci;
+        if (!wrap_turn(a.g, ii, jj, kk, cr, ci)) continue;
         float d1, d2;
-        slab_term<HSIDE>(a, axis, ii, jj, kk, lci.v[e], lcj.v[e], out, d1, d2);
+        slab_term<HSIDE>(a, axis, ii, jj, kk, lci.v[e], lcj.v[e], out, d1, d2, cr, ci);
         lci.v[e] -= d1;
         lcj.v[e] += d2;
     }
@@ -558,10 +590,11 @@ __device__ __forceinline__ float lc_of(const AdjArgs& a, int comp, int i, int j,
 // lc of one component at a neighbour (wrapped with the halo rule; zero in a zero halo).
 template <bool HSIDE>
 __device__ __forceinline__ float lc_nb(const AdjArgs& a, int comp, int i, int j, int k) {
-    if (!wrap_idx(a.g, i, j, k)) return 0.f;
+    float cr, ci;
+    if (!wrap_turn(a.g, i, j, k, cr, ci)) return 0.f;
     const long long c = cell_index(a.g, i, j, k);
     const float* L = HSIDE ? a.lH : a.lE;
-    return lc_of<HSIDE>(a, comp, i, j, k, c, L[comp * a.g.N + c]);
+    return lc_of<HSIDE>(a, comp, i, j, k, c, mix_at(L, comp * a.g.N + c, a.g.pother, a.g.psign, cr, ci));
 }
 
 template <bool HSIDE, int VEC>
@@ -578,14 +611,21 @@ template <bool HSIDE, int VEC>
 __device__ __forceinline__ Vec<VEC> lc_row(const AdjArgs& a, int comp, int i, int j, int k0) {
     const Geo& g = a.g;
     Vec<VEC> r;
-    if (!wrap_idx(g, i, j, k0)) {
+    float cr, ci;
+    if (!wrap_turn(g, i, j, k0, cr, ci)) {
 #pragma unroll
         for (int e = 0; e < VEC; ++e) r.v[e] = 0.f;
         return r;
     }
     const long long c = cell_index(g, i, j, k0);
     const float* L = HSIDE ? a.lH : a.lE;
-    return lc_vec<HSIDE, VEC>(a, comp, i, j, k0, c, ldv<VEC>(L + comp * g.N + c));
+    Vec<VEC> l = ldv<VEC>(L + comp * g.N + c);
+    if (ci != 0.f || cr != 1.f) {  // a row wrapped across a Bloch face: the other part mixed in
+        const Vec<VEC> o = ldv<VEC>(L + g.pother + comp * g.N + c);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) l.v[e] = cr * l.v[e] + g.psign * ci * o.v[e];
+    }
+    return lc_vec<HSIDE, VEC>(a, comp, i, j, k0, c, l);
 }
 
 // Transposed H-step: lam E3 += curl_H(lcH), in place.  PML: the differences along each axis
@@ -1173,16 +1213,30 @@ struct AdjDet {
     DBox snap;      // bilinear detectors: (6, box) primal E3 | H3 over [lo - 1, hi + 1)
 };
 
+// The transpose of a wrapped read v_p = cr F_p + psign ci F_q scatters into both parts.
 __device__ __forceinline__ void add_T(const Geo& g, float* F, int comp, int i, int j, int k, float v) {
-    if (!wrap_idx(g, i, j, k)) return;
-    atomicAdd(F + comp * g.N + cell_index(g, i, j, k), v);
+    float cr, ci;
+    if (!wrap_turn(g, i, j, k, cr, ci)) return;
+    const long long off = comp * g.N + cell_index(g, i, j, k);
+    if (ci == 0.f && cr == 1.f) {
+        atomicAdd(F + off, v);
+        return;
+    }
+    atomicAdd(F + off, cr * v);
+    atomicAdd(F + off + g.pother, g.psign * ci * v);
 }
 
 __device__ __forceinline__ void add_hp(const Geo& g, const DBox& hp, int comp, int i, int j, int k, float v) {
-    if (!hp.buf || !wrap_idx(g, i, j, k)) return;
+    float cr, ci;
+    if (!hp.buf || !wrap_turn(g, i, j, k, cr, ci)) return;
     long long q;
     if (!box_local(hp, i, j, k, q)) return;  // the box covers every exact detector's stencil
-    atomicAdd(hp.buf + comp * hp.M + q, v);
+    if (ci == 0.f && cr == 1.f) {
+        atomicAdd(hp.buf + comp * hp.M + q, v);
+        return;
+    }
+    atomicAdd(hp.buf + comp * hp.M + q, cr * v);
+    atomicAdd(hp.buf + hp.other + comp * hp.M + q, g.psign * ci * v);
 }
 
 // Transpose of `colocate` for the cotangent gv[6] of the sample at (i, j, k).
@@ -1288,6 +1342,11 @@ __global__ void __launch_bounds__(kDetBlock) k_adj_det(const __grid_constant__ A
     const int j = d.lo[1] + (int)((r / d.rz) % d.ry);
     const int i = d.lo[0] + (int)(r / ((long long)d.rz * d.ry));
     float gv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // complex (Bloch) fields: a field detector records the real parts only; a phasor the
+    // complex sample (v_re + i v_im) w, whose imaginary part's cotangent is Im(lam) w_re -
+    // Re(lam) w_im; per-cell field, flux and energy entries are cleared by the last part
+    const bool last = a.part == a.nparts - 1;
+    if (d.kind == FDTD_DET_FIELD && a.part != 0) return;
     if (d.kind == FDTD_DET_PHASOR || d.kind == FDTD_DET_FIELD) {
         const int nout = __popc(d.comp_mask & 63);
         int q = 0;
@@ -1305,7 +1364,7 @@ __global__ void __launch_bounds__(kDetBlock) k_adj_det(const __grid_constant__ A
                     } else {
                         z = reinterpret_cast<const float2*>(x.lam)[((long long)fq * nout + q) * d.R + r];
                     }
-                    l += w.x * z.x + w.y * z.y;
+                    l += a.part ? w.x * z.y - w.y * z.x : w.x * z.x + w.y * z.y;
                 }
                 if (d.reduce) l /= (float)d.R;
                 if (d.inverse) l = -l;
@@ -1331,7 +1390,7 @@ __global__ void __launch_bounds__(kDetBlock) k_adj_det(const __grid_constant__ A
             } else {
                 float* p = lam + ((long long)slot * d.ncomp + q) * d.R + r;
                 L[q] = *p;
-                *p = 0.f;
+                if (last) *p = 0.f;
             }
         }
         float v[6];

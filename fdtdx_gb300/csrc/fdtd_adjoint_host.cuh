@@ -29,12 +29,13 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
     const int n3[3] = {d.nx, d.ny, d.nz};
     const bool per[3] = {d.periodic[0] != 0, d.periodic[1] != 0, d.periodic[2] != 0};
     Arena ar;
-    const size_t o_lam = ar.take(sizeof(float) * 6 * (size_t)N);
+    const size_t parts = (size_t)p->parts;  // complex (Bloch) fields: real parts, then imaginary parts
+    const size_t o_lam = ar.take(sizeof(float) * 6 * parts * (size_t)N);
     size_t o_psi[FDTD_MAX_SLABS][4] = {};
     for (int s = 0; s < d.n_slabs; ++s) {
         const DSlab& sl = p->slab[s];
         const size_t cells = (size_t)sl.sx * sl.sy * sl.sz;
-        for (int q = 0; q < 4; ++q) o_psi[s][q] = ar.take(sizeof(float) * cells);
+        for (int q = 0; q < 4; ++q) o_psi[s][q] = ar.take(sizeof(float) * parts * cells);
     }
     // the H-before-update box: union of the exact H-reading detectors' stencils
     DBox hp{};
@@ -55,7 +56,7 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
     if (any) {
         for (int a = 0; a < 3; ++a) { hp.lo[a] = blo[a]; hp.n[a] = bhi[a] - blo[a]; }
         hp.M = (long long)hp.n[0] * hp.n[1] * hp.n[2];
-        o_hp = ar.take(sizeof(float) * 3 * (size_t)hp.M);
+        o_hp = ar.take(sizeof(float) * 3 * parts * (size_t)hp.M);
     }
     DBox snap[FDTD_MAX_DETECTORS] = {};
     size_t o_snap[FDTD_MAX_DETECTORS] = {};
@@ -65,7 +66,7 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
         DBox& b = snap[q];
         for (int a = 0; a < 3; ++a) { b.lo[a] = dd.lo[a] - 1; b.n[a] = dd.hi[a] - dd.lo[a] + 2; }
         b.M = (long long)b.n[0] * b.n[1] * b.n[2];
-        o_snap[q] = ar.take(sizeof(float) * 6 * (size_t)b.M);
+        o_snap[q] = ar.take(sizeof(float) * 6 * parts * (size_t)b.M);
     }
     char* mem = nullptr;
     cudaError_t e = dev_alloc(reinterpret_cast<void**>(&mem), ar.off);
@@ -78,7 +79,7 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
     p->amem = mem;
     p->amem_bytes = ar.off;
     p->lam_twin[0] = reinterpret_cast<float*>(mem + o_lam);
-    p->lam_twin[1] = p->lam_twin[0] + 3 * N;
+    p->lam_twin[1] = p->lam_twin[0] + 3 * (long long)parts * N;
     for (int s = 0; s < d.n_slabs; ++s)
         for (int q = 0; q < 4; ++q) p->lpsi_twin[s][q] = reinterpret_cast<float*>(mem + o_psi[s][q]);
     p->hp = hp;
@@ -97,12 +98,21 @@ struct LamSet {
     float* psi[FDTD_MAX_SLABS][4];
 };
 
+// The transposed step's arguments; `part` 1 selects the imaginary parts of complex (Bloch)
+// fields and of their cotangents (planar buffers).
 AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, const LamSet& cur,
-                 const LamSet& nxt) {
+                 const LamSet& nxt, int part = 0) {
     AdjArgs a{};
     a.g = p->g;
-    a.E = b->E;
-    a.H = b->H;
+    const long long fo = part ? 3 * p->g.N : 0;
+    if (part) {
+        a.g.pother = -3 * p->g.N;
+        a.g.psign = 1.f;
+    }
+    a.part = part;
+    a.nparts = p->parts;
+    a.E = b->E + fo;
+    a.H = b->H + fo;
     a.ie = b->inv_eps;
     a.n_eps = p->d.n_eps;
     a.im = p->d.n_mu ? b->inv_mu : nullptr;
@@ -113,24 +123,32 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
     a.sigH = p->d.n_sigma_H ? b->sigma_H : nullptr;
     a.n_sigH = p->d.n_sigma_H;
     a.n_slab = p->d.n_slabs;
+    long long ps[FDTD_MAX_SLABS] = {};
     for (int s = 0; s < p->d.n_slabs; ++s) {
+        const long long cells = (long long)p->slab[s].sx * p->slab[s].sy * p->slab[s].sz;
+        ps[s] = part ? cells : 0;
+        a.lpother[s] = part ? -cells : cells;
         a.slab[s] = p->slab[s];
-        a.psiE1[s] = b->psi_E[s][0];
-        a.psiE2[s] = b->psi_E[s][1];
-        a.psiH1[s] = b->psi_H[s][0];
-        a.psiH2[s] = b->psi_H[s][1];
-        a.lpE[s][0] = cur.psi[s][0]; a.lpE[s][1] = cur.psi[s][1];
-        a.lpH[s][0] = cur.psi[s][2]; a.lpH[s][1] = cur.psi[s][3];
-        a.lpE_out[s][0] = nxt.psi[s][0]; a.lpE_out[s][1] = nxt.psi[s][1];
-        a.lpH_out[s][0] = nxt.psi[s][2]; a.lpH_out[s][1] = nxt.psi[s][3];
+        a.psiE1[s] = b->psi_E[s][0] + ps[s];
+        a.psiE2[s] = b->psi_E[s][1] + ps[s];
+        a.psiH1[s] = b->psi_H[s][0] + ps[s];
+        a.psiH2[s] = b->psi_H[s][1] + ps[s];
+        a.lpE[s][0] = cur.psi[s][0] + ps[s]; a.lpE[s][1] = cur.psi[s][1] + ps[s];
+        a.lpH[s][0] = cur.psi[s][2] + ps[s]; a.lpH[s][1] = cur.psi[s][3] + ps[s];
+        a.lpE_out[s][0] = nxt.psi[s][0] + ps[s]; a.lpE_out[s][1] = nxt.psi[s][1] + ps[s];
+        a.lpH_out[s][0] = nxt.psi[s][2] + ps[s]; a.lpH_out[s][1] = nxt.psi[s][3] + ps[s];
     }
-    a.lE = cur.E;
-    a.lH = cur.H;
-    a.lE_out = nxt.E;
-    a.lH_out = nxt.H;
+    a.lE = cur.E + fo;
+    a.lH = cur.H + fo;
+    a.lE_out = nxt.E + fo;
+    a.lH_out = nxt.H + fo;
     a.grad_ie = adj->grad_inv_eps;
     a.grad_im = adj->grad_inv_mu;
     a.hp = p->hp;
+    if (a.hp.buf) {
+        a.hp.buf += part ? 3 * a.hp.M : 0;
+        a.hp.other = part ? -3 * a.hp.M : 3 * a.hp.M;
+    }
     for (int x = 0; x < 3; ++x) a.ax_slab[x][0] = a.ax_slab[x][1] = -1;
     for (int s = 0; s < p->d.n_slabs; ++s) {
         const int side = p->d.slabs[s].direction > 0 ? 1 : 0;
@@ -143,11 +161,11 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
             if (s < 0) continue;
             a.axs[x][side] = p->slab[s];
             for (int q = 0; q < 2; ++q) {
-                a.axpE[x][side][q] = b->psi_E[s][q];
-                a.axlp[0][x][side][q] = cur.psi[s][q];
-                a.axlp[1][x][side][q] = cur.psi[s][2 + q];
-                a.axlpo[0][x][side][q] = nxt.psi[s][q];
-                a.axlpo[1][x][side][q] = nxt.psi[s][2 + q];
+                a.axpE[x][side][q] = b->psi_E[s][q] + ps[s];
+                a.axlp[0][x][side][q] = cur.psi[s][q] + ps[s];
+                a.axlp[1][x][side][q] = cur.psi[s][2 + q] + ps[s];
+                a.axlpo[0][x][side][q] = nxt.psi[s][q] + ps[s];
+                a.axlpo[1][x][side][q] = nxt.psi[s][2 + q] + ps[s];
             }
         }
     return a;
@@ -250,36 +268,52 @@ void launch_adj(const FdtdPlan* p, const AdjArgs& a, cudaStream_t st) {
 // One step of the backward loop at t = *d_t: snapshot, reconstruction, transposed step.
 void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, const LamSet& cur,
                          const LamSet& nxt, cudaStream_t st) {
+    const int np = p->parts;
+    const long long fo = 3 * p->g.N;
     for (int q = 0; q < p->d.n_detectors; ++q) {
         if (!adj->lam_det[q] || !p->snap[q].buf) continue;
-        const DBox& sb = p->snap[q];
-        k_adj_snap<<<(unsigned)((sb.M + 255) / 256), 256, 0, st>>>(p->g, sb, p->det[q].slot, p->d_t, b->E, b->H);
+        for (int part = 0; part < np; ++part) {
+            DBox sb = p->snap[q];
+            sb.buf += part * 6 * sb.M;
+            Geo g = p->g;
+            if (part) { g.pother = -fo; g.psign = 1.f; }
+            k_adj_snap<<<(unsigned)((sb.M + 255) / 256), 256, 0, st>>>(g, sb, p->det[q].slot, p->d_t, b->E + part * fo,
+                                                                        b->H + part * fo);
+        }
     }
     interfaces<true>(p, b, b->H, st);
     launch_sources(p, b, false, b->H, 1, st);
-    launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H), st);
+    for (int part = 0; part < np; ++part) launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H, part), st);
     // here H holds H(t) and E still E3: the detector cotangents (which read H(t) for exact
     // interpolation) complete lam H3, and the inv_mu cotangent needs E3 and H(t)
-    const AdjArgs a = make_adj(p, b, adj, cur, nxt);
-    for (int q = 0; q < p->d.n_detectors; ++q) {
-        if (!adj->lam_det[q]) continue;
-        const DDet& dd = p->det[q];
-        AdjDet x{};
-        x.d = dd;
-        x.lam = adj->lam_det[q];
-        x.snap = p->snap[q];
-        k_adj_det<<<dd.nblocks, kDetBlock, 0, st>>>(a, x, p->d_t);
-        if (dd.reduce && dd.kind != FDTD_DET_PHASOR) k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
+    for (int part = 0; part < np; ++part) {
+        const AdjArgs a = make_adj(p, b, adj, cur, nxt, part);
+        for (int q = 0; q < p->d.n_detectors; ++q) {
+            if (!adj->lam_det[q]) continue;
+            const DDet& dd = p->det[q];
+            AdjDet x{};
+            x.d = dd;
+            x.lam = adj->lam_det[q];
+            x.snap = p->snap[q];
+            if (x.snap.buf) x.snap.buf += part * 6 * x.snap.M;
+            k_adj_det<<<dd.nblocks, kDetBlock, 0, st>>>(a, x, p->d_t);
+        }
+        if (a.grad_im) {
+            const unsigned nb = (unsigned)((p->g.N + 255) / 256);
+            if (a.n_slab) k_grad_mu<true><<<nb, 256, 0, st>>>(a);
+            else k_grad_mu<false><<<nb, 256, 0, st>>>(a);
+        }
     }
-    if (a.grad_im) {
-        const unsigned nb = (unsigned)((p->g.N + 255) / 256);
-        if (a.n_slab) k_grad_mu<true><<<nb, 256, 0, st>>>(a);
-        else k_grad_mu<false><<<nb, 256, 0, st>>>(a);
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        const DDet& dd = p->det[q];
+        if (adj->lam_det[q] && dd.reduce && dd.kind != FDTD_DET_PHASOR)
+            k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
     }
     launch_sources(p, b, true, b->E, 1, st);
-    launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E), st);
-    launch_adj<true>(p, a, st);
-    launch_adj<false>(p, a, st);
+    for (int part = 0; part < np; ++part) launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E, part), st);
+    // the transposed H-steps of both parts (each reads lam H3 of both) before either E-step
+    for (int part = 0; part < np; ++part) launch_adj<true>(p, make_adj(p, b, adj, cur, nxt, part), st);
+    for (int part = 0; part < np; ++part) launch_adj<false>(p, make_adj(p, b, adj, cur, nxt, part), st);
     k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
 }
 
@@ -293,7 +327,8 @@ extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjoint
         return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_adjoint)");
     if (int rc = check_bufs(p, b)) return rc;
     if (int rc = check_adj(p, adj)) return rc;
-    if (p->parts != 1) return fail(p, FDTD_EINVAL, "the reversible gradient of complex (Bloch) fields is not supported");
+    if (p->parts != 1 && adj->grad_inv_mu)
+        return fail(p, FDTD_EINVAL, "the inv_mu cotangent of complex (Bloch) fields is not supported (inv_eps is)");
     if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)
         return fail(p, FDTD_EINVAL, "adjoint steps out of the range covered by the plan's tables");
     if (n_steps == 0) return FDTD_OK;
@@ -353,12 +388,12 @@ extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjoint
         std::swap(cur, nxt);
     }
     if (cur != &user) {  // odd step count: the result sits in the twins
-        const size_t fb = sizeof(float) * 3 * (size_t)p->g.N;
+        const size_t fb = sizeof(float) * 3 * (size_t)p->parts * (size_t)p->g.N;
         cudaError_t e = cudaMemcpyAsync(user.E, cur->E, fb, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(user.H, cur->H, fb, cudaMemcpyDeviceToDevice, st);
         for (int s = 0; s < p->d.n_slabs && e == cudaSuccess; ++s) {
             const DSlab& sl = p->slab[s];
-            const size_t pb = sizeof(float) * (size_t)sl.sx * sl.sy * sl.sz;
+            const size_t pb = sizeof(float) * (size_t)p->parts * sl.sx * sl.sy * sl.sz;
             for (int q = 0; q < 4 && e == cudaSuccess; ++q)
                 e = cudaMemcpyAsync(user.psi[s][q], cur->psi[s][q], pb, cudaMemcpyDeviceToDevice, st);
         }

@@ -373,7 +373,6 @@ class Scene:
 
     def __init__(self, objects: ObjectContainer, arrays: ArrayContainer, config: SimulationConfig,
                  record_interfaces: bool = False):
-        self.objects = objects
         self.config = config
         self.desc = N.Desc()
         self._keep: list = []
@@ -414,6 +413,7 @@ class Scene:
             d.bloch_sin[ax] = phases["+"].imag
         self.complex_fields = d.bloch_axes != 0
         self._planar = None
+        self._lam_ws = None
         self.pmls: list[PerfectlyMatchedLayer] = objects.pml_objects
         if len(self.pmls) > N.MAX_SLABS:
             raise ValueError("at most six PML slabs")
@@ -626,8 +626,6 @@ class Scene:
             self._run(arrays, call)
 
     def adjoint(self, arrays: ArrayContainer, lam: dict, t_end: int, n_steps: int, stream=None) -> None:
-        if self.complex_fields:
-            raise NotImplementedError("the reversible gradient of complex (Bloch) fields is not supported")
         """Backward loop of the reversible gradient on the native path (``fdtd_adjoint``).
 
         ``arrays`` holds the forward state at ``t_end`` and is reconstructed in place down to
@@ -635,18 +633,31 @@ class Scene:
         ``"psi_E"`` / ``"psi_H"`` (name -> (psi1, psi2)), ``"det"`` (detector name -> tensor
         of the state's layout, complex states with torch's convention), ``"grad_inv_eps"`` and
         ``"grad_inv_mu"`` (accumulated; either may be absent); all are updated in place.
+        Complex (Bloch) fields and their cotangents (dL/dRe + i dL/dIm) are staged through
+        planar workspaces.
         """
         st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
-        b = self.buffers(arrays)
-        a = N.AdjointBuffers()
         for key in ("E", "H"):
             t = lam[key]
-            if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
-                raise ValueError("cotangents must be contiguous float32 CUDA tensors")
-        a.lam_E, a.lam_H = N.ptr(lam["E"]), N.ptr(lam["H"])
+            want = torch.complex64 if self.complex_fields else torch.float32
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == want):
+                raise ValueError(f"cotangents must be contiguous {want} CUDA tensors")
+        lw = None
+        if self.complex_fields:
+            if lam.get("grad_inv_mu") is not None:
+                raise NotImplementedError("the inv_mu cotangent of complex (Bloch) fields is not supported")
+            if self._lam_ws is None or not self._lam_ws.fits(lam):
+                self._lam_ws = PlanarLam(lam, self.pmls)
+            lw = self._lam_ws
+        a = N.AdjointBuffers()
+        src = lw if lw is not None else None
+        a.lam_E, a.lam_H = (N.ptr(lw.E), N.ptr(lw.H)) if lw is not None else (N.ptr(lam["E"]), N.ptr(lam["H"]))
         for s, p in enumerate(self.pmls):
-            a.lam_psi_E[s][0], a.lam_psi_E[s][1] = N.ptr(lam["psi_E"][p.name][0]), N.ptr(lam["psi_E"][p.name][1])
-            a.lam_psi_H[s][0], a.lam_psi_H[s][1] = N.ptr(lam["psi_H"][p.name][0]), N.ptr(lam["psi_H"][p.name][1])
+            pe = lw.psi_E[p.name] if lw is not None else lam["psi_E"][p.name]
+            ph = lw.psi_H[p.name] if lw is not None else lam["psi_H"][p.name]
+            a.lam_psi_E[s][0], a.lam_psi_E[s][1] = N.ptr(pe[0]), N.ptr(pe[1])
+            a.lam_psi_H[s][0], a.lam_psi_H[s][1] = N.ptr(ph[0]), N.ptr(ph[1])
+        del src
         dets = lam.get("det", {})
         for q, det in enumerate(self.detectors):
             t = dets.get(det.name)
@@ -655,9 +666,18 @@ class Scene:
             a.lam_det[q] = N.ptr(t)
         a.grad_inv_eps = N.ptr(lam.get("grad_inv_eps"))
         a.grad_inv_mu = N.ptr(lam.get("grad_inv_mu"))
-        rc = N.load().fdtd_adjoint(self.plan, C.byref(b), C.byref(a), int(t_end), int(n_steps),
-                                   C.c_void_p(st.cuda_stream))
-        N.check(rc, self.plan, "fdtd_adjoint")
+
+        def call(b):
+            rc = N.load().fdtd_adjoint(self.plan, C.byref(b), C.byref(a), int(t_end), int(n_steps),
+                                       C.c_void_p(st.cuda_stream))
+            N.check(rc, self.plan, "fdtd_adjoint")
+
+        with torch.cuda.stream(st):
+            if lw is not None:
+                lw.load(lam)
+            self._run(arrays, call)
+            if lw is not None:
+                lw.store(lam)
 
 
 class PlanarFields:
@@ -710,6 +730,46 @@ class PlanarFields:
 
     def store(self, arrays: ArrayContainer) -> None:
         for c, w in self._pairs(arrays):
+            r = torch.view_as_real(c)
+            r[..., 0].copy_(w[0])
+            r[..., 1].copy_(w[1])
+
+
+class PlanarLam:
+    """The planar float32 workspace of a complex (Bloch) scene's cotangents: lam E, lam H and
+    the psi cotangent pairs as (2, ...) tensors, dL/dRe parts first, then dL/dIm."""
+
+    def __init__(self, lam: dict, pmls):
+        self.key = self._key(lam)
+        dev = lam["E"].device
+        self.E = torch.empty((2, *lam["E"].shape), dtype=torch.float32, device=dev)
+        self.H = torch.empty((2, *lam["H"].shape), dtype=torch.float32, device=dev)
+        self.psi_E = {p.name: tuple(torch.empty((2, *t.shape), dtype=torch.float32, device=dev)
+                                    for t in lam["psi_E"][p.name]) for p in pmls}
+        self.psi_H = {p.name: tuple(torch.empty((2, *t.shape), dtype=torch.float32, device=dev)
+                                    for t in lam["psi_H"][p.name]) for p in pmls}
+
+    @staticmethod
+    def _key(lam: dict):
+        return (tuple(lam["E"].shape), tuple((k, tuple(a.shape)) for k, (a, _b) in lam["psi_E"].items()))
+
+    def fits(self, lam: dict) -> bool:
+        return self._key(lam) == self.key
+
+    def _pairs(self, lam: dict):
+        out = [(lam["E"], self.E), (lam["H"], self.H)]
+        for k in self.psi_E:
+            out += list(zip(lam["psi_E"][k], self.psi_E[k])) + list(zip(lam["psi_H"][k], self.psi_H[k]))
+        return out
+
+    def load(self, lam: dict) -> None:
+        for c, w in self._pairs(lam):
+            r = torch.view_as_real(c)
+            w[0].copy_(r[..., 0])
+            w[1].copy_(r[..., 1])
+
+    def store(self, lam: dict) -> None:
+        for c, w in self._pairs(lam):
             r = torch.view_as_real(c)
             r[..., 0].copy_(w[0])
             r[..., 1].copy_(w[1])

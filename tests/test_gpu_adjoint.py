@@ -366,3 +366,36 @@ def test_adjoint_inv_mu_cpml_detectors():
     _check_eps_mu("adjoint_inv_mu_cpml", ge, gm, objects, arrays, cfg,
                   lambda f: {"ph": {"phasor": 2 * f.det["ph"]["phasor"]},
                              "en": {"energy": w_en * torch.ones_like(f.det["en"]["energy"])}})
+
+
+def test_reversible_runs_release_device_memory_without_gc():
+    """Repeated gradient runs (a new scene each time, as an optimisation loop or a stream of
+    one-at-a-time jobs makes them) return every device tensor when their outputs are dropped,
+    with the cycle collector off: no reference cycle keeps a run's state alive."""
+    import gc
+
+    gc.collect()
+    gc.disable()
+    try:
+        base = None
+        for _ in range(3):
+            objects, arrays, cfg = _periodic_lossy_slab()
+            ga = _to_cuda(objects, arrays)
+            ie = ga.inv_permittivities.clone().requires_grad_(True)
+            _, out = fx.reversible_fdtd(ga.aset("inv_permittivities", ie), objects, cfg)
+            (out.fields.E ** 2).sum().backward()
+            torch.cuda.synchronize()
+            del out, ie, ga, arrays, objects
+            _, res = fx.run_fdtd(*_to_cuda_run(_periodic_lossy_slab()))
+            del res
+            torch.cuda.synchronize()
+            if base is None:
+                base = torch.cuda.memory_allocated()  # after the first run: lazily built global state
+            assert torch.cuda.memory_allocated() == base
+    finally:
+        gc.enable()
+
+
+def _to_cuda_run(placed):
+    objects, arrays, cfg = placed
+    return _to_cuda(objects, arrays), objects, cfg

@@ -6,7 +6,8 @@ phase exp(i k L) (the '+' ghost layer) or its conjugate (the '-' one)
 (fdtdx/fdtd/update.py:92-136, fdtdx/objects/boundaries/bloch.py:59-94).  Sources drive the
 real parts; phasor detectors take the complex sample, field detectors its real part, flux
 detectors Re(E x conj H) and energy detectors |E|^2 and |H|^2.  Tolerance: relative L2 <=
-1e-4 against the float32 oracle (float64 reported).
+1e-4 against the float32 oracle (float64 reported); gradients 1e-3 (the reversible adjoint
+re-rounds 2T steps).
 """
 
 from __future__ import annotations
@@ -20,6 +21,7 @@ import fdtdx_gb300 as fx
 from fdtdx_gb300.engine import Scene
 from oracle import fdtd_oracle as O
 from tests.helpers import compare_states, log_result, rel_l2
+from tests.test_gpu_adjoint import _inner, _to_cuda
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
@@ -184,3 +186,109 @@ def test_bloch_oblique_fresnel_te():
     t_ref = (2.0 * math.cos(tt)) / math.cos(theta) * (2.0 * math.cos(theta) / (math.cos(theta) + 2.0 * math.cos(tt))) ** 2
     log_result("bloch_oblique_fresnel_gpu", T=s1 / s0, T_ref=t_ref)
     assert s0 > 0 and abs(s1 / s0 - t_ref) / t_ref < 0.05, (s1 / s0, t_ref)
+
+
+def _bloch_gradient_scene(steps, ckpt=0):
+    """Bloch x and y (a vector along both), CPML z with kappa != 1, an anisotropic lossy block,
+    a dipole and a plane source, and every detector kind; recorded for the reversible gradient."""
+    dx = 40e-9
+    nx, ny, nz = 14, 12, 30
+    cfg = fx.SimulationConfig(time=steps * 0.99 / math.sqrt(3) * dx / C0, grid=fx.UniformGrid(dx),
+                              gradient_config=fx.GradientConfig(recorder=fx.Recorder(),
+                                                                num_checkpoints_reversible=ckpt))
+    vol = fx.SimulationVolume(shape=(nx, ny, nz))
+    bc = fx.BoundaryConfig.from_uniform_bound(5, override_types={f: "bloch" for f in FACES[:4]},
+                                              bloch_vector=(1.1e6, -0.6e6, 0.0), kappa_end=1.5)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    wc = fx.WaveCharacter(wavelength=1.0e-6)
+    R = ((2, 12), (1, 11), (11, 20))
+    objs += [
+        fx.UniformMaterialObject(name="blk", grid_slice_tuple=((3, 10), (2, 9), (12, 19)),
+                                 material=fx.Material(permittivity=(2.0, 4.0, 3.0), electric_conductivity=2e4)),
+        fx.UniformPlaneSource(name="src", grid_slice_tuple=((0, nx), (0, ny), (8, 9)), direction="+",
+                              fixed_E_polarization_vector=(0, 1, 0), wave_character=wc),
+        fx.PointDipoleSource(name="dip", grid_slice_tuple=((6, 7), (5, 6), (15, 16)), polarization=0,
+                             wave_character=wc),
+        fx.PhasorDetector(name="ph", grid_slice_tuple=R, wave_characters=(wc,)),
+        fx.PhasorDetector(name="ph_red", grid_slice_tuple=R, wave_characters=(wc,), components=("Ex", "Hz"),
+                          reduce_volume=True),
+        fx.FieldDetector(name="f_plane", grid_slice_tuple=((0, nx), (0, ny), (16, 17)), components=("Ey", "Hx")),
+        fx.FieldDetector(name="f_red", grid_slice_tuple=R, reduce_volume=True, exact_interpolation=False),
+        fx.PoyntingFluxDetector(name="flux", grid_slice_tuple=((0, nx), (0, ny), (21, 22)), direction="+"),
+        fx.PoyntingFluxDetector(name="flux_all", grid_slice_tuple=((4, 9), (3, 8), (13, 15)), direction="-",
+                                keep_all_components=True, reduce_volume=False),
+        fx.EnergyDetector(name="en", grid_slice_tuple=R, reduce_volume=True),
+    ]
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cpu")
+    return objects, arrays, cfg
+
+
+def _random_cotangents(arrays, seed):
+    g = torch.Generator().manual_seed(seed)
+
+    def rnd(v):
+        if v.is_complex():
+            return torch.complex(torch.randn(v.shape, generator=g), torch.randn(v.shape, generator=g))
+        return torch.randn(v.shape, generator=g)
+
+    cots = {(dn, k): rnd(v) for dn, st in arrays.detector_states.items() for k, v in st.items()}
+    return cots, rnd(arrays.fields.E), rnd(arrays.fields.H)
+
+
+@pytest.mark.parametrize("ckpt", [0, 2])
+def test_bloch_reversible_gradient_every_detector(ckpt):
+    """d <cot, outputs> / d inv_eps of a Bloch scene through reversible_fdtd against the oracle's
+    restatement of the custom VJP (fdtdx/fdtd/fdtd.py:215-333) on complex fields: seeded complex
+    cotangents on E, H and every detector state; one slice and three (checkpoint resets)."""
+    objects, arrays, cfg = _bloch_gradient_scene(60, ckpt)
+    assert arrays.fields.E.dtype == torch.complex64
+    cots, cE, cH = _random_cotangents(arrays, 11)
+
+    def loss(out):
+        tot = _inner(cE.cuda(), out.fields.E) + _inner(cH.cuda(), out.fields.H)
+        for (dn, k), c in cots.items():
+            v = out.detector_states[dn][k]
+            tot = tot + _inner(c.cuda().to(v.dtype), v)
+        return tot
+
+    ga = _to_cuda(objects, arrays)
+    ie = ga.inv_permittivities.clone().requires_grad_(True)
+    _, out = fx.reversible_fdtd(ga.aset("inv_permittivities", ie), objects, cfg)
+    loss(out).backward()
+    torch.cuda.synchronize()
+    g_gpu = ie.grad.detach().cpu()
+    res = {}
+    for dt in (torch.float32, torch.float64):
+        sc = O.OracleScene(objects, arrays, cfg, dt)
+        cdt = sc.field_dtype
+        f = O.run(sc, cfg.time_steps_total, record_boundaries=True)
+        cd = {}
+        for (dn, k), c in cots.items():
+            cd.setdefault(dn, {})[k] = c.to(cdt if c.is_complex() else dt)
+        res[dt] = O.reversible_gradient(sc, f, cd, cE.to(cdt), cH.to(cdt))
+    # checkpoint resets change the gradient inside the CPML by design (psi is frozen in the
+    # reconstruction); outside it the sliced and the single-slice gradients are the same
+    sl = (slice(None), slice(None), slice(None), slice(6, -6)) if ckpt else (slice(None),) * 4
+    e32, e64 = rel_l2(g_gpu[sl], res[torch.float32][sl]), rel_l2(g_gpu[sl], res[torch.float64][sl])
+    log_result(f"bloch_gradient_ckpt{ckpt}", grad_rel_l2_vs_fp32=e32, grad_rel_l2_vs_fp64=e64,
+               fp32_oracle_vs_fp64=rel_l2(res[torch.float32], res[torch.float64]))
+    assert torch.linalg.vector_norm(res[torch.float64]).item() > 0
+    assert e32 <= 1e-3, (e32, e64)
+
+
+def test_bloch_gradient_matches_autograd_of_the_complex_run():
+    """The Bloch gradient of a phasor objective against float64 autograd through the oracle's
+    complex forward run (a check independent of the reversible restatement), away from the
+    CPML slabs where the reconstruction is not a time reversal."""
+    objects, arrays, cfg = _bloch_gradient_scene(50)
+    ga = _to_cuda(objects, arrays)
+    ie = ga.inv_permittivities.clone().requires_grad_(True)
+    _, out = fx.reversible_fdtd(ga.aset("inv_permittivities", ie), objects, cfg)
+    (out.detector_states["ph"]["phasor"].abs() ** 2).sum().backward()
+    g_gpu = ie.grad.detach().cpu()
+    sc = O.OracleScene(objects, arrays, cfg, torch.float64)
+    g_ad = O.autograd_gradient(sc, lambda det: (det["ph"]["phasor"].abs() ** 2).sum(), cfg.time_steps_total)
+    inner = (slice(None), slice(None), slice(None), slice(6, -6))
+    e = rel_l2(g_gpu[inner], g_ad[inner].float())
+    log_result("bloch_gradient_vs_autograd", rel_l2=e)
+    assert torch.linalg.vector_norm(g_ad).item() > 0 and e <= 1e-3, e

@@ -177,7 +177,8 @@ def test_bloch_oblique_fresnel_te():
 def test_library_bloch_description_and_gradient_refusal():
     """A non-zero Bloch vector gives complex fields (the container's E, H and psi are
     complex64) and a plan description with the axis' phase exp(i k L) on the '+' ghost; the
-    reversible gradient of such a scene is refused before any device work."""
+    inv_permeabilities gradient of such a scene is refused before any device work (the
+    inv_permittivities gradient runs on the device)."""
     from fdtdx_gb300.engine import Scene
 
     kv = (1e6, 0.0, 0.0)
@@ -190,9 +191,9 @@ def test_library_bloch_description_and_gradient_refusal():
     assert scene.complex_fields and d.bloch_axes == 1 and d.periodic[0] == 1
     assert abs(d.bloch_cos[0] - ph.real) < 1e-7 and abs(d.bloch_sin[0] - ph.imag) < 1e-7
     objects, arrays, cfg, _ = _scene({f: "bloch" for f in FACES[:2]}, kv, record=True)
-    ie = arrays.inv_permittivities.clone().requires_grad_(True)
+    mu = torch.ones((1, *arrays.inv_permittivities.shape[1:]), requires_grad=True)
     with pytest.raises(NotImplementedError, match="complex"):
-        fx.reversible_fdtd(arrays.aset("inv_permittivities", ie), objects, cfg)
+        fx.reversible_fdtd(arrays.aset("inv_permeabilities", mu), objects, cfg)
 
 
 @pytest.mark.parametrize("pml", [False, True])
