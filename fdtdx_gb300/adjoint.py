@@ -177,8 +177,6 @@ def reversible_fdtd(
     del key, show_progress
     from fdtdx_gb300.fdtd import _materials_detached, get_scene
 
-    if arrays.inv_permittivities.shape[0] not in (1, 3):
-        raise NotImplementedError("fully anisotropic (9-component) materials are not supported")
     gc = config.gradient_config
     num_ckpt = 0 if gc is None else gc.num_checkpoints_reversible
     T = config.time_steps_total
@@ -205,6 +203,9 @@ def reversible_fdtd(
     ctl = {"scene": scene, "arrays": work, "T": T, "bounds": bounds, "layout": layout,
            "inv_eps": work.inv_permittivities, "inv_mu": work.inv_permeabilities}
     wants = ie_in.requires_grad or (mu_t is not None and mu_t.requires_grad)
+    if wants and torch.is_grad_enabled() and scene.full_tensor:
+        raise NotImplementedError("the reversible gradient of full 3x3 tensor materials is not supported by the GB300 "
+                                  "kernels (their forward and reverse steps are)")
     if wants and torch.is_grad_enabled() and scene.complex_fields and mu_t is not None and mu_t.requires_grad:
         raise NotImplementedError("the inv_permeabilities gradient of complex (Bloch) fields is not supported by the "
                                   "GB300 kernels (the inv_permittivities gradient is)")

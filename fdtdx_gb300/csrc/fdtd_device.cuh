@@ -2,7 +2,8 @@
 //
 // Layout in HBM: every field is (3, nx, ny, nz) float32, C order, z fastest; the
 // component stride is N = nx*ny*nz.  Material arrays are (n, nx, ny, nz) with
-// n in {1, 3}; an isotropic array is read through component 0.  A CPML slab's
+// n in {1, 3, 9}; an isotropic array is read through component 0, a full tensor is stored
+// row-major (entry (r, c) is component 3 r + c).  A CPML slab's
 // psi arrays have the slab's shape: the full domain with `L` cells along the
 // slab axis.
 #pragma once
@@ -172,6 +173,43 @@ __device__ __forceinline__ float ld_halo_sel(const Geo& g, const float* __restri
         return bloch_mix(g, f, off, cr, ci, v);
     }
     return ok ? v : 0.f;
+}
+
+// The 3x3 tensor (row-major) of a material array at cell c: n = 9 (the full tensor), 3 (its
+// diagonal), 1 (isotropic) or no array (the scalar times the identity).
+__device__ __forceinline__ void tensor_at(const float* __restrict__ m, int n, float scalar, long long N, long long c,
+                                          float t[9]) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) t[q] = 0.f;
+    if (!m) {
+        t[0] = t[4] = t[8] = scalar;
+    } else if (n == 9) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) t[q] = __ldg(m + q * N + c);
+    } else if (n == 3) {
+        t[0] = __ldg(m + c);
+        t[4] = __ldg(m + N + c);
+        t[8] = __ldg(m + 2 * N + c);
+    } else {
+        t[0] = t[4] = t[8] = __ldg(m + c);
+    }
+}
+
+// Inverse of a 3x3 matrix by its adjugate (cofactors over the determinant).
+__device__ __forceinline__ void inverse3(const float a[9], float r[9]) {
+    const float c00 = a[4] * a[8] - a[5] * a[7];
+    const float c01 = a[5] * a[6] - a[3] * a[8];
+    const float c02 = a[3] * a[7] - a[4] * a[6];
+    const float inv_det = 1.f / (a[0] * c00 + a[1] * c01 + a[2] * c02);
+    r[0] = c00 * inv_det;
+    r[1] = (a[2] * a[7] - a[1] * a[8]) * inv_det;
+    r[2] = (a[1] * a[5] - a[2] * a[4]) * inv_det;
+    r[3] = c01 * inv_det;
+    r[4] = (a[0] * a[8] - a[2] * a[6]) * inv_det;
+    r[5] = (a[2] * a[3] - a[0] * a[5]) * inv_det;
+    r[6] = c02 * inv_det;
+    r[7] = (a[1] * a[6] - a[0] * a[7]) * inv_det;
+    r[8] = (a[0] * a[4] - a[1] * a[3]) * inv_det;
 }
 
 // Whether component `comp` at (i, j, k) is zeroed by a conductor face in `mask`

@@ -703,7 +703,8 @@ __global__ void __launch_bounds__(256, AXT && VEC == 1 ? (REV ? 5 : 4) : 3) k_up
 // ---------------------------------------------------------------------------------
 __device__ __forceinline__ float mat_at(const float* m, int n, float scalar, long long N, int comp, long long c) {
     if (!m) return scalar;
-    const int cc = comp < n ? comp : n - 1;  // an isotropic array serves every component
+    // an isotropic array serves every component; a full tensor's diagonal entry is comp * 4
+    const int cc = n == 9 ? comp * 4 : (comp < n ? comp : n - 1);
     return __ldg(m + cc * N + c);
 }
 
@@ -751,6 +752,20 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
     const float amp_b = profile_amp(s, teff + ob, ph0 + s.omega_dt * ob);
     const float inc_a = ia * amp_a;
     const float inc_b = ib * amp_b;
+    if (mat && n_mat == 9) {
+        // a full tensor on the face (tfsf.py:287-299, 384-393): every row takes both tangential
+        // terms through its (row, a) and (row, b) entries
+        const int rows[3] = {n, ax, bx};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int row = rows[q];
+            if (face_zero(g, wall, row, i, j, k)) continue;
+            const float mra = __ldg(mat + (row * 3 + ax) * g.N + c), mrb = __ldg(mat + (row * 3 + bx) * g.N + c);
+            const float corr = ESIDE ? mra * inc_b - mrb * inc_a : mrb * inc_a - mra * inc_b;
+            atomicAdd(F + row * g.N + c, sg * (s.coef * corr));
+        }
+        return;
+    }
     if (ESIDE) {
         // E[a] += sign c inv_eps[a] H_inc,b ;  E[b] -= sign c inv_eps[b] H_inc,a
         if (!face_zero(g, wall, ax, i, j, k)) atomicAdd(F + ax * g.N + c, sg * (inc_b * s.coef * ma));
@@ -907,7 +922,24 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
         }
     } else {  // energy: 0.5 sum eps |E|^2 + 0.5 sum mu |H|^2 (fdtdx/core/physics/metrics.py:55-65)
         float e = 0.f, h = 0.f;
-        if (valid) {
+        if (valid && (f.n_eps == 9 || (f.inv_mu && f.n_mu == 9))) {
+            // full tensors: 0.5 Re(E* eps E) + 0.5 Re(H* mu H), eps and mu the inverses of the
+            // stored inverse tensors (metrics.py:34-51)
+            const long long c = cell_index(g, i, j, k);
+            float t[9], m[9];
+            tensor_at(f.inv_eps, f.n_eps, 1.f, g.N, c, t);
+            inverse3(t, m);
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) e += 0.5f * m[p * 3 + q] * (v[p] * v[q] + vi[p] * vi[q]);
+            tensor_at(f.inv_mu, f.n_mu, f.mu_scalar, g.N, c, t);
+            inverse3(t, m);
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) h += 0.5f * m[p * 3 + q] * (v[3 + p] * v[3 + q] + vi[3 + p] * vi[3 + q]);
+        } else if (valid) {
             const long long c = cell_index(g, i, j, k);
 #pragma unroll
             for (int q = 0; q < 3; ++q) {

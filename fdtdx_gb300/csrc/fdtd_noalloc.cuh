@@ -52,8 +52,8 @@ extern "C" int fdtd_detector_sample_noalloc(const FdtdDetectorDesc* det, int32_t
                              (det->kind != FDTD_DET_FIELD || (det->comp_mask & 56) != 0);
     if (needs_hprev && !H_prev)
         return noalloc_reject("H_prev is required with exact interpolation of H components");
-    if (n_eps != 1 && n_eps != 3) return noalloc_reject("n_eps must be 1 or 3");
-    if (n_mu != 0 && n_mu != 1 && n_mu != 3) return noalloc_reject("n_mu must be 0, 1 or 3");
+    if (n_eps != 1 && n_eps != 3 && n_eps != 9) return noalloc_reject("n_eps must be 1, 3 or 9");
+    if (n_mu != 0 && n_mu != 1 && n_mu != 3 && n_mu != 9) return noalloc_reject("n_mu must be 0, 1, 3 or 9");
     if (det->kind == FDTD_DET_ENERGY && (!inv_eps || (n_mu && !inv_mu)))
         return noalloc_reject("the energy sample needs inv_eps (and inv_mu when n_mu > 0)");
 

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "fdtd_kernels.cuh"
+#include "fdtd_aniso.cuh"
 #include "fdtd_adjoint.cuh"
 #include "fdtd_tma.cuh"
 
@@ -33,6 +34,11 @@ struct FdtdPlan {
     float* h_twin = nullptr;     // second H buffer (ping-pong) when a detector needs H before the H update
     bool need_hprev = false;
     int parts = 1;               // 2 for complex (Bloch) fields: real parts, then imaginary parts
+    // full 3x3 tensor half-steps (a 9-component material or conductivity on that side): two
+    // passes through the curl scratch K and the field copy T (each 3 * parts * N floats)
+    bool full_e = false, full_h = false;
+    float* full_k = nullptr;
+    float* full_t = nullptr;
     bool fused[FDTD_MAX_DETECTORS] = {};  // accumulated inside the H half-step
     int n_fused = 0;
     int chunk = 1;                        // x planes per update block
@@ -246,10 +252,11 @@ int validate(const FdtdDesc* d, std::string& why) {
     if ((long long)d->nx * d->ny * d->nz * 3 >= (1ll << 40)) { why = "grid too large"; return FDTD_EINVAL; }
     if (d->nx > 65535) { why = "nx above 65535 is not supported"; return FDTD_EINVAL; }
     if (d->n_steps_total < 0) { why = "n_steps_total must be >= 0"; return FDTD_EINVAL; }
-    if (d->n_eps != 1 && d->n_eps != 3) { why = "n_eps must be 1 or 3"; return FDTD_EINVAL; }
-    if (d->n_mu != 0 && d->n_mu != 1 && d->n_mu != 3) { why = "n_mu must be 0, 1 or 3"; return FDTD_EINVAL; }
-    if (d->n_sigma_E < 0 || d->n_sigma_E > 3 || d->n_sigma_E == 2) { why = "n_sigma_E must be 0, 1 or 3"; return FDTD_EINVAL; }
-    if (d->n_sigma_H < 0 || d->n_sigma_H > 3 || d->n_sigma_H == 2) { why = "n_sigma_H must be 0, 1 or 3"; return FDTD_EINVAL; }
+    auto ncomp_ok = [](int n, bool zero) { return (zero && n == 0) || n == 1 || n == 3 || n == 9; };
+    if (!ncomp_ok(d->n_eps, false)) { why = "n_eps must be 1, 3 or 9"; return FDTD_EINVAL; }
+    if (!ncomp_ok(d->n_mu, true)) { why = "n_mu must be 0, 1, 3 or 9"; return FDTD_EINVAL; }
+    if (!ncomp_ok(d->n_sigma_E, true)) { why = "n_sigma_E must be 0, 1, 3 or 9"; return FDTD_EINVAL; }
+    if (!ncomp_ok(d->n_sigma_H, true)) { why = "n_sigma_H must be 0, 1, 3 or 9"; return FDTD_EINVAL; }
     if (d->n_slabs < 0 || d->n_slabs > FDTD_MAX_SLABS) { why = "too many slabs"; return FDTD_EINVAL; }
     if (d->rec_slots < 0 || (d->rec_slots > 0 && (!d->rec_store || !d->rec_a || !d->rec_b || !d->rec_w))) {
         why = "a recorder time filter needs rec_slots > 0 and all four tables";
@@ -524,13 +531,16 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     p->g.pother = 3 * p->g.N;
     p->g.psign = -1.f;
     p->parts = d.bloch_axes ? 2 : 1;
+    p->full_e = d.n_eps == 9 || d.n_sigma_E == 9;
+    p->full_h = d.n_mu == 9 || d.n_sigma_H == 9;
+    const bool full = p->full_e || p->full_h;
     {
         int dev = 0;
         cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) p->sm_count = 152;
         p->chunk = default_chunk(d.nx, d.ny, d.nz, p->sm_count);
         p->vec = pick_vec(d.nz);
-        p->tma_ok = d.nz % 4 == 0 && d.nz >= 8 && !d.periodic[0] && !d.periodic[1] && !d.periodic[2] && encode_fn();
+        p->tma_ok = d.nz % 4 == 0 && d.nz >= 8 && !d.periodic[0] && !d.periodic[1] && !d.periodic[2] && !full && encode_fn();
         p->tma_ty = 8;
     }
 
@@ -563,7 +573,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         const long long nb = (R + kDetBlock - 1) / kDetBlock;
         const bool red = dd.reduce_volume || dd.kind == FDTD_DET_PHASOR ? dd.reduce_volume : dd.reduce_volume;
         o.partial = red ? ar.take(4 * (size_t)nb * det_ncomp(dd)) : 0;
-        if (det_fusable(dd) && p->n_fused < kMaxFuse && p->parts == 1) {
+        if (det_fusable(dd) && p->n_fused < kMaxFuse && p->parts == 1 && !full) {
             p->fused[q] = true;
             ++p->n_fused;
         } else if (det_needs_h(dd)) {
@@ -572,6 +582,8 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     }
     size_t o_twin = 0;
     if (p->need_hprev) o_twin = ar.take(sizeof(float) * 3 * (size_t)p->parts * (size_t)p->g.N);
+    size_t o_full = 0;
+    if (full) o_full = ar.take(sizeof(float) * 6 * (size_t)p->parts * (size_t)p->g.N);
     size_t o_rec[4] = {0, 0, 0, 0};
     if (d.rec_slots > 0)
         for (int q = 0; q < 4; ++q) o_rec[q] = ar.take(4 * tbl);
@@ -678,6 +690,10 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         if (e == cudaSuccess && dd.kind == FDTD_DET_PHASOR) e = up(o.w, dd.weights, 8 * tbl * dd.n_freq);
     }
     if (p->need_hprev) p->h_twin = reinterpret_cast<float*>(p->dmem + o_twin);
+    if (full) {
+        p->full_k = reinterpret_cast<float*>(p->dmem + o_full);
+        p->full_t = p->full_k + 3 * (size_t)p->parts * (size_t)p->g.N;
+    }
     if (d.rec_slots > 0 && e == cudaSuccess) {
         e = up(o_rec[0], d.rec_store, 4 * tbl);
         if (e == cudaSuccess) e = up(o_rec[1], d.rec_a, 4 * tbl);
@@ -936,10 +952,51 @@ void launch_E(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) { launch_hal
 template <bool REV>
 void launch_H(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st) { launch_half<REV, true>(p, a, st); }
 
+UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout,
+                 int part = 0);
+UpdArgs make_upd_fwd_H(const FdtdPlan* p, const FdtdBuffers* b, const float* Hin, float* Hout);
+
+// A full 3x3 tensor half-step over every part: the curl pass of each part, then the tensor
+// pass of each part (a wrapped neighbour of one part mixes in the other part's K and T).
+template <bool REV, bool HSIDE>
+void launch_full(const FdtdPlan* p, const FdtdBuffers* b, const float* F, const float* Uin, float* Uout, cudaStream_t st) {
+    const long long N3 = 3 * p->g.N;
+    const unsigned blocks = (unsigned)((p->g.N + 255) / 256);
+    const bool inplace = Uin == Uout;
+    for (int part = 0; part < p->parts; ++part)
+        k_full_curl<REV, HSIDE><<<blocks, 256, 0, st>>>(make_upd(p, b, !HSIDE, F, Uin, Uout, part), p->full_k + part * N3,
+                                                        inplace ? p->full_t + part * N3 : nullptr);
+    for (int part = 0; part < p->parts; ++part) {
+        const UpdArgs a = make_upd(p, b, !HSIDE, F, Uin, Uout, part);
+        k_full_apply<REV, HSIDE><<<blocks, 256, 0, st>>>(a, p->full_k + part * N3, inplace ? p->full_t + part * N3 : a.Uin);
+    }
+}
+
+// One half-step of every part: the tensor passes on a full-tensor side, else the core / shell
+// launches part by part (the forward H step of real fields with its fused detectors).
+template <bool REV, bool HSIDE>
+void launch_side(const FdtdPlan* p, const FdtdBuffers* b, const float* F, const float* Uin, float* Uout, cudaStream_t st) {
+    if (HSIDE ? p->full_h : p->full_e) {
+        launch_full<REV, HSIDE>(p, b, F, Uin, Uout, st);
+        return;
+    }
+    if (HSIDE && !REV && p->parts == 1) {
+        launch_half<false, true>(p, make_upd_fwd_H(p, b, Uin, Uout), st);
+        return;
+    }
+    for (int part = 0; part < p->parts; ++part) launch_half<REV, HSIDE>(p, make_upd(p, b, !HSIDE, F, Uin, Uout, part), st);
+}
+
+// Launches of one half-step of every part.
+int side_launches(const FdtdPlan* p, bool hside) {
+    if (hside ? p->full_h : p->full_e) return 2 * p->parts;
+    return p->parts * half_step_launches(p);
+}
+
 // The arguments of one half-step; `part` 1 selects the imaginary parts of complex (Bloch)
 // fields (planar buffers: the real parts, then the imaginary parts).
 UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const float* F, const float* Uin, float* Uout,
-                 int part = 0) {
+                 int part) {
     UpdArgs a{};
     a.g = p->g;
     const long long po = part ? 3 * p->g.N : 0;
@@ -991,7 +1048,7 @@ UpdArgs make_upd(const FdtdPlan* p, const FdtdBuffers* b, bool eside, const floa
 
 // The forward H step also accumulates the fused detectors.
 UpdArgs make_upd_fwd_H(const FdtdPlan* p, const FdtdBuffers* b, const float* Hin, float* Hout) {
-    UpdArgs a = make_upd(p, b, false, b->E, Hin, Hout);
+    UpdArgs a = make_upd(p, b, false, b->E, Hin, Hout, 0);
     for (int q = 0; q < p->d.n_detectors; ++q) {
         if (!p->fused[q]) continue;
         const DDet& dd = p->det[q];
@@ -1061,11 +1118,9 @@ DetFields det_fields(const FdtdPlan* p, const FdtdBuffers* b, const float* Hprev
 // One forward step (fdtdx/fdtd/forward.py:83-156): update_E, E sources (+PEC inside the
 // update), update_H, H sources (+PMC), interface recording, detectors, advance t.
 void launch_forward_step(const FdtdPlan* p, const FdtdBuffers* b, float* Hcur, float* Hnext, cudaStream_t st) {
-    for (int part = 0; part < p->parts; ++part) launch_E<false>(p, make_upd(p, b, true, Hcur, b->E, b->E, part), st);
+    launch_side<false, false>(p, b, Hcur, b->E, b->E, st);
     launch_sources(p, b, true, b->E, 0, st);  // sources are real: they drive the real parts
-    if (p->parts == 1) launch_H<false>(p, make_upd_fwd_H(p, b, Hcur, Hnext), st);
-    else
-        for (int part = 0; part < p->parts; ++part) launch_H<false>(p, make_upd(p, b, false, b->E, Hcur, Hnext, part), st);
+    launch_side<false, true>(p, b, b->E, Hcur, Hnext, st);
     launch_sources(p, b, false, Hnext, 0, st);
     if (p->d.record_interfaces) interfaces<false>(p, b, Hnext, st);
     const DetFields f = det_fields(p, b, Hcur, Hnext);
@@ -1102,7 +1157,7 @@ extern "C" {
 
 int32_t fdtd_launches_per_step(const FdtdPlan* p) {
     if (!p) return 0;
-    int n = 2 * p->parts * half_step_launches(p) + sources_launched(p, true) + sources_launched(p, false) + 1;
+    int n = side_launches(p, false) + side_launches(p, true) + sources_launched(p, true) + sources_launched(p, false) + 1;
     if (p->d.record_interfaces && p->d.n_slabs) n += p->parts;
     for (int q = 0; q < p->d.n_detectors; ++q)
         if (!p->fused[q]) n += p->det[q].reduce ? 2 : 1;
@@ -1195,9 +1250,9 @@ int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_ste
     for (int s = 0; s < n_steps; ++s) {
         interfaces<true>(p, b, b->H, st);
         launch_sources(p, b, false, b->H, 1, st);
-        for (int part = 0; part < p->parts; ++part) launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H, part), st);
+        launch_side<true, true>(p, b, b->E, b->H, b->H, st);
         launch_sources(p, b, true, b->E, 1, st);
-        for (int part = 0; part < p->parts; ++part) launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E, part), st);
+        launch_side<true, false>(p, b, b->H, b->E, b->E, st);
         k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
     }
     cudaError_t e = cudaGetLastError();
@@ -1210,6 +1265,7 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
     const long long N = (long long)d->nx * d->ny * d->nz;
     const int parts = d->bloch_axes ? 2 : 1;
     long long bytes = 4ll * N * (3 * parts + 3 * parts + d->n_eps + d->n_mu + d->n_sigma_E + d->n_sigma_H);
+    if (d->n_eps == 9 || d->n_mu == 9 || d->n_sigma_E == 9 || d->n_sigma_H == 9) bytes += 24ll * parts * N;  // K and T
     const int n3[3] = {d->nx, d->ny, d->nz};
     long long iface = 0, psi = 0;
     for (int s = 0; s < d->n_slabs; ++s) {
@@ -1248,6 +1304,8 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
 extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t0, int32_t n_steps, float* out_ms,
                                     void* stream) {
     if (p && p->parts != 1) return fail(p, FDTD_EINVAL, "per-launch profiling of complex (Bloch) fields is not supported");
+    if (p && (p->full_e || p->full_h))
+        return fail(p, FDTD_EINVAL, "per-launch profiling of full 3x3 tensor materials is not supported");
     if (!p || !out_ms) return FDTD_EINVAL;
     if (int rc = check_bufs(p, b)) return rc;
     if (n_steps <= 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)

@@ -124,15 +124,27 @@ def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> list[
         # dipole, every axis the tilted orientation reaches otherwise (dipole.py:219-232), each
         # scaled by c * amplitude * inv_material[axis] * orientation[axis]
         orient = src.orientation
-        axes = [src.polarization] if not src.is_tilted else [a for a in range(3) if orient[a] != 0.0]
+        full = isinstance(m, torch.Tensor) and m.dim() > 0 and m.shape[0] == 9
+        if full:
+            # a full tensor couples the orientation into every component: sum_j inv_aj p_j
+            # (_contract_orientation, dipole.py:15-37); every component is injected
+            t = m[:, i, j, k].detach().double().cpu().numpy().reshape(3, 3)
+            oriented = t @ np.asarray(orient, dtype=np.float64)
+            axes = [a for a in range(3) if oriented[a] != 0.0]
+        else:
+            axes = [src.polarization] if not src.is_tilted else [a for a in range(3) if orient[a] != 0.0]
         out = []
         for a in axes:
-            local = float(m) if not isinstance(m, torch.Tensor) else float(m[min(a, m.shape[0] - 1), i, j, k])
+            if full:
+                weight = float(oriented[a])
+            else:
+                local = float(m) if not isinstance(m, torch.Tensor) else float(m[min(a, m.shape[0] - 1), i, j, k])
+                weight = local * (1.0 if not src.is_tilted else orient[a])
             da = N.SourceDesc.from_buffer_copy(d)
             da.kind = N.SRC_DIPOLE
             da.component = a
             da.magnetic = 1 if magnetic else 0
-            da.coef = c * src.amplitude * src.static_amplitude_factor * local * (1.0 if not src.is_tilted else orient[a])
+            da.coef = c * src.amplitude * src.static_amplitude_factor * weight
             out.append(SourceTables(da, keep))
         return out
     if isinstance(src, LinearlyPolarizedPlaneSource):
@@ -145,6 +157,54 @@ def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> list[
         d.inc_E, d.inc_H, d.off_E, d.off_H = (x.ctypes.data for x in (incE, incH, offE, offH))
         return [SourceTables(d, keep)]
     raise NotImplementedError(f"source type {type(src).__name__} is not supported")
+
+
+def _tensor3(m, face_shape) -> np.ndarray:
+    """(3, 3, *face) tensor of a (1 | 3 | 9, *face) material slice or a scalar."""
+    if not isinstance(m, np.ndarray):
+        return np.broadcast_to(np.eye(3)[:, :, None, None, None] * m, (3, 3, *face_shape))
+    if m.shape[0] == 9:
+        return m.reshape(3, 3, *m.shape[1:])
+    out = np.zeros((3, 3, *m.shape[1:]))
+    for q in range(3):
+        out[q, q] = m[min(q, m.shape[0] - 1)]
+    return out
+
+
+def _is_full(m) -> bool:
+    return isinstance(m, np.ndarray) and m.shape[0] == 9
+
+
+def _medium_scaling(src, ie, im, E, Hf, e_pol, h_pol):
+    """Energy normalisation and impedance scaling of the incident profiles
+    (linear_polarization.py:186-211).  In tensor media eps and mu are the per-cell inverses of
+    the stored inverse tensors: the energy is 0.5 E.eps.E + 0.5 H.mu.H (metrics.py:34-51) and H
+    is divided by sqrt(mu_eff / eps_eff) with eps_eff = e.eps.e, mu_eff = h.mu.h
+    (tfsf.py:144-190); the plane must then lie in an isotropic tensor, as the reference's time
+    offsets require (fdtdx/core/grid.py:781-861)."""
+    if not (_is_full(ie) or _is_full(im)):
+        if src.normalize_by_energy:
+            energy = (0.5 * (1.0 / ie) * E**2).sum(axis=0) + (0.5 * (1.0 / im) * Hf**2).sum(axis=0)
+            root = math.sqrt(float(energy.sum()))
+            E = E / root
+            Hf = Hf / root
+        return E, Hf / np.sqrt(ie / im)
+    face = E.shape[1:]
+    inv_t = [_tensor3(m, face) for m in (ie, im)]
+    eps_t, mu_t = (np.moveaxis(np.linalg.inv(np.moveaxis(t, (0, 1), (-2, -1))), (-2, -1), (0, 1)) for t in inv_t)
+    if src.normalize_by_energy:
+        energy = 0.5 * np.einsum("ixyz,ijxyz,jxyz->xyz", E, eps_t, E) + 0.5 * np.einsum("ixyz,ijxyz,jxyz->xyz", Hf, mu_t, Hf)
+        root = math.sqrt(float(energy.sum()))
+        E = E / root
+        Hf = Hf / root
+    eps_eff = np.einsum("i,ijxyz,j->xyz", np.asarray(e_pol, np.float64), eps_t, np.asarray(e_pol, np.float64))
+    mu_eff = np.einsum("i,ijxyz,j->xyz", np.asarray(h_pol, np.float64), mu_t, np.asarray(h_pol, np.float64))
+    Hf = Hf / np.sqrt(mu_eff / eps_eff)
+    for m in (ie, im):
+        if _is_full(m):
+            if not (np.allclose(m[[1, 2, 3, 5, 6, 7]], 0.0) and np.allclose(m[0], m[4]) and np.allclose(m[4], m[8])):
+                raise NotImplementedError("Gaussian or planewave sources within anisotropic materials")
+    return E, Hf
 
 
 def plane_source_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContainer, config: SimulationConfig):
@@ -170,12 +230,7 @@ def plane_source_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContai
     ie = arrays.inv_permittivities[sl].detach().double().cpu().numpy()
     mu = arrays.inv_permeabilities
     im = mu[sl].detach().double().cpu().numpy() if isinstance(mu, torch.Tensor) else float(mu)
-    if src.normalize_by_energy:
-        energy = (0.5 * (1.0 / ie) * E**2).sum(axis=0) + (0.5 * (1.0 / im) * Hf**2).sum(axis=0)
-        root = math.sqrt(float(energy.sum()))
-        E = E / root
-        Hf = Hf / root
-    Hf = Hf / np.sqrt(ie / im)
+    E, Hf = _medium_scaling(src, ie, im, E, Hf, e_pol, h_pol)
     # Yee positions along the normal: 0.5 dx for components staggered along it
     stag_E = [0.5 if comp == n else 0.0 for comp in range(3)]
     stag_H = [0.0 if comp == n else 0.5 for comp in range(3)]
@@ -245,12 +300,7 @@ def _tilted_plane_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayConta
     ie = arrays.inv_permittivities[sl].detach().double().cpu().numpy()
     mu = arrays.inv_permeabilities
     im = mu[sl].detach().double().cpu().numpy() if isinstance(mu, torch.Tensor) else float(mu)
-    if src.normalize_by_energy:
-        energy = (0.5 * (1.0 / ie) * E**2).sum(axis=0) + (0.5 * (1.0 / im) * Hf**2).sum(axis=0)
-        root = math.sqrt(float(energy.sum()))
-        E = E / root
-        Hf = Hf / root
-    Hf = Hf / np.sqrt(ie / im)
+    E, Hf = _medium_scaling(src, ie, im, E, Hf, e_pol, h_pol)
     # Yee positions in the plane's frame: component q of E sits half a cell along axis q, of H
     # half a cell along the other two axes; the plane's centre is (ch, cv) cells across, 0 along n
     centre = np.zeros(3)
@@ -385,12 +435,14 @@ class Scene:
         mu = arrays.inv_permeabilities
         d.n_mu = mu.shape[0] if isinstance(mu, torch.Tensor) else 0
         d.inv_mu_scalar = 1.0 if isinstance(mu, torch.Tensor) else float(mu)
-        if d.n_eps not in (1, 3) or d.n_mu not in (0, 1, 3):
-            raise NotImplementedError("fully anisotropic (9-component) materials are not supported by the GB300 kernels")
+        if d.n_eps not in (1, 3, 9) or d.n_mu not in (0, 1, 3, 9):
+            raise ValueError("material arrays have 1, 3 or 9 components")
         if any(getattr(o.material, "is_dispersive", False) for o in objects.static_material_objects):
             raise NotImplementedError("dispersive (ADE) materials are not supported by the GB300 kernels")
         d.n_sigma_E = arrays.electric_conductivity.shape[0] if arrays.electric_conductivity is not None else 0
         d.n_sigma_H = arrays.magnetic_conductivity.shape[0] if arrays.magnetic_conductivity is not None else 0
+        # a 9-component material or conductivity runs that side's tensor half-steps
+        self.full_tensor = 9 in (d.n_eps, d.n_mu, d.n_sigma_E, d.n_sigma_H)
         bloch: dict[int, list] = {}
         for b in objects.boundary_objects:
             side = 1 if b.direction == "+" else 0

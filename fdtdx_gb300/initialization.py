@@ -14,6 +14,7 @@ from __future__ import annotations
 import dataclasses
 from typing import Sequence
 
+import numpy as np
 import torch
 
 from fdtdx_gb300.config import SimulationConfig
@@ -59,16 +60,28 @@ def detector_state_shapes(det: Detector, config: SimulationConfig) -> dict[str, 
 
 
 def _n_components(materials: Sequence[Material], attr: str) -> int:
+    """1 (isotropic), 3 (diagonal) or 9 (a full tensor somewhere) components for ``attr``
+    (fdtdx/fdtd/initialization.py:552-620 picks the array width the same way)."""
     vals = [getattr(m, attr) for m in materials]
     if all(Material._iso(v) for v in vals):
         return 1
     if all(Material._diag(v) for v in vals):
         return 3
-    raise NotImplementedError(f"fully anisotropic (off-diagonal) {attr} is not supported")
+    return 9
 
 
 def _comp_values(t9, n: int) -> list[float]:
+    if n == 9:
+        return list(t9)
     return [t9[0]] if n == 1 else [t9[0], t9[4], t9[8]]
+
+
+def _inverse_values(t9, n: int) -> list[float]:
+    """The stored inverse of a permittivity / permeability: elementwise for 1 or 3 components,
+    the matrix inverse of the row-major tensor for 9 (initialization.py:866-877, 2145-2161)."""
+    if n == 9:
+        return [float(x) for x in np.linalg.inv(np.asarray(t9, dtype=np.float64).reshape(3, 3)).reshape(9)]
+    return [1.0 / v for v in _comp_values(t9, n)]
 
 
 def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None) -> ArrayContainer:
@@ -112,9 +125,9 @@ def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None)
     sig_h = torch.zeros((n_sh, *shape), dtype=torch.float32) if mcond else None
     for o, m in painted:
         sl = (slice(None), *o.grid_slice)
-        inv_eps[sl] = (1.0 / torch.tensor(_comp_values(m.permittivity, n_eps), dtype=torch.float32))[:, None, None, None]
+        inv_eps[sl] = torch.tensor(_inverse_values(m.permittivity, n_eps), dtype=torch.float32)[:, None, None, None]
         if inv_mu is not None:
-            inv_mu[sl] = (1.0 / torch.tensor(_comp_values(m.permeability, n_mu), dtype=torch.float32))[:, None, None, None]
+            inv_mu[sl] = torch.tensor(_inverse_values(m.permeability, n_mu), dtype=torch.float32)[:, None, None, None]
         if sig_e is not None:
             sig_e[sl] = (torch.tensor(_comp_values(m.electric_conductivity, n_se), dtype=torch.float32) * spacing)[
                 :, None, None, None]
@@ -204,5 +217,9 @@ def apply_params(arrays: ArrayContainer, objects: ObjectContainer, params: Param
     for d in objects.devices:
         p = params[d.name]
         eps = d.permittivity_low + p * (d.permittivity_high - d.permittivity_low)
-        inv[(slice(None), *d.grid_slice)] = (1.0 / eps)[None].expand(inv.shape[0], *p.shape)
+        if inv.shape[0] == 9:  # an isotropic device inside a full-tensor array: diag(1 / eps)
+            z = torch.zeros_like(eps)
+            inv[(slice(None), *d.grid_slice)] = torch.stack([1.0 / eps if q % 4 == 0 else z for q in range(9)])
+        else:
+            inv[(slice(None), *d.grid_slice)] = (1.0 / eps)[None].expand(inv.shape[0], *p.shape)
     return dataclasses.replace(arrays, inv_permittivities=inv), objects, {}
