@@ -58,6 +58,8 @@ class SourceDesc(C.Structure):
         ("phase_H", C.c_void_p),
         ("teff", C.c_void_p),
         ("on", C.c_void_p),
+        ("e_table", C.c_void_p),
+        ("n_e_table", C.c_int32),
     ]
 
 
@@ -111,6 +113,8 @@ class Desc(C.Structure):
         ("bloch_axes", C.c_int32),
         ("bloch_cos", C.c_float * 3),
         ("bloch_sin", C.c_float * 3),
+        ("n_poles", C.c_int32),
+        ("n_disp", C.c_int32),
     ]
 
 
@@ -126,6 +130,11 @@ class Buffers(C.Structure):
         ("psi_H", (C.c_void_p * 2) * MAX_SLABS),
         ("det_state", C.c_void_p * MAX_DETECTORS),
         ("recording", C.c_void_p),
+        ("disp_P_curr", C.c_void_p),
+        ("disp_P_prev", C.c_void_p),
+        ("disp_c1", C.c_void_p),
+        ("disp_c2", C.c_void_p),
+        ("disp_c3", C.c_void_p),
     ]
 
 

@@ -177,6 +177,11 @@ def reversible_fdtd(
     del key, show_progress
     from fdtdx_gb300.fdtd import _materials_detached, get_scene
 
+    if arrays.dispersive_c1 is not None or arrays.fields.dispersive_P_curr is not None:
+        # as the reference (fdtd.py:98-104): the ADE polarisation cannot be time-reversed
+        raise NotImplementedError("reversible_fdtd does not support dispersive materials: use the checkpointed "
+                                  "gradient method for dispersive simulations")
+
     gc = config.gradient_config
     num_ckpt = 0 if gc is None else gc.num_checkpoints_reversible
     T = config.time_steps_total

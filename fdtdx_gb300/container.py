@@ -4,9 +4,11 @@
 
 * ``fields.E`` / ``fields.H``           (3, nx, ny, nz) float32
 * ``fields.psi_E`` / ``fields.psi_H``   {pml name: (psi_1, psi_2)}, each ``pml.grid_shape``
-* ``inv_permittivities``                (1|3, nx, ny, nz)
-* ``inv_permeabilities``                float 1.0 (non-magnetic) or (1|3, nx, ny, nz)
-* ``electric_conductivity`` / ``magnetic_conductivity``  None or (1|3, nx, ny, nz), pre-scaled by dx
+* ``inv_permittivities``                (1|3|9, nx, ny, nz) (9: a row-major full tensor)
+* ``inv_permeabilities``                float 1.0 (non-magnetic) or (1|3|9, nx, ny, nz)
+* ``electric_conductivity`` / ``magnetic_conductivity``  None or (1|3|9, nx, ny, nz), pre-scaled by dx
+* ``fields.dispersive_P_curr`` / ``_P_prev``  None or (poles, 3, nx, ny, nz): the ADE polarisation
+* ``dispersive_c1`` / ``_c2`` / ``_c3``  None or (poles, 1|3, nx, ny, nz): its recurrence coefficients
 * ``detector_states``                   {detector name: {key: tensor}}
 * ``recording_state``                   None or ``RecordingState`` of the PML-interface recorder
 """
@@ -55,6 +57,8 @@ class FieldState:
     H: torch.Tensor
     psi_E: PmlAuxField
     psi_H: PmlAuxField
+    dispersive_P_curr: torch.Tensor | None = None
+    dispersive_P_prev: torch.Tensor | None = None
 
     def aset(self, path: str, value) -> "FieldState":
         return _aset(self, path, value)
@@ -70,6 +74,10 @@ class ArrayContainer:
     electric_conductivity: torch.Tensor | None = None
     magnetic_conductivity: torch.Tensor | None = None
     initial_inv_permittivities: torch.Tensor | None = None
+    dispersive_c1: torch.Tensor | None = None
+    dispersive_c2: torch.Tensor | None = None
+    dispersive_c3: torch.Tensor | None = None
+    dispersive_c4: torch.Tensor | None = None
 
     def aset(self, path: str, value) -> "ArrayContainer":
         """Functional update, ``arrays.aset("fields->E", E)`` as in fdtdx."""
@@ -83,6 +91,8 @@ class ArrayContainer:
             H=torch.zeros_like(f.H),
             psi_E={k: (torch.zeros_like(a), torch.zeros_like(b)) for k, (a, b) in f.psi_E.items()},
             psi_H={k: (torch.zeros_like(a), torch.zeros_like(b)) for k, (a, b) in f.psi_H.items()},
+            dispersive_P_curr=None if f.dispersive_P_curr is None else torch.zeros_like(f.dispersive_P_curr),
+            dispersive_P_prev=None if f.dispersive_P_prev is None else torch.zeros_like(f.dispersive_P_prev),
         )
         det = self.detector_states
         if reset_detector_states:

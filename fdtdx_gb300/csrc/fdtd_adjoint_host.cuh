@@ -195,6 +195,7 @@ int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
         return fail(p, FDTD_EINVAL, "grad_inv_mu needs an inv_mu array (n_mu 1 or 3), not a scalar inv_mu");
     if (p->full_e || p->full_h)
         return fail(p, FDTD_EINVAL, "the reversible gradient of full 3x3 tensor materials is not supported");
+    if (p->d.n_poles > 0) return fail(p, FDTD_EINVAL, "the reversible gradient of dispersive materials is not supported");
     return FDTD_OK;
 }
 

@@ -279,6 +279,11 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
             fprintf(stderr, "fdtd_batch_create: simulation %d has complex (Bloch) fields, which batches do not run\n", s);
             return FDTD_EINVAL;
         }
+        if (p->d.n_poles > 0) {
+            delete b;
+            fprintf(stderr, "fdtd_batch_create: simulation %d has dispersive materials, which batches do not run\n", s);
+            return FDTD_EINVAL;
+        }
         if (p->full_e || p->full_h) {
             delete b;
             fprintf(stderr, "fdtd_batch_create: simulation %d has full 3x3 tensor materials, which batches do not run\n", s);

@@ -102,6 +102,8 @@ struct DSource {
     const float* phH;
     const float* teff;
     const uint8_t* on;
+    const float* etab;          // dispersive scenes: the E side's profile at integer steps (or nullptr)
+    int n_etab;
 };
 
 struct DDet {
@@ -238,6 +240,17 @@ __device__ __forceinline__ float profile_amp(const DSource& s, float tau, float 
     }
     const float d = tau - s.t0;
     return expf(-d * d * s.inv2s2) * carrier;
+}
+
+// The tabulated E-side profile of a plane source in a dispersive scene at tau (in steps):
+// linear interpolation between integer steps, 0 outside [0, n - 1] (numpy.interp with zero
+// fill, fdtdx/objects/sources/tfsf.py:256-261).
+__device__ __forceinline__ float table_amp(const DSource& s, float tau) {
+    if (!(tau >= 0.f) || tau > (float)(s.n_etab - 1)) return 0.f;
+    const int i = (int)tau;
+    const float a = __ldg(s.etab + i);
+    const float b = i + 1 < s.n_etab ? __ldg(s.etab + i + 1) : a;
+    return a + (tau - (float)i) * (b - a);
 }
 
 template <typename T>

@@ -748,8 +748,10 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
     if (!s.on[ti]) return;
     const float teff = s.teff[ti] + (ESIDE ? 0.f : 0.5f);
     const float ph0 = ESIDE ? s.phE[ti] : s.phH[ti];
-    const float amp_a = profile_amp(s, teff + oa, ph0 + s.omega_dt * oa);
-    const float amp_b = profile_amp(s, teff + ob, ph0 + s.omega_dt * ob);
+    // E side in a dispersive scene: the broadband-filtered table of the H incident profile
+    const bool tab = ESIDE && s.etab;
+    const float amp_a = tab ? table_amp(s, teff + oa) : profile_amp(s, teff + oa, ph0 + s.omega_dt * oa);
+    const float amp_b = tab ? table_amp(s, teff + ob) : profile_amp(s, teff + ob, ph0 + s.omega_dt * ob);
     const float inc_a = ia * amp_a;
     const float inc_b = ib * amp_b;
     if (mat && n_mat == 9) {
@@ -775,6 +777,39 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
         if (!face_zero(g, wall, bx, i, j, k)) atomicAdd(F + bx * g.N + c, sg * (inc_a * s.coef * mb));
         if (!face_zero(g, wall, ax, i, j, k)) atomicAdd(F + ax * g.N + c, -(sg * (inc_b * s.coef * ma)));
     }
+}
+
+// ADE polarisation step before the E update (fdtdx/fdtd/update.py:316-350), one thread per
+// component and cell: P_hat = c1 P^n + c2 P^(n-1) + c3 E^n for every pole, P^(n-1) <- P^n,
+// P^n <- P_hat, and E^n <- E^n + inv_eps sum_poles (P^n - P_hat) / f with f = 1 - q the
+// conductivity factor, so that the E kernel's (f E + c curl inv_eps) / (1 + q) equals the
+// reference's (f E + c curl inv_eps + inv_eps sum (P^n - P_hat)) / (1 + q).  Cells without a
+// pole hold zero coefficients and stay unchanged.
+__global__ void __launch_bounds__(256) k_ade(const Geo g, float* __restrict__ E, float* __restrict__ Pc,
+                                             float* __restrict__ Pp, const float* __restrict__ c1,
+                                             const float* __restrict__ c2, const float* __restrict__ c3, int np, int nd,
+                                             const float* __restrict__ inv_eps, int n_eps, const float* __restrict__ sig,
+                                             int n_sig) {
+    const long long N = g.N;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * N) return;
+    const int comp = (int)(idx / N);
+    const long long c = idx - comp * N;
+    const float e = E[idx];
+    float delta = 0.f;
+    for (int p = 0; p < np; ++p) {
+        const long long pi = ((long long)p * 3 + comp) * N + c;
+        const long long ci = ((long long)p * nd + (nd == 3 ? comp : 0)) * N + c;
+        const float pc = Pc[pi], pp = Pp[pi];
+        const float ph = __ldg(c1 + ci) * pc + __ldg(c2 + ci) * pp + __ldg(c3 + ci) * e;
+        delta += pc - ph;
+        Pp[pi] = pc;
+        Pc[pi] = ph;
+    }
+    const float m = __ldg(inv_eps + (n_eps == 3 ? comp : 0) * N + c);
+    float add = m * delta;
+    if (sig) add /= 1.f - g.c * __ldg(sig + (n_sig == 3 ? comp : 0) * N + c) * g.eta0 * m / 2.f;
+    E[idx] = e + add;
 }
 
 template <bool ESIDE>

@@ -258,6 +258,15 @@ int validate(const FdtdDesc* d, std::string& why) {
     if (!ncomp_ok(d->n_sigma_E, true)) { why = "n_sigma_E must be 0, 1, 3 or 9"; return FDTD_EINVAL; }
     if (!ncomp_ok(d->n_sigma_H, true)) { why = "n_sigma_H must be 0, 1, 3 or 9"; return FDTD_EINVAL; }
     if (d->n_slabs < 0 || d->n_slabs > FDTD_MAX_SLABS) { why = "too many slabs"; return FDTD_EINVAL; }
+    if (d->n_poles < 0 || (d->n_poles > 0 && d->n_disp != 1 && d->n_disp != 3)) {
+        why = "dispersive poles need n_disp 1 or 3";
+        return FDTD_EINVAL;
+    }
+    if (d->n_poles > 0 && d->bloch_axes) { why = "dispersive materials with complex (Bloch) fields are not supported"; return FDTD_EINVAL; }
+    if (d->n_poles > 0 && (d->n_eps == 9 || d->n_sigma_E == 9)) {
+        why = "dispersive materials with a full-tensor permittivity are not supported";
+        return FDTD_EINVAL;
+    }
     if (d->rec_slots < 0 || (d->rec_slots > 0 && (!d->rec_store || !d->rec_a || !d->rec_b || !d->rec_w))) {
         why = "a recorder time filter needs rec_slots > 0 and all four tables";
         return FDTD_EINVAL;
@@ -287,7 +296,7 @@ int validate(const FdtdDesc* d, std::string& why) {
         if (!so.phase_E || !so.phase_H || !so.teff || !so.on) { why = "source tables missing"; return FDTD_EINVAL; }
         if (so.kind == FDTD_SRC_PLANE) {
             if (so.normal_axis < 0 || so.normal_axis > 2 || so.hi[so.normal_axis] - so.lo[so.normal_axis] != 1 || !so.inc_E ||
-                !so.inc_H || !so.off_E || !so.off_H) {
+                !so.inc_H || !so.off_E || !so.off_H || (so.e_table && so.n_e_table <= 0)) {
                 why = "invalid plane source";
                 return FDTD_EINVAL;
             }
@@ -549,7 +558,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     const size_t o_t = ar.take(sizeof(int) * 4);
     std::vector<size_t> o_slab(d.n_slabs);
     for (int s = 0; s < d.n_slabs; ++s) o_slab[s] = ar.take(sizeof(float) * 6 * d.slabs[s].thickness);
-    struct SrcOff { size_t incE, incH, offE, offH, phE, phH, teff, on; };
+    struct SrcOff { size_t incE, incH, offE, offH, phE, phH, teff, on, etab; };
     std::vector<SrcOff> o_src(d.n_sources);
     const size_t tbl = (size_t)p->n_table;
     for (int s = 0; s < d.n_sources; ++s) {
@@ -559,6 +568,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
             const size_t P = (size_t)face_cells(so);
             o.incE = ar.take(4 * 3 * P); o.incH = ar.take(4 * 3 * P);
             o.offE = ar.take(4 * 3 * P); o.offH = ar.take(4 * 3 * P);
+            o.etab = so.e_table ? ar.take(4 * (size_t)so.n_e_table) : 0;
         }
         o.phE = ar.take(4 * tbl); o.phH = ar.take(4 * tbl); o.teff = ar.take(4 * tbl); o.on = ar.take(tbl);
     }
@@ -651,6 +661,8 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         ds.sign = so.sign; ds.coef = so.coef; ds.omega_dt = so.omega_dt; ds.ramp_inv = so.ramp_inv_steps;
         ds.t0 = so.t0_steps; ds.inv2s2 = so.inv_two_sigma2;
         ds.incE = ds.incH = ds.offE = ds.offH = nullptr;
+        ds.etab = nullptr;
+        ds.n_etab = 0;
         if (so.kind == FDTD_SRC_PLANE) {
             const size_t P = (size_t)face_cells(so);
             ds.incE = reinterpret_cast<const float*>(p->dmem + o.incE);
@@ -661,6 +673,11 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
             if (e == cudaSuccess) e = up(o.incH, so.inc_H, 12 * P);
             if (e == cudaSuccess) e = up(o.offE, so.off_E, 12 * P);
             if (e == cudaSuccess) e = up(o.offH, so.off_H, 12 * P);
+            if (so.e_table) {
+                ds.etab = reinterpret_cast<const float*>(p->dmem + o.etab);
+                ds.n_etab = so.n_e_table;
+                if (e == cudaSuccess) e = up(o.etab, so.e_table, 4 * (size_t)so.n_e_table);
+            }
         }
         ds.phE = reinterpret_cast<const float*>(p->dmem + o.phE);
         ds.phH = reinterpret_cast<const float*>(p->dmem + o.phH);
@@ -716,7 +733,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
     for (int s = 0; s < p->d.n_slabs; ++s) p->d.slabs[s].coef = nullptr;
     for (int s = 0; s < p->d.n_sources; ++s) {
         FdtdSourceDesc& so = p->d.sources[s];
-        so.inc_E = so.inc_H = so.off_E = so.off_H = so.phase_E = so.phase_H = so.teff = nullptr;
+        so.inc_E = so.inc_H = so.off_E = so.off_H = so.phase_E = so.phase_H = so.teff = so.e_table = nullptr;
         so.on = nullptr;
     }
     for (int q = 0; q < p->d.n_detectors; ++q) {
@@ -1118,6 +1135,12 @@ DetFields det_fields(const FdtdPlan* p, const FdtdBuffers* b, const float* Hprev
 // One forward step (fdtdx/fdtd/forward.py:83-156): update_E, E sources (+PEC inside the
 // update), update_H, H sources (+PMC), interface recording, detectors, advance t.
 void launch_forward_step(const FdtdPlan* p, const FdtdBuffers* b, float* Hcur, float* Hnext, cudaStream_t st) {
+    if (p->d.n_poles > 0) {
+        const long long n = 3 * p->g.N;
+        k_ade<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p->g, b->E, b->disp_P_curr, b->disp_P_prev, b->disp_c1, b->disp_c2,
+                                                           b->disp_c3, p->d.n_poles, p->d.n_disp, b->inv_eps, p->d.n_eps,
+                                                           p->d.n_sigma_E ? b->sigma_E : nullptr, p->d.n_sigma_E);
+    }
     launch_side<false, false>(p, b, Hcur, b->E, b->E, st);
     launch_sources(p, b, true, b->E, 0, st);  // sources are real: they drive the real parts
     launch_side<false, true>(p, b, b->E, Hcur, Hnext, st);
@@ -1143,6 +1166,8 @@ int check_bufs(FdtdPlan* p, const FdtdBuffers* b) {
             return fail(p, FDTD_EINVAL, "psi buffers required for every slab");
     for (int q = 0; q < p->d.n_detectors; ++q)
         if (!b->det_state[q]) return fail(p, FDTD_EINVAL, "detector state buffer missing");
+    if (p->d.n_poles > 0 && (!b->disp_P_curr || !b->disp_P_prev || !b->disp_c1 || !b->disp_c2 || !b->disp_c3))
+        return fail(p, FDTD_EINVAL, "a dispersive scene needs the polarisation and coefficient buffers");
     // the update kernels read and write `vec` consecutive floats at once
     const uintptr_t mask = (uintptr_t)(4 * p->vec - 1);
     const void* vecbufs[] = {b->E, b->H, b->inv_eps, b->inv_mu, b->sigma_E, b->sigma_H};
@@ -1158,6 +1183,7 @@ extern "C" {
 int32_t fdtd_launches_per_step(const FdtdPlan* p) {
     if (!p) return 0;
     int n = side_launches(p, false) + side_launches(p, true) + sources_launched(p, true) + sources_launched(p, false) + 1;
+    if (p->d.n_poles > 0) ++n;
     if (p->d.record_interfaces && p->d.n_slabs) n += p->parts;
     for (int q = 0; q < p->d.n_detectors; ++q)
         if (!p->fused[q]) n += p->det[q].reduce ? 2 : 1;
@@ -1244,6 +1270,7 @@ int fdtd_reverse(FdtdPlan* p, const FdtdBuffers* b, int32_t t_end, int32_t n_ste
     if (int rc = check_bufs(p, b)) return rc;
     if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)
         return fail(p, FDTD_EINVAL, "reverse steps out of the range covered by the plan's tables");
+    if (p->d.n_poles > 0) return fail(p, FDTD_EINVAL, "reverse steps of dispersive materials are not supported");
     if (n_steps == 0) return FDTD_OK;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     k_set_step<<<1, 1, 0, st>>>(p->d_t, t_end - 1);
@@ -1266,6 +1293,7 @@ int64_t fdtd_footprint_bytes(const FdtdDesc* d) {
     const int parts = d->bloch_axes ? 2 : 1;
     long long bytes = 4ll * N * (3 * parts + 3 * parts + d->n_eps + d->n_mu + d->n_sigma_E + d->n_sigma_H);
     if (d->n_eps == 9 || d->n_mu == 9 || d->n_sigma_E == 9 || d->n_sigma_H == 9) bytes += 24ll * parts * N;  // K and T
+    if (d->n_poles > 0) bytes += 4ll * N * d->n_poles * (6 + 3 * d->n_disp);  // P pair and c1..c3
     const int n3[3] = {d->nx, d->ny, d->nz};
     long long iface = 0, psi = 0;
     for (int s = 0; s < d->n_slabs; ++s) {
@@ -1306,6 +1334,7 @@ extern "C" int fdtd_profile_forward(FdtdPlan* p, const FdtdBuffers* b, int32_t t
     if (p && p->parts != 1) return fail(p, FDTD_EINVAL, "per-launch profiling of complex (Bloch) fields is not supported");
     if (p && (p->full_e || p->full_h))
         return fail(p, FDTD_EINVAL, "per-launch profiling of full 3x3 tensor materials is not supported");
+    if (p && p->d.n_poles > 0) return fail(p, FDTD_EINVAL, "per-launch profiling of dispersive materials is not supported");
     if (!p || !out_ms) return FDTD_EINVAL;
     if (int rc = check_bufs(p, b)) return rc;
     if (n_steps <= 0 || t0 < 0 || (long long)t0 + n_steps > (long long)p->d.n_steps_total + 1)

@@ -138,7 +138,16 @@ def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> list[
             if full:
                 weight = float(oriented[a])
             else:
-                local = float(m) if not isinstance(m, torch.Tensor) else float(m[min(a, m.shape[0] - 1), i, j, k])
+                if not isinstance(m, torch.Tensor):
+                    local = float(m)
+                else:
+                    loc = m[:, i, j, k].detach().double().cpu().numpy()
+                    if not magnetic and arrays.dispersive_c1 is not None:
+                        # the medium at the carrier in dispersive scenes (dipole.py:168-180)
+                        loc = _carrier_inv_eps(loc.reshape(-1, 1, 1, 1), arrays,
+                                               (slice(i, i + 1), slice(j, j + 1), slice(k, k + 1)),
+                                               src, config).reshape(-1)
+                    local = float(loc[min(a, loc.shape[0] - 1)])
                 weight = local * (1.0 if not src.is_tilted else orient[a])
             da = N.SourceDesc.from_buffer_copy(d)
             da.kind = N.SRC_DIPOLE
@@ -155,8 +164,42 @@ def build_source(src, arrays: ArrayContainer, config: SimulationConfig) -> list[
         incE, incH, offE, offH = plane_source_profiles(src, arrays, config)
         keep += [incE, incH, offE, offH]
         d.inc_E, d.inc_H, d.off_E, d.off_H = (x.ctypes.data for x in (incE, incH, offE, offH))
+        if arrays.dispersive_c1 is not None:
+            # dispersive scenes inject the E side with the broadband impedance-corrected profile,
+            # read at the fractional time by linear interpolation (tfsf.py:21-141, 256-261)
+            tab = np.ascontiguousarray(_plane_e_table(src, arrays, config), dtype=np.float32)
+            keep.append(tab)
+            d.e_table, d.n_e_table = tab.ctypes.data, int(tab.shape[0])
         return [SourceTables(d, keep)]
     raise NotImplementedError(f"source type {type(src).__name__} is not supported")
+
+
+def _carrier_inv_eps(inv_slice: np.ndarray, arrays: ArrayContainer, sl, src, config: SimulationConfig) -> np.ndarray:
+    """inv_eps of a slice as a source sees it in a dispersive scene: 1 / (eps_inf + Re chi) at
+    the source's carrier (effective_inv_permittivity, fdtdx/dispersion.py:1254-1307)."""
+    from fdtdx_gb300.dispersion import effective_inv_permittivity
+
+    cs = [c[(slice(None), slice(None), *sl)].detach().double().cpu().numpy()
+          for c in (arrays.dispersive_c1, arrays.dispersive_c2, arrays.dispersive_c3)]
+    omega = 2 * math.pi * src.wave_character.get_frequency()
+    return effective_inv_permittivity(inv_slice, cs[0], cs[1], cs[2], omega, config.time_step_duration)
+
+
+def _plane_e_table(src, arrays: ArrayContainer, config: SimulationConfig) -> np.ndarray:
+    """The E side's profile of a plane source in a dispersive scene at steps 0 .. T - 1: the raw
+    profile filtered by sqrt(eps(omega) / eps(omega_c)) averaged over the source's cells
+    (_build_dispersive_H_filter, fdtdx/objects/sources/tfsf.py:21-141)."""
+    from fdtdx_gb300.dispersion import dispersive_h_filter
+
+    T, dt = config.time_steps_total, config.time_step_duration
+    raw = np.asarray(src.temporal_profile.get_amplitude(np.arange(T, dtype=np.float64) * dt,
+                                                         src.wave_character.get_period(),
+                                                         src.wave_character.phase_shift), dtype=np.float64)
+    sl = (slice(None), slice(None), *src.grid_slice)
+    cs = [c[sl].detach().double().cpu().numpy() for c in (arrays.dispersive_c1, arrays.dispersive_c2,
+                                                          arrays.dispersive_c3)]
+    inv_inf = arrays.inv_permittivities[(slice(None), *src.grid_slice)].detach().double().cpu().numpy()
+    return dispersive_h_filter(raw, cs[0], cs[1], cs[2], inv_inf, 2 * math.pi * src.wave_character.get_frequency(), dt)
 
 
 def _tensor3(m, face_shape) -> np.ndarray:
@@ -228,6 +271,8 @@ def plane_source_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayContai
     Hf = amp[None] * h_pol[:, None, None, None]
     sl = (slice(None), *src.grid_slice)
     ie = arrays.inv_permittivities[sl].detach().double().cpu().numpy()
+    if arrays.dispersive_c1 is not None:  # impedance, energy and offsets at the carrier (linear_polarization.py:186-211)
+        ie = _carrier_inv_eps(ie, arrays, src.grid_slice, src, config)
     mu = arrays.inv_permeabilities
     im = mu[sl].detach().double().cpu().numpy() if isinstance(mu, torch.Tensor) else float(mu)
     E, Hf = _medium_scaling(src, ie, im, E, Hf, e_pol, h_pol)
@@ -298,6 +343,8 @@ def _tilted_plane_profiles(src: LinearlyPolarizedPlaneSource, arrays: ArrayConta
     Hf = amp[None] * h_pol[:, None, None, None]
     sl = (slice(None), *src.grid_slice)
     ie = arrays.inv_permittivities[sl].detach().double().cpu().numpy()
+    if arrays.dispersive_c1 is not None:  # impedance, energy and offsets at the carrier (linear_polarization.py:186-211)
+        ie = _carrier_inv_eps(ie, arrays, src.grid_slice, src, config)
     mu = arrays.inv_permeabilities
     im = mu[sl].detach().double().cpu().numpy() if isinstance(mu, torch.Tensor) else float(mu)
     E, Hf = _medium_scaling(src, ie, im, E, Hf, e_pol, h_pol)
@@ -437,8 +484,12 @@ class Scene:
         d.inv_mu_scalar = 1.0 if isinstance(mu, torch.Tensor) else float(mu)
         if d.n_eps not in (1, 3, 9) or d.n_mu not in (0, 1, 3, 9):
             raise ValueError("material arrays have 1, 3 or 9 components")
-        if any(getattr(o.material, "is_dispersive", False) for o in objects.static_material_objects):
-            raise NotImplementedError("dispersive (ADE) materials are not supported by the GB300 kernels")
+        c1 = arrays.dispersive_c1
+        if c1 is None and any(getattr(o.material, "is_dispersive", False) for o in objects.static_material_objects):
+            raise ValueError("dispersive materials need the ADE coefficient arrays init_arrays allocates")
+        d.n_poles = c1.shape[0] if c1 is not None else 0
+        d.n_disp = c1.shape[1] if c1 is not None else 0
+        self.dispersive = d.n_poles > 0
         d.n_sigma_E = arrays.electric_conductivity.shape[0] if arrays.electric_conductivity is not None else 0
         d.n_sigma_H = arrays.magnetic_conductivity.shape[0] if arrays.magnetic_conductivity is not None else 0
         # a 9-component material or conductivity runs that side's tensor half-steps
@@ -464,6 +515,9 @@ class Scene:
             d.bloch_cos[ax] = phases["+"].real
             d.bloch_sin[ax] = phases["+"].imag
         self.complex_fields = d.bloch_axes != 0
+        if self.dispersive and (self.complex_fields or 9 in (d.n_eps, d.n_sigma_E)):
+            raise NotImplementedError("dispersive materials with complex (Bloch) fields or a full-tensor permittivity "
+                                      "are not supported by the GB300 kernels")
         self._planar = None
         self._lam_ws = None
         self.pmls: list[PerfectlyMatchedLayer] = objects.pml_objects
@@ -615,6 +669,14 @@ class Scene:
             b.det_state[q] = N.ptr(next(iter(st.values())))
         if arrays.recording_state is not None:
             b.recording = N.ptr(arrays.recording_state.data["interfaces"])
+        if self.dispersive:
+            for t in (f.dispersive_P_curr, f.dispersive_P_prev, arrays.dispersive_c1, arrays.dispersive_c2,
+                      arrays.dispersive_c3):
+                if t is None or not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
+                    raise ValueError("dispersive polarisation and coefficients must be contiguous float32 CUDA tensors")
+            b.disp_P_curr, b.disp_P_prev = N.ptr(f.dispersive_P_curr), N.ptr(f.dispersive_P_prev)
+            b.disp_c1, b.disp_c2, b.disp_c3 = (N.ptr(x) for x in (arrays.dispersive_c1, arrays.dispersive_c2,
+                                                                   arrays.dispersive_c3))
         return b
 
     def _complex_buffers(self, arrays: ArrayContainer) -> N.Buffers:

@@ -42,6 +42,7 @@ def get_scene(objects: ObjectContainer, arrays: ArrayContainer, config: Simulati
         tuple(mu.shape) if isinstance(mu, torch.Tensor) else float(mu),
         None if arrays.electric_conductivity is None else tuple(arrays.electric_conductivity.shape),
         None if arrays.magnetic_conductivity is None else tuple(arrays.magnetic_conductivity.shape),
+        None if arrays.dispersive_c1 is None else tuple(arrays.dispersive_c1.shape),
         record_interfaces,
     )
     fp = _source_fingerprint(objects, arrays)

@@ -84,6 +84,43 @@ def _inverse_values(t9, n: int) -> list[float]:
     return [1.0 / v for v in _comp_values(t9, n)]
 
 
+def dispersive_coefficients(objects: ObjectContainer, config: SimulationConfig):
+    """Per-cell ADE recurrence coefficients (c1, c2, c3), each (poles, 1 | 3, nx, ny, nz) float32,
+    or None without a dispersive material (fdtdx/fdtd/initialization.py:686-700, 795-830,
+    955-1000): every painted material, the volume first, then the material objects in placement
+    order, writes its pole stack over its slice, zero-padded to the scene's largest pole count
+    (all zeros for a material without poles); one component when every pole is isotropic, else
+    three.  Coefficients of fdtdx/dispersion.py:789-857."""
+    from fdtdx_gb300.dispersion import compute_pole_coefficients_per_axis
+
+    painted = [objects.volume] + sorted(objects.static_material_objects, key=lambda o: o.placement_order)
+    models = [o.material.dispersion for o in painted
+              if o.material is not None and o.material.dispersion is not None and o.material.dispersion.num_poles > 0]
+    if not models:
+        return None
+    n_poles = max(m.num_poles for m in models)
+    nc = 1 if all(m.is_isotropic for m in models) else 3
+    shape = objects.volume.grid_shape
+    dt = config.time_step_duration
+    out = [torch.zeros((n_poles, nc, *shape), dtype=torch.float32) for _ in range(3)]
+    for o in painted:
+        if o.material is None:
+            continue
+        block = [np.zeros((n_poles, nc)) for _ in range(3)]
+        disp = o.material.dispersion
+        if disp is not None and disp.num_poles > 0:
+            for pole in disp.poles:
+                if getattr(pole, "orientation", None) is not None:
+                    raise NotImplementedError("oriented dispersive poles are not supported")
+            cs = compute_pole_coefficients_per_axis(disp.poles, dt)
+            for q in range(3):
+                block[q][: disp.num_poles] = cs[q][:, :nc]
+        sl = (slice(None), slice(None), *o.grid_slice)
+        for q in range(3):
+            out[q][sl] = torch.tensor(block[q], dtype=torch.float32)[:, :, None, None, None]
+    return tuple(out)
+
+
 def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None) -> ArrayContainer:
     """Allocate and fill the ArrayContainer of a placed scene."""
     device = torch.device(device) if device is not None else _default_device()
@@ -153,14 +190,22 @@ def init_arrays(objects: ObjectContainer, config: SimulationConfig, device=None)
         data = torch.zeros((gc.recorder.slots(config.time_steps_total), per_step), dtype=rdt, device=device)
         rec = RecordingState(data={"interfaces": data})
 
+    disp = dispersive_coefficients(objects, config)
+    P_curr = P_prev = None
+    if disp is not None:
+        P_curr = torch.zeros((disp[0].shape[0], *N3), dtype=fdt, device=device)
+        P_prev = torch.zeros_like(P_curr)
     return ArrayContainer(
-        fields=FieldState(E=E, H=H, psi_E=psi_E, psi_H=psi_H),
+        fields=FieldState(E=E, H=H, psi_E=psi_E, psi_H=psi_H, dispersive_P_curr=P_curr, dispersive_P_prev=P_prev),
         inv_permittivities=inv_eps.to(device),
         inv_permeabilities=inv_mu.to(device) if inv_mu is not None else 1.0,
         detector_states=det_states,
         recording_state=rec,
         electric_conductivity=sig_e.to(device) if sig_e is not None else None,
         magnetic_conductivity=sig_h.to(device) if sig_h is not None else None,
+        dispersive_c1=None if disp is None else disp[0].to(device),
+        dispersive_c2=None if disp is None else disp[1].to(device),
+        dispersive_c3=None if disp is None else disp[2].to(device),
     )
 
 

@@ -99,6 +99,12 @@ typedef struct {
     const float* phase_H;  /* same at teff + 0.5, H-side time */
     const float* teff;     /* on/off-adjusted time step (fdtdx/objects/sources/source.py:41-49) */
     const uint8_t* on;     /* 1 when the source is on */
+    /* plane in a dispersive scene: host table of the E side's temporal profile (the H incident
+     * field's profile) at every integer step 0 .. n_e_table - 1, read by linear interpolation at
+     * the fractional time and 0 outside (fdtdx/objects/sources/tfsf.py:21-141, 256-261); NULL:
+     * the analytic profile */
+    const float* e_table;
+    int32_t n_e_table;
 } FdtdSourceDesc;
 
 /* One detector.  Tables are host arrays of length n_table (entry t + 1). */
@@ -122,10 +128,10 @@ typedef struct {
     int32_t nx, ny, nz;
     int32_t n_steps_total;  /* T; tables hold T + 2 entries */
     float courant;          /* courant_factor / sqrt(3) */
-    int32_t n_eps;          /* 1 or 3 */
-    int32_t n_mu;           /* 0 (scalar inv_mu), 1 or 3 */
+    int32_t n_eps;          /* 1, 3 or 9 (a full tensor, row-major) */
+    int32_t n_mu;           /* 0 (scalar inv_mu), 1, 3 or 9 */
     float inv_mu_scalar;
-    int32_t n_sigma_E;      /* 0 (no conductivity), 1 or 3 */
+    int32_t n_sigma_E;      /* 0 (no conductivity), 1, 3 or 9 */
     int32_t n_sigma_H;
     int32_t periodic[3];
     int32_t pec_faces;      /* bit (2*axis + side), side 1 = max face */
@@ -152,10 +158,17 @@ typedef struct {
      * bloch_sin[a] on its '+' ghost layer (its conjugate on the '-' one).  The fields are then
      * complex: E, H, every psi array, the H twin and the interface recording hold their real
      * parts followed by their imaginary parts (planar, a leading dimension of 2); detector states
-     * keep their layouts (phasors complex, the rest real).  Forward and reverse steps only. */
+     * keep their layouts (phasors complex, the rest real).  The cotangents of fdtd_adjoint are
+     * planar the same way (dL/dRe, then dL/dIm). */
     int32_t bloch_axes;
     float bloch_cos[3];
     float bloch_sin[3];
+    /* dispersive (ADE) materials (fdtdx/fdtd/update.py:316-350): n_poles > 0 poles per cell
+     * with recurrence coefficients of n_disp (1 or 3) components; the buffers then carry the
+     * polarisation pair and the coefficient arrays.  Forward steps only (the reference's
+     * reversible path refuses dispersion as well). */
+    int32_t n_poles;
+    int32_t n_disp;
 } FdtdDesc;
 
 typedef struct {
@@ -169,6 +182,11 @@ typedef struct {
     float* psi_H[FDTD_MAX_SLABS][2];
     void* det_state[FDTD_MAX_DETECTORS];
     void* recording;            /* (T or rec_slots, fdtd_interface_floats(plan)) in recording_dtype, or NULL */
+    float* disp_P_curr;         /* (n_poles, 3, nx, ny, nz) polarisation P^n (n_poles > 0) */
+    float* disp_P_prev;         /* (n_poles, 3, nx, ny, nz) P^(n-1) */
+    const float* disp_c1;       /* (n_poles, n_disp, nx, ny, nz) recurrence coefficients */
+    const float* disp_c2;
+    const float* disp_c3;
 } FdtdBuffers;
 
 /* Cotangent (adjoint) buffers of the reversible gradient. */

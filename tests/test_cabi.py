@@ -49,8 +49,10 @@ int main(void) {
   O(FdtdSourceDesc, inc_E) O(FdtdSourceDesc, profile) O(FdtdSourceDesc, phase_E) O(FdtdSourceDesc, on)
   O(FdtdDetectorDesc, cell_weight) O(FdtdDetectorDesc, slot) O(FdtdDetectorDesc, weights)
   O(FdtdDesc, slabs) O(FdtdDesc, n_sources) O(FdtdDesc, sources) O(FdtdDesc, detectors) O(FdtdDesc, recording_dtype)
-  O(FdtdDesc, bloch_axes) O(FdtdDesc, bloch_sin)
-  O(FdtdBuffers, psi_E) O(FdtdBuffers, det_state) O(FdtdBuffers, recording)
+  O(FdtdDesc, bloch_axes) O(FdtdDesc, bloch_sin) O(FdtdDesc, n_poles) O(FdtdDesc, n_disp)
+  O(FdtdSourceDesc, e_table) O(FdtdSourceDesc, n_e_table)
+  O(FdtdBuffers, psi_E) O(FdtdBuffers, det_state) O(FdtdBuffers, recording) O(FdtdBuffers, disp_P_curr)
+  O(FdtdBuffers, disp_c3)
   O(FdtdAdjointBuffers, lam_det) O(FdtdAdjointBuffers, grad_inv_eps) O(FdtdAdjointBuffers, grad_inv_mu)
   return 0;
 }

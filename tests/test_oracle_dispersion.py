@@ -1,7 +1,7 @@
 """Dispersive (ADE) materials on the oracle (CPU): Lorentz and Drude poles.
 
-The GB300 kernels do not run dispersive materials, so the library refuses them; the oracle
-states the reference's ADE update (fdtd/update.py:316-350), its per-cell coefficients
+The GB300 kernels run the ADE update in forward steps (tests/test_gpu_dispersion.py); the
+oracle states the reference's ADE update (fdtd/update.py:316-350), its per-cell coefficients
 (dispersion.py:789-857, fdtd/initialization.py:686-1000) and the source corrections at the
 carrier frequency (dipole.py:150-193, linear_polarization.py:186-211, tfsf.py:21-141,
 256-261), so that a kernel for them has its checker ready.  Pins:
@@ -25,10 +25,13 @@ carrier frequency (dipole.py:150-193, linear_polarization.py:186-211, tfsf.py:21
   medium that reflects x and passes y (test_anisotropic_dispersion.py:247-280);
 * the broadband H-side filter leaks less of a Gaussian pulse's energy backwards than the
   carrier-only impedance (ratio below 0.85, test_dispersive_source.py:192-225);
-* the library refuses a dispersive scene before any device work, and the oracle has no
-  reversed step for one (fdtd/initialization.py:674-685).
+* the library's own dispersive setup (painted coefficients, carrier-frequency source
+  coefficients, the filtered E-side table of a plane source) equals the oracle's; the
+  reversible gradient refuses a dispersive scene, and the oracle has no reversed step for one
+  (fdtd/initialization.py:674-685).
 """
 
+import ctypes
 import math
 
 import numpy as np
@@ -41,6 +44,7 @@ from oracle import fdtd_oracle as O
 
 C0 = 299792458.0
 WL = 1e-6
+ctypes_float = ctypes.c_float
 OMEGA = 2 * math.pi * C0 / WL
 
 
@@ -170,12 +174,48 @@ def test_embedded_source_matches_lorentz_impedance():
     assert r["fwd"] > 0 and abs(r["bwd"]) / r["fwd"] < 0.02
 
 
-def test_library_refuses_dispersion_and_oracle_has_no_reverse():
-    mat = fx.Material(permittivity=1.0, dispersion=_lorentz())
-    objects, arrays, cfg, sc = _scene([fx.UniformMaterialObject(name="m", grid_slice_tuple=((0, 3), (0, 3), (5, 30)),
-                                                                material=mat)], dtype=torch.float32)
+def test_library_dispersive_tables_match_oracle_and_reverse_is_refused():
+    """The library's own restatement of the dispersive setup equals the oracle's: the painted
+    ADE coefficients (a Lorentz slab painted over by glass), the carrier-frequency inverse
+    permittivity of an electric dipole inside the slab, the plane source's impedance-divided
+    H profile and its broadband-filtered E-side table.  The reversible gradient refuses the
+    scene before any device work (fdtd.py:98-104), and the oracle has no reversed step."""
+    from fdtdx_gb300.engine import Scene
+
+    mat = fx.Material(permittivity=1.5, dispersion=_lorentz())
+    pulse = fx.GaussianPulseProfile(spectral_width=fx.WaveCharacter(frequency=0.2 * C0 / WL),
+                                    center_wave=fx.WaveCharacter(wavelength=WL))
+    mats = [fx.UniformMaterialObject(name="m", grid_slice_tuple=((0, 3), (0, 3), (5, 30)), material=mat),
+            fx.UniformMaterialObject(name="glass", grid_slice_tuple=((0, 3), (0, 3), (24, 27)),
+                                     material=fx.Material(permittivity=2.25), placement_order=1)]
+    src = fx.UniformPlaneSource(name="pl", grid_slice_tuple=((0, 3), (0, 3), (12, 13)), direction="+",
+                                fixed_E_polarization_vector=(1, 0, 0), wave_character=fx.WaveCharacter(wavelength=WL),
+                                temporal_profile=pulse)
+    dip = fx.PointDipoleSource(name="d", grid_slice_tuple=((1, 2), (1, 2), (18, 19)), polarization=0,
+                               wave_character=fx.WaveCharacter(wavelength=WL))
+    # the float32 oracle: both store the coefficients in float32, as the reference does
+    objects, arrays, cfg, sc = _scene(mats + [dip], src=src, steps=300, dtype=torch.float32)
+    assert arrays.fields.dispersive_P_curr.shape == (1, 3, 3, 3, 40)
+    for c, o in zip((arrays.dispersive_c1, arrays.dispersive_c2, arrays.dispersive_c3), sc.disp):
+        assert torch.equal(c, o)
+    scene = Scene(objects, arrays, cfg)
+    assert scene.dispersive and scene.desc.n_poles == 1 and scene.desc.n_disp == 1
+    recs = [scene.desc.sources[i] for i in range(scene.desc.n_sources)]
+    plane = next(r for r in recs if r.kind == 1)
+    dipole = next(r for r in recs if r.kind == 0)
+    osrc = {s.obj.name: s for s in sc.sources}
+    T = cfg.time_steps_total
+    table = np.ctypeslib.as_array((ctypes_float * plane.n_e_table).from_address(plane.e_table))
+    want = osrc["pl"].h_filter
+    assert plane.n_e_table == T and np.max(np.abs(table - want)) <= 1e-6 * np.max(np.abs(want))
+    inc_h = np.ctypeslib.as_array((ctypes_float * (3 * 9)).from_address(plane.inc_H)).reshape(3, 9)
+    assert np.allclose(inc_h, osrc["pl"].H_inc.reshape(3, -1).numpy(), rtol=1e-6, atol=1e-9)
+    local = float(osrc["d"].inv_local[0].reshape(-1)[0])
+    assert math.isclose(dipole.coef, cfg.courant_number * local * dip.amplitude * dip.static_amplitude_factor,
+                        rel_tol=1e-6)
+    ie = arrays.inv_permittivities.clone().requires_grad_(True)
     with pytest.raises(NotImplementedError, match="dispersive"):
-        fx.run_fdtd(arrays, objects, cfg)
+        fx.reversible_fdtd(arrays.aset("inv_permittivities", ie), objects, cfg)
     st = O.run(sc, 2)
     with pytest.raises(NotImplementedError):
         O.backward(sc, st)
