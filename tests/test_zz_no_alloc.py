@@ -94,7 +94,9 @@ def _periodic_scene(steps):
                                      wave_character=fx.WaveCharacter(wavelength=1.0e-6)))
     objs += [
         fx.PoyntingFluxDetector(name="flux_lo", grid_slice_tuple=((0, 1), (0, 18), (0, 16)), direction="-"),
-        fx.PoyntingFluxDetector(name="flux_hi", grid_slice_tuple=((19, 20), (0, 18), (0, 16)), direction="+"),
+        # all three components: the x flux through the last x plane is zero here, on the oracle too
+        fx.PoyntingFluxDetector(name="flux_hi", grid_slice_tuple=((19, 20), (0, 18), (0, 16)), direction="+",
+                                keep_all_components=True),
         fx.EnergyDetector(name="energy_all", grid_slice_tuple=((0, 20), (0, 18), (0, 16)), reduce_volume=True),
         fx.FieldDetector(name="e_only", grid_slice_tuple=((0, 20), (0, 18), (15, 16)), components=("Ex", "Ez"),
                          reduce_volume=True),
