@@ -208,10 +208,13 @@ class Scheduler:
 class Server:
     """The GPU serving loop over a list of timed jobs (``Job.arrival`` in seconds)."""
 
-    def __init__(self, budget_bytes: int = 160 * 10**9, max_slots: int = 64, target_chunk_s: float = 0.05,
+    def __init__(self, budget_bytes: int = 160 * 10**9, max_slots: int = 8, target_chunk_s: float = 0.05,
                  autotune: bool = True, adjoint_lanes: int = 4, keep_results: bool = True):
         """``keep_results=False`` returns each finished job's detector states on the host (in
-        ``Job.detectors``) and frees its device state, as a service answering many requests does."""
+        ``Job.detectors``) and frees its device state, as a service answering many requests does.
+        ``max_slots`` bounds the jobs in flight: few enough that a saturated stream is served close
+        to first-come order (its tail stays short), enough that small grids still fill the device
+        together."""
         self.sched = Scheduler(budget_bytes, max_slots)
         self.keep_results = keep_results
         self.adjoint_lanes = max(1, int(adjoint_lanes))

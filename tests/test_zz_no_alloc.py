@@ -136,7 +136,7 @@ def test_noalloc_periodic_faces_and_magnetic_tensor():
             assert rc == N.OK, det.name
             torch.cuda.synchronize()
             outs.append(out.cpu())
-        assert torch.linalg.vector_norm(exp).item() > 0, det.name
+        assert exp.abs().max().item() > 0, det.name  # (face fluxes are ~1e-24: a float32 norm underflows)
         for out in outs:
             assert torch.allclose(out, exp, rtol=1e-6, atol=1e-6 * exp.abs().max().item()), (det.name, out, exp)
         assert torch.equal(outs[0], outs[1]), det.name
