@@ -209,14 +209,8 @@ def reversible_fdtd(
            "inv_eps": work.inv_permittivities, "inv_mu": work.inv_permeabilities}
     wants = ie_in.requires_grad or (mu_t is not None and mu_t.requires_grad)
     if wants and torch.is_grad_enabled() and scene.full_tensor:
-        from fdtdx_gb300.objects import EnergyDetector
-
-        if mu_t is not None and mu_t.requires_grad:
-            raise NotImplementedError("the inv_permeabilities gradient of full 3x3 tensor materials is not supported "
-                                      "by the GB300 kernels (the inv_permittivities gradient is)")
-        if any(isinstance(d, EnergyDetector) for d in objects.forward_detectors):
-            raise NotImplementedError("the reversible gradient of full 3x3 tensor materials with an energy detector "
-                                      "is not supported by the GB300 kernels")
+        raise NotImplementedError("the reversible gradient of full 3x3 tensor materials is not supported by the GB300 "
+                                  "kernels (their forward and reverse steps are)")
     if wants and torch.is_grad_enabled() and scene.complex_fields and mu_t is not None and mu_t.requires_grad:
         raise NotImplementedError("the inv_permeabilities gradient of complex (Bloch) fields is not supported by the "
                                   "GB300 kernels (the inv_permittivities gradient is)")

@@ -22,7 +22,6 @@
 // cotangent of z is dL/dRe z + i dL/dIm z, so a real sample x entering z as x * w has
 // cotangent Re(conj(w) * lam_z).
 #pragma once
-#include "fdtd_aniso.cuh"
 #include "fdtd_kernels.cuh"
 
 namespace fdtd {
@@ -89,14 +88,6 @@ struct AdjArgs {
     // (the lam fields' offset is g.pother)
     int part, nparts;
     long long lpother[FDTD_MAX_SLABS];
-    // full 3x3 tensor sides (generic kernels only): the curl cotangent field of the E- or
-    // H-step, gathered by k_full_adjprep (used instead of the diagonal c m / d lam), and the
-    // transposed tensor terms of the previous field (lam E(t), the tensor part of lam H(t)),
-    // each this part's planar slice; nullptr on a diagonal side
-    const float* lcE;
-    const float* lcH;
-    const float* lprevE;
-    const float* lprevH;
 };
 
 // The slab mask of this block's box.
@@ -170,15 +161,10 @@ __device__ __forceinline__ void dcell(const AdjArgs& a, int i, int j, int k, boo
     const long long N = g.N;
     const long long c = cell_index(g, i, j, k);
     const float* L = HSIDE ? a.lH : a.lE;
-    const float* LC = HSIDE ? a.lcH : a.lcE;
     const int mask = HSIDE ? g.pmc : g.pec;
     float lc[3];
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-        if (LC) {  // a tensor side: the gathered curl cotangent (walls and materials applied)
-            lc[comp] = mix_at(LC, comp * N + c, g.pother, g.psign, cr, ci);
-            continue;
-        }
         float l1 = mix_at(L, comp * N + c, g.pother, g.psign, cr, ci);
         if (mask && face_zero(g, mask, comp, i, j, k)) l1 = 0.f;
         float m, den = 1.f;
@@ -369,7 +355,6 @@ __global__ void __launch_bounds__(256) k_adj_E(const __grid_constant__ AdjArgs a
                     const float qh = g.c * adj_mat(a.sigH, a.n_sigH, 0.f, N, comp, c + e) / g.eta0 * m / 2.f;
                     l1 *= (1.f - qh) / (1.f + qh);
                 }
-                if (a.lprevH) l1 = a.lprevH[comp * N + c + e];  // a tensor H side
                 float v = l1 + lht[comp];
                 if (in_hp) {
                     float* hp = a.hp.buf + comp * a.hp.M + q;
@@ -407,7 +392,6 @@ __global__ void __launch_bounds__(256) k_adj_E(const __grid_constant__ AdjArgs a
                         dm = (g.c * cu[comp] - hs * (e0 + e1)) / den;
                     }
                 }
-                if (a.lprevE) lo = a.lprevE[comp * N + c + e];  // a tensor E side (its gradient elsewhere)
                 outE[comp].v[e] = lo;
                 if (want_grad) {
                     if (a.n_eps == 3) a.grad_ie[comp * N + c + e] += l1 * dm;
@@ -1567,156 +1551,6 @@ __global__ void k_adj_det_clear(const DDet d, void* lam, const int* __restrict__
     const int slot = __ldg(d.slot + *tp + 1);
     if (slot < 0) return;
     for (int q = threadIdx.x; q < d.ncomp; q += blockDim.x) reinterpret_cast<float*>(lam)[(long long)slot * d.ncomp + q] = 0.f;
-}
-
-// ---------------------------------------------------------------------------------
-// Transposed tensor update of a full 3x3 side (the transpose of k_full_apply's forward form,
-// update.py:474-492 / 791-807).  Forward, row i at cell x:
-//   U3_i(x) = sum_j A_ij(x) F_j@i(x) + s sum_j B_ij(x) K_j@i(x),  then conductor faces zeroed,
-// F_j@i = F_j(x) for j = i, else the mean of F_j at x + {0, o_i, c_j, o_i + c_j} (E type:
-// o_i = +e_i, c_j = -e_j; H type: both negated), the halo wrapped with the forward rule.  Its
-// transpose at cell y, for the cotangent lam of U3 (faces zeroed):
-//   lprev_j(y) = A_jj(y) lam_j(y) + sum_{i != j} sum_delta A_ij(y - delta) lam_i(y - delta) / 4
-//   lcK_j(y)   = s (B_jj(y) lam_j(y) + sum_{i != j} sum_delta B_ij(y - delta) lam_i(y - delta) / 4)
-// (a gather across a Bloch face takes the opposite rotation, as every transposed gather does).
-// lcK is the cotangent of the curl, which the generic transposed kernels take through
-// AdjArgs::lcE / lcH.  With `grad` (E side) the cell also adds d/d inv_eps of its own rows:
-// with G_a[i][j] = lam_i F_j@i and G_b[i][j] = lam_i K_j@i (F the field before the update, K
-// the recomputed forward curl),
-//   dL/d inv = c Mi^T G_b - k Mi^T (2 G_a + c G_b inv^T) Mi^T sigma^T   (k = c eta0 / 2),
-// c G_b without conductivity; reduced to the array's components (9: all, 3: the diagonal,
-// 1: the trace).
-template <bool HSIDE>
-__global__ void __launch_bounds__(256) k_full_adjprep(const __grid_constant__ AdjArgs a, const float* __restrict__ lam,
-                                                      float* __restrict__ lcK, float* __restrict__ lprev,
-                                                      const float* __restrict__ Fo, const float* __restrict__ Kf,
-                                                      float* __restrict__ grad) {
-    const Geo& g = a.g;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.N) return;
-    const int k = (int)(c % g.nz);
-    const long long r = c / g.nz;
-    const int j = (int)(r % g.ny);
-    const int i = (int)(r / g.ny);
-    const long long N = g.N;
-    const float* mat = HSIDE ? a.im : a.ie;
-    const int n_mat = HSIDE ? a.n_mu : a.n_eps;
-    const float scalar = HSIDE ? a.im_scalar : 1.f;
-    const float* sig = HSIDE ? a.sigH : a.sigE;
-    const int n_sig = HSIDE ? a.n_sigH : a.n_sigE;
-    const int wall = HSIDE ? g.pmc : g.pec;
-    const float s = HSIDE ? -1.f : 1.f;
-    float inv[9], sg[9], Mi[9], A[9], B[9];
-    const bool has_sig = full_matrices<false, HSIDE>(g, mat, n_mat, scalar, sig, n_sig, c, inv, sg, Mi, A, B);
-    float ly[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) ly[q] = (wall && face_zero(g, wall, q, i, j, k)) ? 0.f : lam[q * N + c];
-    float lp[3], lk[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        lp[q] = A[q * 4] * ly[q];
-        lk[q] = B[q * 4] * ly[q];
-    }
-    const int so = HSIDE ? -1 : 1, sc = HSIDE ? 1 : -1;
-    for (int row = 0; row < 3; ++row) {
-        for (int col = 0; col < 3; ++col) {
-            if (col == row) continue;
-            // delta = 0: this cell's own row
-            lp[col] += A[row * 3 + col] * ly[row] / 4.f;
-            lk[col] += B[row * 3 + col] * ly[row] / 4.f;
-            for (int q = 1; q < 4; ++q) {
-                int di = 0, dj = 0, dk = 0;
-                if (q & 1) { di += row == 0 ? so : 0; dj += row == 1 ? so : 0; dk += row == 2 ? so : 0; }
-                if (q & 2) { di += col == 0 ? sc : 0; dj += col == 1 ? sc : 0; dk += col == 2 ? sc : 0; }
-                int xi = i - di, xj = j - dj, xk = k - dk;
-                float cr, ci;
-                if (!wrap_turn(g, xi, xj, xk, cr, ci)) continue;
-                if (wall && face_zero(g, wall, row, xi, xj, xk)) continue;
-                const long long cx = cell_index(g, xi, xj, xk);
-                float inv2[9], sg2[9], Mi2[9], A2[9], B2[9];
-                full_matrices<false, HSIDE>(g, mat, n_mat, scalar, sig, n_sig, cx, inv2, sg2, Mi2, A2, B2);
-                const float lx = mix_at(lam, row * N + cx, g.pother, g.psign, cr, ci);
-                lp[col] += A2[row * 3 + col] * lx / 4.f;
-                lk[col] += B2[row * 3 + col] * lx / 4.f;
-            }
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        lprev[q * N + c] = lp[q];
-        lcK[q * N + c] = s * lk[q];
-    }
-    if (HSIDE || !grad) return;
-    // d/d inv_eps of this cell's rows
-    float Ga[9], Gb[9];
-#pragma unroll
-    for (int row = 0; row < 3; ++row)
-#pragma unroll
-        for (int col = 0; col < 3; ++col) {
-            const float fa = col == row ? __ldg(Fo + row * N + c) : avg_onto<false>(g, Fo, col, row, i, j, k);
-            const float fb = col == row ? __ldg(Kf + row * N + c) : avg_onto<false>(g, Kf, col, row, i, j, k);
-            Ga[row * 3 + col] = ly[row] * fa;
-            Gb[row * 3 + col] = ly[row] * fb;
-        }
-    float D[9];
-#pragma unroll
-    for (int row = 0; row < 3; ++row)
-#pragma unroll
-        for (int col = 0; col < 3; ++col) {  // c Mi^T G_b
-            float v = 0.f;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) v += Mi[q * 3 + row] * Gb[q * 3 + col];
-            D[row * 3 + col] = g.c * v;
-        }
-    if (has_sig) {
-        const float kq = g.c * g.eta0 / 2.f;
-        float X[9], Y[9], Z[9];
-#pragma unroll
-        for (int row = 0; row < 3; ++row)
-#pragma unroll
-            for (int col = 0; col < 3; ++col) {  // X = 2 G_a + c G_b inv^T
-                float v = 0.f;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) v += Gb[row * 3 + q] * inv[col * 3 + q];
-                X[row * 3 + col] = 2.f * Ga[row * 3 + col] + g.c * v;
-            }
-#pragma unroll
-        for (int row = 0; row < 3; ++row)
-#pragma unroll
-            for (int col = 0; col < 3; ++col) {  // Y = Mi^T X
-                float v = 0.f;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) v += Mi[q * 3 + row] * X[q * 3 + col];
-                Y[row * 3 + col] = v;
-            }
-#pragma unroll
-        for (int row = 0; row < 3; ++row)
-#pragma unroll
-            for (int col = 0; col < 3; ++col) {  // Z = Y Mi^T
-                float v = 0.f;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) v += Y[row * 3 + q] * Mi[col * 3 + q];
-                Z[row * 3 + col] = v;
-            }
-#pragma unroll
-        for (int row = 0; row < 3; ++row)
-#pragma unroll
-            for (int col = 0; col < 3; ++col) {  // - k Z sigma^T
-                float v = 0.f;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) v += Z[row * 3 + q] * sg[col * 3 + q];
-                D[row * 3 + col] -= kq * v;
-            }
-    }
-    if (a.n_eps == 9) {
-#pragma unroll
-        for (int q = 0; q < 9; ++q) grad[q * N + c] += D[q];
-    } else if (a.n_eps == 3) {
-#pragma unroll
-        for (int q = 0; q < 3; ++q) grad[q * N + c] += D[q * 4];
-    } else {
-        grad[c] += D[0] + D[4] + D[8];
-    }
 }
 
 }  // namespace fdtd

@@ -68,10 +68,6 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
         b.M = (long long)b.n[0] * b.n[1] * b.n[2];
         o_snap[q] = ar.take(sizeof(float) * 6 * parts * (size_t)b.M);
     }
-    // full 3x3 tensor sides: the transposed tensor terms (curl cotangent, previous field's)
-    size_t o_full[4] = {0, 0, 0, 0};
-    for (int q = 0; q < 4; ++q)
-        if (q < 2 ? p->full_e : p->full_h) o_full[q] = ar.take(sizeof(float) * 3 * parts * (size_t)N);
     char* mem = nullptr;
     cudaError_t e = dev_alloc(reinterpret_cast<void**>(&mem), ar.off);
     if (e != cudaSuccess) return fail(p, FDTD_ENOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
@@ -88,8 +84,6 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
         for (int q = 0; q < 4; ++q) p->lpsi_twin[s][q] = reinterpret_cast<float*>(mem + o_psi[s][q]);
     p->hp = hp;
     if (any) p->hp.buf = reinterpret_cast<float*>(mem + o_hp);
-    for (int q = 0; q < 4; ++q)
-        if (q < 2 ? p->full_e : p->full_h) p->full_adj[q] = reinterpret_cast<float*>(mem + o_full[q]);
     for (int q = 0; q < d.n_detectors; ++q) {
         p->snap[q] = snap[q];
         if (det_bilinear(p->det[q])) p->snap[q].buf = reinterpret_cast<float*>(mem + o_snap[q]);
@@ -148,16 +142,8 @@ AdjArgs make_adj(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffe
     a.lH = cur.H + fo;
     a.lE_out = nxt.E + fo;
     a.lH_out = nxt.H + fo;
-    a.grad_ie = p->full_e ? nullptr : adj->grad_inv_eps;  // a tensor E side's: k_full_adjprep
+    a.grad_ie = adj->grad_inv_eps;
     a.grad_im = adj->grad_inv_mu;
-    if (p->full_e && p->full_adj[0]) {
-        a.lcE = p->full_adj[0] + fo;
-        a.lprevE = p->full_adj[1] + fo;
-    }
-    if (p->full_h && p->full_adj[2]) {
-        a.lcH = p->full_adj[2] + fo;
-        a.lprevH = p->full_adj[3] + fo;
-    }
     a.hp = p->hp;
     if (a.hp.buf) {
         a.hp.buf += part ? 3 * a.hp.M : 0;
@@ -207,12 +193,8 @@ int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
             return fail(p, FDTD_EINVAL, "psi cotangent buffers required for every slab");
     if (adj->grad_inv_mu && p->d.n_mu == 0)
         return fail(p, FDTD_EINVAL, "grad_inv_mu needs an inv_mu array (n_mu 1 or 3), not a scalar inv_mu");
-    if ((p->full_e || p->full_h) && adj->grad_inv_mu)
-        return fail(p, FDTD_EINVAL, "the inv_mu cotangent of full 3x3 tensor materials is not supported (inv_eps is)");
     if (p->full_e || p->full_h)
-        for (int q = 0; q < p->d.n_detectors; ++q)
-            if (adj->lam_det[q] && p->det[q].kind == FDTD_DET_ENERGY)
-                return fail(p, FDTD_EINVAL, "energy-detector cotangents with full 3x3 tensor materials are not supported");
+        return fail(p, FDTD_EINVAL, "the reversible gradient of full 3x3 tensor materials is not supported");
     if (p->d.n_poles > 0) return fail(p, FDTD_EINVAL, "the reversible gradient of dispersive materials is not supported");
     return FDTD_OK;
 }
@@ -268,12 +250,6 @@ bool adj_fast_core(const FdtdPlan* p, const AdjArgs& a, const Box& core, bool hs
 // the shell boxes.
 template <bool HSIDE>
 void launch_adj(const FdtdPlan* p, const AdjArgs& a, cudaStream_t st) {
-    if (p->full_e || p->full_h) {  // tensor sides: the generic kernels over the whole grid
-        const Box all{{0, 0, 0}, {p->g.nx, p->g.ny, p->g.nz}};
-        const int ch = kShellChunk;
-        launch_adj_boxes<HSIDE>(p, a, &all, &ch, 1, AdjKind::ShellGeneric, st);
-        return;
-    }
     const Split sp = split_boxes(p, 1);
     AdjKind shell = axis_table_ok(a) ? AdjKind::Shell : AdjKind::ShellGeneric;
     // fast shell: zero halo (no periodic axis), no conductivity, no PEC/PMC, scalar inv_mu (H)
@@ -310,7 +286,7 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
     }
     interfaces<true>(p, b, b->H, st);
     launch_sources(p, b, false, b->H, 1, st);
-    launch_side<true, true>(p, b, b->E, b->H, b->H, st);
+    for (int part = 0; part < np; ++part) launch_H<true>(p, make_upd(p, b, false, b->E, b->H, b->H, part), st);
     // here H holds H(t) and E still E3: the detector cotangents (which read H(t) for exact
     // interpolation) complete lam H3, and the inv_mu cotangent needs E3 and H(t)
     for (int part = 0; part < np; ++part) {
@@ -337,29 +313,9 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
             k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
     }
     launch_sources(p, b, true, b->E, 1, st);
-    launch_side<true, false>(p, b, b->H, b->E, b->E, st);
-    const unsigned nb = (unsigned)((p->g.N + 255) / 256);
-    if (p->full_h)  // the transposed tensor terms of the H-step, from lam H3 (both parts first)
-        for (int part = 0; part < np; ++part) {
-            const AdjArgs a = make_adj(p, b, adj, cur, nxt, part);
-            k_full_adjprep<true><<<nb, 256, 0, st>>>(a, a.lH, const_cast<float*>(a.lcH), const_cast<float*>(a.lprevH),
-                                                     nullptr, nullptr, nullptr);
-        }
+    for (int part = 0; part < np; ++part) launch_E<true>(p, make_upd(p, b, true, b->H, b->E, b->E, part), st);
     // the transposed H-steps of both parts (each reads lam H3 of both) before either E-step
     for (int part = 0; part < np; ++part) launch_adj<true>(p, make_adj(p, b, adj, cur, nxt, part), st);
-    if (p->full_e) {
-        // the forward curl at the reconstructed state (psi advanced, not stored) for d/d inv_eps,
-        // then the transposed tensor terms of the E-step from lam E3 (both parts first)
-        if (adj->grad_inv_eps)
-            for (int part = 0; part < np; ++part)
-                k_full_curl<false, false, false><<<nb, 256, 0, st>>>(make_upd(p, b, true, b->H, b->E, b->E, part),
-                                                                     p->full_k + part * fo, nullptr);
-        for (int part = 0; part < np; ++part) {
-            const AdjArgs a = make_adj(p, b, adj, cur, nxt, part);
-            k_full_adjprep<false><<<nb, 256, 0, st>>>(a, a.lE, const_cast<float*>(a.lcE), const_cast<float*>(a.lprevE),
-                                                      a.E, p->full_k + part * fo, adj->grad_inv_eps);
-        }
-    }
     for (int part = 0; part < np; ++part) launch_adj<false>(p, make_adj(p, b, adj, cur, nxt, part), st);
     k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
 }

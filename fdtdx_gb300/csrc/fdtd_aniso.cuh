@@ -15,10 +15,8 @@
 namespace fdtd {
 
 // Pass 1: K = the curl of the differentiated field at every cell, CPML terms included, and
-// T = the updated field's values (when T is given: an in-place update).  STORE = false (the
-// reversible gradient's recomputation of a forward curl) advances psi into the curl without
-// writing it back.
-template <bool REV, bool HSIDE, bool STORE = !REV>
+// T = the updated field's values (when T is given: an in-place update).
+template <bool REV, bool HSIDE>
 __global__ void __launch_bounds__(256) k_full_curl(const __grid_constant__ UpdArgs a, float* __restrict__ K,
                                                    float* __restrict__ T) {
     const Geo& g = a.g;
@@ -51,7 +49,7 @@ __global__ void __launch_bounds__(256) k_full_curl(const __grid_constant__ UpdAr
     if (a.n_slab) {
         PsiPre pr;
         psi_fetch(a, i, j, k, pr);
-        cpml_apply<REV, HSIDE, STORE>(a, i, j, k, d, cu, pr);
+        cpml_apply<REV, HSIDE>(a, i, j, k, d, cu, pr);
     }
 #pragma unroll
     for (int q = 0; q < 3; ++q) K[q * N + c] = cu[q];
@@ -59,45 +57,6 @@ __global__ void __launch_bounds__(256) k_full_curl(const __grid_constant__ UpdAr
 #pragma unroll
         for (int q = 0; q < 3; ++q) T[q * N + c] = __ldg(a.Uin + q * N + c);
     }
-}
-
-// The update matrices of one cell (misc.py:69-129): inv and sg the cell's inverse material
-// and conductivity tensors, Mi = M1^-1 (forward) or M2^-1 (reverse), M1,2 = I +- (c eta / 2)
-// inv sigma, A = 2 Mi - I, B = c Mi inv; without conductivity Mi = A = I and B = c inv.
-// Returns whether the cell has a conductivity.
-template <bool REV, bool HSIDE>
-__device__ __forceinline__ bool full_matrices(const Geo& g, const float* mat, int n_mat, float scalar, const float* sig,
-                                              int n_sig, long long c, float inv[9], float sg[9], float Mi[9], float A[9],
-                                              float B[9]) {
-    tensor_at(mat, n_mat, scalar, g.N, c, inv);
-    if (sig) {
-        float M[9];
-        tensor_at(sig, n_sig, 0.f, g.N, c, sg);
-        const float kq = HSIDE ? g.c / g.eta0 / 2.f : g.c * g.eta0 / 2.f;
-#pragma unroll
-        for (int row = 0; row < 3; ++row)
-#pragma unroll
-            for (int col = 0; col < 3; ++col) {
-                const float pc = inv[row * 3] * sg[col] + inv[row * 3 + 1] * sg[3 + col] + inv[row * 3 + 2] * sg[6 + col];
-                M[row * 3 + col] = (row == col ? 1.f : 0.f) + (REV ? -kq : kq) * pc;
-            }
-        inverse3(M, Mi);
-#pragma unroll
-        for (int row = 0; row < 3; ++row)
-#pragma unroll
-            for (int col = 0; col < 3; ++col) {
-                A[row * 3 + col] = 2.f * Mi[row * 3 + col] - (row == col ? 1.f : 0.f);
-                B[row * 3 + col] = g.c * (Mi[row * 3] * inv[col] + Mi[row * 3 + 1] * inv[3 + col] + Mi[row * 3 + 2] * inv[6 + col]);
-            }
-        return true;
-    }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        sg[q] = 0.f;
-        Mi[q] = A[q] = (q % 4 == 0) ? 1.f : 0.f;
-        B[q] = g.c * inv[q];
-    }
-    return false;
 }
 
 // Component `comp` of a field averaged onto the Yee location of component `loc`: the E-type
@@ -131,8 +90,34 @@ __global__ void __launch_bounds__(256) k_full_apply(const __grid_constant__ UpdA
     const int j = (int)(r % g.ny);
     const int i = (int)(r / g.ny);
     const long long N = g.N;
-    float inv[9], sg[9], Mi[9], A[9], B[9];
-    full_matrices<REV, HSIDE>(g, a.mat, a.n_mat, a.mat_scalar, a.sig, a.n_sig, c, inv, sg, Mi, A, B);
+    float inv[9], A[9], B[9];
+    tensor_at(a.mat, a.n_mat, a.mat_scalar, N, c, inv);
+    if (a.sig) {
+        float sg[9], M[9], Mi[9];
+        tensor_at(a.sig, a.n_sig, 0.f, N, c, sg);
+        const float kq = HSIDE ? g.c / g.eta0 / 2.f : g.c * g.eta0 / 2.f;
+#pragma unroll
+        for (int row = 0; row < 3; ++row)
+#pragma unroll
+            for (int col = 0; col < 3; ++col) {
+                const float pc = inv[row * 3] * sg[col] + inv[row * 3 + 1] * sg[3 + col] + inv[row * 3 + 2] * sg[6 + col];
+                M[row * 3 + col] = (row == col ? 1.f : 0.f) + (REV ? -kq : kq) * pc;
+            }
+        inverse3(M, Mi);
+#pragma unroll
+        for (int row = 0; row < 3; ++row)
+#pragma unroll
+            for (int col = 0; col < 3; ++col) {
+                A[row * 3 + col] = 2.f * Mi[row * 3 + col] - (row == col ? 1.f : 0.f);
+                B[row * 3 + col] = g.c * (Mi[row * 3] * inv[col] + Mi[row * 3 + 1] * inv[3 + col] + Mi[row * 3 + 2] * inv[6 + col]);
+            }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            A[q] = (q % 4 == 0) ? 1.f : 0.f;
+            B[q] = g.c * inv[q];
+        }
+    }
     const float s = (HSIDE != REV) ? -1.f : 1.f;
     const int wall = HSIDE ? g.pmc : g.pec;
 #pragma unroll

@@ -44,9 +44,8 @@ __device__ __forceinline__ void psi_fetch(const UpdArgs& a, int i, int j, int k,
     }
 }
 
-// cpml_correct with the psi values taken from a prefetch.  STORE (the forward default) writes
-// the advanced psi back; without it the advanced psi only enters the curl.
-template <bool REV, bool HSIDE, bool STORE = !REV>
+// cpml_correct with the psi values taken from a prefetch.
+template <bool REV, bool HSIDE>
 __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k, const float d[6], float cu[3],
                                            const PsiPre& pr, int active = 63) {
     const int idx3[3] = {i, j, k};
@@ -65,11 +64,9 @@ __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k
             const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
             p1 = cb * p1 + ca * d1;
             p2 = cb * p2 + ca * d2;
-            if (STORE) {
-                const long long p = psi_offset(sl, i, j, k);
-                a.psi1[s][p] = p1;
-                a.psi2[s][p] = p2;
-            }
+            const long long p = psi_offset(sl, i, j, k);
+            a.psi1[s][p] = p1;
+            a.psi2[s][p] = p2;
         }
         float c1 = p1, c2 = p2;
         if (!sl.kappa_one) {

@@ -39,9 +39,6 @@ struct FdtdPlan {
     bool full_e = false, full_h = false;
     float* full_k = nullptr;
     float* full_t = nullptr;
-    // and the reversible gradient's transposed tensor terms (adjoint scratch): the curl
-    // cotangents and the previous field's cotangents of the E side [0, 1] and the H side [2, 3]
-    float* full_adj[4] = {nullptr, nullptr, nullptr, nullptr};
     bool fused[FDTD_MAX_DETECTORS] = {};  // accumulated inside the H half-step
     int n_fused = 0;
     int chunk = 1;                        // x planes per update block

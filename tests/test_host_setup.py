@@ -92,17 +92,15 @@ def test_material_painting_in_placement_order():
 
 def test_reversible_fdtd_rejects_unsupported_material_inputs():
     """Gradients the reversible path does not take are refused before any device work: the
-    inv_permeabilities gradient next to a full 3x3 (9-component) permittivity, and a 0-d
-    permeability tensor that asks for a gradient (a permeability gradient needs a
-    (1 | 3, nx, ny, nz) array).  A full tensor itself is taken: the scene runs its tensor
-    half-steps, and its inv_permittivities gradient runs on the device."""
+    gradient of a full 3x3 (9-component) permittivity, and a 0-d permeability tensor that asks
+    for a gradient (a permeability gradient needs a (1 | 3, nx, ny, nz) array).  A full tensor
+    itself is taken: the scene runs its tensor half-steps."""
     from fdtdx_gb300.engine import Scene
 
     objects, arrays, _, cfg, _ = scenes.dipole_boxes(shape=(12, 12, 12), steps=4, n_boxes=1, pml=3, device="cpu")
     inv9 = torch.zeros((9, 12, 12, 12))
     inv9[0] = inv9[4] = inv9[8] = 1.0
-    full = arrays.aset("inv_permittivities", inv9).aset("inv_permeabilities",
-                                                        torch.ones((1, 12, 12, 12), requires_grad=True))
+    full = arrays.aset("inv_permittivities", inv9.requires_grad_(True))
     with pytest.raises(NotImplementedError, match="3x3"):
         fx.reversible_fdtd(full, objects, cfg)
     mu0 = arrays.aset("inv_permeabilities", torch.tensor(1.0, requires_grad=True))
