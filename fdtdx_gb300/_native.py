@@ -147,6 +147,8 @@ class AdjointBuffers(C.Structure):
         ("lam_det", C.c_void_p * MAX_DETECTORS),
         ("grad_inv_eps", C.c_void_p),
         ("grad_inv_mu", C.c_void_p),
+        ("lam_P_curr", C.c_void_p),
+        ("lam_P_prev", C.c_void_p),
     ]
 
 
@@ -168,6 +170,10 @@ SIGNATURES = {
     "fdtd_adjoint": (
         C.c_int,
         [C.c_void_p, C.POINTER(Buffers), C.POINTER(AdjointBuffers), C.c_int32, C.c_int32, C.c_void_p],
+    ),
+    "fdtd_adjoint_stored": (
+        C.c_int,
+        [C.c_void_p, C.POINTER(Buffers), C.c_int32, C.c_int32, C.POINTER(AdjointBuffers), C.c_void_p],
     ),
     "fdtd_launches_per_step": (C.c_int32, [C.c_void_p]),
     "fdtd_plan_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),

@@ -40,6 +40,8 @@ def _clone_fields(f: FieldState) -> FieldState:
         H=f.H.clone(),
         psi_E={k: (a.clone(), b.clone()) for k, (a, b) in f.psi_E.items()},
         psi_H={k: (a.clone(), b.clone()) for k, (a, b) in f.psi_H.items()},
+        dispersive_P_curr=None if f.dispersive_P_curr is None else f.dispersive_P_curr.clone(),
+        dispersive_P_prev=None if f.dispersive_P_prev is None else f.dispersive_P_prev.clone(),
     )
 
 
@@ -51,6 +53,9 @@ def _copy_fields(dst: FieldState, src: FieldState) -> None:
         dst.psi_E[k][1].copy_(src.psi_E[k][1])
         dst.psi_H[k][0].copy_(src.psi_H[k][0])
         dst.psi_H[k][1].copy_(src.psi_H[k][1])
+    if dst.dispersive_P_curr is not None:
+        dst.dispersive_P_curr.copy_(src.dispersive_P_curr)
+        dst.dispersive_P_prev.copy_(src.dispersive_P_prev)
 
 
 class _Layout:
@@ -230,3 +235,104 @@ def reversible_fdtd(
 
 class _NoCtx:
     """Stand-in context for a forward run that needs no backward."""
+
+
+class _CheckpointedRun(torch.autograd.Function):
+    """The exact gradient of GradientConfig(method="checkpointed") (the reference differentiates
+    its checkpointed while loop, fdtdx/fdtd/fdtd.py:421-496): the forward run stores the full
+    state (the dispersive polarisation included) at the start of each of ``num_checkpoints``
+    segments; the backward pass, from the last segment to the first, recomputes the segment's
+    states from its checkpoint and runs the transposed steps over them
+    (``fdtd_adjoint_stored``, the ADE step transposed too).  No reconstruction is involved, so
+    the gradient is exact everywhere, inside the CPML included.  Memory: the checkpoints plus
+    one segment of states."""
+
+    @staticmethod
+    def forward(ctx, ctl: dict, inv_eps: torch.Tensor, inv_mu):
+        scene, arrays, bounds = ctl["scene"], ctl["arrays"], ctl["bounds"]
+        checkpoints = []
+        for seg in range(len(bounds) - 1):
+            checkpoints.append(_clone_fields(arrays.fields))
+            scene.forward(arrays, bounds[seg], bounds[seg + 1] - bounds[seg], check_finite=seg == len(bounds) - 2)
+        from fdtdx_gb300.fdtd import finite_status
+
+        finite_status(scene)
+        ctl["checkpoints"] = checkpoints
+        ctl["final"] = arrays
+        ctx.ctl = ctl
+        return tuple(t.detach() for t in ctl["layout"].flatten(arrays))
+
+    @staticmethod
+    def backward(ctx, *grads):
+        ctl = ctx.ctl
+        scene, layout, bounds = ctl["scene"], ctl["layout"], ctl["bounds"]
+        final: ArrayContainer = ctl["final"]
+        outs = layout.flatten(final)
+
+        def cot(i):
+            g = grads[i]
+            if g is None:
+                return torch.zeros_like(outs[i])
+            return g.detach().to(outs[i].dtype).contiguous().clone()
+
+        lam = {"E": cot(0), "H": cot(1)}
+        i = 2
+        lam["psi_E"], lam["psi_H"] = {}, {}
+        for n in layout.pml_names:
+            lam["psi_E"][n] = (cot(i), cot(i + 1))
+            i += 2
+        for n in layout.pml_names:
+            lam["psi_H"][n] = (cot(i), cot(i + 1))
+            i += 2
+        lam["det"] = {}
+        for n, _k in layout.det_keys:
+            if grads[i] is not None:
+                lam["det"][n] = cot(i)
+            i += 1
+        ie = ctl["inv_eps"]
+        grad = torch.zeros_like(ie, dtype=torch.float32).contiguous()
+        lam["grad_inv_eps"] = grad
+        if final.fields.dispersive_P_curr is not None:  # the polarisation is no output: zero cotangents
+            lam["P_curr"] = torch.zeros_like(final.fields.dispersive_P_curr)
+            lam["P_prev"] = torch.zeros_like(final.fields.dispersive_P_prev)
+        # recompute on scratch state (the detector states accumulate there and are discarded)
+        work = final.aset("fields", _clone_fields(final.fields)).aset(
+            "detector_states", {k: {k2: v2.clone() for k2, v2 in v.items()} for k, v in final.detector_states.items()})
+        for seg in range(len(bounds) - 2, -1, -1):
+            t0, L = bounds[seg], bounds[seg + 1] - bounds[seg]
+            _copy_fields(work.fields, ctl["checkpoints"][seg])
+            states = [_clone_fields(work.fields)]
+            for q in range(L):
+                scene.forward(work, t0 + q, 1, graph=False)
+                states.append(_clone_fields(work.fields))
+            scene.adjoint_stored(work, states, t0, lam)
+            del states
+        scene.status()
+        return None, grad.to(ie.dtype), None
+
+
+def checkpointed_gradient_run(arrays: ArrayContainer, objects: ObjectContainer, config: SimulationConfig):
+    """The forward run of checkpointed_fdtd connected to d/d inv_permittivities through the
+    exact stored-state backward pass (``_CheckpointedRun``); returns the output container."""
+    from fdtdx_gb300.fdtd import _materials_detached, get_scene
+
+    gc = config.gradient_config
+    if gc is None or gc.num_checkpoints is None:
+        raise Exception("Need Checkpoint Number in gradient config to compute checkpointed gradients")
+    mu = arrays.inv_permeabilities
+    if isinstance(mu, torch.Tensor) and mu.requires_grad:
+        raise NotImplementedError("the checkpointed gradient provides d/d inv_permittivities only")
+    T = config.time_steps_total
+    n_seg = max(1, min(int(gc.num_checkpoints), T))
+    bounds = reversible_slice_boundaries(T, n_seg)
+    ie_in = arrays.inv_permittivities
+    work = _materials_detached(arrays).reset()
+    scene = get_scene(objects, work, config, record_interfaces=False)
+    if scene.complex_fields or scene.full_tensor:
+        raise NotImplementedError("the checkpointed gradient of complex (Bloch) fields or full 3x3 tensor materials "
+                                  "is not supported by the GB300 kernels")
+    layout = _Layout(work)
+    ctl = {"scene": scene, "arrays": work, "bounds": bounds, "layout": layout, "inv_eps": work.inv_permittivities}
+    flat = _CheckpointedRun.apply(ctl, ie_in, None)
+    out = layout.unflatten(work, list(flat))
+    return out.aset("inv_permittivities", ie_in)

@@ -1553,4 +1553,59 @@ __global__ void k_adj_det_clear(const DDet d, void* lam, const int* __restrict__
     for (int q = threadIdx.x; q < d.ncomp; q += blockDim.x) reinterpret_cast<float*>(lam)[(long long)slot * d.ncomp + q] = 0.f;
 }
 
+// Transpose of the ADE part of the E-step at t (k_ade folded into the E update,
+// fdtdx/fdtd/update.py:316-350), after the transposed E-step has written lam E(t):
+// E_new = (f E + c curl inv + inv sum_p (Pc_p - P_hat_p)) / d, P_hat_p = c1 Pc_p + c2 Pp_p + c3 E,
+// new Pc = P_hat, new Pp = Pc.  With lam the cotangent of E_new (conductor faces zeroed),
+// w = inv / d and lamPc', lamPp' the cotangents of the new pair:
+//   lam E(t)   += sum_p c3_p (lamPc'_p - w lam)
+//   lam Pc(t)_p = w (1 - c1_p) lam + c1_p lamPc'_p + lamPp'_p
+//   lam Pp(t)_p = c2_p (lamPc'_p - w lam)
+//   d/d inv    += lam sum_p (Pc_p - P_hat_p) / d^2   (the part the transposed E-step lacks)
+// One thread per component and cell; E, Pc, Pp the stored state of step t.
+__global__ void __launch_bounds__(256) k_ade_T(const Geo g, const float* __restrict__ lamE3, float* lamE_out,
+                                               const float* __restrict__ lPc1, const float* __restrict__ lPp1,
+                                               float* __restrict__ lPc0, float* __restrict__ lPp0,
+                                               const float* __restrict__ E, const float* __restrict__ Pc,
+                                               const float* __restrict__ Pp, const float* __restrict__ c1,
+                                               const float* __restrict__ c2, const float* __restrict__ c3, int np,
+                                               int nd, const float* __restrict__ ie, int n_eps,
+                                               const float* __restrict__ sig, int n_sig, float* grad) {
+    const long long N = g.N;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * N) return;
+    const int comp = (int)(idx / N);
+    const long long c = idx - comp * N;
+    const int k = (int)(c % g.nz);
+    const long long r = c / g.nz;
+    const int j = (int)(r % g.ny);
+    const int i = (int)(r / g.ny);
+    float lam = lamE3[idx];
+    if (g.pec && face_zero(g, g.pec, comp, i, j, k)) lam = 0.f;
+    const float m = __ldg(ie + (n_eps == 3 ? comp : 0) * N + c);
+    const float d = sig ? 1.f + g.c * __ldg(sig + (n_sig == 3 ? comp : 0) * N + c) * g.eta0 * m / 2.f : 1.f;
+    const float w = m / d;
+    const float e = __ldg(E + idx);
+    float addE = 0.f, dsum = 0.f;
+    for (int p = 0; p < np; ++p) {
+        const long long pi = ((long long)p * 3 + comp) * N + c;
+        const long long ci = ((long long)p * nd + (nd == 3 ? comp : 0)) * N + c;
+        const float a1 = __ldg(c1 + ci), a2 = __ldg(c2 + ci), a3 = __ldg(c3 + ci);
+        const float lpc = lPc1[pi], lpp = lPp1[pi];
+        addE += a3 * (lpc - w * lam);
+        lPc0[pi] = w * (1.f - a1) * lam + a1 * lpc + lpp;
+        lPp0[pi] = a2 * (lpc - w * lam);
+        if (grad) {
+            const float pc = __ldg(Pc + pi), pp = __ldg(Pp + pi);
+            dsum += pc - (a1 * pc + a2 * pp + a3 * e);
+        }
+    }
+    lamE_out[idx] += addE;
+    if (grad) {
+        const float gv = lam * dsum / (d * d);
+        if (n_eps == 3) grad[comp * N + c] += gv;
+        else atomicAdd(grad + c, gv);  // the three components of one cell share an isotropic entry
+    }
+}
+
 }  // namespace fdtd

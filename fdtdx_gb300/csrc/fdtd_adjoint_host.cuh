@@ -68,6 +68,9 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
         b.M = (long long)b.n[0] * b.n[1] * b.n[2];
         o_snap[q] = ar.take(sizeof(float) * 6 * parts * (size_t)b.M);
     }
+    size_t o_lP[2] = {0, 0};
+    if (d.n_poles > 0)
+        for (int q = 0; q < 2; ++q) o_lP[q] = ar.take(sizeof(float) * 3 * (size_t)d.n_poles * (size_t)N);
     char* mem = nullptr;
     cudaError_t e = dev_alloc(reinterpret_cast<void**>(&mem), ar.off);
     if (e != cudaSuccess) return fail(p, FDTD_ENOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
@@ -84,6 +87,8 @@ int ensure_adjoint_scratch(FdtdPlan* p) {
         for (int q = 0; q < 4; ++q) p->lpsi_twin[s][q] = reinterpret_cast<float*>(mem + o_psi[s][q]);
     p->hp = hp;
     if (any) p->hp.buf = reinterpret_cast<float*>(mem + o_hp);
+    if (d.n_poles > 0)
+        for (int q = 0; q < 2; ++q) p->lP_twin[q] = reinterpret_cast<float*>(mem + o_lP[q]);
     for (int q = 0; q < d.n_detectors; ++q) {
         p->snap[q] = snap[q];
         if (det_bilinear(p->det[q])) p->snap[q].buf = reinterpret_cast<float*>(mem + o_snap[q]);
@@ -96,6 +101,8 @@ struct LamSet {
     float* E;
     float* H;
     float* psi[FDTD_MAX_SLABS][4];
+    float* Pc = nullptr;  // polarisation cotangents (dispersive scenes, stored-state loop)
+    float* Pp = nullptr;
 };
 
 // The transposed step's arguments; `part` 1 selects the imaginary parts of complex (Bloch)
@@ -195,7 +202,6 @@ int check_adj(FdtdPlan* p, const FdtdAdjointBuffers* adj) {
         return fail(p, FDTD_EINVAL, "grad_inv_mu needs an inv_mu array (n_mu 1 or 3), not a scalar inv_mu");
     if (p->full_e || p->full_h)
         return fail(p, FDTD_EINVAL, "the reversible gradient of full 3x3 tensor materials is not supported");
-    if (p->d.n_poles > 0) return fail(p, FDTD_EINVAL, "the reversible gradient of dispersive materials is not supported");
     return FDTD_OK;
 }
 
@@ -320,7 +326,108 @@ void launch_adjoint_step(const FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjo
     k_advance<<<1, 1, 0, st>>>(p->d_t, -1);
 }
 
+// One step of the backward loop over stored states (the exact checkpointing gradient): the
+// transposed forward step at t with the state of step t taken from `s_t` and that of step
+// t + 1 from `s_t1` -- no reconstruction.  Detector cotangents see E3 = E(t + 1) and H(t), the
+// transposed steps E(t), H(t) and the stored psi of step t.
+void launch_adjoint_step_stored(const FdtdPlan* p, const FdtdBuffers* s_t, const FdtdBuffers* s_t1,
+                                const FdtdAdjointBuffers* adj, const LamSet& cur, const LamSet& nxt, int t,
+                                cudaStream_t st) {
+    k_set_step<<<1, 1, 0, st>>>(p->d_t, t);
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (!adj->lam_det[q] || !p->snap[q].buf) continue;
+        const DBox& sb = p->snap[q];
+        k_adj_snap<<<(unsigned)((sb.M + 255) / 256), 256, 0, st>>>(p->g, sb, p->det[q].slot, p->d_t, s_t1->E, s_t1->H);
+    }
+    FdtdBuffers bd = *s_t;
+    bd.E = s_t1->E;
+    const AdjArgs ad = make_adj(p, &bd, adj, cur, nxt, 0);
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        if (!adj->lam_det[q]) continue;
+        AdjDet x{};
+        x.d = p->det[q];
+        x.lam = adj->lam_det[q];
+        x.snap = p->snap[q];
+        k_adj_det<<<p->det[q].nblocks, kDetBlock, 0, st>>>(ad, x, p->d_t);
+    }
+    for (int q = 0; q < p->d.n_detectors; ++q) {
+        const DDet& dd = p->det[q];
+        if (adj->lam_det[q] && dd.reduce && dd.kind != FDTD_DET_PHASOR)
+            k_adj_det_clear<<<1, 32, 0, st>>>(dd, adj->lam_det[q], p->d_t);
+    }
+    launch_adj<true>(p, make_adj(p, s_t, adj, cur, nxt, 0), st);
+    launch_adj<false>(p, make_adj(p, s_t, adj, cur, nxt, 0), st);
+    if (p->d.n_poles > 0) {  // the ADE part of the E-step, after lam E(t) holds the rest
+        const long long n3 = 3 * p->g.N;
+        k_ade_T<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(
+            p->g, cur.E, nxt.E, cur.Pc, cur.Pp, nxt.Pc, nxt.Pp, s_t->E, s_t->disp_P_curr, s_t->disp_P_prev,
+            s_t->disp_c1, s_t->disp_c2, s_t->disp_c3, p->d.n_poles, p->d.n_disp, s_t->inv_eps, p->d.n_eps,
+            p->d.n_sigma_E ? s_t->sigma_E : nullptr, p->d.n_sigma_E, adj->grad_inv_eps);
+    }
+}
+
 }  // namespace
+
+extern "C" int fdtd_adjoint_stored(FdtdPlan* p, const FdtdBuffers* states, int32_t t0, int32_t n_steps,
+                                   const FdtdAdjointBuffers* adj, void* stream) {
+    NvtxRange nvtx_range("fdtd_adjoint_stored");
+    if (!p) return FDTD_EINVAL;
+    if (cudaError_t pre = cudaGetLastError(); pre != cudaSuccess)
+        return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_adjoint_stored)");
+    if (!states) return fail(p, FDTD_EINVAL, "states required");
+    if (n_steps < 0 || t0 < 0 || (long long)t0 + n_steps > p->d.n_steps_total)
+        return fail(p, FDTD_EINVAL, "stored adjoint steps out of the range covered by the plan's tables");
+    for (int q = 0; q <= n_steps; ++q)
+        if (int rc = check_bufs(p, &states[q])) return rc;
+    if (int rc = check_adj(p, adj)) return rc;
+    if (p->parts != 1) return fail(p, FDTD_EINVAL, "the stored-state gradient of complex (Bloch) fields is not supported");
+    if (p->d.n_poles > 0 && (!adj->lam_P_curr || !adj->lam_P_prev))
+        return fail(p, FDTD_EINVAL, "a dispersive scene needs the polarisation cotangent buffers");
+    if (adj->grad_inv_mu) return fail(p, FDTD_EINVAL, "the stored-state gradient provides d/d inv_eps only");
+    if (n_steps == 0) return FDTD_OK;
+    if (int rc = ensure_adjoint_scratch(p)) return rc;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    LamSet user{}, twin{};
+    user.E = adj->lam_E;
+    user.H = adj->lam_H;
+    twin.E = p->lam_twin[0];
+    twin.H = p->lam_twin[1];
+    for (int s = 0; s < p->d.n_slabs; ++s) {
+        user.psi[s][0] = adj->lam_psi_E[s][0]; user.psi[s][1] = adj->lam_psi_E[s][1];
+        user.psi[s][2] = adj->lam_psi_H[s][0]; user.psi[s][3] = adj->lam_psi_H[s][1];
+        for (int q = 0; q < 4; ++q) twin.psi[s][q] = p->lpsi_twin[s][q];
+    }
+    user.Pc = adj->lam_P_curr;
+    user.Pp = adj->lam_P_prev;
+    twin.Pc = p->lP_twin[0];
+    twin.Pp = p->lP_twin[1];
+    const LamSet* cur = &user;
+    const LamSet* nxt = &twin;
+    for (int q = n_steps - 1; q >= 0; --q) {
+        launch_adjoint_step_stored(p, &states[q], &states[q + 1], adj, *cur, *nxt, t0 + q, st);
+        std::swap(cur, nxt);
+    }
+    if (cur != &user) {  // odd step count: the result sits in the twins
+        const size_t fb = sizeof(float) * 3 * (size_t)p->g.N;
+        cudaError_t e = cudaMemcpyAsync(user.E, cur->E, fb, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(user.H, cur->H, fb, cudaMemcpyDeviceToDevice, st);
+        for (int s = 0; s < p->d.n_slabs && e == cudaSuccess; ++s) {
+            const DSlab& sl = p->slab[s];
+            const size_t pb = sizeof(float) * (size_t)sl.sx * sl.sy * sl.sz;
+            for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+                e = cudaMemcpyAsync(user.psi[s][q], cur->psi[s][q], pb, cudaMemcpyDeviceToDevice, st);
+        }
+        if (p->d.n_poles > 0 && e == cudaSuccess) {
+            const size_t pb = sizeof(float) * 3 * (size_t)p->d.n_poles * (size_t)p->g.N;
+            e = cudaMemcpyAsync(user.Pc, cur->Pc, pb, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(user.Pp, cur->Pp, pb, cudaMemcpyDeviceToDevice, st);
+        }
+        if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_adjoint_stored copy-back");
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(p, e, "fdtd_adjoint_stored launch");
+    return FDTD_OK;
+}
 
 extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjointBuffers* adj, int32_t t_end,
                             int32_t n_steps, void* stream) {
@@ -330,6 +437,7 @@ extern "C" int fdtd_adjoint(FdtdPlan* p, const FdtdBuffers* b, const FdtdAdjoint
         return cuda_fail(p, pre, "error left pending by an earlier CUDA call (before fdtd_adjoint)");
     if (int rc = check_bufs(p, b)) return rc;
     if (int rc = check_adj(p, adj)) return rc;
+    if (p->d.n_poles > 0) return fail(p, FDTD_EINVAL, "the reversible gradient of dispersive materials is not supported");
     if (p->parts != 1 && adj->grad_inv_mu)
         return fail(p, FDTD_EINVAL, "the inv_mu cotangent of complex (Bloch) fields is not supported (inv_eps is)");
     if (n_steps < 0 || t_end - n_steps < -1 || t_end > p->d.n_steps_total)

@@ -80,6 +80,7 @@ struct FdtdPlan {
     size_t amem_bytes = 0;
     float* lam_twin[2] = {nullptr, nullptr};      // cotangent twins of E and H
     float* lpsi_twin[FDTD_MAX_SLABS][4] = {};     // twins of the psi_E (1, 2) and psi_H (1, 2) cotangents
+    float* lP_twin[2] = {nullptr, nullptr};       // twins of the polarisation cotangents (dispersive scenes)
     DBox hp{};                                    // H-before-update cotangents of exact detectors
     DBox snap[FDTD_MAX_DETECTORS] = {};           // (E3, H3) snapshots of bilinear detectors
     std::string err;

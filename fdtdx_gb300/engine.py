@@ -793,6 +793,38 @@ class Scene:
             if lw is not None:
                 lw.store(lam)
 
+    def adjoint_stored(self, arrays: ArrayContainer, states: list, t0: int, lam: dict, stream=None) -> None:
+        """Backward loop over stored states (``fdtd_adjoint_stored``): ``states[q]`` is the
+        ``FieldState`` of step ``t0 + q``; the transposed steps run from ``t0 + len(states) - 2``
+        down to ``t0``.  ``arrays`` supplies the materials and detector states; ``lam`` as in
+        ``adjoint`` (real fields; d/d inv_eps only)."""
+        if self.complex_fields:
+            raise NotImplementedError("the stored-state gradient of complex (Bloch) fields is not supported")
+        if lam.get("grad_inv_mu") is not None:
+            raise NotImplementedError("the stored-state gradient provides d/d inv_permittivities only")
+        st = stream if stream is not None else torch.cuda.current_stream(arrays.device)
+        n = len(states) - 1
+        bufs = (N.Buffers * (n + 1))()
+        for q, f in enumerate(states):
+            bufs[q] = self.buffers(arrays.aset("fields", f))
+        a = N.AdjointBuffers()
+        for key in ("E", "H"):
+            t = lam[key]
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
+                raise ValueError("cotangents must be contiguous float32 CUDA tensors")
+        a.lam_E, a.lam_H = N.ptr(lam["E"]), N.ptr(lam["H"])
+        for s, p in enumerate(self.pmls):
+            a.lam_psi_E[s][0], a.lam_psi_E[s][1] = N.ptr(lam["psi_E"][p.name][0]), N.ptr(lam["psi_E"][p.name][1])
+            a.lam_psi_H[s][0], a.lam_psi_H[s][1] = N.ptr(lam["psi_H"][p.name][0]), N.ptr(lam["psi_H"][p.name][1])
+        dets = lam.get("det", {})
+        for q, det in enumerate(self.detectors):
+            a.lam_det[q] = N.ptr(dets.get(det.name))
+        a.grad_inv_eps = N.ptr(lam.get("grad_inv_eps"))
+        if self.dispersive:
+            a.lam_P_curr, a.lam_P_prev = N.ptr(lam["P_curr"]), N.ptr(lam["P_prev"])
+        rc = N.load().fdtd_adjoint_stored(self.plan, bufs, int(t0), int(n), C.byref(a), C.c_void_p(st.cuda_stream))
+        N.check(rc, self.plan, "fdtd_adjoint_stored")
+
 
 class PlanarFields:
     """The planar float32 workspace of a complex (Bloch) scene's state: E, H, the psi pairs and

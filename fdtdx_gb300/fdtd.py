@@ -90,8 +90,14 @@ def checkpointed_fdtd(
     del key, show_progress
     if stopping_condition is not None:
         raise NotImplementedError("custom stopping conditions are not supported")
-    if arrays.inv_permittivities.requires_grad:
-        raise NotImplementedError("gradients of checkpointed_fdtd are not provided; use GradientConfig(method='reversible')")
+    if arrays.inv_permittivities.requires_grad and torch.is_grad_enabled():
+        # the exact gradient through stored states (fdtd.py:421-496 differentiated by JAX)
+        from fdtdx_gb300.adjoint import checkpointed_gradient_run
+
+        out = checkpointed_gradient_run(arrays, objects, config)
+        if progress_callback is not None:
+            progress_callback(config.time_steps_total, config.time_steps_total)
+        return config.time_steps_total, out
     arrays = _materials_detached(arrays).reset()
     scene = get_scene(objects, arrays, config, record_interfaces=config.invertible_optimization)
     T = config.time_steps_total

@@ -24,7 +24,7 @@
  *
  * Conventions
  *   - Every buffer is caller-owned device memory, float32, C order, z fastest.
- *     Fields are (3, nx, ny, nz).  Material arrays are (n, nx, ny, nz), n in {1, 3}.
+ *     Fields are (3, nx, ny, nz).  Material arrays are (n, nx, ny, nz), n in {1, 3, 9}.
  *   - The plan copies the small host tables of FdtdDesc (PML coefficients,
  *     per-step source and detector tables, plane-source profiles) to device
  *     memory it owns, plus scratch for reductions.  It never touches caller buffers
@@ -203,6 +203,10 @@ typedef struct {
     /* (n_mu, nx, ny, nz), accumulated (+=), or NULL; needs an inv_mu array (n_mu 1 or 3).
      * The reference's custom VJP returns this cotangent as cot[6] (fdtdx/fdtd/fdtd.py:331). */
     float* grad_inv_mu;
+    /* dispersive scenes (fdtd_adjoint_stored only): cotangents of the polarisation pair,
+     * (n_poles, 3, nx, ny, nz) each, updated in place like lam_E */
+    float* lam_P_curr;
+    float* lam_P_prev;
 } FdtdAdjointBuffers;
 
 typedef struct FdtdPlan FdtdPlan;
@@ -244,6 +248,19 @@ int fdtd_reverse(FdtdPlan* plan, const FdtdBuffers* bufs, int32_t t_end, int32_t
  * fdtd_plan_device_bytes counts it from then on. */
 int fdtd_adjoint(FdtdPlan* plan, const FdtdBuffers* bufs, const FdtdAdjointBuffers* adj, int32_t t_end,
                  int32_t n_steps, void* stream);
+
+/* Backward loop over stored states: the exact gradient of GradientConfig(method="checkpointed"),
+ * where the reference differentiates its checkpointed while loop (fdtdx/fdtd/fdtd.py:421-496).
+ * states[q], q = 0 .. n_steps, hold the full state (E, H, psi; materials and detector states
+ * as in any FdtdBuffers) of step t0 + q, recomputed by the caller from a checkpoint.  For
+ * t = t0 + n_steps - 1 down to t0 the transposed forward step at t runs at the stored states
+ * of steps t and t + 1 -- no reconstruction, so psi is exact and so is the gradient inside
+ * the CPML.  adj as in fdtd_adjoint (cotangents of state t0 + n_steps in, of state t0 out;
+ * grad_inv_eps accumulates).  Real fields with 1 or 3 material components; dispersive scenes
+ * transpose the ADE step as well (their states carry the polarisation pair, adj its
+ * cotangents lam_P_curr / lam_P_prev); grad_inv_mu is not provided (FDTD_EINVAL). */
+int fdtd_adjoint_stored(FdtdPlan* plan, const FdtdBuffers* states, int32_t t0, int32_t n_steps,
+                        const FdtdAdjointBuffers* adj, void* stream);
 
 /* Tuning of the update kernels: `chunk` x planes per block, `vec` z cells per thread
  * (1, 2 or 4, dividing nz); 0 restores a default.  Invalidates a cached CUDA graph.

@@ -54,6 +54,7 @@ int main(void) {
   O(FdtdBuffers, psi_E) O(FdtdBuffers, det_state) O(FdtdBuffers, recording) O(FdtdBuffers, disp_P_curr)
   O(FdtdBuffers, disp_c3)
   O(FdtdAdjointBuffers, lam_det) O(FdtdAdjointBuffers, grad_inv_eps) O(FdtdAdjointBuffers, grad_inv_mu)
+  O(FdtdAdjointBuffers, lam_P_prev)
   return 0;
 }
 """

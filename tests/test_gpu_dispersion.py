@@ -142,3 +142,46 @@ def test_dispersive_reverse_is_refused():
     with pytest.raises(N.NativeError, match="dispersive"):
         scene.reverse(arrays, 2, 2)
     scene.close()
+
+
+@pytest.mark.parametrize("segments", [1, 4])
+def test_dispersive_checkpointed_gradient(segments):
+    """The reference's gradient method for dispersive materials, GradientConfig(method=
+    "checkpointed"): d|phasor|^2 / d inv_eps through the stored-state backward pass with the ADE
+    step transposed (k_ade_T), against autograd through the oracle's forward run over the whole
+    grid (float32 oracle asserted: both store the ADE coefficients in float32; float64
+    reported)."""
+    dx = 25e-9
+    nx, ny, nz = 6, 6, 70
+    wc = fx.WaveCharacter(wavelength=WL)
+    pulse = fx.GaussianPulseProfile(spectral_width=fx.WaveCharacter(frequency=0.2 * C0 / WL), center_wave=wc)
+    gc = fx.GradientConfig(method="checkpointed", num_checkpoints=segments)
+    cfg = fx.SimulationConfig(time=160 * 0.99 / math.sqrt(3) * dx / C0, grid=fx.UniformGrid(dx), gradient_config=gc)
+    vol = fx.SimulationVolume(shape=(nx, ny, nz))
+    bc = fx.BoundaryConfig.from_uniform_bound(8, override_types={"min_x": "periodic", "max_x": "periodic",
+                                                                 "min_y": "periodic", "max_y": "periodic"})
+    poles = _lorentz().poles + (fx.DrudePole(plasma_frequency=1.5 * OMEGA, damping=0.05 * OMEGA),)
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    objs += [
+        fx.UniformMaterialObject(name="slab", grid_slice_tuple=((0, nx), (0, ny), (30, 50)), material=fx.Material(
+            permittivity=1.5, electric_conductivity=2e3, dispersion=fx.DispersionModel(poles=poles))),
+        fx.UniformPlaneSource(name="pl", grid_slice_tuple=((0, nx), (0, ny), (15, 16)), direction="+",
+                              fixed_E_polarization_vector=(1, 0, 0), wave_character=wc, temporal_profile=pulse),
+        fx.PhasorDetector(name="ph", grid_slice_tuple=((0, nx), (0, ny), (25, 55)), wave_characters=(wc,)),
+    ]
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg, device="cuda")
+    ie = arrays.inv_permittivities.clone().requires_grad_(True)
+    _, out = fx.run_fdtd(arrays.aset("inv_permittivities", ie), objects, cfg)
+    (out.detector_states["ph"]["phasor"].abs() ** 2).sum().backward()
+    g_gpu = ie.grad.detach().cpu()
+    res = {}
+    for dt in (torch.float32, torch.float64):
+        sc = O.OracleScene(objects, arrays, cfg, dt)
+        res[dt] = O.autograd_gradient(sc, lambda det: (det["ph"]["phasor"].abs() ** 2).sum(), cfg.time_steps_total)
+    e32 = float(torch.linalg.vector_norm(g_gpu.double() - res[torch.float32].double().cpu())
+                / torch.linalg.vector_norm(res[torch.float32].double()))
+    e64 = float(torch.linalg.vector_norm(g_gpu.double() - res[torch.float64].double().cpu())
+                / torch.linalg.vector_norm(res[torch.float64].double()))
+    log_result(f"dispersion_checkpointed_gradient_{segments}", grad_rel_l2_vs_fp32_autograd=e32,
+               grad_rel_l2_vs_fp64_autograd=e64)
+    assert torch.linalg.vector_norm(res[torch.float64]).item() > 0 and e32 <= 1e-3, (e32, e64)
