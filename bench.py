@@ -450,6 +450,22 @@ def _batch_case(sims, cells, steps: int) -> dict:
     bt = time.perf_counter() - t0
     tune = b.tuning()
     launches = b.launches_per_step()
+    # each execution mode on its own (CUDA graph where the mode has one), fewer steps
+    mode_steps = min(steps, 400)
+    modes = {}
+    for mode in ("persistent", "branches", "fused"):
+        b.set_mode(mode)
+        b.advance(64, t0=[0] * len(sims), graph=True, autotune=False)
+        for w in b.arrays:
+            _zero_state(w)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.advance(mode_steps, t0=[0] * len(sims), graph=True, autotune=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        # launches per batch step; the fused mode reports 1: one launch runs all the steps of a call
+        modes[mode] = {"steps": mode_steps, "s": round(dt, 4), "cell_updates_per_s": cells * mode_steps / dt,
+                       "launches_per_step": b.launches_per_step()}
     b.close()
     return {
         "cells_total": cells,
@@ -460,6 +476,7 @@ def _batch_case(sims, cells, steps: int) -> dict:
         "sequential_s": round(seq_s, 3),
         "launches_per_batch_step": launches,
         "tiles": tune,
+        "modes": modes,
     }
 
 

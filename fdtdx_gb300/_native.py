@@ -17,7 +17,7 @@ MAX_FREQS = 16
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENONFINITE = range(6)
 FWD_GRAPH, FWD_CHECK_FINITE = 1, 2
-INJECT_ALLOC, INJECT_WAIT_EXPIRY = 1, 2
+INJECT_ALLOC, INJECT_WAIT_EXPIRY, INJECT_BARRIER_EXPIRY = 1, 2, 3
 PROFILE_CW, PROFILE_GAUSSIAN = 0, 1
 SRC_DIPOLE, SRC_PLANE = 0, 1
 DET_FIELD, DET_PHASOR, DET_FLUX, DET_ENERGY = 0, 1, 2, 3

@@ -97,10 +97,10 @@ class SimulationBatch:
 
     @property
     def mode(self) -> str:
-        return {0: "persistent", 1: "branches"}[int(N.load().fdtd_batch_mode(self._h))]
+        return {0: "persistent", 1: "branches", 2: "fused"}[int(N.load().fdtd_batch_mode(self._h))]
 
     def set_mode(self, mode: str) -> None:
-        rc = N.load().fdtd_batch_set_mode(self._h, {"persistent": 0, "branches": 1}[mode])
+        rc = N.load().fdtd_batch_set_mode(self._h, {"persistent": 0, "branches": 1, "fused": 2}[mode])
         self._check(rc, "fdtd_batch_set_mode")
 
     def launches_per_step(self) -> int:

@@ -12,6 +12,7 @@
 // the arithmetic), so tuning costs no extra simulation work.
 #pragma once
 #include "fdtd_batch_kernels.cuh"
+#include "fdtd_fused.h"
 
 struct FdtdBatch {
     int n = 0;
@@ -52,7 +53,12 @@ struct FdtdBatch {
     cudaStream_t cap_stream = nullptr;
     // mode 1 ("branches"): each simulation's own launch chain (TMA cores) on its own stream,
     // forked from and joined to the caller's stream -- parallel branches of one graph
+    // mode 2 ("fused"): all steps of a call in one cooperative launch (fdtd_fused.cu) with a
+    // bounded grid barrier between phases; fbar / ferr are its barrier and error words
     int mode = 0;
+    unsigned* fbar = nullptr;
+    int* ferr = nullptr;
+    mutable int fused_rc = 0;
     std::vector<cudaStream_t> sim_streams;
     std::vector<cudaEvent_t> join_ev;
     cudaEvent_t fork_ev = nullptr;
@@ -249,8 +255,53 @@ void batch_run_branches(const FdtdBatch* b, int parity, int steps, cudaStream_t 
     }
 }
 
+// The fused mode's tables: the batch's own device tables, read by one persistent kernel.
+FdtdFusedTables fused_tables(const FdtdBatch* b) {
+    FdtdFusedTables t{};
+    t.units = b->units;
+    t.n_units = b->n_units;
+    for (int q = 0; q < 5; ++q) t.class_start[q] = b->class_start[q];
+    t.argsE = b->argsE;
+    t.argsH = b->argsH;
+    t.max_args = b->max_args;
+    t.src_unitsE = b->src_unitsE;
+    t.n_src_unitsE = b->n_src_unitsE;
+    t.srcE = b->srcE;
+    t.src_unitsH = b->src_unitsH;
+    t.n_src_unitsH = b->n_src_unitsH;
+    t.srcH = b->srcH;
+    t.iface_units = b->iface_units;
+    for (int q = 0; q < 4; ++q) t.iface_start[q] = b->iface_start[q];
+    t.ifaces = b->ifaces;
+    t.det_units = b->det_units;
+    t.n_det_units = b->n_det_units;
+    t.dets = b->dets;
+    t.det_red = b->det_red;
+    t.n_det_red = b->n_det_red;
+    t.tps = b->tps;
+    t.n_sims = b->n;
+    t.any_hprev = b->any_hprev ? 1 : 0;
+    t.bar = b->fbar;
+    t.err = b->ferr;
+    t.spin_limit = 1ll << 26;  // >= 4 s of polling at 64 ns per poll
+    return t;
+}
+
 // Runs `steps` steps from `parity` with direct launches; returns the parity after them.
 int batch_run_direct(const FdtdBatch* b, int parity, int steps, cudaStream_t st) {
+    if (b->mode == 2) {
+        if (steps <= 0) return parity;
+        FdtdFusedTables t = fused_tables(b);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cs);
+        if (cs == cudaStreamCaptureStatusNone && take_injected(g_inject_barrier)) {
+            t.inject_skip = 1;
+            t.spin_limit = 1 << 16;
+        }
+        const int rc = fdtd_fused_launch(&t, steps, parity, st);
+        if (rc && !b->fused_rc) b->fused_rc = rc;
+        return b->any_hprev ? parity ^ (steps & 1) : parity;
+    }
     if (b->mode == 1) {
         batch_run_branches(b, parity, steps, st);
         return b->any_hprev ? parity ^ (steps & 1) : parity;
@@ -344,6 +395,7 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     const size_t oD = ar.take(sizeof(BDet) * std::max(1, dets)), oDU = ar.take(sizeof(int2) * std::max(1, du));
     const size_t oDR = ar.take(sizeof(int) * std::max(1, dred)), oT = ar.take(sizeof(int*) * n);
     const size_t oI = ar.take(sizeof(BIface) * std::max(1, nif)), oIU = ar.take(sizeof(int2) * std::max(1, ifu));
+    const size_t oFB = ar.take(2 * sizeof(unsigned)), oFE = ar.take(sizeof(int));
     cudaError_t e = dev_alloc(reinterpret_cast<void**>(&b->dmem), ar.off);
     if (e != cudaSuccess) {
         fprintf(stderr, "fdtd_batch_create: cudaMalloc(%zu): %s\n", ar.off, cudaGetErrorString(e));
@@ -363,6 +415,12 @@ int fdtd_batch_create(FdtdPlan* const* plans, const FdtdBuffers* bufs, int32_t n
     b->tps = reinterpret_cast<int**>(b->dmem + oT);
     b->ifaces = reinterpret_cast<BIface*>(b->dmem + oI);
     b->iface_units = reinterpret_cast<int2*>(b->dmem + oIU);
+    b->fbar = reinterpret_cast<unsigned*>(b->dmem + oFB);
+    b->ferr = reinterpret_cast<int*>(b->dmem + oFE);
+    if (cudaMemset(b->fbar, 0, 2 * sizeof(unsigned)) != cudaSuccess || cudaMemset(b->ferr, 0, sizeof(int)) != cudaSuccess) {
+        fdtd_batch_destroy(b);
+        return FDTD_ECUDA;
+    }
     // sources, detectors, step counters (independent of the tile choice)
     std::vector<BSrc> hsE, hsH;
     std::vector<int2> huE, huH, hdu;
@@ -492,8 +550,14 @@ int fdtd_batch_tuning(const FdtdBatch* b, int32_t* out4) {
 }
 
 int fdtd_batch_set_mode(FdtdBatch* b, int32_t mode) {
-    if (!b || (mode != 0 && mode != 1)) return bfail(b, FDTD_EINVAL, "mode must be 0 (persistent) or 1 (branches)");
+    if (!b || mode < 0 || mode > 2) return bfail(b, FDTD_EINVAL, "mode must be 0 (persistent), 1 (branches) or 2 (fused)");
     if (mode == 1 && !batch_branch_streams(b)) return bfail(b, FDTD_ECUDA, "branch streams could not be created");
+    if (mode == 2) {
+        int dev = 0, coop = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+            !coop)
+            return bfail(b, FDTD_EINVAL, "the fused mode needs a device with cooperative launches");
+    }
     cudaDeviceSynchronize();
     b->mode = mode;
     batch_drop_graph(b);
@@ -504,6 +568,7 @@ int32_t fdtd_batch_mode(const FdtdBatch* b) { return b ? b->mode : -1; }
 
 int32_t fdtd_batch_launches_per_step(const FdtdBatch* b) {
     if (!b) return 0;
+    if (b->mode == 2) return 1;  // one launch for all the steps of a call
     if (b->mode == 1) {
         int n = 0;
         for (const FdtdPlan* p : b->plans) n += fdtd_launches_per_step(p);
@@ -521,30 +586,69 @@ int32_t fdtd_batch_launches_per_step(const FdtdBatch* b) {
 
 namespace {
 
+// Times `steps` steps from *parity (updating it): under a CUDA graph captured for the purpose
+// when `graph` is set (the way fdtd_batch_forward will run them; the fused mode is one launch
+// either way), else as direct launches.  Returns the milliseconds, or -1 on failure.
+float batch_time_steps(FdtdBatch* b, int* parity, int steps, bool graph, cudaStream_t st, cudaEvent_t e0,
+                       cudaEvent_t e1) {
+    float ms = -1.f;
+    if (graph && b->mode != 2) {
+        if (!b->cap_stream && cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) return -1.f;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1.f;
+        const int after = batch_run_direct(b, *parity, steps, b->cap_stream);
+        const bool ok = cudaStreamEndCapture(b->cap_stream, &g) == cudaSuccess && g &&
+                        cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+        if (ok) {
+            cudaEventRecord(e0, st);
+            if (cudaGraphLaunch(ge, st) == cudaSuccess) {
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                cudaEventElapsedTime(&ms, e0, e1);
+                *parity = after;
+            } else {
+                ms = -1.f;
+            }
+        }
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+        return ok ? ms : -1.f;
+    }
+    cudaEventRecord(e0, st);
+    *parity = batch_run_direct(b, *parity, steps, st);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+}
+
 // Online autotuning: times candidate tile choices on real steps (coordinate search over
-// the core chunk scale, the shell chunk and the resident blocks per SM) and keeps the
-// fastest.  Returns the steps it ran and leaves the parity in *parity.
-int batch_autotune(FdtdBatch* b, int budget, int* parity, cudaStream_t st) {
+// the core chunk scale, the shell chunk and the resident blocks per SM, with direct
+// launches), then the best of them, the branch mode and the fused mode the way the call will
+// run them (under a CUDA graph when `graph`), and keeps the fastest.  Returns the steps it
+// ran and leaves the parity in *parity.
+int batch_autotune(FdtdBatch* b, int budget, int* parity, bool graph, cudaStream_t st) {
     const int per = b->any_hprev ? 4 : 3;  // timed steps per candidate (even with a parity twin)
+    const int warm = b->any_hprev ? 2 : 1;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     int used = 0;
-    auto trial = [&](int num, int den, int shell, int bps) -> float {
-        if (used + per + (b->any_hprev ? 2 : 1) > budget) return -1.f;
-        b->chunk_scale_num = num; b->chunk_scale_den = den; b->shell_chunk = shell; b->blocks_per_sm = bps;
-        if (batch_build_updates(b)) return -1.f;
-        const int warm = b->any_hprev ? 2 : 1;
+    auto fits = [&]() { return used + per + warm <= budget; };
+    auto run = [&](bool as_graph) -> float {
         *parity = batch_run_direct(b, *parity, warm, st);
-        cudaEventRecord(e0, st);
-        *parity = batch_run_direct(b, *parity, per, st);
-        cudaEventRecord(e1, st);
-        cudaEventSynchronize(e1);
+        const float ms = batch_time_steps(b, parity, per, as_graph, st, e0, e1);
         used += warm + per;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
         return ms;
     };
+    auto trial = [&](int num, int den, int shell, int bps) -> float {
+        if (!fits()) return -1.f;
+        b->chunk_scale_num = num; b->chunk_scale_den = den; b->shell_chunk = shell; b->blocks_per_sm = bps;
+        if (batch_build_updates(b)) return -1.f;
+        return run(false);
+    };
+    b->mode = 0;
     int best[4] = {1, 1, kShellChunk, 8};
     float best_ms = trial(best[0], best[1], best[2], best[3]);
     const int scales[][2] = {{1, 2}, {2, 1}, {4, 1}};
@@ -562,20 +666,26 @@ int batch_autotune(FdtdBatch* b, int budget, int* parity, cudaStream_t st) {
     }
     b->chunk_scale_num = best[0]; b->chunk_scale_den = best[1]; b->shell_chunk = best[2]; b->blocks_per_sm = best[3];
     batch_build_updates(b);
-    // the branch mode (each simulation's own kernels, overlapped across simulations)
-    const int warm = b->any_hprev ? 2 : 1;
-    if (used + warm + per <= budget && batch_branch_streams(b)) {
+    // the modes, each timed as the call runs it: 0 with the chosen tiles, 1 (each simulation's
+    // own kernels on its own stream), 2 (one cooperative launch for all the steps)
+    int dev = 0, coop = 0;
+    const bool can_fuse = cudaGetDevice(&dev) == cudaSuccess &&
+                          cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop;
+    float mode_ms[3] = {-1.f, -1.f, -1.f};
+    if (fits()) mode_ms[0] = graph ? run(true) : best_ms;
+    else mode_ms[0] = best_ms;
+    if (fits() && batch_branch_streams(b)) {
         b->mode = 1;
-        *parity = batch_run_direct(b, *parity, warm, st);
-        cudaEventRecord(e0, st);
-        *parity = batch_run_direct(b, *parity, per, st);
-        cudaEventRecord(e1, st);
-        cudaEventSynchronize(e1);
-        used += warm + per;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (!(ms > 0.f && (best_ms < 0.f || ms < best_ms))) b->mode = 0;
+        mode_ms[1] = run(graph);
     }
+    if (fits() && can_fuse) {
+        b->mode = 2;
+        mode_ms[2] = run(false);
+        if (b->fused_rc) mode_ms[2] = -1.f;
+    }
+    b->mode = 0;
+    for (int m = 1; m < 3; ++m)
+        if (mode_ms[m] > 0.f && (mode_ms[b->mode] <= 0.f || mode_ms[m] < mode_ms[b->mode])) b->mode = m;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     batch_drop_graph(b);
@@ -605,8 +715,8 @@ extern "C" int fdtd_batch_forward(FdtdBatch* b, const int32_t* t0, int32_t n_ste
         }
     if (n_steps == 0) return FDTD_OK;
     int parity = 0, done = 0;
-    if ((flags & 2) && !b->tuned) done += batch_autotune(b, n_steps / 4, &parity, st);
-    const bool use_graph = (flags & 1) != 0;
+    if ((flags & 2) && !b->tuned) done += batch_autotune(b, n_steps / 4, &parity, (flags & 1) != 0, st);
+    const bool use_graph = (flags & 1) != 0 && b->mode != 2;  // the fused mode is one launch already
     // one fixed graph length, so calls with different step counts reuse the same graph
     constexpr int G = 32;
     if (use_graph && n_steps - done >= G + 1) {
@@ -645,5 +755,22 @@ extern "C" int fdtd_batch_forward(FdtdBatch* b, const int32_t* t0, int32_t n_ste
     for (int s = 0; s < b->n; ++s) b->t[s] += n_steps;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+    if (b->fused_rc) {
+        const int rc = b->fused_rc;
+        b->fused_rc = 0;
+        return bfail(b, FDTD_ECUDA, std::string("fused batch launch: ") + cudaGetErrorString((cudaError_t)rc));
+    }
+    if (b->mode == 2) {  // read the barrier's error word (the call waits for its launch here)
+        int herr = 0;
+        e = cudaMemcpyAsync(&herr, b->ferr, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return bfail(b, FDTD_ECUDA, std::string("fused batch launch: ") + cudaGetErrorString(e));
+        if (herr) {
+            cudaMemsetAsync(b->ferr, 0, sizeof(int), st);
+            cudaMemsetAsync(b->fbar, 0, 2 * sizeof(unsigned), st);
+            cudaStreamSynchronize(st);
+            return bfail(b, herr, "fused batch launch: a grid barrier wait ran out (the steps of this call are incomplete)");
+        }
+    }
     return FDTD_OK;
 }

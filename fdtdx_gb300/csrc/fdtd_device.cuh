@@ -15,6 +15,20 @@
 
 #include "fdtd_gb300.h"
 
+// Loads of data that another block of the same launch may have written.  The per-phase
+// kernels are separate launches, so the read-only path (__ldg) and plain loads see every
+// earlier write.  A translation unit that runs several phases in one persistent launch (grid
+// barriers between them) defines FDTD_COHERENT_LOADS: the read-only path may then not be
+// used for anything the launch writes, and its loads are plain (weak) loads, which see the
+// other blocks' writes once the barrier's gpu-scope acquire fence has run.
+#ifdef FDTD_COHERENT_LOADS
+#define FDTD_LDG(p) (*(p))
+#define FDTD_LDC(p) (*(p))
+#else
+#define FDTD_LDG(p) __ldg(p)
+#define FDTD_LDC(p) (*(p))
+#endif
+
 namespace fdtd {
 
 struct DSlab {
@@ -140,7 +154,7 @@ __device__ __forceinline__ void bloch_turn(const Geo& g, int a, bool from_above,
 __device__ __forceinline__ float bloch_mix(const Geo& g, const float* __restrict__ f, long long off, float cr, float ci,
                                            float v) {
     if (ci == 0.f && cr == 1.f) return v;
-    return cr * v + g.psign * ci * __ldg(f + g.pother + off);
+    return cr * v + g.psign * ci * FDTD_LDG(f + g.pother + off);
 }
 
 __device__ __forceinline__ float ld_halo(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k) {
@@ -152,7 +166,7 @@ __device__ __forceinline__ float ld_halo(const Geo& g, const float* __restrict__
     if (k < 0) { if (!g.pz) return 0.f; k += g.nz; bloch_turn(g, 2, false, cr, ci); }
     else if (k >= g.nz) { if (!g.pz) return 0.f; k -= g.nz; bloch_turn(g, 2, true, cr, ci); }
     const long long off = comp * g.N + cell_index(g, i, j, k);
-    const float v = __ldg(f + off);
+    const float v = FDTD_LDG(f + off);
     return g.bloch ? bloch_mix(g, f, off, cr, ci, v) : v;
 }
 
@@ -166,7 +180,7 @@ __device__ __forceinline__ float ld_halo_sel(const Geo& g, const float* __restri
     const int jj = lj ? j + g.ny : (uj ? j - g.ny : j);
     const int kk = lk ? k + g.nz : (uk ? k - g.nz : k);
     const long long off = comp * g.N + cell_index(g, ok ? ii : 0, ok ? jj : 0, ok ? kk : 0);
-    const float v = __ldg(f + off);
+    const float v = FDTD_LDG(f + off);
     if (g.bloch && ok && (li || ui || lj || uj || lk || uk)) {
         float cr = 1.f, ci = 0.f;
         if (li || ui) bloch_turn(g, 0, ui, cr, ci);
@@ -187,13 +201,13 @@ __device__ __forceinline__ void tensor_at(const float* __restrict__ m, int n, fl
         t[0] = t[4] = t[8] = scalar;
     } else if (n == 9) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) t[q] = __ldg(m + q * N + c);
+        for (int q = 0; q < 9; ++q) t[q] = FDTD_LDG(m + q * N + c);
     } else if (n == 3) {
-        t[0] = __ldg(m + c);
-        t[4] = __ldg(m + N + c);
-        t[8] = __ldg(m + 2 * N + c);
+        t[0] = FDTD_LDG(m + c);
+        t[4] = FDTD_LDG(m + N + c);
+        t[8] = FDTD_LDG(m + 2 * N + c);
     } else {
-        t[0] = t[4] = t[8] = __ldg(m + c);
+        t[0] = t[4] = t[8] = FDTD_LDG(m + c);
     }
 }
 
@@ -248,8 +262,8 @@ __device__ __forceinline__ float profile_amp(const DSource& s, float tau, float 
 __device__ __forceinline__ float table_amp(const DSource& s, float tau) {
     if (!(tau >= 0.f) || tau > (float)(s.n_etab - 1)) return 0.f;
     const int i = (int)tau;
-    const float a = __ldg(s.etab + i);
-    const float b = i + 1 < s.n_etab ? __ldg(s.etab + i + 1) : a;
+    const float a = FDTD_LDG(s.etab + i);
+    const float b = i + 1 < s.n_etab ? FDTD_LDG(s.etab + i + 1) : a;
     return a + (tau - (float)i) * (b - a);
 }
 

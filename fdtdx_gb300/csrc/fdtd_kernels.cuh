@@ -61,7 +61,7 @@ __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k
         const float* co = sl.coef + (HSIDE ? 3 * sl.L : 0);
         float p1 = pr.v[s][0], p2 = pr.v[s][1];
         if (!REV) {
-            const float ca = __ldg(co + l), cb = __ldg(co + sl.L + l);
+            const float ca = FDTD_LDG(co + l), cb = FDTD_LDG(co + sl.L + l);
             p1 = cb * p1 + ca * d1;
             p2 = cb * p2 + ca * d2;
             const long long p = psi_offset(sl, i, j, k);
@@ -70,7 +70,7 @@ __device__ __forceinline__ void cpml_apply(const UpdArgs& a, int i, int j, int k
         }
         float c1 = p1, c2 = p2;
         if (!sl.kappa_one) {
-            const float ikm1 = __ldg(co + 2 * sl.L + l) - 1.f;
+            const float ikm1 = FDTD_LDG(co + 2 * sl.L + l) - 1.f;
             c1 = ikm1 * d1 + p1;
             c2 = ikm1 * d2 + p2;
         }
@@ -140,7 +140,7 @@ __device__ __forceinline__ void ax_term(const UpdArgs& a, int side, int l, int i
     const float* co = FDTD_AX_SEL(AX, side, coef) + (HSIDE ? 3 * L : 0);
     float p1 = pv.x, p2 = pv.y;
     if (!REV) {
-        const float ca = __ldg(co + l), cb = __ldg(co + L + l);
+        const float ca = FDTD_LDG(co + l), cb = FDTD_LDG(co + L + l);
         p1 = cb * p1 + ca * d1;
         p2 = cb * p2 + ca * d2;
         const int o = ax_off<AX>(FDTD_AX_SEL(AX, side, lo), FDTD_AX_SEL(AX, side, sy), FDTD_AX_SEL(AX, side, sz), i, j, k);
@@ -149,7 +149,7 @@ __device__ __forceinline__ void ax_term(const UpdArgs& a, int side, int l, int i
     }
     float c1 = p1, c2 = p2;
     if (!FDTD_AX_SEL(AX, side, kappa_one)) {
-        const float ikm1 = __ldg(co + 2 * L + l) - 1.f;
+        const float ikm1 = FDTD_LDG(co + 2 * L + l) - 1.f;
         c1 = ikm1 * d1 + p1;
         c2 = ikm1 * d2 + p2;
     }
@@ -163,7 +163,7 @@ __device__ __forceinline__ void ax_term(const UpdArgs& a, int side, int l, int i
 // Neighbour on one axis with the halo rule (wrap on a periodic axis, else zero).
 __device__ __forceinline__ float nb(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp, int i,
                                     int j, int k) {
-    return inside ? __ldg(f + off) : ld_halo(g, f, comp, i, j, k);
+    return inside ? FDTD_LDG(f + off) : ld_halo(g, f, comp, i, j, k);
 }
 
 // VEC consecutive z values (16/8/4-byte aligned: nz is a multiple of VEC).
@@ -176,13 +176,13 @@ template <int VEC>
 __device__ __forceinline__ Vec<VEC> ldv(const float* __restrict__ p) {
     Vec<VEC> r;
     if constexpr (VEC == 4) {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        const float4 q = FDTD_LDG(reinterpret_cast<const float4*>(p));
         r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
     } else if constexpr (VEC == 2) {
-        const float2 q = __ldg(reinterpret_cast<const float2*>(p));
+        const float2 q = FDTD_LDG(reinterpret_cast<const float2*>(p));
         r.v[0] = q.x; r.v[1] = q.y;
     } else {
-        r.v[0] = __ldg(p);
+        r.v[0] = FDTD_LDG(p);
     }
     return r;
 }
@@ -192,13 +192,13 @@ template <int VEC>
 __device__ __forceinline__ Vec<VEC> ldv_rw(const float* p) {
     Vec<VEC> r;
     if constexpr (VEC == 4) {
-        const float4 q = *reinterpret_cast<const float4*>(p);
+        const float4 q = FDTD_LDC(reinterpret_cast<const float4*>(p));
         r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
     } else if constexpr (VEC == 2) {
-        const float2 q = *reinterpret_cast<const float2*>(p);
+        const float2 q = FDTD_LDC(reinterpret_cast<const float2*>(p));
         r.v[0] = q.x; r.v[1] = q.y;
     } else {
-        r.v[0] = *p;
+        r.v[0] = FDTD_LDC(p);
     }
     return r;
 }
@@ -231,14 +231,14 @@ template <bool ZH>
 __device__ __forceinline__ float ld_halo_t(const Geo& g, const float* __restrict__ f, int comp, int i, int j, int k) {
     if (!ZH) return ld_halo(g, f, comp, i, j, k);
     const bool in = (unsigned)i < (unsigned)g.nx && (unsigned)j < (unsigned)g.ny && (unsigned)k < (unsigned)g.nz;
-    return in ? __ldg(f + comp * g.N + cell_index(g, i, j, k)) : 0.f;
+    return in ? FDTD_LDG(f + comp * g.N + cell_index(g, i, j, k)) : 0.f;
 }
 
 template <bool ZH>
 __device__ __forceinline__ float nb_t(const Geo& g, const float* __restrict__ f, long long off, bool inside, int comp,
                                       int i, int j, int k) {
     if (!ZH) return nb(g, f, off, inside, comp, i, j, k);
-    return inside ? __ldg(f + off) : 0.f;
+    return inside ? FDTD_LDG(f + off) : 0.f;
 }
 
 template <int VEC, bool ZH>
@@ -302,7 +302,7 @@ __device__ __forceinline__ float material_update(const UpdArgs& a, float u0, flo
                                                  long long so) {
     const Geo& g = a.g;
     if (sig_p) {
-        const float sg = __ldg(sig_p + so);
+        const float sg = FDTD_LDG(sig_p + so);
         const float q = HSIDE ? g.c * sg / g.eta0 * m / 2.f : g.c * sg * g.eta0 * m / 2.f;
         if (!HSIDE) {
             if (!REV) return ((1.f - q) * u0 + g.c * cu * m) / (1.f + q);
@@ -526,13 +526,13 @@ __device__ __forceinline__ void update_H_body(const UpdArgs& a, int blk) {
     for (int q = 0; q < kMaxFuse; ++q) {
         slot[q] = -1;
         if (REV || q >= a.n_fuse) continue;
-        const int t = *a.tp;
-        slot[q] = __ldg(a.fuse[q].slot + t + 1);
+        const int t = FDTD_LDC(a.tp);
+        slot[q] = FDTD_LDG(a.fuse[q].slot + t + 1);
         any |= slot[q] >= 0;
 #pragma unroll
         for (int f = 0; f < kMaxFuseFreq; ++f)
             w[q][f] = (slot[q] >= 0 && f < a.fuse[q].nfreq && a.fuse[q].kind == FDTD_DET_PHASOR)
-                          ? __ldg(a.fuse[q].w + (long long)(t + 1) * a.fuse[q].nfreq + f)
+                          ? FDTD_LDG(a.fuse[q].w + (long long)(t + 1) * a.fuse[q].nfreq + f)
                           : make_float2(0.f, 0.f);
     }
 
@@ -705,7 +705,7 @@ __device__ __forceinline__ float mat_at(const float* m, int n, float scalar, lon
     if (!m) return scalar;
     // an isotropic array serves every component; a full tensor's diagonal entry is comp * 4
     const int cc = n == 9 ? comp * 4 : (comp < n ? comp : n - 1);
-    return __ldg(m + cc * N + c);
+    return FDTD_LDG(m + cc * N + c);
 }
 
 template <bool ESIDE>
@@ -717,7 +717,7 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
         if (ESIDE == (bool)s.magnetic) return;
         const int i = s.lo[0], j = s.lo[1], k = s.lo[2];
         if (face_zero(g, wall, s.comp, i, j, k)) return;
-        const int ti = *tp + 1;
+        const int ti = FDTD_LDC(tp) + 1;
         if (!s.on[ti]) return;
         const float amp = profile_amp(s, s.teff[ti] + (ESIDE ? 0.f : 0.5f), ESIDE ? s.phE[ti] : s.phH[ti]);
         const float sg = inverse ? 1.f : -1.f;
@@ -741,10 +741,10 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
     // and the field is updated by atomic adds (no read of it; sources that overlap, which a
     // batched launch runs together, add up in any order), so the kernel waits on two memory
     // round trips instead of five
-    const float oa = __ldg(off + ax * P + f), ob = __ldg(off + bx * P + f);
-    const float ia = __ldg(inc + ax * P + f), ib = __ldg(inc + bx * P + f);
+    const float oa = FDTD_LDG(off + ax * P + f), ob = FDTD_LDG(off + bx * P + f);
+    const float ia = FDTD_LDG(inc + ax * P + f), ib = FDTD_LDG(inc + bx * P + f);
     const float ma = mat_at(mat, n_mat, mat_scalar, g.N, ax, c), mb = mat_at(mat, n_mat, mat_scalar, g.N, bx, c);
-    const int ti = *tp + 1;
+    const int ti = FDTD_LDC(tp) + 1;
     if (!s.on[ti]) return;
     const float teff = s.teff[ti] + (ESIDE ? 0.f : 0.5f);
     const float ph0 = ESIDE ? s.phE[ti] : s.phH[ti];
@@ -762,7 +762,7 @@ __device__ __forceinline__ void source_body(const Geo& g, const DSource& s, cons
         for (int q = 0; q < 3; ++q) {
             const int row = rows[q];
             if (face_zero(g, wall, row, i, j, k)) continue;
-            const float mra = __ldg(mat + (row * 3 + ax) * g.N + c), mrb = __ldg(mat + (row * 3 + bx) * g.N + c);
+            const float mra = FDTD_LDG(mat + (row * 3 + ax) * g.N + c), mrb = FDTD_LDG(mat + (row * 3 + bx) * g.N + c);
             const float corr = ESIDE ? mra * inc_b - mrb * inc_a : mrb * inc_a - mra * inc_b;
             atomicAdd(F + row * g.N + c, sg * (s.coef * corr));
         }
@@ -801,14 +801,14 @@ __global__ void __launch_bounds__(256) k_ade(const Geo g, float* __restrict__ E,
         const long long pi = ((long long)p * 3 + comp) * N + c;
         const long long ci = ((long long)p * nd + (nd == 3 ? comp : 0)) * N + c;
         const float pc = Pc[pi], pp = Pp[pi];
-        const float ph = __ldg(c1 + ci) * pc + __ldg(c2 + ci) * pp + __ldg(c3 + ci) * e;
+        const float ph = FDTD_LDG(c1 + ci) * pc + FDTD_LDG(c2 + ci) * pp + FDTD_LDG(c3 + ci) * e;
         delta += pc - ph;
         Pp[pi] = pc;
         Pc[pi] = ph;
     }
-    const float m = __ldg(inv_eps + (n_eps == 3 ? comp : 0) * N + c);
+    const float m = FDTD_LDG(inv_eps + (n_eps == 3 ? comp : 0) * N + c);
     float add = m * delta;
-    if (sig) add /= 1.f - g.c * __ldg(sig + (n_sig == 3 ? comp : 0) * N + c) * g.eta0 * m / 2.f;
+    if (sig) add /= 1.f - g.c * FDTD_LDG(sig + (n_sig == 3 ? comp : 0) * N + c) * g.eta0 * m / 2.f;
     E[idx] = e + add;
 }
 
@@ -844,8 +844,8 @@ __device__ void colocate(const Geo& g, const DetFields& f, int exact, int mask, 
     if (!exact) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            v[q] = (mask >> q & 1) ? __ldg(f.E + q * g.N + c) : 0.f;
-            v[3 + q] = (mask >> (3 + q) & 1) ? __ldg(f.H + q * g.N + c) : 0.f;
+            v[q] = (mask >> q & 1) ? FDTD_LDG(f.E + q * g.N + c) : 0.f;
+            v[3 + q] = (mask >> (3 + q) & 1) ? FDTD_LDG(f.H + q * g.N + c) : 0.f;
         }
         return;
     }
@@ -859,7 +859,7 @@ __device__ void colocate(const Geo& g, const DetFields& f, int exact, int mask, 
         const float up = 0.5f * (ld_halo_sel(g, f.E, 1, i, j, k + 1) + ld_halo_sel(g, f.E, 1, i, j - 1, k + 1));
         v[1] = (lo + up) / 2.f;
     }
-    if (mask & 4) v[2] = __ldg(f.E + 2 * g.N + c);
+    if (mask & 4) v[2] = FDTD_LDG(f.E + 2 * g.N + c);
     if (mask & 8) v[3] = 0.5f * (hav(g, f, 0, i, j, k) + hav(g, f, 0, i, j - 1, k));
     if (mask & 16) v[4] = 0.5f * (hav(g, f, 1, i, j, k) + hav(g, f, 1, i - 1, j, k));
     if (mask & 32) {
@@ -922,8 +922,8 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
             colocate(gi, fi, d.exact, need, i, j, k, vi);
         }
     }
-    const int t = *tp;
-    const int slot = __ldg(d.slot + t + 1);
+    const int t = FDTD_LDC(tp);
+    const int slot = FDTD_LDG(d.slot + t + 1);
     if (slot < 0) return;
 
     // gather the recorded values of this cell (outi: the imaginary parts of complex phasor
@@ -993,7 +993,7 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
             if (!valid) return;
             float2* st = reinterpret_cast<float2*>(state);
             for (int fq = 0; fq < d.nfreq; ++fq) {
-                const float2 w = __ldg(wt + fq);
+                const float2 w = FDTD_LDG(wt + fq);
                 for (int q = 0; q < nout; ++q) {
                     float2* p = st + ((long long)fq * nout + q) * d.R + r;
                     float2 z = *p;
@@ -1009,7 +1009,7 @@ __device__ __forceinline__ void detector_body(const Geo& g, const DDet& d, const
         }
         // volume mean of the complex samples: partials (2 floats per freq and component)
         for (int fq = 0; fq < d.nfreq; ++fq) {
-            const float2 w = __ldg(wt + fq);
+            const float2 w = FDTD_LDG(wt + fq);
             for (int q = 0; q < nout; ++q) {
                 const float ar = f.im ? out[q] * w.x - outi[q] * w.y : out[q] * w.x;
                 const float ai = f.im ? out[q] * w.y + outi[q] * w.x : out[q] * w.y;
@@ -1044,12 +1044,12 @@ __global__ void __launch_bounds__(kDetBlock) k_detector(const Geo g, const DDet 
 // and writes (field, flux, energy) or accumulates (phasor) the state entry.
 __device__ __forceinline__ void detector_finalize_body(const DDet& d, const int* __restrict__ tp, void* state) {
     __shared__ float sh[kDetBlock / 32];
-    const int t = *tp;
-    const int slot = __ldg(d.slot + t + 1);
+    const int t = FDTD_LDC(tp);
+    const int slot = FDTD_LDG(d.slot + t + 1);
     if (slot < 0) return;
     for (int q = 0; q < d.ncomp; ++q) {
         float acc = 0.f;
-        for (int b = threadIdx.x; b < d.nblocks; b += blockDim.x) acc += d.partial[(long long)b * d.ncomp + q];
+        for (int b = threadIdx.x; b < d.nblocks; b += blockDim.x) acc += FDTD_LDC(d.partial + (long long)b * d.ncomp + q);
         const float s = block_sum<kDetBlock>(acc, sh);
         if (threadIdx.x == 0) {
             if (d.kind == FDTD_DET_PHASOR) {
@@ -1106,20 +1106,20 @@ __device__ __forceinline__ void interfaces_body(const Geo& g, const IfaceDev& if
     if (!RESTORE) {
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp) {
-            v[comp] = E[comp * g.N + c];
-            v[3 + comp] = H[comp * g.N + c];
+            v[comp] = FDTD_LDC(E + comp * g.N + c);
+            v[3 + comp] = FDTD_LDC(H + comp * g.N + c);
         }
     }
-    int t = *tp, tb = t;
+    int t = FDTD_LDC(tp), tb = t;
     float w = 0.f;
     if (ifc.store) {  // time filter: store every k-th step, restore by linear interpolation
         const int ti = t + 1;
         if (RESTORE) {
-            tb = __ldg(ifc.rb + ti);
-            w = __ldg(ifc.rw + ti);
-            t = __ldg(ifc.ra + ti);
+            tb = FDTD_LDG(ifc.rb + ti);
+            w = FDTD_LDG(ifc.rw + ti);
+            t = FDTD_LDG(ifc.ra + ti);
         } else {
-            t = tb = __ldg(ifc.store + ti);
+            t = tb = FDTD_LDG(ifc.store + ti);
             if (t < 0) return;
         }
     } else {
@@ -1161,7 +1161,7 @@ __global__ void __launch_bounds__(256) k_check_finite(const float* __restrict__ 
     bool bad = false;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
-        bad |= !isfinite(__ldg(f + q));
+        bad |= !isfinite(FDTD_LDG(f + q));
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(err, FDTD_ENONFINITE);
 }
 

@@ -102,6 +102,7 @@ struct NvtxRange {
 // Injected failures still to deliver (fdtd_debug_inject): process-wide counters.
 std::atomic<int> g_inject_alloc{0};
 std::atomic<int> g_inject_expiry{0};
+std::atomic<int> g_inject_barrier{0};
 
 bool take_injected(std::atomic<int>& counter) {
     int v = counter.load();
@@ -1489,6 +1490,7 @@ extern "C" int fdtd_debug_inject(int32_t kind, int32_t count) {
     if (count < 0) return FDTD_EINVAL;
     if (kind == FDTD_INJECT_ALLOC) g_inject_alloc.store(count);
     else if (kind == FDTD_INJECT_WAIT_EXPIRY) g_inject_expiry.store(count);
+    else if (kind == FDTD_INJECT_BARRIER_EXPIRY) g_inject_barrier.store(count);
     else return FDTD_EINVAL;
     return FDTD_OK;
 }

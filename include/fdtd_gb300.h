@@ -302,10 +302,15 @@ int fdtd_plan_status(FdtdPlan* plan);
  *   FDTD_INJECT_WAIT_EXPIRY  the next `count` TMA half-step launches issued outside stream
  *                            capture take their bounded-wait error exit before issuing any
  *                            copy: they update nothing, and the plan's next fdtd_plan_status
- *                            returns FDTD_ETIMEOUT.
+ *                            returns FDTD_ETIMEOUT;
+ *   FDTD_INJECT_BARRIER_EXPIRY the next `count` fused batch launches (fdtd_batch_set_mode 2)
+ *                            run with one block that never arrives at the first grid barrier
+ *                            and a short wait limit: the other blocks' waits run out and the
+ *                            fdtd_batch_forward call returns FDTD_ETIMEOUT.
  * count = 0 clears a kind.  Process-wide; returns FDTD_EINVAL for an unknown kind. */
 #define FDTD_INJECT_ALLOC 1
 #define FDTD_INJECT_WAIT_EXPIRY 2
+#define FDTD_INJECT_BARRIER_EXPIRY 3
 int fdtd_debug_inject(int32_t kind, int32_t count);
 
 /* Number of launches of this library's kernels one forward step issues. */
@@ -345,11 +350,15 @@ int fdtd_batch_tune(FdtdBatch* batch, int32_t chunk_num, int32_t chunk_den, int3
 int fdtd_batch_tuning(const FdtdBatch* batch, int32_t* out4);
 /* Execution mode: 0 = persistent launches over the unit lists (default), 1 = each
  * simulation's own per-plan launch chain on its own stream, forked from and joined to the
- * caller's stream (parallel branches of one CUDA graph).  The autotuner (fdtd_batch_forward
- * flag bit 1) times both and keeps the faster. */
+ * caller's stream (parallel branches of one CUDA graph), 2 = every step of a
+ * fdtd_batch_forward call in ONE cooperative launch, the phases of a step separated by a
+ * grid-wide barrier whose waits are bounded (an expired wait makes the call return
+ * FDTD_ETIMEOUT); in mode 2 fdtd_batch_forward waits for its launch before it returns.
+ * The autotuner (fdtd_batch_forward flag bit 1) times the modes and keeps the fastest. */
 int fdtd_batch_set_mode(FdtdBatch* batch, int32_t mode);
 int32_t fdtd_batch_mode(const FdtdBatch* batch);
-/* Launches of this library's kernels one batch step issues (for the whole batch). */
+/* Launches of this library's kernels one batch step issues (for the whole batch; 1 in
+ * mode 2, where one launch runs all the steps of a call). */
 int32_t fdtd_batch_launches_per_step(const FdtdBatch* batch);
 
 /* Allocation-free sample of one volume-reducing detector (no counterpart in the

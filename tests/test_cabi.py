@@ -137,3 +137,4 @@ def test_debug_inject_rejects_unknown_kinds(lib):
     assert lib.fdtd_debug_inject(N.INJECT_ALLOC, -1) == N.EINVAL
     assert lib.fdtd_debug_inject(N.INJECT_ALLOC, 0) == N.OK
     assert lib.fdtd_debug_inject(N.INJECT_WAIT_EXPIRY, 0) == N.OK
+    assert lib.fdtd_debug_inject(N.INJECT_BARRIER_EXPIRY, 0) == N.OK

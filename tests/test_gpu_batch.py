@@ -89,7 +89,7 @@ def test_batch_matches_single_runs(graph, autotune):
     if autotune:
         t = batch.tuning()
         assert t["shell_chunk"] in (2, 4, 8) and t["blocks_per_sm"] in (4, 8, 16)
-        assert t["mode"] in ("persistent", "branches")
+        assert t["mode"] in ("persistent", "branches", "fused")
     else:
         assert batch.launches_per_step() <= 13
     batch.close()
@@ -109,6 +109,72 @@ def test_batch_branch_mode_matches_single_runs(graph):
         for k, v in _states(batch.arrays[q]).items():
             assert torch.equal(v, _states(ref)[k]), (q, k)
     batch.close()
+
+
+def test_batch_fused_mode_matches_persistent_mode_and_oracle():
+    """Mode 'fused': every step of a call in ONE cooperative launch, the phases separated by
+    bounded grid barriers.  The same device bodies as the persistent mode, so each simulation
+    matches the persistent-mode batch (relative L2 <= 1e-6: detector sums may add in another
+    order) and the single runs (<= 1e-5); two calls (an odd first chunk, so the parity twin
+    is handed back) against the float32 / float64 oracle (<= 1e-4)."""
+    sims = _sims()
+    n = len(sims)
+    ref = SimulationBatch(sims)
+    ref.advance(STEPS, t0=[0] * n, graph=False, autotune=False)
+    fused = SimulationBatch(sims)
+    fused.set_mode("fused")
+    assert fused.mode == "fused" and fused.launches_per_step() == 1
+    fused.advance(23, t0=[0] * n, graph=True, autotune=False)
+    fused.advance(STEPS - 23, graph=True, autotune=False)
+    torch.cuda.synchronize()
+    for q, (arrays, objects, config) in enumerate(sims):
+        got, want = _states(fused.arrays[q]), _states(ref.arrays[q])
+        errs = {k: rel_l2(v, want[k]) for k, v in got.items()}
+        log_result(f"batch_fused_vs_persistent_{q}", **errs)
+        for k, e in errs.items():
+            assert e <= 1e-6, (q, k, e)
+        alone = _states(_alone(arrays, objects, config, STEPS))
+        for k, v in got.items():
+            assert rel_l2(v, alone[k]) <= 1e-5, (q, k)
+    for q in range(2):
+        arrays, objects, config = sims[q]
+        sc32 = O.OracleScene(objects, arrays, config, torch.float32)
+        sc64 = O.OracleScene(objects, arrays, config, torch.float64)
+        compare_states(f"batch_fused_oracle_{q}", fused.arrays[q], O.run(sc32, STEPS), O.run(sc64, STEPS), 1e-4)
+    ref.close()
+    fused.close()
+
+
+def test_batch_fused_mode_barrier_expiry_is_reported_and_the_batch_stays_usable():
+    """An injected block that never arrives at the first grid barrier: the other blocks' bounded
+    waits run out, the call raises FDTD_ETIMEOUT, and the next call runs normally."""
+    from fdtdx_gb300 import _native as N
+
+    sims = _sims()[:2]
+    ref = SimulationBatch(sims)
+    ref.set_mode("fused")
+    ref.advance(20, t0=[0, 0], graph=False, autotune=False)
+    torch.cuda.synchronize()
+    b = SimulationBatch(sims)
+    b.set_mode("fused")
+    assert N.load().fdtd_debug_inject(N.INJECT_BARRIER_EXPIRY, 1) == N.OK
+    with pytest.raises(N.NativeError) as ei:
+        b.advance(10, t0=[0, 0], graph=False, autotune=False)
+    assert ei.value.code == N.ETIMEOUT
+    for a in b.arrays:  # back to step 0 in place (the batch holds these tensors)
+        for v in [a.fields.E, a.fields.H, *[x for pair in (*a.fields.psi_E.values(), *a.fields.psi_H.values())
+                                              for x in pair]]:
+            v.zero_()
+        for st in a.detector_states.values():
+            for v in st.values():
+                v.zero_()
+    b.advance(20, t0=[0, 0], graph=False, autotune=False)
+    torch.cuda.synchronize()
+    for q in range(2):
+        for k, v in _states(b.arrays[q]).items():
+            assert torch.allclose(v, _states(ref.arrays[q])[k], rtol=1e-6, atol=0), (q, k)
+    ref.close()
+    b.close()
 
 
 def test_batch_against_oracle_and_continuation():
