@@ -517,6 +517,28 @@ def bench_batch(dev, n_sims: int = 64, steps: int = 2000) -> dict:
     return out
 
 
+def bench_batch_modes(dev, n_sims: int = 32, steps: int = 6) -> dict:
+    """Profiling case of the batch execution modes on small strips (32..96 per axis, 8-cell
+    CPML), direct launches: per mode a 2-step warm-up call, then one timed call of ``steps``
+    steps.  The fused mode runs first, so its timed call is the second k_batch_fused launch and
+    the persistent mode's k_batch_update launches follow it."""
+    from fdtdx_gb300.batch import SimulationBatch
+
+    sims, cells = _strip_sims(n_sims, steps + 2, dev, seed=1, lo=(32, 32, 32), hi=(96, 96, 96), pml=8)
+    b = SimulationBatch(sims)
+    out = {"workload": f"{n_sims} small Si strips, seeded grids 32-96 per axis @25nm, 8-cell CPML", "cells": cells}
+    for mode in ("fused", "persistent", "branches"):
+        b.set_mode(mode)
+        b.advance(2, t0=[0] * n_sims, graph=False, autotune=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.advance(steps, graph=False, autotune=False)
+        torch.cuda.synchronize()
+        out[mode] = {"steps": steps, "ms": round((time.perf_counter() - t0) * 1e3, 3)}
+    b.close()
+    return out
+
+
 def bench_serving(capacity: float, n_jobs: int = 200, seed: int = 0, load: float = 1.5) -> dict:
     """Poisson stream: grids log-uniform in [32,384]x[32,384]x[32,192] @50 nm, steps uniform
     in [500, 10000], 70% forward / 30% forward+gradient, random boxes (20% diagonal-
@@ -681,7 +703,7 @@ def main():
     ap.add_argument("--batch-sims", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2000)
     ap.add_argument("--serve-jobs", type=int, default=200)
-    ap.add_argument("--case", default="all", choices=["all", "gradient", "batch", "serving"],
+    ap.add_argument("--case", default="all", choices=["all", "gradient", "batch", "batch-modes", "serving"],
                     help="run one secondary measurement alone and print its record (profiling)")
     ap.add_argument("--grad-steps", type=int, default=3000, help="steps of the gradient case (profiling: fewer)")
     args = ap.parse_args()
@@ -696,6 +718,8 @@ def main():
             out = bench_gradient(dev, args.grad_steps)
         elif args.case == "batch":
             out = bench_batch(dev, args.batch_sims, args.batch_steps)
+        elif args.case == "batch-modes":
+            out = bench_batch_modes(dev, args.batch_sims, args.batch_steps)
         else:
             out = bench_serving(2.0e10, args.serve_jobs)
         print(json.dumps({"case": args.case, **out}))
