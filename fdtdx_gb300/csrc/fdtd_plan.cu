@@ -7,12 +7,14 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "fdtd_kernels.cuh"
 #include "fdtd_aniso.cuh"
 #include "fdtd_adjoint.cuh"
 #include "fdtd_tma.cuh"
+#include "fdtd_split.cuh"
 
 #include <cudaTypedefs.h>
 #include <nvtx3/nvToolsExt.h>
@@ -56,9 +58,15 @@ struct FdtdPlan {
     // mode 1 widens the core to the whole x and y extent (the x and y slab terms in the PML
     // kernels) and leaves the two z boxes to the register-queue shell kernel; mode 2 runs the
     // whole grid in one PML launch per half-step (z terms too); mode 0 runs all six slab boxes
-    // on the shell kernel
-    int shell_tma = 0;                    // requested mode
+    // on the shell kernel; mode 3 (the default where admitted; forward steps) runs the plain
+    // TMA kernels over the whole grid and then the slab cells' corrections (fdtd_split.cuh):
+    // 0.906 against 0.941 ms per step on the 400 x 400 x 200 coupler
+    int shell_tma = 3;                    // requested mode
     bool m1_ok = false, m2_ok = false;    // admissible
+    // mode 3 (forward steps): the plain TMA kernels over the whole grid (m2_tz tile), then the
+    // CPML corrections of the slab cells (fdtd_split.cuh), one launch per axis
+    bool m3_ok = false;
+    int m3_chunk = 1, m3_chunk_e = 1;
     int m1_chunk = 1, m1_chunk_e = 1;     // x planes per block (H, E), mode 1
     int m2_tz = 0;                        // z extent of the mode-2 tile (the core's ty rows)
     int m2_chunk = 1, m2_chunk_e = 1;
@@ -400,7 +408,7 @@ int staged_planes(const FdtdPlan* p) {
 // the PML kernels over the whole grid, with the z extent of their tile picked for nz.  x
 // chunks of about ten (E) and six (H) waves of resident blocks, as for the core.
 void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
-    p->m1_ok = p->m2_ok = false;
+    p->m1_ok = p->m2_ok = p->m3_ok = false;
     if (!sp.split || p->d.n_slabs == 0) return;
     // one slab per face (the per-axis table) and 32-bit psi offsets
     int faces[3] = {0, 0, 0};
@@ -450,6 +458,29 @@ void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
             p->m2_chunk = chunk_for(6, oh, tiles, nx);
             p->m2_ok = true;
         }
+        // mode 3: the plain kernels on the same whole-grid tile; real, non-dispersive fields
+        // and, per axis, two disjoint slabs (the corrections of an axis run in one launch)
+        bool disjoint = true;
+        for (int x = 0; x < 3; ++x) {
+            int lo = -1, hi = -1, llo = 0;
+            for (int s = 0; s < p->d.n_slabs; ++s) {
+                const DSlab& sl = p->slab[s];
+                if (sl.axis != x) continue;
+                if (p->d.slabs[s].direction > 0) hi = sl.lo;
+                else { lo = sl.lo; llo = sl.L; }
+            }
+            if (lo >= 0 && hi >= 0 && lo + llo > hi) disjoint = false;
+        }
+        const size_t smE = tma_smem(tma_cfg(tz2, ty, p->tma_ns, false, p->d.n_eps, p->d.n_sigma_E, nullptr));
+        const size_t smH = tma_smem(tma_cfg(tz2, ty, p->tma_ns, true, p->d.n_mu, p->d.n_sigma_H, nullptr, staged_planes(p)));
+        const int pe = occ_of((const void*)k_tma_E<false, false>, ty * tz2 / 2, smE);
+        const int ph = occ_of((const void*)k_tma_H<false, false>, ty * tz2 / 2, smH);
+        if (disjoint && pe > 0 && ph > 0 && p->parts == 1 && p->d.n_poles == 0 && !p->full_e && !p->full_h) {
+            const long long tiles = (long long)((nz + tz2 - 1) / tz2) * ((ny + ty - 1) / ty);
+            p->m3_chunk_e = chunk_for(10, pe, tiles, nx);
+            p->m3_chunk = chunk_for(6, ph, tiles, nx);
+            p->m3_ok = p->m2_ok;
+        }
     }
     cudaGetLastError();
 }
@@ -457,6 +488,7 @@ void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
 // The shell mode the launches use: the requested one, lowered to what the scene admits.
 int shell_tma_mode(const FdtdPlan* p) {
     if (!p->use_tma) return 0;
+    if (p->shell_tma == 3 && p->m3_ok) return 3;
     if (p->shell_tma == 2 && p->m2_ok) return 2;
     if (p->shell_tma == 1 && p->m1_ok) return 1;
     return 0;
@@ -908,6 +940,22 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
     }
 }
 
+// The CPML corrections of a split forward half-step: one launch per axis holding slabs (both
+// faces in one grid, blockIdx.y the face), in x, y, z order.
+template <bool HSIDE>
+void launch_pml_corr(const UpdArgs& a, cudaStream_t st) {
+    auto run = [&](auto ax_tag) {
+        constexpr int AX = decltype(ax_tag)::value;
+        const long long n0 = (long long)a.axs[AX][0].sx * a.axs[AX][0].sy * a.axs[AX][0].sz * (a.axs[AX][0].L > 0);
+        const long long n1 = (long long)a.axs[AX][1].sx * a.axs[AX][1].sy * a.axs[AX][1].sz * (a.axs[AX][1].L > 0);
+        const long long n = std::max(n0, n1);
+        if (n > 0) k_pml_corr<HSIDE, AX><<<dim3((unsigned)((n + 255) / 256), 2), 256, 0, st>>>(a);
+    };
+    run(std::integral_constant<int, 0>{});
+    run(std::integral_constant<int, 1>{});
+    run(std::integral_constant<int, 2>{});
+}
+
 // `mid` (optional) is recorded between the core and the shell launches (profiling).
 template <bool REV, bool HSIDE>
 void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent_t mid = nullptr) {
@@ -919,6 +967,16 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
         return;
     }
     const int mode = a.axt == 2 ? shell_tma_mode(p) : 0;
+    if (mode == 3 && !REV) {
+        // the plain update of every cell in one TMA launch, then the slab cells' CPML terms
+        UpdArgs ax = a;
+        for (int x = 0; x < 3; ++x) { ax.lo[x] = 0; ax.hi[x] = x == 0 ? p->g.nx : x == 1 ? p->g.ny : p->g.nz; }
+        if (launch_tma<REV, HSIDE, false>(p, ax, st, p->m2_tz, HSIDE ? p->m3_chunk : p->m3_chunk_e)) {
+            if (mid) cudaEventRecord(mid, st);
+            launch_pml_corr<HSIDE>(a, st);
+            return;
+        }
+    }
     if (mode == 2) {
         // the whole grid in one launch of the PML kernels (every slab term in the tiles)
         UpdArgs ax = a;
@@ -960,6 +1018,15 @@ int half_step_launches(const FdtdPlan* p) {
     const Split sp = split_boxes(p);
     if (!sp.split) return 1;
     const int mode = shell_tma_mode(p);
+    if (mode == 3) {  // forward steps: the plain launch and one correction launch per slab axis
+        int axes = 0;
+        for (int x = 0; x < 3; ++x) {
+            bool any = false;
+            for (int s = 0; s < p->d.n_slabs; ++s) any = any || p->slab[s].axis == x;
+            axes += any;
+        }
+        return 1 + axes;
+    }
     if (mode == 2) return 1;
     if (mode == 1) return 1 + ((sp.core.lo[2] > 0 || sp.core.hi[2] < p->g.nz) ? 1 : 0);
     return 1 + (sp.n_shell > 0);
@@ -1451,8 +1518,8 @@ extern "C" int32_t fdtd_plan_uses_tma(const FdtdPlan* p) { return p && p->use_tm
 
 extern "C" int fdtd_plan_tune_shell_tma(FdtdPlan* p, int32_t mode, int32_t tz, int32_t chunk) {
     if (!p) return FDTD_EINVAL;
-    if (mode < 0 || mode > 2 || tz < 0 || tz % 4 || tz > 120 || chunk < 0)
-        return fail(p, FDTD_EINVAL, "invalid slab-cell mode (0, 1 or 2) or tile (tz a multiple of 4, <= 120)");
+    if (mode < 0 || mode > 3 || tz < 0 || tz % 4 || tz > 120 || chunk < 0)
+        return fail(p, FDTD_EINVAL, "invalid slab-cell mode (0 to 3) or tile (tz a multiple of 4, <= 120)");
     p->shell_tma = mode;
     p->m2_tz = tz;
     configure_tma(p);
@@ -1464,6 +1531,7 @@ extern "C" int fdtd_plan_tune_shell_tma(FdtdPlan* p, int32_t mode, int32_t tz, i
     if (chunk > 0) {
         if (mode == 1) p->m1_chunk = p->m1_chunk_e = std::min(chunk, p->g.nx);
         if (mode == 2) p->m2_chunk = p->m2_chunk_e = std::min(chunk, p->g.nx);
+        if (mode == 3) p->m3_chunk = p->m3_chunk_e = std::min(chunk, p->g.nx);
     }
     drop_graphs(p);
     return FDTD_OK;

@@ -629,7 +629,9 @@ class Scene:
     def tune_shell_tma(self, mode: int = 2, tz: int = 0, chunk: int = 0) -> None:
         """Where the CPML slab cells run with a TMA core: 0 the register-queue shell kernel, 1 the
         x and y slabs in the TMA kernels (z boxes on the shell kernel), 2 the whole grid in one
-        TMA launch (tile z extent ``tz``, 0: picked for nz)."""
+        TMA launch (tile z extent ``tz``, 0: picked for nz), 3 split: the plain TMA kernels over
+        the whole grid, then the slab cells' CPML corrections, one launch per axis (forward
+        steps; reverse steps run mode 0)."""
         N.check(N.load().fdtd_plan_tune_shell_tma(self.plan, int(mode), int(tz), int(chunk)), self.plan,
                 "fdtd_plan_tune_shell_tma")
 

@@ -284,8 +284,11 @@ int32_t fdtd_plan_uses_tma(const FdtdPlan* plan);
  * core runs on the TMA kernels: mode 0, the register-queue shell kernel over the six slab
  * boxes; mode 1, the TMA kernels with in-tile slab terms over the whole x and y extent (the x
  * and y slabs) and the shell kernel over the two z boxes; mode 2, the whole grid in one launch
- * of the TMA kernels with every slab term in the tiles (tile z extent `tz`, 0: picked for nz).
- * `chunk` x planes per block (0: a default).  fdtd_plan_shell_tma returns the mode in use. */
+ * of the TMA kernels with every slab term in the tiles (tile z extent `tz`, 0: picked for nz);
+ * mode 3 (split, forward steps; reverse steps run mode 0), the plain TMA kernels over the
+ * whole grid on the mode-2 tile, then the CPML corrections of the slab cells, one launch per
+ * axis.  `chunk` x planes per block (0: a default).  fdtd_plan_shell_tma returns the mode in
+ * use. */
 int fdtd_plan_tune_shell_tma(FdtdPlan* plan, int32_t mode, int32_t tz, int32_t chunk);
 int32_t fdtd_plan_shell_tma(const FdtdPlan* plan);
 

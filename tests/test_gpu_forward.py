@@ -260,7 +260,10 @@ def test_shell_tiling_variants_agree():
 @pytest.mark.parametrize("tile", [(0, 0, 0, 0), (16, 8, 2, 3), (24, 4, 3, 7), (64, 8, 6, 0)])
 def test_tma_kernels_match_register_kernels(tile):
     """The TMA-pipelined half-steps agree with the register-queue half-steps (every tile shape,
-    partial tiles in y and z, chunked x, CPML, conductivity, fused detectors)."""
+    partial tiles in y and z, chunked x, CPML, conductivity, fused detectors): the TMA core with
+    the register-queue shell (slab mode 0, rounding-close) and the split form (mode 3: the plain
+    TMA kernels over the whole grid, then the slab corrections; a rounding apart per step, which
+    psi integrates: measured 1.2e-6 after 50 steps)."""
     tz, ty, ns, chunk = tile
     cfg = _cfg(50)
     vol = fx.SimulationVolume(shape=(30, 27, 44))
@@ -275,29 +278,33 @@ def test_tma_kernels_match_register_kernels(tile):
                                   wave_characters=(fx.WaveCharacter(wavelength=1.55e-6),), components=("Ex", "Ey", "Ez")))
     objs.append(fx.FieldDetector(name="ez", grid_slice_tuple=((0, 30), (0, 27), (20, 21)), components=("Ez", "Ey")))
     objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
-    outs = []
-    for tma in (True, False):
+    outs = {}
+    for run in ("register", 0, 3):
         a = arrays.reset()
         s = Scene(objects, a, cfg)
-        if tma:
-            s.tune_tma(True, tz, ty, ns, chunk)
-            assert s.uses_tma
-        else:
+        if run == "register":
             s.tune_tma(False)
+        else:
+            s.tune_tma(True, tz, ty, ns, chunk)
+            s.tune_shell_tma(run)
+            assert s.uses_tma and s.shell_tma == run
         s.forward(a, 0, 50)
         s.status()
         torch.cuda.synchronize()
-        outs.append(a)
+        outs[run] = a
         s.close()
-    for k in ("E", "H"):
-        assert rel_l2(getattr(outs[0].fields, k), getattr(outs[1].fields, k)) < 1e-6
-    for dn in ("ph", "ez"):
-        for kk, v in outs[0].detector_states[dn].items():
-            assert rel_l2(v, outs[1].detector_states[dn][kk]) < 1e-6
-    for n in outs[0].fields.psi_E:
-        for q in range(2):
-            assert rel_l2(outs[0].fields.psi_E[n][q], outs[1].fields.psi_E[n][q]) < 1e-6
-            assert rel_l2(outs[0].fields.psi_H[n][q], outs[1].fields.psi_H[n][q]) < 1e-6
+    ref = outs["register"]
+    for run, tol, tol_psi in ((0, 1e-6, 1e-6), (3, 2e-6, 5e-6)):
+        got = outs[run]
+        for k in ("E", "H"):
+            assert rel_l2(getattr(got.fields, k), getattr(ref.fields, k)) < tol, (run, k)
+        for dn in ("ph", "ez"):
+            for kk, v in got.detector_states[dn].items():
+                assert rel_l2(v, ref.detector_states[dn][kk]) < tol, (run, dn)
+        for n in got.fields.psi_E:
+            for q in range(2):
+                assert rel_l2(got.fields.psi_E[n][q], ref.fields.psi_E[n][q]) < tol_psi, (run, n)
+                assert rel_l2(got.fields.psi_H[n][q], ref.fields.psi_H[n][q]) < tol_psi, (run, n)
 
 
 def test_plans_of_different_tile_memory_coexist():
@@ -319,13 +326,14 @@ def test_plans_of_different_tile_memory_coexist():
     assert s1.uses_tma
 
 
-@pytest.mark.parametrize("mode,tz,chunk", [(1, 0, 0), (2, 0, 0), (2, 20, 3)])
+@pytest.mark.parametrize("mode,tz,chunk", [(1, 0, 0), (2, 0, 0), (2, 20, 3), (3, 0, 0), (3, 20, 5)])
 def test_shell_tma_matches_register_shell(mode, tz, chunk):
     """The CPML slab cells on the TMA kernels with in-tile slab terms (mode 1: the x and y
-    slabs, the core widened over them; mode 2: the whole grid in one launch) against the
-    register-queue shell kernel: forward steps with kappa != 1, a conductor and a dipole inside
-    the slabs and a fused full-volume phasor, then time-reversed steps with the recorded
-    interfaces (psi frozen)."""
+    slabs, the core widened over them; mode 2: the whole grid in one launch), or split (mode 3:
+    the plain TMA kernels over the whole grid, then the slab cells' CPML corrections per axis)
+    against the register-queue shell kernel: forward steps with kappa != 1, a conductor and a
+    dipole inside the slabs and a fused full-volume phasor, then time-reversed steps with the
+    recorded interfaces (psi frozen)."""
     cfg = _cfg(60, record=True)
     vol = fx.SimulationVolume(shape=(30, 27, 44))
     bc = fx.BoundaryConfig.from_uniform_bound(6, "pml", kappa_end=1.8)
@@ -346,7 +354,7 @@ def test_shell_tma_matches_register_shell(mode, tz, chunk):
     for m in (mode, 0):
         a = arrays.reset()
         s = Scene(objects, a, cfg, record_interfaces=True)
-        s.tune_shell_tma(m, tz if m == 2 else 0, chunk if m else 0)
+        s.tune_shell_tma(m, tz if m in (2, 3) else 0, chunk if m else 0)
         assert s.uses_tma and s.shell_tma == m
         s.forward(a, 0, 60)
         s.status()
@@ -358,5 +366,15 @@ def test_shell_tma_matches_register_shell(mode, tz, chunk):
         torch.cuda.synchronize()
         outs.append((fwd, [a.fields.E.clone(), a.fields.H.clone()]))
         s.close()
-    for x, y in zip(outs[0][0] + outs[0][1], outs[1][0] + outs[1][1]):
-        assert rel_l2(x, y) < 1e-6
+    # modes 1 and 2 add the slab terms in the shell kernel's order (bitwise-close); mode 3 adds
+    # them after the plain update, a rounding apart per step: after 60 steps E, H and the
+    # phasor within 4e-7 and psi within 1e-6, except the psi of the two slabs holding the
+    # second dipole (1.4e-5 / 7.6e-6: their small norm is dominated by the source cell's
+    # neighbourhood); the 30 reverse steps amplify the difference inside the CPML, where a
+    # reverse step is no exact time reversal
+    n3 = 3  # E, H, phasor
+    tol_f, tol_p, tol_r = (2e-6, 5e-5, 1e-4) if mode == 3 else (1e-6, 1e-6, 1e-6)
+    for q, (x, y) in enumerate(zip(outs[0][0], outs[1][0])):
+        assert rel_l2(x, y) < (tol_f if q < n3 else tol_p), q
+    for x, y in zip(outs[0][1], outs[1][1]):
+        assert rel_l2(x, y) < tol_r
