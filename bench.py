@@ -687,9 +687,10 @@ def main():
     ap.add_argument("--shell-chunk", type=int, default=0, help="x planes per CPML shell block (0: plan default)")
     ap.add_argument("--shell-vec", type=int, default=0, help="z cells per CPML shell thread (0: plan default)")
     ap.add_argument("--tma", default="auto", choices=["auto", "0", "1"], help="TMA-pipelined update kernels")
-    ap.add_argument("--shell-tma", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+    ap.add_argument("--shell-tma", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5],
                     help="CPML slab cells on the TMA kernels: 0 none, 1 x and y slabs, 2 all, 3 split "
-                         "(plain TMA over the grid + per-axis corrections) (-1: default)")
+                         "(plain TMA over the grid + per-axis corrections), 4 split with the z slabs in the "
+                         "tiles, 5 mode 4 for E and 3 for H (-1: default)")
     ap.add_argument("--pml-tz", type=int, default=0, help="z extent of the whole-grid TMA tile (shell mode 2)")
     ap.add_argument("--pml-chunk", type=int, default=0, help="x planes per block of the slab-cell TMA launch")
     ap.add_argument("--tz", type=int, default=0)

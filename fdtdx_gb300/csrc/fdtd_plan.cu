@@ -58,15 +58,22 @@ struct FdtdPlan {
     // mode 1 widens the core to the whole x and y extent (the x and y slab terms in the PML
     // kernels) and leaves the two z boxes to the register-queue shell kernel; mode 2 runs the
     // whole grid in one PML launch per half-step (z terms too); mode 0 runs all six slab boxes
-    // on the shell kernel; mode 3 (the default where admitted; forward steps) runs the plain
-    // TMA kernels over the whole grid and then the slab cells' corrections (fdtd_split.cuh):
-    // 0.906 against 0.941 ms per step on the 400 x 400 x 200 coupler
-    int shell_tma = 3;                    // requested mode
+    // on the shell kernel; modes 3-5 (forward steps) run the plain TMA kernels over the whole
+    // grid and then the slab cells' corrections (fdtd_split.cuh).  Measured on the
+    // 400 x 400 x 200 coupler (ms per step, one box): mode 0 0.939, mode 3 0.906, mode 4 0.894;
+    // mode 5 (the default where admitted) takes each half-step's faster form
+    int shell_tma = 5;                    // requested mode
     bool m1_ok = false, m2_ok = false;    // admissible
     // mode 3 (forward steps): the plain TMA kernels over the whole grid (m2_tz tile), then the
     // CPML corrections of the slab cells (fdtd_split.cuh), one launch per axis
     bool m3_ok = false;
     int m3_chunk = 1, m3_chunk_e = 1;
+    // mode 4: as mode 3, with the z slabs' terms inside the TMA tiles (a column's z layer is
+    // fixed along its x-march) and only the x and y slabs corrected afterwards
+    bool m4_ok = false;
+    int m4_chunk = 1, m4_chunk_e = 1;
+    // mode 5: mode 4 for the E half-step and mode 3 for the H half-step (the H kernel with z
+    // terms needs 116 registers against 80 and loses more than its corrections cost)
     int m1_chunk = 1, m1_chunk_e = 1;     // x planes per block (H, E), mode 1
     int m2_tz = 0;                        // z extent of the mode-2 tile (the core's ty rows)
     int m2_chunk = 1, m2_chunk_e = 1;
@@ -408,7 +415,7 @@ int staged_planes(const FdtdPlan* p) {
 // the PML kernels over the whole grid, with the z extent of their tile picked for nz.  x
 // chunks of about ten (E) and six (H) waves of resident blocks, as for the core.
 void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
-    p->m1_ok = p->m2_ok = p->m3_ok = false;
+    p->m1_ok = p->m2_ok = p->m3_ok = p->m4_ok = false;
     if (!sp.split || p->d.n_slabs == 0) return;
     // one slab per face (the per-axis table) and 32-bit psi offsets
     int faces[3] = {0, 0, 0};
@@ -475,11 +482,19 @@ void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
         const size_t smH = tma_smem(tma_cfg(tz2, ty, p->tma_ns, true, p->d.n_mu, p->d.n_sigma_H, nullptr, staged_planes(p)));
         const int pe = occ_of((const void*)k_tma_E<false, false>, ty * tz2 / 2, smE);
         const int ph = occ_of((const void*)k_tma_H<false, false>, ty * tz2 / 2, smH);
-        if (disjoint && pe > 0 && ph > 0 && p->parts == 1 && p->d.n_poles == 0 && !p->full_e && !p->full_h) {
-            const long long tiles = (long long)((nz + tz2 - 1) / tz2) * ((ny + ty - 1) / ty);
+        const bool split_ok = disjoint && p->parts == 1 && p->d.n_poles == 0 && !p->full_e && !p->full_h;
+        const long long tiles = (long long)((nz + tz2 - 1) / tz2) * ((ny + ty - 1) / ty);
+        if (split_ok && pe > 0 && ph > 0) {
             p->m3_chunk_e = chunk_for(10, pe, tiles, nx);
             p->m3_chunk = chunk_for(6, ph, tiles, nx);
             p->m3_ok = p->m2_ok;
+        }
+        const int ze = occ_of((const void*)k_tma_E<false, 2>, ty * tz2 / 2, smE);
+        const int zh = occ_of((const void*)k_tma_H<false, 2>, ty * tz2 / 2, smH);
+        if (split_ok && ze > 0 && zh > 0) {
+            p->m4_chunk_e = chunk_for(10, ze, tiles, nx);
+            p->m4_chunk = chunk_for(6, zh, tiles, nx);
+            p->m4_ok = p->m2_ok;
         }
     }
     cudaGetLastError();
@@ -488,6 +503,8 @@ void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
 // The shell mode the launches use: the requested one, lowered to what the scene admits.
 int shell_tma_mode(const FdtdPlan* p) {
     if (!p->use_tma) return 0;
+    if (p->shell_tma == 5 && p->m4_ok && p->m3_ok) return 5;
+    if (p->shell_tma == 4 && p->m4_ok) return 4;
     if (p->shell_tma == 3 && p->m3_ok) return 3;
     if (p->shell_tma == 2 && p->m2_ok) return 2;
     if (p->shell_tma == 1 && p->m1_ok) return 1;
@@ -824,7 +841,7 @@ bool make_map(CUtensorMap* m, const float* base, int ncomp, const Geo& g, int bz
 // Launch of a TMA-pipelined half-step over the core box, or (ZP) over the z-slab shell boxes
 // with their CPML terms; false when a tensor map cannot be built (the caller then uses the
 // register-queue kernel).
-template <bool REV, bool HSIDE, bool PML = false>
+template <bool REV, bool HSIDE, int PML = 0>
 bool launch_tma(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, int tz, int chunk) {
     const Geo& g = p->g;
     const int ty = p->tma_ty;
@@ -943,9 +960,10 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
 // The CPML corrections of a split forward half-step: one launch per axis holding slabs (both
 // faces in one grid, blockIdx.y the face), in x, y, z order.
 template <bool HSIDE>
-void launch_pml_corr(const UpdArgs& a, cudaStream_t st) {
+void launch_pml_corr(const UpdArgs& a, cudaStream_t st, int axes) {
     auto run = [&](auto ax_tag) {
         constexpr int AX = decltype(ax_tag)::value;
+        if (!(axes >> AX & 1)) return;
         const long long n0 = (long long)a.axs[AX][0].sx * a.axs[AX][0].sy * a.axs[AX][0].sz * (a.axs[AX][0].L > 0);
         const long long n1 = (long long)a.axs[AX][1].sx * a.axs[AX][1].sy * a.axs[AX][1].sz * (a.axs[AX][1].L > 0);
         const long long n = std::max(n0, n1);
@@ -966,14 +984,18 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
         launch_plain_boxes<REV, HSIDE, true>(p, a, &all, &p->chunk, 1, st);
         return;
     }
-    const int mode = a.axt == 2 ? shell_tma_mode(p) : 0;
-    if (mode == 3 && !REV) {
-        // the plain update of every cell in one TMA launch, then the slab cells' CPML terms
+    const int mode0 = a.axt == 2 ? shell_tma_mode(p) : 0;
+    const int mode = mode0 == 5 ? (HSIDE ? 3 : 4) : mode0;
+    if ((mode == 3 || mode == 4) && !REV) {
+        // the plain update of every cell in one TMA launch (mode 4: with the z slabs' terms in
+        // the tiles), then the other slab cells' CPML terms
         UpdArgs ax = a;
         for (int x = 0; x < 3; ++x) { ax.lo[x] = 0; ax.hi[x] = x == 0 ? p->g.nx : x == 1 ? p->g.ny : p->g.nz; }
-        if (launch_tma<REV, HSIDE, false>(p, ax, st, p->m2_tz, HSIDE ? p->m3_chunk : p->m3_chunk_e)) {
+        const bool ok = mode == 4 ? launch_tma<REV, HSIDE, 2>(p, ax, st, p->m2_tz, HSIDE ? p->m4_chunk : p->m4_chunk_e)
+                                  : launch_tma<REV, HSIDE, 0>(p, ax, st, p->m2_tz, HSIDE ? p->m3_chunk : p->m3_chunk_e);
+        if (ok) {
             if (mid) cudaEventRecord(mid, st);
-            launch_pml_corr<HSIDE>(a, st);
+            launch_pml_corr<HSIDE>(a, st, mode == 4 ? 3 : 7);
             return;
         }
     }
@@ -1014,18 +1036,15 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
     launch_plain_boxes<REV, HSIDE, true>(p, a, sp.shell, chunks, sp.n_shell, st, p->shell_vec);
 }
 
-int half_step_launches(const FdtdPlan* p) {
+int half_step_launches(const FdtdPlan* p, bool hside) {
     const Split sp = split_boxes(p);
     if (!sp.split) return 1;
-    const int mode = shell_tma_mode(p);
-    if (mode == 3) {  // forward steps: the plain launch and one correction launch per slab axis
-        int axes = 0;
-        for (int x = 0; x < 3; ++x) {
-            bool any = false;
-            for (int s = 0; s < p->d.n_slabs; ++s) any = any || p->slab[s].axis == x;
-            axes += any;
-        }
-        return 1 + axes;
+    const int mode0 = shell_tma_mode(p);
+    const int mode = mode0 == 5 ? (hside ? 3 : 4) : mode0;
+    if (mode == 3 || mode == 4) {  // forward steps: the plain launch, one correction launch per slab axis
+        int axes[3] = {0, 0, 0};
+        for (int s = 0; s < p->d.n_slabs; ++s) axes[p->slab[s].axis] = 1;
+        return 1 + axes[0] + axes[1] + (mode == 3 ? axes[2] : 0);
     }
     if (mode == 2) return 1;
     if (mode == 1) return 1 + ((sp.core.lo[2] > 0 || sp.core.hi[2] < p->g.nz) ? 1 : 0);
@@ -1076,7 +1095,7 @@ void launch_side(const FdtdPlan* p, const FdtdBuffers* b, const float* F, const 
 // Launches of one half-step of every part.
 int side_launches(const FdtdPlan* p, bool hside) {
     if (hside ? p->full_h : p->full_e) return 2 * p->parts;
-    return p->parts * half_step_launches(p);
+    return p->parts * half_step_launches(p, hside);
 }
 
 // The arguments of one half-step; `part` 1 selects the imaginary parts of complex (Bloch)
@@ -1518,8 +1537,8 @@ extern "C" int32_t fdtd_plan_uses_tma(const FdtdPlan* p) { return p && p->use_tm
 
 extern "C" int fdtd_plan_tune_shell_tma(FdtdPlan* p, int32_t mode, int32_t tz, int32_t chunk) {
     if (!p) return FDTD_EINVAL;
-    if (mode < 0 || mode > 3 || tz < 0 || tz % 4 || tz > 120 || chunk < 0)
-        return fail(p, FDTD_EINVAL, "invalid slab-cell mode (0 to 3) or tile (tz a multiple of 4, <= 120)");
+    if (mode < 0 || mode > 5 || tz < 0 || tz % 4 || tz > 120 || chunk < 0)
+        return fail(p, FDTD_EINVAL, "invalid slab-cell mode (0 to 5) or tile (tz a multiple of 4, <= 120)");
     p->shell_tma = mode;
     p->m2_tz = tz;
     configure_tma(p);
@@ -1532,6 +1551,8 @@ extern "C" int fdtd_plan_tune_shell_tma(FdtdPlan* p, int32_t mode, int32_t tz, i
         if (mode == 1) p->m1_chunk = p->m1_chunk_e = std::min(chunk, p->g.nx);
         if (mode == 2) p->m2_chunk = p->m2_chunk_e = std::min(chunk, p->g.nx);
         if (mode == 3) p->m3_chunk = p->m3_chunk_e = std::min(chunk, p->g.nx);
+        if (mode == 4 || mode == 5) p->m4_chunk = p->m4_chunk_e = std::min(chunk, p->g.nx);
+        if (mode == 5) p->m3_chunk = p->m3_chunk_e = std::min(chunk, p->g.nx);
     }
     drop_graphs(p);
     return FDTD_OK;

@@ -186,12 +186,16 @@ struct PsiPf {
     XPlane xp;
 };
 
-template <bool HSIDE>
+template <bool HSIDE, bool ZONLY = false>
 __device__ __forceinline__ void pml_fetch(const UpdArgs& a, const ZCol& zc, const YCol& yc, int i, int j, int k0,
                                           bool valid, PsiPf& f) {
     int o0, o1;
     zcol_off(zc, i, o0, o1);
     psi_load_pair(zc.p1, zc.p2, o0, o1, f.z[0], f.z[1]);
+    if (ZONLY) {  // z terms only (the x and y slabs are corrected by their own launches)
+        f.xp.side = -1;
+        return;
+    }
     ycol_off(yc, i, o0, o1);
     psi_load_pair(yc.p1, yc.p2, o0, o1, f.y[0], f.y[1]);
     xplane_init<HSIDE>(a, i, f.xp);
@@ -225,24 +229,27 @@ __device__ __forceinline__ float2 tma_slab_term(float ca, float cb, float km, in
 }
 
 // The slab terms of cell e (axis order x, y, z); q holds the psi pairs to store.
-template <bool REV>
+template <bool REV, bool ZONLY = false>
 __device__ __forceinline__ void pml_terms(const PsiPf& f, const YCol& yc, const ZCol& zc, int e, const float d[6],
                                           float cu[3], float2 q[3]) {
-    if (f.xp.side >= 0) q[0] = tma_slab_term<REV, 0>(f.xp.ca, f.xp.cb, f.xp.km, f.xp.kone, f.x[e], d, cu);
-    if (yc.o[e] >= 0) q[1] = tma_slab_term<REV, 1>(yc.ca, yc.cb, yc.km, yc.kone, f.y[e], d, cu);
+    if (!ZONLY && f.xp.side >= 0) q[0] = tma_slab_term<REV, 0>(f.xp.ca, f.xp.cb, f.xp.km, f.xp.kone, f.x[e], d, cu);
+    if (!ZONLY && yc.o[e] >= 0) q[1] = tma_slab_term<REV, 1>(yc.ca, yc.cb, yc.km, yc.kone, f.y[e], d, cu);
     if (zc.o[e] >= 0) q[2] = tma_slab_term<REV, 2>(zc.ca[e], zc.cb[e], zc.km[e], zc.kone, f.z[e], d, cu);
 }
 
 // The forward step's psi stores of both cells at plane i.
+template <bool ZONLY = false>
 __device__ __forceinline__ void pml_store(const UpdArgs& a, const PsiPf& f, const YCol& yc, const ZCol& zc, int i, int j,
                                           int k0, const float2 q[2][3]) {
     int o0, o1;
-    if (f.xp.side >= 0) {
-        o0 = xplane_off(a, f.xp, j, k0);
-        psi_store_pair(f.xp.p1, f.xp.p2, o0, o0 + 1, q[0][0], q[1][0]);
+    if (!ZONLY) {
+        if (f.xp.side >= 0) {
+            o0 = xplane_off(a, f.xp, j, k0);
+            psi_store_pair(f.xp.p1, f.xp.p2, o0, o0 + 1, q[0][0], q[1][0]);
+        }
+        ycol_off(yc, i, o0, o1);
+        psi_store_pair(yc.p1, yc.p2, o0, o1, q[0][1], q[1][1]);
     }
-    ycol_off(yc, i, o0, o1);
-    psi_store_pair(yc.p1, yc.p2, o0, o1, q[0][1], q[1][1]);
     zcol_off(zc, i, o0, o1);
     psi_store_pair(zc.p1, zc.p2, o0, o1, q[0][2], q[1][2]);
 }
@@ -304,7 +311,7 @@ __device__ __forceinline__ void drain(uint64_t* bar, int ns, int from, int to) {
 //   E, inv_eps, sigma_E on the tile
 // Loads cover planes i0-1 .. i1-1; the first only seeds H(i-1) of each column.
 // ---------------------------------------------------------------------------------
-template <bool REV, bool PML = false>
+template <bool REV, int PML = 0>
 __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -327,7 +334,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
     YCol yc{};
     if (PML) {
         zcol_init<false>(a, j, k0, valid, zc);
-        ycol_init<false>(a, j, k0, valid, yc);
+        if (PML == 1) ycol_init<false>(a, j, k0, valid, yc);
     }
     if (tc.expire) {  // injected wait expiry: the error path, with no copy issued
         if (tid == 0) atomicExch(tc.err, FDTD_ETIMEOUT);
@@ -359,7 +366,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
         const int i = i0 - 1 + p;
         if (PML) {
             pf = pn;
-            if (p + 1 < P) pml_fetch<false>(a, zc, yc, i + 1, j, k0, valid, pn);
+            if (p + 1 < P) pml_fetch<false, PML == 2>(a, zc, yc, i + 1, j, k0, valid, pn);
         }
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)((p / NS) & 1));
         const float* F = sm + s * tc.stage_floats;
@@ -391,7 +398,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
                 Hy_m[e] = Hy;
                 Hz_m[e] = Hz;
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (PML) pml_terms<REV>(pf, yc, zc, e, d, cu, qn[e]);
+                if (PML) pml_terms<REV, PML == 2>(pf, yc, zc, e, d, cu, qn[e]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -412,7 +419,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (PML && !REV) pml_store(a, pf, yc, zc, i, j, k0, qn);
+            if (PML && !REV) pml_store<PML == 2>(a, pf, yc, zc, i, j, k0, qn);
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -435,7 +442,7 @@ __global__ void __launch_bounds__(256) k_tma_E(const __grid_constant__ UpdArgs a
 //   H, inv_mu, sigma_H on the tile
 // Loads cover planes i0 .. i1; plane i is computed once the loads of i and i+1 landed.
 // ---------------------------------------------------------------------------------
-template <bool REV, bool PML = false>
+template <bool REV, int PML = 0>
 __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a, const __grid_constant__ CUtensorMap mF,
                                                const __grid_constant__ CUtensorMap mU,
                                                const __grid_constant__ CUtensorMap mM,
@@ -459,7 +466,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
     YCol yc{};
     if (PML) {
         zcol_init<true>(a, j, k0, valid, zc);
-        ycol_init<true>(a, j, k0, valid, yc);
+        if (PML == 1) ycol_init<true>(a, j, k0, valid, yc);
     }
 
     int slot[kMaxFuse];
@@ -510,13 +517,13 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
         for (int e = 0; e < 3; ++e) Exm[e] = ld_halo(g, a.F, 0, i0 - 1, j, k0 + e);
     }
     PsiPf pf{}, pn{};  // psi of the plane being updated and of the next one
-    if (PML && P > 1) pml_fetch<true>(a, zc, yc, i0, j, k0, valid, pn);
+    if (PML && P > 1) pml_fetch<true, PML == 2>(a, zc, yc, i0, j, k0, valid, pn);
     for (int p = 0; p + 1 < P; ++p) {
         const int s = p % NS, s1 = (p + 1) % NS;
         const int i = i0 + p;
         if (PML) {
             pf = pn;
-            if (p + 2 < P) pml_fetch<true>(a, zc, yc, i + 1, j, k0, valid, pn);
+            if (p + 2 < P) pml_fetch<true, PML == 2>(a, zc, yc, i + 1, j, k0, valid, pn);
         }
         ok = ok && mbar_wait_bounded(&bar[s1], (uint32_t)(((p + 1) / NS) & 1));
         if (ok && valid) {
@@ -547,7 +554,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
                 const float Ey_ip = E1[(1 * EY + r0) * EZ + kk];
                 const float d[6] = {Ez_jp - Ez, Ey_kp - Ey, Ex_kp - Ex, Ez_ip - Ez, Ey_ip - Ey, Ex_jp - Ex};
                 float cu[3] = {d[0] - d[1], d[2] - d[3], d[4] - d[5]};
-                if (PML) pml_terms<REV>(pf, yc, zc, e, d, cu, qn[e]);
+                if (PML) pml_terms<REV, PML == 2>(pf, yc, zc, e, d, cu, qn[e]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const float u0 = U[(comp * TY + ty) * TZ + cz];
@@ -611,7 +618,7 @@ __global__ void __launch_bounds__(256) k_tma_H(const __grid_constant__ UpdArgs a
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp)
                 *reinterpret_cast<float2*>(a.Uout + comp * N + c) = make_float2(out[comp][0], out[comp][1]);
-            if (PML && !REV) pml_store(a, pf, yc, zc, i, j, k0, qn);
+            if (PML && !REV) pml_store<PML == 2>(a, pf, yc, zc, i, j, k0, qn);
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {

@@ -630,8 +630,9 @@ class Scene:
         """Where the CPML slab cells run with a TMA core: 0 the register-queue shell kernel, 1 the
         x and y slabs in the TMA kernels (z boxes on the shell kernel), 2 the whole grid in one
         TMA launch (tile z extent ``tz``, 0: picked for nz), 3 split: the plain TMA kernels over
-        the whole grid, then the slab cells' CPML corrections, one launch per axis (forward
-        steps; reverse steps run mode 0)."""
+        the whole grid, then the slab cells' CPML corrections, one launch per axis, 4 the same
+        with the z slabs' terms in the TMA tiles, 5 (the default where admitted) mode 4 for the E
+        half-step and 3 for the H half-step (modes 3-5: forward steps; reverse steps run mode 0)."""
         N.check(N.load().fdtd_plan_tune_shell_tma(self.plan, int(mode), int(tz), int(chunk)), self.plan,
                 "fdtd_plan_tune_shell_tma")
 

@@ -279,7 +279,7 @@ def test_tma_kernels_match_register_kernels(tile):
     objs.append(fx.FieldDetector(name="ez", grid_slice_tuple=((0, 30), (0, 27), (20, 21)), components=("Ez", "Ey")))
     objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
     outs = {}
-    for run in ("register", 0, 3):
+    for run in ("register", 0, 3, 4, 5):
         a = arrays.reset()
         s = Scene(objects, a, cfg)
         if run == "register":
@@ -294,7 +294,7 @@ def test_tma_kernels_match_register_kernels(tile):
         outs[run] = a
         s.close()
     ref = outs["register"]
-    for run, tol, tol_psi in ((0, 1e-6, 1e-6), (3, 2e-6, 5e-6)):
+    for run, tol, tol_psi in ((0, 1e-6, 1e-6), (3, 2e-6, 5e-6), (4, 2e-6, 5e-6), (5, 2e-6, 5e-6)):
         got = outs[run]
         for k in ("E", "H"):
             assert rel_l2(getattr(got.fields, k), getattr(ref.fields, k)) < tol, (run, k)
@@ -326,11 +326,12 @@ def test_plans_of_different_tile_memory_coexist():
     assert s1.uses_tma
 
 
-@pytest.mark.parametrize("mode,tz,chunk", [(1, 0, 0), (2, 0, 0), (2, 20, 3), (3, 0, 0), (3, 20, 5)])
+@pytest.mark.parametrize("mode,tz,chunk", [(1, 0, 0), (2, 0, 0), (2, 20, 3), (3, 0, 0), (3, 20, 5), (4, 0, 0), (4, 20, 3), (5, 0, 0)])
 def test_shell_tma_matches_register_shell(mode, tz, chunk):
     """The CPML slab cells on the TMA kernels with in-tile slab terms (mode 1: the x and y
     slabs, the core widened over them; mode 2: the whole grid in one launch), or split (mode 3:
-    the plain TMA kernels over the whole grid, then the slab cells' CPML corrections per axis)
+    the plain TMA kernels over the whole grid, then the slab cells' CPML corrections per axis;
+    mode 4: the same with the z slabs' terms inside the tiles; mode 5: mode 4 for E, 3 for H)
     against the register-queue shell kernel: forward steps with kappa != 1, a conductor and a
     dipole inside the slabs and a fused full-volume phasor, then time-reversed steps with the
     recorded interfaces (psi frozen)."""
@@ -354,7 +355,7 @@ def test_shell_tma_matches_register_shell(mode, tz, chunk):
     for m in (mode, 0):
         a = arrays.reset()
         s = Scene(objects, a, cfg, record_interfaces=True)
-        s.tune_shell_tma(m, tz if m in (2, 3) else 0, chunk if m else 0)
+        s.tune_shell_tma(m, tz if m >= 2 else 0, chunk if m else 0)
         assert s.uses_tma and s.shell_tma == m
         s.forward(a, 0, 60)
         s.status()
@@ -373,7 +374,7 @@ def test_shell_tma_matches_register_shell(mode, tz, chunk):
     # neighbourhood); the 30 reverse steps amplify the difference inside the CPML, where a
     # reverse step is no exact time reversal
     n3 = 3  # E, H, phasor
-    tol_f, tol_p, tol_r = (2e-6, 5e-5, 1e-4) if mode == 3 else (1e-6, 1e-6, 1e-6)
+    tol_f, tol_p, tol_r = (2e-6, 5e-5, 1e-4) if mode >= 3 else (1e-6, 1e-6, 1e-6)
     for q, (x, y) in enumerate(zip(outs[0][0], outs[1][0])):
         assert rel_l2(x, y) < (tol_f if q < n3 else tol_p), q
     for x, y in zip(outs[0][1], outs[1][1]):
