@@ -58,14 +58,17 @@ struct FdtdPlan {
     // mode 1 widens the core to the whole x and y extent (the x and y slab terms in the PML
     // kernels) and leaves the two z boxes to the register-queue shell kernel; mode 2 runs the
     // whole grid in one PML launch per half-step (z terms too); mode 0 runs all six slab boxes
-    // on the shell kernel; modes 3-5 (forward steps) run the plain TMA kernels over the whole
-    // grid and then the slab cells' corrections (fdtd_split.cuh).  Measured on the
-    // 400 x 400 x 200 coupler (ms per step, one box): mode 0 0.939, mode 3 0.906, mode 4 0.894;
-    // mode 5 (the default where admitted) takes each half-step's faster form
-    int shell_tma = 5;                    // requested mode
+    // on the shell kernel; modes 3-5 run the plain TMA kernels over the whole grid and then
+    // the slab cells' corrections (fdtd_split.cuh), forward and reverse steps.  Measured on the
+    // 400 x 400 x 200 coupler (ms per step, one box): mode 0 0.939, mode 3 0.906, mode 4 0.894,
+    // mode 5 0.884 (each half-step's faster form); on the 200 x 200 x 100 inverse-design scene
+    // mode 5 lost (forward with recording 0.479 s against 0.394 s for 3000 steps: the extra
+    // launches and the coarser whole-grid tiles weigh more on a small grid).  Default: mode 5
+    // from kSplitCells cells up, else mode 0 (set at plan creation)
+    int shell_tma = 0;                    // requested mode
     bool m1_ok = false, m2_ok = false;    // admissible
-    // mode 3 (forward steps): the plain TMA kernels over the whole grid (m2_tz tile), then the
-    // CPML corrections of the slab cells (fdtd_split.cuh), one launch per axis
+    // mode 3: the plain TMA kernels over the whole grid (m2_tz tile), then the CPML corrections
+    // of the slab cells (fdtd_split.cuh), one launch per axis
     bool m3_ok = false;
     int m3_chunk = 1, m3_chunk_e = 1;
     // mode 4: as mode 3, with the z slabs' terms inside the TMA tiles (a column's z layer is
@@ -202,6 +205,7 @@ bool det_fusable(const FdtdDetectorDesc& dd) {
 }
 
 constexpr int kUpdThreads = 256;
+constexpr long long kSplitCells = 16ll << 20;  // grids from this size up default to shell mode 5
 
 int pick_vec(int nz) { return nz % 2 == 0 ? 2 : 1; }  // 4 measured slower (register pressure)
 
@@ -480,8 +484,10 @@ void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
         }
         const size_t smE = tma_smem(tma_cfg(tz2, ty, p->tma_ns, false, p->d.n_eps, p->d.n_sigma_E, nullptr));
         const size_t smH = tma_smem(tma_cfg(tz2, ty, p->tma_ns, true, p->d.n_mu, p->d.n_sigma_H, nullptr, staged_planes(p)));
-        const int pe = occ_of((const void*)k_tma_E<false, false>, ty * tz2 / 2, smE);
-        const int ph = occ_of((const void*)k_tma_H<false, false>, ty * tz2 / 2, smH);
+        const int pe = std::min(occ_of((const void*)k_tma_E<false, 0>, ty * tz2 / 2, smE),
+                                occ_of((const void*)k_tma_E<true, 0>, ty * tz2 / 2, smE));
+        const int ph = std::min(occ_of((const void*)k_tma_H<false, 0>, ty * tz2 / 2, smH),
+                                occ_of((const void*)k_tma_H<true, 0>, ty * tz2 / 2, smH));
         const bool split_ok = disjoint && p->parts == 1 && p->d.n_poles == 0 && !p->full_e && !p->full_h;
         const long long tiles = (long long)((nz + tz2 - 1) / tz2) * ((ny + ty - 1) / ty);
         if (split_ok && pe > 0 && ph > 0) {
@@ -489,8 +495,10 @@ void configure_shell_tma(FdtdPlan* p, const Split& sp, int optin) {
             p->m3_chunk = chunk_for(6, ph, tiles, nx);
             p->m3_ok = p->m2_ok;
         }
-        const int ze = occ_of((const void*)k_tma_E<false, 2>, ty * tz2 / 2, smE);
-        const int zh = occ_of((const void*)k_tma_H<false, 2>, ty * tz2 / 2, smH);
+        const int ze = std::min(occ_of((const void*)k_tma_E<false, 2>, ty * tz2 / 2, smE),
+                                occ_of((const void*)k_tma_E<true, 2>, ty * tz2 / 2, smE));
+        const int zh = std::min(occ_of((const void*)k_tma_H<false, 2>, ty * tz2 / 2, smH),
+                                occ_of((const void*)k_tma_H<true, 2>, ty * tz2 / 2, smH));
         if (split_ok && ze > 0 && zh > 0) {
             p->m4_chunk_e = chunk_for(10, ze, tiles, nx);
             p->m4_chunk = chunk_for(6, zh, tiles, nx);
@@ -797,6 +805,7 @@ int fdtd_plan_create(const FdtdDesc* desc, FdtdPlan** out) {
         const Split sp = split_boxes(p);
         p->tma_tz = pick_tz(sp.split ? sp.core.hi[2] - sp.core.lo[2] : p->g.nz);
     }
+    p->shell_tma = p->g.N >= kSplitCells ? 5 : 0;
     configure_tma(p);
     *out = p;
     return FDTD_OK;
@@ -959,7 +968,7 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
 
 // The CPML corrections of a split forward half-step: one launch per axis holding slabs (both
 // faces in one grid, blockIdx.y the face), in x, y, z order.
-template <bool HSIDE>
+template <bool REV, bool HSIDE>
 void launch_pml_corr(const UpdArgs& a, cudaStream_t st, int axes) {
     auto run = [&](auto ax_tag) {
         constexpr int AX = decltype(ax_tag)::value;
@@ -967,7 +976,7 @@ void launch_pml_corr(const UpdArgs& a, cudaStream_t st, int axes) {
         const long long n0 = (long long)a.axs[AX][0].sx * a.axs[AX][0].sy * a.axs[AX][0].sz * (a.axs[AX][0].L > 0);
         const long long n1 = (long long)a.axs[AX][1].sx * a.axs[AX][1].sy * a.axs[AX][1].sz * (a.axs[AX][1].L > 0);
         const long long n = std::max(n0, n1);
-        if (n > 0) k_pml_corr<HSIDE, AX><<<dim3((unsigned)((n + 255) / 256), 2), 256, 0, st>>>(a);
+        if (n > 0) k_pml_corr<REV, HSIDE, AX><<<dim3((unsigned)((n + 255) / 256), 2), 256, 0, st>>>(a);
     };
     run(std::integral_constant<int, 0>{});
     run(std::integral_constant<int, 1>{});
@@ -986,7 +995,7 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
     }
     const int mode0 = a.axt == 2 ? shell_tma_mode(p) : 0;
     const int mode = mode0 == 5 ? (HSIDE ? 3 : 4) : mode0;
-    if ((mode == 3 || mode == 4) && !REV) {
+    if (mode == 3 || mode == 4) {
         // the plain update of every cell in one TMA launch (mode 4: with the z slabs' terms in
         // the tiles), then the other slab cells' CPML terms
         UpdArgs ax = a;
@@ -995,7 +1004,7 @@ void launch_half(const FdtdPlan* p, const UpdArgs& a, cudaStream_t st, cudaEvent
                                   : launch_tma<REV, HSIDE, 0>(p, ax, st, p->m2_tz, HSIDE ? p->m3_chunk : p->m3_chunk_e);
         if (ok) {
             if (mid) cudaEventRecord(mid, st);
-            launch_pml_corr<HSIDE>(a, st, mode == 4 ? 3 : 7);
+            launch_pml_corr<REV, HSIDE>(a, st, mode == 4 ? 3 : 7);
             return;
         }
     }
@@ -1041,7 +1050,7 @@ int half_step_launches(const FdtdPlan* p, bool hside) {
     if (!sp.split) return 1;
     const int mode0 = shell_tma_mode(p);
     const int mode = mode0 == 5 ? (hside ? 3 : 4) : mode0;
-    if (mode == 3 || mode == 4) {  // forward steps: the plain launch, one correction launch per slab axis
+    if (mode == 3 || mode == 4) {  // the plain launch, one correction launch per slab axis
         int axes[3] = {0, 0, 0};
         for (int s = 0; s < p->d.n_slabs; ++s) axes[p->slab[s].axis] = 1;
         return 1 + axes[0] + axes[1] + (mode == 3 ? axes[2] : 0);

@@ -13,16 +13,19 @@
 // as the fused kernels add them, so a cell in two or three slabs (an edge or a corner) sees
 // its corrections one launch after another; the two slabs of an axis are disjoint.
 //
+// A reverse step (fdtdx/fdtd/update.py:751-807 inverting the update with psi frozen) splits
+// the same way: E_old = [(1 + q) E - s c m curl] / (1 - q) = [plain reverse] - s c m dcurl /
+// (1 - q), dcurl from the stored psi, which the reverse step does not advance.
+//
 // One thread per slab cell in psi order (a slab's psi array is dense over the slab box), so
-// psi is read and written with unit stride.  Forward steps only: a reverse step keeps psi
-// frozen and runs the fused shell kernels.  Needs the per-axis slab table of a scene without
-// a periodic axis (zero halo, UpdArgs::axt == 2).
+// psi is read (and, forward, written) with unit stride.  Needs the per-axis slab table of a
+// scene without a periodic axis (zero halo, UpdArgs::axt == 2).
 #pragma once
 #include "fdtd_kernels.cuh"
 
 namespace fdtd {
 
-template <bool HSIDE, int AX>
+template <bool REV, bool HSIDE, int AX>
 __global__ void __launch_bounds__(256) k_pml_corr(const __grid_constant__ UpdArgs a) {
     const int side = blockIdx.y;
     const DSlab& sl = a.axs[AX][side];
@@ -62,11 +65,14 @@ __global__ void __launch_bounds__(256) k_pml_corr(const __grid_constant__ UpdArg
     const float* co = sl.coef + (HSIDE ? 3 * L : 0);
     float* __restrict__ p1 = a.axp[AX][side][0];
     float* __restrict__ p2 = a.axp[AX][side][1];
-    const float ca = __ldg(co + l), cb = __ldg(co + L + l);
-    const float q1 = cb * p1[q] + ca * d1;
-    const float q2 = cb * p2[q] + ca * d2;
-    p1[q] = q1;
-    p2[q] = q2;
+    float q1 = p1[q], q2 = p2[q];
+    if (!REV) {
+        const float ca = __ldg(co + l), cb = __ldg(co + L + l);
+        q1 = cb * q1 + ca * d1;
+        q2 = cb * q2 + ca * d2;
+        p1[q] = q1;
+        p2[q] = q2;
+    }
     float c1 = q1, c2 = q2;
     if (!sl.kappa_one) {
         const float ikm1 = __ldg(co + 2 * L + l) - 1.f;
@@ -75,7 +81,7 @@ __global__ void __launch_bounds__(256) k_pml_corr(const __grid_constant__ UpdArg
     }
     // curl component (AX + 1) % 3 gets -c1, component (AX + 2) % 3 gets +c2
     const int wall = HSIDE ? g.pmc : g.pec;
-    const float s = HSIDE ? -g.c : g.c;
+    const float s = (HSIDE != REV) ? -g.c : g.c;
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
         const int comp = t == 0 ? C2 : C1;
@@ -85,7 +91,8 @@ __global__ void __launch_bounds__(256) k_pml_corr(const __grid_constant__ UpdArg
         float f = s * m * dc;
         if (a.sig) {
             const float sg = __ldg(a.sig + (a.n_sig == 3 ? comp * N : 0) + c);
-            f /= 1.f + (HSIDE ? g.c * sg / g.eta0 * m / 2.f : g.c * sg * g.eta0 * m / 2.f);
+            const float qs = HSIDE ? g.c * sg / g.eta0 * m / 2.f : g.c * sg * g.eta0 * m / 2.f;
+            f /= REV ? 1.f - qs : 1.f + qs;
         }
         a.Uout[comp * N + c] += f;
     }

@@ -632,7 +632,7 @@ class Scene:
         TMA launch (tile z extent ``tz``, 0: picked for nz), 3 split: the plain TMA kernels over
         the whole grid, then the slab cells' CPML corrections, one launch per axis, 4 the same
         with the z slabs' terms in the TMA tiles, 5 (the default where admitted) mode 4 for the E
-        half-step and 3 for the H half-step (modes 3-5: forward steps; reverse steps run mode 0)."""
+        half-step and 3 for the H half-step (modes 3-5 split forward and reverse steps alike)."""
         N.check(N.load().fdtd_plan_tune_shell_tma(self.plan, int(mode), int(tz), int(chunk)), self.plan,
                 "fdtd_plan_tune_shell_tma")
 

@@ -285,9 +285,8 @@ int32_t fdtd_plan_uses_tma(const FdtdPlan* plan);
  * boxes; mode 1, the TMA kernels with in-tile slab terms over the whole x and y extent (the x
  * and y slabs) and the shell kernel over the two z boxes; mode 2, the whole grid in one launch
  * of the TMA kernels with every slab term in the tiles (tile z extent `tz`, 0: picked for nz);
- * mode 3 (split, forward steps; reverse steps run mode 0), the plain TMA kernels over the
- * whole grid on the mode-2 tile, then the CPML corrections of the slab cells, one launch per
- * axis; mode 4, the same with the z slabs' terms inside the TMA tiles; mode 5 (the default
+ * mode 3 (split), the plain TMA kernels over the whole grid on the mode-2 tile, then the
+ * CPML corrections of the slab cells, one launch per axis (forward and reverse steps); mode 4, the same with the z slabs' terms inside the TMA tiles; mode 5 (the default
  * where the scene admits it), mode 4 for the E half-step and mode 3 for the H half-step.
  * `chunk` x planes per block (0: a default).  fdtd_plan_shell_tma returns the mode in use. */
 int fdtd_plan_tune_shell_tma(FdtdPlan* plan, int32_t mode, int32_t tz, int32_t chunk);

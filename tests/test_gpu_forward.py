@@ -367,12 +367,12 @@ def test_shell_tma_matches_register_shell(mode, tz, chunk):
         torch.cuda.synchronize()
         outs.append((fwd, [a.fields.E.clone(), a.fields.H.clone()]))
         s.close()
-    # modes 1 and 2 add the slab terms in the shell kernel's order (bitwise-close); mode 3 adds
-    # them after the plain update, a rounding apart per step: after 60 steps E, H and the
+    # modes 1 and 2 add the slab terms in the shell kernel's order (bitwise-close); modes 3-5
+    # add them after the plain update, a rounding apart per step: after 60 steps E, H and the
     # phasor within 4e-7 and psi within 1e-6, except the psi of the two slabs holding the
     # second dipole (1.4e-5 / 7.6e-6: their small norm is dominated by the source cell's
-    # neighbourhood); the 30 reverse steps amplify the difference inside the CPML, where a
-    # reverse step is no exact time reversal
+    # neighbourhood); the 30 reverse steps (split too) amplify the difference inside the CPML,
+    # where a reverse step is no exact time reversal
     n3 = 3  # E, H, phasor
     tol_f, tol_p, tol_r = (2e-6, 5e-5, 1e-4) if mode >= 3 else (1e-6, 1e-6, 1e-6)
     for q, (x, y) in enumerate(zip(outs[0][0], outs[1][0])):
