@@ -265,7 +265,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(budget_s=args.cpu_budget)
     launches = scene.launches_per_step() * K + 1
-    # the other forms of the benchmark spec, each on its own workload (reported, not the headline)
+    # the gradient, batch and serving measurements, each on its own workload (reported, not the headline)
     extra = {}
     scene.close()
     del arrays, base, host_eps

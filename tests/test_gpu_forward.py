@@ -1,6 +1,6 @@
 """Forward-path parity of the GB300 kernels against the oracle (float32: asserted; float64: reported).
 
-Tolerance (the spec bar): relative L2 <= 1e-4 on fields and detector states
+Tolerance: relative L2 <= 1e-4 on fields and detector states
 against the float32 restatement of the reference after the full run.
 """
 
