@@ -259,7 +259,9 @@ def run_gpu(args):
         h2d = host_eps.numel() * 4
         d2h = sum(r.numel() * 8 for r in res)
         e2e = {"value": ncell * K * ws / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / K,
-               "d2h_bytes_per_step": d2h / K, "api": "fdtdx_gb300.run_fdtd"}
+               "d2h_bytes_per_step": d2h / K, "api": "fdtdx_gb300.run_fdtd",
+               "copies": "in: inv_permittivities from pinned host memory each call; out: the two flux-plane "
+                         "phasors (the run's result); E, H and the full-volume phasor stay on the device"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
