@@ -379,3 +379,47 @@ def test_shell_tma_matches_register_shell(mode, tz, chunk):
         assert rel_l2(x, y) < (tol_f if q < n3 else tol_p), q
     for x, y in zip(outs[0][1], outs[1][1]):
         assert rel_l2(x, y) < tol_r
+
+
+def test_split_halfsteps_with_conductor_faces_against_oracle():
+    """The split CPML half-steps (slab modes 3 and 5) on a scene whose min-z and max-x faces are
+    PEC and whose min-y face is PMC, CPML on the others (the corrections skip the components
+    a conductor face zeroes), with a lossy anisotropic block reaching into the slabs: against
+    the register-queue shell (mode 0) and the float32 / float64 oracle, forward steps and
+    time-reversed steps."""
+    cfg = _cfg(50, record=True)
+    vol = fx.SimulationVolume(shape=(30, 27, 44))
+    bc = fx.BoundaryConfig.from_uniform_bound(6, "pml", override_types={"min_z": "pec", "max_x": "pec", "min_y": "pmc"})
+    objs = [vol] + list(fx.boundary_objects_from_config(bc, vol).values())
+    objs.append(fx.UniformMaterialObject(name="blk", grid_slice_tuple=((2, 25), (1, 22), (0, 40)),
+                                         material=fx.Material(permittivity=(4.0, 3.0, 5.0), electric_conductivity=1e4)))
+    objs.append(fx.PointDipoleSource(name="d", grid_slice_tuple=((15, 16), (13, 14), (30, 31)), polarization=0,
+                                     wave_character=fx.WaveCharacter(wavelength=1.55e-6),
+                                     temporal_profile=scenes.pulse_5fs()))
+    objs.append(fx.PhasorDetector(name="ph", grid_slice_tuple=((0, 30), (0, 27), (0, 44)),
+                                  wave_characters=(fx.WaveCharacter(wavelength=1.55e-6),), components=("Ex", "Ey", "Ez")))
+    objects, arrays, _, cfg, _ = fx.place_objects(objs, cfg)
+    outs = {}
+    for m in (0, 3, 5):
+        a = arrays.reset()
+        s = Scene(objects, a, cfg, record_interfaces=True)
+        s.tune_shell_tma(m)
+        assert s.uses_tma and s.shell_tma == m
+        s.forward(a, 0, 50)
+        s.status()
+        torch.cuda.synchronize()
+        outs[m] = ([a.fields.E.clone(), a.fields.H.clone(), a.detector_states["ph"]["phasor"].clone()], None)
+        if m == 5:
+            _, r32 = oracle_run(objects, arrays, cfg, torch.float32, 50)
+            _, r64 = oracle_run(objects, arrays, cfg, torch.float64, 50)
+            compare_states("split_conductor_faces", a, r32, r64, 1e-4)
+        s.reverse(a, 50, 25)
+        s.status()
+        torch.cuda.synchronize()
+        outs[m] = (outs[m][0], [a.fields.E.clone(), a.fields.H.clone()])
+        s.close()
+    for m in (3, 5):
+        for q, (x, y) in enumerate(zip(outs[m][0], outs[0][0])):
+            assert rel_l2(x, y) < 2e-6, (m, q)
+        for x, y in zip(outs[m][1], outs[0][1]):
+            assert rel_l2(x, y) < 1e-4, m
