@@ -63,8 +63,9 @@ struct FdtdPlan {
     // 400 x 400 x 200 coupler (ms per step, one box): mode 0 0.939, mode 3 0.906, mode 4 0.894,
     // mode 5 0.884 (each half-step's faster form); on the 200 x 200 x 100 inverse-design scene
     // mode 5 lost (forward with recording 0.479 s against 0.394 s for 3000 steps: the extra
-    // launches and the coarser whole-grid tiles weigh more on a small grid).  Default: mode 5
-    // from kSplitCells cells up, else mode 0 (set at plan creation)
+    // launches and the coarser whole-grid tiles weigh more on a small grid; the coupler at
+    // 200^3: 0.313 ms mode 0 against 0.336, at 320 x 320 x 160: 0.566 against 0.532).
+    // Default: mode 5 from kSplitCells cells up, else mode 0 (set at plan creation)
     int shell_tma = 0;                    // requested mode
     bool m1_ok = false, m2_ok = false;    // admissible
     // mode 3: the plain TMA kernels over the whole grid (m2_tz tile), then the CPML corrections
