@@ -971,13 +971,27 @@ void launch_plain_boxes(const FdtdPlan* p, UpdArgs a, const Box* boxes, const in
 // faces in one grid, blockIdx.y the face), in x, y, z order.
 template <bool REV, bool HSIDE>
 void launch_pml_corr(const UpdArgs& a, cudaStream_t st, int axes) {
+    auto al8 = [](const void* q) { return q == nullptr || ((uintptr_t)q & 7) == 0; };
     auto run = [&](auto ax_tag) {
         constexpr int AX = decltype(ax_tag)::value;
         if (!(axes >> AX & 1)) return;
         const long long n0 = (long long)a.axs[AX][0].sx * a.axs[AX][0].sy * a.axs[AX][0].sz * (a.axs[AX][0].L > 0);
         const long long n1 = (long long)a.axs[AX][1].sx * a.axs[AX][1].sy * a.axs[AX][1].sz * (a.axs[AX][1].L > 0);
         const long long n = std::max(n0, n1);
-        if (n > 0) k_pml_corr<REV, HSIDE, AX><<<dim3((unsigned)((n + 255) / 256), 2), 256, 0, st>>>(a);
+        if (n <= 0) return;
+        if (AX == 2) {  // two cells per thread where the rows, origins and arrays allow float2 access
+            bool pairs = a.g.nz % 2 == 0 && al8(a.F) && al8(a.Uout) && al8(a.mat) && al8(a.sig);
+            for (int side = 0; side < 2; ++side) {
+                const DSlab& sl = a.axs[2][side];
+                if (sl.L == 0) continue;
+                pairs = pairs && sl.L % 2 == 0 && sl.lo % 2 == 0 && al8(a.axp[2][side][0]) && al8(a.axp[2][side][1]);
+            }
+            if (pairs) {
+                k_pml_corr_z2<REV, HSIDE><<<dim3((unsigned)((n / 2 + 255) / 256), 2), 256, 0, st>>>(a);
+                return;
+            }
+        }
+        k_pml_corr<REV, HSIDE, AX><<<dim3((unsigned)((n + 255) / 256), 2), 256, 0, st>>>(a);
     };
     run(std::integral_constant<int, 0>{});
     run(std::integral_constant<int, 1>{});
