@@ -206,7 +206,7 @@ bool det_fusable(const FdtdDetectorDesc& dd) {
 }
 
 constexpr int kUpdThreads = 256;
-constexpr long long kSplitCells = 16ll << 20;  // grids from this size up default to shell mode 5
+constexpr long long kSplitCells = 12ll << 20;  // grids from this size up default to shell mode 5
 
 int pick_vec(int nz) { return nz % 2 == 0 ? 2 : 1; }  // 4 measured slower (register pressure)
 
